@@ -1,0 +1,318 @@
+"""Benchmark: Richardson-Lucy (ISRA) iterations per second on a 1005 x 1005 x 31
+volume (Nnum 15, 67 x 67 lenslets, PSF 345 x 345 x 15 x 15 x 31), one GPU.
+
+A step is one ISRA iteration (deconvRL.m:46-87): one forward projection, one
+back projection and the fused multiplicative update, computed by libsid with
+the method chosen by --method (default: the mixed-precision spectral form,
+FP16-stored tap spectra with FP32 arithmetic).  Inputs are seeded synthetic
+data with the shapes of the benchmark configuration.
+
+Prints ONE JSON line (rank 0).  --impl reference times the CPU restatement of
+the reference's projection (the FP32 lenslet-sparse loop of oracle/sid_oracle.c,
+OpenMP over all host cores) on a bounded column sample, extrapolated to whole
+iterations.  Multi-GPU runs (torchrun) are independent replicas: the path has
+no exchange step.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "RL iter/s (1005^2x31)"
+UNIT = "iter/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="sid", choices=["sid", "reference"])
+    ap.add_argument("--method", default="spectral_f16", choices=["direct", "spectral_f32", "spectral_f16"])
+    ap.add_argument("--compare", default="direct,spectral_f32",
+                    help="other methods timed after the main region (comma list, '' for none)")
+    ap.add_argument("--compare-steps", type=int, default=3)
+    ap.add_argument("--config", default="cfg1", choices=["cfg0", "cfg1"])
+    ap.add_argument("--cpu-seconds", type=float, default=15.0, help="budget of the CPU baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def workload(config):
+    from sid_gb300 import synthetic
+    H, V = synthetic.config_inputs(config)
+    return H, V
+
+
+def cpu_sample(H, V, seconds, nthreads=0):
+    """Time the FP32 lenslet-sparse forward projection of oracle/ on a growing
+    number of sensor columns until `seconds` of work; returns (seconds per
+    projection extrapolated to all columns, columns timed)."""
+    from oracle import oracle
+    Y = V.shape[1]
+    cols, spent = 0, 0.0
+    step = 1
+    while spent < seconds and cols < Y:
+        n = min(step, Y - cols)
+        t0 = time.perf_counter()
+        oracle.baseline_forward_f32(H, V, cols, cols + n, nthreads)
+        spent += time.perf_counter() - t0
+        cols += n
+        step = min(step * 2, 64)
+    return spent / cols * Y, cols
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during a region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.lines = []
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except Exception:
+                self.proc.kill()
+                out = ""
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in getattr(self, "lines", []):
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    H, V = workload(args.config)
+    nthreads = os.cpu_count() or 1
+    per = []
+    cols = 0
+    budget = max(1.0, args.cpu_seconds / max(1, args.steps + args.warmup))
+    for i in range(args.warmup + args.steps):
+        t_proj, cols = cpu_sample(H, V, budget, nthreads)
+        if i >= args.warmup:
+            per.append(2.0 * t_proj)  # one RL iteration = forward + back projection
+    t_iter = statistics.median(per)
+    value = 1.0 / t_iter
+    sample = (f"FP32 lenslet-sparse forward projection (oracle/sid_oracle.c baseline_forward_f32) on {cols} of "
+              f"{V.shape[1]} sensor columns per step, extrapolated linearly to all columns; one RL iteration "
+              f"= 2 projections (forward + equal-cost back projection)")
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_iter * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"{args.config}: ISRA on 1005x1005x31, PSF 345^2x15^2x31", "parallelism":
+                       "host cores (OpenMP)"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    import numpy as np
+    import torch
+
+    import sid_gb300 as s
+    from oracle import oracle
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    H, Vt = workload(args.config)
+    X, Y, Z = Vt.shape
+    methods = [args.method] + [m for m in args.compare.split(",") if m and m != args.method]
+    P = s.Projector(H, (X, Y), None, methods=tuple(methods))
+    info = P.info()
+    # RL input: Htf = A^T y with y = A V_true (the reference starts ISRA at Xguess = Htf)
+    y = P.forward(Vt, method=args.method)
+    Htf = P.adjoint(y, method=args.method)
+    X0 = Htf.clone()
+    torch.cuda.synchronize()
+
+    def step(x, m):
+        from sid_gb300 import _lib
+        _lib.call("sid_deconv_isra", P._plan, _lib.METHODS[m], Htf.data_ptr(), x.data_ptr(), 1, 0.0,
+                  s.lfm._stream_ptr())
+
+    x = X0.clone()
+    for _ in range(args.warmup):
+        step(x, args.method)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    P.timing(True)
+    stream = torch.cuda.current_stream()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    with Clocks(local) as clk:
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(args.steps):
+            step(x, args.method)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    P.timing(False)
+    ms = e0.elapsed_time(e1)
+    k_ms, k_n = P.timing_read()
+    P.sync()
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_per_step = ms / args.steps
+    value = world * args.steps / (ms / 1e3)
+
+    # roofline of the dominant kernel (the spectral contraction streams the tap spectra)
+    n_out, n_in = info["Nnum"] ** 2, info["Nnum"] ** 2 * info["Z"]
+    nf = (info["L"] // 2 + 1) * info["L"]
+    hbm, peak_kind = peaks()
+    roof = None
+    if args.method.startswith("spectral") and k_n:
+        esz = 4 if args.method == "spectral_f16" else 8
+        alg_bytes = nf * n_out * n_in * esz + nf * (n_in + n_out) * 8
+        avg_s = k_ms / k_n / 1e3
+        achieved = alg_bytes / avg_s / 1e9
+        traffic = None
+        tf = os.path.join(ROOT, "profiles", "traffic.json")
+        if os.path.exists(tf):
+            traffic = json.load(open(tf)).get(f"k_spec_{args.method}")
+        roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                "traffic": traffic, "kernel": "k_spec_fwd/k_spec_adj (tap-spectra contraction)",
+                "launches": k_n, "avg_launch_ms": k_ms / k_n, "algorithmic_bytes_per_launch": alg_bytes,
+                "peak_source": f"{peak_kind} hbm_gbs (MEASURED_PEAKS.json)"}
+
+    # end to end: the host-array ISRA entry point (copies inside the timed region)
+    xh = s.to_numpy(X0)
+    hh = s.to_numpy(Htf)
+    P.isra_host(hh, xh, 1, method=args.method)
+    t0 = time.perf_counter()
+    e2e_steps = max(3, args.steps // 4)
+    for _ in range(e2e_steps):
+        xh = P.isra_host(hh, xh, 1, method=args.method)
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    vol_bytes = X * Y * Z * 4
+
+    # accuracy of the timed method: forward projection vs the FP64 oracle at 256 sampled pixels
+    rng = np.random.default_rng(0)
+    pix = np.stack([rng.integers(0, X, 256), rng.integers(0, Y, 256)], 1)
+    ref_pix = oracle.forward_project_pixels(H, Vt, pix)
+    got = s.to_numpy(P.forward(Vt, method=args.method))[pix[:, 0], pix[:, 1]]
+    fwd_err = float(np.linalg.norm(got - ref_pix) / np.linalg.norm(ref_pix))
+
+    # other methods (fewer steps, same workload) for the mixed-vs-FP32 comparison
+    others = {}
+    for m in methods[1:]:
+        xm = X0.clone()
+        step(xm, m)
+        torch.cuda.synchronize()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(args.compare_steps):
+            step(xm, m)
+        b.record(stream)
+        torch.cuda.synchronize()
+        tm = a.elapsed_time(b) / args.compare_steps
+        gm = s.to_numpy(P.forward(Vt, method=m))[pix[:, 0], pix[:, 1]]
+        others[m] = {"rl_iter_s": 1e3 / tm, "ms_per_iter": tm,
+                     "fwd_rel_err_vs_fp64": float(np.linalg.norm(gm - ref_pix) / np.linalg.norm(ref_pix))}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        t_proj, cols = cpu_sample(H, Vt, args.cpu_seconds, os.cpu_count() or 1)
+        cpu = {"value": 1.0 / (2.0 * t_proj), "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
+               "sample": f"FP32 lenslet-sparse forward projection (oracle/sid_oracle.c) on {cols}/{Y} sensor "
+                         f"columns, extrapolated; RL iteration = 2 projections"}
+
+    if rank == 0:
+        launches_per_step = {"direct": 7, "spectral_f32": 10, "spectral_f16": 10}[args.method]
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 (FP16-stored spectra)" if args.method == "spectral_f16" else "f32",
+            "data": "synthetic (seeded Gaussian PSF + blob volume, shapes of the 1005^2x31 configuration)",
+            "config": {"workload": f"{args.config}: ISRA iteration on 1005x1005x31, Nnum 15, PSF 345^2x15^2x31",
+                       "method": args.method, "parallelism": "replicas" if world > 1 else "1 GPU",
+                       "l2": "per-iteration working set (tap spectra, "
+                             f"{nf * n_out * n_in * (4 if args.method == 'spectral_f16' else 8) / 1e9:.1f} GB) "
+                             "exceeds L2; no flush needed"},
+            "roofline": roof,
+            "cpu_baseline": cpu,
+            "e2e": {"value": 1.0 / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 2 * vol_bytes,
+                    "d2h_bytes_per_step": vol_bytes,
+                    "api": "sid_deconv_isra_host (host arrays, maxIter=1 per step)"},
+            "gpu_launches": launches_per_step * args.steps,
+            "clocks": clk.summary(),
+            "accuracy": {"fwd_rel_l2_vs_fp64_256px": fwd_err},
+            "compare": others,
+            "mixed_vs_fp32_direct": (value / world) / others["direct"]["rl_iter_s"] if "direct" in others else None,
+            "plan": {"L": info["L"], "D": info["D"], "device_gb": info["device_bytes"] / 1e9},
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

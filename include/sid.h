@@ -1,0 +1,112 @@
+/*
+ * sid.h -- C ABI of libsid, the GB300 (sm_103a) implementation of SID's
+ * light-field projection / deconvolution / NNLS hot path.
+ *
+ * Conventions
+ *   - Arrays are MATLAB column-major with the reference's shapes.
+ *   - Sizes are int64_t.  Every call returns an int status: SID_OK (0) or a
+ *     negative code; sid_last_error() returns a thread-local message.
+ *   - Unless a name ends in _host, array arguments are DEVICE pointers and the
+ *     call is ordered on `stream` (a cudaStream_t passed as void*, NULL = the
+ *     legacy default stream).  _host entry points take host arrays, copy them
+ *     in, compute and copy the result out before returning (the MEX path for
+ *     non-gpuArray inputs).
+ *   - The caller owns every array it passes.  A plan owns its PSF copy,
+ *     spectra and workspaces; one plan serves one stream at a time.
+ */
+#ifndef SID_H
+#define SID_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    SID_OK = 0,
+    SID_EINVAL = -1,   /* bad argument (shape, pointer, option) */
+    SID_ENOMEM = -2,   /* device allocation failed */
+    SID_ECUDA = -3,    /* CUDA runtime error */
+    SID_ETIMEOUT = -4, /* a device-side wait exceeded its budget */
+    SID_ENOCONV = -5,  /* solver hit its iteration cap (NQP.m:116-119) */
+    SID_ENOTSUP = -6   /* the plan was not built for the requested method */
+};
+
+/* Plan flags: which operator forms to build at plan creation. */
+#define SID_PLAN_DIRECT       0x1 /* FP32 lenslet taps for the direct kernels */
+#define SID_PLAN_SPECTRAL_F32 0x2 /* lenslet-grid spectra, FP32 */
+#define SID_PLAN_SPECTRAL_F16 0x4 /* lenslet-grid spectra, FP16 storage, FP32 math */
+
+/* Projection methods. */
+#define SID_METHOD_DIRECT       0
+#define SID_METHOD_SPECTRAL_F32 1
+#define SID_METHOD_SPECTRAL_F16 2
+
+typedef struct sid_plan sid_plan;
+
+/* Thread-local description of the last failure. */
+const char* sid_last_error(void);
+/* Library version, major*10000 + minor*100 + patch. */
+int sid_version(void);
+
+/* ---- Projector plan ------------------------------------------------------
+ * H: HOST array, M x M x Nnum x Nnum x Z single (psf_ballistic.H).
+ * CAindex: HOST Z x 2 int32, 1-based per-depth crop (psf_ballistic.CAindex),
+ *   or NULL for the uncropped PSF (the forwardProjectGPU semantics).
+ * X, Y: volume / sensor size.  flags: SID_PLAN_* bits.
+ * Replaces the PSF upload that forwardProjectGPU.m:19 and
+ * backwardProjectGPU_new.m:19 repeat for every slice of every call. */
+int sid_plan_create(const float* H, int64_t M, int64_t Nnum, int64_t Z,
+                    const int32_t* CAindex, int64_t X, int64_t Y, int flags,
+                    sid_plan** plan);
+int sid_plan_destroy(sid_plan* plan);
+/* info[0..11] = M, Nnum, Z, X, Y, Lx, Ly, D (taps per axis), L (DFT length),
+ * device bytes held, flags, adjoint-taps-separate. */
+int sid_plan_info(const sid_plan* plan, int64_t* info);
+
+/* TOTALprojection = forwardProjectGPU(H, realspace)   forwardProjectGPU.m:1
+ *                 = forwardProjectACC(H, realspace, CAindex)  forwardProjectACC.m:1
+ * V: X x Y x Z single, I: X x Y single (device). */
+int sid_forward(sid_plan* plan, int method, const float* V, float* I, void* stream);
+/* Backprojection = backwardProjectGPU_new(H, projection)  backwardProjectGPU_new.m:1
+ *                = backwardProjectACC_new(H, projection, CAindex)  backwardProjectACC_new.m:1
+ * I: X x Y single, V: X x Y x Z single (device). */
+int sid_adjoint(sid_plan* plan, int method, const float* I, float* V, void* stream);
+/* Host-array forms of the two calls above. */
+int sid_forward_host(sid_plan* plan, int method, const float* V, float* I);
+int sid_adjoint_host(sid_plan* plan, int method, const float* I, float* V);
+
+/* Wait for `stream`, then report SID_ETIMEOUT if a device-side wait of a
+ * kernel launched on this plan ran out of budget since the last check. */
+int sid_plan_sync(sid_plan* plan, void* stream);
+
+/* CUDA-event timing of the plan's dominant kernel launches (the spectral
+ * contraction, or the direct projection kernel), recorded on the launch
+ * stream.  Enable, run, then read the summed milliseconds and the number of
+ * timed launches (reading resets the counters). */
+int sid_plan_timing_enable(sid_plan* plan, int on);
+int sid_plan_timing_read(sid_plan* plan, double* total_ms, int64_t* launches);
+
+/* ---- Deconvolution -------------------------------------------------------
+ * Xguess = deconvRL(fwd, bwd, Htf, maxIter, Xguess, opts)   deconvRL.m:1
+ * ISRA: X <- X .* Htf ./ (A'A X + lambda) with inf -> 0 and NaN -> 0
+ * (deconvRL.m:46-87, mode 'basic', p = 1; lambda = 0 is the unpenalised form).
+ * Htf, X: X x Y x Z single (device); X holds Xguess on entry. */
+int sid_deconv_isra(sid_plan* plan, int method, const float* Htf, float* X,
+                    int maxIter, float lambda, void* stream);
+/* Host-array form of sid_deconv_isra (copies in, iterates, copies X out). */
+int sid_deconv_isra_host(sid_plan* plan, int method, const float* Htf, float* X,
+                         int maxIter, float lambda);
+/* Xguess = LS_deconv(fwd, bwd, df, opts)   LS_deconv.m:1
+ * Projected gradient with exact line search on ||y - A x||^2 + lamb_L2 ||x||^2
+ * + lamb_L1 ||x||_1, x >= 0 (LS_deconv.m:49-93; TV terms not supported).
+ * X: X x Y x Z single (device); holds df = A'y on entry, the solution on exit. */
+int sid_deconv_ls(sid_plan* plan, int method, float* X, int max_iter,
+                  float lamb_L1, float lamb_L2, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SID_H */

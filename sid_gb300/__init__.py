@@ -1,0 +1,21 @@
+"""sid_gb300: GB300-native (sm_103a) implementation of SID's hot path.
+
+The compute lives in ``libsid.so`` (hand-written CUDA behind the C ABI of
+``include/sid.h``); this package mirrors the reference's MATLAB functions on
+top of it.  Import does not require a GPU; calling the operators does.
+"""
+from ._lib import SidError  # noqa: F401
+from .lfm import (  # noqa: F401
+    LS_deconv,
+    Projector,
+    backwardProjectACC_new,
+    backwardProjectGPU_new,
+    deconvRL,
+    forwardProjectACC,
+    forwardProjectGPU,
+    set_default_method,
+    to_device,
+    to_numpy,
+)
+
+__version__ = "1.0.0"

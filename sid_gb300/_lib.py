@@ -1,0 +1,96 @@
+"""ctypes binding of libsid.so (the C ABI declared in include/sid.h).
+
+The library is built in-tree by ``sid_gb300.build`` and loaded from
+``sid_gb300/_build/libsid.so``.  There is no fallback: if the shared library is
+missing or fails to load, every entry point raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import re
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "libsid.so")
+HEADER = os.path.join(os.path.dirname(_HERE), "include", "sid.h")
+
+SID_OK, SID_EINVAL, SID_ENOMEM, SID_ECUDA, SID_ETIMEOUT, SID_ENOCONV, SID_ENOTSUP = 0, -1, -2, -3, -4, -5, -6
+PLAN_DIRECT, PLAN_SPECTRAL_F32, PLAN_SPECTRAL_F16 = 0x1, 0x2, 0x4
+METHODS = {"direct": 0, "spectral_f32": 1, "spectral_f16": 2}
+PLAN_FLAG_FOR_METHOD = {"direct": PLAN_DIRECT, "spectral_f32": PLAN_SPECTRAL_F32, "spectral_f16": PLAN_SPECTRAL_F16}
+
+_CODES = {SID_EINVAL: "SID_EINVAL", SID_ENOMEM: "SID_ENOMEM", SID_ECUDA: "SID_ECUDA",
+          SID_ETIMEOUT: "SID_ETIMEOUT", SID_ENOCONV: "SID_ENOCONV", SID_ENOTSUP: "SID_ENOTSUP"}
+
+
+class SidError(RuntimeError):
+    """A libsid call returned a non-zero status."""
+
+    def __init__(self, code, msg):
+        super().__init__(f"{_CODES.get(code, code)}: {msg}")
+        self.code = code
+
+
+P = ctypes.c_void_p
+I64 = ctypes.c_int64
+I32 = ctypes.c_int
+F32 = ctypes.c_float
+F64 = ctypes.c_double
+PP = ctypes.POINTER(ctypes.c_void_p)
+
+# name -> argtypes; restype is int unless listed in _RESTYPES
+SIGNATURES = {
+    "sid_last_error": [],
+    "sid_version": [],
+    "sid_plan_create": [P, I64, I64, I64, P, I64, I64, I32, PP],
+    "sid_plan_destroy": [P],
+    "sid_plan_info": [P, P],
+    "sid_forward": [P, I32, P, P, P],
+    "sid_adjoint": [P, I32, P, P, P],
+    "sid_forward_host": [P, I32, P, P],
+    "sid_adjoint_host": [P, I32, P, P],
+    "sid_plan_sync": [P, P],
+    "sid_deconv_isra": [P, I32, P, P, I32, F32, P],
+    "sid_deconv_ls": [P, I32, P, I32, F32, F32, P],
+    "sid_deconv_isra_host": [P, I32, P, P, I32, F32],
+    "sid_plan_timing_enable": [P, I32],
+    "sid_plan_timing_read": [P, P, P],
+}
+_RESTYPES = {"sid_last_error": ctypes.c_char_p}
+
+_lib = None
+
+
+def header_functions(path: str = HEADER):
+    """Names of the functions declared in include/sid.h."""
+    text = open(path).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"^\s*(?:const\s+)?\w+\s*\*?\s*(sid_\w+)\s*\(", text, flags=re.M)))
+
+
+def load(path: str = LIB_PATH):
+    """Load libsid.so and attach signatures (raises if it is missing)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(f"libsid.so not built ({path}); run sid_gb300.build.build() first")
+    lib = ctypes.CDLL(path)
+    for name, args in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = _RESTYPES.get(name, ctypes.c_int)
+    _lib = lib
+    return lib
+
+
+def check(rc: int, what: str):
+    if rc != SID_OK:
+        msg = load().sid_last_error()
+        raise SidError(rc, f"{what}: {msg.decode() if msg else ''}")
+
+
+def call(name: str, *args):
+    rc = getattr(load(), name)(*args)
+    check(rc, name)
+    return rc

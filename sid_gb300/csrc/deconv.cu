@@ -1,0 +1,312 @@
+// deconv.cu -- C-ABI projector entry points and the deconvolution solvers.
+//
+// Solvers keep their state in the polyphase layout of the projector kernels
+// (Vp[c][b][a][v][u]), so an iteration is: forward (polyphase in/out),
+// adjoint, and one fused elementwise pass; the V <-> Vp transposes run only at
+// entry and exit.
+#include <cmath>
+
+#include "sid_internal.cuh"
+
+namespace sid {
+
+static cudaStream_t as_stream(void* s) { return static_cast<cudaStream_t>(s); }
+
+int fwd_poly(sid_plan* p, int method, const float* vp, float* ip, cudaStream_t st)
+{
+    switch (method) {
+    case SID_METHOD_DIRECT: return direct_forward(p, vp, ip, p->errflag.as<int>(), st);
+    case SID_METHOD_SPECTRAL_F32: return spectral_forward(p, false, vp, ip, st);
+    case SID_METHOD_SPECTRAL_F16: return spectral_forward(p, true, vp, ip, st);
+    default: set_error("unknown projection method %d", method); return SID_EINVAL;
+    }
+}
+
+int adj_poly(sid_plan* p, int method, const float* ip, float* bp, cudaStream_t st)
+{
+    switch (method) {
+    case SID_METHOD_DIRECT: return direct_adjoint(p, ip, bp, p->errflag.as<int>(), st);
+    case SID_METHOD_SPECTRAL_F32: return spectral_adjoint(p, false, ip, bp, st);
+    case SID_METHOD_SPECTRAL_F16: return spectral_adjoint(p, true, ip, bp, st);
+    default: set_error("unknown projection method %d", method); return SID_EINVAL;
+    }
+}
+
+int ensure_proj_ws(sid_plan* p)
+{
+    SID_TRY(p->vp.alloc((size_t)(vol_plane_elems(p) * p->Z) * sizeof(float)));
+    SID_TRY(p->bp.alloc((size_t)(vol_plane_elems(p) * p->Z) * sizeof(float)));
+    SID_TRY(p->ip.alloc((size_t)vol_plane_elems(p) * sizeof(float)));
+    SID_TRY(p->red.alloc(4096 * sizeof(double)));
+    return SID_OK;
+}
+
+// Synchronise `st` and turn an expired device wait into SID_ETIMEOUT.
+int plan_sync(sid_plan* p, cudaStream_t st)
+{
+    SID_CUDA_TRY(cudaStreamSynchronize(st));
+    int flag = 0;
+    SID_CUDA_TRY(cudaMemcpy(&flag, p->errflag.p, sizeof(int), cudaMemcpyDeviceToHost));
+    if (flag) {
+        cudaMemset(p->errflag.p, 0, sizeof(int));
+        set_error("a device-side wait exceeded its budget (code %d)", flag);
+        return SID_ETIMEOUT;
+    }
+    return SID_OK;
+}
+
+// ------------------------------------------------------ elementwise + sums --
+constexpr int kRedBlocks = 1024;
+
+// partial[block] = sum over the block's grid-stride range of a[i]*b[i] (double)
+__global__ void k_dot_partial(const float* __restrict__ a, const float* __restrict__ b, int64_t n,
+                              double* __restrict__ partial)
+{
+    __shared__ double red[256];
+    double s = 0.0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        s += (double)a[i] * (double)b[i];
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) partial[blockIdx.x] = red[0];
+}
+
+__global__ void k_sum_partials(const double* __restrict__ partial, int n, double* __restrict__ out)
+{
+    __shared__ double red[256];
+    double s = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) s += partial[i];
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *out = red[0];
+}
+
+// out = sum a.*b, deterministic two-stage reduction into `out` (device double)
+static int dot(const float* a, const float* b, int64_t n, double* scratch, double* out, cudaStream_t st)
+{
+    k_dot_partial<<<kRedBlocks, 256, 0, st>>>(a, b, n, scratch);
+    SID_CHECK_LAUNCH();
+    k_sum_partials<<<1, 256, 0, st>>>(scratch, kRedBlocks, out);
+    SID_CHECK_LAUNCH();
+    return SID_OK;
+}
+
+// ISRA update, deconvRL.m:52,55,85-87:
+//   e = Htf ./ (B + lambda); e(isinf(e)) = 0; X = X .* e; X(isnan(X)) = 0
+__global__ void k_isra_update(float* __restrict__ x, const float* __restrict__ htf, const float* __restrict__ b,
+                              float lambda, int64_t n)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const float den = (lambda != 0.f) ? b[i] + lambda : b[i];
+        float e = __fdiv_rn(htf[i], den);
+        if (isinf(e)) e = 0.f;
+        float v = x[i] * e;
+        if (isnan(v)) v = 0.f;
+        x[i] = v;
+    }
+}
+
+// d = B + l2*x - x + l1  (LS_deconv.m:73-75: df = Q(df) - df + lamb_L1 with x = df)
+__global__ void k_ls_init(float* __restrict__ d, const float* __restrict__ b, const float* __restrict__ x,
+                          float l1, float l2, int64_t n)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        d[i] = b[i] + l2 * x[i] - x[i] + l1;
+}
+
+// d_ = ((x > 0) | (d < 0)) .* d   (LS_deconv.m:80-81)
+__global__ void k_ls_passive(const float* __restrict__ x, const float* __restrict__ d, float* __restrict__ dm,
+                             int64_t n)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const float di = d[i];
+        dm[i] = (x[i] > 0.f || di < 0.f) ? di : 0.f;
+    }
+}
+
+// alpha = s1/s2 (nan/inf -> 0); xn = max(x - alpha*d_, 0); dm <- xn - x; x <- xn
+// (LS_deconv.m:86-91)
+__global__ void k_ls_step(float* __restrict__ x, float* __restrict__ dm, const double* __restrict__ s12,
+                          int64_t n)
+{
+    double a = s12[0] / s12[1];
+    if (!isfinite(a)) a = 0.0;
+    const float alpha = (float)a;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const float xo = x[i];
+        float xn = xo - alpha * dm[i];
+        if (xn < 0.f) xn = 0.f;
+        dm[i] = xn - xo;
+        x[i] = xn;
+    }
+}
+
+// d += B + l2 * step   (LS_deconv.m:92: df = df + Q(df_ - Xguess))
+__global__ void k_ls_grad(float* __restrict__ d, const float* __restrict__ b, const float* __restrict__ step,
+                          float l2, int64_t n)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        d[i] += b[i] + l2 * step[i];
+}
+
+}  // namespace sid
+
+using namespace sid;
+
+extern "C" int sid_forward(sid_plan* p, int method, const float* V, float* I, void* stream)
+{
+    SID_REQUIRE(p && V && I, "sid_forward: NULL argument");
+    cudaStream_t st = as_stream(stream);
+    SID_TRY(ensure_proj_ws(p));
+    SID_TRY(v_to_vp(p, V, p->vp.as<float>(), p->Z, st));
+    SID_TRY(fwd_poly(p, method, p->vp.as<float>(), p->ip.as<float>(), st));
+    SID_TRY(vp_to_v(p, p->ip.as<float>(), I, 1, st));
+    return SID_OK;
+}
+
+extern "C" int sid_adjoint(sid_plan* p, int method, const float* I, float* V, void* stream)
+{
+    SID_REQUIRE(p && V && I, "sid_adjoint: NULL argument");
+    cudaStream_t st = as_stream(stream);
+    SID_TRY(ensure_proj_ws(p));
+    SID_TRY(v_to_vp(p, I, p->ip.as<float>(), 1, st));
+    SID_TRY(adj_poly(p, method, p->ip.as<float>(), p->bp.as<float>(), st));
+    SID_TRY(vp_to_v(p, p->bp.as<float>(), V, p->Z, st));
+    return SID_OK;
+}
+
+template <class F>
+static int with_device_copies(sid_plan* p, const float* in_h, size_t in_n, float* out_h, size_t out_n, F fn)
+{
+    DBuf din, dout;
+    SID_TRY(din.alloc(in_n * sizeof(float)));
+    int st = dout.alloc(out_n * sizeof(float));
+    if (st == SID_OK) {
+        cudaError_t e = cudaMemcpy(din.p, in_h, in_n * sizeof(float), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) { set_error("host copy in failed: %s", cudaGetErrorString(e)); st = SID_ECUDA; }
+    }
+    if (st == SID_OK) st = fn(din.as<float>(), dout.as<float>());
+    if (st == SID_OK) st = plan_sync(p, 0);
+    if (st == SID_OK) {
+        cudaError_t e = cudaMemcpy(out_h, dout.p, out_n * sizeof(float), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) { set_error("host copy out failed: %s", cudaGetErrorString(e)); st = SID_ECUDA; }
+    }
+    din.release();
+    dout.release();
+    return st;
+}
+
+extern "C" int sid_forward_host(sid_plan* p, int method, const float* V, float* I)
+{
+    SID_REQUIRE(p && V && I, "sid_forward_host: NULL argument");
+    return with_device_copies(p, V, (size_t)(p->X * p->Y * p->Z), I, (size_t)(p->X * p->Y),
+                              [&](const float* dv, float* di) { return sid_forward(p, method, dv, di, nullptr); });
+}
+
+extern "C" int sid_adjoint_host(sid_plan* p, int method, const float* I, float* V)
+{
+    SID_REQUIRE(p && V && I, "sid_adjoint_host: NULL argument");
+    return with_device_copies(p, I, (size_t)(p->X * p->Y), V, (size_t)(p->X * p->Y * p->Z),
+                              [&](const float* di, float* dv) { return sid_adjoint(p, method, di, dv, nullptr); });
+}
+
+extern "C" int sid_deconv_isra(sid_plan* p, int method, const float* Htf, float* X, int maxIter, float lambda,
+                               void* stream)
+{
+    SID_REQUIRE(p && Htf && X, "sid_deconv_isra: NULL argument");
+    SID_REQUIRE(maxIter >= 0, "sid_deconv_isra: maxIter < 0");
+    cudaStream_t st = as_stream(stream);
+    SID_TRY(ensure_proj_ws(p));
+    const int64_t n = vol_plane_elems(p) * p->Z;
+    SID_TRY(p->ws[0].alloc((size_t)n * sizeof(float)));
+    SID_TRY(p->ws[1].alloc((size_t)n * sizeof(float)));
+    float* xp = p->ws[0].as<float>();
+    float* hp = p->ws[1].as<float>();
+    SID_TRY(v_to_vp(p, Htf, hp, p->Z, st));
+    SID_TRY(v_to_vp(p, X, xp, p->Z, st));
+    for (int it = 0; it < maxIter; ++it) {
+        SID_TRY(fwd_poly(p, method, xp, p->ip.as<float>(), st));
+        SID_TRY(adj_poly(p, method, p->ip.as<float>(), p->bp.as<float>(), st));
+        k_isra_update<<<2048, 256, 0, st>>>(xp, hp, p->bp.as<float>(), lambda, n);
+        SID_CHECK_LAUNCH();
+    }
+    SID_TRY(vp_to_v(p, xp, X, p->Z, st));
+    return SID_OK;
+}
+
+extern "C" int sid_deconv_ls(sid_plan* p, int method, float* X, int max_iter, float lamb_L1, float lamb_L2,
+                             void* stream)
+{
+    SID_REQUIRE(p && X, "sid_deconv_ls: NULL argument");
+    SID_REQUIRE(max_iter >= 0, "sid_deconv_ls: max_iter < 0");
+    cudaStream_t st = as_stream(stream);
+    SID_TRY(ensure_proj_ws(p));
+    const int64_t n = vol_plane_elems(p) * p->Z;
+    const int64_t ni = vol_plane_elems(p);
+    for (int k = 0; k < 3; ++k) SID_TRY(p->ws[k].alloc((size_t)n * sizeof(float)));
+    float* xp = p->ws[0].as<float>();
+    float* dp = p->ws[1].as<float>();
+    float* tp = p->ws[2].as<float>();
+    double* red = p->red.as<double>();
+    double* s12 = red + kRedBlocks;  // two scalars after the partials
+    SID_TRY(v_to_vp(p, X, xp, p->Z, st));
+    // df = Q(x0) - x0 + lamb_L1 with x0 = df
+    SID_TRY(fwd_poly(p, method, xp, p->ip.as<float>(), st));
+    SID_TRY(adj_poly(p, method, p->ip.as<float>(), p->bp.as<float>(), st));
+    k_ls_init<<<2048, 256, 0, st>>>(dp, p->bp.as<float>(), xp, lamb_L1, lamb_L2, n);
+    SID_CHECK_LAUNCH();
+    SID_TRY(mask_vp(p, dp, p->Z, st));
+    for (int it = 0; it < max_iter; ++it) {
+        k_ls_passive<<<2048, 256, 0, st>>>(xp, dp, tp, n);
+        SID_CHECK_LAUNCH();
+        SID_TRY(dot(tp, tp, n, red, s12, st));
+        SID_TRY(fwd_poly(p, method, tp, p->ip.as<float>(), st));
+        SID_TRY(dot(p->ip.as<float>(), p->ip.as<float>(), ni, red, s12 + 1, st));
+        k_ls_step<<<2048, 256, 0, st>>>(xp, tp, s12, n);
+        SID_CHECK_LAUNCH();
+        SID_TRY(fwd_poly(p, method, tp, p->ip.as<float>(), st));
+        SID_TRY(adj_poly(p, method, p->ip.as<float>(), p->bp.as<float>(), st));
+        k_ls_grad<<<2048, 256, 0, st>>>(dp, p->bp.as<float>(), tp, lamb_L2, n);
+        SID_CHECK_LAUNCH();
+    }
+    SID_TRY(vp_to_v(p, xp, X, p->Z, st));
+    return SID_OK;
+}
+
+extern "C" int sid_plan_sync(sid_plan* p, void* stream)
+{
+    SID_REQUIRE(p, "sid_plan_sync: NULL plan");
+    return plan_sync(p, as_stream(stream));
+}
+
+extern "C" int sid_deconv_isra_host(sid_plan* p, int method, const float* Htf, float* X, int maxIter,
+                                    float lambda)
+{
+    SID_REQUIRE(p && Htf && X, "sid_deconv_isra_host: NULL argument");
+    const size_t n = (size_t)(p->X * p->Y * p->Z);
+    DBuf dh, dx;
+    SID_TRY(dh.alloc(n * sizeof(float)));
+    int st = dx.alloc(n * sizeof(float));
+    if (st == SID_OK) {
+        cudaError_t e = cudaMemcpy(dh.p, Htf, n * sizeof(float), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaMemcpy(dx.p, X, n * sizeof(float), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) { set_error("host copy in failed: %s", cudaGetErrorString(e)); st = SID_ECUDA; }
+    }
+    if (st == SID_OK) st = sid_deconv_isra(p, method, dh.as<float>(), dx.as<float>(), maxIter, lambda, nullptr);
+    if (st == SID_OK) st = plan_sync(p, 0);
+    if (st == SID_OK) {
+        cudaError_t e = cudaMemcpy(X, dx.p, n * sizeof(float), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) { set_error("host copy out failed: %s", cudaGetErrorString(e)); st = SID_ECUDA; }
+    }
+    dh.release();
+    dx.release();
+    return st;
+}

@@ -1,0 +1,159 @@
+// sid_internal.cuh -- shared definitions of the libsid CUDA library.
+//
+// Geometry (MATLAB column-major, 0-based here):
+//   H(i,j,a,b,c)  PSF, M x M x N x N x Z  (i,j sensor offsets, (a,b) lenslet phase, c depth)
+//   V(x,y,c)      volume, X x Y x Z;  I(x,y) sensor image, X x Y.
+// Lenslet (polyphase) decomposition used by every projector kernel:
+//   x = a + N*u  (a = phase in [0,N), u = lenslet index in [0,Lx), Lx = ceil(X/N))
+//   Vp[c][b][a][v][u] = V(a+N*u, b+N*v, c)      (zero where x >= X or y >= Y)
+//   Ip[b'][a'][t][s]  = I(a'+N*s, b'+N*t)
+// Forward projection (forwardProjectACC.m:14-29, conv2 'same' alignment):
+//   Ip[b'a'](s,t) = sum_{abc} sum_{m1,m2} Vp[abc](s-m1-dlo, t-m2-dlo) * K[abc][b'a'](m1,m2)
+//   K[abc][b'a'](m1,m2) = H(a'-a+cf_c+lo_c+N*(m1+dlo), b'-b+cf_c+lo_c+N*(m2+dlo), a, b, c)
+// and the adjoint (backwardProjectACC_new.m:14-26) uses the same taps with cf
+// replaced by cb = Mc-1-floor(Mc/2) (equal for odd Mc).
+#pragma once
+#include <cuda_runtime.h>
+#include <cuda_fp16.h>
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "../../include/sid.h"
+
+namespace sid {
+
+void set_error(const char* fmt, ...);
+
+#define SID_CUDA_TRY(expr)                                                      \
+    do {                                                                        \
+        cudaError_t _e = (expr);                                                \
+        if (_e != cudaSuccess) {                                                \
+            ::sid::set_error("%s:%d %s: %s", __FILE__, __LINE__, #expr,         \
+                             cudaGetErrorString(_e));                           \
+            return (_e == cudaErrorMemoryAllocation) ? SID_ENOMEM : SID_ECUDA;  \
+        }                                                                       \
+    } while (0)
+
+#define SID_CHECK_LAUNCH() SID_CUDA_TRY(cudaGetLastError())
+
+#define SID_REQUIRE(cond, ...)                                                  \
+    do {                                                                        \
+        if (!(cond)) {                                                          \
+            ::sid::set_error(__VA_ARGS__);                                      \
+            return SID_EINVAL;                                                  \
+        }                                                                       \
+    } while (0)
+
+#define SID_TRY(expr)                                                           \
+    do {                                                                        \
+        int _s = (expr);                                                        \
+        if (_s != SID_OK) return _s;                                            \
+    } while (0)
+
+inline int64_t cdiv(int64_t a, int64_t b) { return (a + b - 1) / b; }
+inline int64_t floordiv(int64_t a, int64_t b) { return (a >= 0) ? a / b : -((-a + b - 1) / b); }
+inline int64_t ceildiv_signed(int64_t a, int64_t b) { return -floordiv(-a, b); }
+
+// Device buffer owned by a plan.
+struct DBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    int alloc(size_t n) {
+        if (bytes >= n && p) return SID_OK;
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+        if (n == 0) return SID_OK;
+        cudaError_t e = cudaMalloc(&p, n);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            set_error("cudaMalloc(%zu bytes) failed: %s", n, cudaGetErrorString(e));
+            return SID_ENOMEM;
+        }
+        bytes = n;
+        return SID_OK;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    template <class T> T* as() const { return static_cast<T*>(p); }
+};
+
+// CUDA-event timing of the dominant kernel launches of a plan (opt-in).
+struct KTimer {
+    bool on = false;
+    std::vector<cudaEvent_t> beg, end;
+    size_t used = 0;
+    void begin(cudaStream_t st) {
+        if (!on) return;
+        if (used == beg.size()) {
+            cudaEvent_t a, b;
+            cudaEventCreate(&a);
+            cudaEventCreate(&b);
+            beg.push_back(a);
+            end.push_back(b);
+        }
+        cudaEventRecord(beg[used], st);
+    }
+    void finish(cudaStream_t st) {
+        if (!on) return;
+        cudaEventRecord(end[used], st);
+        ++used;
+    }
+    void release() {
+        for (auto e : beg) cudaEventDestroy(e);
+        for (auto e : end) cudaEventDestroy(e);
+        beg.clear();
+        end.clear();
+        used = 0;
+    }
+};
+
+// Lenslet-tap geometry shared by the direct and spectral projectors.
+struct TapGeom {
+    int64_t N, Z, X, Y, Lx, Ly;
+    int64_t dlo, dhi, D;  // tap range along each axis (lenslet units)
+};
+
+}  // namespace sid
+
+// The opaque plan (declared in sid.h as struct sid_plan).
+struct sid_plan {
+    int64_t M, N, Z, X, Y, Lx, Ly;
+    int flags;
+    int device;
+    bool adj_separate;          // adjoint taps differ from forward taps (even crop width)
+    sid::TapGeom g;
+    sid::DBuf taps_f;           // [c][b][a][b'][a'][m1][m2] float, forward taps
+    sid::DBuf taps_b;           // same layout, adjoint taps (only if adj_separate)
+    // spectral form
+    int64_t L;                  // lenslet-grid DFT length (>= Lx + max(dhi,-dlo))
+    int64_t nf;                 // number of r2c frequencies = (L/2+1) * L
+    bool spec_f32, spec_f16;
+    float spec_scale;           // fp16 spectra hold K^ * spec_scale
+    sid::DBuf khat_f32;         // [f][b'a'][abc] float2
+    sid::DBuf khat_f16;         // [f][b'a'][abc] half2
+    sid::DBuf twiddle;          // L float2: exp(-2 pi i k / L)
+    // workspaces
+    sid::DBuf vp, ip, bp, ipart, vhat, ihat, bhat, red;
+    sid::DBuf ws[6];            // solver state (polyphase volumes)
+    sid::DBuf errflag;          // device int: nonzero after a bounded wait expired
+    sid::KTimer timer;          // dominant-kernel timing (sid_plan_timing_*)
+    int zsplit;
+};
+
+namespace sid {
+// projector building blocks (polyphase in, polyphase out)
+int direct_forward(sid_plan* p, const float* vp, float* ip, int* err, cudaStream_t st);
+int direct_adjoint(sid_plan* p, const float* ip, float* bp, int* err, cudaStream_t st);
+int spectral_forward(sid_plan* p, bool f16, const float* vp, float* ip, cudaStream_t st);
+int spectral_adjoint(sid_plan* p, bool f16, const float* ip, float* bp, cudaStream_t st);
+int v_to_vp(const sid_plan* p, const float* V, float* vp, int64_t Z, cudaStream_t st);
+int vp_to_v(const sid_plan* p, const float* vp, float* V, int64_t Z, cudaStream_t st);
+int mask_vp(const sid_plan* p, float* vp, int64_t Z, cudaStream_t st);
+inline int64_t vol_plane_elems(const sid_plan* p) { return p->N * p->N * p->Lx * p->Ly; }
+}  // namespace sid

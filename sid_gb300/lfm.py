@@ -1,0 +1,283 @@
+"""Light-field projector and deconvolution, mirroring the reference's MATLAB API.
+
+Reference functions mirrored here (names, argument meaning, error behaviour):
+
+* ``forwardProjectGPU(H, realspace)``            forwardProjectGPU.m:1
+* ``backwardProjectGPU_new(H, projection)``       backwardProjectGPU_new.m:1
+* ``forwardProjectACC(H, realspace, CAindex)``    forwardProjectACC.m:1
+* ``backwardProjectACC_new(H, projection, CAindex)`` backwardProjectACC_new.m:1
+* ``deconvRL(forwardFUN, backwardFUN, Htf, maxIter, Xguess, opts)`` deconvRL.m:1
+* ``LS_deconv(forwardFUN, backwardFUN, df, opts)`` LS_deconv.m:1
+
+Arrays use MATLAB's shapes and column-major layout: a NumPy array in Fortran
+order, or a CUDA ``torch.Tensor`` whose reversed-dimension view is contiguous
+(e.g. ``torch.empty(Z, Y, X).permute(2, 1, 0)``).  All arithmetic runs in
+libsid on the GPU; this module only moves buffers and checks arguments.
+
+The reference passes projectors as function handles.  Here a ``Projector``
+owns the resident PSF plan; its ``forward`` / ``adjoint`` methods are the
+handles, and the solvers recognise them and run the whole iteration natively.
+"""
+from __future__ import annotations
+
+import ctypes
+import weakref
+
+import numpy as np
+import torch
+
+from . import _lib
+
+_DEFAULT_METHOD = "direct"
+
+
+def set_default_method(method: str):
+    """Projection form used by the function-style API: 'direct' (FP32 lenslet
+    convolution), 'spectral_f32' or 'spectral_f16' (lenslet-grid spectra)."""
+    global _DEFAULT_METHOD
+    if method not in _lib.METHODS:
+        raise ValueError(f"unknown method {method!r}")
+    _DEFAULT_METHOD = method
+
+
+def _require_cuda():
+    if not torch.cuda.is_available():
+        raise RuntimeError("sid_gb300 needs a CUDA GPU: the projector has no CPU implementation")
+
+
+def _fortran_tensor(shape, device):
+    """Uninitialised float32 CUDA tensor with MATLAB column-major strides."""
+    return torch.empty(tuple(reversed(shape)), dtype=torch.float32, device=device).permute(
+        *reversed(range(len(shape))))
+
+
+def _is_fortran(t: torch.Tensor) -> bool:
+    return t.permute(*reversed(range(t.dim()))).is_contiguous()
+
+
+def to_device(a, device=None) -> torch.Tensor:
+    """MATLAB-layout float32 CUDA tensor from a NumPy array or tensor."""
+    _require_cuda()
+    if isinstance(a, torch.Tensor):
+        t = a.to(device=device or "cuda", dtype=torch.float32)
+        if not _is_fortran(t):
+            t = t.permute(*reversed(range(t.dim()))).contiguous().permute(*reversed(range(t.dim())))
+        return t
+    arr = np.asfortranarray(np.asarray(a, dtype=np.float32))
+    t = torch.from_numpy(np.ascontiguousarray(arr.T)).to(device or "cuda")
+    return t.permute(*reversed(range(t.dim())))
+
+
+def to_numpy(t: torch.Tensor) -> np.ndarray:
+    """Fortran-ordered NumPy copy of a MATLAB-layout tensor."""
+    return np.asfortranarray(t.permute(*reversed(range(t.dim()))).contiguous().cpu().numpy().T)
+
+
+def _stream_ptr():
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+class Projector:
+    """Resident light-field projector for one PSF (a ``sid_plan``).
+
+    Parameters
+    ----------
+    H : (M, M, Nnum, Nnum, Z) array, the PSF ``psf_ballistic.H``.
+    image_size : (X, Y) sensor / volume lateral size.
+    CAindex : optional (Z, 2) 1-based per-depth crop (``psf_ballistic.CAindex``);
+        None reproduces forwardProjectGPU / backwardProjectGPU_new.
+    methods : operator forms to build ('direct', 'spectral_f32', 'spectral_f16').
+    """
+
+    def __init__(self, H, image_size, CAindex=None, methods=("direct",)):
+        _require_cuda()
+        Hn = np.asfortranarray(np.asarray(H, dtype=np.float32))
+        if Hn.ndim == 4:
+            Hn = Hn[..., None]
+        if Hn.ndim != 5 or Hn.shape[0] != Hn.shape[1] or Hn.shape[2] != Hn.shape[3]:
+            raise ValueError(f"H must be M x M x Nnum x Nnum x Z, got {Hn.shape}")
+        self.M, _, self.Nnum, _, self.Z = Hn.shape
+        self.X, self.Y = int(image_size[0]), int(image_size[1])
+        ca = None
+        if CAindex is not None:
+            ca = np.asfortranarray(np.asarray(CAindex, dtype=np.int32).reshape(self.Z, 2))
+        flags = 0
+        for m in methods:
+            flags |= _lib.PLAN_FLAG_FOR_METHOD[m]
+        self.methods = tuple(methods)
+        self.default_method = self.methods[0]
+        plan = ctypes.c_void_p()
+        torch.cuda.current_device()  # make sure the CUDA context exists
+        _lib.call("sid_plan_create", Hn.ctypes.data, self.M, self.Nnum, self.Z,
+                  ca.ctypes.data if ca is not None else None, self.X, self.Y, flags, ctypes.byref(plan))
+        self._plan = plan
+        self._finalizer = weakref.finalize(self, _lib.load().sid_plan_destroy, plan)
+
+    # -- info ---------------------------------------------------------------
+    def info(self) -> dict:
+        buf = (ctypes.c_int64 * 12)()
+        _lib.call("sid_plan_info", self._plan, ctypes.cast(buf, ctypes.c_void_p))
+        keys = ["M", "Nnum", "Z", "X", "Y", "Lx", "Ly", "D", "L", "device_bytes", "flags", "adj_separate"]
+        return dict(zip(keys, list(buf)))
+
+    def close(self):
+        self._finalizer()
+
+    def _method(self, method):
+        m = method or self.default_method
+        if m not in _lib.METHODS:
+            raise ValueError(f"unknown method {m!r}")
+        return _lib.METHODS[m]
+
+    # -- operators ------------------------------------------------------------
+    def forward(self, V, method=None, out=None) -> torch.Tensor:
+        """Sensor image A V (X, Y) of a volume V (X, Y, Z)."""
+        V = to_device(V)
+        if tuple(V.shape) != (self.X, self.Y, self.Z):
+            raise ValueError(f"volume must be {(self.X, self.Y, self.Z)}, got {tuple(V.shape)}")
+        I = out if out is not None else _fortran_tensor((self.X, self.Y), V.device)
+        _lib.call("sid_forward", self._plan, self._method(method), V.data_ptr(), I.data_ptr(), _stream_ptr())
+        return I
+
+    def adjoint(self, I, method=None, out=None) -> torch.Tensor:
+        """Back projection A^T I (X, Y, Z) of a sensor image I (X, Y)."""
+        I = to_device(I)
+        if tuple(I.shape) != (self.X, self.Y):
+            raise ValueError(f"image must be {(self.X, self.Y)}, got {tuple(I.shape)}")
+        V = out if out is not None else _fortran_tensor((self.X, self.Y, self.Z), I.device)
+        _lib.call("sid_adjoint", self._plan, self._method(method), I.data_ptr(), V.data_ptr(), _stream_ptr())
+        return V
+
+    def forward_host(self, V, method=None) -> np.ndarray:
+        """Host-array form (inputs and result on the host, copies inside)."""
+        Vn = np.asfortranarray(np.asarray(V, dtype=np.float32))
+        I = np.zeros((self.X, self.Y), dtype=np.float32, order="F")
+        _lib.call("sid_forward_host", self._plan, self._method(method), Vn.ctypes.data, I.ctypes.data)
+        return I
+
+    def adjoint_host(self, I, method=None) -> np.ndarray:
+        In = np.asfortranarray(np.asarray(I, dtype=np.float32))
+        V = np.zeros((self.X, self.Y, self.Z), dtype=np.float32, order="F")
+        _lib.call("sid_adjoint_host", self._plan, self._method(method), In.ctypes.data, V.ctypes.data)
+        return V
+
+    def sync(self):
+        """Wait for the current stream; raise if a device-side wait expired."""
+        _lib.call("sid_plan_sync", self._plan, _stream_ptr())
+
+    # -- solvers ----------------------------------------------------------------
+    def isra(self, Htf, Xguess, maxIter, lam=0.0, method=None) -> torch.Tensor:
+        Htf = to_device(Htf)
+        X = to_device(Xguess).clone()
+        _lib.call("sid_deconv_isra", self._plan, self._method(method), Htf.data_ptr(), X.data_ptr(),
+                  int(maxIter), float(lam), _stream_ptr())
+        return X
+
+    def isra_host(self, Htf, Xguess, maxIter, lam=0.0, method=None) -> np.ndarray:
+        """Host-array ISRA (the MEX path for non-gpuArray inputs): copies in,
+        iterates on the GPU, copies the result out."""
+        Hn = np.asfortranarray(np.asarray(Htf, dtype=np.float32))
+        X = np.array(Xguess, dtype=np.float32, order="F", copy=True)
+        _lib.call("sid_deconv_isra_host", self._plan, self._method(method), Hn.ctypes.data, X.ctypes.data,
+                  int(maxIter), float(lam))
+        return X
+
+    def timing(self, on: bool):
+        """Enable/disable CUDA-event timing of the dominant kernel launches."""
+        _lib.call("sid_plan_timing_enable", self._plan, 1 if on else 0)
+
+    def timing_read(self):
+        """(total_ms, launches) of the dominant kernel since the last read."""
+        ms = ctypes.c_double()
+        n = ctypes.c_int64()
+        _lib.call("sid_plan_timing_read", self._plan, ctypes.byref(ms), ctypes.byref(n))
+        return ms.value, n.value
+
+    def ls_deconv(self, df, max_iter=8, lamb_L1=0.0, lamb_L2=0.0, method=None) -> torch.Tensor:
+        X = to_device(df).clone()
+        _lib.call("sid_deconv_ls", self._plan, self._method(method), X.data_ptr(), int(max_iter),
+                  float(lamb_L1), float(lamb_L2), _stream_ptr())
+        return X
+
+
+# ---------------------------------------------------------------------------
+# Function-style API with the reference's names.  A plan is cached per PSF
+# array object (the MEX layer keeps one per psf_ballistic.H in the same way).
+# ---------------------------------------------------------------------------
+_PLANS: dict = {}
+
+
+def _plan_for(H, image_size, CAindex, method):
+    key = (id(H), tuple(np.shape(H)), tuple(image_size), None if CAindex is None else
+           tuple(np.asarray(CAindex).ravel().tolist()), method)
+    pr = _PLANS.get(key)
+    if pr is None or pr[0]() is not H:
+        try:
+            ref = weakref.ref(H)
+        except TypeError:
+            ref = (lambda h=H: h)
+        _PLANS[key] = (ref, Projector(H, image_size, CAindex, methods=(method,)))
+        pr = _PLANS[key]
+    return pr[1]
+
+
+def forwardProjectGPU(H, realspace):
+    """TOTALprojection = forwardProjectGPU(H, realspace) (forwardProjectGPU.m:1)."""
+    shp = tuple(np.shape(realspace))
+    return _plan_for(H, shp[:2], None, _DEFAULT_METHOD).forward(realspace)
+
+
+def backwardProjectGPU_new(H, projection):
+    """Backprojection = backwardProjectGPU_new(H, projection) (backwardProjectGPU_new.m:1)."""
+    shp = tuple(np.shape(projection))
+    return _plan_for(H, shp[:2], None, _DEFAULT_METHOD).adjoint(projection)
+
+
+def forwardProjectACC(H, realspace, CAindex):
+    """TOTALprojection = forwardProjectACC(H, realspace, CAindex) (forwardProjectACC.m:1)."""
+    shp = tuple(np.shape(realspace))
+    return _plan_for(H, shp[:2], CAindex, "direct").forward(realspace)
+
+
+def backwardProjectACC_new(H, projection, CAindex):
+    """Backprojection = backwardProjectACC_new(H, projection, CAindex) (backwardProjectACC_new.m:1)."""
+    shp = tuple(np.shape(projection))
+    return _plan_for(H, shp[:2], CAindex, "direct").adjoint(projection)
+
+
+def _native_pair(forwardFUN, backwardFUN):
+    f = getattr(forwardFUN, "__self__", None)
+    b = getattr(backwardFUN, "__self__", None)
+    if isinstance(f, Projector) and f is b and forwardFUN.__func__ is Projector.forward \
+            and backwardFUN.__func__ is Projector.adjoint:
+        return f
+    return None
+
+
+def deconvRL(forwardFUN, backwardFUN, Htf, maxIter, Xguess, opts=None):
+    """Xguess = deconvRL(forwardFUN, backwardFUN, Htf, maxIter, Xguess, opts)
+    (deconvRL.m:1): ISRA, mode 'basic' with p = 1.  The projector handles must
+    be a Projector's ``forward`` / ``adjoint``."""
+    opts = dict(opts or {"lambda": 0, "p": 1, "mode": "basic"})
+    if opts.get("mode", "basic") != "basic":
+        raise NotImplementedError("deconvRL: only mode 'basic' runs natively")
+    lam = float(np.asarray(opts.get("lambda", 0.0)).ravel()[0])
+    if lam != 0 and opts.get("p", 1) != 1:
+        raise ValueError("deconvRL: mode 'basic' with p != 1 is undefined in the reference")
+    proj = _native_pair(forwardFUN, backwardFUN)
+    if proj is None:
+        raise TypeError("deconvRL: forwardFUN/backwardFUN must be a Projector's forward/adjoint")
+    return proj.isra(Htf, Xguess, maxIter, lam)
+
+
+def LS_deconv(forwardFUN, backwardFUN, df, opts=None):
+    """Xguess = LS_deconv(forwardFUN, backwardFUN, df, opts) (LS_deconv.m:1)."""
+    opts = dict(opts or {})
+    tv = np.asarray(opts.get("lamb_TV_L2", 0.0))
+    if np.any(tv != 0) or opts.get("lamb_TV_L1", 0):
+        raise NotImplementedError("LS_deconv: TV regularisers do not run natively")
+    proj = _native_pair(forwardFUN, backwardFUN)
+    if proj is None:
+        raise TypeError("LS_deconv: forwardFUN/backwardFUN must be a Projector's forward/adjoint")
+    return proj.ls_deconv(df, int(opts.get("max_iter", 8)), float(opts.get("lamb_L1", 0.0)),
+                          float(opts.get("lamb_L2", 0.0)))

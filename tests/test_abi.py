@@ -1,0 +1,60 @@
+"""Host-side checks of the C ABI: the library loads, exports every function the
+header declares, and rejects bad arguments before touching the GPU."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from sid_gb300 import _lib
+
+
+def test_header_lists_functions():
+    names = _lib.header_functions()
+    assert "sid_plan_create" in names and "sid_forward" in names and "sid_adjoint" in names
+    assert len(names) >= 12
+
+
+def test_library_exports_every_declared_symbol(sidlib):
+    missing = [n for n in _lib.header_functions() if not hasattr(sidlib, n)]
+    assert not missing, f"declared in include/sid.h but not exported: {missing}"
+
+
+def test_signatures_cover_header(sidlib):
+    assert set(_lib.header_functions()) <= set(_lib.SIGNATURES), \
+        set(_lib.header_functions()) - set(_lib.SIGNATURES)
+
+
+def test_version(sidlib):
+    assert sidlib.sid_version() >= 10000
+
+
+@pytest.mark.parametrize("M,N,Z,X,Y", [(0, 3, 2, 9, 9), (9, 0, 2, 9, 9), (9, 3, 0, 9, 9), (9, 3, 2, 0, 9),
+                                       (9, 33, 2, 9, 9)])
+def test_plan_create_rejects_bad_sizes(sidlib, M, N, Z, X, Y):
+    H = np.ones(max(1, M * M * N * N * Z), dtype=np.float32)
+    plan = ctypes.c_void_p()
+    rc = sidlib.sid_plan_create(H.ctypes.data, M, N, Z, None, X, Y, _lib.PLAN_DIRECT, ctypes.byref(plan))
+    assert rc == _lib.SID_EINVAL
+    assert plan.value is None
+    assert sidlib.sid_last_error()
+
+
+def test_plan_create_rejects_bad_caindex(sidlib):
+    M, N, Z = 9, 3, 2
+    H = np.ones(M * M * N * N * Z, dtype=np.float32)
+    ca = np.asfortranarray(np.array([[1, 9], [0, 9]], dtype=np.int32))  # 0 is out of range
+    plan = ctypes.c_void_p()
+    rc = sidlib.sid_plan_create(H.ctypes.data, M, N, Z, ca.ctypes.data, 9, 9, _lib.PLAN_DIRECT, ctypes.byref(plan))
+    assert rc == _lib.SID_EINVAL
+    assert b"CAindex" in sidlib.sid_last_error()
+
+
+def test_null_arguments_rejected(sidlib):
+    rc = sidlib.sid_forward(None, 0, None, None, None)
+    assert rc == _lib.SID_EINVAL
+    rc = sidlib.sid_plan_create(None, 9, 3, 2, None, 9, 9, 1, None)
+    assert rc == _lib.SID_EINVAL
+
+
+def test_destroy_null_is_ok(sidlib):
+    assert sidlib.sid_plan_destroy(None) == 0

@@ -1,0 +1,61 @@
+"""ISRA (deconvRL) and LS_deconv on the GPU against the FP64 oracle."""
+import numpy as np
+import pytest
+
+from tests.conftest import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def small(gpu, oracle):
+    from sid_gb300 import Projector, synthetic
+    N, Z, M, L = 5, 3, 31, 9
+    X = N * L
+    H = synthetic.gaussian_psf(M, N, Z, sigma_min=1.0, sigma_max=3.0)
+    Vt = synthetic.blob_volume(X, X, Z, 6, sigma=(1.5, 1.5), seed=4)
+    y = oracle.forward_project(H, Vt)
+    P = Projector(H, (X, X), None, methods=("direct", "spectral_f32", "spectral_f16"))
+    fwd = lambda v: oracle.forward_project(H, v)  # noqa: E731
+    bwd = lambda i: oracle.backward_project(H, i)  # noqa: E731
+    return H, y, P, fwd, bwd
+
+
+@pytest.mark.parametrize("method,tol", [("direct", 1e-5), ("spectral_f32", 1e-5), ("spectral_f16", 1e-4)])
+def test_isra_matches_oracle(small, method, tol):
+    import sid_gb300 as s
+    from oracle import oracle as o
+    H, y, P, fwd, bwd = small
+    Htf = bwd(y).astype(np.float32)
+    ref = o.deconvRL(fwd, bwd, Htf, 8, Htf)
+    P.default_method = method
+    out = s.to_numpy(s.deconvRL(P.forward, P.adjoint, Htf, 8, Htf, {"lambda": 0, "p": 1, "mode": "basic"}))
+    assert rel_l2(out, ref) < 10 * tol, rel_l2(out, ref)
+
+
+@pytest.mark.parametrize("method,tol", [("direct", 1e-5), ("spectral_f32", 1e-5), ("spectral_f16", 1e-4)])
+def test_ls_deconv_matches_oracle(small, method, tol):
+    import sid_gb300 as s
+    from oracle import oracle as o
+    H, y, P, fwd, bwd = small
+    Htf = bwd(y).astype(np.float32)
+    opts = {"max_iter": 8, "lamb_L1": 1e-3, "lamb_L2": 1e-2}
+    ref = o.LS_deconv(fwd, bwd, Htf, opts)
+    P.default_method = method
+    out = s.to_numpy(s.LS_deconv(P.forward, P.adjoint, Htf, opts))
+    assert rel_l2(out, ref) < 10 * tol, rel_l2(out, ref)
+
+
+def test_isra_zero_rules(gpu):
+    """inf -> 0 and NaN -> 0 (deconvRL.m:85-87): zero voxels stay zero."""
+    import sid_gb300 as s
+    from sid_gb300 import synthetic
+    H = synthetic.gaussian_psf(9, 3, 2, sigma_min=1.0, sigma_max=2.0)
+    P = s.Projector(H, (12, 12), None)
+    Htf = np.zeros((12, 12, 2), dtype=np.float32)
+    Htf[5, 5, 0] = 1.0
+    X0 = np.ones((12, 12, 2), dtype=np.float32)
+    X0[0, 0, 1] = 0.0
+    out = s.to_numpy(P.isra(Htf, X0, 2))
+    assert np.all(np.isfinite(out))
+    assert out[0, 0, 1] == 0.0

@@ -1,0 +1,99 @@
+"""The FP64 oracle against the golden fixtures and against properties of the
+maths it restates (CPU only)."""
+import numpy as np
+import pytest
+
+from tests.conftest import rel_l2
+
+GOLDEN = "tests/golden/projector_cases.npz"
+CASES = ["small_full", "ragged", "cropped", "nnum5"]
+
+
+@pytest.fixture(scope="module")
+def golden():
+    import os
+    from tests.conftest import ROOT
+    return np.load(os.path.join(ROOT, GOLDEN))
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_oracle_matches_golden(oracle, golden, case):
+    g = {k.split("/")[1]: golden[k] for k in golden.files if k.startswith(case + "/")}
+    f = oracle.forward_project(g["H"], g["V"], g["CAindex"])
+    b = oracle.backward_project(g["H"], g["I"], g["CAindex"])
+    assert rel_l2(f, g["fwd"]) < 1e-13
+    assert rel_l2(b, g["adj"]) < 1e-13
+
+
+@pytest.mark.parametrize("M", [7, 9, 10])
+def test_oracle_adjoint_identity(oracle, M):
+    """<Ax, y> == <x, A'y> exactly for odd widths; even widths follow the
+    reference's imrotate centring, which is one pixel off the true adjoint."""
+    rng = np.random.default_rng(M)
+    N, Z, X, Y = 3, 2, 14, 11
+    H = rng.random((M, M, N, N, Z)).astype(np.float32)
+    V = rng.random((X, Y, Z))
+    I = rng.random((X, Y))
+    lhs = np.sum(oracle.forward_project(H, V) * I)
+    rhs = np.sum(V * oracle.backward_project(H, I))
+    if M % 2:
+        assert abs(lhs - rhs) <= 1e-12 * abs(lhs)
+    else:
+        assert abs(lhs - rhs) > 1e-9 * abs(lhs)
+
+
+def test_sampled_pixels_match_full(oracle):
+    rng = np.random.default_rng(3)
+    M, N, Z, X, Y = 11, 3, 3, 16, 13
+    H = rng.random((M, M, N, N, Z)).astype(np.float32)
+    V = rng.random((X, Y, Z))
+    I = rng.random((X, Y))
+    full_f = oracle.forward_project(H, V)
+    full_b = oracle.backward_project(H, I)
+    pix = np.stack([rng.integers(0, X, 20), rng.integers(0, Y, 20)], 1)
+    vox = np.stack([rng.integers(0, X, 20), rng.integers(0, Y, 20), rng.integers(0, Z, 20)], 1)
+    np.testing.assert_allclose(oracle.forward_project_pixels(H, V, pix), full_f[pix[:, 0], pix[:, 1]], rtol=1e-14)
+    np.testing.assert_allclose(oracle.backward_project_voxels(H, I, vox), full_b[vox[:, 0], vox[:, 1], vox[:, 2]],
+                               rtol=1e-14)
+
+
+def test_matlab_quantile(oracle):
+    rng = np.random.default_rng(0)
+    v = rng.random(1001)
+    for p in [0.0, 1e-4, 0.3, 0.8, 1 - 1e-4, 1.0]:
+        assert abs(oracle.matlab_quantile(v, p) - np.quantile(v, p, method="hazen")) < 1e-14
+
+
+def test_isra_monotone_objective(oracle):
+    """ISRA does not increase ||y - Ax||^2 (its fixed points are LS solutions)."""
+    rng = np.random.default_rng(5)
+    M, N, Z, X = 9, 3, 2, 12
+    H = rng.random((M, M, N, N, Z)).astype(np.float32)
+    xt = rng.random((X, X, Z))
+    y = oracle.forward_project(H, xt)
+    fwd = lambda v: oracle.forward_project(H, v)  # noqa: E731
+    bwd = lambda i: oracle.backward_project(H, i)  # noqa: E731
+    Htf = bwd(y)
+    prev = None
+    x = Htf.copy()
+    for _ in range(5):
+        x = oracle.deconvRL(fwd, bwd, Htf, 1, x)
+        obj = np.sum((y - fwd(x)) ** 2)
+        if prev is not None:
+            assert obj <= prev * (1 + 1e-12)
+        prev = obj
+
+
+def test_ls_deconv_decreases_objective(oracle):
+    rng = np.random.default_rng(6)
+    M, N, Z, X = 9, 3, 2, 12
+    H = rng.random((M, M, N, N, Z)).astype(np.float32)
+    y = oracle.forward_project(H, rng.random((X, X, Z)))
+    fwd = lambda v: oracle.forward_project(H, v)  # noqa: E731
+    bwd = lambda i: oracle.backward_project(H, i)  # noqa: E731
+    Htf = bwd(y)
+    objs = []
+    for it in [0, 2, 8]:
+        x = oracle.LS_deconv(fwd, bwd, Htf, {"max_iter": it})
+        objs.append(np.sum((y - fwd(x)) ** 2))
+    assert objs[2] < objs[1] < objs[0]
