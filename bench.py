@@ -4,7 +4,7 @@ volume (Nnum 15, 67 x 67 lenslets, PSF 345 x 345 x 15 x 15 x 31), one GPU.
 A step is one ISRA iteration (deconvRL.m:46-87): one forward projection, one
 back projection and the fused multiplicative update, computed by libsid with
 the method chosen by --method (default: the mixed-precision spectral form,
-FP16-stored tap spectra with FP32 arithmetic).  Inputs are seeded synthetic
+tap spectra stored as 16-bit block floating point, FP32 arithmetic).  Inputs are seeded synthetic
 data with the shapes of the benchmark configuration.
 
 Prints ONE JSON line (rank 0).  --impl reference times the CPU restatement of
@@ -36,7 +36,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="sid", choices=["sid", "reference"])
-    ap.add_argument("--method", default="spectral_f16", choices=["direct", "spectral_f32", "spectral_f16"])
+    ap.add_argument("--method", default="spectral_i16", choices=["direct", "spectral_f32", "spectral_i16"])
     ap.add_argument("--compare", default="direct,spectral_f32",
                     help="other methods timed after the main region (comma list, '' for none)")
     ap.add_argument("--compare-steps", type=int, default=3)
@@ -229,7 +229,7 @@ def main():
     hbm, peak_kind = peaks()
     roof = None
     if args.method.startswith("spectral") and k_n:
-        esz = 4 if args.method == "spectral_f16" else 8
+        esz = 4 if args.method == "spectral_i16" else 8
         alg_bytes = nf * n_out * n_in * esz + nf * (n_in + n_out) * 8
         avg_s = k_ms / k_n / 1e3
         achieved = alg_bytes / avg_s / 1e9
@@ -243,13 +243,20 @@ def main():
                 "peak_source": f"{peak_kind} hbm_gbs (MEASURED_PEAKS.json)"}
 
     # end to end: the host-array ISRA entry point (copies inside the timed region)
-    xh = s.to_numpy(X0)
-    hh = s.to_numpy(Htf)
+    def pinned_copy(t):
+        a = s.to_numpy(t)
+        buf = torch.empty(a.size, dtype=torch.float32, pin_memory=True).numpy()
+        out = buf.reshape(a.shape, order="F")
+        out[...] = a
+        return out
+
+    xh = pinned_copy(X0)
+    hh = pinned_copy(Htf)
     P.isra_host(hh, xh, 1, method=args.method)
     t0 = time.perf_counter()
     e2e_steps = max(3, args.steps // 4)
     for _ in range(e2e_steps):
-        xh = P.isra_host(hh, xh, 1, method=args.method)
+        P.isra_host_inplace(hh, xh, 1, method=args.method)
     e2e_s = (time.perf_counter() - t0) / e2e_steps
     vol_bytes = X * Y * Z * 4
 
@@ -286,22 +293,22 @@ def main():
                          f"columns, extrapolated; RL iteration = 2 projections"}
 
     if rank == 0:
-        launches_per_step = {"direct": 7, "spectral_f32": 10, "spectral_f16": 10}[args.method]
+        launches_per_step = {"direct": 7, "spectral_f32": 10, "spectral_i16": 10}[args.method]
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32 (FP16-stored spectra)" if args.method == "spectral_f16" else "f32",
+            "vs_baseline": None, "dtype": "f32 (16-bit block-float spectra)" if args.method == "spectral_i16" else "f32",
             "data": "synthetic (seeded Gaussian PSF + blob volume, shapes of the 1005^2x31 configuration)",
             "config": {"workload": f"{args.config}: ISRA iteration on 1005x1005x31, Nnum 15, PSF 345^2x15^2x31",
                        "method": args.method, "parallelism": "replicas" if world > 1 else "1 GPU",
                        "l2": "per-iteration working set (tap spectra, "
-                             f"{nf * n_out * n_in * (4 if args.method == 'spectral_f16' else 8) / 1e9:.1f} GB) "
+                             f"{nf * n_out * n_in * (4 if args.method == 'spectral_i16' else 8) / 1e9:.1f} GB) "
                              "exceeds L2; no flush needed"},
             "roofline": roof,
             "cpu_baseline": cpu,
             "e2e": {"value": 1.0 / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 2 * vol_bytes,
                     "d2h_bytes_per_step": vol_bytes,
-                    "api": "sid_deconv_isra_host (host arrays, maxIter=1 per step)"},
+                    "api": "sid_deconv_isra_host (pinned host arrays, maxIter=1 per step)"},
             "gpu_launches": launches_per_step * args.steps,
             "clocks": clk.summary(),
             "accuracy": {"fwd_rel_l2_vs_fp64_256px": fwd_err},

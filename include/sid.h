@@ -36,12 +36,14 @@ enum {
 /* Plan flags: which operator forms to build at plan creation. */
 #define SID_PLAN_DIRECT       0x1 /* FP32 lenslet taps for the direct kernels */
 #define SID_PLAN_SPECTRAL_F32 0x2 /* lenslet-grid spectra, FP32 */
-#define SID_PLAN_SPECTRAL_F16 0x4 /* lenslet-grid spectra, FP16 storage, FP32 math */
+#define SID_PLAN_SPECTRAL_I16 0x4 /* lenslet-grid spectra in 16-bit block floating point
+                                     (int16 mantissas, power-of-two step per frequency row),
+                                     FP32 arithmetic: the mixed-precision form */
 
 /* Projection methods. */
 #define SID_METHOD_DIRECT       0
 #define SID_METHOD_SPECTRAL_F32 1
-#define SID_METHOD_SPECTRAL_F16 2
+#define SID_METHOD_SPECTRAL_I16 2
 
 typedef struct sid_plan sid_plan;
 

@@ -155,8 +155,9 @@ void oracle_adjoint_voxels(const float* H, i64 M, i64 N, i64 Z, const int* ca,
 }
 
 /* FP32 lenslet-sparse forward projection, timed as the CPU baseline.  Same sum
- * as oracle_forward, single-precision accumulation, one thread per output
- * column block.  `nthreads` <= 0 means the OpenMP default. */
+ * as oracle_forward (uncropped PSF), single-precision accumulation, OpenMP over
+ * the output pixels of sensor columns [y_begin, y_end).  `nthreads` <= 0 means
+ * the OpenMP default. */
 void baseline_forward_f32(const float* H, i64 M, i64 N, i64 Z,
                           const float* V, i64 X, i64 Y, float* I,
                           i64 y_begin, i64 y_end, int nthreads)
@@ -166,7 +167,7 @@ void baseline_forward_f32(const float* H, i64 M, i64 N, i64 Z,
         omp_set_num_threads(nthreads);
     }
     i64 cf = M / 2;
-#pragma omp parallel for schedule(dynamic, 1)
+#pragma omp parallel for collapse(2) schedule(dynamic, 16)
     for (i64 y = y_begin; y < y_end; ++y) {
         for (i64 x = 0; x < X; ++x) {
             float acc = 0.f;

@@ -37,8 +37,16 @@ def _stale(obj: str, src: str, deps) -> bool:
     return any(os.path.getmtime(d) > t for d in [src, *deps])
 
 
+def _machine_stamp() -> str:
+    import platform
+    return f"{platform.machine()} {' '.join(ARCH)} {' '.join(NVCC_FLAGS)}"
+
+
 def build(verbose: bool = False, force: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
+    stamp = os.path.join(BUILD, "STAMP")
+    if not os.path.exists(stamp) or open(stamp).read() != _machine_stamp():
+        force = True  # objects from another host architecture or other flags
     deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
     deps.append(os.path.join(HERE, "..", "include", "sid.h"))
     exe = nvcc()
@@ -68,6 +76,8 @@ def build(verbose: bool = False, force: bool = False) -> str:
         if r.returncode != 0:
             raise RuntimeError(f"link of libsid.so failed:\n{r.stderr}")
         os.replace(tmp, LIB)
+    with open(stamp, "w") as f:
+        f.write(_machine_stamp())
     return LIB
 
 

@@ -17,7 +17,7 @@ int fwd_poly(sid_plan* p, int method, const float* vp, float* ip, cudaStream_t s
     switch (method) {
     case SID_METHOD_DIRECT: return direct_forward(p, vp, ip, p->errflag.as<int>(), st);
     case SID_METHOD_SPECTRAL_F32: return spectral_forward(p, false, vp, ip, st);
-    case SID_METHOD_SPECTRAL_F16: return spectral_forward(p, true, vp, ip, st);
+    case SID_METHOD_SPECTRAL_I16: return spectral_forward(p, true, vp, ip, st);
     default: set_error("unknown projection method %d", method); return SID_EINVAL;
     }
 }
@@ -27,7 +27,7 @@ int adj_poly(sid_plan* p, int method, const float* ip, float* bp, cudaStream_t s
     switch (method) {
     case SID_METHOD_DIRECT: return direct_adjoint(p, ip, bp, p->errflag.as<int>(), st);
     case SID_METHOD_SPECTRAL_F32: return spectral_adjoint(p, false, ip, bp, st);
-    case SID_METHOD_SPECTRAL_F16: return spectral_adjoint(p, true, ip, bp, st);
+    case SID_METHOD_SPECTRAL_I16: return spectral_adjoint(p, true, ip, bp, st);
     default: set_error("unknown projection method %d", method); return SID_EINVAL;
     }
 }
@@ -183,25 +183,20 @@ extern "C" int sid_adjoint(sid_plan* p, int method, const float* I, float* V, vo
     return SID_OK;
 }
 
+// Host-array calls stage through two plan-owned device buffers (ws[4], ws[5])
+// that persist across calls, so repeated calls allocate nothing.
 template <class F>
 static int with_device_copies(sid_plan* p, const float* in_h, size_t in_n, float* out_h, size_t out_n, F fn)
 {
-    DBuf din, dout;
+    DBuf& din = p->ws[4];
+    DBuf& dout = p->ws[5];
     SID_TRY(din.alloc(in_n * sizeof(float)));
-    int st = dout.alloc(out_n * sizeof(float));
-    if (st == SID_OK) {
-        cudaError_t e = cudaMemcpy(din.p, in_h, in_n * sizeof(float), cudaMemcpyHostToDevice);
-        if (e != cudaSuccess) { set_error("host copy in failed: %s", cudaGetErrorString(e)); st = SID_ECUDA; }
-    }
-    if (st == SID_OK) st = fn(din.as<float>(), dout.as<float>());
-    if (st == SID_OK) st = plan_sync(p, 0);
-    if (st == SID_OK) {
-        cudaError_t e = cudaMemcpy(out_h, dout.p, out_n * sizeof(float), cudaMemcpyDeviceToHost);
-        if (e != cudaSuccess) { set_error("host copy out failed: %s", cudaGetErrorString(e)); st = SID_ECUDA; }
-    }
-    din.release();
-    dout.release();
-    return st;
+    SID_TRY(dout.alloc(out_n * sizeof(float)));
+    SID_CUDA_TRY(cudaMemcpy(din.p, in_h, in_n * sizeof(float), cudaMemcpyHostToDevice));
+    SID_TRY(fn(din.as<float>(), dout.as<float>()));
+    SID_TRY(plan_sync(p, 0));
+    SID_CUDA_TRY(cudaMemcpy(out_h, dout.p, out_n * sizeof(float), cudaMemcpyDeviceToHost));
+    return SID_OK;
 }
 
 extern "C" int sid_forward_host(sid_plan* p, int method, const float* V, float* I)
@@ -292,21 +287,14 @@ extern "C" int sid_deconv_isra_host(sid_plan* p, int method, const float* Htf, f
 {
     SID_REQUIRE(p && Htf && X, "sid_deconv_isra_host: NULL argument");
     const size_t n = (size_t)(p->X * p->Y * p->Z);
-    DBuf dh, dx;
+    DBuf& dh = p->ws[4];
+    DBuf& dx = p->ws[5];
     SID_TRY(dh.alloc(n * sizeof(float)));
-    int st = dx.alloc(n * sizeof(float));
-    if (st == SID_OK) {
-        cudaError_t e = cudaMemcpy(dh.p, Htf, n * sizeof(float), cudaMemcpyHostToDevice);
-        if (e == cudaSuccess) e = cudaMemcpy(dx.p, X, n * sizeof(float), cudaMemcpyHostToDevice);
-        if (e != cudaSuccess) { set_error("host copy in failed: %s", cudaGetErrorString(e)); st = SID_ECUDA; }
-    }
-    if (st == SID_OK) st = sid_deconv_isra(p, method, dh.as<float>(), dx.as<float>(), maxIter, lambda, nullptr);
-    if (st == SID_OK) st = plan_sync(p, 0);
-    if (st == SID_OK) {
-        cudaError_t e = cudaMemcpy(X, dx.p, n * sizeof(float), cudaMemcpyDeviceToHost);
-        if (e != cudaSuccess) { set_error("host copy out failed: %s", cudaGetErrorString(e)); st = SID_ECUDA; }
-    }
-    dh.release();
-    dx.release();
-    return st;
+    SID_TRY(dx.alloc(n * sizeof(float)));
+    SID_CUDA_TRY(cudaMemcpy(dh.p, Htf, n * sizeof(float), cudaMemcpyHostToDevice));
+    SID_CUDA_TRY(cudaMemcpy(dx.p, X, n * sizeof(float), cudaMemcpyHostToDevice));
+    SID_TRY(sid_deconv_isra(p, method, dh.as<float>(), dx.as<float>(), maxIter, lambda, nullptr));
+    SID_TRY(plan_sync(p, 0));
+    SID_CUDA_TRY(cudaMemcpy(X, dx.p, n * sizeof(float), cudaMemcpyDeviceToHost));
+    return SID_OK;
 }

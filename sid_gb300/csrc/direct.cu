@@ -167,6 +167,10 @@ k_fwd_direct(const float* __restrict__ Vp, const float* __restrict__ taps, float
         if (alive) {
             const float* T = Tb + buf * TB + warp * D * D;
             const float* W = Wb + buf * (WQ * WR);
+            // two-level sum: a slice's D*D taps into `part`, slices into `acc`
+            float part[R];
+#pragma unroll
+            for (int k = 0; k < R; ++k) part[k] = 0.f;
 #pragma unroll 1
             for (int m1 = 0; m1 < D; ++m1) {
                 const int r = lane + (D - 1 - m1);
@@ -177,9 +181,11 @@ k_fwd_direct(const float* __restrict__ Vp, const float* __restrict__ taps, float
                 for (int m2 = 0; m2 < D; ++m2) {
                     const float h = T[m1 * D + m2];
 #pragma unroll
-                    for (int k = 0; k < R; ++k) acc[k] = fmaf(h, col[k + D - 1 - m2], acc[k]);
+                    for (int k = 0; k < R; ++k) part[k] = fmaf(h, col[k + D - 1 - m2], part[k]);
                 }
             }
+#pragma unroll
+            for (int k = 0; k < R; ++k) acc[k] += part[k];
         }
         __syncthreads();
     }
@@ -255,6 +261,9 @@ k_adj_direct(const float* __restrict__ Ip, const float* __restrict__ taps, float
         if (alive) {
             const float* T = Tb + buf * TB + warp * D * D;
             const float* W = Wb + buf * (WQ * WR);
+            float part[R];
+#pragma unroll
+            for (int k = 0; k < R; ++k) part[k] = 0.f;
 #pragma unroll 1
             for (int m1 = 0; m1 < D; ++m1) {
                 const int r = lane + m1;
@@ -265,9 +274,11 @@ k_adj_direct(const float* __restrict__ Ip, const float* __restrict__ taps, float
                 for (int m2 = 0; m2 < D; ++m2) {
                     const float h = T[m1 * D + m2];
 #pragma unroll
-                    for (int k = 0; k < R; ++k) acc[k] = fmaf(h, col[k + m2], acc[k]);
+                    for (int k = 0; k < R; ++k) part[k] = fmaf(h, col[k + m2], part[k]);
                 }
             }
+#pragma unroll
+            for (int k = 0; k < R; ++k) acc[k] += part[k];
         }
         __syncthreads();
     }

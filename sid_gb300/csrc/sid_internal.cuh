@@ -133,10 +133,10 @@ struct sid_plan {
     // spectral form
     int64_t L;                  // lenslet-grid DFT length (>= Lx + max(dhi,-dlo))
     int64_t nf;                 // number of r2c frequencies = (L/2+1) * L
-    bool spec_f32, spec_f16;
-    float spec_scale;           // fp16 spectra hold K^ * spec_scale
+    bool spec_f32, spec_i16;
     sid::DBuf khat_f32;         // [f][b'a'][abc] float2
-    sid::DBuf khat_f16;         // [f][b'a'][abc] half2
+    sid::DBuf khat_i16;         // [f][b'a'][abc] short2 mantissas
+    sid::DBuf rstep;            // [f][b'a'] power-of-two step of each 16-bit row
     sid::DBuf twiddle;          // L float2: exp(-2 pi i k / L)
     // workspaces
     sid::DBuf vp, ip, bp, ipart, vhat, ihat, bhat, red;
@@ -150,8 +150,8 @@ namespace sid {
 // projector building blocks (polyphase in, polyphase out)
 int direct_forward(sid_plan* p, const float* vp, float* ip, int* err, cudaStream_t st);
 int direct_adjoint(sid_plan* p, const float* ip, float* bp, int* err, cudaStream_t st);
-int spectral_forward(sid_plan* p, bool f16, const float* vp, float* ip, cudaStream_t st);
-int spectral_adjoint(sid_plan* p, bool f16, const float* ip, float* bp, cudaStream_t st);
+int spectral_forward(sid_plan* p, bool i16, const float* vp, float* ip, cudaStream_t st);
+int spectral_adjoint(sid_plan* p, bool i16, const float* ip, float* bp, cudaStream_t st);
 int v_to_vp(const sid_plan* p, const float* V, float* vp, int64_t Z, cudaStream_t st);
 int vp_to_v(const sid_plan* p, const float* vp, float* V, int64_t Z, cudaStream_t st);
 int mask_vp(const sid_plan* p, float* vp, int64_t Z, cudaStream_t st);

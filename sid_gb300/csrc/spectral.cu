@@ -8,8 +8,9 @@
 // convolution never wraps into the kept outputs):
 //   Ihat[b'a'](f) = sum_abc Khat[f][b'a'][abc] * Vhat[abc](f)            (forward)
 //   Bhat[abc](f)  = sum_b'a' conj(Khat[f][b'a'][abc]) * Ihat[b'a'](f)    (adjoint)
-// The tap spectra Khat are computed once per plan and kept resident (FP32, or
-// FP16 with one power-of-two scale).  Per projection the cost is one streaming
+// The tap spectra Khat are computed once per plan and kept resident, in FP32
+// or in 16-bit block floating point (int16 mantissas, one power-of-two step
+// per frequency row: 15-bit precision where the row's energy is).  Per projection the cost is one streaming
 // pass over Khat (HBM bound) plus small real DFTs of the N*N*Z input and N*N
 // output channels.  Real inputs use the half spectrum f1 in [0, L/2].
 #include <cmath>
@@ -21,21 +22,20 @@ namespace sid {
 
 static inline int64_t spec_nin_pad(const sid_plan* p) { return cdiv(p->N * p->N * p->Z, 8) * 8; }
 
-// ----------------------------------------------------------------- helpers --
-__device__ __forceinline__ float2 cmul(float2 a, float2 b)
-{
-    return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
-}
-
 // --------------------------------------------------------- tap spectra -----
 // grid (n_out, ceil(n_in/8)); each CTA transforms the tap arrays of 8
 // consecutive input channels for one output phase and writes 8 consecutive
 // entries of every frequency row.
+//   mode 0: write FP32 spectra (if k32) and the per-row max |Re|,|Im| (rowmax,
+//           float bits, atomicMax; values are >= 0 so integer order = float order)
+//   mode 1: write 16-bit block-floating-point spectra: int16 mantissas with the
+//           row's power-of-two step rstep[f*n_out + o] (value = mantissa * step)
 constexpr int KB_CH = 8;
 
 __global__ void k_build_khat(const float* __restrict__ taps, const float2* __restrict__ tw,
-                             float2* __restrict__ k32, __half2* __restrict__ k16, float scale, int N,
-                             int n_in, int64_t n_in_pad, int D, int dlo, int L, int64_t tbs)
+                             float2* __restrict__ k32, short2* __restrict__ k16,
+                             unsigned int* __restrict__ rowmax, const float* __restrict__ rstep, int mode,
+                             int N, int n_in, int64_t n_in_pad, int D, int dlo, int L, int64_t tbs)
 {
     extern __shared__ float2 sm[];
     const int H1 = L / 2 + 1;
@@ -72,48 +72,54 @@ __global__ void k_build_khat(const float* __restrict__ taps, const float2* __res
     }
     __syncthreads();
     // stage 2 (along m2 / v): Khat[f][o][k0+ch] = sum_m2 G[ch][m2][f1] w^{-f2 p2}
-    for (int i = threadIdx.x; i < nf * KB_CH; i += blockDim.x) {
-        const int f = i / KB_CH, ch = i - (i / KB_CH) * KB_CH;
+    // (blockDim is a multiple of KB_CH, so the KB_CH lanes of one f are adjacent)
+    const int nitems = nf * KB_CH;
+    for (int i0 = 0; i0 < nitems; i0 += blockDim.x) {
+        const int i = i0 + threadIdx.x;
+        const bool live = i < nitems;
+        const int f = live ? i / KB_CH : 0, ch = i - (i / KB_CH) * KB_CH;
         const int f2 = f / H1, f1 = f - (f / H1) * H1;
         float2 acc = make_float2(0.f, 0.f);
-        for (int m2 = 0; m2 < D; ++m2) {
-            int p2 = (m2 + dlo) % L;
-            if (p2 < 0) p2 += L;
-            float2 w = stw[(f2 * p2) % L];
-            w.y = -w.y;
-            const float2 g = G[(ch * D + m2) * H1 + f1];
-            acc.x += g.x * w.x - g.y * w.y;
-            acc.y += g.x * w.y + g.y * w.x;
+        if (live) {
+            for (int m2 = 0; m2 < D; ++m2) {
+                int p2 = (m2 + dlo) % L;
+                if (p2 < 0) p2 += L;
+                float2 w = stw[(f2 * p2) % L];
+                w.y = -w.y;
+                const float2 g = G[(ch * D + m2) * H1 + f1];
+                acc.x += g.x * w.x - g.y * w.y;
+                acc.y += g.x * w.y + g.y * w.x;
+            }
         }
         const int64_t idx = ((int64_t)f * n_out + o) * n_in_pad + k0 + ch;
-        if (k0 + ch < n_in_pad) {
-            if (k32) k32[idx] = acc;
-            if (k16) k16[idx] = __floats2half2_rn(acc.x * scale, acc.y * scale);
+        if (mode == 0) {
+            if (live && k32) k32[idx] = acc;
+            float m = fmaxf(fabsf(acc.x), fabsf(acc.y));
+#pragma unroll
+            for (int off = KB_CH / 2; off > 0; off >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, off));
+            if (live && ch == 0 && m > 0.f) atomicMax(rowmax + (int64_t)f * n_out + o, __float_as_uint(m));
+        } else if (live) {
+            const float inv = 1.0f / rstep[(int64_t)f * n_out + o];  // exact: power of two
+            const float re = fminf(fmaxf(rintf(acc.x * inv), -32767.f), 32767.f);
+            const float im = fminf(fmaxf(rintf(acc.y * inv), -32767.f), 32767.f);
+            k16[idx] = make_short2((short)re, (short)im);
         }
     }
 }
 
-// Largest l1 norm of one tap array (an upper bound of |Khat|).  Tap array
-// (abc, b', a') starts at (abc*N + b')*tbs + a'*D*D.
-__global__ void k_tap_l1(const float* __restrict__ taps, float* __restrict__ out, int64_t narr, int N,
-                         int D2, int64_t tbs)
+// step = smallest power of two with rowmax / step <= 32767 (1 for empty rows)
+__global__ void k_row_steps(const unsigned int* __restrict__ rowmax, float* __restrict__ rstep, int64_t n)
 {
-    __shared__ float red[256];
-    float m = 0.f;
-    for (int64_t ai = blockIdx.x; ai < narr; ai += gridDim.x) {
-        const float* t = taps + (ai / N) * tbs + (ai % N) * (int64_t)D2;
-        float s = 0.f;
-        for (int i = threadIdx.x; i < D2; i += blockDim.x) s += fabsf(t[i]);
-        red[threadIdx.x] = s;
-        __syncthreads();
-        for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-            if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
-            __syncthreads();
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const float m = __uint_as_float(rowmax[i]);
+        float st = 1.f;
+        if (m > 0.f) {
+            int e;
+            frexpf(m / 32767.f, &e);  // m/32767 = f * 2^e with f in [0.5, 1)
+            st = ldexpf(1.f, e);
         }
-        if (threadIdx.x == 0) m = fmaxf(m, red[0]);
-        __syncthreads();
+        rstep[i] = st;
     }
-    if (threadIdx.x == 0) out[blockIdx.x] = m;
 }
 
 int build_spectra(sid_plan* p)
@@ -135,45 +141,48 @@ int build_spectra(sid_plan* p)
     SID_CUDA_TRY(cudaMemcpy(p->twiddle.p, tw.data(), L * sizeof(float2), cudaMemcpyHostToDevice));
 
     const int64_t tbs = cdiv(N * D * D, 32) * 32;
-    float scale = 1.f;
-    if (p->flags & SID_PLAN_SPECTRAL_F16) {
-        // one power-of-two scale keeps the largest |Khat| near 2^14 in FP16
-        const int64_t narr = Z * N * N * N * N;  // one tap array per (abc, b'a')
-        DBuf part;
-        SID_TRY(part.alloc(1024 * sizeof(float)));
-        k_tap_l1<<<1024, 256>>>(p->taps_f.as<float>(), part.as<float>(), narr, (int)N, (int)(D * D), tbs);
-        cudaError_t e = cudaGetLastError();
-        std::vector<float> h(1024);
-        if (e == cudaSuccess) e = cudaMemcpy(h.data(), part.p, 1024 * sizeof(float), cudaMemcpyDeviceToHost);
-        part.release();
-        SID_CUDA_TRY(e);
-        float mx = 0.f;
-        for (float v : h) mx = std::max(mx, v);
-        if (mx > 0.f) scale = std::ldexp(1.0f, (int)std::floor(std::log2(16384.0 / (double)mx)));
-    }
-    p->spec_scale = scale;
     const size_t nent = (size_t)(p->nf * n_out * n_in_pad);
+    const int64_t nrows = p->nf * n_out;
     if (p->flags & SID_PLAN_SPECTRAL_F32) {
         SID_TRY(p->khat_f32.alloc(nent * sizeof(float2)));
         SID_CUDA_TRY(cudaMemset(p->khat_f32.p, 0, nent * sizeof(float2)));
         p->spec_f32 = true;
     }
-    if (p->flags & SID_PLAN_SPECTRAL_F16) {
-        SID_TRY(p->khat_f16.alloc(nent * sizeof(__half2)));
-        SID_CUDA_TRY(cudaMemset(p->khat_f16.p, 0, nent * sizeof(__half2)));
-        p->spec_f16 = true;
+    const bool want16 = (p->flags & SID_PLAN_SPECTRAL_I16) != 0;
+    if (want16) {
+        SID_TRY(p->khat_i16.alloc(nent * sizeof(short2)));
+        SID_CUDA_TRY(cudaMemset(p->khat_i16.p, 0, nent * sizeof(short2)));
+        SID_TRY(p->rstep.alloc((size_t)nrows * sizeof(float)));
+        SID_CUDA_TRY(cudaMemset(p->rstep.p, 0, (size_t)nrows * sizeof(float)));  // row max bits first
+        p->spec_i16 = true;
     }
     const size_t smem = (size_t)(KB_CH * D * H1 + L) * sizeof(float2) + (size_t)(KB_CH * D * D) * sizeof(float);
     SID_REQUIRE(smem <= 200 * 1024, "spectral plan: tap arrays too large for the spectra builder (D=%lld, L=%lld)",
                 (long long)D, (long long)L);
     SID_CUDA_TRY(cudaFuncSetAttribute(k_build_khat, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     dim3 grid((unsigned)n_out, (unsigned)cdiv(n_in, KB_CH));
-    k_build_khat<<<grid, 256, smem>>>(p->taps_f.as<float>(), p->twiddle.as<float2>(),
-                                      p->spec_f32 ? p->khat_f32.as<float2>() : nullptr,
-                                      p->spec_f16 ? p->khat_f16.as<__half2>() : nullptr, scale, (int)N,
-                                      (int)n_in, n_in_pad, (int)D, (int)p->g.dlo, (int)L, tbs);
-    SID_CHECK_LAUNCH();
-    SID_CUDA_TRY(cudaDeviceSynchronize());
+    unsigned int* rowmax = want16 ? p->rstep.as<unsigned int>() : nullptr;
+    // pass 1: FP32 spectra and row maxima
+    if (p->spec_f32 || want16) {
+        DBuf dummy;
+        if (!rowmax) { SID_TRY(dummy.alloc((size_t)nrows * sizeof(unsigned))); rowmax = dummy.as<unsigned int>(); }
+        k_build_khat<<<grid, 256, smem>>>(p->taps_f.as<float>(), p->twiddle.as<float2>(),
+                                          p->spec_f32 ? p->khat_f32.as<float2>() : nullptr, nullptr, rowmax,
+                                          nullptr, 0, (int)N, (int)n_in, n_in_pad, (int)D, (int)p->g.dlo, (int)L, tbs);
+        SID_CHECK_LAUNCH();
+        SID_CUDA_TRY(cudaDeviceSynchronize());
+        dummy.release();
+    }
+    // pass 2: 16-bit mantissas with per-row power-of-two steps
+    if (want16) {
+        k_row_steps<<<1024, 256>>>(p->rstep.as<unsigned int>(), p->rstep.as<float>(), nrows);
+        SID_CHECK_LAUNCH();
+        k_build_khat<<<grid, 256, smem>>>(p->taps_f.as<float>(), p->twiddle.as<float2>(), nullptr,
+                                          p->khat_i16.as<short2>(), nullptr, p->rstep.as<float>(), 1, (int)N,
+                                          (int)n_in, n_in_pad, (int)D, (int)p->g.dlo, (int)L, tbs);
+        SID_CHECK_LAUNCH();
+        SID_CUDA_TRY(cudaDeviceSynchronize());
+    }
     if (!(p->flags & SID_PLAN_DIRECT)) p->taps_f.release();
     return SID_OK;
 }
@@ -281,106 +290,138 @@ __global__ void k_dft_c2r(const float2* __restrict__ in, float* __restrict__ out
 }
 
 // ------------------------------------------------------------ GEMV kernels --
-// Forward: per frequency f, Ihat[o][f] = (1/scale) sum_k Khat[f][o][k] Vhat[k][f].
-template <bool F16>
+// Storage formats of the tap spectra: FP32 complex (float2, 2 per 16-byte
+// load) or 16-bit block floating point (short2 mantissas, 4 per load, with a
+// power-of-two step per frequency row).
+template <bool I16> struct KLoad;
+template <> struct KLoad<false> {
+    static constexpr int EPL = 2;
+    __device__ static void unpack(const uint4& q, float2 (&k)[2])
+    {
+        k[0] = make_float2(__uint_as_float(q.x), __uint_as_float(q.y));
+        k[1] = make_float2(__uint_as_float(q.z), __uint_as_float(q.w));
+    }
+};
+template <> struct KLoad<true> {
+    static constexpr int EPL = 4;
+    __device__ static void unpack(const uint4& q, float2 (&k)[4])
+    {
+        const uint32_t w[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+        for (int e = 0; e < 4; ++e)
+            k[e] = make_float2((float)(short)(w[e] & 0xffffu), (float)(short)(w[e] >> 16));
+    }
+};
+
+// Forward: per frequency f, Ihat[o][f] = step(f,o) * sum_k Khat[f][o][k] Vhat[k][f].
+// One CTA per frequency; each warp streams RB rows at once (RB independent
+// 16-byte loads in flight per lane) and reduces them with warp shuffles.
+constexpr int kRB = 4;
+
+template <bool I16>
 __global__ void __launch_bounds__(512)
-k_spec_fwd(const void* __restrict__ khat, const float2* __restrict__ vhat, float2* __restrict__ ihat,
-           int n_in, int64_t n_in_pad, int n_out, int nf, float inv_scale)
+k_spec_fwd(const uint4* __restrict__ khat, const float* __restrict__ rstep, const float2* __restrict__ vhat,
+           float2* __restrict__ ihat, int n_in, int64_t n_in_pad, int n_out, int nf)
 {
+    using KL = KLoad<I16>;
+    constexpr int EPL = KL::EPL;
     extern __shared__ float2 xv[];  // [n_in_pad]
     const int f = blockIdx.x;
     for (int k = threadIdx.x; k < n_in_pad; k += blockDim.x)
         xv[k] = (k < n_in) ? vhat[(int64_t)k * nf + f] : make_float2(0.f, 0.f);
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    for (int o = warp; o < n_out; o += nw) {
-        float ar = 0.f, ai = 0.f;
-        const int64_t row = ((int64_t)f * n_out + o) * n_in_pad;
-        if (F16) {
-            // 4 complex (16 bytes) per lane per step
-            const uint4* kr = reinterpret_cast<const uint4*>(reinterpret_cast<const __half2*>(khat) + row);
-            const int nvec = (int)(n_in_pad / 4);
-#pragma unroll 4
-            for (int j = lane; j < nvec; j += 32) {
-                const uint4 q = __ldcs(kr + j);
-                const __half2* h = reinterpret_cast<const __half2*>(&q);
+    const int nvec = (int)(n_in_pad / EPL);
+    const int64_t rowvec = n_in_pad / EPL;  // uint4 per row
+    for (int o0 = warp * kRB; o0 < n_out; o0 += nw * kRB) {
+        float ar[kRB], ai[kRB];
+        const uint4* kr[kRB];
 #pragma unroll
-                for (int e = 0; e < 4; ++e) {
-                    const float2 kk = __half22float2(h[e]);
-                    const float2 x = xv[4 * j + e];
-                    ar = fmaf(kk.x, x.x, ar);
-                    ar = fmaf(-kk.y, x.y, ar);
-                    ai = fmaf(kk.x, x.y, ai);
-                    ai = fmaf(kk.y, x.x, ai);
+        for (int r = 0; r < kRB; ++r) {
+            ar[r] = ai[r] = 0.f;
+            const int o = min(o0 + r, n_out - 1);
+            kr[r] = khat + ((int64_t)f * n_out + o) * rowvec;
+        }
+#pragma unroll 2
+        for (int j = lane; j < nvec; j += 32) {
+            uint4 q[kRB];
+#pragma unroll
+            for (int r = 0; r < kRB; ++r) q[r] = __ldcs(kr[r] + j);
+            float2 x[EPL];
+#pragma unroll
+            for (int e = 0; e < EPL; ++e) x[e] = xv[EPL * j + e];
+#pragma unroll
+            for (int r = 0; r < kRB; ++r) {
+                float2 kk[EPL];
+                KL::unpack(q[r], kk);
+#pragma unroll
+                for (int e = 0; e < EPL; ++e) {
+                    ar[r] = fmaf(kk[e].x, x[e].x, ar[r]);
+                    ar[r] = fmaf(-kk[e].y, x[e].y, ar[r]);
+                    ai[r] = fmaf(kk[e].x, x[e].y, ai[r]);
+                    ai[r] = fmaf(kk[e].y, x[e].x, ai[r]);
                 }
             }
-        } else {
-            const float4* kr = reinterpret_cast<const float4*>(reinterpret_cast<const float2*>(khat) + row);
-            const int nvec = (int)(n_in_pad / 2);
-#pragma unroll 4
-            for (int j = lane; j < nvec; j += 32) {
-                const float4 q = __ldcs(kr + j);
-                const float2 x0 = xv[2 * j], x1 = xv[2 * j + 1];
-                ar = fmaf(q.x, x0.x, ar); ar = fmaf(-q.y, x0.y, ar);
-                ai = fmaf(q.x, x0.y, ai); ai = fmaf(q.y, x0.x, ai);
-                ar = fmaf(q.z, x1.x, ar); ar = fmaf(-q.w, x1.y, ar);
-                ai = fmaf(q.z, x1.y, ai); ai = fmaf(q.w, x1.x, ai);
-            }
         }
 #pragma unroll
-        for (int off = 16; off > 0; off >>= 1) {
-            ar += __shfl_xor_sync(0xffffffffu, ar, off);
-            ai += __shfl_xor_sync(0xffffffffu, ai, off);
+        for (int r = 0; r < kRB; ++r) {
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) {
+                ar[r] += __shfl_xor_sync(0xffffffffu, ar[r], off);
+                ai[r] += __shfl_xor_sync(0xffffffffu, ai[r], off);
+            }
         }
-        if (lane == 0) ihat[(int64_t)o * nf + f] = make_float2(ar * inv_scale, ai * inv_scale);
+        if (lane < kRB && o0 + lane < n_out) {
+            float re = ar[0], im = ai[0];
+#pragma unroll
+            for (int r = 1; r < kRB; ++r)
+                if (lane == r) { re = ar[r]; im = ai[r]; }
+            const int o = o0 + lane;
+            const float st = I16 ? rstep[(int64_t)f * n_out + o] : 1.f;
+            ihat[(int64_t)o * nf + f] = make_float2(re * st, im * st);
+        }
     }
 }
 
-// Adjoint: per frequency f, Bhat[k][f] = (1/scale) sum_o conj(Khat[f][o][k]) Ihat[o][f].
-template <bool F16>
+// Adjoint: per frequency f, Bhat[k][f] = sum_o conj(Khat[f][o][k]) * step(f,o) * Ihat[o][f].
+template <bool I16>
 __global__ void __launch_bounds__(512)
-k_spec_adj(const void* __restrict__ khat, const float2* __restrict__ ihat, float2* __restrict__ bhat,
-           int n_in, int64_t n_in_pad, int n_out, int nf, float inv_scale)
+k_spec_adj(const uint4* __restrict__ khat, const float* __restrict__ rstep, const float2* __restrict__ ihat,
+           float2* __restrict__ bhat, int n_in, int64_t n_in_pad, int n_out, int nf)
 {
-    extern __shared__ float2 yv[];  // [n_out]
+    using KL = KLoad<I16>;
+    constexpr int V = KL::EPL;
+    extern __shared__ float2 yv[];  // [n_out], pre-multiplied by the row steps
     const int f = blockIdx.x;
-    for (int o = threadIdx.x; o < n_out; o += blockDim.x) yv[o] = ihat[(int64_t)o * nf + f];
+    for (int o = threadIdx.x; o < n_out; o += blockDim.x) {
+        const float2 y = ihat[(int64_t)o * nf + f];
+        const float st = I16 ? rstep[(int64_t)f * n_out + o] : 1.f;
+        yv[o] = make_float2(y.x * st, y.y * st);
+    }
     __syncthreads();
-    constexpr int V = F16 ? 4 : 2;  // complex entries per 16-byte load
     const int nvec = (int)(n_in_pad / V);
-    const int64_t base = (int64_t)f * n_out * n_in_pad;
+    const int64_t rowvec = n_in_pad / V;
+    const uint4* base = khat + (int64_t)f * n_out * rowvec;
     for (int j = threadIdx.x; j < nvec; j += blockDim.x) {
         float ar[V], ai[V];
 #pragma unroll
         for (int e = 0; e < V; ++e) ar[e] = ai[e] = 0.f;
+        const uint4* col = base + j;
 #pragma unroll 4
         for (int o = 0; o < n_out; ++o) {
             const float2 y = yv[o];
-            if (F16) {
-                const uint4 q = __ldcs(reinterpret_cast<const uint4*>(
-                                           reinterpret_cast<const __half2*>(khat) + base + (int64_t)o * n_in_pad) + j);
-                const __half2* h = reinterpret_cast<const __half2*>(&q);
+            float2 kk[V];
+            KL::unpack(__ldcs(col + (int64_t)o * rowvec), kk);
 #pragma unroll
-                for (int e = 0; e < V; ++e) {
-                    const float2 kk = __half22float2(h[e]);
-                    ar[e] = fmaf(kk.x, y.x, ar[e]); ar[e] = fmaf(kk.y, y.y, ar[e]);
-                    ai[e] = fmaf(kk.x, y.y, ai[e]); ai[e] = fmaf(-kk.y, y.x, ai[e]);
-                }
-            } else {
-                const float4 q = __ldcs(reinterpret_cast<const float4*>(
-                                            reinterpret_cast<const float2*>(khat) + base + (int64_t)o * n_in_pad) + j);
-                const float kx[2] = {q.x, q.z}, ky[2] = {q.y, q.w};
-#pragma unroll
-                for (int e = 0; e < V; ++e) {
-                    ar[e] = fmaf(kx[e], y.x, ar[e]); ar[e] = fmaf(ky[e], y.y, ar[e]);
-                    ai[e] = fmaf(kx[e], y.y, ai[e]); ai[e] = fmaf(-ky[e], y.x, ai[e]);
-                }
+            for (int e = 0; e < V; ++e) {
+                ar[e] = fmaf(kk[e].x, y.x, ar[e]); ar[e] = fmaf(kk[e].y, y.y, ar[e]);
+                ai[e] = fmaf(kk[e].x, y.y, ai[e]); ai[e] = fmaf(-kk[e].y, y.x, ai[e]);
             }
         }
 #pragma unroll
         for (int e = 0; e < V; ++e) {
             const int k = V * j + e;
-            if (k < n_in) bhat[(int64_t)k * nf + f] = make_float2(ar[e] * inv_scale, ai[e] * inv_scale);
+            if (k < n_in) bhat[(int64_t)k * nf + f] = make_float2(ar[e], ai[e]);
         }
     }
 }
@@ -415,22 +456,22 @@ static int configure_dft(const sid_plan* p)
     return SID_OK;
 }
 
-static int spec_check(const sid_plan* p, bool f16)
+static int spec_check(const sid_plan* p, bool i16)
 {
-    if (f16 && !p->spec_f16) {
-        set_error("spectral projector: plan was built without SID_PLAN_SPECTRAL_F16");
+    if (i16 && !p->spec_i16) {
+        set_error("spectral projector: plan was built without SID_PLAN_SPECTRAL_I16");
         return SID_ENOTSUP;
     }
-    if (!f16 && !p->spec_f32) {
+    if (!i16 && !p->spec_f32) {
         set_error("spectral projector: plan was built without SID_PLAN_SPECTRAL_F32");
         return SID_ENOTSUP;
     }
     return SID_OK;
 }
 
-int spectral_forward(sid_plan* p, bool f16, const float* vp, float* ip, cudaStream_t st)
+int spectral_forward(sid_plan* p, bool i16, const float* vp, float* ip, cudaStream_t st)
 {
-    SID_TRY(spec_check(p, f16));
+    SID_TRY(spec_check(p, i16));
     SID_TRY(ensure_spec_ws(p));
     SID_TRY(configure_dft(p));
     const int64_t n_in = p->N * p->N * p->Z, n_out = p->N * p->N, n_in_pad = spec_nin_pad(p);
@@ -438,16 +479,17 @@ int spectral_forward(sid_plan* p, bool f16, const float* vp, float* ip, cudaStre
                                                          (int)p->Lx, (int)p->Ly, (int)p->L);
     SID_CHECK_LAUNCH();
     const size_t sm = (size_t)n_in_pad * sizeof(float2);
-    const float inv = 1.0f / (f16 ? p->spec_scale : 1.0f);
     p->timer.begin(st);
-    if (f16) {
+    if (i16) {
         SID_CUDA_TRY(cudaFuncSetAttribute(k_spec_fwd<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-        k_spec_fwd<true><<<(unsigned)p->nf, 512, sm, st>>>(p->khat_f16.p, p->vhat.as<float2>(), p->ihat.as<float2>(),
-                                                          (int)n_in, n_in_pad, (int)n_out, (int)p->nf, inv);
+        k_spec_fwd<true><<<(unsigned)p->nf, 512, sm, st>>>(p->khat_i16.as<uint4>(), p->rstep.as<float>(),
+                                                          p->vhat.as<float2>(), p->ihat.as<float2>(), (int)n_in,
+                                                          n_in_pad, (int)n_out, (int)p->nf);
     } else {
         SID_CUDA_TRY(cudaFuncSetAttribute(k_spec_fwd<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-        k_spec_fwd<false><<<(unsigned)p->nf, 512, sm, st>>>(p->khat_f32.p, p->vhat.as<float2>(), p->ihat.as<float2>(),
-                                                           (int)n_in, n_in_pad, (int)n_out, (int)p->nf, inv);
+        k_spec_fwd<false><<<(unsigned)p->nf, 512, sm, st>>>(p->khat_f32.as<uint4>(), nullptr, p->vhat.as<float2>(),
+                                                           p->ihat.as<float2>(), (int)n_in, n_in_pad, (int)n_out,
+                                                           (int)p->nf);
     }
     p->timer.finish(st);
     SID_CHECK_LAUNCH();
@@ -457,9 +499,9 @@ int spectral_forward(sid_plan* p, bool f16, const float* vp, float* ip, cudaStre
     return SID_OK;
 }
 
-int spectral_adjoint(sid_plan* p, bool f16, const float* ip, float* bp, cudaStream_t st)
+int spectral_adjoint(sid_plan* p, bool i16, const float* ip, float* bp, cudaStream_t st)
 {
-    SID_TRY(spec_check(p, f16));
+    SID_TRY(spec_check(p, i16));
     SID_TRY(ensure_spec_ws(p));
     SID_TRY(configure_dft(p));
     const int64_t n_in = p->N * p->N * p->Z, n_out = p->N * p->N, n_in_pad = spec_nin_pad(p);
@@ -467,14 +509,15 @@ int spectral_adjoint(sid_plan* p, bool f16, const float* ip, float* bp, cudaStre
                                                           (int)p->Lx, (int)p->Ly, (int)p->L);
     SID_CHECK_LAUNCH();
     const size_t sm = (size_t)n_out * sizeof(float2);
-    const float inv = 1.0f / (f16 ? p->spec_scale : 1.0f);
     p->timer.begin(st);
-    if (f16)
-        k_spec_adj<true><<<(unsigned)p->nf, 512, sm, st>>>(p->khat_f16.p, p->ihat.as<float2>(), p->vhat.as<float2>(),
-                                                          (int)n_in, n_in_pad, (int)n_out, (int)p->nf, inv);
+    if (i16)
+        k_spec_adj<true><<<(unsigned)p->nf, 512, sm, st>>>(p->khat_i16.as<uint4>(), p->rstep.as<float>(),
+                                                          p->ihat.as<float2>(), p->vhat.as<float2>(), (int)n_in,
+                                                          n_in_pad, (int)n_out, (int)p->nf);
     else
-        k_spec_adj<false><<<(unsigned)p->nf, 512, sm, st>>>(p->khat_f32.p, p->ihat.as<float2>(), p->vhat.as<float2>(),
-                                                           (int)n_in, n_in_pad, (int)n_out, (int)p->nf, inv);
+        k_spec_adj<false><<<(unsigned)p->nf, 512, sm, st>>>(p->khat_f32.as<uint4>(), nullptr, p->ihat.as<float2>(),
+                                                           p->vhat.as<float2>(), (int)n_in, n_in_pad, (int)n_out,
+                                                           (int)p->nf);
     p->timer.finish(st);
     SID_CHECK_LAUNCH();
     k_dft_c2r<<<(unsigned)n_in, 256, c2r_smem(p), st>>>(p->vhat.as<float2>(), bp, p->twiddle.as<float2>(),

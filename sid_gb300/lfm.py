@@ -33,7 +33,7 @@ _DEFAULT_METHOD = "direct"
 
 def set_default_method(method: str):
     """Projection form used by the function-style API: 'direct' (FP32 lenslet
-    convolution), 'spectral_f32' or 'spectral_f16' (lenslet-grid spectra)."""
+    convolution), 'spectral_f32' or 'spectral_i16' (lenslet-grid spectra)."""
     global _DEFAULT_METHOD
     if method not in _lib.METHODS:
         raise ValueError(f"unknown method {method!r}")
@@ -86,7 +86,7 @@ class Projector:
     image_size : (X, Y) sensor / volume lateral size.
     CAindex : optional (Z, 2) 1-based per-depth crop (``psf_ballistic.CAindex``);
         None reproduces forwardProjectGPU / backwardProjectGPU_new.
-    methods : operator forms to build ('direct', 'spectral_f32', 'spectral_f16').
+    methods : operator forms to build ('direct', 'spectral_f32', 'spectral_i16').
     """
 
     def __init__(self, H, image_size, CAindex=None, methods=("direct",)):
@@ -178,6 +178,15 @@ class Projector:
         iterates on the GPU, copies the result out."""
         Hn = np.asfortranarray(np.asarray(Htf, dtype=np.float32))
         X = np.array(Xguess, dtype=np.float32, order="F", copy=True)
+        _lib.call("sid_deconv_isra_host", self._plan, self._method(method), Hn.ctypes.data, X.ctypes.data,
+                  int(maxIter), float(lam))
+        return X
+
+    def isra_host_inplace(self, Htf, X, maxIter, lam=0.0, method=None):
+        """Like isra_host, updating the Fortran-ordered float32 host array X."""
+        if not (isinstance(X, np.ndarray) and X.dtype == np.float32 and X.flags.f_contiguous):
+            raise TypeError("X must be a Fortran-ordered float32 array")
+        Hn = np.asfortranarray(np.asarray(Htf, dtype=np.float32))
         _lib.call("sid_deconv_isra_host", self._plan, self._method(method), Hn.ctypes.data, X.ctypes.data,
                   int(maxIter), float(lam))
         return X

@@ -15,13 +15,13 @@ def small(gpu, oracle):
     H = synthetic.gaussian_psf(M, N, Z, sigma_min=1.0, sigma_max=3.0)
     Vt = synthetic.blob_volume(X, X, Z, 6, sigma=(1.5, 1.5), seed=4)
     y = oracle.forward_project(H, Vt)
-    P = Projector(H, (X, X), None, methods=("direct", "spectral_f32", "spectral_f16"))
+    P = Projector(H, (X, X), None, methods=("direct", "spectral_f32", "spectral_i16"))
     fwd = lambda v: oracle.forward_project(H, v)  # noqa: E731
     bwd = lambda i: oracle.backward_project(H, i)  # noqa: E731
     return H, y, P, fwd, bwd
 
 
-@pytest.mark.parametrize("method,tol", [("direct", 1e-5), ("spectral_f32", 1e-5), ("spectral_f16", 1e-4)])
+@pytest.mark.parametrize("method,tol", [("direct", 1e-5), ("spectral_f32", 1e-5), ("spectral_i16", 1e-4)])
 def test_isra_matches_oracle(small, method, tol):
     import sid_gb300 as s
     from oracle import oracle as o
@@ -33,7 +33,7 @@ def test_isra_matches_oracle(small, method, tol):
     assert rel_l2(out, ref) < 10 * tol, rel_l2(out, ref)
 
 
-@pytest.mark.parametrize("method,tol", [("direct", 1e-5), ("spectral_f32", 1e-5), ("spectral_f16", 1e-4)])
+@pytest.mark.parametrize("method,tol", [("direct", 1e-5), ("spectral_f32", 1e-5), ("spectral_i16", 1e-4)])
 def test_ls_deconv_matches_oracle(small, method, tol):
     import sid_gb300 as s
     from oracle import oracle as o
