@@ -37,7 +37,7 @@ enum {
 #define SID_PLAN_DIRECT       0x1 /* FP32 lenslet taps for the direct kernels */
 #define SID_PLAN_SPECTRAL_F32 0x2 /* lenslet-grid spectra, FP32 */
 #define SID_PLAN_SPECTRAL_I16 0x4 /* lenslet-grid spectra in 16-bit block floating point
-                                     (int16 mantissas, power-of-two step per frequency row),
+                                     (int16 mantissas, one FP32 step per frequency row),
                                      FP32 arithmetic: the mixed-precision form */
 
 /* Projection methods. */
@@ -106,6 +106,31 @@ int sid_deconv_isra_host(sid_plan* plan, int method, const float* Htf, float* X,
  * X: X x Y x Z single (device); holds df = A'y on entry, the solution on exit. */
 int sid_deconv_ls(sid_plan* plan, int method, float* X, int max_iter,
                   float lamb_L1, float lamb_L2, void* stream);
+
+/* ---- NNLS contractions -----------------------------------------------------
+ * A solver context owns the workspaces of the contractions and NNLS solvers
+ * (16-bit operand copies, split-K partials, iteration state). */
+typedef struct sid_ctx sid_ctx;
+int sid_ctx_create(sid_ctx** ctx);
+int sid_ctx_destroy(sid_ctx* ctx);
+/* Wait for `stream`; SID_ETIMEOUT if a device-side wait ran out of budget. */
+int sid_ctx_sync(sid_ctx* ctx, void* stream);
+
+/* Precision of the contractions. */
+#define SID_PREC_FP32  0 /* FP32 SIMT: the plain path */
+#define SID_PREC_SPLIT 1 /* tcgen05 tensor cores on 16-bit hi/lo splits, FP32 accumulation */
+#define SID_PREC_BF16  2 /* one 16-bit tensor-core pass */
+/* Element types of movie arrays. */
+#define SID_DTYPE_F32 0
+#define SID_DTYPE_F16 1
+
+/* G = A'*A (K x K, column-major)   LS_nnls.m:82, fast_nnls.m:54, T_update.m:24
+ * A: P x K single (device, column-major). */
+int sid_gram(sid_ctx* ctx, const float* A, int64_t P, int64_t K, float* G, int prec, void* stream);
+/* h = A'*Y (K x F)   LS_nnls.m:76, fast_nnls.m:57, T_update.m:25
+ * Y: P x F single or half (ydtype). */
+int sid_cross(sid_ctx* ctx, const float* A, const void* Y, int ydtype, int64_t P, int64_t K, int64_t F,
+              float* h, int prec, void* stream);
 
 #ifdef __cplusplus
 }

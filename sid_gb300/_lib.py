@@ -55,7 +55,14 @@ SIGNATURES = {
     "sid_deconv_isra_host": [P, I32, P, P, I32, F32],
     "sid_plan_timing_enable": [P, I32],
     "sid_plan_timing_read": [P, P, P],
+    "sid_ctx_create": [PP],
+    "sid_ctx_destroy": [P],
+    "sid_ctx_sync": [P, P],
+    "sid_gram": [P, P, I64, I64, P, I32, P],
+    "sid_cross": [P, P, P, I32, I64, I64, I64, P, I32, P],
 }
+PREC = {"fp32": 0, "split": 1, "bf16": 2}
+DTYPE_F32, DTYPE_F16 = 0, 1
 _RESTYPES = {"sid_last_error": ctypes.c_char_p}
 
 _lib = None

@@ -71,7 +71,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
     objs = [os.path.join(BUILD, os.path.basename(s)[:-3] + ".o") for s in sources()]
     if force or jobs or not os.path.exists(LIB):
         tmp = LIB + ".tmp"
-        cmd = [exe, *ARCH, "-shared", "-o", tmp, *objs, "-lcuda"]
+        cmd = [exe, *ARCH, "-shared", "-o", tmp, *objs]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link of libsid.so failed:\n{r.stderr}")

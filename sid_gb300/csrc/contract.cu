@@ -1,0 +1,177 @@
+// contract.cu -- solver context and the Gram / cross-product entry points.
+//
+// G = A'A and h = A'Y are the only dense contractions of the NNLS path
+// (LS_nnls.m:76,82; fast_nnls.m:54-57; T_update.m:24-25;
+// incremental_temporal_update_gpu.m:83,89).  Three precisions:
+//   SID_PREC_FP32  FP32 SIMT (gemm_simt.cu) -- the plain path;
+//   SID_PREC_SPLIT tensor cores (gemm_tc.cu) on 16-bit hi/lo splits of the
+//                  FP32 operands (hi*hi + hi*lo + lo*hi, FP32 accumulation in
+//                  TMEM); FP16 movies enter unsplit (A_hi*Y + A_lo*Y);
+//   SID_PREC_BF16  one BF16 tensor-core pass.
+#include <cmath>
+#include <cstring>
+
+#include "sid_internal.cuh"
+
+namespace sid {
+int gemm_tn(const void* const* A, const void* const* B, int npass, int64_t m, int64_t n, int64_t k, int64_t lda,
+            int64_t ldb, bool bf16, float* C, int64_t ldc, float alpha, float beta, int bn, int splitk, float* ws,
+            int64_t ws_elems, int* err, cudaStream_t st);
+void gemm_autotune(int m, int n, int nkb, int* bn, int* splitk);
+int sgemm_tn(const float* A, const float* B, int64_t m, int64_t n, int64_t k, int64_t lda, int64_t ldb, float* C,
+             int64_t ldc, float alpha, float beta, float* ws, int64_t ws_elems, cudaStream_t st);
+int64_t sgemm_ws_elems(int64_t m, int64_t n, int64_t k);
+int split16(const float* src, int64_t rows, int64_t cols, int64_t lds, uint16_t* hi, uint16_t* lo, int64_t ld,
+            bool bf16, float scale, cudaStream_t st);
+int copy16_pad(const uint16_t* src, int64_t rows, int64_t cols, int64_t lds, uint16_t* dst, int64_t ld,
+               cudaStream_t st);
+int absmax(const float* x, int64_t n, unsigned int* out, cudaStream_t st);
+}  // namespace sid
+
+struct sid_ctx {
+    int device;
+    sid::DBuf a_hi, a_lo, b_hi, b_lo, ws, scal, errflag;
+    sid::DBuf nn[12];  // NNLS state
+};
+
+namespace sid {
+
+int ctx_sync(sid_ctx* c, cudaStream_t st)
+{
+    SID_CUDA_TRY(cudaStreamSynchronize(st));
+    int flag = 0;
+    SID_CUDA_TRY(cudaMemcpy(&flag, c->errflag.p, sizeof(int), cudaMemcpyDeviceToHost));
+    if (flag) {
+        cudaMemset(c->errflag.p, 0, sizeof(int));
+        set_error("a device-side wait exceeded its budget (code %d)", flag);
+        return SID_ETIMEOUT;
+    }
+    return SID_OK;
+}
+
+static inline int64_t pad8(int64_t v) { return cdiv(v, 8) * 8; }
+
+// Largest power of two s with max|x| * s <= 2^14 (FP16 operand scaling).
+static int pow2_scale(sid_ctx* c, const float* x, int64_t n, float* scale, cudaStream_t st)
+{
+    SID_TRY(c->scal.alloc(64));
+    SID_TRY(absmax(x, n, c->scal.as<unsigned int>(), st));
+    unsigned int bits = 0;
+    SID_CUDA_TRY(cudaMemcpyAsync(&bits, c->scal.p, sizeof(bits), cudaMemcpyDeviceToHost, st));
+    SID_CUDA_TRY(cudaStreamSynchronize(st));
+    float mx;
+    std::memcpy(&mx, &bits, sizeof(mx));
+    *scale = (mx > 0.f) ? std::ldexp(1.0f, (int)std::floor(std::log2(16384.0 / (double)mx))) : 1.f;
+    return SID_OK;
+}
+
+// C (m x n) = alpha * A'B + beta*C with A: k x m (lda), B: k x n (ldb), FP32
+// operands, at precision `prec`.  B may instead be FP16 (b_f16 != 0).
+int contract(sid_ctx* c, const float* A, const void* B, bool b_f16, int64_t m, int64_t n, int64_t k, int64_t lda,
+             int64_t ldb, float* C, int64_t ldc, float alpha, float beta, int prec, cudaStream_t st)
+{
+    int* err = c->errflag.as<int>();
+    if (prec == SID_PREC_FP32) {
+        SID_REQUIRE(!b_f16, "FP32 contraction needs an FP32 right operand");
+        SID_TRY(c->ws.alloc((size_t)sgemm_ws_elems(m, n, k) * sizeof(float)));
+        return sgemm_tn(A, static_cast<const float*>(B), m, n, k, lda, ldb, C, ldc, alpha, beta, c->ws.as<float>(),
+                        (int64_t)(c->ws.bytes / sizeof(float)), st);
+    }
+    SID_REQUIRE(prec == SID_PREC_SPLIT || prec == SID_PREC_BF16, "unknown precision %d", prec);
+    const int64_t kp = pad8(k);
+    int bn = 0, splitk = 0;
+    gemm_autotune((int)m, (int)n, (int)cdiv(k, 64), &bn, &splitk);
+    SID_TRY(c->ws.alloc((size_t)(splitk * m * n) * sizeof(float)));
+    const bool split = prec == SID_PREC_SPLIT;
+    if (b_f16) {
+        // FP16 right operand used as is; A split into FP16 hi/lo with a power-of-two scale
+        float sa = 1.f;
+        SID_TRY(pow2_scale(c, A, m * lda, &sa, st));  // over the whole stored matrix
+        SID_TRY(c->a_hi.alloc((size_t)(kp * m) * 2));
+        if (split) SID_TRY(c->a_lo.alloc((size_t)(kp * m) * 2));
+        SID_TRY(split16(A, k, m, lda, c->a_hi.as<uint16_t>(), split ? c->a_lo.as<uint16_t>() : nullptr, kp, false,
+                        sa, st));
+        const void* bptr = B;
+        int64_t ldbb = ldb;
+        if (ldb % 8 != 0 || ((uintptr_t)B & 15) != 0) {
+            SID_TRY(c->b_hi.alloc((size_t)(kp * n) * 2));
+            SID_TRY(copy16_pad(static_cast<const uint16_t*>(B), k, n, ldb, c->b_hi.as<uint16_t>(), kp, st));
+            bptr = c->b_hi.p;
+            ldbb = kp;
+        }
+        const void* As[2] = {c->a_hi.p, c->a_lo.p};
+        const void* Bs[2] = {bptr, bptr};
+        return gemm_tn(As, Bs, split ? 2 : 1, m, n, k, kp, ldbb, false, C, ldc, alpha / sa, beta, bn, splitk,
+                       c->ws.as<float>(), (int64_t)(c->ws.bytes / sizeof(float)), err, st);
+    }
+    // FP32 x FP32: BF16 hi/lo splits of both (no scaling needed: BF16 keeps the FP32 exponent range)
+    const bool same = (static_cast<const void*>(A) == B && lda == ldb && m == n);
+    SID_TRY(c->a_hi.alloc((size_t)(kp * m) * 2));
+    if (split) SID_TRY(c->a_lo.alloc((size_t)(kp * m) * 2));
+    SID_TRY(split16(A, k, m, lda, c->a_hi.as<uint16_t>(), split ? c->a_lo.as<uint16_t>() : nullptr, kp, true, 1.f, st));
+    const void *bh = c->a_hi.p, *bl = c->a_lo.p;
+    if (!same) {
+        SID_TRY(c->b_hi.alloc((size_t)(kp * n) * 2));
+        if (split) SID_TRY(c->b_lo.alloc((size_t)(kp * n) * 2));
+        SID_TRY(split16(static_cast<const float*>(B), k, n, ldb, c->b_hi.as<uint16_t>(),
+                        split ? c->b_lo.as<uint16_t>() : nullptr, kp, true, 1.f, st));
+        bh = c->b_hi.p;
+        bl = c->b_lo.p;
+    }
+    const void* As[3] = {c->a_hi.p, c->a_hi.p, c->a_lo.p};
+    const void* Bs[3] = {bh, bl, bh};
+    return gemm_tn(As, Bs, split ? 3 : 1, m, n, k, kp, kp, true, C, ldc, alpha, beta, bn, splitk,
+                   c->ws.as<float>(), (int64_t)(c->ws.bytes / sizeof(float)), err, st);
+}
+
+}  // namespace sid
+
+using namespace sid;
+
+extern "C" int sid_ctx_create(sid_ctx** out)
+{
+    SID_REQUIRE(out, "sid_ctx_create: NULL output");
+    sid_ctx* c = new sid_ctx();
+    cudaGetDevice(&c->device);
+    if (c->errflag.alloc(sizeof(int)) != SID_OK || cudaMemset(c->errflag.p, 0, sizeof(int)) != cudaSuccess) {
+        delete c;
+        *out = nullptr;
+        return SID_ENOMEM;
+    }
+    *out = c;
+    return SID_OK;
+}
+
+extern "C" int sid_ctx_destroy(sid_ctx* c)
+{
+    if (!c) return SID_OK;
+    DBuf* b[] = {&c->a_hi, &c->a_lo, &c->b_hi, &c->b_lo, &c->ws, &c->scal, &c->errflag};
+    for (DBuf* x : b) x->release();
+    for (DBuf& x : c->nn) x.release();
+    delete c;
+    return SID_OK;
+}
+
+extern "C" int sid_ctx_sync(sid_ctx* c, void* stream)
+{
+    SID_REQUIRE(c, "sid_ctx_sync: NULL context");
+    return ctx_sync(c, static_cast<cudaStream_t>(stream));
+}
+
+extern "C" int sid_gram(sid_ctx* c, const float* A, int64_t P, int64_t K, float* G, int prec, void* stream)
+{
+    SID_REQUIRE(c && A && G, "sid_gram: NULL argument");
+    SID_REQUIRE(P > 0 && K > 0, "sid_gram: empty matrix");
+    return contract(c, A, A, false, K, K, P, P, P, G, K, 1.f, 0.f, prec, static_cast<cudaStream_t>(stream));
+}
+
+extern "C" int sid_cross(sid_ctx* c, const float* A, const void* Y, int ydtype, int64_t P, int64_t K, int64_t F,
+                         float* h, int prec, void* stream)
+{
+    SID_REQUIRE(c && A && Y && h, "sid_cross: NULL argument");
+    SID_REQUIRE(P > 0 && K > 0 && F > 0, "sid_cross: empty matrix");
+    SID_REQUIRE(ydtype == SID_DTYPE_F32 || ydtype == SID_DTYPE_F16, "sid_cross: unknown Y dtype %d", ydtype);
+    const bool f16 = ydtype == SID_DTYPE_F16;
+    SID_REQUIRE(!(f16 && prec == SID_PREC_FP32), "sid_cross: an FP16 movie needs SID_PREC_SPLIT or SID_PREC_BF16");
+    return contract(c, A, Y, f16, K, F, P, P, P, h, K, 1.f, 0.f, prec, static_cast<cudaStream_t>(stream));
+}

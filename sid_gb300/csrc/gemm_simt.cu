@@ -1,0 +1,229 @@
+// gemm_simt.cu -- FP32 SIMT GEMM (the plain-precision path of the NNLS
+// contractions) and the FP32 -> 16-bit operand split kernels for gemm_tc.cu.
+//
+// SGEMM, "TN" like the tensor-core kernel: C (m x n, col-major) = A^T B with
+// A k x m and B k x n column-major (k contiguous).  128 x 128 CTA tile,
+// 256 threads, 8 x 8 outputs per thread, BK = 16 staged through shared memory
+// (transposed to [k][m] so the inner loop is an outer product of two float4
+// pairs), register double buffering of the next K slice.
+#include <cuda_bf16.h>
+
+#include "sid_internal.cuh"
+
+namespace sid {
+
+constexpr int SG_BM = 128, SG_BN = 128, SG_BK = 16;
+
+__global__ void __launch_bounds__(256)
+k_sgemm_tn(const float* __restrict__ A, const float* __restrict__ B, float* __restrict__ C, int m, int n, int k,
+           int64_t lda, int64_t ldb, int64_t ldc, int kb_per, int64_t split_stride)
+{
+    __shared__ __align__(16) float As[2][SG_BK][SG_BM + 4];
+    __shared__ __align__(16) float Bs[2][SG_BK][SG_BN + 4];
+    const int tid = threadIdx.x;
+    const int m0 = blockIdx.x * SG_BM, n0 = blockIdx.y * SG_BN;
+    const int kbeg = blockIdx.z * kb_per * SG_BK;
+    const int kend = min(k, kbeg + kb_per * SG_BK);
+    // loader mapping: 256 threads x 8 values = 128 rows x 16 k
+    const int lr = tid >> 1;            // row (m or n) 0..127
+    const int lk = (tid & 1) * 8;       // k offset 0 or 8
+    const int tm = (tid & 15) * 4, tn = (tid >> 4) * 4;  // compute mapping: two 4-wide groups per dim
+
+    float acc[8][8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+#pragma unroll
+        for (int j = 0; j < 8; ++j) acc[i][j] = 0.f;
+
+    float ra[8], rb[8];
+    auto gload = [&](int k0) {
+        const int gm = m0 + lr, gn = n0 + lr;
+#pragma unroll
+        for (int e = 0; e < 8; ++e) {
+            const int kk = k0 + lk + e;
+            ra[e] = (gm < m && kk < kend) ? A[(int64_t)gm * lda + kk] : 0.f;
+            rb[e] = (gn < n && kk < kend) ? B[(int64_t)gn * ldb + kk] : 0.f;
+        }
+    };
+    auto sstore = [&](int buf) {
+#pragma unroll
+        for (int e = 0; e < 8; ++e) {
+            As[buf][lk + e][lr] = ra[e];
+            Bs[buf][lk + e][lr] = rb[e];
+        }
+    };
+    int buf = 0;
+    if (kbeg < kend) {
+        gload(kbeg);
+        sstore(0);
+    }
+    __syncthreads();
+    for (int k0 = kbeg; k0 < kend; k0 += SG_BK) {
+        const bool more = k0 + SG_BK < kend;
+        if (more) gload(k0 + SG_BK);
+#pragma unroll
+        for (int kk = 0; kk < SG_BK; ++kk) {
+            const float4 a0 = *reinterpret_cast<const float4*>(&As[buf][kk][tm]);
+            const float4 a1 = *reinterpret_cast<const float4*>(&As[buf][kk][tm + 64]);
+            const float4 b0 = *reinterpret_cast<const float4*>(&Bs[buf][kk][tn]);
+            const float4 b1 = *reinterpret_cast<const float4*>(&Bs[buf][kk][tn + 64]);
+            const float av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+            const float bv[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+#pragma unroll
+            for (int i = 0; i < 8; ++i)
+#pragma unroll
+                for (int j = 0; j < 8; ++j) acc[i][j] = fmaf(av[i], bv[j], acc[i][j]);
+        }
+        if (more) {
+            sstore(buf ^ 1);
+            __syncthreads();
+            buf ^= 1;
+        }
+    }
+    float* out = C + (int64_t)blockIdx.z * split_stride;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        const int r = m0 + tm + (i < 4 ? i : 60 + i);
+        if (r >= m) continue;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const int c = n0 + tn + (j < 4 ? j : 60 + j);
+            if (c < n) out[(int64_t)r + ldc * c] = acc[i][j];
+        }
+    }
+}
+
+__global__ void k_splitk_reduce_simt(const float* __restrict__ part, int nsplit, int64_t split_stride, int m, int n,
+                                     float* __restrict__ C, int64_t ldc, float alpha, float beta)
+{
+    const int64_t total = (int64_t)m * n;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+        const int r = (int)(i % m);
+        const int64_t c = i / m;
+        float s = 0.f;
+        for (int z = 0; z < nsplit; ++z) s += part[z * split_stride + r + (int64_t)m * c];
+        float* d = C + r + ldc * c;
+        *d = (beta != 0.f) ? alpha * s + beta * *d : alpha * s;
+    }
+}
+
+// C = alpha * A^T B + beta * C (FP32).  ws >= splitk*m*n floats when splitk > 1
+// or alpha/beta are not (1, 0).
+int sgemm_tn(const float* A, const float* B, int64_t m, int64_t n, int64_t k, int64_t lda, int64_t ldb, float* C,
+             int64_t ldc, float alpha, float beta, float* ws, int64_t ws_elems, cudaStream_t st)
+{
+    SID_REQUIRE(m > 0 && n > 0 && k > 0, "sgemm: empty problem");
+    const int64_t tiles = cdiv(m, SG_BM) * cdiv(n, SG_BN);
+    const int64_t nkb = cdiv(k, SG_BK);
+    int splitk = 1;
+    while (tiles * splitk < 4 * 152 && nkb / (splitk + 1) >= 16) ++splitk;
+    const int kb_per = (int)cdiv(nkb, splitk);
+    splitk = (int)cdiv(nkb, kb_per);
+    const bool direct = splitk == 1 && alpha == 1.f && beta == 0.f;
+    float* out = C;
+    int64_t ldo = ldc, ss = 0;
+    if (!direct) {
+        ss = m * n;
+        SID_REQUIRE(ws && ws_elems >= splitk * ss, "sgemm: workspace too small");
+        out = ws;
+        ldo = m;
+    }
+    dim3 grid((unsigned)cdiv(m, SG_BM), (unsigned)cdiv(n, SG_BN), (unsigned)splitk);
+    k_sgemm_tn<<<grid, 256, 0, st>>>(A, B, out, (int)m, (int)n, (int)k, lda, ldb, ldo, kb_per, ss);
+    SID_CHECK_LAUNCH();
+    if (!direct) {
+        k_splitk_reduce_simt<<<1024, 256, 0, st>>>(ws, splitk, ss, (int)m, (int)n, C, ldc, alpha, beta);
+        SID_CHECK_LAUNCH();
+    }
+    return SID_OK;
+}
+
+int64_t sgemm_ws_elems(int64_t m, int64_t n, int64_t k)
+{
+    const int64_t tiles = cdiv(m, SG_BM) * cdiv(n, SG_BN);
+    const int64_t nkb = cdiv(k, SG_BK);
+    int splitk = 1;
+    while (tiles * splitk < 4 * 152 && nkb / (splitk + 1) >= 16) ++splitk;
+    return (int64_t)splitk * m * n;
+}
+
+// ------------------------------------------------ FP32 -> 16-bit splits ----
+// dst_hi/dst_lo: (rows x cols) with leading dimension ld (>= rows, multiple of
+// 8), rows = the reduction dimension (contiguous).  hi = round(src*scale),
+// lo = round(src*scale - hi).  Padding rows [rows, ld) are zero.
+template <bool BF16>
+__global__ void k_split16(const float* __restrict__ src, int64_t rows, int64_t cols, int64_t lds,
+                          uint16_t* __restrict__ hi, uint16_t* __restrict__ lo, int64_t ld, float scale)
+{
+    const int64_t total = ld * cols;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = i % ld, c = i / ld;
+        const float v = (r < rows) ? src[r + lds * c] * scale : 0.f;
+        uint16_t h, l;
+        if (BF16) {
+            const __nv_bfloat16 bh = __float2bfloat16_rn(v);
+            const __nv_bfloat16 bl = __float2bfloat16_rn(v - __bfloat162float(bh));
+            h = __bfloat16_as_ushort(bh);
+            l = __bfloat16_as_ushort(bl);
+        } else {
+            const __half fh = __float2half_rn(v);
+            const __half fl = __float2half_rn(v - __half2float(fh));
+            h = __half_as_ushort(fh);
+            l = __half_as_ushort(fl);
+        }
+        hi[i] = h;
+        if (lo) lo[i] = l;
+    }
+}
+
+// 16-bit copy with row padding (for FP16 inputs whose leading dimension is
+// not a multiple of 8).
+__global__ void k_copy16_pad(const uint16_t* __restrict__ src, int64_t rows, int64_t cols, int64_t lds,
+                             uint16_t* __restrict__ dst, int64_t ld)
+{
+    const int64_t total = ld * cols;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = i % ld, c = i / ld;
+        dst[i] = (r < rows) ? src[r + lds * c] : (uint16_t)0;
+    }
+}
+
+// max |x| over n floats -> out (float bits, atomicMax; out must start at 0)
+__global__ void k_absmax(const float* __restrict__ x, int64_t n, unsigned int* __restrict__ out)
+{
+    float m = 0.f;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        m = fmaxf(m, fabsf(x[i]));
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, off));
+    if ((threadIdx.x & 31) == 0 && m > 0.f) atomicMax(out, __float_as_uint(m));
+}
+
+int split16(const float* src, int64_t rows, int64_t cols, int64_t lds, uint16_t* hi, uint16_t* lo, int64_t ld,
+            bool bf16, float scale, cudaStream_t st)
+{
+    if (bf16)
+        k_split16<true><<<2048, 256, 0, st>>>(src, rows, cols, lds, hi, lo, ld, scale);
+    else
+        k_split16<false><<<2048, 256, 0, st>>>(src, rows, cols, lds, hi, lo, ld, scale);
+    SID_CHECK_LAUNCH();
+    return SID_OK;
+}
+
+int copy16_pad(const uint16_t* src, int64_t rows, int64_t cols, int64_t lds, uint16_t* dst, int64_t ld,
+               cudaStream_t st)
+{
+    k_copy16_pad<<<2048, 256, 0, st>>>(src, rows, cols, lds, dst, ld);
+    SID_CHECK_LAUNCH();
+    return SID_OK;
+}
+
+int absmax(const float* x, int64_t n, unsigned int* out, cudaStream_t st)
+{
+    SID_CUDA_TRY(cudaMemsetAsync(out, 0, sizeof(unsigned int), st));
+    k_absmax<<<1024, 256, 0, st>>>(x, n, out);
+    SID_CHECK_LAUNCH();
+    return SID_OK;
+}
+
+}  // namespace sid

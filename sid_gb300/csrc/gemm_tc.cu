@@ -1,0 +1,411 @@
+// gemm_tc.cu -- tcgen05 tensor-core GEMM for the NNLS Gram and cross products.
+//
+//   C (m x n, column-major, ldc) = sum_{p < npass} A_p^T B_p
+//   A_p: k x m column-major 16-bit (the reduction index k is contiguous),
+//   B_p: k x n column-major 16-bit, both BF16 or both FP16; FP32 accumulation.
+// This is the "TN" form every contraction of the path takes: S'S and S'Y with
+// the library and the movie stored pixel-major (LS_nnls.m:76,82,
+// fast_nnls.m:54-57, T_update.m:24-25), and G*x in the NNLS iterations.
+// Passing (hi, lo) splits of FP32 operands as extra passes gives the split
+// precision products (hi*hi + hi*lo + lo*hi) with FP32 accumulation in TMEM.
+//
+// Kernel: one 128 x BN output tile per CTA (optionally a K range of it, for
+// split-K), 6 warps.  One thread drives a STAGES-deep TMA ring (128B-swizzled
+// 64-element K blocks, completion on "full" mbarriers); one thread issues
+// tcgen05.mma (cta_group::1, M=128, N=BN, K=16 per instruction) into one of two
+// TMEM accumulators and releases each stage through tcgen05.commit on its
+// "empty" mbarrier; four warps read finished accumulators back with tcgen05.ld
+// (warp w owns TMEM lanes 32w..32w+31 = tile rows) and add them to the output.
+// Every mbarrier wait is bounded (ptx.cuh); on a timeout the CTA records the
+// error, stops issuing, waits (bounded) for issued MMAs, frees TMEM and exits.
+#include <cuda.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "ptx.cuh"
+#include "sid_internal.cuh"
+
+namespace sid {
+
+constexpr int GEMM_BM = 128;
+constexpr int GEMM_BK = 64;  // 64 x 16-bit = 128 bytes: one swizzle row
+constexpr int GEMM_MAXPASS = 3;
+constexpr int kErrTimeoutGemm = 2;
+
+struct GemmMaps {
+    CUtensorMap a[GEMM_MAXPASS];
+    CUtensorMap b[GEMM_MAXPASS];
+};
+
+__device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t saddr)
+{
+    // tcgen05 shared-memory descriptor, K-major operand, 128-byte swizzle:
+    // start address >> 4 (bits 0-13), leading byte offset 16 B (ignored for
+    // swizzled K-major), stride byte offset 1024 B = 8 rows x 128 B (bits 32-45),
+    // fixed 0b001 at bits 46-48, swizzle mode 2 = 128B at bits 61-63.
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
+    d |= (uint64_t)(16u >> 4) << 16;
+    d |= (uint64_t)(1024u >> 4) << 32;
+    d |= (uint64_t)1 << 46;
+    d |= (uint64_t)2 << 61;
+    return d;
+}
+
+__device__ __forceinline__ uint32_t instr_desc(int n, bool bf16)
+{
+    // kind::f16 instruction descriptor: D = F32 (bits 4-5 = 1), A/B format
+    // (bits 7-9, 10-12: 0 = F16, 1 = BF16), both K-major, N>>3 at bits 17-22,
+    // M>>4 at bits 24-28.
+    const uint32_t fmt = bf16 ? 1u : 0u;
+    return (1u << 4) | (fmt << 7) | (fmt << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(GEMM_BM >> 4) << 24);
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y, uint64_t* bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+            smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc, int acc)
+{
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc)
+        : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t* bar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32])
+{
+    uint32_t r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+template <int BN, int STAGES>
+struct GemmSmem {
+    static constexpr int A_BYTES = GEMM_BM * GEMM_BK * 2;  // 16 KB
+    static constexpr int B_BYTES = BN * GEMM_BK * 2;
+    static constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
+    static constexpr int TOTAL = STAGES * STAGE_BYTES + 1024 /* alignment slack */;
+};
+
+// grid: (ceil(m/128), ceil(n/BN), splitk).  out + z*split_stride receives the
+// partial sum of K blocks [z*kb_per, (z+1)*kb_per) of every pass.
+//
+// Warp roles (192 threads): warps 0-3 drain the accumulator (warp w owns TMEM
+// lanes 32w..32w+31, i.e. tile rows), warp 4 lane 0 is the TMA producer, warp 5
+// lane 0 issues the MMAs.  The tensor-core FP32 accumulator does not round to
+// nearest, so long K chains drift: the K range is cut into chunks of KCHUNK
+// blocks, each accumulated in one of two TMEM buffers while the previous chunk
+// is drained and added (round-to-nearest) into the output tile.
+constexpr int GEMM_KCHUNK = 16;  // 16 x 64 = 1024 reduction elements per chain
+
+template <int BN, int STAGES>
+__global__ void __launch_bounds__(192, 1)
+k_gemm_tc(const __grid_constant__ GemmMaps maps, int npass, int m, int n, int nkb, int kb_per, int bf16,
+          float* __restrict__ out, int64_t ldc, int64_t split_stride, int* __restrict__ err)
+{
+    using SM = GemmSmem<BN, STAGES>;
+    constexpr uint32_t ACC_COLS = BN <= 32 ? 32 : (BN <= 64 ? 64 : (BN <= 128 ? 128 : 256));
+    constexpr uint32_t TMEM_COLS = 2 * ACC_COLS;  // two accumulators
+    extern __shared__ uint8_t gsm_raw[];
+    uint8_t* gsm = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(gsm_raw) + 1023) & ~uintptr_t(1023));
+    __shared__ __align__(8) uint64_t full[STAGES], empty[STAGES], tfull[2], tempty[2];
+    __shared__ uint32_t tmem_slot;
+    __shared__ int abort_flag;
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int m0 = blockIdx.x * GEMM_BM, n0 = blockIdx.y * BN;
+    const int kb0 = blockIdx.z * kb_per;
+    const int kb1 = min(nkb, kb0 + kb_per);
+    const int nloc = kb1 > kb0 ? (kb1 - kb0) : 0;
+    const int nchunk = (nloc + GEMM_KCHUNK - 1) / GEMM_KCHUNK;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < STAGES; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(&tfull[b], 1);
+            mbar_init(&tempty[b], 128);
+        }
+        abort_flag = 0;
+        fence_mbar_init();
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
+                     "n"(TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tmem_slot;
+    float* dst = out + (int64_t)blockIdx.z * split_stride;
+
+    if (warp == 4) {
+        if (lane == 0) {
+            // TMA producer: chunk -> pass -> k block
+            int it = 0;
+            for (int c = 0; c < nchunk && !abort_flag; ++c) {
+                const int cb0 = kb0 + c * GEMM_KCHUNK, cb1 = min(kb1, cb0 + GEMM_KCHUNK);
+                for (int pass = 0; pass < npass; ++pass) {
+                    for (int kb = cb0; kb < cb1; ++kb, ++it) {
+                        const int s = it % STAGES;
+                        if (it >= STAGES && !mbar_wait(&empty[s], (uint32_t)(((it / STAGES) - 1) & 1), err)) {
+                            atomicExch(&abort_flag, 1);
+                            break;
+                        }
+                        if (*(volatile int*)&abort_flag) break;
+                        uint8_t* sa = gsm + s * SM::STAGE_BYTES;
+                        uint8_t* sb = sa + SM::A_BYTES;
+                        mbar_arrive_expect_tx(&full[s], SM::STAGE_BYTES);
+                        tma_load_2d(sa, &maps.a[pass], kb * GEMM_BK, m0, &full[s]);
+                        tma_load_2d(sb, &maps.b[pass], kb * GEMM_BK, n0, &full[s]);
+                    }
+                    if (*(volatile int*)&abort_flag) break;
+                }
+            }
+        }
+    } else if (warp == 5) {
+        if (lane == 0) {
+            // MMA issuer: chunk c accumulates into TMEM buffer c & 1
+            const uint32_t idesc = instr_desc(BN, bf16 != 0);
+            int it = 0;
+            bool ok = true;
+            for (int c = 0; c < nchunk && ok; ++c) {
+                const int b = c & 1;
+                if (c >= 2 && !mbar_wait(&tempty[b], (uint32_t)(((c >> 1) - 1) & 1), err)) {
+                    ok = false;
+                    break;
+                }
+                tc_fence_after();
+                const uint32_t acc = tmem + (uint32_t)(b * ACC_COLS);
+                const int cb0 = kb0 + c * GEMM_KCHUNK, cb1 = min(kb1, cb0 + GEMM_KCHUNK);
+                bool first = true;
+                for (int pass = 0; pass < npass && ok; ++pass) {
+                    for (int kb = cb0; kb < cb1; ++kb, ++it) {
+                        const int s = it % STAGES;
+                        if (!mbar_wait(&full[s], (uint32_t)((it / STAGES) & 1), err)) {
+                            ok = false;
+                            break;
+                        }
+                        tc_fence_after();
+                        const uint32_t sa = smem_u32(gsm + s * SM::STAGE_BYTES);
+                        const uint32_t sb = sa + SM::A_BYTES;
+#pragma unroll
+                        for (int kk = 0; kk < GEMM_BK / 16; ++kk) {
+                            // advance 16 elements = 32 bytes inside the 128-byte swizzle row
+                            mma_bf16(acc, smem_desc_sw128(sa + kk * 32), smem_desc_sw128(sb + kk * 32), idesc,
+                                     first ? 0 : 1);
+                            first = false;
+                        }
+                        mma_commit(&empty[s]);
+                    }
+                }
+                mma_commit(&tfull[b]);  // arrives when this chunk's MMAs have completed
+            }
+            if (!ok) atomicExch(&abort_flag, 1);
+        }
+    } else {
+        // drain warps 0-3: add each finished chunk into the output tile
+        const int row = m0 + warp * 32 + lane;
+        for (int c = 0; c < nchunk; ++c) {
+            const int b = c & 1;
+            const bool ok = __all_sync(0xffffffffu, mbar_wait(&tfull[b], (uint32_t)((c >> 1) & 1), err));
+            if (!ok) break;
+            tc_fence_after();
+#pragma unroll 1
+            for (int c0 = 0; c0 < BN; c0 += 32) {
+                float v[32];
+                tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(b * ACC_COLS + c0), v);
+                if (row < m) {
+#pragma unroll
+                    for (int j = 0; j < 32; ++j) {
+                        const int col = n0 + c0 + j;
+                        if (col < n) {
+                            float* d = dst + (int64_t)row + ldc * col;
+                            *d = (c == 0) ? v[j] : *d + v[j];
+                        }
+                    }
+                }
+            }
+            tc_fence_before();
+            mbar_arrive(&tempty[b]);
+        }
+        if (nchunk == 0 && row < m)
+            for (int col = n0; col < min(n, n0 + BN); ++col) dst[(int64_t)row + ldc * col] = 0.f;
+    }
+    __syncwarp();
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "n"(TMEM_COLS) : "memory");
+    }
+    if (threadIdx.x == 0 && abort_flag && err) atomicExch(err, kErrTimeoutGemm);
+}
+
+// Sum split-K partials: C = alpha * sum_z P[z] + beta * C (beta == 0 ignores C).
+__global__ void k_splitk_reduce(const float* __restrict__ part, int nsplit, int64_t split_stride, int m, int n,
+                                int64_t ldp, float* __restrict__ C, int64_t ldc, float alpha, float beta)
+{
+    const int64_t total = (int64_t)m * n;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+        const int r = (int)(i % m);
+        const int64_t c = i / m;
+        float s = 0.f;
+        for (int z = 0; z < nsplit; ++z) s += part[z * split_stride + r + ldp * c];
+        float* d = C + r + ldc * c;
+        *d = (beta != 0.f) ? alpha * s + beta * *d : alpha * s;
+    }
+}
+
+// ----------------------------------------------------------- host side ----
+static int make_map(CUtensorMap* map, const void* base, int64_t rows, int64_t kdim, int64_t ld, int box_rows,
+                    bool bf16)
+{
+    // 2-D tensor: inner dimension k (contiguous), outer dimension rows with stride ld elements
+    SID_REQUIRE(((uintptr_t)base & 15) == 0, "gemm: operand base address not 16-byte aligned");
+    SID_REQUIRE((ld * 2) % 16 == 0, "gemm: leading dimension %lld not a multiple of 8 elements", (long long)ld);
+    cuuint64_t dims[2] = {(cuuint64_t)kdim, (cuuint64_t)rows};
+    cuuint64_t strides[1] = {(cuuint64_t)(ld * 2)};
+    cuuint32_t box[2] = {GEMM_BK, (cuuint32_t)box_rows};
+    cuuint32_t estr[2] = {1, 1};
+    // resolved through the runtime so libsid does not link libcuda directly
+    using EncodeFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+    static EncodeFn encode = nullptr;
+    if (!encode) {
+        void* fn = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess || q != cudaDriverEntryPointSuccess || !fn) {
+            set_error("cuTensorMapEncodeTiled is not available from the driver");
+            return SID_ECUDA;
+        }
+        encode = reinterpret_cast<EncodeFn>(fn);
+    }
+    CUresult r = encode(map, bf16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16,
+                                        2, const_cast<void*>(base), dims, strides, box, estr,
+                                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                                        CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        set_error("cuTensorMapEncodeTiled failed (CUresult %d)", (int)r);
+        return SID_ECUDA;
+    }
+    return SID_OK;
+}
+
+template <int BN, int STAGES>
+static int launch_gemm(const GemmMaps& maps, int npass, int m, int n, int nkb, int splitk, bool bf16, float* out,
+                       int64_t ldc, int64_t split_stride, int* err, cudaStream_t st)
+{
+    using SM = GemmSmem<BN, STAGES>;
+    static bool configured = false;
+    if (!configured) {
+        SID_CUDA_TRY(cudaFuncSetAttribute(k_gemm_tc<BN, STAGES>, cudaFuncAttributeMaxDynamicSharedMemorySize, SM::TOTAL));
+        configured = true;
+    }
+    const int kb_per = (int)cdiv(nkb, splitk);
+    dim3 grid((unsigned)cdiv(m, GEMM_BM), (unsigned)cdiv(n, BN), (unsigned)splitk);
+    k_gemm_tc<BN, STAGES><<<grid, 192, SM::TOTAL, st>>>(maps, npass, m, n, nkb, kb_per, bf16 ? 1 : 0, out, ldc,
+                                                         split_stride, err);
+    SID_CHECK_LAUNCH();
+    return SID_OK;
+}
+
+// Tile width and split-K choice: the widest tile whose tile count fills the
+// 152 SMs best, then split K until there are >= 4 waves of work or the K
+// range per split would drop below 8 blocks.
+void gemm_autotune(int m, int n, int nkb, int* bn, int* splitk)
+{
+    const int sms = 152;
+    const int cands[3] = {256, 128, 64};
+    double best = -1.0;
+    int bbn = 128;
+    for (int c : cands) {
+        const int64_t tiles = cdiv(m, GEMM_BM) * cdiv(n, c);
+        const double waves = (double)tiles / sms;
+        const double eff = waves / std::ceil(waves) * ((double)n / (double)(cdiv(n, c) * c));
+        if (eff > best + 1e-9) { best = eff; bbn = c; }
+    }
+    const int64_t tiles = cdiv(m, GEMM_BM) * cdiv(n, bbn);
+    int s = 1;
+    while (tiles * s < 4 * sms && nkb / (s + 1) >= 8) ++s;
+    *bn = bbn;
+    *splitk = s;
+}
+
+// out (m x n, ldc) = sum_p A_p^T B_p; A_p: k x m (lda), B_p: k x n (ldb), 16-bit.
+// ws: >= splitk * ldc * n floats when splitk > 1.
+int gemm_tn(const void* const* A, const void* const* B, int npass, int64_t m, int64_t n, int64_t k, int64_t lda,
+            int64_t ldb, bool bf16, float* C, int64_t ldc, float alpha, float beta, int bn, int splitk,
+            float* ws, int64_t ws_elems, int* err, cudaStream_t st)
+{
+    SID_REQUIRE(npass >= 1 && npass <= GEMM_MAXPASS, "gemm: npass %d outside [1,3]", npass);
+    SID_REQUIRE(m > 0 && n > 0 && k > 0, "gemm: empty problem");
+    const int nkb = (int)cdiv(k, GEMM_BK);
+    if (bn <= 0 || splitk <= 0) gemm_autotune((int)m, (int)n, nkb, &bn, &splitk);
+    splitk = std::max(1, std::min(splitk, nkb));
+    GemmMaps maps;
+    std::memset(&maps, 0, sizeof(maps));
+    for (int p = 0; p < npass; ++p) {
+        SID_TRY(make_map(&maps.a[p], A[p], m, k, lda, GEMM_BM, bf16));
+        SID_TRY(make_map(&maps.b[p], B[p], n, k, ldb, bn, bf16));
+    }
+    const bool direct = (splitk == 1 && alpha == 1.f && beta == 0.f);
+    float* out = C;
+    int64_t ldo = ldc, sstride = 0;
+    if (!direct) {
+        ldo = m;
+        sstride = m * n;
+        SID_REQUIRE(ws && ws_elems >= splitk * sstride, "gemm: split-K workspace too small");
+        out = ws;
+    }
+    int rc;
+    switch (bn) {
+    case 256: rc = launch_gemm<256, 4>(maps, npass, (int)m, (int)n, nkb, splitk, bf16, out, ldo, sstride, err, st); break;
+    case 128: rc = launch_gemm<128, 6>(maps, npass, (int)m, (int)n, nkb, splitk, bf16, out, ldo, sstride, err, st); break;
+    case 64: rc = launch_gemm<64, 8>(maps, npass, (int)m, (int)n, nkb, splitk, bf16, out, ldo, sstride, err, st); break;
+    default: set_error("gemm: unsupported tile width %d", bn); return SID_EINVAL;
+    }
+    SID_TRY(rc);
+    if (!direct) {
+        k_splitk_reduce<<<1024, 256, 0, st>>>(ws, splitk, sstride, (int)m, (int)n, m, C, ldc, alpha, beta);
+        SID_CHECK_LAUNCH();
+    }
+    return SID_OK;
+}
+
+}  // namespace sid

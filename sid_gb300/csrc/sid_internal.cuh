@@ -136,7 +136,7 @@ struct sid_plan {
     bool spec_f32, spec_i16;
     sid::DBuf khat_f32;         // [f][b'a'][abc] float2
     sid::DBuf khat_i16;         // [f][b'a'][abc] short2 mantissas
-    sid::DBuf rstep;            // [f][b'a'] power-of-two step of each 16-bit row
+    sid::DBuf rstep;            // [f][b'a'] step (rowmax/32767) of each 16-bit row
     sid::DBuf twiddle;          // L float2: exp(-2 pi i k / L)
     // workspaces
     sid::DBuf vp, ip, bp, ipart, vhat, ihat, bhat, red;

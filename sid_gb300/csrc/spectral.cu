@@ -9,8 +9,8 @@
 //   Ihat[b'a'](f) = sum_abc Khat[f][b'a'][abc] * Vhat[abc](f)            (forward)
 //   Bhat[abc](f)  = sum_b'a' conj(Khat[f][b'a'][abc]) * Ihat[b'a'](f)    (adjoint)
 // The tap spectra Khat are computed once per plan and kept resident, in FP32
-// or in 16-bit block floating point (int16 mantissas, one power-of-two step
-// per frequency row: 15-bit precision where the row's energy is).  Per projection the cost is one streaming
+// or in 16-bit block floating point (int16 mantissas, one FP32 step per
+// frequency row: 15-bit precision relative to the row's largest entry).  Per projection the cost is one streaming
 // pass over Khat (HBM bound) plus small real DFTs of the N*N*Z input and N*N
 // output channels.  Real inputs use the half spectrum f1 in [0, L/2].
 #include <cmath>
@@ -29,7 +29,7 @@ static inline int64_t spec_nin_pad(const sid_plan* p) { return cdiv(p->N * p->N 
 //   mode 0: write FP32 spectra (if k32) and the per-row max |Re|,|Im| (rowmax,
 //           float bits, atomicMax; values are >= 0 so integer order = float order)
 //   mode 1: write 16-bit block-floating-point spectra: int16 mantissas with the
-//           row's power-of-two step rstep[f*n_out + o] (value = mantissa * step)
+//           row's step rstep[f*n_out + o] = rowmax/32767 (value = mantissa * step)
 constexpr int KB_CH = 8;
 
 __global__ void k_build_khat(const float* __restrict__ taps, const float2* __restrict__ tw,
@@ -99,26 +99,20 @@ __global__ void k_build_khat(const float* __restrict__ taps, const float2* __res
             for (int off = KB_CH / 2; off > 0; off >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, off));
             if (live && ch == 0 && m > 0.f) atomicMax(rowmax + (int64_t)f * n_out + o, __float_as_uint(m));
         } else if (live) {
-            const float inv = 1.0f / rstep[(int64_t)f * n_out + o];  // exact: power of two
-            const float re = fminf(fmaxf(rintf(acc.x * inv), -32767.f), 32767.f);
-            const float im = fminf(fmaxf(rintf(acc.y * inv), -32767.f), 32767.f);
+            const float st = rstep[(int64_t)f * n_out + o];
+            const float re = fminf(fmaxf(rintf(acc.x / st), -32767.f), 32767.f);
+            const float im = fminf(fmaxf(rintf(acc.y / st), -32767.f), 32767.f);
             k16[idx] = make_short2((short)re, (short)im);
         }
     }
 }
 
-// step = smallest power of two with rowmax / step <= 32767 (1 for empty rows)
+// step = rowmax / 32767 (the row's largest component maps to +-32767), 1 for empty rows
 __global__ void k_row_steps(const unsigned int* __restrict__ rowmax, float* __restrict__ rstep, int64_t n)
 {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const float m = __uint_as_float(rowmax[i]);
-        float st = 1.f;
-        if (m > 0.f) {
-            int e;
-            frexpf(m / 32767.f, &e);  // m/32767 = f * 2^e with f in [0.5, 1)
-            st = ldexpf(1.f, e);
-        }
-        rstep[i] = st;
+        rstep[i] = (m > 0.f) ? m / 32767.f : 1.f;
     }
 }
 
