@@ -132,6 +132,36 @@ int sid_gram(sid_ctx* ctx, const float* A, int64_t P, int64_t K, float* G, int p
 int sid_cross(sid_ctx* ctx, const float* A, const void* Y, int ydtype, int64_t P, int64_t K, int64_t F,
               float* h, int prec, void* stream);
 
+/* ---- NNLS solvers -----------------------------------------------------------
+ * Options mirror the reference's opts fields and defaults. */
+typedef struct {
+    double lambda;     /* L1 weight: LS_nnls h = A'Y - lambda; fast_nnls df = -A'Y + lambda */
+    int64_t sample;    /* convergence-fit window: LS_nnls 300, fast_nnls 30 */
+    double tol;        /* LS_nnls 1e-7, fast_nnls 1e-6 */
+    double tol_;       /* fit-residual tolerance: LS_nnls 1e-2, fast_nnls 1e-1 */
+    int64_t max_iter;  /* 2000 */
+    int use_std;       /* LS_nnls: least standard deviation instead of least squares */
+    int tol_p;         /* fast_nnls: 1 = log l1 step, 2 = log l2 step */
+} sid_nnls_opts;
+void sid_ls_nnls_defaults(sid_nnls_opts* opts);   /* LS_nnls.m:59-73 */
+void sid_fast_nnls_defaults(sid_nnls_opts* opts); /* fast_nnls.m:21-51 */
+
+/* [X, G] = LS_nnls(A, Y, opts, G, x)   LS_nnls.m:1
+ * A: P x K single; Y: P x F single or half (ydtype); all device arrays.
+ * G: K x K, read when g_given, else written when non-NULL.
+ * X: K x F, the start point when x_given (else zeros), the solution on return.
+ * iters (optional, F int32): iteration at which each column retired.
+ * prec: SID_PREC_FP32 or SID_PREC_SPLIT. */
+int sid_ls_nnls(sid_ctx* ctx, const float* A, const void* Y, int ydtype, int64_t P, int64_t K, int64_t F,
+                const sid_nnls_opts* opts, float* G, int g_given, float* X, int x_given, int prec,
+                int32_t* iters, void* stream);
+/* [xx, Q] = fast_nnls(A, Y, opts) with opts.warm_start = warm_start (K x F, or
+ * NULL for a zero start)   fast_nnls.m:1.  Q_out (optional): the normalised
+ * Gram.  X: K x F solution (diag(h) * x, fast_nnls.m:197-199). */
+int sid_fast_nnls(sid_ctx* ctx, const float* A, const void* Y, int ydtype, int64_t P, int64_t K, int64_t F,
+                  const sid_nnls_opts* opts, const float* warm_start, float* X, float* Q_out, int prec,
+                  int32_t* iters, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

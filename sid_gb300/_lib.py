@@ -60,10 +60,15 @@ SIGNATURES = {
     "sid_ctx_sync": [P, P],
     "sid_gram": [P, P, I64, I64, P, I32, P],
     "sid_cross": [P, P, P, I32, I64, I64, I64, P, I32, P],
+    "sid_ls_nnls_defaults": [P],
+    "sid_fast_nnls_defaults": [P],
+    "sid_ls_nnls": [P, P, P, I32, I64, I64, I64, P, P, I32, P, I32, I32, P, P],
+    "sid_fast_nnls": [P, P, P, I32, I64, I64, I64, P, P, P, P, I32, P, P],
 }
 PREC = {"fp32": 0, "split": 1, "bf16": 2}
 DTYPE_F32, DTYPE_F16 = 0, 1
-_RESTYPES = {"sid_last_error": ctypes.c_char_p}
+_RESTYPES = {"sid_last_error": ctypes.c_char_p, "sid_ls_nnls_defaults": None,
+             "sid_fast_nnls_defaults": None}
 
 _lib = None
 

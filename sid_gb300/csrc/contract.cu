@@ -28,12 +28,6 @@ int copy16_pad(const uint16_t* src, int64_t rows, int64_t cols, int64_t lds, uin
 int absmax(const float* x, int64_t n, unsigned int* out, cudaStream_t st);
 }  // namespace sid
 
-struct sid_ctx {
-    int device;
-    sid::DBuf a_hi, a_lo, b_hi, b_lo, ws, scal, errflag;
-    sid::DBuf nn[12];  // NNLS state
-};
-
 namespace sid {
 
 int ctx_sync(sid_ctx* c, cudaStream_t st)

@@ -157,3 +157,10 @@ int vp_to_v(const sid_plan* p, const float* vp, float* V, int64_t Z, cudaStream_
 int mask_vp(const sid_plan* p, float* vp, int64_t Z, cudaStream_t st);
 inline int64_t vol_plane_elems(const sid_plan* p) { return p->N * p->N * p->Lx * p->Ly; }
 }  // namespace sid
+
+// NNLS / contraction context (declared in sid.h as struct sid_ctx).
+struct sid_ctx {
+    int device;
+    sid::DBuf a_hi, a_lo, b_hi, b_lo, ws, scal, errflag;
+    sid::DBuf nn[16];  // NNLS iteration state
+};

@@ -67,3 +67,97 @@ class Context:
         _lib.call("sid_cross", self._ctx, A.data_ptr(), Yd.data_ptr(), _lib.DTYPE_F16 if half else _lib.DTYPE_F32,
                   P, K, F, h.data_ptr(), _lib.PREC[prec], _stream_ptr())
         return h
+
+
+class NnlsOpts(ctypes.Structure):
+    """sid_nnls_opts: the reference's opts fields for LS_nnls / fast_nnls."""
+    _fields_ = [("lambda_", ctypes.c_double), ("sample", ctypes.c_int64), ("tol", ctypes.c_double),
+                ("tol_", ctypes.c_double), ("max_iter", ctypes.c_int64), ("use_std", ctypes.c_int),
+                ("tol_p", ctypes.c_int)]
+
+
+def _opts(kind: str, opts: dict | None) -> NnlsOpts:
+    o = NnlsOpts()
+    getattr(_lib.load(), f"sid_{kind}_defaults")(ctypes.byref(o))
+    for k, v in (opts or {}).items():
+        if k == "lambda":
+            o.lambda_ = float(v)
+        elif k in ("sample", "max_iter"):
+            setattr(o, k, int(v))
+        elif k in ("tol", "tol_"):
+            setattr(o, k, float(v))
+        elif k in ("use_std", "tol_p"):
+            setattr(o, k, int(bool(v)) if k == "use_std" else int(v))
+        elif k in ("warm_start", "gpu", "gpu_id", "gpu_ids", "display", "total"):
+            if k == "total" and v:
+                raise NotImplementedError("fast_nnls: opts.total (one line search for all columns) is not supported")
+        else:
+            raise ValueError(f"unknown NNLS option {k!r}")
+    return o
+
+
+def _movie(Y):
+    half = (isinstance(Y, torch.Tensor) and Y.dtype == torch.float16) or \
+           (isinstance(Y, np.ndarray) and Y.dtype == np.float16)
+    return (_to_device_half(Y) if half else to_device(Y)), half
+
+
+def _ls_nnls(self, A, Y, opts=None, G=None, x=None, prec="split", return_iters=False):
+    """[X, G] = LS_nnls(A, Y, opts, G, x) (LS_nnls.m:1) on the GPU."""
+    A = to_device(A)
+    Yd, half = _movie(Y)
+    P, K = A.shape
+    F = Yd.shape[1]
+    o = _opts("ls_nnls", opts)
+    Gd = to_device(G) if G is not None else _fortran_tensor((K, K), A.device)
+    X = to_device(x).clone() if x is not None else _fortran_tensor((K, F), A.device)
+    it = torch.zeros(F, dtype=torch.int32, device=A.device)
+    _lib.call("sid_ls_nnls", self._ctx, A.data_ptr(), Yd.data_ptr(), _lib.DTYPE_F16 if half else _lib.DTYPE_F32,
+              P, K, F, ctypes.byref(o), Gd.data_ptr(), 1 if G is not None else 0, X.data_ptr(),
+              1 if x is not None else 0, _lib.PREC[prec], it.data_ptr(), _stream_ptr())
+    return (X, Gd, it) if return_iters else (X, Gd)
+
+
+def _fast_nnls(self, A, Y, opts=None, prec="split", return_iters=False):
+    """[xx, Q] = fast_nnls(A, Y, opts) (fast_nnls.m:1) on the GPU; opts may
+    carry warm_start (K x F)."""
+    A = to_device(A)
+    Yd, half = _movie(Y)
+    P, K = A.shape
+    F = Yd.shape[1]
+    opts = dict(opts or {})
+    warm = opts.get("warm_start", None)
+    if warm is not None and np.ndim(warm) == 0:
+        raise NotImplementedError("fast_nnls: warm_start == 1 (inverse-Gram start) is not supported")
+    W = to_device(warm) if warm is not None and np.size(warm) else None
+    o = _opts("fast_nnls", opts)
+    X = _fortran_tensor((K, F), A.device)
+    Q = _fortran_tensor((K, K), A.device)
+    it = torch.zeros(F, dtype=torch.int32, device=A.device)
+    _lib.call("sid_fast_nnls", self._ctx, A.data_ptr(), Yd.data_ptr(), _lib.DTYPE_F16 if half else _lib.DTYPE_F32,
+              P, K, F, ctypes.byref(o), W.data_ptr() if W is not None else None, X.data_ptr(), Q.data_ptr(),
+              _lib.PREC[prec], it.data_ptr(), _stream_ptr())
+    return (X, Q, it) if return_iters else (X, Q)
+
+
+Context.ls_nnls = _ls_nnls
+Context.fast_nnls = _fast_nnls
+
+_DEFAULT_CTX = None
+
+
+def _ctx():
+    global _DEFAULT_CTX
+    if _DEFAULT_CTX is None:
+        _DEFAULT_CTX = Context()
+    return _DEFAULT_CTX
+
+
+def LS_nnls(A, Y, opts=None, G=None, x=None):
+    """[X, G] = LS_nnls(A, Y, opts, G, x) (LS_nnls.m:1)."""
+    return _ctx().ls_nnls(A, Y, opts, G, x)
+
+
+def fast_nnls(A, Y, opts=None):
+    """[xx, Q] = fast_nnls(A, Y, opts) (fast_nnls.m:1)."""
+    return _ctx().fast_nnls(A, Y, opts)

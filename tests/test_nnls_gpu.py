@@ -1,0 +1,93 @@
+"""Batched NNLS (LS_nnls / fast_nnls semantics) on the GPU against the FP64
+oracle restatement and against the exact NNLS optimum (KKT conditions)."""
+import numpy as np
+import pytest
+
+from tests.conftest import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+def problem(P, K, F, seed, noise=0.01):
+    rng = np.random.default_rng(seed)
+    A = np.asfortranarray((rng.random((P, K)) * (rng.random((P, K)) < 0.3)).astype(np.float32))
+    T = rng.random((K, F)) * (rng.random((K, F)) < 0.4)
+    Y = A.astype(np.float64) @ T + noise * rng.standard_normal((P, F))
+    return A, np.asfortranarray(Y.astype(np.float32)), T
+
+
+def kkt(A, Y, X):
+    A = A.astype(np.float64)
+    g = A.T @ (A @ X - Y.astype(np.float64))
+    scale = np.abs(A.T @ Y.astype(np.float64)).max()
+    return float(np.abs(np.where(X > 0, g, np.minimum(g, 0))).max() / scale), float(X.min())
+
+
+@pytest.fixture(scope="module")
+def ctx(gpu):
+    from sid_gb300 import Context
+    return Context()
+
+
+@pytest.mark.parametrize("prec", ["fp32", "split"])
+def test_ls_nnls_matches_oracle(ctx, oracle, prec):
+    from sid_gb300 import to_numpy
+    A, Y, _ = problem(1500, 40, 96, 1)
+    Xg, G, it = ctx.ls_nnls(A, Y, {"max_iter": 2000}, prec=prec, return_iters=True)
+    Xg = to_numpy(Xg)
+    ctx.sync()
+    Xo, Go, ito = oracle.LS_nnls(A, Y, {"max_iter": 2000}, return_iters=True)
+    assert rel_l2(Xg, Xo) < 1e-4, rel_l2(Xg, Xo)
+    assert rel_l2(to_numpy(G), Go) < 1e-5
+    viol, mn = kkt(A, Y, Xg)
+    assert mn >= 0 and viol < 1e-4, viol
+
+
+@pytest.mark.parametrize("prec", ["fp32", "split"])
+def test_fast_nnls_matches_oracle(ctx, oracle, prec):
+    from sid_gb300 import to_numpy
+    A, Y, _ = problem(1200, 30, 80, 2)
+    Xg, Q = ctx.fast_nnls(A, Y, {}, prec=prec)
+    Xg = to_numpy(Xg)
+    ctx.sync()
+    Xo, Qo, _, _ = oracle.fast_nnls(A, Y, {})
+    assert rel_l2(to_numpy(Q), Qo) < 1e-5
+    assert rel_l2(Xg, Xo) < 1e-3, rel_l2(Xg, Xo)
+    viol, mn = kkt(A, Y, Xg)
+    assert mn >= 0 and viol < 1e-3, viol
+
+
+def test_fast_nnls_warm_start(ctx, oracle):
+    from sid_gb300 import to_numpy
+    A, Y, T = problem(1200, 30, 64, 3)
+    W = np.asfortranarray(T.astype(np.float32))
+    Xg, _ = ctx.fast_nnls(A, Y, {"warm_start": W}, prec="split")
+    Xo, _, _, _ = oracle.fast_nnls(A, Y, {"warm_start": W.astype(np.float64)})
+    assert rel_l2(to_numpy(Xg), Xo) < 1e-3
+
+
+def test_ls_nnls_half_movie_and_lambda(ctx, oracle):
+    from sid_gb300 import to_numpy
+    A, Y, _ = problem(2000, 32, 64, 4)
+    Yh = np.asfortranarray(np.abs(Y).astype(np.float16))
+    Xg, _ = ctx.ls_nnls(A, Yh, {"lambda": 0.05}, prec="split")
+    Xo, _ = oracle.LS_nnls(A, Yh.astype(np.float64), {"lambda": 0.05})
+    assert rel_l2(to_numpy(Xg), Xo) < 1e-4
+
+
+def test_ls_nnls_use_std(ctx, oracle):
+    from sid_gb300 import to_numpy
+    A, Y, _ = problem(800, 20, 40, 5)
+    Xg, _ = ctx.ls_nnls(A, Y, {"use_std": True, "max_iter": 300}, prec="fp32")
+    Xo, _ = oracle.LS_nnls(A, Y, {"use_std": True, "max_iter": 300})
+    assert rel_l2(to_numpy(Xg), Xo) < 1e-3, rel_l2(to_numpy(Xg), Xo)
+
+
+def test_ls_nnls_warm_start_and_given_gram(ctx, oracle):
+    from sid_gb300 import to_numpy
+    A, Y, T = problem(1500, 40, 48, 6)
+    G = np.asfortranarray((A.astype(np.float64).T @ A).astype(np.float32))
+    x0 = np.asfortranarray(T.astype(np.float32))
+    Xg, _ = ctx.ls_nnls(A, Y, {}, G=G, x=x0, prec="split")
+    Xo, _ = oracle.LS_nnls(A, Y, {}, G=G.astype(np.float64), x=x0.astype(np.float64))
+    assert rel_l2(to_numpy(Xg), Xo) < 1e-4
