@@ -36,7 +36,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="sid", choices=["sid", "reference"])
-    ap.add_argument("--method", default="spectral_i16", choices=["direct", "spectral_f32", "spectral_i16"])
+    ap.add_argument("--method", default="spectral_mixed",
+                    choices=["direct", "spectral_f32", "spectral_i16", "spectral_mixed"])
     ap.add_argument("--compare", default="direct,spectral_f32",
                     help="other methods timed after the main region (comma list, '' for none)")
     ap.add_argument("--compare-steps", type=int, default=3)
@@ -229,8 +230,11 @@ def main():
     hbm, peak_kind = peaks()
     roof = None
     if args.method.startswith("spectral") and k_n:
-        esz = 4 if args.method == "spectral_i16" else 8
-        alg_bytes = nf * n_out * n_in * esz + nf * (n_in + n_out) * 8
+        # per step one forward and one back-projection contraction; each streams
+        # its tap spectra once (4 bytes per complex entry in 16-bit, 8 in FP32)
+        esz_f = 4 if args.method in ("spectral_i16", "spectral_mixed") else 8
+        esz_b = 4 if args.method == "spectral_i16" else 8
+        alg_bytes = (nf * n_out * n_in * (esz_f + esz_b) + 2 * nf * (n_in + n_out) * 8) / 2
         avg_s = k_ms / k_n / 1e3
         achieved = alg_bytes / avg_s / 1e9
         traffic = None
@@ -293,16 +297,18 @@ def main():
                          f"columns, extrapolated; RL iteration = 2 projections"}
 
     if rank == 0:
-        launches_per_step = {"direct": 7, "spectral_f32": 10, "spectral_i16": 10}[args.method]
+        launches_per_step = {"direct": 7, "spectral_f32": 10, "spectral_i16": 10, "spectral_mixed": 10}[args.method]
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32 (16-bit block-float spectra)" if args.method == "spectral_i16" else "f32",
+            "vs_baseline": None, "dtype": {"spectral_i16": "f32 (16-bit block-float spectra)",
+                                           "spectral_mixed": "f32 (16-bit forward / FP32 back-projection spectra)"}
+            .get(args.method, "f32"),
             "data": "synthetic (seeded Gaussian PSF + blob volume, shapes of the 1005^2x31 configuration)",
             "config": {"workload": f"{args.config}: ISRA iteration on 1005x1005x31, Nnum 15, PSF 345^2x15^2x31",
                        "method": args.method, "parallelism": "replicas" if world > 1 else "1 GPU",
                        "l2": "per-iteration working set (tap spectra, "
-                             f"{nf * n_out * n_in * (4 if args.method == 'spectral_i16' else 8) / 1e9:.1f} GB) "
+                             f"{nf * n_out * n_in * 8 / 1e9:.1f} GB FP32 / {nf * n_out * n_in * 4 / 1e9:.1f} GB 16-bit) "
                              "exceeds L2; no flush needed"},
             "roofline": roof,
             "cpu_baseline": cpu,

@@ -44,6 +44,13 @@ enum {
 #define SID_METHOD_DIRECT       0
 #define SID_METHOD_SPECTRAL_F32 1
 #define SID_METHOD_SPECTRAL_I16 2
+/* Forward projection with the 16-bit spectra, back projection with the FP32
+ * spectra (needs both plan flags).  The 16-bit error is absolute (spread over
+ * the whole sensor), which the forward image tolerates (no sensor pixel is near
+ * zero) but a back projection does not: voxels whose PSF falls mostly outside
+ * the sensor have back projections ~1e-9 of the maximum, and ISRA divides by
+ * them (deconvRL.m:52).  This split keeps ISRA within the mixed-precision bar. */
+#define SID_METHOD_SPECTRAL_MIXED 3
 
 typedef struct sid_plan sid_plan;
 

@@ -15,33 +15,30 @@ def small(gpu, oracle):
     H = synthetic.gaussian_psf(M, N, Z, sigma_min=1.0, sigma_max=3.0)
     Vt = synthetic.blob_volume(X, X, Z, 6, sigma=(1.5, 1.5), seed=4)
     y = oracle.forward_project(H, Vt)
-    P = Projector(H, (X, X), None, methods=("direct", "spectral_f32", "spectral_i16"))
+    P = Projector(H, (X, X), None, methods=("direct", "spectral_f32", "spectral_mixed"))
     fwd = lambda v: oracle.forward_project(H, v)  # noqa: E731
     bwd = lambda i: oracle.backward_project(H, i)  # noqa: E731
     return H, y, P, fwd, bwd
 
 
-@pytest.mark.parametrize("method,iters,tol", [("direct", 8, 1e-5), ("spectral_f32", 8, 1e-5),
-                                              ("spectral_i16", 2, 1e-4)])
-def test_isra_matches_oracle(small, method, iters, tol):
-    """Small adversarial geometry (6 blobs, Nnum 5): the 16-bit spectra keep the
-    mixed bar for the first iterations; over longer runs ISRA amplifies their
-    1e-5 perturbation once a near-zero voxel changes sign (a property of the
-    multiplicative update, measured and recorded; the configuration-scale runs
-    below hold the bar)."""
+@pytest.mark.parametrize("method,tol", [("direct", 1e-5), ("spectral_f32", 1e-5), ("spectral_mixed", 1e-4)])
+def test_isra_matches_oracle(small, method, tol):
     import sid_gb300 as s
     from oracle import oracle as o
     H, y, P, fwd, bwd = small
     Htf = bwd(y).astype(np.float32)
-    ref = o.deconvRL(fwd, bwd, Htf, iters, Htf)
+    ref = o.deconvRL(fwd, bwd, Htf, 8, Htf)
     P.default_method = method
-    out = s.to_numpy(s.deconvRL(P.forward, P.adjoint, Htf, iters, Htf, {"lambda": 0, "p": 1, "mode": "basic"}))
+    out = s.to_numpy(s.deconvRL(P.forward, P.adjoint, Htf, 8, Htf, {"lambda": 0, "p": 1, "mode": "basic"}))
     assert rel_l2(out, ref) < 10 * tol, rel_l2(out, ref)
 
 
 def test_isra_cfg0_mixed_vs_fp64(gpu, oracle):
     """8 ISRA iterations on the 225 x 225 x 11 configuration (Nnum 15, PSF 195):
-    the mixed-precision spectral form against the FP64 oracle, bar 1e-4."""
+    the mixed-precision spectral form against the FP64 oracle, bar 1e-4.
+    (16-bit spectra in the back projection are not used for ISRA: border
+    voxels whose PSF leaves the sensor have back projections ~1e-9 of the
+    maximum, below the 16-bit absolute error, and the division diverges.)"""
     import sid_gb300 as s
     from sid_gb300 import synthetic
     H, V = synthetic.config_inputs("cfg0")
@@ -50,13 +47,13 @@ def test_isra_cfg0_mixed_vs_fp64(gpu, oracle):
     bwd = lambda i: oracle.backward_project(H, i)  # noqa: E731
     Htf = bwd(y)
     ref = oracle.deconvRL(fwd, bwd, Htf, 8, Htf)
-    P = s.Projector(H, V.shape[:2], None, methods=("spectral_i16", "spectral_f32"))
-    for m, tol in (("spectral_i16", 1e-4), ("spectral_f32", 1e-5)):
+    P = s.Projector(H, V.shape[:2], None, methods=("spectral_mixed",))
+    for m, tol in (("spectral_mixed", 1e-4), ("spectral_f32", 1e-5)):
         out = s.to_numpy(P.isra(Htf.astype(np.float32), Htf.astype(np.float32), 8, method=m))
         assert rel_l2(out, ref) < tol, (m, rel_l2(out, ref))
 
 
-@pytest.mark.parametrize("method,tol", [("direct", 1e-5), ("spectral_f32", 1e-5), ("spectral_i16", 1e-4)])
+@pytest.mark.parametrize("method,tol", [("direct", 1e-5), ("spectral_f32", 1e-5), ("spectral_mixed", 1e-4)])
 def test_ls_deconv_matches_oracle(small, method, tol):
     import sid_gb300 as s
     from oracle import oracle as o

@@ -78,9 +78,10 @@ def test_ls_nnls_half_movie_and_lambda(ctx, oracle):
 def test_ls_nnls_use_std(ctx, oracle):
     from sid_gb300 import to_numpy
     A, Y, _ = problem(800, 20, 40, 5)
-    Xg, _ = ctx.ls_nnls(A, Y, {"use_std": True, "max_iter": 300}, prec="fp32")
-    Xo, _ = oracle.LS_nnls(A, Y, {"use_std": True, "max_iter": 300})
-    assert rel_l2(to_numpy(Xg), Xo) < 1e-3, rel_l2(to_numpy(Xg), Xo)
+    # use_std never retires a column early: both run max_iter iterations
+    Xg, _ = ctx.ls_nnls(A, Y, {"use_std": True, "max_iter": 2000}, prec="fp32")
+    Xo, _ = oracle.LS_nnls(A, Y, {"use_std": True, "max_iter": 2000})
+    assert rel_l2(to_numpy(Xg), Xo) < 1e-4, rel_l2(to_numpy(Xg), Xo)
 
 
 def test_ls_nnls_warm_start_and_given_gram(ctx, oracle):
