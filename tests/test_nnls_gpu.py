@@ -76,12 +76,22 @@ def test_ls_nnls_half_movie_and_lambda(ctx, oracle):
 
 
 def test_ls_nnls_use_std(ctx, oracle):
+    """use_std (LS_nnls.m:101-106) fits the frame-centred residual, which does
+    not see a per-component offset shared by all frames: the minimiser is not
+    unique, so the two runs are compared on the objective they minimise."""
     from sid_gb300 import to_numpy
     A, Y, _ = problem(800, 20, 40, 5)
     # use_std never retires a column early: both run max_iter iterations
     Xg, _ = ctx.ls_nnls(A, Y, {"use_std": True, "max_iter": 2000}, prec="fp32")
     Xo, _ = oracle.LS_nnls(A, Y, {"use_std": True, "max_iter": 2000})
-    assert rel_l2(to_numpy(Xg), Xo) < 1e-4, rel_l2(to_numpy(Xg), Xo)
+    Xg = to_numpy(Xg).astype(np.float64)
+
+    def std_obj(X):
+        R = Y.astype(np.float64) - A.astype(np.float64) @ X
+        return float(np.sum((R - R.mean(axis=1, keepdims=True)) ** 2))
+
+    assert Xg.min() >= 0
+    assert abs(std_obj(Xg) - std_obj(Xo)) <= 1e-4 * std_obj(Xo), (std_obj(Xg), std_obj(Xo))
 
 
 def test_ls_nnls_warm_start_and_given_gram(ctx, oracle):
