@@ -169,6 +169,19 @@ int sid_fast_nnls(sid_ctx* ctx, const float* A, const void* Y, int ydtype, int64
                   const sid_nnls_opts* opts, const float* warm_start, float* X, float* Q_out, int prec,
                   int32_t* iters, void* stream);
 
+/* ---- Allocation-free Gram product ---------------------------------------------
+ * No counterpart in the reference: an addition for callers that cannot let a
+ * library allocate device memory (a MEX function whose memory belongs to
+ * MATLAB's gpuArray manager, or a program that reserves all device memory up
+ * front).  G = A'*A in FP32 (same result as sid_gram with SID_PREC_FP32),
+ * without a context: split-K partials live in a fixed 16 MiB device array
+ * compiled into libsid, so K is limited to 2048 (SID_EINVAL beyond).  The
+ * array is shared by every call and keeps the last call's contents; calls
+ * whose kernels overlap on the GPU race on it.  The first call on a device
+ * looks the array up (cudaGetSymbolAddress) and should precede any stream
+ * capture.  A: P x K single, G: K x K single (device). */
+int sid_gram_noalloc(const float* A, int64_t P, int64_t K, float* G, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -65,6 +65,7 @@ SIGNATURES = {
     "sid_fast_nnls_defaults": [P],
     "sid_ls_nnls": [P, P, P, I32, I64, I64, I64, P, P, I32, P, I32, I32, P, P],
     "sid_fast_nnls": [P, P, P, I32, I64, I64, I64, P, P, P, P, I32, P, P],
+    "sid_gram_noalloc": [P, I64, I64, P, P],
 }
 PREC = {"fp32": 0, "split": 1, "bf16": 2}
 DTYPE_F32, DTYPE_F16 = 0, 1
