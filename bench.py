@@ -44,6 +44,9 @@ def parse():
     ap.add_argument("--config", default="cfg1", choices=["cfg0", "cfg1"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="budget of the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-nnls", action="store_true", help="skip the library + temporal NNLS measurement")
+    ap.add_argument("--nnls-frames", type=int, default=3000)
+    ap.add_argument("--nnls-neurons", type=int, default=800)
     return ap.parse_args()
 
 
@@ -126,6 +129,117 @@ class Clocks:
                     reasons.add(nm)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
                 "samples": len(sm)}
+
+
+def nnls_workload(args, P_proj):
+    """Library generation (800 anisotropic Gaussian neurons, sigma_xy U(2,4),
+    sigma_z U(1,2), uniform in the 1005^2 x 31 volume) followed by the temporal
+    NNLS of 3000 FP16 frames Y = S'T + b + noise (SNR 10), T sparse exponential
+    transients (0.5 Hz events at 20 Hz, tau 0.3 s).  Times fast_nnls (the SID
+    temporal update, temporal_SID_update.m:45) at split tensor-core precision
+    and at FP32, and the Gram / cross contractions on their own."""
+    import numpy as np
+    import torch
+
+    import sid_gb300 as s
+    from sid_gb300 import synthetic
+    K, F = args.nnls_neurons, args.nnls_frames
+    X, Y, Z = P_proj.X, P_proj.Y, P_proj.Z
+    P = X * Y
+    rng = np.random.default_rng(5)
+    cx, cy, cz = rng.uniform(1, X, K), rng.uniform(1, Y, K), rng.uniform(1, Z, K)
+    sxy, sz = rng.uniform(2, 4, K), rng.uniform(1, 2, K)
+    vol = np.zeros((X, Y, Z), dtype=np.float32, order="F")
+    for k in range(K):
+        r, rz = int(np.ceil(3 * sxy[k])), int(np.ceil(3 * sz[k]))
+        x0, x1 = max(int(cx[k]) - 1 - r, 0), min(int(cx[k]) + r, X)
+        y0, y1 = max(int(cy[k]) - 1 - r, 0), min(int(cy[k]) + r, Y)
+        z0, z1 = max(int(cz[k]) - 1 - rz, 0), min(int(cz[k]) + rz, Z)
+        gx = np.exp(-0.5 * ((np.arange(x0, x1) + 1 - cx[k]) / sxy[k]) ** 2)
+        gy = np.exp(-0.5 * ((np.arange(y0, y1) + 1 - cy[k]) / sxy[k]) ** 2)
+        gz = np.exp(-0.5 * ((np.arange(z0, z1) + 1 - cz[k]) / sz[k]) ** 2)
+        vol[x0:x1, y0:y1, z0:z1] += (gx[:, None, None] * gy[None, :, None] * gz[None, None, :]).astype(np.float32)
+    centers = np.stack([cx, cy, cz], 1)
+    neur_id = np.ones((K, 1), dtype=bool)
+    opts = {"neur_rad": 12, "axial": 2.0}
+    recon = [s.to_device(vol)]
+    # library through the bench's plan (direct taps)
+    import ctypes
+    from sid_gb300 import _lib
+    A = s.lfm._fortran_tensor((P, K), "cuda")
+    ptrs = (ctypes.c_void_p * 1)(recon[0].data_ptr())
+    c = np.asfortranarray(centers)
+    ids = np.asfortranarray(neur_id.astype(np.uint8))
+    lib_ms = []
+    for _ in range(2):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        _lib.call("sid_library", P_proj._plan, ctypes.cast(ptrs, ctypes.c_void_p), 1, c.ctypes.data,
+                  ids.ctypes.data, K, 12, 2.0, A.data_ptr(), 1, s.lfm._stream_ptr())
+        torch.cuda.synchronize()
+        lib_ms.append((time.perf_counter() - t0) * 1e3)
+    # L2-normalise library rows (temporal_SID_update.m:42)
+    nrm = torch.linalg.vector_norm(A, dim=0)
+    A.div_(nrm.clamp_min(1e-30))
+    # T_true: events at 0.5 Hz (p = 0.025 per 20 Hz frame), exponential kernel tau = 6 frames
+    g = torch.Generator(device="cuda").manual_seed(7)
+    ev = (torch.rand(K, F, generator=g, device="cuda") < 0.025).float() * (0.5 + torch.rand(K, F, generator=g,
+                                                                                              device="cuda"))
+    kern = torch.exp(-torch.arange(0, 40, device="cuda", dtype=torch.float32) / 6.0)
+    T = torch.nn.functional.conv1d(ev[:, None, :], kern.flip(0)[None, None, :], padding=39)[:, 0, :F]
+    sig = (A.T.contiguous().T @ T)  # synthetic movie (data generation, not the measured path)
+    rms = sig.pow(2).mean().sqrt()
+    Yf = sig + 0.1 * rms + 0.1 * rms * torch.randn(sig.shape, generator=g, device="cuda")
+    del sig
+    Y16 = Yf.half()
+    Yf = Yf.T.contiguous().T  # column-major P x F
+    Y16 = Y16.T.contiguous().T
+    ctx = s.Context()
+    out = {"workload": f"library {K} neurons (cfg2) + temporal NNLS {K} x {F} frames, P = {P} (cfg3), FP16 movie"}
+    out["library_ms"] = min(lib_ms)
+    out["library_neurons_per_s"] = K / (min(lib_ms) / 1e3)
+
+    def timed(fn, reps=1):
+        torch.cuda.synchronize()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(reps):
+            r = fn()
+        b.record()
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / reps, r
+
+    # contractions alone
+    ctx.gram(A, "split"); ctx.cross(A, Y16, "split")
+    t_gram, G = timed(lambda: ctx.gram(A, "split"), 3)
+    t_cross, _ = timed(lambda: ctx.cross(A, Y16, "split"), 3)
+    t_gram32, G32 = timed(lambda: ctx.gram(A, "fp32"))
+    peak = 1929.9
+    try:
+        peak = float(json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["bf16_tflops"])
+    except Exception:
+        pass
+    out["gram_split"] = {"ms": t_gram, "alg_tflops": 2 * K * K * P / t_gram / 1e9,
+                         "tensor_tflops": 3 * 2 * K * K * P / t_gram / 1e9,
+                         "tensor_frac_of_bf16_peak": 3 * 2 * K * K * P / t_gram / 1e9 / peak,
+                         "rel_l2_vs_fp32": float(torch.linalg.norm(G - G32) / torch.linalg.norm(G32))}
+    out["cross_split_f16"] = {"ms": t_cross, "alg_tflops": 2 * K * P * F / t_cross / 1e9,
+                              "tensor_tflops": 2 * 2 * K * P * F / t_cross / 1e9,
+                              "tensor_frac_of_bf16_peak": 2 * 2 * K * P * F / t_cross / 1e9 / peak}
+    out["gram_fp32_ms"] = t_gram32
+    # fast_nnls, split tensor-core precision (FP16 movie) vs the plain FP32 path
+    t_split, (Xs, _, its) = timed(lambda: ctx.fast_nnls(A, Y16, {}, prec="split", return_iters=True))
+    t_fp32, (X32, _, it32) = timed(lambda: ctx.fast_nnls(A, Yf, {}, prec="fp32", return_iters=True))
+    out["fast_nnls_split"] = {"ms": t_split, "frames_per_s": F / (t_split / 1e3),
+                              "iters_median": float(its.float().median()), "iters_max": int(its.max())}
+    out["fast_nnls_fp32"] = {"ms": t_fp32, "frames_per_s": F / (t_fp32 / 1e3),
+                             "iters_median": float(it32.float().median()), "iters_max": int(it32.max())}
+    out["split_vs_fp32_speedup"] = t_fp32 / t_split
+    out["rel_l2_split_vs_fp32"] = float(torch.linalg.norm(Xs - X32) / torch.linalg.norm(X32))
+    out["rel_l2_vs_T_true"] = float(torch.linalg.norm(Xs - T) / torch.linalg.norm(T))
+    ctx.sync()
+    return out
 
 
 def peaks():
@@ -289,6 +403,10 @@ def main():
         others[m] = {"rl_iter_s": 1e3 / tm, "ms_per_iter": tm,
                      "fwd_rel_err_vs_fp64": float(np.linalg.norm(gm - ref_pix) / np.linalg.norm(ref_pix))}
 
+    nnls = None
+    if not args.no_nnls and "direct" in methods:
+        nnls = nnls_workload(args, P)
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         t_proj, cols = cpu_sample(H, Vt, args.cpu_seconds, os.cpu_count() or 1)
@@ -321,6 +439,7 @@ def main():
             "compare": others,
             "mixed_vs_fp32_direct": (value / world) / others["direct"]["rl_iter_s"] if "direct" in others else None,
             "plan": {"L": info["L"], "D": info["D"], "device_gb": info["device_bytes"] / 1e9},
+            "nnls": nnls,
         }
         print(json.dumps(line), flush=True)
     if world > 1:

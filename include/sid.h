@@ -114,6 +114,23 @@ int sid_deconv_isra_host(sid_plan* plan, int method, const float* Htf, float* X,
 int sid_deconv_ls(sid_plan* plan, int method, float* X, int max_iter,
                   float lamb_L1, float lamb_L2, void* stream);
 
+/* ---- Library generation -----------------------------------------------------
+ * forward_model = generate_LFM_library_GPU(recon, centers, neur_id, psf, options)
+ *                                              generate_LFM_library_GPU.m:1
+ * All neurons in one batched launch.  recon: HOST array of n_comp DEVICE
+ * pointers, each an X x Y x Z single volume; centers: HOST n_neur x 3 double
+ * (1-based, column-major); neur_id: HOST n_neur x n_comp uint8 (column-major);
+ * neur_rad, axial: options.neur_rad / options.axial.  out (device):
+ * out_layout 0 = n_neur x P (the reference's forward_model), 1 = P x n_neur.
+ * Needs a plan built with SID_PLAN_DIRECT.  Synchronises the stream. */
+int sid_library(sid_plan* plan, const float* const* recon, int64_t n_comp, const double* centers,
+                const uint8_t* neur_id, int64_t n_neur, int64_t neur_rad, double axial, float* out,
+                int out_layout, void* stream);
+/* The crop boxes the call above uses (host only): boxes[6n..6n+5] = 0-based
+ * half-open x0 x1 y0 y1 z0 z1 of neuron n (generate_LFM_library_GPU.m:68-88). */
+int sid_library_boxes(const double* centers, int64_t n_neur, int64_t neur_rad, double axial, int64_t X,
+                      int64_t Y, int64_t Z, int32_t* boxes);
+
 /* ---- NNLS contractions -----------------------------------------------------
  * A solver context owns the workspaces of the contractions and NNLS solvers
  * (16-bit operand copies, split-K partials, iteration state). */

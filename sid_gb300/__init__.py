@@ -14,6 +14,8 @@ from .lfm import (  # noqa: F401
     deconvRL,
     forwardProjectACC,
     forwardProjectGPU,
+    generate_LFM_library_GPU,
+    library_boxes,
     set_default_method,
     to_device,
     to_numpy,

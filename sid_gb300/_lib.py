@@ -66,6 +66,8 @@ SIGNATURES = {
     "sid_ls_nnls": [P, P, P, I32, I64, I64, I64, P, P, I32, P, I32, I32, P, P],
     "sid_fast_nnls": [P, P, P, I32, I64, I64, I64, P, P, P, P, I32, P, P],
     "sid_gram_noalloc": [P, I64, I64, P, P],
+    "sid_library": [P, P, I64, P, P, I64, I64, F64, P, I32, P],
+    "sid_library_boxes": [P, I64, I64, F64, I64, I64, I64, P],
 }
 PREC = {"fp32": 0, "split": 1, "bf16": 2}
 DTYPE_F32, DTYPE_F16 = 0, 1

@@ -1,0 +1,209 @@
+// library.cu -- batched LFM library generation (generate_LFM_library_GPU.m).
+//
+// For neuron n the reference builds a volume that is zero except for a box
+// around the neuron's centre, filled with the mean of the reconstructions of
+// the components it was found in, and forward-projects it with the PSF sliced
+// to the box's depth window (generate_LFM_library_GPU.m:63-109).  Zero depths
+// contribute nothing, so the row equals the full-depth forward projection of
+// the boxed volume.  Here every neuron is one batch entry of one launch:
+//   1. k_lib_average: the boxed, averaged sub-volumes (packed, one per neuron);
+//   2. k_lib_project: one CTA per (neuron, output phase a'b'); threads own the
+//      output lenslets around the box; per box channel (a,b,c) the D x D tap
+//      array K[abc][b'a'] is staged in shared memory and applied to the box's
+//      lattice points of that phase (the same lenslet-tap algebra as
+//      direct.cu), so only the box's own channels are visited;
+//   3. the rest of each row is zero (one memset of the output).
+// Box and window arithmetic (MATLAB round, clipping at 1 and the volume size,
+// ceil(neur_rad/axial)) is done on the host, bit-exact with the reference.
+#include <cmath>
+#include <vector>
+
+#include "sid_internal.cuh"
+
+namespace sid {
+
+struct LibBox {
+    int x0, x1, y0, y1, z0, z1;  // 0-based half-open box
+    int off;                     // offset of the packed sub-volume
+    int ncomp;                   // components averaged
+    int s0, s1, t0, t1;          // output lenslet window (half-open)
+};
+
+// packed[b.off + (x-x0) + bw*((y-y0) + bh*(z-z0))] = mean_k recon_k(x, y, z)
+__global__ void k_lib_average(const float* const* __restrict__ recon, const uint8_t* __restrict__ neur_id,
+                              int64_t n_neur, const LibBox* __restrict__ boxes, int n_comp, int64_t X, int64_t Y,
+                              float* __restrict__ packed)
+{
+    const int n = blockIdx.x;
+    const LibBox b = boxes[n];
+    const int bw = b.x1 - b.x0, bh = b.y1 - b.y0, bd = b.z1 - b.z0;
+    const int total = bw * bh * bd;
+    for (int i = threadIdx.x; i < total; i += blockDim.x) {
+        const int dx = i % bw, r = i / bw, dy = r % bh, dz = r / bh;
+        const int64_t idx = (b.x0 + dx) + X * ((int64_t)(b.y0 + dy) + Y * (int64_t)(b.z0 + dz));
+        float s = 0.f;
+        for (int k = 0; k < n_comp; ++k)
+            if (neur_id[n + n_neur * (int64_t)k]) s += recon[k][idx];
+        packed[b.off + i] = s / (float)b.ncomp;
+    }
+}
+
+// One CTA per (neuron, output phase).  Output written to
+// out[n * ldn + pixel * ldp] with pixel = x + X*y.
+__global__ void __launch_bounds__(256)
+k_lib_project(const float* __restrict__ taps, const float* __restrict__ packed, const LibBox* __restrict__ boxes,
+              int N, int D, int dlo, int64_t tbs, int Lx, int Ly, int64_t X, int64_t Y, float* __restrict__ out,
+              int64_t ldn, int64_t ldp)
+{
+    extern __shared__ float tap[];  // D*D
+    const int n = blockIdx.x;
+    const int o = blockIdx.y;       // b'*N + a'
+    const int bp = o / N, ap = o - (o / N) * N;
+    const LibBox b = boxes[n];
+    const int bw = b.x1 - b.x0, bh = b.y1 - b.y0;
+    const int ns = b.s1 - b.s0, nt = b.t1 - b.t0;
+    const int nl = ns * nt;
+    constexpr int PER = 8;  // output lenslets per thread
+    float acc[PER];
+#pragma unroll
+    for (int q = 0; q < PER; ++q) acc[q] = 0.f;
+    for (int c = b.z0; c < b.z1; ++c) {
+        for (int bb = 0; bb < N; ++bb) {
+            // lattice rows v of phase bb inside the box: y = bb + N v in [y0, y1)
+            const int vlo = (b.y0 - bb) > 0 ? (b.y0 - bb + N - 1) / N : 0;
+            const int vhi = (b.y1 - 1 - bb) >= 0 ? (b.y1 - 1 - bb) / N : -1;
+            if (vhi < vlo) continue;
+            for (int a = 0; a < N; ++a) {
+                const int ulo = (b.x0 - a) > 0 ? (b.x0 - a + N - 1) / N : 0;
+                const int uhi = (b.x1 - 1 - a) >= 0 ? (b.x1 - 1 - a) / N : -1;
+                if (uhi < ulo) continue;
+                const int64_t blk = (((int64_t)c * N + bb) * N + a) * N + bp;
+                __syncthreads();
+                for (int i = threadIdx.x; i < D * D; i += blockDim.x)
+                    tap[i] = taps[blk * tbs + (int64_t)ap * D * D + i];
+                __syncthreads();
+                for (int v = vlo; v <= vhi; ++v) {
+                    const int y = bb + N * v;
+                    for (int u = ulo; u <= uhi; ++u) {
+                        const int x = a + N * u;
+                        const float val = packed[b.off + (x - b.x0) + bw * ((y - b.y0) + bh * (c - b.z0))];
+                        if (val == 0.f) continue;
+#pragma unroll
+                        for (int q = 0; q < PER; ++q) {
+                            const int l = threadIdx.x + q * blockDim.x;
+                            if (l >= nl) break;
+                            const int t = b.t0 + l % nt, s = b.s0 + l / nt;
+                            const int m1 = s - u - dlo, m2 = t - v - dlo;
+                            if (m1 >= 0 && m1 < D && m2 >= 0 && m2 < D) acc[q] = fmaf(val, tap[m1 * D + m2], acc[q]);
+                        }
+                    }
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < PER; ++q) {
+        const int l = threadIdx.x + q * blockDim.x;
+        if (l >= nl) break;
+        const int t = b.t0 + l % nt, s = b.s0 + l / nt;
+        const int64_t x = ap + (int64_t)N * s, y = bp + (int64_t)N * t;
+        if (s < Lx && t < Ly && x < X && y < Y) out[(int64_t)n * ldn + (x + X * y) * ldp] = acc[q];
+    }
+}
+
+static int mround(double v) { return (int)(v < 0 ? -std::floor(-v + 0.5) : std::floor(v + 0.5)); }
+
+// Box of neuron n: x = round(centre), [max(x-r,1), min(x+r,size)] laterally,
+// [max(z-ceil(r/axial),1), min(z+ceil(r/axial),Z)] axially (1-based), returned
+// 0-based half-open.  generate_LFM_library_GPU.m:68-88.
+static void neuron_box(const double* centers, int64_t n_neur, int64_t n, int64_t neur_rad, double axial, int64_t X,
+                       int64_t Y, int64_t Z, int* box6)
+{
+    const int64_t zr = (int64_t)std::ceil((double)neur_rad / axial);
+    const int x = mround(centers[n]), y = mround(centers[n + n_neur]), z = mround(centers[n + 2 * n_neur]);
+    box6[0] = (int)std::max<int64_t>(x - neur_rad, 1) - 1;
+    box6[1] = (int)std::min<int64_t>(x + neur_rad, X);
+    box6[2] = (int)std::max<int64_t>(y - neur_rad, 1) - 1;
+    box6[3] = (int)std::min<int64_t>(y + neur_rad, Y);
+    box6[4] = (int)std::max<int64_t>(z - zr, 1) - 1;
+    box6[5] = (int)std::min<int64_t>(z + zr, Z);
+}
+
+}  // namespace sid
+
+using namespace sid;
+
+extern "C" int sid_library_boxes(const double* centers, int64_t n_neur, int64_t neur_rad, double axial, int64_t X,
+                                 int64_t Y, int64_t Z, int32_t* boxes)
+{
+    SID_REQUIRE(centers && boxes && n_neur >= 0 && neur_rad >= 0 && axial > 0, "sid_library_boxes: bad argument");
+    for (int64_t n = 0; n < n_neur; ++n) neuron_box(centers, n_neur, n, neur_rad, axial, X, Y, Z, boxes + 6 * n);
+    return SID_OK;
+}
+
+extern "C" int sid_library(sid_plan* p, const float* const* recon, int64_t n_comp, const double* centers,
+                           const uint8_t* neur_id, int64_t n_neur, int64_t neur_rad, double axial, float* out,
+                           int out_layout, void* stream)
+{
+    SID_REQUIRE(p && recon && centers && neur_id && out, "sid_library: NULL argument");
+    SID_REQUIRE(n_comp >= 1 && n_neur >= 1 && neur_rad >= 0 && axial > 0,
+                "sid_library: need n_comp >= 1, n_neur >= 1, neur_rad >= 0, axial > 0");
+    SID_REQUIRE(out_layout == 0 || out_layout == 1, "sid_library: out_layout must be 0 (n x P) or 1 (P x n)");
+    SID_REQUIRE(p->taps_f.p, "sid_library: the plan needs SID_PLAN_DIRECT (lenslet taps)");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const int64_t N = p->N, D = p->g.D;
+    std::vector<LibBox> boxes(n_neur);
+    int64_t off = 0;
+    int max_nl = 0;
+    for (int64_t n = 0; n < n_neur; ++n) {
+        int bx[6];
+        neuron_box(centers, n_neur, n, neur_rad, axial, p->X, p->Y, p->Z, bx);
+        LibBox b;
+        b.x0 = bx[0]; b.x1 = bx[1]; b.y0 = bx[2]; b.y1 = bx[3]; b.z0 = bx[4]; b.z1 = bx[5];
+        int nc = 0;
+        for (int64_t k = 0; k < n_comp; ++k) nc += neur_id[n + n_neur * k] ? 1 : 0;
+        SID_REQUIRE(nc > 0, "sid_library: neuron %lld is in no component (neur_id row is empty)", (long long)(n + 1));
+        SID_REQUIRE(b.x1 > b.x0 && b.y1 > b.y0 && b.z1 > b.z0,
+                    "sid_library: neuron %lld has an empty box (centre outside the volume)", (long long)(n + 1));
+        b.ncomp = nc;
+        b.off = (int)off;
+        off += (int64_t)(b.x1 - b.x0) * (b.y1 - b.y0) * (b.z1 - b.z0);
+        // output lenslets reached from the box: s = u + m + dlo
+        const int umin = b.x0 / (int)N, umax = (b.x1 - 1) / (int)N;
+        const int vmin = b.y0 / (int)N, vmax = (b.y1 - 1) / (int)N;
+        b.s0 = (int)std::max<int64_t>(0, umin + p->g.dlo);
+        b.s1 = (int)std::min<int64_t>(p->Lx, umax + p->g.dhi + 1);
+        b.t0 = (int)std::max<int64_t>(0, vmin + p->g.dlo);
+        b.t1 = (int)std::min<int64_t>(p->Ly, vmax + p->g.dhi + 1);
+        max_nl = std::max(max_nl, (b.s1 - b.s0) * (b.t1 - b.t0));
+        boxes[n] = b;
+    }
+    SID_REQUIRE(off < INT32_MAX, "sid_library: boxes too large");
+    SID_REQUIRE(max_nl <= 256 * 8, "sid_library: neuron radius too large for one CTA (%d output lenslets)", max_nl);
+    DBuf& dbox = p->ws[3];
+    DBuf& dpack = p->ws[2];
+    DBuf& dmeta = p->ws[1];
+    SID_TRY(dbox.alloc(boxes.size() * sizeof(LibBox)));
+    SID_TRY(dpack.alloc((size_t)off * sizeof(float)));
+    SID_TRY(dmeta.alloc((size_t)(n_comp * sizeof(float*) + n_neur * n_comp)));
+    SID_CUDA_TRY(cudaMemcpyAsync(dbox.p, boxes.data(), boxes.size() * sizeof(LibBox), cudaMemcpyHostToDevice, st));
+    SID_CUDA_TRY(cudaMemcpyAsync(dmeta.p, recon, (size_t)n_comp * sizeof(float*), cudaMemcpyHostToDevice, st));
+    uint8_t* did = dmeta.as<uint8_t>() + n_comp * sizeof(float*);
+    SID_CUDA_TRY(cudaMemcpyAsync(did, neur_id, (size_t)(n_neur * n_comp), cudaMemcpyHostToDevice, st));
+    k_lib_average<<<(unsigned)n_neur, 256, 0, st>>>(dmeta.as<const float*>(), did, n_neur, dbox.as<LibBox>(),
+                                                    (int)n_comp, p->X, p->Y, dpack.as<float>());
+    SID_CHECK_LAUNCH();
+    const int64_t P = p->X * p->Y;
+    SID_CUDA_TRY(cudaMemsetAsync(out, 0, (size_t)(P * n_neur) * sizeof(float), st));
+    const int64_t tbs = cdiv(N * D * D, 32) * 32;
+    const int64_t ldn = out_layout == 0 ? 1 : P, ldp = out_layout == 0 ? n_neur : 1;
+    dim3 grid((unsigned)n_neur, (unsigned)(N * N));
+    k_lib_project<<<grid, 256, (size_t)(D * D) * sizeof(float), st>>>(
+        p->taps_f.as<float>(), dpack.as<float>(), dbox.as<LibBox>(), (int)N, (int)D, (int)p->g.dlo, tbs, (int)p->Lx,
+        (int)p->Ly, p->X, p->Y, out, ldn, ldp);
+    SID_CHECK_LAUNCH();
+    // the staging buffers are read by the kernels above: wait before the host
+    // vectors go out of scope and before the workspaces can be reused
+    SID_CUDA_TRY(cudaStreamSynchronize(st));
+    return SID_OK;
+}

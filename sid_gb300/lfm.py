@@ -292,3 +292,39 @@ def LS_deconv(forwardFUN, backwardFUN, df, opts=None):
         raise TypeError("LS_deconv: forwardFUN/backwardFUN must be a Projector's forward/adjoint")
     return proj.ls_deconv(df, int(opts.get("max_iter", 8)), float(opts.get("lamb_L1", 0.0)),
                           float(opts.get("lamb_L2", 0.0)))
+
+
+def library_boxes(centers, neur_rad, axial, size):
+    """Crop boxes of generate_LFM_library_GPU.m:68-88 as 0-based half-open
+    (x0, x1, y0, y1, z0, z1) rows, computed by libsid's host code."""
+    c = np.asfortranarray(np.asarray(centers, dtype=np.float64).reshape(-1, 3))
+    n = c.shape[0]
+    out = np.zeros((n, 6), dtype=np.int32)
+    X, Y, Z = size
+    _lib.call("sid_library_boxes", c.ctypes.data, n, int(neur_rad), float(axial), X, Y, Z, out.ctypes.data)
+    return out
+
+
+def generate_LFM_library_GPU(recon, centers, neur_id, psf, options, layout="rows"):
+    """forward_model = generate_LFM_library_GPU(recon, centers, neur_id, psf, options)
+    (generate_LFM_library_GPU.m:1).  recon: list of (X, Y, Z) volumes; centers:
+    (n, 3) 1-based; neur_id: (n, n_comp) logical; psf: dict with 'H';
+    options: dict with 'neur_rad', 'axial'.  Returns the (n, X*Y) library on
+    the GPU ('rows', the reference's layout) or its transpose (X*Y, n)
+    ('columns', the layout the NNLS solvers take)."""
+    H = psf["H"] if isinstance(psf, dict) else psf
+    vols = [to_device(r) for r in recon]
+    X, Y, Z = vols[0].shape
+    proj = _plan_for(H, (X, Y), None, "direct")
+    c = np.asfortranarray(np.asarray(centers, dtype=np.float64).reshape(-1, 3))
+    n = c.shape[0]
+    ids = np.asfortranarray(np.asarray(neur_id).reshape(n, len(vols)).astype(np.uint8))
+    ptrs = (ctypes.c_void_p * len(vols))(*[v.data_ptr() for v in vols])
+    if layout == "rows":
+        out = _fortran_tensor((n, X * Y), vols[0].device)
+    else:
+        out = _fortran_tensor((X * Y, n), vols[0].device)
+    _lib.call("sid_library", proj._plan, ctypes.cast(ptrs, ctypes.c_void_p), len(vols), c.ctypes.data,
+              ids.ctypes.data, n, int(options["neur_rad"]), float(options["axial"]), out.data_ptr(),
+              0 if layout == "rows" else 1, _stream_ptr())
+    return out

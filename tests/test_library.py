@@ -1,0 +1,46 @@
+"""Library generation: bit-exact crop boxes (CPU) and batched projection
+against the FP64 oracle (GPU)."""
+import numpy as np
+import pytest
+
+from tests.conftest import rel_l2
+
+
+def test_boxes_bit_exact(sidlib, oracle):
+    from sid_gb300 import library_boxes
+    rng = np.random.default_rng(0)
+    X, Y, Z = 60, 45, 9
+    # include exact .5 centres (MATLAB rounds half away from zero), edges and corners
+    c = np.stack([rng.uniform(-2, X + 2, 200), rng.uniform(-2, Y + 2, 200), rng.uniform(0.5, Z + 0.4, 200)], 1)
+    c[:10, 0] = np.arange(10) + 0.5
+    c[10:20, 2] = 0.5 + np.arange(10) % Z
+    c = c[(np.round(c[:, 0]) + 5 >= 1) & (np.round(c[:, 1]) + 5 >= 1)]
+    for r, ax in [(5, 2.0), (3, 1.5), (0, 1.0)]:
+        got = library_boxes(c, r, ax, (X, Y, Z))
+        ref = oracle.library_boxes(c, (X, Y), Z, r, ax)
+        np.testing.assert_array_equal(got, ref)
+
+
+@pytest.mark.gpu
+def test_library_matches_oracle(gpu, oracle):
+    import sid_gb300 as s
+    from sid_gb300 import synthetic
+    N, Z, M, L = 5, 7, 41, 12
+    X = N * L
+    H = synthetic.gaussian_psf(M, N, Z, sigma_min=1.5, sigma_max=6.0)
+    rng = np.random.default_rng(3)
+    recon = [synthetic.blob_volume(X, X, Z, 30, sigma=(1.5, 3.0), seed=10 + k) for k in range(3)]
+    centers = np.stack([rng.uniform(1, X, 12), rng.uniform(1, X, 12), rng.uniform(1, Z, 12)], 1)
+    centers[0] = [1.0, 1.0, 1.0]          # corner
+    centers[1] = [X - 0.2, X / 2, Z]      # far edge
+    neur_id = rng.random((12, 3)) < 0.6
+    neur_id[:, 0] = True
+    opts = {"neur_rad": 4, "axial": 2.0}
+    got = s.to_numpy(s.generate_LFM_library_GPU(recon, centers, neur_id, {"H": H}, opts))
+    ref = oracle.generate_library(recon, centers, neur_id, H, 4, 2.0)
+    assert got.shape == ref.shape
+    assert rel_l2(got, ref) < 1e-5, rel_l2(got, ref)
+    for n in range(12):
+        assert rel_l2(got[n], ref[n]) < 1e-5, n
+    cols = s.to_numpy(s.generate_LFM_library_GPU(recon, centers, neur_id, {"H": H}, opts, layout="columns"))
+    np.testing.assert_array_equal(cols, got.T)
