@@ -186,6 +186,18 @@ int sid_fast_nnls(sid_ctx* ctx, const float* A, const void* Y, int ydtype, int64
                   const sid_nnls_opts* opts, const float* warm_start, float* X, float* Q_out, int prec,
                   int32_t* iters, void* stream);
 
+/* forward_model = update_spatial_component(timeseries, sensor_movie, template, opts)
+ *                                            update_spatial_component.m:1
+ * Every template pixel's regularised NNLS (reg_nnls.m:40-69, NQP.m:42-178 with
+ * default options, FP64 active set) in one launch.  T: R x F single (the
+ * timeseries; with bg_sub the last row is the background); Y: P x F single or
+ * half; tmpl: (R - bg_sub) x P uint8 template; forward_model: R x P single
+ * (dense).  status (optional, P int32): 0 ok, 1 more than 32 components cover
+ * the pixel, 2 NQP iteration cap; SID_ENOCONV if any pixel failed. */
+int sid_spatial_update(sid_ctx* ctx, const float* T, const void* Y, int ydtype, const uint8_t* tmpl, int64_t R,
+                       int64_t F, int64_t P, double lamb_L1, double lamb_L2, double lamb_orth_L1, int use_std,
+                       int bg_sub, float* forward_model, int32_t* status, void* stream);
+
 /* ---- Allocation-free Gram product ---------------------------------------------
  * No counterpart in the reference: an addition for callers that cannot let a
  * library allocate device memory (a MEX function whose memory belongs to

@@ -5,7 +5,7 @@ The compute lives in ``libsid.so`` (hand-written CUDA behind the C ABI of
 top of it.  Import does not require a GPU; calling the operators does.
 """
 from ._lib import SidError  # noqa: F401
-from .nnls import Context, LS_nnls, fast_nnls  # noqa: F401
+from .nnls import Context, LS_nnls, fast_nnls, update_spatial_component  # noqa: F401
 from .lfm import (  # noqa: F401
     LS_deconv,
     Projector,

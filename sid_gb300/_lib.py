@@ -68,6 +68,7 @@ SIGNATURES = {
     "sid_gram_noalloc": [P, I64, I64, P, P],
     "sid_library": [P, P, I64, P, P, I64, I64, F64, P, I32, P],
     "sid_library_boxes": [P, I64, I64, F64, I64, I64, I64, P],
+    "sid_spatial_update": [P, P, P, I32, P, I64, I64, I64, F64, F64, F64, I32, I32, P, P, P],
 }
 PREC = {"fp32": 0, "split": 1, "bf16": 2}
 DTYPE_F32, DTYPE_F16 = 0, 1

@@ -345,26 +345,38 @@ static int launch_gemm(const GemmMaps& maps, int npass, int m, int n, int nkb, i
     return SID_OK;
 }
 
-// Tile width and split-K choice: the widest tile whose tile count fills the
-// 152 SMs best, then split K until there are >= 4 waves of work or the K
-// range per split would drop below 8 blocks.
+// Tile width and split-K choice (the project's autotuner for this kernel).
+// For each tile width BN in {256, 128, 64} split K until there are >= 4 waves
+// of CTAs on the 152 SMs (or a split would hold fewer than 8 K blocks), then
+// estimate the time as waves x K blocks per CTA x BN / efficiency(BN) and keep
+// the fastest.  The efficiencies model tcgen05's shared-memory operand traffic
+// per MMA: A (128 x 16) plus B (BN x 16) must be read for 128*BN*16 MACs, so
+// BN = 64 is limited by shared-memory bandwidth (measured) and BN = 256
+// amortises A best.
 void gemm_autotune(int m, int n, int nkb, int* bn, int* splitk)
 {
     const int sms = 152;
     const int cands[3] = {256, 128, 64};
-    double best = -1.0;
-    int bbn = 128;
-    for (int c : cands) {
+    const double eff[3] = {1.0, 0.85, 0.45};
+    double best = 1e300;
+    int bbn = 256, bs = 1;
+    for (int i = 0; i < 3; ++i) {
+        const int c = cands[i];
         const int64_t tiles = cdiv(m, GEMM_BM) * cdiv(n, c);
-        const double waves = (double)tiles / sms;
-        const double eff = waves / std::ceil(waves) * ((double)n / (double)(cdiv(n, c) * c));
-        if (eff > best + 1e-9) { best = eff; bbn = c; }
+        int s = 1;
+        while (tiles * s < 4 * sms && nkb / (s + 1) >= 8) ++s;
+        const int64_t kb_per = cdiv(nkb, s);
+        s = (int)cdiv(nkb, kb_per);
+        const int64_t waves = cdiv(tiles * s, sms);
+        const double t = (double)waves * (double)kb_per * (double)c / eff[i];
+        if (t < best * (1.0 - 1e-9)) {
+            best = t;
+            bbn = c;
+            bs = s;
+        }
     }
-    const int64_t tiles = cdiv(m, GEMM_BM) * cdiv(n, bbn);
-    int s = 1;
-    while (tiles * s < 4 * sms && nkb / (s + 1) >= 8) ++s;
     *bn = bbn;
-    *splitk = s;
+    *splitk = bs;
 }
 
 // out (m x n, ldc) = sum_p A_p^T B_p; A_p: k x m (lda), B_p: k x n (ldb), 16-bit.

@@ -1,0 +1,362 @@
+// spatial.cu -- SID spatial update: per-pixel regularised NNLS
+// (update_spatial_component.m:45-131 -> reg_nnls.m:40-69 -> NQP.m:42-178).
+//
+// The reference loops over neurons (ascending template size) and, for every
+// not-yet-visited pixel of the neuron's template, solves a small non-negative
+// quadratic program over the neurons whose templates cover that pixel (plus the
+// background component).  Which neurons enter a pixel's problem depends only
+// on the original template (a pixel is solved once, by the first neuron that
+// reaches it, with every neuron covering it), so all pixel problems are
+// independent and run here in one launch:
+//   1. G = T T' (R x R) and C = Y T' (P x R)  -- contractions;
+//   2. per pixel: ||y||, sum(y), and the covering neurons in ascending order,
+//      background last (update_spatial_component.m:59-79);
+//   3. per pixel, FP64: Q = G(idx,idx) + l2*I + lo*hilf [- s s'/F],
+//      q = -C(p,idx)/||y|| + l1 [+ s sum(y)/(F ||y||)] (reg_nnls.m:48-67),
+//      Lawson-Hanson active set with an incrementally extended Cholesky factor
+//      (NQP.m:93-178, default options), x * ||y|| into the forward model;
+//   4. pixels outside every template get the background row C(p, bg)
+//      (update_spatial_component.m:128-131).
+#include <cfloat>
+#include <vector>
+
+#include "sid_internal.cuh"
+
+namespace sid {
+
+int contract(sid_ctx* c, const float* A, const void* B, bool b_f16, int64_t m, int64_t n, int64_t k, int64_t lda,
+             int64_t ldb, float* C, int64_t ldc, float alpha, float beta, int prec, cudaStream_t st);
+int ctx_sync(sid_ctx* c, cudaStream_t st);
+
+constexpr int kNqpMax = 32;  // largest number of components covering one pixel
+
+// --------------------------------------------- C = Y T' (FP32, NT layout) --
+// C (m x n, col-major) = A B' with A m x k (m contiguous) and B n x k (n
+// contiguous): the frame contraction of a pixel-major movie.  128 x 64 tile,
+// 256 threads, 8 x 4 outputs per thread.
+__global__ void __launch_bounds__(256)
+k_sgemm_nt(const float* __restrict__ A, const void* __restrict__ Bv, const float* __restrict__ Bscale, int m, int n,
+           int k, int64_t lda, int64_t ldb, float* __restrict__ C, int64_t ldc, int a_f16)
+{
+    __shared__ __align__(16) float As[16][128];
+    __shared__ __align__(16) float Bs[16][64];
+    const float* B = static_cast<const float*>(Bv);
+    const int tid = threadIdx.x;
+    const int m0 = blockIdx.x * 128, n0 = blockIdx.y * 64;
+    const int tm = (tid & 31) * 4, tn = (tid >> 5) * 8;
+    float acc[4][8];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 8; ++j) acc[i][j] = 0.f;
+    (void)Bscale;
+    for (int k0 = 0; k0 < k; k0 += 16) {
+        for (int e = tid; e < 16 * 128; e += 256) {
+            const int kk = e >> 7, mm = e & 127;
+            const int gm = m0 + mm, gk = k0 + kk;
+            float v = 0.f;
+            if (gm < m && gk < k) {
+                if (a_f16) v = __half2float(reinterpret_cast<const __half*>(A)[gm + lda * (int64_t)gk]);
+                else v = A[gm + lda * (int64_t)gk];
+            }
+            As[kk][mm] = v;
+        }
+        for (int e = tid; e < 16 * 64; e += 256) {
+            const int kk = e >> 6, nn = e & 63;
+            const int gn = n0 + nn, gk = k0 + kk;
+            Bs[kk][nn] = (gn < n && gk < k) ? B[gn + ldb * (int64_t)gk] : 0.f;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < 16; ++kk) {
+            const float4 a = *reinterpret_cast<const float4*>(&As[kk][tm]);
+            const float4 b0 = *reinterpret_cast<const float4*>(&Bs[kk][tn]);
+            const float4 b1 = *reinterpret_cast<const float4*>(&Bs[kk][tn + 4]);
+            const float av[4] = {a.x, a.y, a.z, a.w};
+            const float bv[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int j = 0; j < 8; ++j) acc[i][j] = fmaf(av[i], bv[j], acc[i][j]);
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const int r = m0 + tm + i;
+        if (r >= m) continue;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const int c = n0 + tn + j;
+            if (c < n) C[(int64_t)r + ldc * c] = acc[i][j];
+        }
+    }
+}
+
+// Tt (F x R, column-major) = T' for T (R x F)
+__global__ void k_transpose(const float* __restrict__ T, int R, int F, float* __restrict__ Tt)
+{
+    const int64_t n = (int64_t)R * F;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t f = i % F, r = i / F;
+        Tt[i] = T[r + (int64_t)R * f];
+    }
+}
+
+// per pixel: ||y||, sum(y) (movie P x F, pixel-major)
+__global__ void k_pixel_stats(const void* __restrict__ Y, int f16, int64_t P, int64_t F, float* __restrict__ nrm,
+                              float* __restrict__ sum)
+{
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < P; p += (int64_t)gridDim.x * blockDim.x) {
+        double s = 0.0, q = 0.0;
+        for (int64_t f = 0; f < F; ++f) {
+            const double v = f16 ? (double)__half2float(static_cast<const __half*>(Y)[p + P * f])
+                                 : (double)static_cast<const float*>(Y)[p + P * f];
+            s += v;
+            q += v * v;
+        }
+        nrm[p] = (float)sqrt(q);
+        sum[p] = (float)s;
+    }
+}
+
+// s(r) = sum over frames of T(r, :)
+__global__ void k_row_sums(const float* __restrict__ T, int R, int F, float* __restrict__ s)
+{
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < R; r += gridDim.x * blockDim.x) {
+        double a = 0.0;
+        for (int f = 0; f < F; ++f) a += T[r + (int64_t)R * f];
+        s[r] = (float)a;
+    }
+}
+
+struct SpatialOpts {
+    double l1, l2, lo;  // lamb_L1, lamb_L2, lamb_orth_L1
+    int use_std, bg_sub;
+};
+
+// One thread per pixel: collect the covering components and solve the NQP in
+// FP64.  status[p]: 0 ok, 1 too many components, 2 iteration cap (NQP.m:116-119).
+__global__ void __launch_bounds__(128)
+k_pixel_nqp(const uint8_t* __restrict__ tmpl, int Rt, int64_t P, const float* __restrict__ G, int R,
+            const float* __restrict__ C, int64_t ldc, const float* __restrict__ pnrm, const float* __restrict__ psum,
+            const float* __restrict__ tsum, int F, SpatialOpts o, float* __restrict__ out, int* __restrict__ status,
+            int* __restrict__ nfail)
+{
+    const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (p >= P) return;
+    int idx[kNqpMax];
+    int n = 0;
+    bool over = false;
+    for (int r = 0; r < Rt; ++r) {
+        if (tmpl[r + (int64_t)Rt * p]) {
+            if (n < kNqpMax) idx[n++] = r;
+            else over = true;
+        }
+    }
+    if (n == 0) {
+        // outside every template: background row, if any (update_spatial_component.m:128-131)
+        if (o.bg_sub) out[(R - 1) + (int64_t)R * p] = C[p + ldc * (R - 1)];
+        status[p] = 0;
+        return;
+    }
+    if (o.bg_sub) {
+        if (n < kNqpMax) idx[n++] = R - 1;
+        else over = true;
+    }
+    if (over) {
+        status[p] = 1;
+        atomicAdd(nfail, 1);
+        return;
+    }
+    const double yn = (double)pnrm[p];
+    if (!(yn > 0.0)) {
+        for (int i = 0; i < n; ++i) out[idx[i] + (int64_t)R * p] = 0.f;
+        status[p] = 0;
+        return;
+    }
+    // Q(i,j) and b = -q (NQP works with b = -q, NQP.m:145)
+    auto Qij = [&](int i, int j) -> double {
+        double v = (double)G[idx[i] + (int64_t)R * idx[j]];
+        if (i == j) v += o.l2;
+        else if (!(o.bg_sub && (i == n - 1 || j == n - 1))) v += o.lo;  // hilf = ones - eye, bg row/col zero
+        if (o.use_std) v -= (double)tsum[idx[i]] * (double)tsum[idx[j]] / (double)F;
+        return v;
+    };
+    double b[kNqpMax], x[kNqpMax], z[kNqpMax], w[kNqpMax], wsc[kNqpMax], t[kNqpMax];
+    double L[kNqpMax * (kNqpMax + 1) / 2];  // packed lower triangle, row-major
+    int pn[kNqpMax];
+    bool Pset[kNqpMax];
+    for (int i = 0; i < n; ++i) {
+        double q = -(double)C[p + ldc * idx[i]] / yn;
+        if (o.use_std) q += (double)tsum[idx[i]] * (double)psum[p] / yn / (double)F;
+        q += o.l1;
+        b[i] = -q;
+        w[i] = -q;  // w = -b_input, NQP.m:122 (b_input = q)
+        x[i] = 0.0;
+        wsc[i] = 0.0;
+        Pset[i] = false;
+    }
+    const double tol = 3.0 * DBL_EPSILON;
+    double wsc0 = 0.0;
+    for (int i = 0; i < n; ++i) wsc0 += w[i] * w[i];
+    wsc0 = sqrt(wsc0);
+    const int maxiter = 4 * n;
+    int pn1 = 0, pn2 = 0, iter = 0, st = 0;
+#define LIJ(r, c) L[(r) * ((r) + 1) / 2 + (c)]
+    for (;;) {
+        bool all_p = true, any_up = false;
+        for (int i = 0; i < n; ++i)
+            if (!Pset[i]) {
+                all_p = false;
+                if (w[i] > wsc[i]) any_up = true;
+            }
+        if (all_p || !any_up) break;
+        int best = -1;
+        double bv = 0.0;
+        for (int i = 0; i < n; ++i) {
+            if (Pset[i]) continue;
+            const double v = w[i] - wsc[i];
+            if (best < 0 || v > bv) { best = i; bv = v; }
+        }
+        Pset[best] = true;
+        pn2 = pn1 + 1;
+        pn[pn2 - 1] = best;
+        for (;;) {
+            ++iter;
+            if (iter >= 2 * n) {
+                if (iter > maxiter) { st = 2; goto done; }
+                if (iter % n == 0)
+                    for (int i = 0; i < n; ++i) wsc[i] = (wsc[i] + wsc0 * tol) * 2.0;
+            }
+            for (int i = 0; i < n; ++i) z[i] = 0.0;
+            for (int r = pn1; r < pn2; ++r) {
+                const int vr = pn[r];
+                for (int s = 0; s < r; ++s) {
+                    double acc = Qij(pn[s], vr);
+                    for (int u = 0; u < s; ++u) acc -= LIJ(s, u) * t[u];
+                    t[s] = acc / LIJ(s, s);
+                }
+                const double AA = Qij(vr, vr);
+                double tt = AA;
+                for (int s = 0; s < r; ++s) tt -= t[s] * t[s];
+                tt = (tt <= AA * tol) ? 1e300 : sqrt(tt);
+                for (int s = 0; s < r; ++s) LIJ(r, s) = t[s];
+                LIJ(r, r) = tt;
+            }
+            for (int s = 0; s < pn2; ++s) {
+                double acc = b[pn[s]];
+                for (int u = 0; u < s; ++u) acc -= LIJ(s, u) * t[u];
+                t[s] = acc / LIJ(s, s);
+            }
+            for (int s = pn2 - 1; s >= 0; --s) {
+                double acc = t[s];
+                for (int u = s + 1; u < pn2; ++u) acc -= LIJ(u, s) * z[pn[u]];
+                z[pn[s]] = acc / LIJ(s, s);
+            }
+            pn1 = pn2;
+            bool all_pos = true;
+            for (int i = 0; i < n; ++i)
+                if (Pset[i] && z[i] < 0.0) { all_pos = false; break; }
+            if (all_pos) {
+                for (int i = 0; i < n; ++i) x[i] = z[i];
+                for (int i = 0; i < n; ++i) {
+                    double acc = b[i];
+                    for (int u = 0; u < n; ++u) acc -= Qij(i, u) * x[u];
+                    w[i] = acc;
+                }
+                for (int i = 0; i < n; ++i)
+                    if (Pset[i] && 2.0 * fabs(w[i]) > wsc[i]) wsc[i] = 2.0 * fabs(w[i]);
+                break;
+            }
+            int worst = -1;
+            double alpha = 0.0;
+            for (int i = 0; i < n; ++i) {
+                if (!(z[i] < 0.0)) continue;
+                const double v = x[i] / (x[i] - z[i] + DBL_MIN);
+                if (worst < 0 || v < alpha) { worst = i; alpha = v; }
+            }
+            if (x[worst] == 0.0) {
+                double acc = b[worst];
+                for (int u = 0; u < n; ++u) acc -= Qij(worst, u) * x[u];
+                wsc[worst] = (fabs(acc) + wsc[worst]) * 2.0;
+                w[worst] = acc;
+            }
+            Pset[worst] = false;
+            for (int i = 0; i < n; ++i) x[i] = x[i] - alpha * (x[i] - z[i]);
+            int pos = 0;
+            while (pn[pos] != worst) ++pos;
+            for (int s = pos; s + 1 < pn2; ++s) pn[s] = pn[s + 1];
+            pn1 = pos;
+            pn2 = pn2 - 1;
+        }
+    }
+done:
+#undef LIJ
+    status[p] = st;
+    if (st) {
+        atomicAdd(nfail, 1);
+        return;
+    }
+    for (int i = 0; i < n; ++i) out[idx[i] + (int64_t)R * p] = (float)(x[i] * yn);
+}
+
+}  // namespace sid
+
+using namespace sid;
+
+extern "C" int sid_spatial_update(sid_ctx* c, const float* T, const void* Y, int ydtype, const uint8_t* tmpl,
+                                  int64_t R, int64_t F, int64_t P, double lamb_L1, double lamb_L2,
+                                  double lamb_orth_L1, int use_std, int bg_sub, float* forward_model,
+                                  int32_t* status, void* stream)
+{
+    SID_REQUIRE(c && T && Y && tmpl && forward_model, "sid_spatial_update: NULL argument");
+    SID_REQUIRE(R >= 1 && F >= 1 && P >= 1, "sid_spatial_update: empty problem");
+    SID_REQUIRE(ydtype == SID_DTYPE_F32 || ydtype == SID_DTYPE_F16, "sid_spatial_update: unknown Y dtype");
+    SID_REQUIRE(!bg_sub || R >= 2, "sid_spatial_update: bg_sub needs a background component");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const int64_t Rt = bg_sub ? R - 1 : R;
+    DBuf* nn = c->nn;
+    SID_TRY(nn[0].alloc((size_t)(F * R) * 4));   // T'
+    SID_TRY(nn[1].alloc((size_t)(R * R) * 4));   // G
+    SID_TRY(nn[2].alloc((size_t)(P * R) * 4));   // C = Y T'
+    SID_TRY(nn[3].alloc((size_t)(2 * P + R + 4) * 4));
+    SID_TRY(nn[4].alloc((size_t)P * 4));         // status (when the caller passes none)
+    float* Tt = nn[0].as<float>();
+    float* G = nn[1].as<float>();
+    float* Cm = nn[2].as<float>();
+    float* pn = nn[3].as<float>();
+    float* ps = pn + P;
+    float* ts = ps + P;
+    int* nfail = reinterpret_cast<int*>(ts + R);
+    int* stat = status ? status : nn[4].as<int>();
+    k_transpose<<<1024, 256, 0, st>>>(T, (int)R, (int)F, Tt);
+    SID_CHECK_LAUNCH();
+    // G = T T' (contraction over frames)
+    SID_TRY(contract(c, Tt, Tt, false, R, R, F, F, F, G, R, 1.f, 0.f, SID_PREC_FP32, st));
+    // C = Y T' (P x R)
+    dim3 grid((unsigned)cdiv(P, 128), (unsigned)cdiv(R, 64));
+    k_sgemm_nt<<<grid, 256, 0, st>>>(static_cast<const float*>(Y), T, nullptr, (int)P, (int)R, (int)F, P, R, Cm, P,
+                                     ydtype == SID_DTYPE_F16 ? 1 : 0);
+    SID_CHECK_LAUNCH();
+    k_pixel_stats<<<1024, 256, 0, st>>>(Y, ydtype == SID_DTYPE_F16 ? 1 : 0, P, F, pn, ps);
+    SID_CHECK_LAUNCH();
+    k_row_sums<<<cdiv(R, 256), 256, 0, st>>>(T, (int)R, (int)F, ts);
+    SID_CHECK_LAUNCH();
+    SID_CUDA_TRY(cudaMemsetAsync(forward_model, 0, (size_t)(R * P) * 4, st));
+    SID_CUDA_TRY(cudaMemsetAsync(nfail, 0, sizeof(int), st));
+    SpatialOpts o{lamb_L1, lamb_L2, lamb_orth_L1, use_std ? 1 : 0, bg_sub ? 1 : 0};
+    k_pixel_nqp<<<(unsigned)cdiv(P, 128), 128, 0, st>>>(tmpl, (int)Rt, P, G, (int)R, Cm, P, pn, ps, ts, (int)F, o,
+                                                        forward_model, stat, nfail);
+    SID_CHECK_LAUNCH();
+    int hf = 0;
+    SID_CUDA_TRY(cudaMemcpyAsync(&hf, nfail, sizeof(int), cudaMemcpyDeviceToHost, st));
+    SID_TRY(ctx_sync(c, st));
+    if (hf) {
+        set_error("sid_spatial_update: %d pixel problems failed (more than %d covering components, or the "
+                  "NQP iteration cap of NQP.m:116-119); see the status array",
+                  hf, kNqpMax);
+        return SID_ENOCONV;
+    }
+    return SID_OK;
+}

@@ -1,0 +1,5 @@
+function Backprojection = backwardProjectGPU_new(H, projection)
+% Drop-in for backwardProjectGPU_new.m (same signature).
+plan = sid_plan_for(H, [], size(projection, 1), size(projection, 2));
+Backprojection = sid_mex('adjoint', plan, single(projection), 1);
+end

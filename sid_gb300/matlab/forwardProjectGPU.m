@@ -1,0 +1,6 @@
+function TOTALprojection = forwardProjectGPU(H, realspace)
+% Drop-in for forwardProjectGPU.m (same signature): libsid projection with
+% the PSF resident on the GPU.
+plan = sid_plan_for(H, [], size(realspace, 1), size(realspace, 2));
+TOTALprojection = sid_mex('forward', plan, single(realspace), 3);
+end

@@ -161,3 +161,39 @@ def LS_nnls(A, Y, opts=None, G=None, x=None):
 def fast_nnls(A, Y, opts=None):
     """[xx, Q] = fast_nnls(A, Y, opts) (fast_nnls.m:1)."""
     return _ctx().fast_nnls(A, Y, opts)
+
+
+def _spatial_update(self, timeseries, sensor_movie, template, opts=None):
+    """forward_model = update_spatial_component(timeseries, sensor_movie,
+    template, opts) (update_spatial_component.m:1), dense (R x P)."""
+    opts = dict(opts or {})
+    T = to_device(timeseries)
+    Yd, half = _movie(sensor_movie)
+    R, F = T.shape
+    P = Yd.shape[0]
+    tm = template
+    if isinstance(tm, torch.Tensor):
+        tm = tm.to(device="cuda", dtype=torch.uint8)
+        tm = tm.permute(1, 0).contiguous().permute(1, 0)
+    else:
+        arr = np.asfortranarray(np.asarray(tm).astype(np.uint8))
+        tm = torch.from_numpy(np.ascontiguousarray(arr.T)).to("cuda").permute(1, 0)
+    bg = 1 if opts.get("bg_sub", 1) else 0
+    if tm.shape != (R - bg, P):
+        raise ValueError(f"template must be {(R - bg, P)}, got {tuple(tm.shape)}")
+    out = _fortran_tensor((R, P), T.device)
+    status = torch.zeros(P, dtype=torch.int32, device=T.device)
+    _lib.call("sid_spatial_update", self._ctx, T.data_ptr(), Yd.data_ptr(),
+              _lib.DTYPE_F16 if half else _lib.DTYPE_F32, tm.data_ptr(), R, F, P,
+              float(opts.get("lamb_L1", 0.0)), float(opts.get("lamb_L2", 0.0)),
+              float(opts.get("lamb_orth_L1", 0.0)), 1 if opts.get("use_std", False) else 0, bg,
+              out.data_ptr(), status.data_ptr(), _stream_ptr())
+    return out
+
+
+Context.spatial_update = _spatial_update
+
+
+def update_spatial_component(timeseries, sensor_movie, template, opts=None):
+    """forward_model = update_spatial_component(timeseries, sensor_movie, template, opts)."""
+    return _ctx().spatial_update(timeseries, sensor_movie, template, opts)
