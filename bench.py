@@ -297,7 +297,10 @@ def main():
     H, Vt = workload(args.config)
     X, Y, Z = Vt.shape
     methods = [args.method] + [m for m in args.compare.split(",") if m and m != args.method]
-    P = s.Projector(H, (X, Y), None, methods=tuple(methods))
+    plan_methods = list(methods)
+    if not args.no_nnls and "direct" not in plan_methods:
+        plan_methods.append("direct")  # the library generation reads the lenslet taps
+    P = s.Projector(H, (X, Y), None, methods=tuple(plan_methods))
     info = P.info()
     # RL input: Htf = A^T y with y = A V_true (the reference starts ISRA at Xguess = Htf)
     y = P.forward(Vt, method=args.method)
@@ -404,7 +407,7 @@ def main():
                      "fwd_rel_err_vs_fp64": float(np.linalg.norm(gm - ref_pix) / np.linalg.norm(ref_pix))}
 
     nnls = None
-    if not args.no_nnls and "direct" in methods:
+    if not args.no_nnls:
         nnls = nnls_workload(args, P)
 
     cpu = None

@@ -528,9 +528,14 @@ def fast_nnls(A, Y, opts=None, Q=None, df=None, h=None, return_iters=False):
 # ----------------------------------------------------------------------------
 # NMF steps: T_update.m:5-78 and S_update.m:4-80
 # ----------------------------------------------------------------------------
-def _zscore_rows(T):
-    mu = T.mean(axis=1, keepdims=True)
-    sd = T.std(axis=1, ddof=1, keepdims=True)
+def _matlab_zscore(T):
+    """MATLAB zscore(T): along the first non-singleton dimension (columns of
+    an R x F matrix with R > 1), N-1 normalisation, a zero standard deviation
+    replaced by 1."""
+    ax = 0 if T.shape[0] > 1 else 1
+    mu = T.mean(axis=ax, keepdims=True)
+    sd = T.std(axis=ax, ddof=1, keepdims=True)
+    sd[sd == 0] = 1.0
     return (T - mu) / sd
 
 
@@ -557,7 +562,7 @@ def T_update(Y, T, S, opts):
         Qf = lambda v: Q_S @ v  # noqa: E731
     lamb_temp = opts.get("lamb_temp", 0.0)
     if lamb_corr:
-        zsc = _zscore_rows(T)
+        zsc = _matlab_zscore(T)  # T_update.m:38
         d = T.std(axis=1, ddof=1)
         hilf = (zsc @ zsc.T) @ zsc - zsc
         hilf = (1.0 / d)[:, None] * (hilf - (hilf.sum(axis=1, keepdims=True) * np.ones_like(T)) / F

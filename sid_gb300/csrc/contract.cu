@@ -14,17 +14,17 @@
 #include "sid_internal.cuh"
 
 namespace sid {
-int gemm_tn(const void* const* A, const void* const* B, int npass, int64_t m, int64_t n, int64_t k, int64_t lda,
-            int64_t ldb, bool bf16, float* C, int64_t ldc, float alpha, float beta, int bn, int splitk, float* ws,
-            int64_t ws_elems, int* err, cudaStream_t st);
+int gemm_tn(const void* const* A, const void* const* B, int npass, int64_t m, int64_t n, int64_t k, bool bf16,
+            float* C, int64_t ldc, float alpha, float beta, int bn, int splitk, float* ws, int64_t ws_elems, int* err,
+            cudaStream_t st);
 void gemm_autotune(int m, int n, int nkb, int* bn, int* splitk);
 int sgemm_tn(const float* A, const float* B, int64_t m, int64_t n, int64_t k, int64_t lda, int64_t ldb, float* C,
              int64_t ldc, float alpha, float beta, float* ws, int64_t ws_elems, cudaStream_t st);
 int64_t sgemm_ws_elems(int64_t m, int64_t n, int64_t k);
-int split16(const float* src, int64_t rows, int64_t cols, int64_t lds, uint16_t* hi, uint16_t* lo, int64_t ld,
-            bool bf16, float scale, cudaStream_t st);
-int copy16_pad(const uint16_t* src, int64_t rows, int64_t cols, int64_t lds, uint16_t* dst, int64_t ld,
-               cudaStream_t st);
+int split16(const float* src, int64_t k, int64_t rows, int64_t lds, uint16_t* hi, uint16_t* lo, bool bf16,
+            float scale, cudaStream_t st);
+int copy16_blk(const uint16_t* src, int64_t k, int64_t rows, int64_t lds, uint16_t* dst, cudaStream_t st);
+int64_t blk16_elems(int64_t k, int64_t rows);
 int absmax(const float* x, int64_t n, unsigned int* out, cudaStream_t st);
 }  // namespace sid
 
@@ -42,8 +42,6 @@ int ctx_sync(sid_ctx* c, cudaStream_t st)
     }
     return SID_OK;
 }
-
-static inline int64_t pad8(int64_t v) { return cdiv(v, 8) * 8; }
 
 // Largest power of two s with max|x| * s <= 2^14 (FP16 operand scaling).
 static int pow2_scale(sid_ctx* c, const float* x, int64_t n, float* scale, cudaStream_t st)
@@ -72,50 +70,43 @@ int contract(sid_ctx* c, const float* A, const void* B, bool b_f16, int64_t m, i
                         (int64_t)(c->ws.bytes / sizeof(float)), st);
     }
     SID_REQUIRE(prec == SID_PREC_SPLIT || prec == SID_PREC_BF16, "unknown precision %d", prec);
-    const int64_t kp = pad8(k);
     int bn = 0, splitk = 0;
     gemm_autotune((int)m, (int)n, (int)cdiv(k, 64), &bn, &splitk);
     SID_TRY(c->ws.alloc((size_t)(splitk * m * n) * sizeof(float)));
     const bool split = prec == SID_PREC_SPLIT;
+    const size_t abytes = (size_t)blk16_elems(k, m) * 2, bbytes = (size_t)blk16_elems(k, n) * 2;
     if (b_f16) {
-        // FP16 right operand used as is; A split into FP16 hi/lo with a power-of-two scale
+        // FP16 right operand used unsplit; A split into FP16 hi/lo with a power-of-two scale
         float sa = 1.f;
         SID_TRY(pow2_scale(c, A, m * lda, &sa, st));  // over the whole stored matrix
-        SID_TRY(c->a_hi.alloc((size_t)(kp * m) * 2));
-        if (split) SID_TRY(c->a_lo.alloc((size_t)(kp * m) * 2));
-        SID_TRY(split16(A, k, m, lda, c->a_hi.as<uint16_t>(), split ? c->a_lo.as<uint16_t>() : nullptr, kp, false,
-                        sa, st));
-        const void* bptr = B;
-        int64_t ldbb = ldb;
-        if (ldb % 8 != 0 || ((uintptr_t)B & 15) != 0) {
-            SID_TRY(c->b_hi.alloc((size_t)(kp * n) * 2));
-            SID_TRY(copy16_pad(static_cast<const uint16_t*>(B), k, n, ldb, c->b_hi.as<uint16_t>(), kp, st));
-            bptr = c->b_hi.p;
-            ldbb = kp;
-        }
+        SID_TRY(c->a_hi.alloc(abytes));
+        if (split) SID_TRY(c->a_lo.alloc(abytes));
+        SID_TRY(split16(A, k, m, lda, c->a_hi.as<uint16_t>(), split ? c->a_lo.as<uint16_t>() : nullptr, false, sa, st));
+        SID_TRY(c->b_hi.alloc(bbytes));
+        SID_TRY(copy16_blk(static_cast<const uint16_t*>(B), k, n, ldb, c->b_hi.as<uint16_t>(), st));
         const void* As[2] = {c->a_hi.p, c->a_lo.p};
-        const void* Bs[2] = {bptr, bptr};
-        return gemm_tn(As, Bs, split ? 2 : 1, m, n, k, kp, ldbb, false, C, ldc, alpha / sa, beta, bn, splitk,
-                       c->ws.as<float>(), (int64_t)(c->ws.bytes / sizeof(float)), err, st);
+        const void* Bs[2] = {c->b_hi.p, c->b_hi.p};
+        return gemm_tn(As, Bs, split ? 2 : 1, m, n, k, false, C, ldc, alpha / sa, beta, bn, splitk, c->ws.as<float>(),
+                       (int64_t)(c->ws.bytes / sizeof(float)), err, st);
     }
     // FP32 x FP32: BF16 hi/lo splits of both (no scaling needed: BF16 keeps the FP32 exponent range)
     const bool same = (static_cast<const void*>(A) == B && lda == ldb && m == n);
-    SID_TRY(c->a_hi.alloc((size_t)(kp * m) * 2));
-    if (split) SID_TRY(c->a_lo.alloc((size_t)(kp * m) * 2));
-    SID_TRY(split16(A, k, m, lda, c->a_hi.as<uint16_t>(), split ? c->a_lo.as<uint16_t>() : nullptr, kp, true, 1.f, st));
+    SID_TRY(c->a_hi.alloc(abytes));
+    if (split) SID_TRY(c->a_lo.alloc(abytes));
+    SID_TRY(split16(A, k, m, lda, c->a_hi.as<uint16_t>(), split ? c->a_lo.as<uint16_t>() : nullptr, true, 1.f, st));
     const void *bh = c->a_hi.p, *bl = c->a_lo.p;
     if (!same) {
-        SID_TRY(c->b_hi.alloc((size_t)(kp * n) * 2));
-        if (split) SID_TRY(c->b_lo.alloc((size_t)(kp * n) * 2));
+        SID_TRY(c->b_hi.alloc(bbytes));
+        if (split) SID_TRY(c->b_lo.alloc(bbytes));
         SID_TRY(split16(static_cast<const float*>(B), k, n, ldb, c->b_hi.as<uint16_t>(),
-                        split ? c->b_lo.as<uint16_t>() : nullptr, kp, true, 1.f, st));
+                        split ? c->b_lo.as<uint16_t>() : nullptr, true, 1.f, st));
         bh = c->b_hi.p;
         bl = c->b_lo.p;
     }
     const void* As[3] = {c->a_hi.p, c->a_hi.p, c->a_lo.p};
     const void* Bs[3] = {bh, bl, bh};
-    return gemm_tn(As, Bs, split ? 3 : 1, m, n, k, kp, kp, true, C, ldc, alpha, beta, bn, splitk,
-                   c->ws.as<float>(), (int64_t)(c->ws.bytes / sizeof(float)), err, st);
+    return gemm_tn(As, Bs, split ? 3 : 1, m, n, k, true, C, ldc, alpha, beta, bn, splitk, c->ws.as<float>(),
+                   (int64_t)(c->ws.bytes / sizeof(float)), err, st);
 }
 
 }  // namespace sid

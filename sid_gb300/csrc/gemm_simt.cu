@@ -8,6 +8,8 @@
 // pairs), register double buffering of the next K slice.
 #include <cuda_bf16.h>
 
+#include <algorithm>
+
 #include "sid_internal.cuh"
 
 namespace sid {
@@ -148,43 +150,76 @@ int64_t sgemm_ws_elems(int64_t m, int64_t n, int64_t k)
 }
 
 // ------------------------------------------------ FP32 -> 16-bit splits ----
-// dst_hi/dst_lo: (rows x cols) with leading dimension ld (>= rows, multiple of
-// 8), rows = the reduction dimension (contiguous).  hi = round(src*scale),
-// lo = round(src*scale - hi).  Padding rows [rows, ld) are zero.
+// Source: element (kk, r) of a k x rows matrix at src[kk + lds*r] (the
+// reduction index contiguous).  Destination: the K-blocked layout of the
+// tensor-core GEMM, element (kk, r) at ((kk/64)*rows + r)*64 + kk%64, with
+// zeros past k.  hi = round(src*scale), lo = round(src*scale - hi).
+// One thread per 4 consecutive elements of one row: 16-byte reads when the
+// source allows them, 8-byte writes; a warp covers two 128-byte block rows.
 template <bool BF16>
-__global__ void k_split16(const float* __restrict__ src, int64_t rows, int64_t cols, int64_t lds,
-                          uint16_t* __restrict__ hi, uint16_t* __restrict__ lo, int64_t ld, float scale)
+__global__ void k_split16_blk(const float* __restrict__ src, int64_t k, int64_t rows, int64_t lds,
+                              uint16_t* __restrict__ hi, uint16_t* __restrict__ lo, float scale, int vec4)
 {
-    const int64_t total = ld * cols;
+    const int64_t nkb = (k + 63) / 64;
+    const int64_t total = nkb * rows * 16;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t r = i % ld, c = i / ld;
-        const float v = (r < rows) ? src[r + lds * c] * scale : 0.f;
-        uint16_t h, l;
-        if (BF16) {
-            const __nv_bfloat16 bh = __float2bfloat16_rn(v);
-            const __nv_bfloat16 bl = __float2bfloat16_rn(v - __bfloat162float(bh));
-            h = __bfloat16_as_ushort(bh);
-            l = __bfloat16_as_ushort(bl);
+        const int g = (int)(i & 15);
+        const int64_t rr = i >> 4;
+        const int64_t r = rr % rows, kb = rr / rows;
+        const int64_t kk = kb * 64 + g * 4;
+        float v[4];
+        const float* sp = src + kk + lds * r;
+        if (vec4 && kk + 3 < k) {
+            const float4 q = *reinterpret_cast<const float4*>(sp);
+            v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
         } else {
-            const __half fh = __float2half_rn(v);
-            const __half fl = __float2half_rn(v - __half2float(fh));
-            h = __half_as_ushort(fh);
-            l = __half_as_ushort(fl);
+#pragma unroll
+            for (int e = 0; e < 4; ++e) v[e] = (kk + e < k) ? sp[e] : 0.f;
         }
-        hi[i] = h;
-        if (lo) lo[i] = l;
+        uint16_t h[4], l[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            const float x = v[e] * scale;
+            if (BF16) {
+                const __nv_bfloat16 bh = __float2bfloat16_rn(x);
+                h[e] = __bfloat16_as_ushort(bh);
+                l[e] = __bfloat16_as_ushort(__float2bfloat16_rn(x - __bfloat162float(bh)));
+            } else {
+                const __half fh = __float2half_rn(x);
+                h[e] = __half_as_ushort(fh);
+                l[e] = __half_as_ushort(__float2half_rn(x - __half2float(fh)));
+            }
+        }
+        const int64_t o = rr * 64 + g * 4;  // (kb*rows + r)*64 + 4g
+        *reinterpret_cast<uint2*>(hi + o) = make_uint2(h[0] | ((uint32_t)h[1] << 16), h[2] | ((uint32_t)h[3] << 16));
+        if (lo) *reinterpret_cast<uint2*>(lo + o) = make_uint2(l[0] | ((uint32_t)l[1] << 16), l[2] | ((uint32_t)l[3] << 16));
     }
 }
 
-// 16-bit copy with row padding (for FP16 inputs whose leading dimension is
-// not a multiple of 8).
-__global__ void k_copy16_pad(const uint16_t* __restrict__ src, int64_t rows, int64_t cols, int64_t lds,
-                             uint16_t* __restrict__ dst, int64_t ld)
+// 16-bit copy of a k x rows matrix (src[kk + lds*r]) into the K-blocked
+// layout.  One thread per 8 elements: 16-byte writes, 16-byte reads when aligned.
+__global__ void k_copy16_blk(const uint16_t* __restrict__ src, int64_t k, int64_t rows, int64_t lds,
+                             uint16_t* __restrict__ dst, int vec8)
 {
-    const int64_t total = ld * cols;
+    const int64_t nkb = (k + 63) / 64;
+    const int64_t total = nkb * rows * 8;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t r = i % ld, c = i / ld;
-        dst[i] = (r < rows) ? src[r + lds * c] : (uint16_t)0;
+        const int g = (int)(i & 7);
+        const int64_t rr = i >> 3;
+        const int64_t r = rr % rows, kb = rr / rows;
+        const int64_t kk = kb * 64 + g * 8;
+        const uint16_t* sp = src + kk + lds * r;
+        uint4 out;
+        if (vec8 && kk + 7 < k) {
+            out = *reinterpret_cast<const uint4*>(sp);
+        } else {
+            uint16_t t[8];
+#pragma unroll
+            for (int e = 0; e < 8; ++e) t[e] = (kk + e < k) ? sp[e] : (uint16_t)0;
+            out = make_uint4(t[0] | ((uint32_t)t[1] << 16), t[2] | ((uint32_t)t[3] << 16),
+                             t[4] | ((uint32_t)t[5] << 16), t[6] | ((uint32_t)t[7] << 16));
+        }
+        *reinterpret_cast<uint4*>(dst + rr * 64 + g * 8) = out;
     }
 }
 
@@ -199,21 +234,27 @@ __global__ void k_absmax(const float* __restrict__ x, int64_t n, unsigned int* _
     if ((threadIdx.x & 31) == 0 && m > 0.f) atomicMax(out, __float_as_uint(m));
 }
 
-int split16(const float* src, int64_t rows, int64_t cols, int64_t lds, uint16_t* hi, uint16_t* lo, int64_t ld,
-            bool bf16, float scale, cudaStream_t st)
+int64_t blk16_elems(int64_t k, int64_t rows) { return cdiv(k, 64) * 64 * rows; }
+
+// K-blocked 16-bit split of a k x rows FP32 matrix (see k_split16_blk)
+int split16(const float* src, int64_t k, int64_t rows, int64_t lds, uint16_t* hi, uint16_t* lo, bool bf16,
+            float scale, cudaStream_t st)
 {
-    if (bf16)
-        k_split16<true><<<2048, 256, 0, st>>>(src, rows, cols, lds, hi, lo, ld, scale);
-    else
-        k_split16<false><<<2048, 256, 0, st>>>(src, rows, cols, lds, hi, lo, ld, scale);
+    const int vec4 = ((lds & 3) == 0 && ((uintptr_t)src & 15) == 0) ? 1 : 0;
+    const int64_t total = cdiv(k, 64) * rows * 16;
+    const unsigned grid = (unsigned)std::min<int64_t>(cdiv(total, 256), 152 * 32);
+    if (bf16) k_split16_blk<true><<<grid, 256, 0, st>>>(src, k, rows, lds, hi, lo, scale, vec4);
+    else k_split16_blk<false><<<grid, 256, 0, st>>>(src, k, rows, lds, hi, lo, scale, vec4);
     SID_CHECK_LAUNCH();
     return SID_OK;
 }
 
-int copy16_pad(const uint16_t* src, int64_t rows, int64_t cols, int64_t lds, uint16_t* dst, int64_t ld,
-               cudaStream_t st)
+int copy16_blk(const uint16_t* src, int64_t k, int64_t rows, int64_t lds, uint16_t* dst, cudaStream_t st)
 {
-    k_copy16_pad<<<2048, 256, 0, st>>>(src, rows, cols, lds, dst, ld);
+    const int vec8 = ((lds & 7) == 0 && ((uintptr_t)src & 15) == 0) ? 1 : 0;
+    const int64_t total = cdiv(k, 64) * rows * 8;
+    const unsigned grid = (unsigned)std::min<int64_t>(cdiv(total, 256), 152 * 32);
+    k_copy16_blk<<<grid, 256, 0, st>>>(src, k, rows, lds, dst, vec8);
     SID_CHECK_LAUNCH();
     return SID_OK;
 }

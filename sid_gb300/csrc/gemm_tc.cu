@@ -1,8 +1,14 @@
 // gemm_tc.cu -- tcgen05 tensor-core GEMM for the NNLS Gram and cross products.
 //
 //   C (m x n, column-major, ldc) = sum_{p < npass} A_p^T B_p
-//   A_p: k x m column-major 16-bit (the reduction index k is contiguous),
-//   B_p: k x n column-major 16-bit, both BF16 or both FP16; FP32 accumulation.
+//   A_p (k x m) and B_p (k x n): 16-bit operands, both BF16 or both FP16, in
+//   the K-BLOCKED layout [k/64][row][64] (element (kk, r) at
+//   ((kk/64)*rows + r)*64 + kk%64), zero-padded to whole 64-element blocks;
+//   FP32 accumulation.
+// The blocked layout makes every 64 x BN TMA box one contiguous run of memory:
+// with a plain column-major operand the rows of a box are a whole column apart
+// (2 MB for a 1M-pixel movie), so each box touched BN pages and the GEMM ran
+// at a third of its speed on full-size problems.
 // This is the "TN" form every contraction of the path takes: S'S and S'Y with
 // the library and the movie stored pixel-major (LS_nnls.m:76,82,
 // fast_nnls.m:54-57, T_update.m:24-25), and G*x in the NNLS iterations.
@@ -10,12 +16,12 @@
 // precision products (hi*hi + hi*lo + lo*hi) with FP32 accumulation in TMEM.
 //
 // Kernel: one 128 x BN output tile per CTA (optionally a K range of it, for
-// split-K), 6 warps.  One thread drives a STAGES-deep TMA ring (128B-swizzled
+// split-K), 10 warps.  One thread drives a STAGES-deep TMA ring (128B-swizzled
 // 64-element K blocks, completion on "full" mbarriers); one thread issues
 // tcgen05.mma (cta_group::1, M=128, N=BN, K=16 per instruction) into one of two
 // TMEM accumulators and releases each stage through tcgen05.commit on its
-// "empty" mbarrier; four warps read finished accumulators back with tcgen05.ld
-// (warp w owns TMEM lanes 32w..32w+31 = tile rows) and add them to the output.
+// "empty" mbarrier; eight warps read finished accumulators back with tcgen05.ld
+// and sum them in registers, writing the tile once.
 // Every mbarrier wait is bounded (ptx.cuh); on a timeout the CTA records the
 // error, stops issuing, waits (bounded) for issued MMAs, frees TMEM and exits.
 #include <cuda.h>
@@ -64,12 +70,12 @@ __device__ __forceinline__ uint32_t instr_desc(int n, bool bf16)
     return (1u << 4) | (fmt << 7) | (fmt << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(GEMM_BM >> 4) << 24);
 }
 
-__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y, uint64_t* bar)
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int x, int y, int z, uint64_t* bar)
 {
     asm volatile(
-        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(
             smem_u32(dst)),
-        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
         : "memory");
 }
 
@@ -120,22 +126,28 @@ struct GemmSmem {
 // grid: (ceil(m/128), ceil(n/BN), splitk).  out + z*split_stride receives the
 // partial sum of K blocks [z*kb_per, (z+1)*kb_per) of every pass.
 //
-// Warp roles (192 threads): warps 0-3 drain the accumulator (warp w owns TMEM
-// lanes 32w..32w+31, i.e. tile rows), warp 4 lane 0 is the TMA producer, warp 5
-// lane 0 issues the MMAs.  The tensor-core FP32 accumulator does not round to
-// nearest, so long K chains drift: the K range is cut into chunks of KCHUNK
-// blocks, each accumulated in one of two TMEM buffers while the previous chunk
-// is drained and added (round-to-nearest) into the output tile.
+// Warp roles (320 threads): warps 0-7 drain the accumulator -- warp w reads
+// TMEM lanes 32*(w%4)..+31 (tile rows) and columns [(w/4)*BN/2, (w/4+1)*BN/2)
+// -- warp 8 lane 0 is the TMA producer, warp 9 lane 0 issues the MMAs.  The
+// tensor-core FP32 accumulator does not round to nearest, so long K chains
+// drift (a 70000-deep chain lost 9e-5): the K range is cut into chunks of
+// GEMM_KCHUNK blocks, each accumulated in one of two TMEM buffers while the
+// previous chunk is drained and added, round-to-nearest, into registers; the
+// tile is written once at the end.
 constexpr int GEMM_KCHUNK = 16;  // 16 x 64 = 1024 reduction elements per chain
+constexpr int GEMM_DRAIN_WARPS = 8;
+constexpr int GEMM_THREADS = (GEMM_DRAIN_WARPS + 2) * 32;
 
 template <int BN, int STAGES>
-__global__ void __launch_bounds__(192, 1)
+__global__ void __launch_bounds__(GEMM_THREADS, 1)
 k_gemm_tc(const __grid_constant__ GemmMaps maps, int npass, int m, int n, int nkb, int kb_per, int bf16,
           float* __restrict__ out, int64_t ldc, int64_t split_stride, int* __restrict__ err)
 {
     using SM = GemmSmem<BN, STAGES>;
     constexpr uint32_t ACC_COLS = BN <= 32 ? 32 : (BN <= 64 ? 64 : (BN <= 128 ? 128 : 256));
     constexpr uint32_t TMEM_COLS = 2 * ACC_COLS;  // two accumulators
+    constexpr int HALF = BN / 2;                  // columns per drain thread
+    static_assert(HALF % 32 == 0, "BN must be a multiple of 64");
     extern __shared__ uint8_t gsm_raw[];
     uint8_t* gsm = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(gsm_raw) + 1023) & ~uintptr_t(1023));
     __shared__ __align__(8) uint64_t full[STAGES], empty[STAGES], tfull[2], tempty[2];
@@ -148,6 +160,7 @@ k_gemm_tc(const __grid_constant__ GemmMaps maps, int npass, int m, int n, int nk
     const int kb1 = min(nkb, kb0 + kb_per);
     const int nloc = kb1 > kb0 ? (kb1 - kb0) : 0;
     const int nchunk = (nloc + GEMM_KCHUNK - 1) / GEMM_KCHUNK;
+    constexpr int PRODUCER = GEMM_DRAIN_WARPS, ISSUER = GEMM_DRAIN_WARPS + 1;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES; ++s) {
@@ -156,7 +169,7 @@ k_gemm_tc(const __grid_constant__ GemmMaps maps, int npass, int m, int n, int nk
         }
         for (int b = 0; b < 2; ++b) {
             mbar_init(&tfull[b], 1);
-            mbar_init(&tempty[b], 128);
+            mbar_init(&tempty[b], GEMM_DRAIN_WARPS * 32);
         }
         abort_flag = 0;
         fence_mbar_init();
@@ -173,7 +186,7 @@ k_gemm_tc(const __grid_constant__ GemmMaps maps, int npass, int m, int n, int nk
     const uint32_t tmem = tmem_slot;
     float* dst = out + (int64_t)blockIdx.z * split_stride;
 
-    if (warp == 4) {
+    if (warp == PRODUCER) {
         if (lane == 0) {
             // TMA producer: chunk -> pass -> k block
             int it = 0;
@@ -190,14 +203,14 @@ k_gemm_tc(const __grid_constant__ GemmMaps maps, int npass, int m, int n, int nk
                         uint8_t* sa = gsm + s * SM::STAGE_BYTES;
                         uint8_t* sb = sa + SM::A_BYTES;
                         mbar_arrive_expect_tx(&full[s], SM::STAGE_BYTES);
-                        tma_load_2d(sa, &maps.a[pass], kb * GEMM_BK, m0, &full[s]);
-                        tma_load_2d(sb, &maps.b[pass], kb * GEMM_BK, n0, &full[s]);
+                        tma_load_3d(sa, &maps.a[pass], 0, m0, kb, &full[s]);
+                        tma_load_3d(sb, &maps.b[pass], 0, n0, kb, &full[s]);
                     }
                     if (*(volatile int*)&abort_flag) break;
                 }
             }
         }
-    } else if (warp == 5) {
+    } else if (warp == ISSUER) {
         if (lane == 0) {
             // MMA issuer: chunk c accumulates into TMEM buffer c & 1
             const uint32_t idesc = instr_desc(BN, bf16 != 0);
@@ -238,33 +251,36 @@ k_gemm_tc(const __grid_constant__ GemmMaps maps, int npass, int m, int n, int nk
             if (!ok) atomicExch(&abort_flag, 1);
         }
     } else {
-        // drain warps 0-3: add each finished chunk into the output tile
-        const int row = m0 + warp * 32 + lane;
+        // drain warps: add each finished chunk into registers
+        const int lg = warp & 3;           // TMEM lane group = tile rows 32*lg..
+        const int ch0 = (warp >> 2) * HALF;  // first column of this warp
+        const int row = m0 + lg * 32 + lane;
+        float accr[HALF];
+#pragma unroll
+        for (int j = 0; j < HALF; ++j) accr[j] = 0.f;
+        bool ok = true;
         for (int c = 0; c < nchunk; ++c) {
             const int b = c & 1;
-            const bool ok = __all_sync(0xffffffffu, mbar_wait(&tfull[b], (uint32_t)((c >> 1) & 1), err));
+            ok = __all_sync(0xffffffffu, mbar_wait(&tfull[b], (uint32_t)((c >> 1) & 1), err));
             if (!ok) break;
             tc_fence_after();
-#pragma unroll 1
-            for (int c0 = 0; c0 < BN; c0 += 32) {
-                float v[32];
-                tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(b * ACC_COLS + c0), v);
-                if (row < m) {
 #pragma unroll
-                    for (int j = 0; j < 32; ++j) {
-                        const int col = n0 + c0 + j;
-                        if (col < n) {
-                            float* d = dst + (int64_t)row + ldc * col;
-                            *d = (c == 0) ? v[j] : *d + v[j];
-                        }
-                    }
-                }
+            for (int c0 = 0; c0 < HALF; c0 += 32) {
+                float v[32];
+                tmem_ld32(tmem + ((uint32_t)(lg * 32) << 16) + (uint32_t)(b * ACC_COLS + ch0 + c0), v);
+#pragma unroll
+                for (int j = 0; j < 32; ++j) accr[c0 + j] += v[j];
             }
             tc_fence_before();
             mbar_arrive(&tempty[b]);
         }
-        if (nchunk == 0 && row < m)
-            for (int col = n0; col < min(n, n0 + BN); ++col) dst[(int64_t)row + ldc * col] = 0.f;
+        if (ok && row < m) {
+#pragma unroll
+            for (int j = 0; j < HALF; ++j) {
+                const int col = n0 + ch0 + j;
+                if (col < n) dst[(int64_t)row + ldc * col] = accr[j];
+            }
+        }
     }
     __syncwarp();
     tc_fence_before();
@@ -291,16 +307,14 @@ __global__ void k_splitk_reduce(const float* __restrict__ part, int nsplit, int6
 }
 
 // ----------------------------------------------------------- host side ----
-static int make_map(CUtensorMap* map, const void* base, int64_t rows, int64_t kdim, int64_t ld, int box_rows,
-                    bool bf16)
+static int make_map(CUtensorMap* map, const void* base, int64_t rows, int64_t nkb, int box_rows, bool bf16)
 {
-    // 2-D tensor: inner dimension k (contiguous), outer dimension rows with stride ld elements
+    // K-blocked operand: dims {64, rows, nkb}, byte strides {128, rows*128}
     SID_REQUIRE(((uintptr_t)base & 15) == 0, "gemm: operand base address not 16-byte aligned");
-    SID_REQUIRE((ld * 2) % 16 == 0, "gemm: leading dimension %lld not a multiple of 8 elements", (long long)ld);
-    cuuint64_t dims[2] = {(cuuint64_t)kdim, (cuuint64_t)rows};
-    cuuint64_t strides[1] = {(cuuint64_t)(ld * 2)};
-    cuuint32_t box[2] = {GEMM_BK, (cuuint32_t)box_rows};
-    cuuint32_t estr[2] = {1, 1};
+    cuuint64_t dims[3] = {(cuuint64_t)GEMM_BK, (cuuint64_t)rows, (cuuint64_t)nkb};
+    cuuint64_t strides[2] = {(cuuint64_t)(GEMM_BK * 2), (cuuint64_t)(rows * GEMM_BK * 2)};
+    cuuint32_t box[3] = {GEMM_BK, (cuuint32_t)box_rows, 1};
+    cuuint32_t estr[3] = {1, 1, 1};
     // resolved through the runtime so libsid does not link libcuda directly
     using EncodeFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
@@ -316,10 +330,10 @@ static int make_map(CUtensorMap* map, const void* base, int64_t rows, int64_t kd
         }
         encode = reinterpret_cast<EncodeFn>(fn);
     }
-    CUresult r = encode(map, bf16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16,
-                                        2, const_cast<void*>(base), dims, strides, box, estr,
-                                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
-                                        CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    CUresult r = encode(map, bf16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 3,
+                        const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                        CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) {
         set_error("cuTensorMapEncodeTiled failed (CUresult %d)", (int)r);
         return SID_ECUDA;
@@ -339,7 +353,7 @@ static int launch_gemm(const GemmMaps& maps, int npass, int m, int n, int nkb, i
     }
     const int kb_per = (int)cdiv(nkb, splitk);
     dim3 grid((unsigned)cdiv(m, GEMM_BM), (unsigned)cdiv(n, BN), (unsigned)splitk);
-    k_gemm_tc<BN, STAGES><<<grid, 192, SM::TOTAL, st>>>(maps, npass, m, n, nkb, kb_per, bf16 ? 1 : 0, out, ldc,
+    k_gemm_tc<BN, STAGES><<<grid, GEMM_THREADS, SM::TOTAL, st>>>(maps, npass, m, n, nkb, kb_per, bf16 ? 1 : 0, out, ldc,
                                                          split_stride, err);
     SID_CHECK_LAUNCH();
     return SID_OK;
@@ -379,11 +393,11 @@ void gemm_autotune(int m, int n, int nkb, int* bn, int* splitk)
     *splitk = bs;
 }
 
-// out (m x n, ldc) = sum_p A_p^T B_p; A_p: k x m (lda), B_p: k x n (ldb), 16-bit.
-// ws: >= splitk * ldc * n floats when splitk > 1.
-int gemm_tn(const void* const* A, const void* const* B, int npass, int64_t m, int64_t n, int64_t k, int64_t lda,
-            int64_t ldb, bool bf16, float* C, int64_t ldc, float alpha, float beta, int bn, int splitk,
-            float* ws, int64_t ws_elems, int* err, cudaStream_t st)
+// out (m x n, ldc) = sum_p A_p^T B_p; A_p: k x m, B_p: k x n, 16-bit K-blocked.
+// ws: >= splitk * m * n floats when splitk > 1 or (alpha, beta) != (1, 0).
+int gemm_tn(const void* const* A, const void* const* B, int npass, int64_t m, int64_t n, int64_t k, bool bf16,
+            float* C, int64_t ldc, float alpha, float beta, int bn, int splitk, float* ws, int64_t ws_elems, int* err,
+            cudaStream_t st)
 {
     SID_REQUIRE(npass >= 1 && npass <= GEMM_MAXPASS, "gemm: npass %d outside [1,3]", npass);
     SID_REQUIRE(m > 0 && n > 0 && k > 0, "gemm: empty problem");
@@ -393,8 +407,8 @@ int gemm_tn(const void* const* A, const void* const* B, int npass, int64_t m, in
     GemmMaps maps;
     std::memset(&maps, 0, sizeof(maps));
     for (int p = 0; p < npass; ++p) {
-        SID_TRY(make_map(&maps.a[p], A[p], m, k, lda, GEMM_BM, bf16));
-        SID_TRY(make_map(&maps.b[p], B[p], n, k, ldb, bn, bf16));
+        SID_TRY(make_map(&maps.a[p], A[p], m, nkb, GEMM_BM, bf16));
+        SID_TRY(make_map(&maps.b[p], B[p], n, nkb, bn, bf16));
     }
     const bool direct = (splitk == 1 && alpha == 1.f && beta == 0.f);
     float* out = C;

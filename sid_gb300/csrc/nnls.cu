@@ -32,15 +32,16 @@
 namespace sid {
 int contract(sid_ctx* c, const float* A, const void* B, bool b_f16, int64_t m, int64_t n, int64_t k, int64_t lda,
              int64_t ldb, float* C, int64_t ldc, float alpha, float beta, int prec, cudaStream_t st);
-int gemm_tn(const void* const* A, const void* const* B, int npass, int64_t m, int64_t n, int64_t k, int64_t lda,
-            int64_t ldb, bool bf16, float* C, int64_t ldc, float alpha, float beta, int bn, int splitk, float* ws,
-            int64_t ws_elems, int* err, cudaStream_t st);
+int gemm_tn(const void* const* A, const void* const* B, int npass, int64_t m, int64_t n, int64_t k, bool bf16,
+            float* C, int64_t ldc, float alpha, float beta, int bn, int splitk, float* ws, int64_t ws_elems, int* err,
+            cudaStream_t st);
 void gemm_autotune(int m, int n, int nkb, int* bn, int* splitk);
 int sgemm_tn(const float* A, const float* B, int64_t m, int64_t n, int64_t k, int64_t lda, int64_t ldb, float* C,
              int64_t ldc, float alpha, float beta, float* ws, int64_t ws_elems, cudaStream_t st);
 int64_t sgemm_ws_elems(int64_t m, int64_t n, int64_t k);
-int split16(const float* src, int64_t rows, int64_t cols, int64_t lds, uint16_t* hi, uint16_t* lo, int64_t ld,
-            bool bf16, float scale, cudaStream_t st);
+int split16(const float* src, int64_t k, int64_t rows, int64_t lds, uint16_t* hi, uint16_t* lo, bool bf16,
+            float scale, cudaStream_t st);
+int64_t blk16_elems(int64_t k, int64_t rows);
 int ctx_sync(sid_ctx* c, cudaStream_t st);
 
 struct NnlsCounters {
@@ -55,7 +56,7 @@ enum { SOLVER_LS = 0, SOLVER_FAST = 1 };
 struct ColBufs {
     double *x, *df;      // K x F FP64 iterate and gradient
     float* v;            // K x F FP32 operand of the next contraction (SIMT path)
-    uint16_t *vhi, *vlo; // ld16 x F BF16 split operand (tensor-core path)
+    uint16_t *vhi, *vlo; // K x F BF16 split operand, K-blocked (tensor-core path)
     float* g;            // K x F contraction result
     double* test;        // sample x F window of step statistics
     double *s1, *fit, *anyp, *xmax;  // per column
@@ -63,53 +64,19 @@ struct ColBufs {
     float *u, *gu;       // use_std: column-sum vector and G * it
     int* active;
     NnlsCounters* cnt;
-    int64_t ld16;
+    int F;
 };
-
-__device__ __forceinline__ double block_sum_d(double v, double* red)
-{
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
-    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-    __syncthreads();
-    if (l == 0) red[w] = v;
-    __syncthreads();
-    if (threadIdx.x < 32) {
-        double s = (l < (int)(blockDim.x >> 5)) ? red[l] : 0.0;
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
-        if (l == 0) red[0] = s;
-    }
-    __syncthreads();
-    return red[0];
-}
-
-__device__ __forceinline__ double block_max_d(double v, double* red)
-{
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, off));
-    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-    __syncthreads();
-    if (l == 0) red[w] = v;
-    __syncthreads();
-    if (threadIdx.x < 32) {
-        double s = (l < (int)(blockDim.x >> 5)) ? red[l] : -INFINITY;
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1) s = fmax(s, __shfl_xor_sync(0xffffffffu, s, off));
-        if (l == 0) red[0] = s;
-    }
-    __syncthreads();
-    return red[0];
-}
 
 // write the next contraction operand: FP32 copy or BF16 hi/lo split
 __device__ __forceinline__ void put_operand(const ColBufs& b, int64_t o, int j, int k, double val)
 {
     if (b.vhi) {
+        // K-blocked layout of the tensor-core GEMM: ((k/64)*F + j)*64 + k%64
+        const int64_t i = (((int64_t)(k >> 6) * b.F + j) << 6) + (k & 63);
         const float f = (float)val;
         const __nv_bfloat16 h = __float2bfloat16_rn(f);
-        b.vhi[(int64_t)j * b.ld16 + k] = __bfloat16_as_ushort(h);
-        b.vlo[(int64_t)j * b.ld16 + k] = __bfloat16_as_ushort(__float2bfloat16_rn(f - __bfloat162float(h)));
+        b.vhi[i] = __bfloat16_as_ushort(h);
+        b.vlo[i] = __bfloat16_as_ushort(__float2bfloat16_rn(f - __bfloat162float(h)));
     } else {
         b.v[o + k] = (float)val;
     }
@@ -117,15 +84,33 @@ __device__ __forceinline__ void put_operand(const ColBufs& b, int64_t o, int j, 
 
 __global__ void k_iter_inc(NnlsCounters* c) { c->iter += 1; }
 
-// passive / masked gradient (LS_nnls.m:120-121, fast_nnls.m:100,163)
-__global__ void k_nn_mask(ColBufs b, int K)
+__device__ __forceinline__ double warp_sum_d(double v)
 {
-    __shared__ double red[32];
-    const int j = blockIdx.x;
-    if (!b.active[j]) return;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    return v;
+}
+
+__device__ __forceinline__ double warp_max_d(double v)
+{
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, off));
+    return v;
+}
+
+// Column kernels: one warp per frame column (8 columns per 256-thread CTA),
+// lanes stride over the K components, warp-shuffle reductions.
+constexpr int kColsPerCta = 8;
+
+// passive / masked gradient (LS_nnls.m:120-121, fast_nnls.m:100,163)
+__global__ void __launch_bounds__(256) k_nn_mask(ColBufs b, int K, int F)
+{
+    const int j = blockIdx.x * kColsPerCta + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (j >= F || !b.active[j]) return;
     const int64_t o = (int64_t)j * K;
     double acc = 0.0, np = 0.0, mx = -INFINITY;
-    for (int k = threadIdx.x; k < K; k += blockDim.x) {
+    for (int k = lane; k < K; k += 32) {
         const double xv = b.x[o + k], dv = b.df[o + k];
         const bool p = xv > 0.0 || dv < 0.0;
         const double dm = p ? dv : 0.0;
@@ -134,10 +119,10 @@ __global__ void k_nn_mask(ColBufs b, int K)
         np += p ? 1.0 : 0.0;
         mx = fmax(mx, xv);
     }
-    acc = block_sum_d(acc, red);
-    np = block_sum_d(np, red);
-    mx = block_max_d(mx, red);
-    if (threadIdx.x == 0) {
+    acc = warp_sum_d(acc);
+    np = warp_sum_d(np);
+    mx = warp_max_d(mx);
+    if (lane == 0) {
         b.s1[j] = acc;
         b.anyp[j] = np;
         b.xmax[j] = mx;
@@ -146,25 +131,26 @@ __global__ void k_nn_mask(ColBufs b, int K)
 
 // exact line search, clamp, step statistic (LS_nnls.m:122-142, fast_nnls.m:119-145).
 // `gu` (use_std) holds G * (column sum of d) / F, subtracted from G d.
-__global__ void k_nn_step(ColBufs b, int K, int F, int solver, int sample, int tol_p, int use_std)
+__global__ void __launch_bounds__(256) k_nn_step(ColBufs b, int K, int F, int solver, int sample, int tol_p,
+                                                 int use_std)
 {
-    __shared__ double red[32];
-    const int j = blockIdx.x;
-    if (!b.active[j]) return;
+    const int j = blockIdx.x * kColsPerCta + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (j >= F || !b.active[j]) return;
     const int64_t o = (int64_t)j * K;
     double s2 = 0.0;
-    for (int k = threadIdx.x; k < K; k += blockDim.x) {
+    for (int k = lane; k < K; k += 32) {
         const double xv = b.x[o + k], dv = b.df[o + k];
         const double dm = (xv > 0.0 || dv < 0.0) ? dv : 0.0;
         double g = (double)b.g[o + k];
         if (use_std) g -= (double)b.gu[k];
         s2 += dm * g;
     }
-    s2 = block_sum_d(s2, red);
+    s2 = warp_sum_d(s2);
     double alpha = b.s1[j] / s2;
     if (isnan(alpha)) alpha = 0.0;
     double a1 = 0.0, a2 = 0.0;
-    for (int k = threadIdx.x; k < K; k += blockDim.x) {
+    for (int k = lane; k < K; k += 32) {
         const double xv = b.x[o + k], dv = b.df[o + k];
         const double dm = (xv > 0.0 || dv < 0.0) ? dv : 0.0;
         double xn = xv - dm * alpha;
@@ -173,16 +159,16 @@ __global__ void k_nn_step(ColBufs b, int K, int F, int solver, int sample, int t
         b.x[o + k] = xn;
         put_operand(b, o, j, k, stp);
         if (solver == SOLVER_LS) {
-            a1 += stp;            // sum(x - x_)
-            a2 += xv * xv;        // sum(x_.^2)
+            a1 += stp;      // sum(x - x_)
+            a2 += xv * xv;  // sum(x_.^2)
         } else {
             a1 += (tol_p == 2) ? stp * stp : fabs(stp);
         }
     }
-    a1 = block_sum_d(a1, red);
-    a2 = block_sum_d(a2, red);
+    a1 = warp_sum_d(a1);
+    a2 = warp_sum_d(a2);
     const int it = b.cnt->iter;
-    if (threadIdx.x == 0 && (it & 1)) {
+    if (lane == 0 && (it & 1)) {
         double t;
         int e;
         if (solver == SOLVER_LS) {
@@ -196,16 +182,16 @@ __global__ void k_nn_step(ColBufs b, int K, int F, int solver, int sample, int t
     }
 }
 
-// df = df + G step  (fast_nnls.m:153)
-__global__ void k_nn_update(ColBufs b, int K, int use_std)
+// df = df + G step  (fast_nnls.m:153), active columns only
+__global__ void k_nn_update(ColBufs b, int K, int F, int use_std)
 {
-    const int j = blockIdx.x;
-    if (!b.active[j]) return;
-    const int64_t o = (int64_t)j * K;
-    for (int k = threadIdx.x; k < K; k += blockDim.x) {
-        double g = (double)b.g[o + k];
-        if (use_std) g -= (double)b.gu[k];
-        b.df[o + k] += g;
+    const int64_t n = (int64_t)K * F;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t j = i / K;
+        if (!b.active[j]) continue;
+        double g = (double)b.g[i];
+        if (use_std) g -= (double)b.gu[i - j * K];
+        b.df[i] += g;
     }
 }
 
@@ -333,7 +319,7 @@ __global__ void k_colsum_operand(ColBufs b, int K, int F)
         for (int j = 0; j < F; ++j) {
             if (!b.active[j]) continue;
             if (b.vhi) {
-                const int64_t i = (int64_t)j * b.ld16 + k;
+                const int64_t i = (((int64_t)(k >> 6) * b.F + j) << 6) + (k & 63);
                 s += (double)__bfloat162float(__ushort_as_bfloat16(b.vhi[i])) +
                      (double)__bfloat162float(__ushort_as_bfloat16(b.vlo[i]));
             } else {
@@ -413,10 +399,9 @@ struct NnlsWork {
     bool split;
 };
 
-static int alloc_work(sid_ctx* c, int64_t K, int64_t F, int sample, bool split, NnlsWork* w)
+static int alloc_work(sid_ctx* c, int64_t K, int64_t F, int sample, bool split, NnlsWork* w, cudaStream_t st)
 {
     const int64_t KF = K * F;
-    const int64_t ld16 = cdiv(K, 8) * 8;
     DBuf* nn = c->nn;
     SID_TRY(nn[0].alloc(KF * 8));  // x
     SID_TRY(nn[1].alloc(KF * 8));  // df
@@ -428,10 +413,13 @@ static int alloc_work(sid_ctx* c, int64_t K, int64_t F, int sample, bool split, 
     SID_TRY(nn[7].alloc((size_t)(K * K + 3 * K + 16) * 4));
     SID_TRY(nn[10].alloc(KF * 4));  // h
     if (split) {
-        SID_TRY(nn[8].alloc((size_t)ld16 * F * 2));
-        SID_TRY(nn[9].alloc((size_t)ld16 * F * 2));
-        SID_TRY(nn[11].alloc((size_t)ld16 * K * 2));
-        SID_TRY(nn[12].alloc((size_t)ld16 * K * 2));
+        SID_TRY(nn[8].alloc((size_t)blk16_elems(K, F) * 2));
+        SID_TRY(nn[9].alloc((size_t)blk16_elems(K, F) * 2));
+        SID_TRY(nn[11].alloc((size_t)blk16_elems(K, K) * 2));
+        SID_TRY(nn[12].alloc((size_t)blk16_elems(K, K) * 2));
+        // zero the K-blocked operands once: entries past K in the last block stay zero
+        SID_CUDA_TRY(cudaMemsetAsync(nn[8].p, 0, (size_t)blk16_elems(K, F) * 2, st));
+        SID_CUDA_TRY(cudaMemsetAsync(nn[9].p, 0, (size_t)blk16_elems(K, F) * 2, st));
     }
     ColBufs& b = w->b;
     b.x = nn[0].as<double>();
@@ -453,7 +441,7 @@ static int alloc_work(sid_ctx* c, int64_t K, int64_t F, int sample, bool split, 
     b.u = w->hs + K;
     b.gu = b.u + K;
     w->h = nn[10].as<float>();
-    b.ld16 = ld16;
+    b.F = (int)F;
     b.vhi = split ? nn[8].as<uint16_t>() : nullptr;
     b.vlo = split ? nn[9].as<uint16_t>() : nullptr;
     w->Ghi = split ? nn[11].as<uint16_t>() : nullptr;
@@ -472,8 +460,8 @@ static int gmul(sid_ctx* c, const NnlsWork& w, int64_t K, int64_t F, cudaStream_
     const void* Bs[3] = {w.b.vhi, w.b.vlo, w.b.vhi};
     int bn = 0, sk = 0;
     gemm_autotune((int)K, (int)F, (int)cdiv(K, 64), &bn, &sk);
-    return gemm_tn(As, Bs, 3, K, F, K, w.b.ld16, w.b.ld16, true, w.b.g, K, 1.f, 0.f, bn, sk, c->ws.as<float>(),
-                   (int64_t)(c->ws.bytes / 4), c->errflag.as<int>(), st);
+    return gemm_tn(As, Bs, 3, K, F, K, true, w.b.g, K, 1.f, 0.f, bn, sk, c->ws.as<float>(), (int64_t)(c->ws.bytes / 4),
+                   c->errflag.as<int>(), st);
 }
 
 static int ensure_gemm_ws(sid_ctx* c, int64_t K, int64_t F, bool split)
@@ -589,13 +577,14 @@ static int iterate(sid_ctx* c, NnlsWork& w, int64_t K, int64_t F, int solver, co
     auto body = [&](cudaStream_t s) -> int {
         k_iter_inc<<<1, 1, 0, s>>>(b.cnt);
         SID_CHECK_LAUNCH();
-        k_nn_mask<<<(unsigned)F, 256, 0, s>>>(b, (int)K);
+        k_nn_mask<<<(unsigned)cdiv(F, kColsPerCta), 256, 0, s>>>(b, (int)K, (int)F);
         SID_CHECK_LAUNCH();
         SID_TRY(gmul_std(s));
-        k_nn_step<<<(unsigned)F, 256, 0, s>>>(b, (int)K, (int)F, solver, sample, (int)o->tol_p, use_std);
+        k_nn_step<<<(unsigned)cdiv(F, kColsPerCta), 256, 0, s>>>(b, (int)K, (int)F, solver, sample, (int)o->tol_p,
+                                                                    use_std);
         SID_CHECK_LAUNCH();
         SID_TRY(gmul_std(s));
-        k_nn_update<<<(unsigned)F, 256, 0, s>>>(b, (int)K, use_std);
+        k_nn_update<<<2048, 256, 0, s>>>(b, (int)K, (int)F, use_std);
         SID_CHECK_LAUNCH();
         k_nn_fit<<<cdiv(F, 256), 256, 0, s>>>(b, (int)F, solver, sample, max_iter, use_std);
         SID_CHECK_LAUNCH();
@@ -651,7 +640,7 @@ extern "C" int sid_ls_nnls(sid_ctx* c, const float* A, const void* Y, int ydtype
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const bool split = prec == SID_PREC_SPLIT;
     NnlsWork w;
-    SID_TRY(alloc_work(c, K, F, (int)o->sample, split, &w));
+    SID_TRY(alloc_work(c, K, F, (int)o->sample, split, &w, st));
     ColBufs& b = w.b;
     const bool f16 = ydtype == SID_DTYPE_F16;
     // h = A'Y   (LS_nnls.m:76)
@@ -673,7 +662,7 @@ extern "C" int sid_ls_nnls(sid_ctx* c, const float* A, const void* Y, int ydtype
         SID_CUDA_TRY(cudaStreamSynchronize(st));
         ys.release();
     }
-    if (split) SID_TRY(split16(w.G, K, K, K, w.Ghi, w.Glo, b.ld16, true, 1.f, st));
+    if (split) SID_TRY(split16(w.G, K, K, K, w.Ghi, w.Glo, true, 1.f, st));
     // df = -h + G x0  (x0 = 0 unless given)
     k_df_init<<<1024, 256, 0, st>>>(w.h, nullptr, b.df, (int)K, K * F, o->lambda, SOLVER_LS);
     SID_CHECK_LAUNCH();
@@ -681,7 +670,7 @@ extern "C" int sid_ls_nnls(sid_ctx* c, const float* A, const void* Y, int ydtype
         k_x_from<<<1024, 256, 0, st>>>(b.x, X, nullptr, (int)K, K * F);
         SID_CHECK_LAUNCH();
         SID_TRY(ensure_gemm_ws(c, K, F, split));
-        if (split) SID_TRY(split16(X, K, F, K, b.vhi, b.vlo, b.ld16, true, 1.f, st));
+        if (split) SID_TRY(split16(X, K, F, K, b.vhi, b.vlo, true, 1.f, st));
         else SID_CUDA_TRY(cudaMemcpyAsync(b.v, X, (size_t)(K * F) * 4, cudaMemcpyDeviceToDevice, st));
         SID_TRY(gmul(c, w, K, F, st));
         if (o->use_std) {
@@ -694,7 +683,7 @@ extern "C" int sid_ls_nnls(sid_ctx* c, const float* A, const void* Y, int ydtype
                              (int64_t)(c->ws.bytes / 4), st));
             k_fill_int<<<64, 256, 0, st>>>(b.active, (int)F, 1);
             SID_CHECK_LAUNCH();
-            k_nn_update<<<(unsigned)F, 256, 0, st>>>(b, (int)K, 1);
+            k_nn_update<<<2048, 256, 0, st>>>(b, (int)K, (int)F, 1);
         } else {
             k_add_g<<<1024, 256, 0, st>>>(b.df, b.g, K * F);
         }
@@ -719,7 +708,7 @@ extern "C" int sid_fast_nnls(sid_ctx* c, const float* A, const void* Y, int ydty
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const bool split = prec == SID_PREC_SPLIT;
     NnlsWork w;
-    SID_TRY(alloc_work(c, K, F, (int)o->sample, split, &w));
+    SID_TRY(alloc_work(c, K, F, (int)o->sample, split, &w, st));
     ColBufs& b = w.b;
     const bool f16 = ydtype == SID_DTYPE_F16;
     // Q = A'A normalised, hs = 1./sqrt(diag), df = diag(hs)(-A'Y + lambda)   (fast_nnls.m:53-57)
@@ -731,7 +720,7 @@ extern "C" int sid_fast_nnls(sid_ctx* c, const float* A, const void* Y, int ydty
     SID_TRY(contract(c, A, Y, f16, K, F, P, P, P, w.h, K, 1.f, 0.f, f16 ? SID_PREC_SPLIT : prec, st));
     k_df_init<<<1024, 256, 0, st>>>(w.h, w.hs, b.df, (int)K, K * F, o->lambda, SOLVER_FAST);
     SID_CHECK_LAUNCH();
-    if (split) SID_TRY(split16(w.G, K, K, K, w.Ghi, w.Glo, b.ld16, true, 1.f, st));
+    if (split) SID_TRY(split16(w.G, K, K, K, w.Ghi, w.Glo, true, 1.f, st));
     if (warm_start) {
         // x = diag(1./hs) W; df = df + Q x   (fast_nnls.m:72-73)
         k_x_from<<<1024, 256, 0, st>>>(b.x, warm_start, w.hs, (int)K, K * F);
@@ -741,7 +730,7 @@ extern "C" int sid_fast_nnls(sid_ctx* c, const float* A, const void* Y, int ydty
         k_x_out<<<1024, 256, 0, st>>>(xf, b.x, nullptr, (int)K, K * F);
         SID_CHECK_LAUNCH();
         SID_TRY(ensure_gemm_ws(c, K, F, split));
-        if (split) SID_TRY(split16(xf, K, F, K, b.vhi, b.vlo, b.ld16, true, 1.f, st));
+        if (split) SID_TRY(split16(xf, K, F, K, b.vhi, b.vlo, true, 1.f, st));
         else SID_CUDA_TRY(cudaMemcpyAsync(b.v, xf, (size_t)(K * F) * 4, cudaMemcpyDeviceToDevice, st));
         SID_TRY(gmul(c, w, K, F, st));
         k_add_g<<<1024, 256, 0, st>>>(b.df, b.g, K * F);

@@ -38,6 +38,17 @@ def test_ls_nnls_matches_oracle(ctx, oracle, prec):
     ctx.sync()
     Xo, Go, ito = oracle.LS_nnls(A, Y, {"max_iter": 2000}, return_iters=True)
     assert rel_l2(Xg, Xo) < 1e-4, rel_l2(Xg, Xo)
+    # Columns retired early by the reference's convergence test must be
+    # converged.  (On this well-conditioned problem both runs reach FP64
+    # precision before the first test at iteration 601; the reference's
+    # recomputed gradient then only shows rounding noise, so which columns it
+    # retires is arbitrary, while the incremental FP64 gradient keeps shrinking
+    # and retires them at the first test.)
+    it = it.cpu().numpy()
+    early = it < 2001
+    if early.any():
+        viol, _ = kkt(A, Y[:, early], Xg[:, early])
+        assert viol < 1e-4, viol
     assert rel_l2(to_numpy(G), Go) < 1e-5
     viol, mn = kkt(A, Y, Xg)
     assert mn >= 0 and viol < 1e-4, viol
@@ -47,10 +58,13 @@ def test_ls_nnls_matches_oracle(ctx, oracle, prec):
 def test_fast_nnls_matches_oracle(ctx, oracle, prec):
     from sid_gb300 import to_numpy
     A, Y, _ = problem(1200, 30, 80, 2)
-    Xg, Q = ctx.fast_nnls(A, Y, {}, prec=prec)
+    Xg, Q, it = ctx.fast_nnls(A, Y, {}, prec=prec, return_iters=True)
     Xg = to_numpy(Xg)
     ctx.sync()
-    Xo, Qo, _, _ = oracle.fast_nnls(A, Y, {})
+    Xo, Qo, _, _, ito = oracle.fast_nnls(A, Y, {}, return_iters=True)
+    it = it.cpu().numpy()
+    assert abs(np.mean(it < 2001) - np.mean(ito < 2001)) <= 0.1, (np.mean(it < 2001), np.mean(ito < 2001))
+    assert abs(np.median(it) - np.median(ito)) <= 0.2 * np.median(ito) + 4, (np.median(it), np.median(ito))
     assert rel_l2(to_numpy(Q), Qo) < 1e-5
     assert rel_l2(Xg, Xo) < 1e-3, rel_l2(Xg, Xo)
     viol, mn = kkt(A, Y, Xg)
