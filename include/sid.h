@@ -198,6 +198,86 @@ int sid_spatial_update(sid_ctx* ctx, const float* T, const void* Y, int ydtype, 
                        int64_t F, int64_t P, double lamb_L1, double lamb_L2, double lamb_orth_L1, int use_std,
                        int bg_sub, float* forward_model, int32_t* status, void* stream);
 
+/* ---- Quantiles and component reconstruction ---------------------------------
+ * MATLAB quantile of a vector (sorted non-NaN data at probabilities
+ * (k - 0.5)/n, linear interpolation, clamped to the extremes; NaN when no
+ * value is left): out[i] = quantile(x(exclude == 0), p[i]) for np <= 64
+ * probabilities.  x: n single (device); exclude: n uint8 (device) or NULL;
+ * out: HOST doubles.  Synchronises the stream.  (reconstruct_S.m:132,137,169,193) */
+int sid_quantile(sid_ctx* ctx, const float* x, int64_t n, const uint8_t* exclude, const double* p, int np,
+                 double* out, void* stream);
+
+typedef struct {
+    double q;       /* background quantile of the non-microlens pixels (0.8) */
+    double lamb_L1; /* L1 weight, capped by the (1 - 1e-4) quantile of Htf (0) */
+    double lamb_L2; /* L2 weight (0) */
+    int solver;     /* 0 = 'fast_nnls' (LS_deconv, the default), 1 = 'ISRA' (deconvRL) */
+    int max_iter;   /* iterations of the solver (8) */
+} sid_recon_opts;
+void sid_recon_defaults(sid_recon_opts* opts); /* reconstruct_S.m:47-95 */
+/* recon_nnmf{ii} for one component image (reconstruct_S.m:130-148, 168-205):
+ * background clip at quantile q of the pixels with microlenses == 0, divide
+ * by the maximum, back-project img/||img||, cap lamb_L1, solve, scale by
+ * ||img||.  img: X x Y single, microlenses: X x Y uint8 or NULL, X: X x Y x Z
+ * single output (all device).  lamb_used (optional, host): the capped lamb_L1.
+ * Reads the capped weight back to the host (one stream synchronisation). */
+int sid_reconstruct_component(sid_plan* plan, int method, const float* img, const uint8_t* microlenses,
+                              const sid_recon_opts* opts, float* X, double* lamb_used, void* stream);
+
+/* ---- NMF steps (fast_NMF.m:185-186) ------------------------------------------
+ * One projected-gradient step with exact line search on T or on S for
+ * Y ~ S*T.  Y: P x F single or half (ydtype); S: P x R single; T: R x F
+ * single; all device arrays, updated in place (NaNs zeroed first, as the
+ * reference does).  Options mirror the reference's opts fields; zero = off. */
+typedef struct {
+    double lamb_temp;    /* T_update: L1 weight on T */
+    double lamb_corr;    /* T_update: correlation penalty (rows of T renormalised, S rescaled) */
+    double lamb_temp_TV; /* T_update: temporal total variation, [-1 2 -1] */
+    double lamb_spat;    /* S_update: L1 weight on S */
+    double lamb_spat_TV; /* S_update: must be 0 (the reference's term calls an undefined 'laplace') */
+    double lamb_orth_L1; /* S_update: Q_T += lamb_orth_L1 * hilf; S columns renormalised */
+    double lamb_orth_L2; /* S_update: L2 orthogonality (step floored at 1e-6) */
+    int use_std;         /* both: least standard deviation (needs ymean = opts.Y) */
+    int pointwise;       /* both: one step per frame (T) / per pixel (S) */
+} sid_nmf_opts;
+void sid_nmf_defaults(sid_nmf_opts* opts);
+
+/* [S, T] = T_update(Y, T, S, opts)   T_update.m:1
+ * active: P uint8 (opts.active; NULL = every pixel); ymean: P single (opts.Y,
+ * read with use_std).  S is written too: NaNs zeroed and, with lamb_corr > 0,
+ * its columns rescaled by the norms of T's rows.  prec: precision of S'S and
+ * S'Y (an FP16 movie always uses SID_PREC_SPLIT). */
+int sid_t_update(sid_ctx* ctx, const void* Y, int ydtype, float* T, float* S, int64_t P, int64_t R, int64_t F,
+                 const uint8_t* active, const float* ymean, const sid_nmf_opts* opts, int prec, void* stream);
+/* [S, T] = S_update(Y, S, T, opts)   S_update.m:1
+ * ymean: P single (opts.Y, use_std); hilf: R x R single (opts.hilf, read when
+ * an orthogonality weight is set).  T is written too: NaNs zeroed and, with an
+ * orthogonality weight, its rows rescaled by the norms of S's columns.
+ * prec: precision of S'S (L2 orthogonality); Y*T' is FP32 SIMT. */
+int sid_s_update(sid_ctx* ctx, const void* Y, int ydtype, float* S, float* T, int64_t P, int64_t R, int64_t F,
+                 const float* ymean, const float* hilf, const sid_nmf_opts* opts, int prec, void* stream);
+
+/* ---- Timeseries extraction (incremental_temporal_update_gpu.m:76-100) ----------
+ * Least-squares branch: Q = inv(F*F')*F once (:83-84), then T = Q*(Y ./ b) for
+ * each chunk of frames (:66-68, 89, 99).  The handle keeps a pixel-major copy
+ * of F and inv(F*F') in FP64 (blocked Cholesky, then inverse); a chunk costs
+ * the contraction F*Y and the FP64 product inv(F*F')*(F*Y), the reference's
+ * product re-associated so that the K x P matrix Q is never formed.  The
+ * non-negative branch (opts.non_neg_on) is sid_ls_nnls. */
+typedef struct sid_pinv sid_pinv;
+/* F: K x P single (layout 0, the reference's forward_model) or P x K
+ * (layout 1, the library's pixel-major columns), device.  prec: precision of
+ * F*F' and F*Y (SID_PREC_FP32 or SID_PREC_SPLIT).  Synchronises the stream;
+ * SID_EINVAL when F*F' is not positive definite.  The handle uses ctx for
+ * its contractions: keep ctx alive and do not use it on another stream meanwhile. */
+int sid_pinv_create(sid_ctx* ctx, const float* F, int64_t K, int64_t P, int layout, int prec, sid_pinv** out,
+                    void* stream);
+/* T (K x n, leading dimension ldt) = Q * (Y ./ baseline): Y P x n single or
+ * half (ydtype); baseline: n single per-frame divisors, or NULL. */
+int sid_pinv_apply(sid_pinv* q, const void* Y, int ydtype, int64_t n, const float* baseline, float* T, int64_t ldt,
+                   void* stream);
+int sid_pinv_destroy(sid_pinv* q);
+
 /* ---- Allocation-free Gram product ---------------------------------------------
  * No counterpart in the reference: an addition for callers that cannot let a
  * library allocate device memory (a MEX function whose memory belongs to

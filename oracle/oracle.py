@@ -145,10 +145,14 @@ def baseline_forward_f32(H, V, y_begin=0, y_end=None, nthreads=0):
 # MATLAB helpers restated
 # ----------------------------------------------------------------------------
 def matlab_quantile(v, p):
-    """MATLAB quantile of a vector: sorted data at positions (k-0.5)/n with
-    linear interpolation, clamped to the extremes (NumPy's 'hazen' rule)."""
-    v = np.sort(np.asarray(v, dtype=np.float64).ravel())
+    """MATLAB quantile of a vector: NaNs dropped, sorted data at positions
+    (k-0.5)/n with linear interpolation, clamped to the extremes (NumPy's
+    'hazen' rule); NaN when no value is left."""
+    v = np.asarray(v, dtype=np.float64).ravel()
+    v = np.sort(v[~np.isnan(v)])
     n = v.size
+    if n == 0:
+        return np.nan
     t = n * p + 0.5  # 1-based fractional position
     if t <= 1:
         return v[0]
@@ -279,10 +283,11 @@ def LS_deconv(forward, backward, df, opts=None):
 
 
 def reconstruct_S_one(img, forward, backward, opts=None, microlenses=None):
-    """One component of reconstruct_S.m:130-148 (CPU branch): background clip
-    at quantile q of the non-microlens pixels, normalise by max then by the
-    L2 norm, back-project, cap lamb_L1 by the (1-1e-4) quantile of Htf,
-    solve, rescale by the norm."""
+    """One component of reconstruct_S (GPU branch, reconstruct_S.m:168-205;
+    the CPU branch :130-148 computes the same): background clip at quantile q
+    of the non-microlens pixels, normalise by max then by the L2 norm,
+    back-project, cap lamb_L1 by the (1-1e-4) quantile of Htf, solve with
+    max_iter iterations, rescale by the norm."""
     opts = dict(opts or {})
     q = opts.get("q", 0.8)
     img = np.asarray(img, dtype=np.float64)
@@ -294,7 +299,7 @@ def reconstruct_S_one(img, forward, backward, opts=None, microlenses=None):
     opts["lamb_L1"] = min(matlab_quantile(Htf, 1 - 1e-4), opts.get("lamb_L1", 0.0))
     solver = opts.get("whichSolver", "fast_nnls")
     if solver == "ISRA":
-        X = deconvRL(forward, backward, Htf, opts.get("maxIter", 8), Htf, opts)
+        X = deconvRL(forward, backward, Htf, opts.get("max_iter", 8), Htf, opts)
     elif solver == "fast_nnls":
         X = LS_deconv(forward, backward, Htf, opts)
     else:
@@ -629,7 +634,7 @@ def S_update(Y, S, T, opts):
         else:
             alpha = np.array(np.sum(v * df) / np.sum(v * (v @ Q_T)))
             if l2o != 0:
-                alpha = np.maximum(alpha, 1e-6)
+                alpha = np.fmax(alpha, 1e-6)  # MATLAB max ignores NaN (S_update.m:63)
     alpha = np.where(np.isfinite(alpha), alpha, 0.0)
     S = S - alpha * v
     S[S < 0] = 0.0

@@ -5,7 +5,9 @@ The compute lives in ``libsid.so`` (hand-written CUDA behind the C ABI of
 top of it.  Import does not require a GPU; calling the operators does.
 """
 from ._lib import SidError  # noqa: F401
-from .nnls import Context, LS_nnls, fast_nnls, update_spatial_component  # noqa: F401
+from .nnls import Context, LS_nnls, fast_nnls, quantile, update_spatial_component  # noqa: F401
+from .nmf import S_update, T_update  # noqa: F401
+from .extract import Extractor, incremental_temporal_update_gpu  # noqa: F401
 from .lfm import (  # noqa: F401
     LS_deconv,
     Projector,
@@ -16,6 +18,7 @@ from .lfm import (  # noqa: F401
     forwardProjectGPU,
     generate_LFM_library_GPU,
     library_boxes,
+    reconstruct_S,
     set_default_method,
     to_device,
     to_numpy,

@@ -69,11 +69,21 @@ SIGNATURES = {
     "sid_library": [P, P, I64, P, P, I64, I64, F64, P, I32, P],
     "sid_library_boxes": [P, I64, I64, F64, I64, I64, I64, P],
     "sid_spatial_update": [P, P, P, I32, P, I64, I64, I64, F64, F64, F64, I32, I32, P, P, P],
+    "sid_nmf_defaults": [P],
+    "sid_t_update": [P, P, I32, P, P, I64, I64, I64, P, P, P, I32, P],
+    "sid_s_update": [P, P, I32, P, P, I64, I64, I64, P, P, P, I32, P],
+    "sid_pinv_create": [P, P, I64, I64, I32, I32, PP, P],
+    "sid_pinv_apply": [P, P, I32, I64, P, P, I64, P],
+    "sid_pinv_destroy": [P],
+    "sid_quantile": [P, P, I64, P, P, I32, P, P],
+    "sid_recon_defaults": [P],
+    "sid_reconstruct_component": [P, I32, P, P, P, P, P, P],
 }
 PREC = {"fp32": 0, "split": 1, "bf16": 2}
 DTYPE_F32, DTYPE_F16 = 0, 1
 _RESTYPES = {"sid_last_error": ctypes.c_char_p, "sid_ls_nnls_defaults": None,
-             "sid_fast_nnls_defaults": None}
+             "sid_fast_nnls_defaults": None, "sid_nmf_defaults": None,
+             "sid_recon_defaults": None}
 
 _lib = None
 

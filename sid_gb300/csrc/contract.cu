@@ -133,6 +133,7 @@ extern "C" int sid_ctx_destroy(sid_ctx* c)
     DBuf* b[] = {&c->a_hi, &c->a_lo, &c->b_hi, &c->b_lo, &c->ws, &c->scal, &c->errflag};
     for (DBuf* x : b) x->release();
     for (DBuf& x : c->nn) x.release();
+    for (DBuf& x : c->mf) x.release();
     delete c;
     return SID_OK;
 }

@@ -1,0 +1,683 @@
+// nmf.cu -- the two projected-gradient steps of the SID matrix factorisation
+// Y ~ S*T (fast_NMF.m:185-186): T_update.m:1-78 and S_update.m:1-80.
+//
+// Shapes (MATLAB column-major): Y P x F (movie, FP32 or FP16), S P x R
+// (spatial components), T R x F (timeseries).  Each step is one gradient
+// evaluation, a projection onto the non-negativity constraint, an exact line
+// search and a clamped update.  The pixel-long contractions (S'S, S'Y) run
+// through the tensor-core contraction at the requested precision; the frame-
+// and rank-long products (R x R and R x F, or P x R with an R-deep
+// reduction) run on the FP32 SIMT GEMMs; every reduction of the line search
+// accumulates in FP64.  Nothing is copied to the host: the step sizes stay in
+// device memory, so a step is stream-ordered and graph-capturable.
+#include <cmath>
+#include <cstring>
+
+#include "sid_internal.cuh"
+
+namespace sid {
+
+int contract(sid_ctx* c, const float* A, const void* B, bool b_f16, int64_t m, int64_t n, int64_t k, int64_t lda,
+             int64_t ldb, float* C, int64_t ldc, float alpha, float beta, int prec, cudaStream_t st);
+int sgemm_nt(const void* A, int a_f16, const float* B, int64_t m, int64_t n, int64_t k, int64_t lda, int64_t ldb,
+             float* C, int64_t ldc, cudaStream_t st);
+
+namespace {
+
+constexpr int kRedBlocks = 1024;  // partial-sum slots of the global reductions
+
+__device__ __forceinline__ double warp_sum(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__device__ __forceinline__ float finite_or_zero(double a) { return isfinite(a) ? (float)a : 0.f; }
+
+__global__ void k_nan_zero(float* __restrict__ x, int64_t n)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        if (isnan(x[i])) x[i] = 0.f;
+}
+
+// out (cols x rows) = in' for in (rows x cols), both column-major; 32 x 32 tiles
+__global__ void k_transpose_tile(const float* __restrict__ in, int64_t rows, int64_t cols, float* __restrict__ out)
+{
+    __shared__ float tile[32][33];
+    const int64_t r0 = (int64_t)blockIdx.x * 32, c0 = (int64_t)blockIdx.y * 32;
+    for (int j = threadIdx.y; j < 32; j += blockDim.y) {
+        const int64_t r = r0 + threadIdx.x, c = c0 + j;
+        if (r < rows && c < cols) tile[j][threadIdx.x] = in[r + rows * c];
+    }
+    __syncthreads();
+    for (int j = threadIdx.y; j < 32; j += blockDim.y) {
+        const int64_t c = c0 + threadIdx.x, r = r0 + j;
+        if (r < rows && c < cols) out[c + cols * r] = tile[threadIdx.x][j];
+    }
+}
+
+int transpose(const float* in, int64_t rows, int64_t cols, float* out, cudaStream_t st)
+{
+    SID_REQUIRE(cdiv(cols, 32) <= 65535, "transpose: too many columns");
+    dim3 grid((unsigned)cdiv(rows, 32), (unsigned)cdiv(cols, 32)), block(32, 8);
+    k_transpose_tile<<<grid, block, 0, st>>>(in, rows, cols, out);
+    SID_CHECK_LAUNCH();
+    return SID_OK;
+}
+
+// Per row r of an R x F matrix: sum and sum of squares over the F columns
+// (one warp per row).
+__global__ void k_row_moments(const float* __restrict__ T, int R, int64_t F, double* __restrict__ s1,
+                              double* __restrict__ s2)
+{
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (warp >= R) return;
+    double a = 0.0, b = 0.0;
+    for (int64_t f = lane; f < F; f += 32) {
+        const double v = T[warp + (int64_t)R * f];
+        a += v;
+        b += v * v;
+    }
+    a = warp_sum(a);
+    b = warp_sum(b);
+    if (lane == 0) {
+        s1[warp] = a;
+        if (s2) s2[warp] = b;
+    }
+}
+
+// sd(r) = std(T(r, :)) with N-1 normalisation (two passes; 0 for one frame)
+__global__ void k_row_std(const float* __restrict__ T, int R, int64_t F, double* __restrict__ sd)
+{
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (warp >= R) return;
+    double a = 0.0;
+    for (int64_t f = lane; f < F; f += 32) a += T[warp + (int64_t)R * f];
+    const double mu = warp_sum(a) / (double)F;
+    double b = 0.0;
+    for (int64_t f = lane; f < F; f += 32) {
+        const double d = T[warp + (int64_t)R * f] - mu;
+        b += d * d;
+    }
+    b = warp_sum(b);
+    if (lane == 0) sd[warp] = F > 1 ? sqrt(b / (double)(F - 1)) : 0.0;
+}
+
+// T(r, :) /= platz(r), S(:, r) *= platz(r) with platz = ||T(r, :)||  (T_update.m:14-19)
+__global__ void k_renorm_rows(float* __restrict__ T, int R, int64_t F, float* __restrict__ S, int64_t P,
+                              const double* __restrict__ sq)
+{
+    const int64_t nT = (int64_t)R * F, nS = P * R;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nT + nS;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        if (i < nT) {
+            const float pl = (float)sqrt(sq[i % R]);
+            T[i] = T[i] / pl;
+        } else {
+            const int64_t j = i - nT;
+            const float pl = (float)sqrt(sq[j / P]);
+            S[j] = S[j] * pl;
+        }
+    }
+}
+
+// Sm(p, r) = active(p) ? S(p, r) : 0  (S(opts.active, :), T_update.m:24-25)
+__global__ void k_mask_rows(const float* __restrict__ S, const uint8_t* __restrict__ active, int64_t P, int64_t R,
+                            float* __restrict__ Sm)
+{
+    const int64_t n = P * R;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        Sm[i] = active[i % P] ? S[i] : 0.f;
+}
+
+// out(r, f) = v(r, f) - rowsum(r) / F: the use_std centring inside Q(x)
+// (T_update.m:29: Q_S*x - Q_S*sum(x,2)/F = Q_S*(x - sum(x,2)/F))
+__global__ void k_centre_rows(const float* __restrict__ v, const double* __restrict__ rs, int R, int64_t F,
+                              float* __restrict__ out)
+{
+    const int64_t n = (int64_t)R * F;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = (float)((double)v[i] - rs[i % R] / (double)F);
+}
+
+// zscore along the first dimension of an n1 x n2 matrix (MATLAB zscore: N-1
+// normalisation, zero deviation replaced by 1), one warp per column.
+__global__ void k_zscore_cols(const float* __restrict__ T, int64_t n1, int64_t n2, float* __restrict__ z)
+{
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (warp >= n2) return;
+    const float* col = T + n1 * warp;
+    double a = 0.0;
+    for (int64_t i = lane; i < n1; i += 32) a += col[i];
+    const double mu = warp_sum(a) / (double)n1;
+    double b = 0.0;
+    for (int64_t i = lane; i < n1; i += 32) {
+        const double d = col[i] - mu;
+        b += d * d;
+    }
+    b = warp_sum(b);
+    double sd = n1 > 1 ? sqrt(b / (double)(n1 - 1)) : 0.0;
+    if (sd == 0.0) sd = 1.0;
+    for (int64_t i = lane; i < n1; i += 32) z[n1 * warp + i] = (float)((col[i] - mu) / sd);
+}
+
+// Correlation-penalty row terms (T_update.m:40-41): with H1 = C1*zsc - zsc,
+// rs(r) = sum_f H1(r, f) and dg(r) = sum_f H1(r, f) zsc(r, f).
+__global__ void k_corr_rows(const float* __restrict__ C1z, const float* __restrict__ zsc, int R, int64_t F,
+                            double* __restrict__ rs, double* __restrict__ dg)
+{
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (warp >= R) return;
+    double a = 0.0, b = 0.0;
+    for (int64_t f = lane; f < F; f += 32) {
+        const int64_t i = warp + (int64_t)R * f;
+        const double h = (double)C1z[i] - (double)zsc[i];
+        a += h;
+        b += h * (double)zsc[i];
+    }
+    a = warp_sum(a);
+    b = warp_sum(b);
+    if (lane == 0) {
+        rs[warp] = a;
+        dg[warp] = b;
+    }
+}
+
+struct TGrad {
+    const float* qT;   // S_a' Y_a  (R x F)
+    const float* QT;   // Q(T)      (R x F)
+    const float* T;
+    const float* zsc;  // lamb_corr terms (or null)
+    const float* C1z;
+    const double* rs;
+    const double* dg;
+    const double* sd;  // d = std(T, [], 2)
+    const double* wq;  // use_std: S_a' opts.Y(active) (R; divided by F here) or null
+    float* dT;         // out: the projected gradient df_T_
+    double lamb_temp, lamb_corr, lamb_tv;
+    int R;
+    int64_t F;
+};
+
+// df_T = -q_T + Q(T) + lamb_temp [+ lamb_corr hilf] [+ lamb_temp_TV tv]
+// (T_update.m:36-56), then df_T_ = passive .* df_T  (:59-60)
+__global__ void k_t_grad(TGrad g)
+{
+    const int64_t n = (int64_t)g.R * g.F;
+    const double Fd = (double)g.F;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int r = (int)(i % g.R);
+        const int64_t f = i / g.R;
+        double q = (double)g.qT[i];
+        if (g.wq) q -= g.wq[r] / Fd;
+        double df = -q + (double)g.QT[i] + g.lamb_temp;
+        if (g.zsc) {
+            const double h1 = (double)g.C1z[i] - (double)g.zsc[i];
+            const double hilf = (h1 - g.rs[r] / Fd - g.dg[r] * (double)g.zsc[i] / Fd) / g.sd[r];
+            df += g.lamb_corr * hilf;
+        }
+        if (g.lamb_tv != 0.0) {
+            // padded row p(0) = T(1), p(1..F) = T(0..F-1), p(F+1) = T(F-2); tv = -p(f) + 2p(f+1) - p(f+2)
+            const float* row = g.T + r;
+            const int64_t R = g.R;
+            const double left = f == 0 ? row[R * 1] : row[R * (f - 1)];
+            const double right = f == g.F - 1 ? row[R * (g.F - 2)] : row[R * (f + 1)];
+            df += g.lamb_tv * (-left + 2.0 * (double)row[R * f] - right);
+        }
+        const bool passive = g.T[i] > 0.f || df < 0.0;
+        g.dT[i] = passive ? (float)df : 0.f;
+    }
+}
+
+// Per column f of two R x F matrices: num(f) = sum_r a^2 (or a.b2), den(f) = sum_r a.b
+// (one warp per column; R contiguous)
+__global__ void k_col_dots(const float* __restrict__ a, const float* __restrict__ b2, const float* __restrict__ b,
+                           int R, int64_t F, double* __restrict__ num, double* __restrict__ den)
+{
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (warp >= F) return;
+    double x = 0.0, y = 0.0;
+    for (int r = lane; r < R; r += 32) {
+        const int64_t i = r + (int64_t)R * warp;
+        const double av = a[i];
+        x += av * (b2 ? (double)b2[i] : av);
+        y += av * (double)b[i];
+    }
+    x = warp_sum(x);
+    y = warp_sum(y);
+    if (lane == 0) {
+        num[warp] = x;
+        den[warp] = y;
+    }
+}
+
+// Step sizes from per-slot sums.  pointwise: alpha(i) = num(i) / den(i);
+// else alpha(0) = sum num / sum den, optionally max(alpha, floor) with MATLAB's
+// NaN-ignoring max.  NaN and Inf become 0 (T_update.m:68-69, S_update.m:59-67).
+__global__ void k_alpha(const double* __restrict__ num, const double* __restrict__ den, int64_t n, int pointwise,
+                        double floor_, float* __restrict__ alpha)
+{
+    if (pointwise) {
+        for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+            alpha[i] = finite_or_zero(num[i] / den[i]);
+        return;
+    }
+    if (blockIdx.x != 0) return;
+    __shared__ double sn[32], sd[32];
+    double x = 0.0, y = 0.0;
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+        x += num[i];
+        y += den[i];
+    }
+    x = warp_sum(x);
+    y = warp_sum(y);
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) {
+        sn[w] = x;
+        sd[w] = y;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = 0.0, b = 0.0;
+        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) {
+            a += sn[i];
+            b += sd[i];
+        }
+        double al = a / b;
+        if (floor_ > 0.0) al = isnan(al) ? floor_ : fmax(al, floor_);
+        alpha[0] = finite_or_zero(al);
+    }
+}
+
+// x = max(x - alpha .* d, 0); alpha per column of a rows x cols matrix
+// (per_col), per row (per_row) or one scalar.
+__global__ void k_pg_step(float* __restrict__ x, const float* __restrict__ d, int64_t rows, int64_t cols,
+                          const float* __restrict__ alpha, int mode)
+{
+    const int64_t n = rows * cols;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const float a = mode == 0 ? alpha[0] : (mode == 1 ? alpha[i / rows] : alpha[i % rows]);
+        const float v = x[i] - d[i] * a;
+        x[i] = v < 0.f ? 0.f : v;
+    }
+}
+
+// ---- S_update kernels ----
+
+// Q_T(i, j) += -ts(i) ts(j) / F (use_std) + l1o * hilf(i, j)   (S_update.m:14,20)
+__global__ void k_qt_adjust(float* __restrict__ QT, int R, const double* __restrict__ ts, double invF,
+                            const float* __restrict__ hilf, double l1o)
+{
+    const int64_t n = (int64_t)R * R;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double q = QT[i];
+        if (ts) q -= ts[i % R] * ts[i / R] * invF;
+        if (hilf) q += l1o * (double)hilf[i];
+        QT[i] = (float)q;
+    }
+}
+
+// df_S = -q_S [+ opts.Y .* ts' / F] + S*Q_T + lamb_spat  (S_update.m:8-34), in place of SQ
+__global__ void k_s_grad(const float* __restrict__ qS, float* __restrict__ SQ, int64_t P, int R,
+                         const float* __restrict__ ymean, const double* __restrict__ ts, double invF, double lamb_spat)
+{
+    const int64_t n = P * R;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double q = qS[i];
+        if (ymean) q -= (double)ymean[i % P] * ts[i / P] * invF;
+        SQ[i] = (float)(-q + (double)SQ[i] + lamb_spat);
+    }
+}
+
+// Direction of the S step (S_update.m:38-53), one thread per pixel:
+// orth:  v = df [+ l2o * M2]; z = sum_r S.*v; v = v - S.*z; v = passive(S, v) .* v
+// else:  v = passive(S, df) .* df
+__global__ void k_s_dir(const float* __restrict__ S, const float* __restrict__ df, const float* __restrict__ M2,
+                        double l2o, int orth, int64_t P, int R, float* __restrict__ v)
+{
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < P; p += (int64_t)gridDim.x * blockDim.x) {
+        if (!orth) {
+            for (int r = 0; r < R; ++r) {
+                const int64_t i = p + P * r;
+                const float d = df[i];
+                v[i] = (S[i] > 0.f || d < 0.f) ? d : 0.f;
+            }
+            continue;
+        }
+        double z = 0.0;
+        for (int r = 0; r < R; ++r) {
+            const int64_t i = p + P * r;
+            const double vi = (double)df[i] + (M2 ? l2o * (double)M2[i] : 0.0);
+            z += (double)S[i] * (double)(float)vi;
+        }
+        for (int r = 0; r < R; ++r) {
+            const int64_t i = p + P * r;
+            const float vi = (float)((double)df[i] + (M2 ? l2o * (double)M2[i] : 0.0));
+            const float w = (float)((double)vi - (double)S[i] * z);
+            v[i] = (S[i] > 0.f || w < 0.f) ? w : 0.f;
+        }
+    }
+}
+
+// Per pixel: num = sum_r v.*df, den = sum_r v.*vQ.  pointwise: alpha(p) directly;
+// else per-block partial sums into part[2 * block] (reduced by k_alpha).
+__global__ void k_s_sums(const float* __restrict__ v, const float* __restrict__ df, const float* __restrict__ vQ,
+                         int64_t P, int R, int pointwise, float* __restrict__ alpha, double* __restrict__ part)
+{
+    double bn = 0.0, bd = 0.0;
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < P; p += (int64_t)gridDim.x * blockDim.x) {
+        double x = 0.0, y = 0.0;
+        for (int r = 0; r < R; ++r) {
+            const int64_t i = p + P * r;
+            x += (double)v[i] * (double)df[i];
+            y += (double)v[i] * (double)vQ[i];
+        }
+        if (pointwise) alpha[p] = finite_or_zero(x / y);
+        bn += x;
+        bd += y;
+    }
+    if (pointwise) return;
+    __shared__ double sn[32], sd[32];
+    bn = warp_sum(bn);
+    bd = warp_sum(bd);
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) {
+        sn[w] = bn;
+        sd[w] = bd;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = 0.0, b = 0.0;
+        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) {
+            a += sn[i];
+            b += sd[i];
+        }
+        part[blockIdx.x] = a;
+        part[kRedBlocks + blockIdx.x] = b;
+    }
+}
+
+// Column norms of S (P x R), one block per column
+__global__ void k_col_norm2(const float* __restrict__ S, int64_t P, double* __restrict__ out)
+{
+    const float* col = S + P * blockIdx.x;
+    double a = 0.0;
+    for (int64_t p = threadIdx.x; p < P; p += blockDim.x) {
+        const double v = col[p];
+        a += v * v;
+    }
+    __shared__ double sh[32];
+    a = warp_sum(a);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = a;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) s += sh[i];
+        out[blockIdx.x] = s;
+    }
+}
+
+// T(r, :) *= platz(r), S(:, r) /= platz(r)   (S_update.m:75-79)
+__global__ void k_unit_cols(float* __restrict__ S, int64_t P, int R, float* __restrict__ T, int64_t F,
+                            const double* __restrict__ sq)
+{
+    const int64_t nS = P * R, nT = (int64_t)R * F;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nS + nT;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        if (i < nS) {
+            const float pl = (float)sqrt(sq[i / P]);
+            S[i] = S[i] / pl;
+        } else {
+            const int64_t j = i - nS;
+            const float pl = (float)sqrt(sq[j % R]);
+            T[j] = pl * T[j];
+        }
+    }
+}
+
+inline unsigned grid_for(int64_t n, int per = 256) { return (unsigned)std::max<int64_t>(1, std::min<int64_t>(cdiv(n, per), 152 * 16)); }
+
+// C (m x n) = A' B, FP32 SIMT (through the contraction entry, which owns the workspace)
+inline int tn32(sid_ctx* c, const float* A, const float* B, int64_t m, int64_t n, int64_t k, int64_t lda, int64_t ldb,
+                float* C, cudaStream_t st)
+{
+    return contract(c, A, B, false, m, n, k, lda, ldb, C, m, 1.f, 0.f, SID_PREC_FP32, st);
+}
+
+}  // namespace
+}  // namespace sid
+
+using namespace sid;
+
+static int nmf_checks(sid_ctx* c, const void* Y, int ydtype, const float* S, const float* T, int64_t P, int64_t R,
+                      int64_t F, const sid_nmf_opts* o, int prec, const char* who)
+{
+    SID_REQUIRE(c && Y && S && T && o, "%s: NULL argument", who);
+    SID_REQUIRE(P >= 1 && R >= 1 && F >= 1, "%s: empty problem (P %lld, R %lld, F %lld)", who, (long long)P,
+                (long long)R, (long long)F);
+    SID_REQUIRE(R <= INT32_MAX && F <= INT32_MAX, "%s: dimension too large", who);
+    SID_REQUIRE(ydtype == SID_DTYPE_F32 || ydtype == SID_DTYPE_F16, "%s: unknown Y dtype %d", who, ydtype);
+    SID_REQUIRE(prec == SID_PREC_FP32 || prec == SID_PREC_SPLIT || prec == SID_PREC_BF16, "%s: unknown precision %d",
+                who, prec);
+    return SID_OK;
+}
+
+extern "C" void sid_nmf_defaults(sid_nmf_opts* o)
+{
+    std::memset(o, 0, sizeof(*o));
+}
+
+extern "C" int sid_t_update(sid_ctx* c, const void* Y, int ydtype, float* T, float* S, int64_t P, int64_t R,
+                            int64_t F, const uint8_t* active, const float* ymean, const sid_nmf_opts* o, int prec,
+                            void* stream)
+{
+    SID_TRY(nmf_checks(c, Y, ydtype, S, T, P, R, F, o, prec, "T_update"));
+    SID_REQUIRE(!o->use_std || ymean, "T_update: use_std needs opts.Y (ymean)");
+    SID_REQUIRE(o->lamb_temp_TV == 0.0 || F >= 2, "T_update: lamb_temp_TV needs at least 2 frames");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const int64_t RF = R * F;
+    DBuf* b = c->mf;
+    SID_TRY(b[0].alloc((size_t)(R * R) * 4 * 2));  // Q_S, Q_S'
+    SID_TRY(b[1].alloc((size_t)RF * 4 * 5));       // q_T, Q(T), dT, Q(dT), scratch
+    SID_TRY(b[2].alloc((size_t)(6 * R + 2 * F + 8) * 8));
+    SID_TRY(b[3].alloc((size_t)(F + 1) * 4));      // alpha
+    float* QS = b[0].as<float>();
+    float* QSt = QS + R * R;
+    float* qT = b[1].as<float>();
+    float* QTm = qT + RF;
+    float* dT = QTm + RF;
+    float* Qd = dT + RF;
+    float* tmp = Qd + RF;
+    double* s1 = b[2].as<double>();
+    double* s2 = s1 + R;
+    double* rs = s2 + R;
+    double* dg = rs + R;
+    double* wq = dg + R;
+    double* vs = wq + R;
+    double* num = vs + R;
+    double* den = num + F;
+    float* alpha = b[3].as<float>();
+
+    // NaN -> 0 (T_update.m:5-6)
+    k_nan_zero<<<grid_for(P * R), 256, 0, st>>>(S, P * R);
+    k_nan_zero<<<grid_for(RF), 256, 0, st>>>(T, RF);
+    SID_CHECK_LAUNCH();
+    // unit-norm rows of T, S rescaled (T_update.m:14-19)
+    if (o->lamb_corr > 0) {
+        k_row_moments<<<(unsigned)cdiv(R * 32, 256), 256, 0, st>>>(T, (int)R, F, s1, s2);
+        k_renorm_rows<<<grid_for(RF + P * R), 256, 0, st>>>(T, (int)R, F, S, P, s2);
+        SID_CHECK_LAUNCH();
+    }
+    // Q_S = S_a' S_a, q_T = S_a' Y_a (T_update.m:24-25)
+    const float* Sa = S;
+    if (active) {
+        SID_TRY(b[4].alloc((size_t)(P * R) * 4));
+        k_mask_rows<<<grid_for(P * R), 256, 0, st>>>(S, active, P, R, b[4].as<float>());
+        SID_CHECK_LAUNCH();
+        Sa = b[4].as<float>();
+    }
+    SID_TRY(contract(c, Sa, Sa, false, R, R, P, P, P, QS, R, 1.f, 0.f, prec, st));
+    SID_TRY(contract(c, Sa, Y, ydtype == SID_DTYPE_F16, R, F, P, P, P, qT, R, 1.f, 0.f,
+                     (ydtype == SID_DTYPE_F16 && prec == SID_PREC_FP32) ? SID_PREC_SPLIT : prec, st));
+    SID_TRY(transpose(QS, R, R, QSt, st));
+    // use_std: q_T -= S_a' opts.Y(active) / F  (T_update.m:30)
+    const double* wqp = nullptr;
+    if (o->use_std) {
+        float* w32 = tmp;  // R floats
+        SID_TRY(tn32(c, Sa, ymean, R, 1, P, P, P, w32, st));
+        // wq = w32 widened to FP64 (the row-moment kernel on an R x 1 matrix)
+        k_row_moments<<<(unsigned)cdiv(R * 32, 256), 256, 0, st>>>(w32, (int)R, 1, wq, nullptr);
+        SID_CHECK_LAUNCH();
+        wqp = wq;
+    }
+    auto Qf = [&](const float* v, float* out) -> int {
+        // Q(x) = Q_S x [- Q_S sum(x, 2) / F]  (T_update.m:29,32)
+        const float* src = v;
+        if (o->use_std) {
+            k_row_moments<<<(unsigned)cdiv(R * 32, 256), 256, 0, st>>>(v, (int)R, F, vs, nullptr);
+            k_centre_rows<<<grid_for(RF), 256, 0, st>>>(v, vs, (int)R, F, tmp);
+            SID_CHECK_LAUNCH();
+            src = tmp;
+        }
+        return tn32(c, QSt, src, R, F, R, R, R, out, st);
+    };
+    SID_TRY(Qf(T, QTm));
+    TGrad g{};
+    g.qT = qT;
+    g.QT = QTm;
+    g.T = T;
+    g.wq = wqp;
+    g.dT = dT;
+    g.lamb_temp = o->lamb_temp;
+    g.lamb_corr = o->lamb_corr;
+    g.lamb_tv = o->lamb_temp_TV;
+    g.R = (int)R;
+    g.F = F;
+    if (o->lamb_corr != 0.0) {
+        // zsc = zscore(T) (columns; a single row is standardised along the frames),
+        // C1 = zsc zsc', C1z = C1 zsc  (T_update.m:38-41)
+        SID_TRY(b[5].alloc((size_t)(RF * 3 + R * R) * 4));
+        float* zsc = b[5].as<float>();
+        float* zt = zsc + RF;
+        float* C1z = zt + RF;
+        float* C1 = C1z + RF;
+        if (R > 1) k_zscore_cols<<<(unsigned)cdiv(F * 32, 256), 256, 0, st>>>(T, R, F, zsc);
+        else k_zscore_cols<<<1, 256, 0, st>>>(T, F, 1, zsc);
+        SID_CHECK_LAUNCH();
+        SID_TRY(transpose(zsc, R, F, zt, st));
+        SID_TRY(tn32(c, zt, zt, R, R, F, F, F, C1, st));
+        SID_TRY(tn32(c, C1, zsc, R, F, R, R, R, C1z, st));  // C1 is symmetric
+        // d = std(T, [], 2) of the (renormalised) T
+        k_row_std<<<(unsigned)cdiv(R * 32, 256), 256, 0, st>>>(T, (int)R, F, s1);
+        k_corr_rows<<<(unsigned)cdiv(R * 32, 256), 256, 0, st>>>(C1z, zsc, (int)R, F, rs, dg);
+        SID_CHECK_LAUNCH();
+        g.zsc = zsc;
+        g.C1z = C1z;
+        g.rs = rs;
+        g.dg = dg;
+        g.sd = s1;
+    }
+    k_t_grad<<<grid_for(RF), 256, 0, st>>>(g);
+    SID_CHECK_LAUNCH();
+    // exact line search (T_update.m:64-70)
+    SID_TRY(Qf(dT, Qd));
+    k_col_dots<<<(unsigned)cdiv(F * 32, 256), 256, 0, st>>>(dT, nullptr, Qd, (int)R, F, num, den);
+    k_alpha<<<o->pointwise ? grid_for(F) : 1, 256, 0, st>>>(num, den, F, o->pointwise, 0.0, alpha);
+    k_pg_step<<<grid_for(RF), 256, 0, st>>>(T, dT, R, F, alpha, o->pointwise ? 1 : 0);
+    SID_CHECK_LAUNCH();
+    return SID_OK;
+}
+
+extern "C" int sid_s_update(sid_ctx* c, const void* Y, int ydtype, float* S, float* T, int64_t P, int64_t R,
+                            int64_t F, const float* ymean, const float* hilf, const sid_nmf_opts* o, int prec,
+                            void* stream)
+{
+    SID_TRY(nmf_checks(c, Y, ydtype, S, T, P, R, F, o, prec, "S_update"));
+    SID_REQUIRE(!o->use_std || ymean, "S_update: use_std needs opts.Y (ymean)");
+    SID_REQUIRE(o->lamb_orth_L1 == 0.0 && o->lamb_orth_L2 == 0.0 ? true : hilf != nullptr,
+                "S_update: the orthogonality penalties need opts.hilf");
+    SID_REQUIRE(o->lamb_spat_TV == 0.0,
+                "S_update: lamb_spat_TV is not supported (the reference's spatial TV term calls an undefined "
+                "'laplace')");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const int64_t PR = P * R, RF = R * F;
+    const bool orth = (o->lamb_orth_L1 + o->lamb_orth_L2) > 0;
+    DBuf* b = c->mf;
+    SID_TRY(b[0].alloc((size_t)(R * R) * 4 * 4));  // Q_T, Q_T', S'S, M1'
+    SID_TRY(b[1].alloc((size_t)RF * 4));           // T'
+    SID_TRY(b[2].alloc((size_t)(2 * R + 2 * kRedBlocks + 8) * 8));
+    SID_TRY(b[3].alloc((size_t)(P + 1) * 4));      // alpha
+    SID_TRY(b[4].alloc((size_t)PR * 4 * 3));       // q_S / vQ, df, v
+    float* QT = b[0].as<float>();
+    float* QTt = QT + R * R;
+    float* SS = QTt + R * R;
+    float* M1t = SS + R * R;
+    float* Tt = b[1].as<float>();
+    double* ts = b[2].as<double>();
+    double* sq = ts + R;
+    double* part = sq + R;
+    float* alpha = b[3].as<float>();
+    float* qS = b[4].as<float>();
+    float* df = qS + PR;
+    float* v = df + PR;
+
+    k_nan_zero<<<grid_for(RF), 256, 0, st>>>(T, RF);
+    k_nan_zero<<<grid_for(PR), 256, 0, st>>>(S, PR);
+    SID_CHECK_LAUNCH();
+    // Q_T = T T', q_S = Y T'  (S_update.m:8-9)
+    SID_TRY(transpose(T, R, F, Tt, st));
+    SID_TRY(tn32(c, Tt, Tt, R, R, F, F, F, QT, st));
+    SID_TRY(sgemm_nt(Y, ydtype == SID_DTYPE_F16 ? 1 : 0, T, P, R, F, P, R, qS, P, st));
+    // use_std (S_update.m:11-15), orthogonality L1 (:19-21)
+    const double invF = 1.0 / (double)F;
+    if (o->use_std) {
+        k_row_moments<<<(unsigned)cdiv(R * 32, 256), 256, 0, st>>>(T, (int)R, F, ts, nullptr);
+        SID_CHECK_LAUNCH();
+    }
+    if (o->use_std || o->lamb_orth_L1 != 0.0) {
+        k_qt_adjust<<<grid_for(R * R), 256, 0, st>>>(QT, (int)R, o->use_std ? ts : nullptr, invF,
+                                                     o->lamb_orth_L1 != 0.0 ? hilf : nullptr, o->lamb_orth_L1);
+        SID_CHECK_LAUNCH();
+    }
+    SID_TRY(transpose(QT, R, R, QTt, st));
+    // df_S = -q_S + S*Q_T + lamb_spat  (:32)
+    SID_TRY(sgemm_nt(S, 0, QTt, P, R, R, P, R, df, P, st));
+    k_s_grad<<<grid_for(PR), 256, 0, st>>>(qS, df, P, (int)R, o->use_std ? ymean : nullptr, ts, invF, o->lamb_spat);
+    SID_CHECK_LAUNCH();
+    // direction (:38-53); M2 = S*(hilf*(S'*S)) for the L2 orthogonality term, in the q_S buffer
+    const float* M2 = nullptr;
+    if (orth && o->lamb_orth_L2 != 0.0) {
+        SID_TRY(contract(c, S, S, false, R, R, P, P, P, SS, R, 1.f, 0.f, prec, st));
+        SID_TRY(b[5].alloc((size_t)(R * R) * 4 * 2));
+        float* hT = b[5].as<float>();  // hilf'
+        float* M1 = hT + R * R;        // hilf * (S'S)
+        SID_TRY(transpose(hilf, R, R, hT, st));
+        SID_TRY(tn32(c, hT, SS, R, R, R, R, R, M1, st));
+        SID_TRY(transpose(M1, R, R, M1t, st));
+        SID_TRY(sgemm_nt(S, 0, M1t, P, R, R, P, R, qS, P, st));
+        M2 = qS;
+    }
+    k_s_dir<<<grid_for(P), 256, 0, st>>>(S, df, M2, o->lamb_orth_L2, orth ? 1 : 0, P, (int)R, v);
+    SID_CHECK_LAUNCH();
+    // exact line search (:57-68): vQ = v*Q_T into the q_S buffer
+    SID_TRY(sgemm_nt(v, 0, QTt, P, R, R, P, R, qS, P, st));
+    if (o->pointwise) {
+        k_s_sums<<<grid_for(P), 256, 0, st>>>(v, df, qS, P, (int)R, 1, alpha, part);
+    } else {
+        k_s_sums<<<kRedBlocks, 256, 0, st>>>(v, df, qS, P, (int)R, 0, alpha, part);
+        k_alpha<<<1, 256, 0, st>>>(part, part + kRedBlocks, kRedBlocks, 0, o->lamb_orth_L2 != 0.0 ? 1e-6 : 0.0,
+                                   alpha);
+    }
+    k_pg_step<<<grid_for(PR), 256, 0, st>>>(S, v, P, R, alpha, o->pointwise ? 2 : 0);
+    SID_CHECK_LAUNCH();
+    // unit-norm columns of S, T rescaled (:75-79)
+    if (orth) {
+        k_col_norm2<<<(unsigned)R, 256, 0, st>>>(S, P, sq);
+        k_unit_cols<<<grid_for(PR + RF), 256, 0, st>>>(S, P, (int)R, T, F, sq);
+        SID_CHECK_LAUNCH();
+    }
+    return SID_OK;
+}

@@ -140,7 +140,7 @@ struct sid_plan {
     sid::DBuf twiddle;          // L float2: exp(-2 pi i k / L)
     // workspaces
     sid::DBuf vp, ip, bp, ipart, vhat, ihat, bhat, red;
-    sid::DBuf ws[6];            // solver state (polyphase volumes)
+    sid::DBuf ws[9];            // solver state (polyphase volumes); [6..8] component reconstruction
     sid::DBuf errflag;          // device int: nonzero after a bounded wait expired
     sid::KTimer timer;          // dominant-kernel timing (sid_plan_timing_*)
     int zsplit;
@@ -163,4 +163,5 @@ struct sid_ctx {
     int device;
     sid::DBuf a_hi, a_lo, b_hi, b_lo, ws, scal, errflag;
     sid::DBuf nn[16];  // NNLS iteration state
+    sid::DBuf mf[8];   // NMF step workspaces (T_update / S_update)
 };

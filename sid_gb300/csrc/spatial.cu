@@ -93,6 +93,20 @@ k_sgemm_nt(const float* __restrict__ A, const void* __restrict__ Bv, const float
     }
 }
 
+// C (m x n) = A B' with A m x k (FP32 or FP16, m contiguous) and B n x k (FP32,
+// n contiguous); no split-K (the callers' m is the pixel count).
+int sgemm_nt(const void* A, int a_f16, const float* B, int64_t m, int64_t n, int64_t k, int64_t lda, int64_t ldb,
+             float* C, int64_t ldc, cudaStream_t st)
+{
+    SID_REQUIRE(m > 0 && n > 0 && k > 0, "sgemm_nt: empty problem");
+    SID_REQUIRE(m < INT32_MAX && n < INT32_MAX && k < INT32_MAX, "sgemm_nt: dimension too large");
+    dim3 grid((unsigned)cdiv(m, 128), (unsigned)cdiv(n, 64));
+    k_sgemm_nt<<<grid, 256, 0, st>>>(static_cast<const float*>(A), B, nullptr, (int)m, (int)n, (int)k, lda, ldb, C,
+                                     ldc, a_f16);
+    SID_CHECK_LAUNCH();
+    return SID_OK;
+}
+
 // Tt (F x R, column-major) = T' for T (R x F)
 __global__ void k_transpose(const float* __restrict__ T, int R, int F, float* __restrict__ Tt)
 {

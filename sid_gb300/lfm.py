@@ -79,6 +79,12 @@ def _stream_ptr():
     return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
 
 
+class ReconOpts(ctypes.Structure):
+    """sid_recon_opts: the reconstruct_S options the component driver reads."""
+    _fields_ = [("q", ctypes.c_double), ("lamb_L1", ctypes.c_double), ("lamb_L2", ctypes.c_double),
+                ("solver", ctypes.c_int), ("max_iter", ctypes.c_int)]
+
+
 class Projector:
     """Resident light-field projector for one PSF (a ``sid_plan``).
 
@@ -204,6 +210,40 @@ class Projector:
         _lib.call("sid_plan_timing_read", self._plan, ctypes.byref(ms), ctypes.byref(n))
         return ms.value, n.value
 
+    def reconstruct_component(self, img, microlenses=None, opts=None, method=None, return_lambda=False):
+        """nrm * solve(A'(img / nrm)) for one component image after the
+        background clip of reconstruct_S (reconstruct_S.m:168-205); opts:
+        q, lamb_L1, lamb_L2, whichSolver ('fast_nnls' or 'ISRA'), max_iter."""
+        opts = dict(opts or {})
+        o = ReconOpts()
+        _lib.load().sid_recon_defaults(ctypes.byref(o))
+        o.q = float(opts.get("q", o.q))
+        o.lamb_L1 = float(opts.get("lamb_L1", o.lamb_L1))
+        o.lamb_L2 = float(opts.get("lamb_L2", o.lamb_L2))
+        o.max_iter = int(opts.get("max_iter", o.max_iter))
+        solver = opts.get("whichSolver", "fast_nnls")
+        if solver not in ("fast_nnls", "ISRA"):
+            raise NotImplementedError(f"reconstruct_S: solver {solver!r} does not run natively")
+        o.solver = 0 if solver == "fast_nnls" else 1
+        im = to_device(img)
+        if tuple(im.shape) != (self.X, self.Y):
+            raise ValueError(f"component image must be {(self.X, self.Y)}, got {tuple(im.shape)}")
+        ml = None
+        if microlenses is not None:  # X x Y mask, flattened column-major
+            if isinstance(microlenses, torch.Tensor):
+                ml = microlenses.to(device="cuda", dtype=torch.uint8).permute(1, 0).contiguous().reshape(-1)
+            else:
+                m = np.asarray(microlenses) != 0
+                ml = torch.from_numpy(np.ascontiguousarray(m.astype(np.uint8).ravel(order="F"))).to("cuda")
+            if ml.numel() != self.X * self.Y:
+                raise ValueError("microlenses must be X x Y")
+        X = _fortran_tensor((self.X, self.Y, self.Z), im.device)
+        lam = ctypes.c_double()
+        _lib.call("sid_reconstruct_component", self._plan, self._method(method), im.data_ptr(),
+                  ml.data_ptr() if ml is not None else None, ctypes.byref(o), X.data_ptr(), ctypes.byref(lam),
+                  _stream_ptr())
+        return (X, lam.value) if return_lambda else X
+
     def ls_deconv(self, df, max_iter=8, lamb_L1=0.0, lamb_L2=0.0, method=None) -> torch.Tensor:
         X = to_device(df).clone()
         _lib.call("sid_deconv_ls", self._plan, self._method(method), X.data_ptr(), int(max_iter),
@@ -292,6 +332,30 @@ def LS_deconv(forwardFUN, backwardFUN, df, opts=None):
         raise TypeError("LS_deconv: forwardFUN/backwardFUN must be a Projector's forward/adjoint")
     return proj.ls_deconv(df, int(opts.get("max_iter", 8)), float(opts.get("lamb_L1", 0.0)),
                           float(opts.get("lamb_L2", 0.0)))
+
+
+def reconstruct_S(S, psf_ballistic, opts=None):
+    """recon_nnmf = reconstruct_S(S, psf_ballistic, opts) (reconstruct_S.m:1),
+    the GPU branch (:158-211): every component S(ii, :, :) reconstructed on
+    one resident plan.  S: (n, X, Y); psf_ballistic: dict or object with H;
+    opts: q, lamb_L1, lamb_L2, whichSolver, max_iter, microlenses.  Returns a
+    list of X x Y x Z CUDA tensors.  The neuron-kernel composition
+    (opts.ker_param) does not run natively."""
+    opts = dict(opts or {})
+    if "ker_param" in opts:
+        raise NotImplementedError("reconstruct_S: opts.ker_param (kernel composition) does not run natively")
+    tv = np.asarray(opts.get("lamb_TV_L2", 0.0))
+    if np.any(tv != 0) or opts.get("lamb_TV_L1", 0):
+        raise NotImplementedError("reconstruct_S: TV regularisers do not run natively")
+    H = psf_ballistic["H"] if isinstance(psf_ballistic, dict) else psf_ballistic.H
+    S = S if isinstance(S, torch.Tensor) else np.asarray(S)
+    n, X, Y = S.shape
+    method = opts.get("method", _DEFAULT_METHOD)
+    P = _plan_for(H, (X, Y), None, method)
+    out = []
+    for ii in range(n):
+        out.append(P.reconstruct_component(S[ii], opts.get("microlenses"), opts, method=method))
+    return out
 
 
 def library_boxes(centers, neur_rad, axial, size):

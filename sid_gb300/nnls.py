@@ -140,6 +140,33 @@ def _fast_nnls(self, A, Y, opts=None, prec="split", return_iters=False):
     return (X, Q, it) if return_iters else (X, Q)
 
 
+def _flat_f(a, dtype):
+    """1-D contiguous CUDA tensor of a's elements in column-major order."""
+    if isinstance(a, torch.Tensor):
+        t = a.to(device="cuda", dtype=dtype)
+        return t.permute(*reversed(range(t.dim()))).contiguous().reshape(-1)
+    arr = np.asarray(a)
+    arr = arr.astype(np.float32 if dtype == torch.float32 else np.uint8)
+    return torch.from_numpy(np.ascontiguousarray(arr.ravel(order="F"))).to("cuda")
+
+
+def _quantile(self, x, p, exclude=None):
+    """MATLAB quantile(x(exclude == 0), p) of a vector (NaN ignored), computed
+    by libsid's radix select; returns a float or a NumPy array like p."""
+    xd = _flat_f(x, torch.float32)
+    ex = None
+    if exclude is not None:
+        ex = _flat_f(exclude, torch.uint8)
+        if ex.numel() != xd.numel():
+            raise ValueError("exclude must have one entry per value")
+    ps = np.atleast_1d(np.asarray(p, dtype=np.float64))
+    out = np.zeros(ps.size)
+    _lib.call("sid_quantile", self._ctx, xd.data_ptr(), xd.numel(), ex.data_ptr() if ex is not None else None,
+              ps.ctypes.data, ps.size, out.ctypes.data, _stream_ptr())
+    return float(out[0]) if np.ndim(p) == 0 else out.reshape(np.shape(p))
+
+
+Context.quantile = _quantile
 Context.ls_nnls = _ls_nnls
 Context.fast_nnls = _fast_nnls
 
@@ -151,6 +178,11 @@ def _ctx():
     if _DEFAULT_CTX is None:
         _DEFAULT_CTX = Context()
     return _DEFAULT_CTX
+
+
+def quantile(x, p, exclude=None):
+    """MATLAB quantile of a vector on the GPU (see Context.quantile)."""
+    return _ctx().quantile(x, p, exclude)
 
 
 def LS_nnls(A, Y, opts=None, G=None, x=None):

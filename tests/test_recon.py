@@ -1,0 +1,128 @@
+"""MATLAB quantiles and the per-component reconstruction of reconstruct_S
+(reconstruct_S.m:168-205) on the GPU against the FP64 oracle."""
+import numpy as np
+import pytest
+
+from tests.conftest import rel_l2
+
+
+def test_oracle_quantile_nan_and_empty(oracle):
+    assert np.isnan(oracle.matlab_quantile(np.array([np.nan, np.nan]), 0.5))
+    assert oracle.matlab_quantile(np.array([3.0, np.nan, 1.0, 2.0]), 0.5) == 2.0
+    assert oracle.matlab_quantile(np.array([5.0]), 0.9) == 5.0
+
+
+QUANTILE_P = [0.0, 1e-4, 0.25, 0.5, 0.8, 0.9999, 1.0]
+
+
+def quantile_cases():
+    rng = np.random.default_rng(0)
+    yield "normal", rng.standard_normal(1_000_003).astype(np.float32), None
+    yield "integers", rng.integers(0, 10, 200_001).astype(np.float32), None
+    v = rng.standard_normal(50_000).astype(np.float32)
+    v[::7] = np.nan
+    v[::11] = -0.0
+    yield "nan_negzero", v, None
+    w = rng.random(300_000).astype(np.float32)
+    yield "masked", w, (rng.random(300_000) < 0.3)
+    yield "one", np.array([2.5], np.float32), None
+    yield "two", np.array([4.0, -1.0], np.float32), None
+    yield "clipped", np.maximum(rng.standard_normal(400_000), 0).astype(np.float32), None
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", [c[0] for c in quantile_cases()])
+def test_quantile_gpu_bit_exact(gpu, oracle, case):
+    import sid_gb300 as s
+    name, v, mask = next(c for c in quantile_cases() if c[0] == case)
+    got = s.quantile(v, np.array(QUANTILE_P), exclude=mask)
+    keep = v if mask is None else v[~mask]
+    want = np.array([oracle.matlab_quantile(keep, p) for p in QUANTILE_P])
+    np.testing.assert_array_equal(got, want)
+
+
+@pytest.mark.gpu
+def test_quantile_gpu_empty_is_nan(gpu):
+    import sid_gb300 as s
+    v = np.ones(100, np.float32)
+    assert np.isnan(s.quantile(v, 0.5, exclude=np.ones(100, bool)))
+    assert np.isnan(s.quantile(np.full(10, np.nan, np.float32), 0.3))
+
+
+@pytest.mark.gpu
+def test_quantile_gpu_large(gpu, oracle):
+    """A volume-sized input (1005 x 1005 x 31 values) at the Htf cap's p."""
+    import torch
+    import sid_gb300 as s
+    g = torch.Generator(device="cuda").manual_seed(3)
+    x = torch.rand(1005 * 1005 * 31, generator=g, device="cuda") ** 3
+    got = s.quantile(x, 1 - 1e-4)
+    want = oracle.matlab_quantile(x.cpu().numpy(), 1 - 1e-4)
+    assert got == want
+
+
+@pytest.fixture(scope="module")
+def small(gpu, oracle):
+    from sid_gb300 import Projector, synthetic
+    N, Z, M, L = 5, 3, 31, 9
+    X = N * L
+    H = synthetic.gaussian_psf(M, N, Z, sigma_min=1.0, sigma_max=3.0)
+    Vt = synthetic.blob_volume(X, X, Z, 6, sigma=(1.5, 1.5), seed=4)
+    rng = np.random.default_rng(9)
+    img = (oracle.forward_project(H, Vt) + 0.02 * rng.random((X, X))).astype(np.float32)
+    P = Projector(H, (X, X), None, methods=("direct", "spectral_f32", "spectral_mixed"))
+    fwd = lambda v: oracle.forward_project(H, v)  # noqa: E731
+    bwd = lambda i: oracle.backward_project(H, i)  # noqa: E731
+    return H, np.asfortranarray(img), P, fwd, bwd
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("method,opts,tol", [
+    ("direct", {}, 1e-4),
+    ("spectral_f32", {"lamb_L1": 1e-3, "lamb_L2": 1e-2}, 1e-4),
+    ("spectral_mixed", {"q": 0.5}, 1e-3),
+    ("direct", {"whichSolver": "ISRA", "max_iter": 6}, 1e-4),
+])
+def test_reconstruct_component_matches_oracle(small, oracle, method, opts, tol):
+    import sid_gb300 as s
+    H, img, P, fwd, bwd = small
+    ref = oracle.reconstruct_S_one(img, fwd, bwd, opts)
+    out, lam = P.reconstruct_component(img, None, opts, method=method, return_lambda=True)
+    assert rel_l2(s.to_numpy(out), ref) < tol, rel_l2(s.to_numpy(out), ref)
+    assert lam <= opts.get("lamb_L1", 0.0)
+
+
+@pytest.mark.gpu
+def test_reconstruct_component_l1_cap(small, oracle):
+    """A large lamb_L1 is capped by the (1 - 1e-4) quantile of Htf
+    (reconstruct_S.m:193)."""
+    H, img, P, fwd, bwd = small
+    im = np.maximum(img.astype(np.float64) - oracle.matlab_quantile(img, 0.8), 0.0)
+    im = im / im.max()
+    Htf = bwd(im / np.sqrt(np.sum(im * im)))
+    want = oracle.matlab_quantile(Htf, 1 - 1e-4)
+    _, lam = P.reconstruct_component(img, None, {"lamb_L1": 1e6}, method="direct", return_lambda=True)
+    assert abs(lam - want) <= 1e-5 * abs(want)
+
+
+@pytest.mark.gpu
+def test_reconstruct_component_microlens_mask(small, oracle):
+    import sid_gb300 as s
+    H, img, P, fwd, bwd = small
+    ml = np.zeros(img.shape, dtype=np.uint8)
+    ml[2::5, 2::5] = 1  # lenslet centres excluded from the background quantile
+    ref = oracle.reconstruct_S_one(img, fwd, bwd, {}, microlenses=ml)
+    out = P.reconstruct_component(img, ml, {}, method="direct")
+    assert rel_l2(s.to_numpy(out), ref) < 1e-4
+
+
+@pytest.mark.gpu
+def test_reconstruct_S_function_api(small, oracle):
+    import sid_gb300 as s
+    H, img, P, fwd, bwd = small
+    S = np.stack([img, np.asfortranarray(img[::-1, :])])
+    recon = s.reconstruct_S(S, {"H": H}, {"method": "direct"})
+    assert len(recon) == 2
+    for k in range(2):
+        ref = oracle.reconstruct_S_one(S[k], fwd, bwd, {})
+        assert rel_l2(s.to_numpy(recon[k]), ref) < 1e-4
