@@ -182,104 +182,260 @@ int build_spectra(sid_plan* p)
 }
 
 // -------------------------------------------------------------- real DFTs --
-// Analysis: polyphase planes [ch][Ly][Lx] (zero-extended to L x L) -> half
-// spectra [ch][nf], f = f1 + H1*f2, X(f1,f2) = sum_{u,v} x(u,v) w^{-(f1 u + f2 v)}.
-__global__ void k_dft_r2c(const float* __restrict__ in, float2* __restrict__ out,
-                          const float2* __restrict__ tw, int Lx, int Ly, int L)
+// Both transforms are small complex matrix products per channel, computed as
+// register-blocked GEMMs against twiddle tables held in shared memory (built
+// once per CTA; the CTAs are persistent over channels):
+//   analysis   G(v, f1)  = sum_u  x(v, u) conj(w^(u f1))         (real x complex, K = Lx)
+//              X(f2, f1) = sum_v  conj(w^(v f2)) G(v, f1)         (complex, K = Ly)
+//   synthesis  Gt(f1, t) = sum_f2 w^(t f2) S(f2, f1)              (complex, K = L)
+//              x(t, s)   = 1/L^2 sum_f1 c(f1) Re(Gt(f1, t) w^(s f1))  (K = H1; c = 1 at f1 = 0
+//                          and at the Nyquist column of an even L, 2 elsewhere)
+// with w = exp(2 pi i / L), planes [ch][Ly][Lx] zero-extended to L x L and
+// half spectra [ch][nf], f = f1 + H1 f2.  Each thread owns an 8 x 2 (complex)
+// or 8 x 4 (real) output block: per reduction step it reads 4-6 16-byte words
+// from shared memory for 32-64 FMAs.
+struct DftDims {
+    int Lx, Ly, L, H1;
+    int H1p, Lyp, Lxp, Lp;  // padded: 2 | H1p, 8 | Lyp, 4 | Lxp, 8 | Lp
+    int N;
+    int64_t X, Y;
+};
+
+constexpr int kDftThreads = 224;
+
+static DftDims dft_dims(const sid_plan* p)
 {
-    extern __shared__ float2 sm2[];
-    const int H1 = L / 2 + 1, nf = H1 * L;
-    float2* G = sm2;               // [Ly][H1]
-    float2* stw = G + Ly * H1;     // [L]
-    float* img = reinterpret_cast<float*>(stw + L);  // [Ly][Lx]
-    const int64_t ch = blockIdx.x;
-    const float* src = in + ch * (int64_t)Ly * Lx;
-    for (int i = threadIdx.x; i < L; i += blockDim.x) stw[i] = tw[i];
-    for (int i = threadIdx.x; i < Ly * Lx; i += blockDim.x) img[i] = src[i];
-    __syncthreads();
-    for (int i = threadIdx.x; i < Ly * H1; i += blockDim.x) {
-        const int v = i / H1, f1 = i - (i / H1) * H1;
-        const float* row = img + v * Lx;
-        float ax = 0.f, ay = 0.f;
-        int k = 0;
-        for (int u = 0; u < Lx; ++u) {
-            const float2 w = stw[k];
-            ax = fmaf(row[u], w.x, ax);
-            ay = fmaf(-row[u], w.y, ay);
-            k += f1;
-            if (k >= L) k -= L;
-        }
-        G[i] = make_float2(ax, ay);
+    DftDims d;
+    d.Lx = (int)p->Lx;
+    d.Ly = (int)p->Ly;
+    d.L = (int)p->L;
+    d.H1 = d.L / 2 + 1;
+    d.H1p = (int)cdiv(d.H1, 2) * 2;
+    d.Lyp = (int)cdiv(d.Ly, 8) * 8;
+    d.Lxp = (int)cdiv(d.Lx, 4) * 4;
+    d.Lp = (int)cdiv(d.L, 8) * 8;
+    d.N = (int)p->N;
+    d.X = p->X;
+    d.Y = p->Y;
+    return d;
+}
+
+static size_t r2c_smem(const DftDims& d)
+{
+    return (size_t)(d.Lx * d.H1p + d.Ly * d.Lp + d.Lyp * d.H1p) * sizeof(float2) +
+           (size_t)(d.Lx * d.Lyp) * sizeof(float);
+}
+static size_t c2r_smem(const DftDims& d)
+{
+    const size_t u = std::max((size_t)d.L * d.H1p, (size_t)d.H1 * d.Lxp);
+    return ((size_t)d.L * d.Lyp + (size_t)d.H1p * d.Lyp + u) * sizeof(float2);
+}
+
+__device__ __forceinline__ float2 cconj(float2 a) { return make_float2(a.x, -a.y); }
+
+__global__ void __launch_bounds__(kDftThreads, 2)
+k_dft_r2c(const float* __restrict__ in, float2* __restrict__ out, const float2* __restrict__ tw, DftDims d,
+          int64_t nch)
+{
+    extern __shared__ __align__(16) unsigned char dft_sm[];
+    float2* C1 = reinterpret_cast<float2*>(dft_sm);         // [Lx][H1p]  conj(w^(u f1))
+    float2* C2 = C1 + d.Lx * d.H1p;                          // [Ly][Lp]   conj(w^(v f2))
+    float2* G = C2 + d.Ly * d.Lp;                            // [Lyp][H1p]
+    float* img = reinterpret_cast<float*>(G + d.Lyp * d.H1p);  // [Lx][Lyp] (transposed plane)
+    const int L = d.L, H1 = d.H1, nf = H1 * L;
+    for (int i = threadIdx.x; i < d.Lx * d.H1p; i += blockDim.x) {
+        const int u = i / d.H1p, f1 = i - u * d.H1p;
+        C1[i] = f1 < H1 ? cconj(tw[(u * f1) % L]) : make_float2(0.f, 0.f);
     }
+    for (int i = threadIdx.x; i < d.Ly * d.Lp; i += blockDim.x) {
+        const int v = i / d.Lp, f2 = i - v * d.Lp;
+        C2[i] = f2 < L ? cconj(tw[(v * f2) % L]) : make_float2(0.f, 0.f);
+    }
+    for (int i = threadIdx.x; i < d.Lx * d.Lyp; i += blockDim.x) img[i] = 0.f;  // rows v >= Ly stay zero
     __syncthreads();
-    float2* dst = out + ch * (int64_t)nf;
-    for (int i = threadIdx.x; i < nf; i += blockDim.x) {
-        const int f2 = i / H1, f1 = i - (i / H1) * H1;
-        float ax = 0.f, ay = 0.f;
-        int k = 0;
-        for (int v = 0; v < Ly; ++v) {
-            const float2 g = G[v * H1 + f1];
-            const float2 w = stw[k];  // multiply by conj(w)
-            ax += g.x * w.x + g.y * w.y;
-            ay += g.y * w.x - g.x * w.y;
-            k += f2;
-            if (k >= L) k -= L;
+    const int nvb = d.Lyp / 8, nfb = d.H1p / 2, nf2b = d.Lp / 8;
+    for (int64_t ch = blockIdx.x; ch < nch; ch += gridDim.x) {
+        const float* src = in + ch * (int64_t)d.Ly * d.Lx;
+        for (int i = threadIdx.x; i < d.Ly * d.Lx; i += blockDim.x) {
+            const int v = i / d.Lx, u = i - v * d.Lx;
+            img[u * d.Lyp + v] = src[i];
         }
-        dst[i] = make_float2(ax, ay);
+        __syncthreads();
+        // G = x * C1: rows v (8 per thread), column pairs f1
+        for (int task = threadIdx.x; task < nvb * nfb; task += blockDim.x) {
+            const int fb = task % nfb, vb = task / nfb;
+            float acc[8][4];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
+            const float* ap = img + vb * 8;
+            const float2* cp = C1 + fb * 2;
+            for (int u = 0; u < d.Lx; ++u) {
+                const float4 a0 = *reinterpret_cast<const float4*>(ap + u * d.Lyp);
+                const float4 a1 = *reinterpret_cast<const float4*>(ap + u * d.Lyp + 4);
+                const float4 c = *reinterpret_cast<const float4*>(cp + u * d.H1p);
+                const float a[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+#pragma unroll
+                for (int j = 0; j < 8; ++j) {
+                    acc[j][0] = fmaf(a[j], c.x, acc[j][0]);
+                    acc[j][1] = fmaf(a[j], c.y, acc[j][1]);
+                    acc[j][2] = fmaf(a[j], c.z, acc[j][2]);
+                    acc[j][3] = fmaf(a[j], c.w, acc[j][3]);
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < 8; ++j)
+                *reinterpret_cast<float4*>(G + (vb * 8 + j) * d.H1p + fb * 2) =
+                    make_float4(acc[j][0], acc[j][1], acc[j][2], acc[j][3]);
+        }
+        __syncthreads();
+        // X = C2' * G: rows f2 (8 per thread), column pairs f1
+        float2* dst = out + ch * (int64_t)nf;
+        for (int task = threadIdx.x; task < nf2b * nfb; task += blockDim.x) {
+            const int fb = task % nfb, f2b = task / nfb;
+            float acc[8][4];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
+            const float2* gp = G + fb * 2;
+            const float2* wp = C2 + f2b * 8;
+            for (int v = 0; v < d.Ly; ++v) {
+                const float4 g = *reinterpret_cast<const float4*>(gp + v * d.H1p);
+                float2 w[8];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const float4 t = *reinterpret_cast<const float4*>(wp + v * d.Lp + 2 * q);
+                    w[2 * q] = make_float2(t.x, t.y);
+                    w[2 * q + 1] = make_float2(t.z, t.w);
+                }
+#pragma unroll
+                for (int j = 0; j < 8; ++j) {
+                    acc[j][0] = fmaf(w[j].x, g.x, fmaf(-w[j].y, g.y, acc[j][0]));
+                    acc[j][1] = fmaf(w[j].x, g.y, fmaf(w[j].y, g.x, acc[j][1]));
+                    acc[j][2] = fmaf(w[j].x, g.z, fmaf(-w[j].y, g.w, acc[j][2]));
+                    acc[j][3] = fmaf(w[j].x, g.w, fmaf(w[j].y, g.z, acc[j][3]));
+                }
+            }
+            const int f1 = fb * 2;
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                const int f2 = f2b * 8 + j;
+                if (f2 >= L) break;
+                dst[f2 * H1 + f1] = make_float2(acc[j][0], acc[j][1]);
+                if (f1 + 1 < H1) dst[f2 * H1 + f1 + 1] = make_float2(acc[j][2], acc[j][3]);
+            }
+        }
+        // no barrier: the next plane load writes only img, which this pass does not read
     }
 }
 
-// Synthesis: half spectra [ch][nf] -> planes [ch][Ly][Lx], x = (1/L^2) sum X w^{+...}.
 // Lattice positions outside the X x Y frame are written as zero.
-__global__ void k_dft_c2r(const float2* __restrict__ in, float* __restrict__ out,
-                          const float2* __restrict__ tw, int Lx, int Ly, int L, int N, int64_t X,
-                          int64_t Y)
+__global__ void __launch_bounds__(kDftThreads, 2)
+k_dft_c2r(const float2* __restrict__ in, float* __restrict__ out, const float2* __restrict__ tw, DftDims d,
+          int64_t nch)
 {
-    extern __shared__ float2 sm2[];
-    const int H1 = L / 2 + 1, nf = H1 * L;
-    float2* S = sm2;              // [nf]
-    float2* G = S + nf;           // [Ly][H1]
-    float2* stw = G + Ly * H1;    // [L]
-    const int64_t ch = blockIdx.x;
-    const int a = (int)(ch % N), b = (int)((ch / N) % N);
-    const float2* src = in + ch * (int64_t)nf;
-    for (int i = threadIdx.x; i < L; i += blockDim.x) stw[i] = tw[i];
-    for (int i = threadIdx.x; i < nf; i += blockDim.x) S[i] = src[i];
-    __syncthreads();
-    for (int i = threadIdx.x; i < Ly * H1; i += blockDim.x) {
-        const int t = i / H1, f1 = i - (i / H1) * H1;
-        float ax = 0.f, ay = 0.f;
-        int k = 0;
-        for (int f2 = 0; f2 < L; ++f2) {
-            const float2 s = S[f2 * H1 + f1];
-            const float2 w = stw[k];
-            ax += s.x * w.x - s.y * w.y;
-            ay += s.x * w.y + s.y * w.x;
-            k += t;
-            if (k >= L) k -= L;
-        }
-        G[i] = make_float2(ax, ay);
-    }
-    __syncthreads();
-    const float inv = 1.0f / ((float)L * (float)L);
+    extern __shared__ __align__(16) unsigned char dft_sm[];
+    float2* D1 = reinterpret_cast<float2*>(dft_sm);  // [L][Lyp]  w^(t f2)
+    float2* Gt = D1 + d.L * d.Lyp;                   // [H1p][Lyp]
+    float2* S = Gt + d.H1p * d.Lyp;                  // [L][H1p] spectrum, then E [H1][Lxp]
+    float2* E = S;
+    const int L = d.L, H1 = d.H1, nf = H1 * L;
     const bool even = (L % 2) == 0;
-    float* dst = out + ch * (int64_t)Ly * Lx;
-    for (int i = threadIdx.x; i < Ly * Lx; i += blockDim.x) {
-        const int t = i / Lx, s = i - (i / Lx) * Lx;
-        const float2* g = G + t * H1;
-        float acc = g[0].x;
-        int k = s;
-        if (k >= L) k -= L;
-        const int last = even ? H1 - 1 : H1;
-        for (int f1 = 1; f1 < last; ++f1) {
-            const float2 w = stw[k];
-            acc += 2.f * (g[f1].x * w.x - g[f1].y * w.y);
-            k += s;
-            if (k >= L) k -= L;
+    for (int i = threadIdx.x; i < d.L * d.Lyp; i += blockDim.x) {
+        const int f2 = i / d.Lyp, t = i - f2 * d.Lyp;
+        D1[i] = t < d.Ly ? tw[(t * f2) % L] : make_float2(0.f, 0.f);
+    }
+    const float inv = 1.0f / ((float)L * (float)L);
+    const int ntb = d.Lyp / 8, nfb = d.H1p / 2, nsb = d.Lxp / 4;
+    for (int64_t ch = blockIdx.x; ch < nch; ch += gridDim.x) {
+        const float2* src = in + ch * (int64_t)nf;
+        for (int i = threadIdx.x; i < d.L * d.H1p; i += blockDim.x) {
+            const int f2 = i / d.H1p, f1 = i - f2 * d.H1p;
+            S[i] = f1 < H1 ? src[f2 * H1 + f1] : make_float2(0.f, 0.f);
         }
-        if (even) acc += (s & 1) ? -g[H1 - 1].x : g[H1 - 1].x;
-        const bool inside = (a + (int64_t)N * s) < X && (b + (int64_t)N * t) < Y;
-        dst[i] = inside ? acc * inv : 0.f;
+        __syncthreads();
+        // Gt = (D1' S)': rows t (8 per thread), column pairs f1
+        for (int task = threadIdx.x; task < ntb * nfb; task += blockDim.x) {
+            const int fb = task % nfb, tb = task / nfb;
+            float acc[8][4];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
+            const float2* sp = S + fb * 2;
+            const float2* wp = D1 + tb * 8;
+            for (int f2 = 0; f2 < L; ++f2) {
+                const float4 g = *reinterpret_cast<const float4*>(sp + f2 * d.H1p);
+                float2 w[8];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const float4 t = *reinterpret_cast<const float4*>(wp + f2 * d.Lyp + 2 * q);
+                    w[2 * q] = make_float2(t.x, t.y);
+                    w[2 * q + 1] = make_float2(t.z, t.w);
+                }
+#pragma unroll
+                for (int j = 0; j < 8; ++j) {
+                    acc[j][0] = fmaf(w[j].x, g.x, fmaf(-w[j].y, g.y, acc[j][0]));
+                    acc[j][1] = fmaf(w[j].x, g.y, fmaf(w[j].y, g.x, acc[j][1]));
+                    acc[j][2] = fmaf(w[j].x, g.z, fmaf(-w[j].y, g.w, acc[j][2]));
+                    acc[j][3] = fmaf(w[j].x, g.w, fmaf(w[j].y, g.z, acc[j][3]));
+                }
+            }
+#pragma unroll
+            for (int m = 0; m < 2; ++m) {
+                float2* gr = Gt + (fb * 2 + m) * d.Lyp + tb * 8;
+#pragma unroll
+                for (int j = 0; j < 8; j += 2)
+                    *reinterpret_cast<float4*>(gr + j) =
+                        make_float4(acc[j][2 * m], acc[j][2 * m + 1], acc[j + 1][2 * m], acc[j + 1][2 * m + 1]);
+            }
+        }
+        __syncthreads();
+        // E(f1, s) = c(f1) w^(s f1) over the spectrum's space
+        for (int i = threadIdx.x; i < H1 * d.Lxp; i += blockDim.x) {
+            const int f1 = i / d.Lxp, s = i - f1 * d.Lxp;
+            const float c = (f1 == 0 || (even && f1 == H1 - 1)) ? 1.f : 2.f;
+            const float2 w = tw[(s * f1) % L];
+            E[i] = s < d.Lx ? make_float2(c * w.x, c * w.y) : make_float2(0.f, 0.f);
+        }
+        __syncthreads();
+        // x = Re(Gt' E) / L^2: rows t (8 per thread), columns s (4 per thread)
+        const int a = (int)(ch % d.N), b = (int)((ch / d.N) % d.N);
+        float* dst = out + ch * (int64_t)d.Ly * d.Lx;
+        for (int task = threadIdx.x; task < ntb * nsb; task += blockDim.x) {
+            const int sb = task % nsb, tb = task / nsb;
+            float acc[8][4];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
+            const float2* gp = Gt + tb * 8;
+            const float2* ep = E + sb * 4;
+            for (int f1 = 0; f1 < H1; ++f1) {
+                float2 g[8];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const float4 t = *reinterpret_cast<const float4*>(gp + f1 * d.Lyp + 2 * q);
+                    g[2 * q] = make_float2(t.x, t.y);
+                    g[2 * q + 1] = make_float2(t.z, t.w);
+                }
+                const float4 e0 = *reinterpret_cast<const float4*>(ep + f1 * d.Lxp);
+                const float4 e1 = *reinterpret_cast<const float4*>(ep + f1 * d.Lxp + 2);
+                const float2 e[4] = {make_float2(e0.x, e0.y), make_float2(e0.z, e0.w), make_float2(e1.x, e1.y),
+                                     make_float2(e1.z, e1.w)};
+#pragma unroll
+                for (int j = 0; j < 8; ++j)
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) acc[j][k] = fmaf(g[j].x, e[k].x, fmaf(-g[j].y, e[k].y, acc[j][k]));
+            }
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                const int t = tb * 8 + j;
+                if (t >= d.Ly) break;
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    const int s = sb * 4 + k;
+                    if (s >= d.Lx) break;
+                    const bool inside = (a + (int64_t)d.N * s) < d.X && (b + (int64_t)d.N * t) < d.Y;
+                    dst[t * d.Lx + s] = inside ? acc[j][k] * inv : 0.f;
+                }
+            }
+        }
+        __syncthreads();
     }
 }
 
@@ -429,24 +585,33 @@ static int ensure_spec_ws(sid_plan* p)
     return SID_OK;
 }
 
-static size_t r2c_smem(const sid_plan* p)
-{
-    const int64_t H1 = p->L / 2 + 1;
-    return (size_t)(p->Ly * H1 + p->L) * sizeof(float2) + (size_t)(p->Ly * p->Lx) * sizeof(float);
-}
-static size_t c2r_smem(const sid_plan* p)
-{
-    const int64_t H1 = p->L / 2 + 1;
-    return (size_t)(p->nf + p->Ly * H1 + p->L) * sizeof(float2);
-}
-
 static int configure_dft(const sid_plan* p)
 {
-    SID_REQUIRE(r2c_smem(p) <= 220 * 1024 && c2r_smem(p) <= 220 * 1024,
+    const DftDims d = dft_dims(p);
+    SID_REQUIRE(r2c_smem(d) <= 220 * 1024 && c2r_smem(d) <= 220 * 1024,
                 "spectral projector: lenslet grid %lldx%lld (L=%lld) exceeds the DFT kernels' shared memory",
                 (long long)p->Lx, (long long)p->Ly, (long long)p->L);
-    SID_CUDA_TRY(cudaFuncSetAttribute(k_dft_r2c, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)r2c_smem(p)));
-    SID_CUDA_TRY(cudaFuncSetAttribute(k_dft_c2r, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c2r_smem(p)));
+    SID_CUDA_TRY(cudaFuncSetAttribute(k_dft_r2c, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)r2c_smem(d)));
+    SID_CUDA_TRY(cudaFuncSetAttribute(k_dft_c2r, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c2r_smem(d)));
+    return SID_OK;
+}
+
+// persistent DFT grids: at most two CTAs per SM (shared-memory bound)
+static unsigned dft_grid(int64_t nch) { return (unsigned)std::min<int64_t>(nch, 2 * 152); }
+
+static int dft_r2c(const sid_plan* p, const float* in, float2* out, int64_t nch, cudaStream_t st)
+{
+    const DftDims d = dft_dims(p);
+    k_dft_r2c<<<dft_grid(nch), kDftThreads, r2c_smem(d), st>>>(in, out, p->twiddle.as<float2>(), d, nch);
+    SID_CHECK_LAUNCH();
+    return SID_OK;
+}
+
+static int dft_c2r(const sid_plan* p, const float2* in, float* out, int64_t nch, cudaStream_t st)
+{
+    const DftDims d = dft_dims(p);
+    k_dft_c2r<<<dft_grid(nch), kDftThreads, c2r_smem(d), st>>>(in, out, p->twiddle.as<float2>(), d, nch);
+    SID_CHECK_LAUNCH();
     return SID_OK;
 }
 
@@ -469,9 +634,7 @@ int spectral_forward(sid_plan* p, bool i16, const float* vp, float* ip, cudaStre
     SID_TRY(ensure_spec_ws(p));
     SID_TRY(configure_dft(p));
     const int64_t n_in = p->N * p->N * p->Z, n_out = p->N * p->N, n_in_pad = spec_nin_pad(p);
-    k_dft_r2c<<<(unsigned)n_in, 256, r2c_smem(p), st>>>(vp, p->vhat.as<float2>(), p->twiddle.as<float2>(),
-                                                         (int)p->Lx, (int)p->Ly, (int)p->L);
-    SID_CHECK_LAUNCH();
+    SID_TRY(dft_r2c(p, vp, p->vhat.as<float2>(), n_in, st));
     const size_t sm = (size_t)n_in_pad * sizeof(float2);
     p->timer.begin(st);
     if (i16) {
@@ -487,9 +650,7 @@ int spectral_forward(sid_plan* p, bool i16, const float* vp, float* ip, cudaStre
     }
     p->timer.finish(st);
     SID_CHECK_LAUNCH();
-    k_dft_c2r<<<(unsigned)n_out, 256, c2r_smem(p), st>>>(p->ihat.as<float2>(), ip, p->twiddle.as<float2>(),
-                                                          (int)p->Lx, (int)p->Ly, (int)p->L, (int)p->N, p->X, p->Y);
-    SID_CHECK_LAUNCH();
+    SID_TRY(dft_c2r(p, p->ihat.as<float2>(), ip, n_out, st));
     return SID_OK;
 }
 
@@ -499,9 +660,7 @@ int spectral_adjoint(sid_plan* p, bool i16, const float* ip, float* bp, cudaStre
     SID_TRY(ensure_spec_ws(p));
     SID_TRY(configure_dft(p));
     const int64_t n_in = p->N * p->N * p->Z, n_out = p->N * p->N, n_in_pad = spec_nin_pad(p);
-    k_dft_r2c<<<(unsigned)n_out, 256, r2c_smem(p), st>>>(ip, p->ihat.as<float2>(), p->twiddle.as<float2>(),
-                                                          (int)p->Lx, (int)p->Ly, (int)p->L);
-    SID_CHECK_LAUNCH();
+    SID_TRY(dft_r2c(p, ip, p->ihat.as<float2>(), n_out, st));
     const size_t sm = (size_t)n_out * sizeof(float2);
     p->timer.begin(st);
     if (i16)
@@ -514,9 +673,7 @@ int spectral_adjoint(sid_plan* p, bool i16, const float* ip, float* bp, cudaStre
                                                            (int)p->nf);
     p->timer.finish(st);
     SID_CHECK_LAUNCH();
-    k_dft_c2r<<<(unsigned)n_in, 256, c2r_smem(p), st>>>(p->vhat.as<float2>(), bp, p->twiddle.as<float2>(),
-                                                         (int)p->Lx, (int)p->Ly, (int)p->L, (int)p->N, p->X, p->Y);
-    SID_CHECK_LAUNCH();
+    SID_TRY(dft_c2r(p, p->vhat.as<float2>(), bp, n_in, st));
     return SID_OK;
 }
 

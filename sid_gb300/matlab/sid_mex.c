@@ -13,7 +13,16 @@
  *   X        = sid_mex('ls_deconv', plan, df, max_iter, lamb_L1, lamb_L2, method)
  *   [X, G]   = sid_mex('ls_nnls', A, Y, opts)
  *   [X, Q]   = sid_mex('fast_nnls', A, Y, opts)
+ *   [S, T]   = sid_mex('t_update', Y, T, S, opts)        opts.active, opts.Y optional
+ *   [S, T]   = sid_mex('s_update', Y, S, T, opts)        opts.Y, opts.hilf optional
+ *   q        = sid_mex('quantile', x, p)
+ *   h        = sid_mex('pinv_create', F)                  F: K x P forward model
+ *   T        = sid_mex('pinv_apply', h, Y, baseline)      baseline may be []
+ *   sid_mex('pinv_destroy', h)
+ *   [X, lam] = sid_mex('reconstruct', plan, img, microlenses, opts, method)
  *   sid_mex('destroy', plan)
+ * Matrix arguments of the NNLS / NMF / extraction commands are single
+ * gpuArrays (the movie Y may be half); results are gpuArrays.
  * gpuArray inputs use the device entry points directly (mxGPUArray); other
  * inputs go through the _host entry points.  A non-zero libsid status becomes a
  * MATLAB error with identifier 'sid:<command>' and sid_last_error() as text.
@@ -26,8 +35,14 @@
 #include "sid.h"
 
 #define MAX_PLANS 64
+#define MAX_PINV 16
 static sid_plan* g_plans[MAX_PLANS];
+static sid_pinv* g_pinv[MAX_PINV];
+static int64_t g_pinv_K[MAX_PINV];
 static sid_ctx* g_ctx = NULL;
+
+static double field_or(const mxArray* s, const char* name, double dflt);
+static void check(int rc, const char* cmd);
 
 static void cleanup(void)
 {
@@ -36,10 +51,53 @@ static void cleanup(void)
             sid_plan_destroy(g_plans[i]);
             g_plans[i] = NULL;
         }
+    for (int i = 0; i < MAX_PINV; ++i)
+        if (g_pinv[i]) {
+            sid_pinv_destroy(g_pinv[i]);
+            g_pinv[i] = NULL;
+        }
     if (g_ctx) {
         sid_ctx_destroy(g_ctx);
         g_ctx = NULL;
     }
+}
+
+static sid_ctx* ctx(const char* cmd)
+{
+    if (!g_ctx) check(sid_ctx_create(&g_ctx), cmd);
+    return g_ctx;
+}
+
+/* single (or, where allowed, half) gpuArray argument */
+static const mxGPUArray* gpu_arg(const mxArray* a, int allow_half, const char* cmd)
+{
+    if (!mxIsGPUArray(a)) mexErrMsgIdAndTxt("sid:type", "%s: gpuArray arguments expected", cmd);
+    const mxGPUArray* g = mxGPUCreateFromMxArray(a);
+    const mxClassID c = mxGPUGetClassID(g);
+    if (c != mxSINGLE_CLASS && !(allow_half && c == mxUINT16_CLASS))
+        mexErrMsgIdAndTxt("sid:type", "%s: single gpuArray expected", cmd);
+    return g;
+}
+
+static int ydtype(const mxGPUArray* g) { return mxGPUGetClassID(g) == mxSINGLE_CLASS ? SID_DTYPE_F32 : SID_DTYPE_F16; }
+
+static mxGPUArray* gpu_copy(const mxGPUArray* g)
+{
+    return mxGPUCopyGPUArray(g);
+}
+
+static void nmf_opts(const mxArray* o, sid_nmf_opts* out)
+{
+    sid_nmf_defaults(out);
+    out->lamb_temp = field_or(o, "lamb_temp", 0.0);
+    out->lamb_corr = field_or(o, "lamb_corr", 0.0);
+    out->lamb_temp_TV = field_or(o, "lamb_temp_TV", 0.0);
+    out->lamb_spat = field_or(o, "lamb_spat", 0.0);
+    out->lamb_spat_TV = field_or(o, "lamb_spat_TV", 0.0);
+    out->lamb_orth_L1 = field_or(o, "lamb_orth_L1", 0.0);
+    out->lamb_orth_L2 = field_or(o, "lamb_orth_L2", 0.0);
+    out->use_std = (int)field_or(o, "use_std", 0.0);
+    out->pointwise = (int)field_or(o, "pointwise", 0.0);
 }
 
 static void check(int rc, const char* cmd)
@@ -197,6 +255,189 @@ void mexFunction(int nlhs, mxArray* plhs[], int nrhs, const mxArray* prhs[])
         if (nlhs > 1) plhs[1] = mxGPUCreateMxArrayOnGPU(G);
         mxGPUDestroyGPUArray(X);
         mxGPUDestroyGPUArray(G);
+        return;
+    }
+    if (!strcmp(cmd, "ls_deconv")) {
+        /* X = sid_mex('ls_deconv', plan, df, max_iter, lamb_L1, lamb_L2, method): df single, host or gpuArray;
+         * the result lives where df did */
+        sid_plan* p = plan_arg(prhs[1]);
+        const int method = method_arg(nrhs, prhs, 6);
+        const int on_gpu = mxIsGPUArray(prhs[2]);
+        if (!on_gpu && !mxIsSingle(prhs[2])) mexErrMsgIdAndTxt("sid:type", "ls_deconv: df must be single");
+        const mxGPUArray* df = mxGPUCreateFromMxArray(prhs[2]); /* host arrays are copied to the device */
+        if (mxGPUGetClassID(df) != mxSINGLE_CLASS) mexErrMsgIdAndTxt("sid:type", "ls_deconv: df must be single");
+        mxGPUArray* X = gpu_copy(df);
+        mxGPUDestroyGPUArray(df);
+        int rc = sid_deconv_ls(p, method, (float*)mxGPUGetData(X), (int)mxGetScalar(prhs[3]),
+                               (float)mxGetScalar(prhs[4]), (float)mxGetScalar(prhs[5]), NULL);
+        if (rc == SID_OK) rc = sid_plan_sync(p, NULL);
+        if (rc != SID_OK) mxGPUDestroyGPUArray(X);
+        check(rc, cmd);
+        plhs[0] = on_gpu ? mxGPUCreateMxArrayOnGPU(X) : mxGPUCreateMxArrayOnCPU(X);
+        mxGPUDestroyGPUArray(X);
+        return;
+    }
+    if (!strcmp(cmd, "t_update") || !strcmp(cmd, "s_update")) {
+        /* [S, T] = sid_mex('t_update', Y, T, S, opts)  /  [S, T] = sid_mex('s_update', Y, S, T, opts) */
+        const int tu = !strcmp(cmd, "t_update");
+        const mxArray* o = nrhs > 4 ? prhs[4] : NULL;
+        const mxGPUArray* Y = gpu_arg(prhs[1], 1, cmd);
+        const mxGPUArray* A1 = gpu_arg(prhs[2], 0, cmd); /* T (t_update) or S (s_update) */
+        const mxGPUArray* A2 = gpu_arg(prhs[3], 0, cmd);
+        mxGPUArray* T = gpu_copy(tu ? A1 : A2);
+        mxGPUArray* S = gpu_copy(tu ? A2 : A1);
+        const mwSize* ds = mxGPUGetDimensions(S);
+        const mwSize* dt = mxGPUGetDimensions(T);
+        const int64_t P = (int64_t)ds[0], R = (int64_t)ds[1], F = (int64_t)dt[1];
+        sid_nmf_opts no;
+        nmf_opts(o, &no);
+        const mxGPUArray *act = NULL, *ym = NULL, *hl = NULL;
+        mxArray* tmp_act = NULL;
+        if (o && mxIsStruct(o)) {
+            const mxArray* f;
+            if (tu && (f = mxGetField(o, 0, "active")) && !mxIsEmpty(f)) {
+                /* logical P-vector -> uint8 gpuArray */
+                tmp_act = mxCreateNumericMatrix((mwSize)P, 1, mxUINT8_CLASS, mxREAL);
+                const mxLogical* src = mxGetLogicals(f);
+                uint8_t* dst = (uint8_t*)mxGetData(tmp_act);
+                for (int64_t i = 0; i < P; ++i) dst[i] = src[i] ? 1 : 0;
+                act = mxGPUCreateFromMxArray(tmp_act);
+            }
+            if ((f = mxGetField(o, 0, "Y")) && !mxIsEmpty(f) && no.use_std) ym = mxGPUCreateFromMxArray(f);
+            if (!tu && (f = mxGetField(o, 0, "hilf")) && !mxIsEmpty(f)) hl = mxGPUCreateFromMxArray(f);
+        }
+        int rc;
+        if (tu)
+            rc = sid_t_update(ctx(cmd), mxGPUGetDataReadOnly(Y), ydtype(Y), (float*)mxGPUGetData(T),
+                              (float*)mxGPUGetData(S), P, R, F, act ? (const uint8_t*)mxGPUGetDataReadOnly(act) : NULL,
+                              ym ? (const float*)mxGPUGetDataReadOnly(ym) : NULL, &no, SID_PREC_SPLIT, NULL);
+        else
+            rc = sid_s_update(ctx(cmd), mxGPUGetDataReadOnly(Y), ydtype(Y), (float*)mxGPUGetData(S),
+                              (float*)mxGPUGetData(T), P, R, F, ym ? (const float*)mxGPUGetDataReadOnly(ym) : NULL,
+                              hl ? (const float*)mxGPUGetDataReadOnly(hl) : NULL, &no, SID_PREC_SPLIT, NULL);
+        if (rc == SID_OK) rc = sid_ctx_sync(g_ctx, NULL);
+        mxGPUDestroyGPUArray(Y);
+        mxGPUDestroyGPUArray(A1);
+        mxGPUDestroyGPUArray(A2);
+        if (act) mxGPUDestroyGPUArray(act);
+        if (tmp_act) mxDestroyArray(tmp_act);
+        if (ym) mxGPUDestroyGPUArray(ym);
+        if (hl) mxGPUDestroyGPUArray(hl);
+        if (rc != SID_OK) {
+            mxGPUDestroyGPUArray(S);
+            mxGPUDestroyGPUArray(T);
+            check(rc, cmd);
+        }
+        plhs[0] = mxGPUCreateMxArrayOnGPU(S);
+        if (nlhs > 1) plhs[1] = mxGPUCreateMxArrayOnGPU(T);
+        mxGPUDestroyGPUArray(S);
+        mxGPUDestroyGPUArray(T);
+        return;
+    }
+    if (!strcmp(cmd, "quantile")) {
+        /* q = sid_mex('quantile', x, p): x single gpuArray, p double vector */
+        const mxGPUArray* x = gpu_arg(prhs[1], 0, cmd);
+        const int np = (int)mxGetNumberOfElements(prhs[2]);
+        plhs[0] = mxCreateDoubleMatrix(1, (mwSize)np, mxREAL);
+        const int rc = sid_quantile(ctx(cmd), (const float*)mxGPUGetDataReadOnly(x),
+                                    (int64_t)mxGPUGetNumberOfElements(x), NULL, mxGetPr(prhs[2]), np,
+                                    mxGetPr(plhs[0]), NULL);
+        mxGPUDestroyGPUArray(x);
+        check(rc, cmd);
+        return;
+    }
+    if (!strcmp(cmd, "pinv_create")) {
+        /* h = sid_mex('pinv_create', F): F K x P single gpuArray (the forward model) */
+        const mxGPUArray* F = gpu_arg(prhs[1], 0, cmd);
+        const mwSize* d = mxGPUGetDimensions(F);
+        int slot = -1;
+        for (int i = 0; i < MAX_PINV; ++i)
+            if (!g_pinv[i]) { slot = i; break; }
+        if (slot < 0) {
+            mxGPUDestroyGPUArray(F);
+            mexErrMsgIdAndTxt("sid:pinv", "too many extraction handles");
+        }
+        const int rc = sid_pinv_create(ctx(cmd), (const float*)mxGPUGetDataReadOnly(F), (int64_t)d[0],
+                                       (int64_t)d[1], 0, SID_PREC_SPLIT, &g_pinv[slot], NULL);
+        g_pinv_K[slot] = (int64_t)d[0];
+        mxGPUDestroyGPUArray(F);
+        check(rc, cmd);
+        plhs[0] = mxCreateDoubleScalar((double)slot);
+        return;
+    }
+    if (!strcmp(cmd, "pinv_apply")) {
+        /* T = sid_mex('pinv_apply', h, Y, baseline): Y P x n single/half gpuArray, baseline n single gpuArray or [] */
+        const int h = (int)mxGetScalar(prhs[1]);
+        if (h < 0 || h >= MAX_PINV || !g_pinv[h]) mexErrMsgIdAndTxt("sid:pinv", "invalid extraction handle");
+        const mxGPUArray* Y = gpu_arg(prhs[2], 1, cmd);
+        const mwSize* dy = mxGPUGetDimensions(Y);
+        const int64_t n = (int64_t)dy[1];
+        const mxGPUArray* b = (nrhs > 3 && !mxIsEmpty(prhs[3])) ? gpu_arg(prhs[3], 0, cmd) : NULL;
+        mwSize dt[2] = {(mwSize)g_pinv_K[h], (mwSize)n};
+        mxGPUArray* T = mxGPUCreateGPUArray(2, dt, mxSINGLE_CLASS, mxREAL, MX_GPU_DO_NOT_INITIALIZE);
+        int rc = sid_pinv_apply(g_pinv[h], mxGPUGetDataReadOnly(Y), ydtype(Y), n,
+                                b ? (const float*)mxGPUGetDataReadOnly(b) : NULL, (float*)mxGPUGetData(T),
+                                g_pinv_K[h], NULL);
+        if (rc == SID_OK) rc = sid_ctx_sync(g_ctx, NULL);
+        mxGPUDestroyGPUArray(Y);
+        if (b) mxGPUDestroyGPUArray(b);
+        if (rc != SID_OK) mxGPUDestroyGPUArray(T);
+        check(rc, cmd);
+        plhs[0] = mxGPUCreateMxArrayOnGPU(T);
+        mxGPUDestroyGPUArray(T);
+        return;
+    }
+    if (!strcmp(cmd, "pinv_destroy")) {
+        const int h = (int)mxGetScalar(prhs[1]);
+        if (h >= 0 && h < MAX_PINV && g_pinv[h]) {
+            sid_pinv_destroy(g_pinv[h]);
+            g_pinv[h] = NULL;
+        }
+        return;
+    }
+    if (!strcmp(cmd, "reconstruct")) {
+        /* [X, lam] = sid_mex('reconstruct', plan, img, microlenses, opts, method): img X x Y single gpuArray */
+        sid_plan* p = plan_arg(prhs[1]);
+        const mxGPUArray* img = gpu_arg(prhs[2], 0, cmd);
+        const mxGPUArray* ml = NULL;
+        mxArray* tmp_ml = NULL;
+        if (nrhs > 3 && !mxIsEmpty(prhs[3])) {
+            const mwSize nm = mxGetNumberOfElements(prhs[3]);
+            tmp_ml = mxCreateNumericMatrix(nm, 1, mxUINT8_CLASS, mxREAL);
+            uint8_t* dst = (uint8_t*)mxGetData(tmp_ml);
+            for (mwSize i = 0; i < nm; ++i) dst[i] = mxGetPr(prhs[3])[i] != 0.0;
+            ml = mxGPUCreateFromMxArray(tmp_ml);
+        }
+        const mxArray* o = nrhs > 4 ? prhs[4] : NULL;
+        sid_recon_opts ro;
+        sid_recon_defaults(&ro);
+        ro.q = field_or(o, "q", ro.q);
+        ro.lamb_L1 = field_or(o, "lamb_L1", ro.lamb_L1);
+        ro.lamb_L2 = field_or(o, "lamb_L2", ro.lamb_L2);
+        ro.max_iter = (int)field_or(o, "max_iter", ro.max_iter);
+        if (o && mxIsStruct(o)) {
+            const mxArray* w = mxGetField(o, 0, "whichSolver");
+            char sv[16] = "fast_nnls";
+            if (w && mxIsChar(w)) mxGetString(w, sv, sizeof(sv));
+            ro.solver = !strcmp(sv, "ISRA") ? 1 : 0;
+        }
+        int64_t info[12];
+        sid_plan_info(p, info);
+        mwSize dv[3] = {(mwSize)info[3], (mwSize)info[4], (mwSize)info[2]};
+        mxGPUArray* X = mxGPUCreateGPUArray(3, dv, mxSINGLE_CLASS, mxREAL, MX_GPU_DO_NOT_INITIALIZE);
+        double lam = 0.0;
+        int rc = sid_reconstruct_component(p, method_arg(nrhs, prhs, 5), (const float*)mxGPUGetDataReadOnly(img),
+                                           ml ? (const uint8_t*)mxGPUGetDataReadOnly(ml) : NULL, &ro,
+                                           (float*)mxGPUGetData(X), &lam, NULL);
+        if (rc == SID_OK) rc = sid_plan_sync(p, NULL);
+        mxGPUDestroyGPUArray(img);
+        if (ml) mxGPUDestroyGPUArray(ml);
+        if (tmp_ml) mxDestroyArray(tmp_ml);
+        if (rc != SID_OK) mxGPUDestroyGPUArray(X);
+        check(rc, cmd);
+        plhs[0] = mxGPUCreateMxArrayOnGPU(X);
+        if (nlhs > 1) plhs[1] = mxCreateDoubleScalar(lam);
+        mxGPUDestroyGPUArray(X);
         return;
     }
     mexErrMsgIdAndTxt("sid:usage", "unknown command '%s'", cmd);

@@ -79,7 +79,9 @@ def small(gpu, oracle):
 @pytest.mark.gpu
 @pytest.mark.parametrize("method,opts,tol", [
     ("direct", {}, 1e-4),
-    ("spectral_f32", {"lamb_L1": 1e-3, "lamb_L2": 1e-2}, 1e-4),
+    # Htf of a unit-norm image is ~0.02 here: an L1 weight of 2e-5 is the 0.1 %
+    # threshold the LS_deconv parity test uses on unnormalised data
+    ("spectral_f32", {"lamb_L1": 2e-5, "lamb_L2": 1e-2}, 1e-4),
     ("spectral_mixed", {"q": 0.5}, 1e-3),
     ("direct", {"whichSolver": "ISRA", "max_iter": 6}, 1e-4),
 ])
