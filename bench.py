@@ -42,6 +42,9 @@ def parse():
                     help="other methods timed after the main region (comma list, '' for none)")
     ap.add_argument("--compare-steps", type=int, default=3)
     ap.add_argument("--config", default="cfg1", choices=["cfg0", "cfg1"])
+    ap.add_argument("--depths", type=int, default=0,
+                    help="keep only the first Z depth planes (a smaller case of the same lateral geometry, for "
+                         "profiling captures; the line then names the reduced workload)")
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="budget of the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-nnls", action="store_true", help="skip the library + temporal NNLS measurement")
@@ -57,9 +60,13 @@ def dist_env():
     return rank, world, local
 
 
-def workload(config):
+def workload(config, depths=0):
+    import numpy as np
     from sid_gb300 import synthetic
     H, V = synthetic.config_inputs(config)
+    if depths and depths < H.shape[4]:
+        H = np.asfortranarray(H[..., :depths])
+        V = np.asfortranarray(V[..., :depths])
     return H, V
 
 
@@ -294,7 +301,7 @@ def main():
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
-    H, Vt = workload(args.config)
+    H, Vt = workload(args.config, args.depths)
     X, Y, Z = Vt.shape
     methods = [args.method] + [m for m in args.compare.split(",") if m and m != args.method]
     plan_methods = list(methods)
@@ -308,14 +315,16 @@ def main():
     X0 = Htf.clone()
     torch.cuda.synchronize()
 
-    def step(x, m):
+    def iterate(x, m, k):
+        # k ISRA iterations in one deconvRL call (the reference runs maxIter = 8..30
+        # iterations per call, reconstruct_S.m:195): the volume <-> polyphase
+        # conversions happen once per call, every iteration is a full step
         from sid_gb300 import _lib
-        _lib.call("sid_deconv_isra", P._plan, _lib.METHODS[m], Htf.data_ptr(), x.data_ptr(), 1, 0.0,
+        _lib.call("sid_deconv_isra", P._plan, _lib.METHODS[m], Htf.data_ptr(), x.data_ptr(), k, 0.0,
                   s.lfm._stream_ptr())
 
     x = X0.clone()
-    for _ in range(args.warmup):
-        step(x, args.method)
+    iterate(x, args.method, args.warmup)
     torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
@@ -326,8 +335,7 @@ def main():
     with Clocks(local) as clk:
         torch.cuda.synchronize()
         e0.record(stream)
-        for _ in range(args.steps):
-            step(x, args.method)
+        iterate(x, args.method, args.steps)
         e1.record(stream)
         torch.cuda.synchronize()
     P.timing(False)
@@ -392,13 +400,12 @@ def main():
     others = {}
     for m in methods[1:]:
         xm = X0.clone()
-        step(xm, m)
+        iterate(xm, m, 1)
         torch.cuda.synchronize()
         a = torch.cuda.Event(enable_timing=True)
         b = torch.cuda.Event(enable_timing=True)
         a.record(stream)
-        for _ in range(args.compare_steps):
-            step(xm, m)
+        iterate(xm, m, args.compare_steps)
         b.record(stream)
         torch.cuda.synchronize()
         tm = a.elapsed_time(b) / args.compare_steps
@@ -418,7 +425,9 @@ def main():
                          f"columns, extrapolated; RL iteration = 2 projections"}
 
     if rank == 0:
-        launches_per_step = {"direct": 7, "spectral_f32": 10, "spectral_i16": 10, "spectral_mixed": 10}[args.method]
+        # per iteration: direct 4 (two projections with their depth reductions) or spectral 6
+        # (r2c, contraction, c2r for each projection), plus the ISRA update; 3 layout kernels per call
+        launches_per_iter = {"direct": 4, "spectral_f32": 7, "spectral_i16": 7, "spectral_mixed": 7}[args.method]
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
@@ -426,7 +435,8 @@ def main():
                                            "spectral_mixed": "f32 (16-bit forward / FP32 back-projection spectra)"}
             .get(args.method, "f32"),
             "data": "synthetic (seeded Gaussian PSF + blob volume, shapes of the 1005^2x31 configuration)",
-            "config": {"workload": f"{args.config}: ISRA iteration on 1005x1005x31, Nnum 15, PSF 345^2x15^2x31",
+            "config": {"workload": f"{args.config}: ISRA iteration on {X}x{Y}x{Z}, Nnum {info['Nnum']}, "
+                                   f"PSF {info['M']}^2x{info['Nnum']}^2x{Z}",
                        "method": args.method, "parallelism": "replicas" if world > 1 else "1 GPU",
                        "l2": "per-iteration working set (tap spectra, "
                              f"{nf * n_out * n_in * 8 / 1e9:.1f} GB FP32 / {nf * n_out * n_in * 4 / 1e9:.1f} GB 16-bit) "
@@ -436,7 +446,7 @@ def main():
             "e2e": {"value": 1.0 / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 2 * vol_bytes,
                     "d2h_bytes_per_step": vol_bytes,
                     "api": "sid_deconv_isra_host (pinned host arrays, maxIter=1 per step)"},
-            "gpu_launches": launches_per_step * args.steps,
+            "gpu_launches": launches_per_iter * args.steps + 3,
             "clocks": clk.summary(),
             "accuracy": {"fwd_rel_l2_vs_fp64_256px": fwd_err},
             "compare": others,

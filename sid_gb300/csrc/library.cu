@@ -48,54 +48,73 @@ __global__ void k_lib_average(const float* const* __restrict__ recon, const uint
     }
 }
 
-// One CTA per (neuron, output phase).  Output written to
-// out[n * ldn + pixel * ldp] with pixel = x + X*y.
+// One CTA per (neuron, output phase a'b'); output written to
+// out[n * ldn + pixel * ldp] with pixel = x + X*y.  Each thread owns up to PER
+// output lenslets (s, t) of the neuron's window.  Per depth c and input row
+// phase b the D x D tap arrays of all N input column phases a are staged in
+// shared memory inside a zero border of R taps (R = the box's lattice span), so
+// that for every box lattice point (u, v) the tap index of an output is its
+// fixed base plus a per-point offset: one add, one shared load and one FMA per
+// output and point, no range checks, two barriers per (c, b).
+template <int PER>
 __global__ void __launch_bounds__(256)
 k_lib_project(const float* __restrict__ taps, const float* __restrict__ packed, const LibBox* __restrict__ boxes,
-              int N, int D, int dlo, int64_t tbs, int Lx, int Ly, int64_t X, int64_t Y, float* __restrict__ out,
-              int64_t ldn, int64_t ldp)
+              int N, int D, int dlo, int R, int64_t tbs, int Lx, int Ly, int64_t X, int64_t Y,
+              float* __restrict__ out, int64_t ldn, int64_t ldp)
 {
-    extern __shared__ float tap[];  // D*D
+    extern __shared__ float tile[];  // [N][Dp][Dp], then DD ints: padded offset of tap r
+    const int Dp = D + 2 * R, tsz = Dp * Dp, DD = D * D;
+    int* padoff = reinterpret_cast<int*>(tile + N * tsz);
     const int n = blockIdx.x;
-    const int o = blockIdx.y;       // b'*N + a'
+    const int o = blockIdx.y;  // b'*N + a'
     const int bp = o / N, ap = o - (o / N) * N;
     const LibBox b = boxes[n];
     const int bw = b.x1 - b.x0, bh = b.y1 - b.y0;
     const int ns = b.s1 - b.s0, nt = b.t1 - b.t0;
     const int nl = ns * nt;
-    constexpr int PER = 8;  // output lenslets per thread
+    for (int i = threadIdx.x; i < N * tsz; i += blockDim.x) tile[i] = 0.f;
+    for (int r = threadIdx.x; r < DD; r += blockDim.x) padoff[r] = (r / D + R) * Dp + (r - (r / D) * D) + R;
+    int base[PER];
+    bool ok[PER];
     float acc[PER];
 #pragma unroll
-    for (int q = 0; q < PER; ++q) acc[q] = 0.f;
+    for (int q = 0; q < PER; ++q) {
+        const int l = threadIdx.x + q * blockDim.x;
+        ok[q] = l < nl;
+        const int ls = ok[q] ? l / nt : 0, lt = ok[q] ? l - (l / nt) * nt : 0;
+        base[q] = (ls + R) * Dp + (lt + R);
+        acc[q] = 0.f;
+    }
     for (int c = b.z0; c < b.z1; ++c) {
         for (int bb = 0; bb < N; ++bb) {
             // lattice rows v of phase bb inside the box: y = bb + N v in [y0, y1)
             const int vlo = (b.y0 - bb) > 0 ? (b.y0 - bb + N - 1) / N : 0;
             const int vhi = (b.y1 - 1 - bb) >= 0 ? (b.y1 - 1 - bb) / N : -1;
             if (vhi < vlo) continue;
+            __syncthreads();  // the previous row's taps are no longer read
+            const int64_t rowblk = ((int64_t)c * N + bb) * N;
+            for (int a = 0; a < N; ++a) {
+                const float* src = taps + ((rowblk + a) * N + bp) * tbs + (int64_t)ap * DD;
+                float* dst = tile + a * tsz;
+                for (int r = threadIdx.x; r < DD; r += blockDim.x) dst[padoff[r]] = src[r];
+            }
+            __syncthreads();
             for (int a = 0; a < N; ++a) {
                 const int ulo = (b.x0 - a) > 0 ? (b.x0 - a + N - 1) / N : 0;
                 const int uhi = (b.x1 - 1 - a) >= 0 ? (b.x1 - 1 - a) / N : -1;
                 if (uhi < ulo) continue;
-                const int64_t blk = (((int64_t)c * N + bb) * N + a) * N + bp;
-                __syncthreads();
-                for (int i = threadIdx.x; i < D * D; i += blockDim.x)
-                    tap[i] = taps[blk * tbs + (int64_t)ap * D * D + i];
-                __syncthreads();
+                const float* ta = tile + a * tsz;
                 for (int v = vlo; v <= vhi; ++v) {
                     const int y = bb + N * v;
+                    const int e2 = b.t0 - v - dlo;
+                    const float* prow = packed + b.off + bw * ((y - b.y0) + bh * (c - b.z0)) - b.x0;
                     for (int u = ulo; u <= uhi; ++u) {
-                        const int x = a + N * u;
-                        const float val = packed[b.off + (x - b.x0) + bw * ((y - b.y0) + bh * (c - b.z0))];
+                        const float val = prow[a + N * u];
                         if (val == 0.f) continue;
+                        const int off = (b.s0 - u - dlo) * Dp + e2;
 #pragma unroll
-                        for (int q = 0; q < PER; ++q) {
-                            const int l = threadIdx.x + q * blockDim.x;
-                            if (l >= nl) break;
-                            const int t = b.t0 + l % nt, s = b.s0 + l / nt;
-                            const int m1 = s - u - dlo, m2 = t - v - dlo;
-                            if (m1 >= 0 && m1 < D && m2 >= 0 && m2 < D) acc[q] = fmaf(val, tap[m1 * D + m2], acc[q]);
-                        }
+                        for (int q = 0; q < PER; ++q)
+                            if (ok[q]) acc[q] = fmaf(val, ta[base[q] + off], acc[q]);
                     }
                 }
             }
@@ -103,8 +122,8 @@ k_lib_project(const float* __restrict__ taps, const float* __restrict__ packed, 
     }
 #pragma unroll
     for (int q = 0; q < PER; ++q) {
+        if (!ok[q]) continue;
         const int l = threadIdx.x + q * blockDim.x;
-        if (l >= nl) break;
         const int t = b.t0 + l % nt, s = b.s0 + l / nt;
         const int64_t x = ap + (int64_t)N * s, y = bp + (int64_t)N * t;
         if (s < Lx && t < Ly && x < X && y < Y) out[(int64_t)n * ldn + (x + X * y) * ldp] = acc[q];
@@ -154,7 +173,7 @@ extern "C" int sid_library(sid_plan* p, const float* const* recon, int64_t n_com
     const int64_t N = p->N, D = p->g.D;
     std::vector<LibBox> boxes(n_neur);
     int64_t off = 0;
-    int max_nl = 0;
+    int max_nl = 0, span = 0;
     for (int64_t n = 0; n < n_neur; ++n) {
         int bx[6];
         neuron_box(centers, n_neur, n, neur_rad, axial, p->X, p->Y, p->Z, bx);
@@ -176,10 +195,14 @@ extern "C" int sid_library(sid_plan* p, const float* const* recon, int64_t n_com
         b.t0 = (int)std::max<int64_t>(0, vmin + p->g.dlo);
         b.t1 = (int)std::min<int64_t>(p->Ly, vmax + p->g.dhi + 1);
         max_nl = std::max(max_nl, (b.s1 - b.s0) * (b.t1 - b.t0));
+        span = std::max(span, std::max(umax - umin, vmax - vmin));
         boxes[n] = b;
     }
     SID_REQUIRE(off < INT32_MAX, "sid_library: boxes too large");
     SID_REQUIRE(max_nl <= 256 * 8, "sid_library: neuron radius too large for one CTA (%d output lenslets)", max_nl);
+    const int Dp = (int)D + 2 * span;
+    const size_t tile_bytes = (size_t)N * Dp * Dp * sizeof(float) + (size_t)(D * D) * sizeof(int);
+    SID_REQUIRE(tile_bytes <= 200 * 1024, "sid_library: tap tiles (%zu bytes) exceed shared memory", tile_bytes);
     DBuf& dbox = p->ws[3];
     DBuf& dpack = p->ws[2];
     DBuf& dmeta = p->ws[1];
@@ -198,10 +221,17 @@ extern "C" int sid_library(sid_plan* p, const float* const* recon, int64_t n_com
     const int64_t tbs = cdiv(N * D * D, 32) * 32;
     const int64_t ldn = out_layout == 0 ? 1 : P, ldp = out_layout == 0 ? n_neur : 1;
     dim3 grid((unsigned)n_neur, (unsigned)(N * N));
-    k_lib_project<<<grid, 256, (size_t)(D * D) * sizeof(float), st>>>(
-        p->taps_f.as<float>(), dpack.as<float>(), dbox.as<LibBox>(), (int)N, (int)D, (int)p->g.dlo, tbs, (int)p->Lx,
-        (int)p->Ly, p->X, p->Y, out, ldn, ldp);
-    SID_CHECK_LAUNCH();
+    auto launch = [&](auto kern) -> int {
+        SID_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tile_bytes));
+        kern<<<grid, 256, tile_bytes, st>>>(p->taps_f.as<float>(), dpack.as<float>(), dbox.as<LibBox>(), (int)N,
+                                            (int)D, (int)p->g.dlo, span, tbs, (int)p->Lx, (int)p->Ly, p->X, p->Y,
+                                            out, ldn, ldp);
+        SID_CHECK_LAUNCH();
+        return SID_OK;
+    };
+    if (max_nl <= 256 * 2) SID_TRY(launch(k_lib_project<2>));
+    else if (max_nl <= 256 * 4) SID_TRY(launch(k_lib_project<4>));
+    else SID_TRY(launch(k_lib_project<8>));
     // the staging buffers are read by the kernels above: wait before the host
     // vectors go out of scope and before the workspaces can be reused
     SID_CUDA_TRY(cudaStreamSynchronize(st));

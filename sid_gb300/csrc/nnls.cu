@@ -6,14 +6,15 @@
 //   G d     (contraction: tcgen05 split precision, or FP32 SIMT)
 //   step:   alpha = s1 / sum(d .* G d), x_new = max(x - alpha d, 0),
 //           step = x_new - x, convergence statistic of the step
-//   G step  (contraction)
-//   update: df = df + G step
+//   G step  (contraction; the next iteration's mask kernel applies
+//            df = df + G step before it reads df)
 //   retire: the reference's log-linear extrapolation test
-// The iterate x and the gradient df are FP64 and the gradient is updated
-// incrementally (fast_nnls.m:153 does exactly this; LS_nnls.m:119 recomputes
-// df = -h + G x, which is the same quantity): the contraction's rounding then
-// shrinks with the steps, so the step statistics keep falling as they do in
-// the reference's FP64 arithmetic and its convergence test can fire.  With a
+// The iterate x and the gradient df are double-float (about 44 significant
+// bits, FP32 arithmetic) and the gradient is updated incrementally
+// (fast_nnls.m:153 does exactly this; LS_nnls.m:119 recomputes df = -h + G x,
+// which is the same quantity): the contraction's rounding then shrinks with
+// the steps, so the step statistics keep falling as they do in the
+// reference's FP64 arithmetic and its convergence test can fire.  With a
 // gradient recomputed from a 16- or 32-bit product every iteration the steps
 // stall at the product's noise floor and no column ever retires early.
 //
@@ -53,8 +54,29 @@ struct NnlsCounters {
 
 enum { SOLVER_LS = 0, SOLVER_FAST = 1 };
 
+// Double-float numbers: value = hi + lo with |lo| <= ulp(hi)/2 (about 44
+// significant bits), updated with error-free FP32 transformations (TwoSum,
+// then a Fast2Sum renormalisation).  The NNLS iterate and gradient need more
+// than FP32 (the reference's log-linear retirement test resolves steps far
+// below FP32 resolution of the gradient), and GB300's FP64 pipe runs at a
+// small fraction of its FP32 rate.
+__device__ __forceinline__ float2 dd_add(float2 a, float b)
+{
+    const float s = a.x + b;
+    const float bb = s - a.x;
+    const float e = ((a.x - (s - bb)) + (b - bb)) + a.y;
+    const float hi = s + e;
+    return make_float2(hi, e - (hi - s));
+}
+__device__ __forceinline__ float2 dd_from(double v)
+{
+    const float hi = (float)v;
+    return make_float2(hi, (float)(v - (double)hi));
+}
+__device__ __forceinline__ double dd_to(float2 a) { return (double)a.x + (double)a.y; }
+
 struct ColBufs {
-    double *x, *df;      // K x F FP64 iterate and gradient
+    float2 *x, *df;      // K x F double-float iterate and gradient
     float* v;            // K x F FP32 operand of the next contraction (SIMT path)
     uint16_t *vhi, *vlo; // K x F BF16 split operand, K-blocked (tensor-core path)
     float* g;            // K x F contraction result
@@ -68,17 +90,17 @@ struct ColBufs {
 };
 
 // write the next contraction operand: FP32 copy or BF16 hi/lo split
-__device__ __forceinline__ void put_operand(const ColBufs& b, int64_t o, int j, int k, double val)
+__device__ __forceinline__ void put_operand(const ColBufs& b, int64_t o, int j, int k, float val)
 {
     if (b.vhi) {
         // K-blocked layout of the tensor-core GEMM: ((k/64)*F + j)*64 + k%64
         const int64_t i = (((int64_t)(k >> 6) * b.F + j) << 6) + (k & 63);
-        const float f = (float)val;
+        const float f = val;
         const __nv_bfloat16 h = __float2bfloat16_rn(f);
         b.vhi[i] = __bfloat16_as_ushort(h);
         b.vlo[i] = __bfloat16_as_ushort(__float2bfloat16_rn(f - __bfloat162float(h)));
     } else {
-        b.v[o + k] = (float)val;
+        b.v[o + k] = val;
     }
 }
 
@@ -98,34 +120,75 @@ __device__ __forceinline__ double warp_max_d(double v)
     return v;
 }
 
-// Column kernels: one warp per frame column (8 columns per 256-thread CTA),
-// lanes stride over the K components, warp-shuffle reductions.
-constexpr int kColsPerCta = 8;
+// Column kernels: four warps per frame column (two columns per 256-thread
+// CTA), lanes stride over the K components; warp-shuffle reductions, then one
+// shared-memory exchange across the column's warps.  Inactive columns skip
+// the work but still reach the barriers.
+constexpr int kWarpsPerCol = 4;
+constexpr int kColsPerCta = 2;
+constexpr int kColThreads = 32 * kWarpsPerCol;
 
-// passive / masked gradient (LS_nnls.m:120-121, fast_nnls.m:100,163)
-__global__ void __launch_bounds__(256) k_nn_mask(ColBufs b, int K, int F)
+struct ColIdx {
+    int cl, wc, lane, j;
+};
+
+__device__ __forceinline__ ColIdx col_idx()
 {
-    const int j = blockIdx.x * kColsPerCta + (threadIdx.x >> 5);
-    const int lane = threadIdx.x & 31;
-    if (j >= F || !b.active[j]) return;
-    const int64_t o = (int64_t)j * K;
-    double acc = 0.0, np = 0.0, mx = -INFINITY;
-    for (int k = lane; k < K; k += 32) {
-        const double xv = b.x[o + k], dv = b.df[o + k];
-        const bool p = xv > 0.0 || dv < 0.0;
-        const double dm = p ? dv : 0.0;
-        put_operand(b, o, j, k, dm);
-        acc += dm * dm;
-        np += p ? 1.0 : 0.0;
-        mx = fmax(mx, xv);
+    ColIdx c;
+    c.cl = threadIdx.x / kColThreads;
+    c.wc = (threadIdx.x >> 5) % kWarpsPerCol;
+    c.lane = threadIdx.x & 31;
+    c.j = blockIdx.x * kColsPerCta + c.cl;
+    return c;
+}
+
+// The pending gradient update df += G step of the previous iteration
+// (fast_nnls.m:153; the incremental form of LS_nnls.m:119), then the passive
+// set and masked gradient (LS_nnls.m:120-121, fast_nnls.m:100,163).  g holds
+// G step (zero before the first iteration).
+__global__ void __launch_bounds__(256) k_nn_mask(ColBufs b, int K, int F, int use_std)
+{
+    __shared__ double red[kColsPerCta][kWarpsPerCol][3];
+    const ColIdx c = col_idx();
+    const bool act = c.j < F && b.active[c.j];
+    float acc_f = 0.f, mx_f = -INFINITY;
+    int np_i = 0;
+    if (act) {
+        const int64_t o = (int64_t)c.j * K;
+#pragma unroll 2
+        for (int k = c.wc * 32 + c.lane; k < K; k += kColThreads) {
+            float g = b.g[o + k];
+            if (use_std) g -= b.gu[k];
+            const float2 xv = b.x[o + k];
+            const float2 dv = dd_add(b.df[o + k], g);
+            b.df[o + k] = dv;
+            const bool p = xv.x > 0.f || dv.x < 0.f;
+            const float dm = p ? dv.x + dv.y : 0.f;
+            put_operand(b, o, c.j, k, dm);
+            acc_f = fmaf(dm, dm, acc_f);
+            np_i += p ? 1 : 0;
+            mx_f = fmaxf(mx_f, xv.x);
+        }
     }
-    acc = warp_sum_d(acc);
-    np = warp_sum_d(np);
-    mx = warp_max_d(mx);
-    if (lane == 0) {
-        b.s1[j] = acc;
-        b.anyp[j] = np;
-        b.xmax[j] = mx;
+    const double acc = warp_sum_d((double)acc_f);
+    const double np = warp_sum_d((double)np_i);
+    const double mx = warp_max_d((double)mx_f);
+    if (c.lane == 0) {
+        red[c.cl][c.wc][0] = acc;
+        red[c.cl][c.wc][1] = np;
+        red[c.cl][c.wc][2] = mx;
+    }
+    __syncthreads();
+    if (act && c.wc == 0 && c.lane == 0) {
+        double s = 0.0, n = 0.0, m = -INFINITY;
+        for (int w = 0; w < kWarpsPerCol; ++w) {
+            s += red[c.cl][w][0];
+            n += red[c.cl][w][1];
+            m = fmax(m, red[c.cl][w][2]);
+        }
+        b.s1[c.j] = s;
+        b.anyp[c.j] = n;
+        b.xmax[c.j] = m;
     }
 }
 
@@ -134,64 +197,91 @@ __global__ void __launch_bounds__(256) k_nn_mask(ColBufs b, int K, int F)
 __global__ void __launch_bounds__(256) k_nn_step(ColBufs b, int K, int F, int solver, int sample, int tol_p,
                                                  int use_std)
 {
-    const int j = blockIdx.x * kColsPerCta + (threadIdx.x >> 5);
-    const int lane = threadIdx.x & 31;
-    if (j >= F || !b.active[j]) return;
-    const int64_t o = (int64_t)j * K;
-    double s2 = 0.0;
-    for (int k = lane; k < K; k += 32) {
-        const double xv = b.x[o + k], dv = b.df[o + k];
-        const double dm = (xv > 0.0 || dv < 0.0) ? dv : 0.0;
-        double g = (double)b.g[o + k];
-        if (use_std) g -= (double)b.gu[k];
-        s2 += dm * g;
-    }
-    s2 = warp_sum_d(s2);
-    double alpha = b.s1[j] / s2;
-    if (isnan(alpha)) alpha = 0.0;
-    double a1 = 0.0, a2 = 0.0;
-    for (int k = lane; k < K; k += 32) {
-        const double xv = b.x[o + k], dv = b.df[o + k];
-        const double dm = (xv > 0.0 || dv < 0.0) ? dv : 0.0;
-        double xn = xv - dm * alpha;
-        if (xn < 0.0) xn = 0.0;
-        const double stp = xn - xv;
-        b.x[o + k] = xn;
-        put_operand(b, o, j, k, stp);
-        if (solver == SOLVER_LS) {
-            a1 += stp;      // sum(x - x_)
-            a2 += xv * xv;  // sum(x_.^2)
-        } else {
-            a1 += (tol_p == 2) ? stp * stp : fabs(stp);
+    __shared__ double red[kColsPerCta][kWarpsPerCol][2];
+    const ColIdx c = col_idx();
+    const bool act = c.j < F && b.active[c.j];
+    const int64_t o = (int64_t)c.j * K;
+    float s2_f = 0.f;
+    if (act) {
+#pragma unroll 2
+        for (int k = c.wc * 32 + c.lane; k < K; k += kColThreads) {
+            const float2 xv = b.x[o + k], dv = b.df[o + k];
+            const float dm = (xv.x > 0.f || dv.x < 0.f) ? dv.x + dv.y : 0.f;
+            float g = b.g[o + k];
+            if (use_std) g -= b.gu[k];
+            s2_f = fmaf(dm, g, s2_f);
         }
     }
-    a1 = warp_sum_d(a1);
-    a2 = warp_sum_d(a2);
+    const double s2 = warp_sum_d((double)s2_f);
+    if (c.lane == 0) red[c.cl][c.wc][0] = s2;
+    __syncthreads();
+    double den = 0.0;
+    for (int w = 0; w < kWarpsPerCol; ++w) den += red[c.cl][w][0];
+    float a1_f = 0.f, a2_f = 0.f;
+    if (act) {
+        double alpha = b.s1[c.j] / den;
+        if (isnan(alpha)) alpha = 0.0;
+        const float alpha_f = (float)alpha;
+#pragma unroll 2
+        for (int k = c.wc * 32 + c.lane; k < K; k += kColThreads) {
+            const float2 xv = b.x[o + k], dv = b.df[o + k];
+            const float dm = (xv.x > 0.f || dv.x < 0.f) ? dv.x + dv.y : 0.f;
+            const float pstep = dm * alpha_f;
+            float2 xn = dd_add(xv, -pstep);
+            // the step x_new - x exactly: -alpha d, or -x where the bound clamps
+            float stp = -pstep;
+            if (xn.x < 0.f) {
+                xn = make_float2(0.f, 0.f);
+                stp = -(xv.x + xv.y);
+            }
+            b.x[o + k] = xn;
+            put_operand(b, o, c.j, k, stp);
+            if (solver == SOLVER_LS) {
+                a1_f += stp;                     // sum(x - x_)
+                a2_f = fmaf(xv.x, xv.x, a2_f);   // sum(x_.^2)
+            } else {
+                a1_f += (tol_p == 2) ? stp * stp : fabsf(stp);
+            }
+        }
+    }
+    const double a1 = warp_sum_d((double)a1_f);
+    const double a2 = warp_sum_d((double)a2_f);
+    __syncthreads();  // everyone has read the first exchange
+    if (c.lane == 0) {
+        red[c.cl][c.wc][0] = a1;
+        red[c.cl][c.wc][1] = a2;
+    }
+    __syncthreads();
     const int it = b.cnt->iter;
-    if (lane == 0 && (it & 1)) {
+    if (act && c.wc == 0 && c.lane == 0 && (it & 1)) {
+        double t1 = 0.0, t2 = 0.0;
+        for (int w = 0; w < kWarpsPerCol; ++w) {
+            t1 += red[c.cl][w][0];
+            t2 += red[c.cl][w][1];
+        }
         double t;
         int e;
         if (solver == SOLVER_LS) {
-            t = log(a1 * a1 / a2) / 2.0;  // LS_nnls.m:136
+            t = log(t1 * t1 / t2) / 2.0;  // LS_nnls.m:136
             e = (it - 1) / 2;
         } else {
-            t = (tol_p == 2) ? log(sqrt(a1)) : log(a1);  // fast_nnls.m:138-141
+            t = (tol_p == 2) ? log(sqrt(t1)) : log(t1);  // fast_nnls.m:138-141
             e = (it - 3) / 2;
         }
-        if (e >= 0) b.test[(int64_t)(e % sample) * F + j] = t;
+        if (e >= 0) b.test[(int64_t)(e % sample) * F + c.j] = t;
     }
 }
 
-// df = df + G step  (fast_nnls.m:153), active columns only
+// df = df + G x0 for a warm start with use_std (G x0 minus its column-sum term)
 __global__ void k_nn_update(ColBufs b, int K, int F, int use_std)
 {
     const int64_t n = (int64_t)K * F;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const int64_t j = i / K;
         if (!b.active[j]) continue;
-        double g = (double)b.g[i];
-        if (use_std) g -= (double)b.gu[i - j * K];
-        b.df[i] += g;
+        float g = b.g[i];
+        if (use_std) g -= b.gu[i - j * K];
+        b.df[i] = dd_add(b.df[i], g);
     }
 }
 
@@ -280,35 +370,35 @@ __global__ void k_nn_retire(ColBufs b, int32_t* __restrict__ iters, int K, int F
 
 // ------------------------------------------------------------ set-up kernels --
 // df = -(h - lambda) for LS_nnls (h = A'Y), df = hs .* (-h + lambda) for fast_nnls
-__global__ void k_df_init(const float* __restrict__ h, const float* __restrict__ hs, double* __restrict__ df, int K,
+__global__ void k_df_init(const float* __restrict__ h, const float* __restrict__ hs, float2* __restrict__ df, int K,
                           int64_t n, double lambda, int solver)
 {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const double hv = (double)h[i];
-        df[i] = (solver == SOLVER_LS) ? -(hv - lambda) : (double)hs[i % K] * (-hv + lambda);
+        df[i] = dd_from((solver == SOLVER_LS) ? -(hv - lambda) : (double)hs[i % K] * (-hv + lambda));
     }
 }
 
 // df += g (FP32 contraction of the start point), x given in FP32
-__global__ void k_add_g(double* __restrict__ df, const float* __restrict__ g, int64_t n)
+__global__ void k_add_g(float2* __restrict__ df, const float* __restrict__ g, int64_t n)
 {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        df[i] += (double)g[i];
+        df[i] = dd_add(df[i], g[i]);
 }
 
-__global__ void k_x_from(double* __restrict__ x, const float* __restrict__ src, const float* __restrict__ hs, int K,
+__global__ void k_x_from(float2* __restrict__ x, const float* __restrict__ src, const float* __restrict__ hs, int K,
                          int64_t n)
 {
     // x = src (LS_nnls start point) or diag(1./hs) * W (fast_nnls.m:72)
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        x[i] = hs ? (double)src[i] / (double)hs[i % K] : (double)src[i];
+        x[i] = dd_from(hs ? (double)src[i] / (double)hs[i % K] : (double)src[i]);
 }
 
-__global__ void k_x_out(float* __restrict__ X, const double* __restrict__ x, const float* __restrict__ hs, int K,
+__global__ void k_x_out(float* __restrict__ X, const float2* __restrict__ x, const float* __restrict__ hs, int K,
                         int64_t n)
 {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        X[i] = hs ? (float)((double)hs[i % K] * x[i]) : (float)x[i];
+        X[i] = hs ? (float)((double)hs[i % K] * dd_to(x[i])) : (float)dd_to(x[i]);
 }
 
 // use_std (LS_nnls.m:107): u = sum over active columns of the operand / F
@@ -422,8 +512,8 @@ static int alloc_work(sid_ctx* c, int64_t K, int64_t F, int sample, bool split, 
         SID_CUDA_TRY(cudaMemsetAsync(nn[9].p, 0, (size_t)blk16_elems(K, F) * 2, st));
     }
     ColBufs& b = w->b;
-    b.x = nn[0].as<double>();
-    b.df = nn[1].as<double>();
+    b.x = nn[0].as<float2>();
+    b.df = nn[1].as<float2>();
     b.v = nn[2].as<float>();
     b.g = nn[3].as<float>();
     b.test = nn[4].as<double>();
@@ -560,6 +650,10 @@ static int iterate(sid_ctx* c, NnlsWork& w, int64_t K, int64_t F, int solver, co
     SID_TRY(ensure_gemm_ws(c, K, F, w.split));
     // one contraction outside the capture configures the kernels
     SID_TRY(gmul(c, w, K, F, st));
+    // the mask kernel applies the previous iteration's df += G step from g:
+    // nothing is pending before the first iteration
+    SID_CUDA_TRY(cudaMemsetAsync(b.g, 0, (size_t)(K * F) * sizeof(float), st));
+    SID_CUDA_TRY(cudaMemsetAsync(b.gu, 0, (size_t)K * sizeof(float), st));
     SID_CUDA_TRY(cudaStreamSynchronize(st));
     const int use_std = (solver == SOLVER_LS && o->use_std) ? 1 : 0;
     const int max_iter = (int)o->max_iter;
@@ -577,15 +671,13 @@ static int iterate(sid_ctx* c, NnlsWork& w, int64_t K, int64_t F, int solver, co
     auto body = [&](cudaStream_t s) -> int {
         k_iter_inc<<<1, 1, 0, s>>>(b.cnt);
         SID_CHECK_LAUNCH();
-        k_nn_mask<<<(unsigned)cdiv(F, kColsPerCta), 256, 0, s>>>(b, (int)K, (int)F);
+        k_nn_mask<<<(unsigned)cdiv(F, kColsPerCta), kColsPerCta * kColThreads, 0, s>>>(b, (int)K, (int)F, use_std);
         SID_CHECK_LAUNCH();
         SID_TRY(gmul_std(s));
-        k_nn_step<<<(unsigned)cdiv(F, kColsPerCta), 256, 0, s>>>(b, (int)K, (int)F, solver, sample, (int)o->tol_p,
-                                                                    use_std);
+        k_nn_step<<<(unsigned)cdiv(F, kColsPerCta), kColsPerCta * kColThreads, 0, s>>>(
+            b, (int)K, (int)F, solver, sample, (int)o->tol_p, use_std);
         SID_CHECK_LAUNCH();
-        SID_TRY(gmul_std(s));
-        k_nn_update<<<2048, 256, 0, s>>>(b, (int)K, (int)F, use_std);
-        SID_CHECK_LAUNCH();
+        SID_TRY(gmul_std(s));  // G step: applied by the next iteration's mask kernel
         k_nn_fit<<<cdiv(F, 256), 256, 0, s>>>(b, (int)F, solver, sample, max_iter, use_std);
         SID_CHECK_LAUNCH();
         if (solver == SOLVER_LS) {

@@ -269,6 +269,7 @@ k_dft_r2c(const float* __restrict__ in, float2* __restrict__ out, const float2* 
             for (int j = 0; j < 8; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
             const float* ap = img + vb * 8;
             const float2* cp = C1 + fb * 2;
+#pragma unroll 2
             for (int u = 0; u < d.Lx; ++u) {
                 const float4 a0 = *reinterpret_cast<const float4*>(ap + u * d.Lyp);
                 const float4 a1 = *reinterpret_cast<const float4*>(ap + u * d.Lyp + 4);
@@ -297,6 +298,7 @@ k_dft_r2c(const float* __restrict__ in, float2* __restrict__ out, const float2* 
             for (int j = 0; j < 8; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
             const float2* gp = G + fb * 2;
             const float2* wp = C2 + f2b * 8;
+#pragma unroll 2
             for (int v = 0; v < d.Ly; ++v) {
                 const float4 g = *reinterpret_cast<const float4*>(gp + v * d.H1p);
                 float2 w[8];
@@ -360,6 +362,7 @@ k_dft_c2r(const float2* __restrict__ in, float* __restrict__ out, const float2* 
             for (int j = 0; j < 8; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
             const float2* sp = S + fb * 2;
             const float2* wp = D1 + tb * 8;
+#pragma unroll 2
             for (int f2 = 0; f2 < L; ++f2) {
                 const float4 g = *reinterpret_cast<const float4*>(sp + f2 * d.H1p);
                 float2 w[8];
@@ -405,6 +408,7 @@ k_dft_c2r(const float2* __restrict__ in, float* __restrict__ out, const float2* 
             for (int j = 0; j < 8; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
             const float2* gp = Gt + tb * 8;
             const float2* ep = E + sb * 4;
+#pragma unroll 2
             for (int f1 = 0; f1 < H1; ++f1) {
                 float2 g[8];
 #pragma unroll

@@ -76,22 +76,56 @@ def small(gpu, oracle):
     return H, np.asfortranarray(img), P, fwd, bwd
 
 
+def _oracle_solve_from(oracle, Htf, nrm, fwd, bwd, opts):
+    """The part of reconstruct_S.m:193-205 after the back projection, in FP64."""
+    o = dict(opts)
+    o["lamb_L1"] = min(oracle.matlab_quantile(Htf, 1 - 1e-4), o.get("lamb_L1", 0.0))
+    if o.get("whichSolver", "fast_nnls") == "ISRA":
+        return nrm * oracle.deconvRL(fwd, bwd, Htf, o.get("max_iter", 8), Htf, o)
+    return nrm * oracle.LS_deconv(fwd, bwd, Htf, o)
+
+
 @pytest.mark.gpu
-@pytest.mark.parametrize("method,opts,tol", [
-    ("direct", {}, 1e-4),
-    # Htf of a unit-norm image is ~0.02 here: an L1 weight of 2e-5 is the 0.1 %
-    # threshold the LS_deconv parity test uses on unnormalised data
-    ("spectral_f32", {"lamb_L1": 2e-5, "lamb_L2": 1e-2}, 1e-4),
-    ("spectral_mixed", {"q": 0.5}, 1e-3),
-    ("direct", {"whichSolver": "ISRA", "max_iter": 6}, 1e-4),
-])
-def test_reconstruct_component_matches_oracle(small, oracle, method, opts, tol):
+@pytest.mark.parametrize("opts", [{}, {"whichSolver": "ISRA", "max_iter": 6}, {"lamb_L1": 1e-4, "lamb_L2": 1e-2}])
+def test_reconstruct_component_direct_matches_oracle(small, oracle, opts):
+    """FP32 direct projector: end to end against the FP64 oracle."""
     import sid_gb300 as s
     H, img, P, fwd, bwd = small
     ref = oracle.reconstruct_S_one(img, fwd, bwd, opts)
-    out, lam = P.reconstruct_component(img, None, opts, method=method, return_lambda=True)
-    assert rel_l2(s.to_numpy(out), ref) < tol, rel_l2(s.to_numpy(out), ref)
+    out, lam = P.reconstruct_component(img, None, opts, method="direct", return_lambda=True)
+    assert rel_l2(s.to_numpy(out), ref) < 1e-4, rel_l2(s.to_numpy(out), ref)
     assert lam <= opts.get("lamb_L1", 0.0)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("method,opts,tol", [
+    ("spectral_f32", {"lamb_L1": 2e-5, "lamb_L2": 1e-2}, 1e-5),
+    # ISRA divides by the back projection: the projector's absolute rounding at
+    # near-zero voxels is amplified there, hence the wider bar
+    ("spectral_f32", {"whichSolver": "ISRA", "max_iter": 6}, 1e-4),
+    ("spectral_mixed", {"q": 0.5}, 1e-4),
+])
+def test_reconstruct_component_spectral_stages(small, oracle, method, opts, tol):
+    """Spectral projectors, stage by stage.  Their rounding error is absolute
+    (spread over the field), so near-zero back-projection values change sign;
+    LS_deconv's first passive set (x > 0) depends on those signs, which moves
+    the reference's own solution by ~1e-3 between two such starting points
+    (measured).  So: the back projection is compared with the oracle's, and the
+    solve with the oracle's solve from the same back projection."""
+    import sid_gb300 as s
+    H, img, P, fwd, bwd = small
+    im = np.maximum(img.astype(np.float64) - oracle.matlab_quantile(img, opts.get("q", 0.8)), 0.0)
+    im = im / im.max()
+    nrm = np.sqrt(np.sum(im * im))
+    Htf = bwd(im / nrm)
+    o0 = dict(opts, max_iter=0)
+    if o0.get("whichSolver") == "ISRA":
+        o0.pop("whichSolver")
+    Hg = s.to_numpy(P.reconstruct_component(img, None, o0, method=method)).astype(np.float64) / nrm
+    assert rel_l2(Hg, Htf) < 1e-6, rel_l2(Hg, Htf)
+    out = s.to_numpy(P.reconstruct_component(img, None, opts, method=method))
+    ref = _oracle_solve_from(oracle, Hg, nrm, fwd, bwd, opts)
+    assert rel_l2(out, ref) < tol, rel_l2(out, ref)
 
 
 @pytest.mark.gpu
