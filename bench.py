@@ -37,7 +37,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="sid", choices=["sid", "reference"])
     ap.add_argument("--method", default="spectral_mixed",
-                    choices=["direct", "spectral_f32", "spectral_i16", "spectral_mixed"])
+                    choices=["direct", "spectral_f32", "spectral_i16", "spectral_mixed", "spectral_mixed_f32"])
     ap.add_argument("--compare", default="direct,spectral_f32",
                     help="other methods timed after the main region (comma list, '' for none)")
     ap.add_argument("--compare-steps", type=int, default=3)
@@ -58,6 +58,19 @@ def dist_env():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     return rank, world, local
+
+
+def replica_throughput(ms, steps, world, device):
+    """Whole-job throughput of `world` independent replicas (one per GPU, no
+    exchange step): the slowest rank's time (all-reduce MAX over the process
+    group) and world * steps iterations in that time."""
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([ms], device=device, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    return ms, world * steps / (ms / 1e3)
 
 
 def workload(config, depths=0):
@@ -342,23 +355,22 @@ def main():
     ms = e0.elapsed_time(e1)
     k_ms, k_n = P.timing_read()
     P.sync()
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms, value = replica_throughput(ms, args.steps, world, "cuda")
     ms_per_step = ms / args.steps
-    value = world * args.steps / (ms / 1e3)
 
     # roofline of the dominant kernel (the spectral contraction streams the tap spectra)
     n_out, n_in = info["Nnum"] ** 2, info["Nnum"] ** 2 * info["Z"]
     nf = (info["L"] // 2 + 1) * info["L"]
     hbm, peak_kind = peaks()
     roof = None
+    esz = {"spectral_f32": (8, 8), "spectral_i16": (4, 4), "spectral_mixed": (4, 6), "spectral_mixed_f32": (4, 8)}
+    ws_gb = nf * n_out * n_in * sum(esz.get(args.method, (0, 0))) / 1e9
+    if args.method == "direct":
+        ws_gb = info["device_bytes"] / 1e9  # the lenslet taps and workspaces
     if args.method.startswith("spectral") and k_n:
-        # per step one forward and one back-projection contraction; each streams
-        # its tap spectra once (4 bytes per complex entry in 16-bit, 8 in FP32)
-        esz_f = 4 if args.method in ("spectral_i16", "spectral_mixed") else 8
-        esz_b = 4 if args.method == "spectral_i16" else 8
+        # per step one forward and one back-projection contraction; each streams its
+        # tap spectra once (bytes per complex entry: 16-bit block float 4, 24-bit float 6, FP32 8)
+        esz_f, esz_b = esz[args.method]
         alg_bytes = (nf * n_out * n_in * (esz_f + esz_b) + 2 * nf * (n_in + n_out) * 8) / 2
         avg_s = k_ms / k_n / 1e3
         achieved = alg_bytes / avg_s / 1e9
@@ -427,19 +439,20 @@ def main():
     if rank == 0:
         # per iteration: direct 4 (two projections with their depth reductions) or spectral 6
         # (r2c, contraction, c2r for each projection), plus the ISRA update; 3 layout kernels per call
-        launches_per_iter = {"direct": 4, "spectral_f32": 7, "spectral_i16": 7, "spectral_mixed": 7}[args.method]
+        launches_per_iter = 4 if args.method == "direct" else 7
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": {"spectral_i16": "f32 (16-bit block-float spectra)",
-                                           "spectral_mixed": "f32 (16-bit forward / FP32 back-projection spectra)"}
+                                           "spectral_mixed": "f32 (16-bit forward / 24-bit float back-projection spectra)",
+                                           "spectral_mixed_f32": "f32 (16-bit forward / FP32 back-projection spectra)"}
             .get(args.method, "f32"),
             "data": "synthetic (seeded Gaussian PSF + blob volume, shapes of the 1005^2x31 configuration)",
             "config": {"workload": f"{args.config}: ISRA iteration on {X}x{Y}x{Z}, Nnum {info['Nnum']}, "
                                    f"PSF {info['M']}^2x{info['Nnum']}^2x{Z}",
                        "method": args.method, "parallelism": "replicas" if world > 1 else "1 GPU",
-                       "l2": "per-iteration working set (tap spectra, "
-                             f"{nf * n_out * n_in * 8 / 1e9:.1f} GB FP32 / {nf * n_out * n_in * 4 / 1e9:.1f} GB 16-bit) "
+                       "l2": "per-iteration working set (tap spectra streamed once per projection, "
+                             f"{ws_gb:.1f} GB per iteration) "
                              "exceeds L2; no flush needed"},
             "roofline": roof,
             "cpu_baseline": cpu,

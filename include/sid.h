@@ -38,19 +38,28 @@ enum {
 #define SID_PLAN_SPECTRAL_F32 0x2 /* lenslet-grid spectra, FP32 */
 #define SID_PLAN_SPECTRAL_I16 0x4 /* lenslet-grid spectra in 16-bit block floating point
                                      (int16 mantissas, one FP32 step per frequency row),
-                                     FP32 arithmetic: the mixed-precision form */
+                                     FP32 arithmetic: the forward of the mixed forms */
+#define SID_PLAN_SPECTRAL_F24 0x8 /* lenslet-grid spectra as 24-bit floats (sign, 8-bit
+                                     exponent, 15-bit mantissa: 16 significant bits),
+                                     FP32 arithmetic: the back projection of
+                                     SID_METHOD_SPECTRAL_MIXED */
 
 /* Projection methods. */
 #define SID_METHOD_DIRECT       0
 #define SID_METHOD_SPECTRAL_F32 1
 #define SID_METHOD_SPECTRAL_I16 2
-/* Forward projection with the 16-bit spectra, back projection with the FP32
- * spectra (needs both plan flags).  The 16-bit error is absolute (spread over
- * the whole sensor), which the forward image tolerates (no sensor pixel is near
- * zero) but a back projection does not: voxels whose PSF falls mostly outside
- * the sensor have back projections ~1e-9 of the maximum, and ISRA divides by
- * them (deconvRL.m:52).  This split keeps ISRA within the mixed-precision bar. */
+/* Forward projection with the 16-bit block-floating-point spectra, back
+ * projection with the 24-bit float spectra (plan flags SPECTRAL_I16 and
+ * SPECTRAL_F24).  The 16-bit error is absolute (relative to each frequency
+ * row's largest entry), which the forward image tolerates (no sensor pixel is
+ * near zero) but a back projection does not: ISRA divides by the back
+ * projection (deconvRL.m:52) and voxels whose PSF falls mostly outside the
+ * sensor have tiny back projections.  The 24-bit floats keep 16 significant
+ * bits of every entry, which holds ISRA within the mixed-precision bar. */
 #define SID_METHOD_SPECTRAL_MIXED 3
+/* The same with FP32 back-projection spectra (plan flags SPECTRAL_I16 and
+ * SPECTRAL_F32). */
+#define SID_METHOD_SPECTRAL_MIXED_F32 4
 
 typedef struct sid_plan sid_plan;
 

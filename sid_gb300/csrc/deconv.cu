@@ -19,6 +19,7 @@ int fwd_poly(sid_plan* p, int method, const float* vp, float* ip, cudaStream_t s
     case SID_METHOD_SPECTRAL_F32: return spectral_forward(p, false, vp, ip, st);
     case SID_METHOD_SPECTRAL_I16: return spectral_forward(p, true, vp, ip, st);
     case SID_METHOD_SPECTRAL_MIXED: return spectral_forward(p, true, vp, ip, st);
+    case SID_METHOD_SPECTRAL_MIXED_F32: return spectral_forward(p, true, vp, ip, st);
     default: set_error("unknown projection method %d", method); return SID_EINVAL;
     }
 }
@@ -27,9 +28,10 @@ int adj_poly(sid_plan* p, int method, const float* ip, float* bp, cudaStream_t s
 {
     switch (method) {
     case SID_METHOD_DIRECT: return direct_adjoint(p, ip, bp, p->errflag.as<int>(), st);
-    case SID_METHOD_SPECTRAL_F32: return spectral_adjoint(p, false, ip, bp, st);
-    case SID_METHOD_SPECTRAL_I16: return spectral_adjoint(p, true, ip, bp, st);
-    case SID_METHOD_SPECTRAL_MIXED: return spectral_adjoint(p, false, ip, bp, st);
+    case SID_METHOD_SPECTRAL_F32: return spectral_adjoint(p, FMT_F32, ip, bp, st);
+    case SID_METHOD_SPECTRAL_I16: return spectral_adjoint(p, FMT_I16, ip, bp, st);
+    case SID_METHOD_SPECTRAL_MIXED: return spectral_adjoint(p, FMT_F24, ip, bp, st);
+    case SID_METHOD_SPECTRAL_MIXED_F32: return spectral_adjoint(p, FMT_F32, ip, bp, st);
     default: set_error("unknown projection method %d", method); return SID_EINVAL;
     }
 }

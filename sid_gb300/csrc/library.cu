@@ -49,82 +49,86 @@ __global__ void k_lib_average(const float* const* __restrict__ recon, const uint
 }
 
 // One CTA per (neuron, output phase a'b'); output written to
-// out[n * ldn + pixel * ldp] with pixel = x + X*y.  Each thread owns up to PER
-// output lenslets (s, t) of the neuron's window.  Per depth c and input row
-// phase b the D x D tap arrays of all N input column phases a are staged in
-// shared memory inside a zero border of R taps (R = the box's lattice span), so
-// that for every box lattice point (u, v) the tap index of an output is its
-// fixed base plus a per-point offset: one add, one shared load and one FMA per
-// output and point, no range checks, two barriers per (c, b).
-template <int PER>
+// out[n * ldn + pixel * ldp] with pixel = x + X*y.  Each thread owns four
+// consecutive output lenslets (s, t..t+3) of the neuron's window.  Per depth c
+// and input row phase b the D x D tap arrays of all N input column phases a
+// are staged in shared memory inside a zero border of R taps (R = the box's
+// lattice span), so for every box lattice point (u, v) a thread's four taps
+// sit at one offset from its base: one address, four shared loads and four
+// FMAs per point, no range checks, two barriers per (c, b).  The lattice
+// ranges of every phase are computed once per CTA.
+constexpr int kLibT = 4;  // consecutive output lenslets per thread
+
 __global__ void __launch_bounds__(256)
 k_lib_project(const float* __restrict__ taps, const float* __restrict__ packed, const LibBox* __restrict__ boxes,
               int N, int D, int dlo, int R, int64_t tbs, int Lx, int Ly, int64_t X, int64_t Y,
               float* __restrict__ out, int64_t ldn, int64_t ldp)
 {
-    extern __shared__ float tile[];  // [N][Dp][Dp], then DD ints: padded offset of tap r
-    const int Dp = D + 2 * R, tsz = Dp * Dp, DD = D * D;
+    extern __shared__ float tile[];  // [N][Dp][Dp + 4], then DD ints (padded tap offsets), then 4N ints (ranges)
+    const int Dp = D + 2 * R, Dq = Dp + kLibT, tsz = Dp * Dq, DD = D * D;
     int* padoff = reinterpret_cast<int*>(tile + N * tsz);
+    int* rng = padoff + DD;  // ulo[a], uhi[a], vlo[b], vhi[b]
     const int n = blockIdx.x;
     const int o = blockIdx.y;  // b'*N + a'
     const int bp = o / N, ap = o - (o / N) * N;
     const LibBox b = boxes[n];
     const int bw = b.x1 - b.x0, bh = b.y1 - b.y0;
     const int ns = b.s1 - b.s0, nt = b.t1 - b.t0;
-    const int nl = ns * nt;
+    const int ntg = (nt + kLibT - 1) / kLibT;  // groups of kLibT along t
     for (int i = threadIdx.x; i < N * tsz; i += blockDim.x) tile[i] = 0.f;
-    for (int r = threadIdx.x; r < DD; r += blockDim.x) padoff[r] = (r / D + R) * Dp + (r - (r / D) * D) + R;
-    int base[PER];
-    bool ok[PER];
-    float acc[PER];
-#pragma unroll
-    for (int q = 0; q < PER; ++q) {
-        const int l = threadIdx.x + q * blockDim.x;
-        ok[q] = l < nl;
-        const int ls = ok[q] ? l / nt : 0, lt = ok[q] ? l - (l / nt) * nt : 0;
-        base[q] = (ls + R) * Dp + (lt + R);
-        acc[q] = 0.f;
+    for (int r = threadIdx.x; r < DD; r += blockDim.x) padoff[r] = (r / D + R) * Dq + (r - (r / D) * D) + R;
+    for (int ph = threadIdx.x; ph < N; ph += blockDim.x) {
+        // lattice columns u of phase ph in the box: x = ph + N u in [x0, x1); rows likewise
+        rng[ph] = (b.x0 - ph) > 0 ? (b.x0 - ph + N - 1) / N : 0;
+        rng[N + ph] = (b.x1 - 1 - ph) >= 0 ? (b.x1 - 1 - ph) / N : -1;
+        rng[2 * N + ph] = (b.y0 - ph) > 0 ? (b.y0 - ph + N - 1) / N : 0;
+        rng[3 * N + ph] = (b.y1 - 1 - ph) >= 0 ? (b.y1 - 1 - ph) / N : -1;
     }
+    const int g = threadIdx.x;
+    const bool ok = g < ns * ntg;
+    const int ls = ok ? g / ntg : 0, lt = ok ? (g - (g / ntg) * ntg) * kLibT : 0;
+    const int base = (ls + R) * Dq + (lt + R);
+    float acc[kLibT];
+#pragma unroll
+    for (int q = 0; q < kLibT; ++q) acc[q] = 0.f;
+    __syncthreads();
     for (int c = b.z0; c < b.z1; ++c) {
         for (int bb = 0; bb < N; ++bb) {
-            // lattice rows v of phase bb inside the box: y = bb + N v in [y0, y1)
-            const int vlo = (b.y0 - bb) > 0 ? (b.y0 - bb + N - 1) / N : 0;
-            const int vhi = (b.y1 - 1 - bb) >= 0 ? (b.y1 - 1 - bb) / N : -1;
+            const int vlo = rng[2 * N + bb], vhi = rng[3 * N + bb];
             if (vhi < vlo) continue;
             __syncthreads();  // the previous row's taps are no longer read
             const int64_t rowblk = ((int64_t)c * N + bb) * N;
             for (int a = 0; a < N; ++a) {
+                if (rng[N + a] < rng[a]) continue;
                 const float* src = taps + ((rowblk + a) * N + bp) * tbs + (int64_t)ap * DD;
                 float* dst = tile + a * tsz;
                 for (int r = threadIdx.x; r < DD; r += blockDim.x) dst[padoff[r]] = src[r];
             }
             __syncthreads();
+            if (!ok) continue;
             for (int a = 0; a < N; ++a) {
-                const int ulo = (b.x0 - a) > 0 ? (b.x0 - a + N - 1) / N : 0;
-                const int uhi = (b.x1 - 1 - a) >= 0 ? (b.x1 - 1 - a) / N : -1;
+                const int ulo = rng[a], uhi = rng[N + a];
                 if (uhi < ulo) continue;
-                const float* ta = tile + a * tsz;
+                const float* ta = tile + a * tsz + base;
                 for (int v = vlo; v <= vhi; ++v) {
-                    const int y = bb + N * v;
                     const int e2 = b.t0 - v - dlo;
-                    const float* prow = packed + b.off + bw * ((y - b.y0) + bh * (c - b.z0)) - b.x0;
+                    const float* prow = packed + b.off + bw * ((bb + N * v - b.y0) + bh * (c - b.z0)) - b.x0 + a;
                     for (int u = ulo; u <= uhi; ++u) {
-                        const float val = prow[a + N * u];
-                        if (val == 0.f) continue;
-                        const int off = (b.s0 - u - dlo) * Dp + e2;
+                        const float val = prow[N * u];
+                        const float* tp = ta + (b.s0 - u - dlo) * Dq + e2;
 #pragma unroll
-                        for (int q = 0; q < PER; ++q)
-                            if (ok[q]) acc[q] = fmaf(val, ta[base[q] + off], acc[q]);
+                        for (int q = 0; q < kLibT; ++q) acc[q] = fmaf(val, tp[q], acc[q]);
                     }
                 }
             }
         }
     }
+    if (!ok) return;
+    const int s = b.s0 + ls;
 #pragma unroll
-    for (int q = 0; q < PER; ++q) {
-        if (!ok[q]) continue;
-        const int l = threadIdx.x + q * blockDim.x;
-        const int t = b.t0 + l % nt, s = b.s0 + l / nt;
+    for (int q = 0; q < kLibT; ++q) {
+        const int t = b.t0 + lt + q;
+        if (lt + q >= nt) break;
         const int64_t x = ap + (int64_t)N * s, y = bp + (int64_t)N * t;
         if (s < Lx && t < Ly && x < X && y < Y) out[(int64_t)n * ldn + (x + X * y) * ldp] = acc[q];
     }
@@ -194,15 +198,15 @@ extern "C" int sid_library(sid_plan* p, const float* const* recon, int64_t n_com
         b.s1 = (int)std::min<int64_t>(p->Lx, umax + p->g.dhi + 1);
         b.t0 = (int)std::max<int64_t>(0, vmin + p->g.dlo);
         b.t1 = (int)std::min<int64_t>(p->Ly, vmax + p->g.dhi + 1);
-        max_nl = std::max(max_nl, (b.s1 - b.s0) * (b.t1 - b.t0));
+        max_nl = std::max(max_nl, (b.s1 - b.s0) * (int)cdiv(b.t1 - b.t0, kLibT));
         span = std::max(span, std::max(umax - umin, vmax - vmin));
         boxes[n] = b;
     }
     SID_REQUIRE(off < INT32_MAX, "sid_library: boxes too large");
-    SID_REQUIRE(max_nl <= 256 * 8, "sid_library: neuron radius too large for one CTA (%d output lenslets)", max_nl);
     const int Dp = (int)D + 2 * span;
-    const size_t tile_bytes = (size_t)N * Dp * Dp * sizeof(float) + (size_t)(D * D) * sizeof(int);
+    const size_t tile_bytes = (size_t)N * Dp * (Dp + kLibT) * sizeof(float) + (size_t)(D * D + 4 * N) * sizeof(int);
     SID_REQUIRE(tile_bytes <= 200 * 1024, "sid_library: tap tiles (%zu bytes) exceed shared memory", tile_bytes);
+    SID_REQUIRE(max_nl <= 256, "sid_library: neuron radius too large for one CTA (%d output groups)", max_nl);
     DBuf& dbox = p->ws[3];
     DBuf& dpack = p->ws[2];
     DBuf& dmeta = p->ws[1];
@@ -221,17 +225,11 @@ extern "C" int sid_library(sid_plan* p, const float* const* recon, int64_t n_com
     const int64_t tbs = cdiv(N * D * D, 32) * 32;
     const int64_t ldn = out_layout == 0 ? 1 : P, ldp = out_layout == 0 ? n_neur : 1;
     dim3 grid((unsigned)n_neur, (unsigned)(N * N));
-    auto launch = [&](auto kern) -> int {
-        SID_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tile_bytes));
-        kern<<<grid, 256, tile_bytes, st>>>(p->taps_f.as<float>(), dpack.as<float>(), dbox.as<LibBox>(), (int)N,
-                                            (int)D, (int)p->g.dlo, span, tbs, (int)p->Lx, (int)p->Ly, p->X, p->Y,
-                                            out, ldn, ldp);
-        SID_CHECK_LAUNCH();
-        return SID_OK;
-    };
-    if (max_nl <= 256 * 2) SID_TRY(launch(k_lib_project<2>));
-    else if (max_nl <= 256 * 4) SID_TRY(launch(k_lib_project<4>));
-    else SID_TRY(launch(k_lib_project<8>));
+    SID_CUDA_TRY(cudaFuncSetAttribute(k_lib_project, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tile_bytes));
+    k_lib_project<<<grid, 256, tile_bytes, st>>>(p->taps_f.as<float>(), dpack.as<float>(), dbox.as<LibBox>(), (int)N,
+                                                 (int)D, (int)p->g.dlo, span, tbs, (int)p->Lx, (int)p->Ly, p->X, p->Y,
+                                                 out, ldn, ldp);
+    SID_CHECK_LAUNCH();
     // the staging buffers are read by the kernels above: wait before the host
     // vectors go out of scope and before the workspaces can be reused
     SID_CUDA_TRY(cudaStreamSynchronize(st));

@@ -109,7 +109,7 @@ extern "C" int sid_plan_create(const float* H, int64_t M, int64_t Nnum, int64_t 
                 "sid_plan_create: sizes must be positive (M=%lld Nnum=%lld Z=%lld X=%lld Y=%lld)",
                 (long long)M, (long long)Nnum, (long long)Z, (long long)X, (long long)Y);
     SID_REQUIRE(Nnum <= 32, "sid_plan_create: Nnum=%lld exceeds 32", (long long)Nnum);
-    SID_REQUIRE((flags & (SID_PLAN_DIRECT | SID_PLAN_SPECTRAL_F32 | SID_PLAN_SPECTRAL_I16)) != 0,
+    SID_REQUIRE((flags & (SID_PLAN_DIRECT | SID_PLAN_SPECTRAL_F32 | SID_PLAN_SPECTRAL_I16 | SID_PLAN_SPECTRAL_F24)) != 0,
                 "sid_plan_create: flags select no operator form");
     std::vector<int> lo(Z), mc(Z), cf(Z), cb(Z);
     for (int64_t c = 0; c < Z; ++c) {
@@ -143,7 +143,7 @@ extern "C" int sid_plan_create(const float* H, int64_t M, int64_t Nnum, int64_t 
     }
     p->g = TapGeom{Nnum, Z, X, Y, p->Lx, p->Ly, dlo, dhi, dhi - dlo + 1};
     p->zsplit = 1;
-    p->L = 0; p->nf = 0; p->spec_f32 = p->spec_i16 = false;
+    p->L = 0; p->nf = 0; p->spec_f32 = p->spec_i16 = p->spec_f24 = false;
 
     if (p->errflag.alloc(sizeof(int)) != SID_OK || cudaMemset(p->errflag.p, 0, sizeof(int)) != cudaSuccess) {
         sid_plan_destroy(p);
@@ -165,7 +165,7 @@ extern "C" int sid_plan_create(const float* H, int64_t M, int64_t Nnum, int64_t 
     if (st == SID_OK && (flags & SID_PLAN_DIRECT))
         st = build_taps(p, dH.as<float>(), lo, mc, p->adj_separate ? cb : cf, p->taps_b, 1);
     dH.release();
-    if (st == SID_OK && (flags & (SID_PLAN_SPECTRAL_F32 | SID_PLAN_SPECTRAL_I16))) {
+    if (st == SID_OK && (flags & (SID_PLAN_SPECTRAL_F32 | SID_PLAN_SPECTRAL_I16 | SID_PLAN_SPECTRAL_F24))) {
         if (p->adj_separate) {
             set_error("sid_plan_create: the spectral form needs odd PSF crop widths "
                       "(even widths shift the reference's back projection by one pixel); "
@@ -183,8 +183,9 @@ extern "C" int sid_plan_create(const float* H, int64_t M, int64_t Nnum, int64_t 
 extern "C" int sid_plan_destroy(sid_plan* p)
 {
     if (!p) return SID_OK;
-    DBuf* bufs[] = {&p->taps_f, &p->taps_b, &p->khat_f32, &p->khat_i16, &p->rstep, &p->twiddle, &p->vp,
-                    &p->ip, &p->bp, &p->ipart, &p->vhat, &p->ihat, &p->bhat, &p->red, &p->errflag};
+    DBuf* bufs[] = {&p->taps_f, &p->taps_b, &p->khat_f32, &p->khat_i16, &p->rstep, &p->khat_f24h, &p->khat_f24l,
+                    &p->twiddle, &p->vp, &p->ip, &p->bp, &p->ipart, &p->vhat, &p->ihat, &p->bhat, &p->red,
+                    &p->errflag};
     for (DBuf* b : bufs) b->release();
     for (DBuf& b : p->ws) b.release();
     p->timer.release();
@@ -195,8 +196,9 @@ extern "C" int sid_plan_destroy(sid_plan* p)
 extern "C" int sid_plan_info(const sid_plan* p, int64_t* info)
 {
     SID_REQUIRE(p && info, "sid_plan_info: NULL argument");
-    const DBuf* bufs[] = {&p->taps_f, &p->taps_b, &p->khat_f32, &p->khat_i16, &p->rstep, &p->twiddle, &p->vp,
-                          &p->ip, &p->bp, &p->ipart, &p->vhat, &p->ihat, &p->bhat, &p->red};
+    const DBuf* bufs[] = {&p->taps_f, &p->taps_b, &p->khat_f32, &p->khat_i16, &p->rstep, &p->khat_f24h,
+                          &p->khat_f24l, &p->twiddle, &p->vp, &p->ip, &p->bp, &p->ipart, &p->vhat, &p->ihat,
+                          &p->bhat, &p->red};
     int64_t bytes = 0;
     for (const DBuf* b : bufs) bytes += (int64_t)b->bytes;
     for (const DBuf& b : p->ws) bytes += (int64_t)b.bytes;

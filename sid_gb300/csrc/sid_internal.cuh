@@ -137,6 +137,9 @@ struct sid_plan {
     sid::DBuf khat_f32;         // [f][b'a'][abc] float2
     sid::DBuf khat_i16;         // [f][b'a'][abc] short2 mantissas
     sid::DBuf rstep;            // [f][b'a'] step (rowmax/32767) of each 16-bit row
+    sid::DBuf khat_f24h;        // [f][b'a'][abc] 24-bit floats: high 16 bits of re, im
+    sid::DBuf khat_f24l;        // [f][b'a'][abc] 24-bit floats: low 8 bits of re, im
+    bool spec_f24;
     sid::DBuf twiddle;          // L float2: exp(-2 pi i k / L)
     // workspaces
     sid::DBuf vp, ip, bp, ipart, vhat, ihat, bhat, red;
@@ -151,7 +154,9 @@ namespace sid {
 int direct_forward(sid_plan* p, const float* vp, float* ip, int* err, cudaStream_t st);
 int direct_adjoint(sid_plan* p, const float* ip, float* bp, int* err, cudaStream_t st);
 int spectral_forward(sid_plan* p, bool i16, const float* vp, float* ip, cudaStream_t st);
-int spectral_adjoint(sid_plan* p, bool i16, const float* ip, float* bp, cudaStream_t st);
+// storage formats of the tap spectra
+enum SpecFmt { FMT_F32 = 0, FMT_I16 = 1, FMT_F24 = 2 };
+int spectral_adjoint(sid_plan* p, int fmt, const float* ip, float* bp, cudaStream_t st);
 int v_to_vp(const sid_plan* p, const float* V, float* vp, int64_t Z, cudaStream_t st);
 int vp_to_v(const sid_plan* p, const float* vp, float* V, int64_t Z, cudaStream_t st);
 int mask_vp(const sid_plan* p, float* vp, int64_t Z, cudaStream_t st);

@@ -28,14 +28,29 @@ static inline int64_t spec_nin_pad(const sid_plan* p) { return cdiv(p->N * p->N 
 // entries of every frequency row.
 //   mode 0: write FP32 spectra (if k32) and the per-row max |Re|,|Im| (rowmax,
 //           float bits, atomicMax; values are >= 0 so integer order = float order)
+//           and, when k24h is set, the 24-bit float planes (f24_split)
 //   mode 1: write 16-bit block-floating-point spectra: int16 mantissas with the
 //           row's step rstep[f*n_out + o] = rowmax/32767 (value = mantissa * step)
 constexpr int KB_CH = 8;
 
+// 24-bit floats: the top 24 bits of an FP32 value (sign, 8-bit exponent, 15
+// mantissa bits; round to nearest, ties to even) stored as a 16-bit high part
+// and an 8-bit low part.  The rounding increment is added to the magnitude bits
+// (sign and magnitude are separate in FP32), so a carry moves into the exponent
+// as it should; spectra are far from the largest finite float.
+__device__ __forceinline__ void f24_split(float v, unsigned short& hi, unsigned char& lo)
+{
+    unsigned u = __float_as_uint(v);
+    u += 0x7Fu + ((u >> 8) & 1u);
+    hi = (unsigned short)(u >> 16);
+    lo = (unsigned char)((u >> 8) & 0xFFu);
+}
+
 __global__ void k_build_khat(const float* __restrict__ taps, const float2* __restrict__ tw,
-                             float2* __restrict__ k32, short2* __restrict__ k16,
-                             unsigned int* __restrict__ rowmax, const float* __restrict__ rstep, int mode,
-                             int N, int n_in, int64_t n_in_pad, int D, int dlo, int L, int64_t tbs)
+                             float2* __restrict__ k32, short2* __restrict__ k16, ushort2* __restrict__ k24h,
+                             uchar2* __restrict__ k24l, unsigned int* __restrict__ rowmax,
+                             const float* __restrict__ rstep, int mode, int N, int n_in, int64_t n_in_pad, int D,
+                             int dlo, int L, int64_t tbs)
 {
     extern __shared__ float2 sm[];
     const int H1 = L / 2 + 1;
@@ -94,6 +109,14 @@ __global__ void k_build_khat(const float* __restrict__ taps, const float2* __res
         const int64_t idx = ((int64_t)f * n_out + o) * n_in_pad + k0 + ch;
         if (mode == 0) {
             if (live && k32) k32[idx] = acc;
+            if (live && k24h) {
+                unsigned short hr, hi_;
+                unsigned char lr, li;
+                f24_split(acc.x, hr, lr);
+                f24_split(acc.y, hi_, li);
+                k24h[idx] = make_ushort2(hr, hi_);
+                k24l[idx] = make_uchar2(lr, li);
+            }
             float m = fmaxf(fabsf(acc.x), fabsf(acc.y));
 #pragma unroll
             for (int off = KB_CH / 2; off > 0; off >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, off));
@@ -142,6 +165,13 @@ int build_spectra(sid_plan* p)
         SID_CUDA_TRY(cudaMemset(p->khat_f32.p, 0, nent * sizeof(float2)));
         p->spec_f32 = true;
     }
+    if (p->flags & SID_PLAN_SPECTRAL_F24) {
+        SID_TRY(p->khat_f24h.alloc(nent * sizeof(ushort2)));
+        SID_TRY(p->khat_f24l.alloc(nent * sizeof(uchar2)));
+        SID_CUDA_TRY(cudaMemset(p->khat_f24h.p, 0, nent * sizeof(ushort2)));
+        SID_CUDA_TRY(cudaMemset(p->khat_f24l.p, 0, nent * sizeof(uchar2)));
+        p->spec_f24 = true;
+    }
     const bool want16 = (p->flags & SID_PLAN_SPECTRAL_I16) != 0;
     if (want16) {
         SID_TRY(p->khat_i16.alloc(nent * sizeof(short2)));
@@ -156,13 +186,15 @@ int build_spectra(sid_plan* p)
     SID_CUDA_TRY(cudaFuncSetAttribute(k_build_khat, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     dim3 grid((unsigned)n_out, (unsigned)cdiv(n_in, KB_CH));
     unsigned int* rowmax = want16 ? p->rstep.as<unsigned int>() : nullptr;
-    // pass 1: FP32 spectra and row maxima
-    if (p->spec_f32 || want16) {
+    // pass 1: FP32 and 24-bit spectra, row maxima
+    if (p->spec_f32 || want16 || p->spec_f24) {
         DBuf dummy;
         if (!rowmax) { SID_TRY(dummy.alloc((size_t)nrows * sizeof(unsigned))); rowmax = dummy.as<unsigned int>(); }
         k_build_khat<<<grid, 256, smem>>>(p->taps_f.as<float>(), p->twiddle.as<float2>(),
-                                          p->spec_f32 ? p->khat_f32.as<float2>() : nullptr, nullptr, rowmax,
-                                          nullptr, 0, (int)N, (int)n_in, n_in_pad, (int)D, (int)p->g.dlo, (int)L, tbs);
+                                          p->spec_f32 ? p->khat_f32.as<float2>() : nullptr, nullptr,
+                                          p->spec_f24 ? p->khat_f24h.as<ushort2>() : nullptr,
+                                          p->spec_f24 ? p->khat_f24l.as<uchar2>() : nullptr, rowmax, nullptr, 0,
+                                          (int)N, (int)n_in, n_in_pad, (int)D, (int)p->g.dlo, (int)L, tbs);
         SID_CHECK_LAUNCH();
         SID_CUDA_TRY(cudaDeviceSynchronize());
         dummy.release();
@@ -172,8 +204,8 @@ int build_spectra(sid_plan* p)
         k_row_steps<<<1024, 256>>>(p->rstep.as<unsigned int>(), p->rstep.as<float>(), nrows);
         SID_CHECK_LAUNCH();
         k_build_khat<<<grid, 256, smem>>>(p->taps_f.as<float>(), p->twiddle.as<float2>(), nullptr,
-                                          p->khat_i16.as<short2>(), nullptr, p->rstep.as<float>(), 1, (int)N,
-                                          (int)n_in, n_in_pad, (int)D, (int)p->g.dlo, (int)L, tbs);
+                                          p->khat_i16.as<short2>(), nullptr, nullptr, nullptr, p->rstep.as<float>(),
+                                          1, (int)N, (int)n_in, n_in_pad, (int)D, (int)p->g.dlo, (int)L, tbs);
         SID_CHECK_LAUNCH();
         SID_CUDA_TRY(cudaDeviceSynchronize());
     }
@@ -537,35 +569,61 @@ k_spec_fwd(const uint4* __restrict__ khat, const float* __restrict__ rstep, cons
     }
 }
 
-// Adjoint: per frequency f, Bhat[k][f] = sum_o conj(Khat[f][o][k]) * step(f,o) * Ihat[o][f].
-template <bool I16>
-__global__ void __launch_bounds__(512)
-k_spec_adj(const uint4* __restrict__ khat, const float* __restrict__ rstep, const float2* __restrict__ ihat,
-           float2* __restrict__ bhat, int n_in, int64_t n_in_pad, int n_out, int nf)
+// 24-bit float spectra: eight complex entries per two 16-byte high-plane
+// words (re, im high halves) and one 16-byte low-plane word (re, im low bytes).
+__device__ __forceinline__ void unpack_f24(const uint4& q0, const uint4& q1, const uint4& l, float2 (&k)[8])
 {
-    using KL = KLoad<I16>;
-    constexpr int V = KL::EPL;
+    const unsigned w[8] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w};
+    const unsigned lw[4] = {l.x, l.y, l.z, l.w};
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+        const unsigned lb = lw[e >> 1] >> (16 * (e & 1));
+        k[e].x = __uint_as_float(((w[e] & 0xFFFFu) << 16) | ((lb & 0xFFu) << 8));
+        k[e].y = __uint_as_float((w[e] & 0xFFFF0000u) | (((lb >> 8) & 0xFFu) << 8));
+    }
+}
+
+// Adjoint: per frequency f, Bhat[k][f] = sum_o conj(Khat[f][o][k]) * step(f,o) * Ihat[o][f].
+// FMT: FMT_F32 (khat float2), FMT_I16 (short2 mantissas and row steps) or
+// FMT_F24 (khat = high plane, klo = low plane).
+template <int FMT>
+__global__ void __launch_bounds__(512)
+k_spec_adj(const uint4* __restrict__ khat, const uint4* __restrict__ klo, const float* __restrict__ rstep,
+           const float2* __restrict__ ihat, float2* __restrict__ bhat, int n_in, int64_t n_in_pad, int n_out, int nf)
+{
+    // channels per thread: one 16-byte word of FP32 (2) or 16-bit (4) entries;
+    // three 16-byte words (two high, one low) of 24-bit entries (8)
+    constexpr int V = FMT == FMT_F32 ? 2 : (FMT == FMT_I16 ? 4 : 8);
     extern __shared__ float2 yv[];  // [n_out], pre-multiplied by the row steps
     const int f = blockIdx.x;
     for (int o = threadIdx.x; o < n_out; o += blockDim.x) {
         const float2 y = ihat[(int64_t)o * nf + f];
-        const float st = I16 ? rstep[(int64_t)f * n_out + o] : 1.f;
+        const float st = FMT == FMT_I16 ? rstep[(int64_t)f * n_out + o] : 1.f;
         yv[o] = make_float2(y.x * st, y.y * st);
     }
     __syncthreads();
     const int nvec = (int)(n_in_pad / V);
-    const int64_t rowvec = n_in_pad / V;
+    // 16-byte words per row: high plane (or the only plane) and low plane
+    const int64_t rowvec = FMT == FMT_F24 ? n_in_pad / 4 : n_in_pad / V;
+    const int64_t rowlo = n_in_pad / 8;
     const uint4* base = khat + (int64_t)f * n_out * rowvec;
+    const uint4* lbase = FMT == FMT_F24 ? klo + (int64_t)f * n_out * rowlo : nullptr;
     for (int j = threadIdx.x; j < nvec; j += blockDim.x) {
         float ar[V], ai[V];
 #pragma unroll
         for (int e = 0; e < V; ++e) ar[e] = ai[e] = 0.f;
-        const uint4* col = base + j;
+        const uint4* col = base + (FMT == FMT_F24 ? 2 * j : j);
+        const uint4* lcol = FMT == FMT_F24 ? lbase + j : nullptr;
 #pragma unroll 4
         for (int o = 0; o < n_out; ++o) {
             const float2 y = yv[o];
             float2 kk[V];
-            KL::unpack(__ldcs(col + (int64_t)o * rowvec), kk);
+            if constexpr (FMT == FMT_F24) {
+                unpack_f24(__ldcs(col + (int64_t)o * rowvec), __ldcs(col + (int64_t)o * rowvec + 1),
+                           __ldcs(lcol + (int64_t)o * rowlo), kk);
+            } else {
+                KLoad<FMT == FMT_I16>::unpack(__ldcs(col + (int64_t)o * rowvec), kk);
+            }
 #pragma unroll
             for (int e = 0; e < V; ++e) {
                 ar[e] = fmaf(kk[e].x, y.x, ar[e]); ar[e] = fmaf(kk[e].y, y.y, ar[e]);
@@ -619,14 +677,18 @@ static int dft_c2r(const sid_plan* p, const float2* in, float* out, int64_t nch,
     return SID_OK;
 }
 
-static int spec_check(const sid_plan* p, bool i16)
+static int spec_check(const sid_plan* p, int fmt)
 {
-    if (i16 && !p->spec_i16) {
+    if (fmt == FMT_I16 && !p->spec_i16) {
         set_error("spectral projector: plan was built without SID_PLAN_SPECTRAL_I16");
         return SID_ENOTSUP;
     }
-    if (!i16 && !p->spec_f32) {
+    if (fmt == FMT_F32 && !p->spec_f32) {
         set_error("spectral projector: plan was built without SID_PLAN_SPECTRAL_F32");
+        return SID_ENOTSUP;
+    }
+    if (fmt == FMT_F24 && !p->spec_f24) {
+        set_error("spectral projector: plan was built without SID_PLAN_SPECTRAL_F24");
         return SID_ENOTSUP;
     }
     return SID_OK;
@@ -634,7 +696,7 @@ static int spec_check(const sid_plan* p, bool i16)
 
 int spectral_forward(sid_plan* p, bool i16, const float* vp, float* ip, cudaStream_t st)
 {
-    SID_TRY(spec_check(p, i16));
+    SID_TRY(spec_check(p, i16 ? FMT_I16 : FMT_F32));
     SID_TRY(ensure_spec_ws(p));
     SID_TRY(configure_dft(p));
     const int64_t n_in = p->N * p->N * p->Z, n_out = p->N * p->N, n_in_pad = spec_nin_pad(p);
@@ -658,23 +720,27 @@ int spectral_forward(sid_plan* p, bool i16, const float* vp, float* ip, cudaStre
     return SID_OK;
 }
 
-int spectral_adjoint(sid_plan* p, bool i16, const float* ip, float* bp, cudaStream_t st)
+int spectral_adjoint(sid_plan* p, int fmt, const float* ip, float* bp, cudaStream_t st)
 {
-    SID_TRY(spec_check(p, i16));
+    SID_TRY(spec_check(p, fmt));
     SID_TRY(ensure_spec_ws(p));
     SID_TRY(configure_dft(p));
     const int64_t n_in = p->N * p->N * p->Z, n_out = p->N * p->N, n_in_pad = spec_nin_pad(p);
     SID_TRY(dft_r2c(p, ip, p->ihat.as<float2>(), n_out, st));
     const size_t sm = (size_t)n_out * sizeof(float2);
     p->timer.begin(st);
-    if (i16)
-        k_spec_adj<true><<<(unsigned)p->nf, 512, sm, st>>>(p->khat_i16.as<uint4>(), p->rstep.as<float>(),
-                                                          p->ihat.as<float2>(), p->vhat.as<float2>(), (int)n_in,
-                                                          n_in_pad, (int)n_out, (int)p->nf);
+    if (fmt == FMT_I16)
+        k_spec_adj<FMT_I16><<<(unsigned)p->nf, 512, sm, st>>>(p->khat_i16.as<uint4>(), nullptr, p->rstep.as<float>(),
+                                                             p->ihat.as<float2>(), p->vhat.as<float2>(), (int)n_in,
+                                                             n_in_pad, (int)n_out, (int)p->nf);
+    else if (fmt == FMT_F24)
+        k_spec_adj<FMT_F24><<<(unsigned)p->nf, 512, sm, st>>>(p->khat_f24h.as<uint4>(), p->khat_f24l.as<uint4>(),
+                                                             nullptr, p->ihat.as<float2>(), p->vhat.as<float2>(),
+                                                             (int)n_in, n_in_pad, (int)n_out, (int)p->nf);
     else
-        k_spec_adj<false><<<(unsigned)p->nf, 512, sm, st>>>(p->khat_f32.as<uint4>(), nullptr, p->ihat.as<float2>(),
-                                                           p->vhat.as<float2>(), (int)n_in, n_in_pad, (int)n_out,
-                                                           (int)p->nf);
+        k_spec_adj<FMT_F32><<<(unsigned)p->nf, 512, sm, st>>>(p->khat_f32.as<uint4>(), nullptr, nullptr,
+                                                             p->ihat.as<float2>(), p->vhat.as<float2>(), (int)n_in,
+                                                             n_in_pad, (int)n_out, (int)p->nf);
     p->timer.finish(st);
     SID_CHECK_LAUNCH();
     SID_TRY(dft_c2r(p, p->vhat.as<float2>(), bp, n_in, st));

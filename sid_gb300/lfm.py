@@ -34,8 +34,9 @@ _DEFAULT_METHOD = "direct"
 def set_default_method(method: str):
     """Projection form used by the function-style API: 'direct' (FP32 lenslet
     convolution), 'spectral_f32' (FP32 lenslet-grid spectra), 'spectral_i16'
-    (16-bit block-floating-point spectra) or 'spectral_mixed' (16-bit forward,
-    FP32 back projection)."""
+    (16-bit block-floating-point spectra), 'spectral_mixed' (16-bit forward,
+    24-bit float back projection) or 'spectral_mixed_f32' (16-bit forward, FP32
+    back projection)."""
     global _DEFAULT_METHOD
     if method not in _lib.METHODS:
         raise ValueError(f"unknown method {method!r}")

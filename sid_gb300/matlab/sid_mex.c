@@ -178,7 +178,7 @@ void mexFunction(int nlhs, mxArray* plhs[], int nrhs, const mxArray* prhs[])
         for (int i = 0; i < MAX_PLANS; ++i)
             if (!g_plans[i]) { slot = i; break; }
         if (slot < 0) mexErrMsgIdAndTxt("sid:plan", "too many plans");
-        const int flags = nrhs > 5 ? (int)mxGetScalar(prhs[5]) : (SID_PLAN_SPECTRAL_F32 | SID_PLAN_SPECTRAL_I16);
+        const int flags = nrhs > 5 ? (int)mxGetScalar(prhs[5]) : (SID_PLAN_SPECTRAL_I16 | SID_PLAN_SPECTRAL_F24);
         check(sid_plan_create((const float*)mxGetData(H), (int64_t)d[0], (int64_t)d[2], Z, ca,
                               (int64_t)mxGetScalar(prhs[3]), (int64_t)mxGetScalar(prhs[4]), flags, &g_plans[slot]),
               cmd);

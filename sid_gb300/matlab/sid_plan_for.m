@@ -7,7 +7,7 @@ if isempty(keys), keys = {}; plans = []; end
 key = sprintf('%s|%s|%d|%d|%.17g', mat2str(size(H)), mat2str(CAindex), X, Y, double(sum(H(:))));
 hit = find(strcmp(keys, key), 1);
 if isempty(hit)
-    if isempty(CAindex), flags = 2 + 4 + 1; else, flags = 1; end   % spectral FP32 + 16-bit + direct / direct
+    if isempty(CAindex), flags = 4 + 8 + 1; else, flags = 1; end   % spectral 16-bit + 24-bit + direct / direct
     plan = sid_mex('plan', single(H), CAindex, X, Y, flags);
     keys{end+1} = key; plans(end+1) = plan;
 else

@@ -10,8 +10,8 @@ from tests.conftest import ROOT, rel_l2
 pytestmark = pytest.mark.gpu
 
 # rel-L2 bars against FP64: plain FP32 path 1e-5, mixed (FP16 spectra) 1e-4
-TOL = {"direct": 1e-5, "spectral_f32": 1e-5, "spectral_i16": 1e-4, "spectral_mixed": 1e-4}
-ALL = ("direct", "spectral_f32", "spectral_i16", "spectral_mixed")
+TOL = {"direct": 1e-5, "spectral_f32": 1e-5, "spectral_i16": 1e-4, "spectral_mixed": 1e-4, "spectral_mixed_f32": 1e-4}
+ALL = ("direct", "spectral_f32", "spectral_i16", "spectral_mixed", "spectral_mixed_f32")
 
 
 def _golden(case):

@@ -122,7 +122,9 @@ def test_reconstruct_component_spectral_stages(small, oracle, method, opts, tol)
     if o0.get("whichSolver") == "ISRA":
         o0.pop("whichSolver")
     Hg = s.to_numpy(P.reconstruct_component(img, None, o0, method=method)).astype(np.float64) / nrm
-    assert rel_l2(Hg, Htf) < 1e-6, rel_l2(Hg, Htf)
+    # FP32 back-projection spectra, or 24-bit floats (16 significant bits) in the mixed form
+    htf_tol = 1e-5 if method == "spectral_mixed" else 1e-6
+    assert rel_l2(Hg, Htf) < htf_tol, rel_l2(Hg, Htf)
     out = s.to_numpy(P.reconstruct_component(img, None, opts, method=method))
     ref = _oracle_solve_from(oracle, Hg, nrm, fwd, bwd, opts)
     assert rel_l2(out, ref) < tol, rel_l2(out, ref)
