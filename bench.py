@@ -377,7 +377,9 @@ def main():
         traffic = None
         tf = os.path.join(ROOT, "profiles", "traffic.json")
         if os.path.exists(tf):
-            traffic = json.load(open(tf)).get(f"k_spec_{args.method}")
+            rec = json.load(open(tf))
+            if rec.get("volume") == [X, Y, Z]:  # captured on this volume size only
+                traffic = rec.get(f"k_spec_{args.method}")
         roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                 "traffic": traffic, "kernel": "k_spec_fwd/k_spec_adj (tap-spectra contraction)",
                 "launches": k_n, "avg_launch_ms": k_ms / k_n, "algorithmic_bytes_per_launch": alg_bytes,

@@ -140,7 +140,7 @@ struct sid_plan {
     sid::DBuf khat_f24h;        // [f][b'a'][abc] 24-bit floats: high 16 bits of re, im
     sid::DBuf khat_f24l;        // [f][b'a'][abc] 24-bit floats: low 8 bits of re, im
     bool spec_f24;
-    sid::DBuf twiddle;          // L float2: exp(-2 pi i k / L)
+    sid::DBuf twiddle;          // L float2: exp(+2 pi i k / L)
     // workspaces
     sid::DBuf vp, ip, bp, ipart, vhat, ihat, bhat, red;
     sid::DBuf ws[9];            // solver state (polyphase volumes); [6..8] component reconstruction

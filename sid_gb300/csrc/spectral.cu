@@ -20,6 +20,8 @@
 
 namespace sid {
 
+bool fft_factor(int64_t L, int* P, int* Q);
+
 static inline int64_t spec_nin_pad(const sid_plan* p) { return cdiv(p->N * p->N * p->Z, 8) * 8; }
 
 // --------------------------------------------------------- tap spectra -----
@@ -143,7 +145,16 @@ int build_spectra(sid_plan* p)
 {
     const int64_t N = p->N, Z = p->Z, D = p->g.D;
     const int64_t Lmin = std::max(p->Lx, p->Ly) + std::max(p->g.dhi, -p->g.dlo);
-    const int64_t L = cdiv(Lmin, 4) * 4;
+    // the smallest multiple of 4 >= Lmin whose odd part is at most 15 (the FFT
+    // kernels' factorisation), or the smallest multiple of 4 if none is near
+    int64_t L = cdiv(Lmin, 4) * 4;
+    for (int64_t c = L; c < L + 64; c += 4) {
+        int fp = 0, fq = 0;
+        if (fft_factor(c, &fp, &fq)) {
+            L = c;
+            break;
+        }
+    }
     const int64_t H1 = L / 2 + 1;
     p->L = L;
     p->nf = H1 * L;
@@ -661,8 +672,15 @@ static int configure_dft(const sid_plan* p)
 // persistent DFT grids: at most two CTAs per SM (shared-memory bound)
 static unsigned dft_grid(int64_t nch) { return (unsigned)std::min<int64_t>(nch, 2 * 152); }
 
+int fft_r2c(const sid_plan* p, const float* in, float2* out, int64_t nch, cudaStream_t st);
+int fft_c2r(const sid_plan* p, const float2* in, float* out, int64_t nch, cudaStream_t st);
+
+// lenslet-grid transforms: mixed-radix FFTs (fft.cu) when L factors as 2^a * odd,
+// else the matrix DFTs above
 static int dft_r2c(const sid_plan* p, const float* in, float2* out, int64_t nch, cudaStream_t st)
 {
+    int P = 0, Q = 0;
+    if (fft_factor(p->L, &P, &Q)) return fft_r2c(p, in, out, nch, st);
     const DftDims d = dft_dims(p);
     k_dft_r2c<<<dft_grid(nch), kDftThreads, r2c_smem(d), st>>>(in, out, p->twiddle.as<float2>(), d, nch);
     SID_CHECK_LAUNCH();
@@ -671,6 +689,8 @@ static int dft_r2c(const sid_plan* p, const float* in, float2* out, int64_t nch,
 
 static int dft_c2r(const sid_plan* p, const float2* in, float* out, int64_t nch, cudaStream_t st)
 {
+    int P = 0, Q = 0;
+    if (fft_factor(p->L, &P, &Q)) return fft_c2r(p, in, out, nch, st);
     const DftDims d = dft_dims(p);
     k_dft_c2r<<<dft_grid(nch), kDftThreads, c2r_smem(d), st>>>(in, out, p->twiddle.as<float2>(), d, nch);
     SID_CHECK_LAUNCH();
