@@ -161,6 +161,50 @@ __global__ void k_ls_grad(float* __restrict__ d, const float* __restrict__ b, co
         d[i] += b[i] + l2 * step[i];
 }
 
+static int isra_update(sid_plan* p, float* xp, const float* hp, float lambda, cudaStream_t st)
+{
+    k_isra_update<<<2048, 256, 0, st>>>(xp, hp, p->bp.as<float>(), lambda, vol_plane_elems(p) * p->Z);
+    SID_CHECK_LAUNCH();
+    return SID_OK;
+}
+
+// Device address of a caller's host array, or nullptr (stage through copies):
+// pinned or registered memory has one; pageable memory is device-accessible
+// where the GPU walks the host's page tables (Grace-class systems).
+static void* host_device_view(const void* h)
+{
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, h) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (a.type == cudaMemoryTypeHost) return a.devicePointer;
+    if (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) return const_cast<void*>(h);
+    int dev = 0, pageable = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess &&
+        cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, dev) == cudaSuccess && pageable)
+        return const_cast<void*>(h);
+    return nullptr;
+}
+
+// The plan's streams for host-array calls, ordered after the caller's work on
+// the legacy default stream.
+static int host_streams(sid_plan* p, cudaStream_t* work, cudaStream_t* side)
+{
+    if (!p->hstream[0]) {
+        int least = 0, greatest = 0;
+        SID_CUDA_TRY(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+        SID_CUDA_TRY(cudaStreamCreateWithPriority(&p->hstream[0], cudaStreamNonBlocking, least));
+        SID_CUDA_TRY(cudaStreamCreateWithPriority(&p->hstream[1], cudaStreamNonBlocking, greatest));
+        for (cudaEvent_t& e : p->hevent) SID_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    }
+    SID_CUDA_TRY(cudaEventRecord(p->hevent[2], 0));
+    SID_CUDA_TRY(cudaStreamWaitEvent(p->hstream[0], p->hevent[2], 0));
+    *work = p->hstream[0];
+    *side = p->hstream[1];
+    return SID_OK;
+}
+
 }  // namespace sid
 
 using namespace sid;
@@ -187,17 +231,27 @@ extern "C" int sid_adjoint(sid_plan* p, int method, const float* I, float* V, vo
     return SID_OK;
 }
 
-// Host-array calls stage through two plan-owned device buffers (ws[4], ws[5])
-// that persist across calls, so repeated calls allocate nothing.
+// Host-array calls: where the device can address the caller's arrays, the
+// layout kernels read the input and write the result over the host link
+// directly (no staging pass); otherwise they stage through two plan-owned
+// device buffers (ws[4], ws[5]) that persist across calls.
 template <class F>
 static int with_device_copies(sid_plan* p, const float* in_h, size_t in_n, float* out_h, size_t out_n, F fn)
 {
+    const float* iv = static_cast<const float*>(host_device_view(in_h));
+    float* ov = static_cast<float*>(host_device_view(out_h));
+    if (iv && ov) {
+        cudaStream_t st, side;
+        SID_TRY(host_streams(p, &st, &side));
+        SID_TRY(fn(iv, ov, st));
+        return plan_sync(p, st);
+    }
     DBuf& din = p->ws[4];
     DBuf& dout = p->ws[5];
     SID_TRY(din.alloc(in_n * sizeof(float)));
     SID_TRY(dout.alloc(out_n * sizeof(float)));
     SID_CUDA_TRY(cudaMemcpy(din.p, in_h, in_n * sizeof(float), cudaMemcpyHostToDevice));
-    SID_TRY(fn(din.as<float>(), dout.as<float>()));
+    SID_TRY(fn(din.as<float>(), dout.as<float>(), (cudaStream_t)0));
     SID_TRY(plan_sync(p, 0));
     SID_CUDA_TRY(cudaMemcpy(out_h, dout.p, out_n * sizeof(float), cudaMemcpyDeviceToHost));
     return SID_OK;
@@ -207,14 +261,14 @@ extern "C" int sid_forward_host(sid_plan* p, int method, const float* V, float* 
 {
     SID_REQUIRE(p && V && I, "sid_forward_host: NULL argument");
     return with_device_copies(p, V, (size_t)(p->X * p->Y * p->Z), I, (size_t)(p->X * p->Y),
-                              [&](const float* dv, float* di) { return sid_forward(p, method, dv, di, nullptr); });
+                              [&](const float* dv, float* di, cudaStream_t st) { return sid_forward(p, method, dv, di, st); });
 }
 
 extern "C" int sid_adjoint_host(sid_plan* p, int method, const float* I, float* V)
 {
     SID_REQUIRE(p && V && I, "sid_adjoint_host: NULL argument");
     return with_device_copies(p, I, (size_t)(p->X * p->Y), V, (size_t)(p->X * p->Y * p->Z),
-                              [&](const float* di, float* dv) { return sid_adjoint(p, method, di, dv, nullptr); });
+                              [&](const float* di, float* dv, cudaStream_t st) { return sid_adjoint(p, method, di, dv, st); });
 }
 
 extern "C" int sid_deconv_isra(sid_plan* p, int method, const float* Htf, float* X, int maxIter, float lambda,
@@ -234,8 +288,7 @@ extern "C" int sid_deconv_isra(sid_plan* p, int method, const float* Htf, float*
     for (int it = 0; it < maxIter; ++it) {
         SID_TRY(fwd_poly(p, method, xp, p->ip.as<float>(), st));
         SID_TRY(adj_poly(p, method, p->ip.as<float>(), p->bp.as<float>(), st));
-        k_isra_update<<<2048, 256, 0, st>>>(xp, hp, p->bp.as<float>(), lambda, n);
-        SID_CHECK_LAUNCH();
+        SID_TRY(isra_update(p, xp, hp, lambda, st));
     }
     SID_TRY(vp_to_v(p, xp, X, p->Z, st));
     return SID_OK;
@@ -290,15 +343,46 @@ extern "C" int sid_deconv_isra_host(sid_plan* p, int method, const float* Htf, f
                                     float lambda)
 {
     SID_REQUIRE(p && Htf && X, "sid_deconv_isra_host: NULL argument");
+    SID_REQUIRE(maxIter >= 0, "sid_deconv_isra_host: maxIter < 0");
     const size_t n = (size_t)(p->X * p->Y * p->Z);
     DBuf& dh = p->ws[4];
-    DBuf& dx = p->ws[5];
     SID_TRY(dh.alloc(n * sizeof(float)));
-    SID_TRY(dx.alloc(n * sizeof(float)));
-    SID_CUDA_TRY(cudaMemcpy(dh.p, Htf, n * sizeof(float), cudaMemcpyHostToDevice));
-    SID_CUDA_TRY(cudaMemcpy(dx.p, X, n * sizeof(float), cudaMemcpyHostToDevice));
-    SID_TRY(sid_deconv_isra(p, method, dh.as<float>(), dx.as<float>(), maxIter, lambda, nullptr));
-    SID_TRY(plan_sync(p, 0));
-    SID_CUDA_TRY(cudaMemcpy(X, dx.p, n * sizeof(float), cudaMemcpyDeviceToHost));
-    return SID_OK;
+    float* xv = static_cast<float*>(host_device_view(X));
+    if (!xv) {
+        DBuf& dx = p->ws[5];
+        SID_TRY(dx.alloc(n * sizeof(float)));
+        SID_CUDA_TRY(cudaMemcpy(dh.p, Htf, n * sizeof(float), cudaMemcpyHostToDevice));
+        SID_CUDA_TRY(cudaMemcpy(dx.p, X, n * sizeof(float), cudaMemcpyHostToDevice));
+        SID_TRY(sid_deconv_isra(p, method, dh.as<float>(), dx.as<float>(), maxIter, lambda, nullptr));
+        SID_TRY(plan_sync(p, 0));
+        SID_CUDA_TRY(cudaMemcpy(X, dx.p, n * sizeof(float), cudaMemcpyDeviceToHost));
+        return SID_OK;
+    }
+    // X crosses the host link inside its layout conversion; Htf (needed first by
+    // the update) crosses on a copy engine while the first projections run; the
+    // result is written back by the inverse conversion.
+    cudaStream_t st, side;
+    SID_TRY(host_streams(p, &st, &side));
+    SID_TRY(ensure_proj_ws(p));
+    const int64_t nv = vol_plane_elems(p) * p->Z;
+    SID_TRY(p->ws[0].alloc((size_t)nv * sizeof(float)));
+    SID_TRY(p->ws[1].alloc((size_t)nv * sizeof(float)));
+    float* xp = p->ws[0].as<float>();
+    float* hp = p->ws[1].as<float>();
+    SID_TRY(v_to_vp(p, xv, xp, p->Z, st));
+    SID_CUDA_TRY(cudaEventRecord(p->hevent[0], st));
+    for (int it = 0; it < maxIter; ++it) {
+        SID_TRY(fwd_poly(p, method, xp, p->ip.as<float>(), st));
+        SID_TRY(adj_poly(p, method, p->ip.as<float>(), p->bp.as<float>(), st));
+        if (it == 0) {
+            SID_CUDA_TRY(cudaStreamWaitEvent(side, p->hevent[0], 0));
+            SID_CUDA_TRY(cudaMemcpyAsync(dh.p, Htf, n * sizeof(float), cudaMemcpyHostToDevice, side));
+            SID_TRY(v_to_vp(p, dh.as<float>(), hp, p->Z, side));
+            SID_CUDA_TRY(cudaEventRecord(p->hevent[1], side));
+            SID_CUDA_TRY(cudaStreamWaitEvent(st, p->hevent[1], 0));
+        }
+        SID_TRY(isra_update(p, xp, hp, lambda, st));
+    }
+    SID_TRY(vp_to_v(p, xp, xv, p->Z, st));
+    return plan_sync(p, st);
 }

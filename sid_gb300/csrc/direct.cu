@@ -24,7 +24,8 @@
 namespace sid {
 
 // ---------------------------------------------------------------- layouts --
-// Vp[c][b][a][v][u] <- V(a+N*u, b+N*v, c); zero outside X x Y.
+// Vp[c][b][a][v][u] <- V(a+N*u, b+N*v, c); zero outside X x Y.  V may be a
+// caller's host array (device view): each CTA reads one contiguous row.
 __global__ void k_v_to_vp(const float* __restrict__ V, float* __restrict__ Vp, int64_t X, int64_t Y,
                           int N, int Lx, int Ly)
 {
@@ -44,9 +45,8 @@ __global__ void k_v_to_vp(const float* __restrict__ V, float* __restrict__ Vp, i
     }
 }
 
-// V(x,y,c) <- Vp (x < X, y < Y).  With `isra` set, writes the fused ISRA
-// update X <- X .* (Htf ./ B) (inf -> 0, NaN -> 0) instead (deconvRL.m:52,85-87),
-// reading X and Htf in V layout.  Not used by the solvers (they stay polyphase).
+// V(x,y,c) <- Vp (x < X, y < Y).  V may be a caller's host array (device
+// view): each CTA writes one contiguous row.
 __global__ void k_vp_to_v(const float* __restrict__ Vp, float* __restrict__ V, int64_t X, int64_t Y,
                           int N, int Lx, int Ly)
 {

@@ -189,6 +189,10 @@ extern "C" int sid_plan_destroy(sid_plan* p)
     for (DBuf* b : bufs) b->release();
     for (DBuf& b : p->ws) b.release();
     p->timer.release();
+    for (cudaStream_t& s : p->hstream)
+        if (s) cudaStreamDestroy(s);
+    for (cudaEvent_t& e : p->hevent)
+        if (e) cudaEventDestroy(e);
     delete p;
     return SID_OK;
 }

@@ -147,6 +147,10 @@ struct sid_plan {
     sid::DBuf errflag;          // device int: nonzero after a bounded wait expired
     sid::KTimer timer;          // dominant-kernel timing (sid_plan_timing_*)
     int zsplit;
+    // host-array calls: [0] work stream, [1] side stream (copies, higher priority);
+    // events: [0] input volume converted, [1] Htf converted, [2] caller's stream 0
+    cudaStream_t hstream[2] = {nullptr, nullptr};
+    cudaEvent_t hevent[3] = {nullptr, nullptr, nullptr};
 };
 
 namespace sid {

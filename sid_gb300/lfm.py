@@ -183,8 +183,9 @@ class Projector:
         return X
 
     def isra_host(self, Htf, Xguess, maxIter, lam=0.0, method=None) -> np.ndarray:
-        """Host-array ISRA (the MEX path for non-gpuArray inputs): copies in,
-        iterates on the GPU, copies the result out."""
+        """Host-array ISRA (the MEX path for non-gpuArray inputs): the input
+        volume and the result cross the host link inside their layout
+        conversions, Htf on a copy engine during the first projections."""
         Hn = np.asfortranarray(np.asarray(Htf, dtype=np.float32))
         X = np.array(Xguess, dtype=np.float32, order="F", copy=True)
         _lib.call("sid_deconv_isra_host", self._plan, self._method(method), Hn.ctypes.data, X.ctypes.data,

@@ -54,6 +54,33 @@ def test_isra_cfg0_mixed_vs_fp64(gpu, oracle):
         assert rel_l2(out, ref) < tol, (m, rel_l2(out, ref))
 
 
+def _pinned_fortran(a):
+    """A Fortran-ordered float32 copy of `a` in page-locked host memory."""
+    import torch
+    buf = torch.empty(a.size, dtype=torch.float32, pin_memory=True).numpy()
+    out = buf.reshape(a.shape, order="F")
+    out[...] = a
+    return out
+
+
+@pytest.mark.parametrize("method", ["direct", "spectral_mixed"])
+def test_isra_host_matches_device(small, method):
+    """The host-array entry point (input and result over the host link, Htf on a
+    side stream) gives the device-array call's result bit for bit, from
+    pageable and from page-locked host arrays, for several iterations and for
+    none."""
+    import sid_gb300 as s
+    H, y, P, fwd, bwd = small
+    Htf = bwd(y).astype(np.float32)
+    X0 = np.asfortranarray(0.5 * Htf + 0.01)
+    for iters in (0, 3):
+        ref = s.to_numpy(P.isra(Htf, X0, iters, method=method))
+        np.testing.assert_array_equal(P.isra_host(Htf, X0, iters, method=method), ref)
+        xp = _pinned_fortran(X0)
+        P.isra_host_inplace(_pinned_fortran(Htf), xp, iters, method=method)
+        np.testing.assert_array_equal(xp, ref)
+
+
 @pytest.mark.parametrize("method,tol", [("direct", 1e-5), ("spectral_f32", 1e-5), ("spectral_mixed", 1e-4)])
 def test_ls_deconv_matches_oracle(small, method, tol):
     import sid_gb300 as s
