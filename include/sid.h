@@ -79,9 +79,18 @@ int sid_plan_create(const float* H, int64_t M, int64_t Nnum, int64_t Z,
                     const int32_t* CAindex, int64_t X, int64_t Y, int flags,
                     sid_plan** plan);
 int sid_plan_destroy(sid_plan* plan);
-/* info[0..11] = M, Nnum, Z, X, Y, Lx, Ly, D (taps per axis), L (DFT length),
- * device bytes held, flags, adjoint-taps-separate. */
+/* info[0..13] = M, Nnum, Z, X, Y, Lx, Ly, D (taps per axis), L (DFT length),
+ * device bytes held, flags, adjoint-taps-separate, weakly observed voxels (column
+ * mass A'1 below 1e-2 of the largest unless set otherwise; the spectral back
+ * projections recompute them exactly from the lenslet taps), kernel launches
+ * that recomputation adds to each spectral back projection. */
 int sid_plan_info(const sid_plan* plan, int64_t* info);
+/* Spectral back projections recompute the weakly observed voxels exactly from
+ * the lenslet taps: those whose column mass A'1 (the PSF mass landing on the
+ * sensor) is below `frac` of the largest (default 1e-2; 0 turns it off).  Their
+ * FFT-based values carry only absolute accuracy, which the multiplicative
+ * solvers' divisions by A'(.) amplify.  Rebuilds the list (synchronous). */
+int sid_plan_set_weak_fraction(sid_plan* plan, double frac);
 
 /* TOTALprojection = forwardProjectGPU(H, realspace)   forwardProjectGPU.m:1
  *                 = forwardProjectACC(H, realspace, CAindex)  forwardProjectACC.m:1
@@ -116,6 +125,15 @@ int sid_deconv_isra(sid_plan* plan, int method, const float* Htf, float* X,
 /* Host-array form of sid_deconv_isra (copies in, iterates, copies X out). */
 int sid_deconv_isra_host(sid_plan* plan, int method, const float* Htf, float* X,
                          int maxIter, float lambda);
+/* Poisson-likelihood Richardson-Lucy, the multiplicative update whose fixed
+ * point maximises sum(y log AX - AX): X <- X .* A'(y ./ AX) ./ A'1, with
+ * y ./ AX -> 0 where it is not finite, inf -> 0 and NaN -> 0 in the update as in
+ * deconvRL.m:85-87.  (The reference's deconvRL, labelled RL, is the ISRA form
+ * above; this is the Poisson counterpart whose gradient A'(1 - y ./ AX) the
+ * log-likelihood checks use.)  y: X x Y single sensor image (device);
+ * X: X x Y x Z single (device), Xguess on entry. */
+int sid_deconv_rl_poisson(sid_plan* plan, int method, const float* y, float* X, int maxIter,
+                          void* stream);
 /* Xguess = LS_deconv(fwd, bwd, df, opts)   LS_deconv.m:1
  * Projected gradient with exact line search on ||y - A x||^2 + lamb_L2 ||x||^2
  * + lamb_L1 ||x||_1, x >= 0 (LS_deconv.m:49-93; TV terms not supported).

@@ -216,6 +216,24 @@ def deconvRL(forward, backward, Htf, maxIter, Xguess, opts=None):
     return X
 
 
+def rl_poisson(forward, backward, y, maxIter, Xguess):
+    """Poisson-likelihood Richardson-Lucy (Richardson 1972, Lucy 1974):
+    X <- X .* A'(y ./ AX) ./ A'1, ratios that are not finite -> 0, then the zero
+    rules of deconvRL.m:85-87 (inf -> 0 in the factor, NaN -> 0 in X)."""
+    X = np.array(Xguess, dtype=np.float64, order="F")
+    y = np.asarray(y, dtype=np.float64)
+    norm = backward(np.ones_like(y))
+    for _ in range(int(maxIter)):
+        with np.errstate(divide="ignore", invalid="ignore"):
+            r = y / forward(X)
+            r[~np.isfinite(r)] = 0.0
+            e = backward(r) / norm
+            e[np.isinf(e)] = 0.0
+            X = X * e
+            X[np.isnan(X)] = 0.0
+    return X
+
+
 def _shift(X, axis, direction):
     """Zero-filled neighbour: direction -1 returns X at index-1 (0 at the lower
     edge), +1 returns X at index+1.  convn(X, e_k, 'same') with a 3-tap unit

@@ -47,6 +47,7 @@ SIGNATURES = {
     "sid_plan_create": [P, I64, I64, I64, P, I64, I64, I32, PP],
     "sid_plan_destroy": [P],
     "sid_plan_info": [P, P],
+    "sid_plan_set_weak_fraction": [P, ctypes.c_double],
     "sid_forward": [P, I32, P, P, P],
     "sid_adjoint": [P, I32, P, P, P],
     "sid_forward_host": [P, I32, P, P],
@@ -55,6 +56,7 @@ SIGNATURES = {
     "sid_deconv_isra": [P, I32, P, P, I32, F32, P],
     "sid_deconv_ls": [P, I32, P, I32, F32, F32, P],
     "sid_deconv_isra_host": [P, I32, P, P, I32, F32],
+    "sid_deconv_rl_poisson": [P, I32, P, P, I32, P],
     "sid_plan_timing_enable": [P, I32],
     "sid_plan_timing_read": [P, P, P],
     "sid_ctx_create": [PP],

@@ -24,16 +24,21 @@ int fwd_poly(sid_plan* p, int method, const float* vp, float* ip, cudaStream_t s
     }
 }
 
+// Spectral back projections are followed by the exact recomputation of the
+// weakly observed voxels (weak.cu).
 int adj_poly(sid_plan* p, int method, const float* ip, float* bp, cudaStream_t st)
 {
+    int fmt = FMT_F32;
     switch (method) {
     case SID_METHOD_DIRECT: return direct_adjoint(p, ip, bp, p->errflag.as<int>(), st);
-    case SID_METHOD_SPECTRAL_F32: return spectral_adjoint(p, FMT_F32, ip, bp, st);
-    case SID_METHOD_SPECTRAL_I16: return spectral_adjoint(p, FMT_I16, ip, bp, st);
-    case SID_METHOD_SPECTRAL_MIXED: return spectral_adjoint(p, FMT_F24, ip, bp, st);
-    case SID_METHOD_SPECTRAL_MIXED_F32: return spectral_adjoint(p, FMT_F32, ip, bp, st);
+    case SID_METHOD_SPECTRAL_F32: fmt = FMT_F32; break;
+    case SID_METHOD_SPECTRAL_I16: fmt = FMT_I16; break;
+    case SID_METHOD_SPECTRAL_MIXED: fmt = FMT_F24; break;
+    case SID_METHOD_SPECTRAL_MIXED_F32: fmt = FMT_F32; break;
     default: set_error("unknown projection method %d", method); return SID_EINVAL;
     }
+    SID_TRY(spectral_adjoint(p, fmt, ip, bp, st));
+    return weak_fix(p, ip, bp, st);
 }
 
 int ensure_proj_ws(sid_plan* p)
@@ -116,6 +121,22 @@ __global__ void k_isra_update(float* __restrict__ x, const float* __restrict__ h
         if (isnan(v)) v = 0.f;
         x[i] = v;
     }
+}
+
+// Poisson RL ratio in sensor space: r = y / AX, 0 where not finite (AX = 0,
+// and the lattice positions outside the sensor, where both are 0).
+__global__ void k_rl_ratio(float* __restrict__ ax, const float* __restrict__ y, int64_t n)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const float r = __fdiv_rn(y[i], ax[i]);
+        ax[i] = isfinite(r) ? r : 0.f;
+    }
+}
+
+__global__ void k_fill(float* __restrict__ x, float v, int64_t n)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        x[i] = v;
 }
 
 // d = B + l2*x - x + l1  (LS_deconv.m:73-75: df = Q(df) - df + lamb_L1 with x = df)
@@ -289,6 +310,43 @@ extern "C" int sid_deconv_isra(sid_plan* p, int method, const float* Htf, float*
         SID_TRY(fwd_poly(p, method, xp, p->ip.as<float>(), st));
         SID_TRY(adj_poly(p, method, p->ip.as<float>(), p->bp.as<float>(), st));
         SID_TRY(isra_update(p, xp, hp, lambda, st));
+    }
+    SID_TRY(vp_to_v(p, xp, X, p->Z, st));
+    return SID_OK;
+}
+
+extern "C" int sid_deconv_rl_poisson(sid_plan* p, int method, const float* y, float* X, int maxIter,
+                                     void* stream)
+{
+    SID_REQUIRE(p && y && X, "sid_deconv_rl_poisson: NULL argument");
+    SID_REQUIRE(maxIter >= 0, "sid_deconv_rl_poisson: maxIter < 0");
+    cudaStream_t st = as_stream(stream);
+    SID_TRY(ensure_proj_ws(p));
+    const int64_t n = vol_plane_elems(p) * p->Z;
+    const int64_t ni = vol_plane_elems(p);
+    SID_TRY(p->ws[0].alloc((size_t)n * sizeof(float)));
+    SID_TRY(p->ws[1].alloc((size_t)n * sizeof(float)));
+    SID_TRY(p->ws[2].alloc((size_t)ni * sizeof(float)));
+    float* xp = p->ws[0].as<float>();
+    float* np_ = p->ws[1].as<float>();  // A'1
+    float* yp = p->ws[2].as<float>();
+    float* ip = p->ip.as<float>();
+    float* bp = p->bp.as<float>();
+    SID_TRY(v_to_vp(p, y, yp, 1, st));
+    SID_TRY(v_to_vp(p, X, xp, p->Z, st));
+    // normaliser A'1: ones on the sensor, zero at lattice positions outside it
+    k_fill<<<1024, 256, 0, st>>>(ip, 1.f, ni);
+    SID_CHECK_LAUNCH();
+    SID_TRY(mask_vp(p, ip, 1, st));
+    SID_TRY(adj_poly(p, method, ip, np_, st));
+    for (int it = 0; it < maxIter; ++it) {
+        SID_TRY(fwd_poly(p, method, xp, ip, st));
+        k_rl_ratio<<<1024, 256, 0, st>>>(ip, yp, ni);
+        SID_CHECK_LAUNCH();
+        SID_TRY(adj_poly(p, method, ip, bp, st));
+        // X <- X .* (A'r ./ A'1): the ISRA update with numerator A'r, denominator A'1
+        k_isra_update<<<2048, 256, 0, st>>>(xp, bp, np_, 0.f, n);
+        SID_CHECK_LAUNCH();
     }
     SID_TRY(vp_to_v(p, xp, X, p->Z, st));
     return SID_OK;

@@ -141,6 +141,11 @@ struct sid_plan {
     sid::DBuf khat_f24l;        // [f][b'a'][abc] 24-bit floats: low 8 bits of re, im
     bool spec_f24;
     sid::DBuf twiddle;          // L float2: exp(+2 pi i k / L)
+    sid::DBuf weak;             // runs (column runs, then row runs) of the weakly observed voxels
+    sid::DBuf weak_pad;         //   (recomputed exactly after each spectral back projection) and the
+    int64_t nweak = 0;          //   zero-padded sensor-lattice copies their kernel reads
+    int64_t nweak_cols = 0, nweak_rows = 0;
+    double weak_frac = 1e-2;    // ... those with column mass A'1 below this fraction of the largest
     // workspaces
     sid::DBuf vp, ip, bp, ipart, vhat, ihat, bhat, red;
     sid::DBuf ws[9];            // solver state (polyphase volumes); [6..8] component reconstruction
@@ -161,6 +166,8 @@ int spectral_forward(sid_plan* p, bool i16, const float* vp, float* ip, cudaStre
 // storage formats of the tap spectra
 enum SpecFmt { FMT_F32 = 0, FMT_I16 = 1, FMT_F24 = 2 };
 int spectral_adjoint(sid_plan* p, int fmt, const float* ip, float* bp, cudaStream_t st);
+int weak_build(sid_plan* p);
+int weak_fix(sid_plan* p, const float* ip, float* bp, cudaStream_t st);
 int v_to_vp(const sid_plan* p, const float* V, float* vp, int64_t Z, cudaStream_t st);
 int vp_to_v(const sid_plan* p, const float* vp, float* V, int64_t Z, cudaStream_t st);
 int mask_vp(const sid_plan* p, float* vp, int64_t Z, cudaStream_t st);

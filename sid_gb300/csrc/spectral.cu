@@ -220,8 +220,9 @@ int build_spectra(sid_plan* p)
         SID_CHECK_LAUNCH();
         SID_CUDA_TRY(cudaDeviceSynchronize());
     }
-    if (!(p->flags & SID_PLAN_DIRECT)) p->taps_f.release();
-    return SID_OK;
+    // the weakly observed voxels keep exact back projections from the taps
+    // (kept for that even without the direct form)
+    return weak_build(p);
 }
 
 // -------------------------------------------------------------- real DFTs --

@@ -1,0 +1,326 @@
+// weak.cu -- exact back projection at the weakly observed voxels of the
+// spectral projector.
+//
+// A voxel whose PSF falls mostly outside the sensor (border voxels at depths
+// where the PSF is narrow and offset outwards by its lenslet phase) has a small
+// column mass s_i = (A'1)_i.  Every back projection (A'u)_i of such a voxel is
+// then small against the absolute rounding level of an FFT-based back
+// projection, which is set by the largest values of the transform rather than
+// by the entry, so the spectral forms give it few or no correct digits (and
+// negative values are possible).  The multiplicative solvers divide by exactly
+// these quantities (ISRA: X .* Htf ./ A'AX, deconvRL.m:52; Poisson RL:
+// X .* A'r ./ A'1) and amplify the error every iteration.  The plan therefore
+// lists, once, the voxels with s_i < frac * max(s) (frac 1e-2 unless the caller
+// sets it; sid_plan_set_weak_fraction) and, after each spectral back
+// projection, recomputes them exactly from the lenslet taps:
+//   B(c,b,a,v,u) = sum_{b',a',m1,m2} K[c][b][a][b'][a'](m1,m2) Ip[b'][a'](v+m2+dlo, u+m1+dlo)
+// (the transpose of the direct forward projection, FP32 sums).
+//
+// The weak voxels of a polyphase plane (c, b, a) lie on its border lines (the
+// column u = 0 or Lx-1, the row v = 0 or Ly-1), so they are grouped into runs
+// of <= 32 consecutive voxels along v (column runs) or u (row runs).  For a
+// column run, lane m1 of a warp holds the D taps K(m1, :) and the lattice
+// column s = u + m1 + dlo over the run's rows plus D - 1 in registers and
+// accumulates all run outputs (run x D FMAs per D + run loads); the warps of
+// the CTA split the N^2 tap arrays.  Row runs do the same on a transposed copy
+// of the lattice.  Both read zero-padded copies of the sensor lattice, so no
+// tap needs a bounds test.
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "sid_internal.cuh"
+
+namespace sid {
+
+namespace {
+
+constexpr int kWeakThreads = 256;
+constexpr int kRunMax = 32;   // voxels per run
+constexpr int kRunDMax = 32;  // largest tap extent the run kernel handles (else per voxel)
+
+struct WeakRun {
+    int plane;  // (c N + b) N + a
+    int fixed;  // u of a column run, v of a row run
+    int start;  // first v (column run) or u (row run)
+    int len;
+};
+
+__global__ void k_fill_ones(float* __restrict__ x, int64_t n)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        x[i] = 1.f;
+}
+
+// Zero-padded copies of the sensor lattice Ip[q][t][s] (q < N^2): pad[q][t + lo][s + lo]
+// (Hp x Wp) and its transpose padT[q][s + lo][t + lo] (Wp x Hp).
+__global__ void k_pad_lattice(const float* __restrict__ ip, float* __restrict__ pad, float* __restrict__ padT,
+                              int nq, int Lx, int Ly, int lo, int Wp, int Hp)
+{
+    const int64_t plane = (int64_t)Wp * Hp, n = plane * nq;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int q = (int)(i / plane);
+        const int64_t r = i - q * plane;
+        const int tp = (int)(r / Wp), sp = (int)(r - (int64_t)tp * Wp);
+        const int t = tp - lo, s = sp - lo;
+        const float v = (t >= 0 && t < Ly && s >= 0 && s < Lx) ? ip[((int64_t)q * Ly + t) * Lx + s] : 0.f;
+        pad[i] = v;
+        if (padT) padT[q * plane + (int64_t)sp * Hp + tp] = v;
+    }
+}
+
+// ROW = false: column runs (fixed u, v = start + j) on pad[q][t][s];
+// ROW = true:  row runs (fixed v, u = start + j) on padT[q][s][t].
+template <bool ROW>
+__global__ void __launch_bounds__(kWeakThreads)
+k_adj_runs(const float* __restrict__ taps, const float* __restrict__ lat, float* __restrict__ bp,
+           const WeakRun* __restrict__ runs, int nrun, int N, int Lx, int Ly, int D, int dlo, int lo, int Wp, int Hp,
+           int64_t tbs)
+{
+    constexpr int NW = kWeakThreads / 32;
+    constexpr int CM = kRunMax + kRunDMax - 1;
+    __shared__ float part[NW][kRunMax];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    // lane = tap index along the cross axis (m1 for column runs, m2 for row runs)
+    const int W = ROW ? Hp : Wp;                 // row pitch of the lattice copy
+    const int64_t plane = (int64_t)Wp * Hp;
+    for (int rk = blockIdx.x; rk < nrun; rk += gridDim.x) {
+        const WeakRun R = runs[rk];
+        const int64_t blk0 = (int64_t)R.plane * N;
+        float acc[kRunMax];
+#pragma unroll
+        for (int j = 0; j < kRunMax; ++j) acc[j] = 0.f;
+        if (lane < D) {
+            for (int q = warp; q < N * N; q += NW) {
+                const int bq = q / N, aq = q - bq * N;
+                const float* kb = taps + (blk0 + bq) * tbs + (int64_t)aq * D * D;
+                // taps along the run axis: K(m1 = lane, m2) (column) or K(m1, m2 = lane) (row)
+                float k[kRunDMax];
+#pragma unroll
+                for (int m = 0; m < kRunDMax; ++m)
+                    k[m] = m < D ? __ldg(ROW ? kb + (int64_t)m * D + lane : kb + (int64_t)lane * D + m) : 0.f;
+                // lattice line along the run axis at cross position fixed + lane + dlo
+                const float* line = lat + q * plane + (int64_t)(R.fixed + lane + dlo + lo) +
+                                    (int64_t)(R.start + dlo + lo) * W;
+                float col[CM];
+#pragma unroll
+                for (int r = 0; r < CM; ++r) col[r] = (r < R.len + D - 1) ? __ldg(line + (int64_t)r * W) : 0.f;
+#pragma unroll
+                for (int j = 0; j < kRunMax; ++j)
+#pragma unroll
+                    for (int m = 0; m < kRunDMax; ++m) acc[j] = fmaf(k[m], col[j + m], acc[j]);
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < kRunMax; ++j) {
+            float a = acc[j];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+            if (lane == 0) part[warp][j] = a;
+        }
+        __syncthreads();
+        if (threadIdx.x < R.len) {
+            float s = 0.f;
+#pragma unroll
+            for (int w = 0; w < NW; ++w) s += part[w][threadIdx.x];
+            const int u = ROW ? R.start + (int)threadIdx.x : R.fixed;
+            const int v = ROW ? R.fixed : R.start + (int)threadIdx.x;
+            bp[((int64_t)R.plane * Ly + v) * Lx + u] = s;
+        }
+        __syncthreads();
+    }
+}
+
+// Generic path (tap extent above kRunDMax): one CTA per voxel.
+__global__ void __launch_bounds__(kWeakThreads)
+k_adj_voxel(const float* __restrict__ taps, const float* __restrict__ ip, float* __restrict__ bp,
+            const int* __restrict__ list, int nweak, int N, int Lx, int Ly, int D, int dlo, int64_t tbs)
+{
+    __shared__ float red[kWeakThreads / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int w = blockIdx.x; w < nweak; w += gridDim.x) {
+        const int64_t i = list[w];
+        const int u = (int)(i % Lx);
+        const int64_t r0 = i / Lx;
+        const int v = (int)(r0 % Ly);
+        const int64_t blk0 = (r0 / Ly) * N;
+        const int m1lo = max(0, -u - dlo), m1hi = min(D, Lx - u - dlo);
+        const int m2lo = max(0, -v - dlo), m2hi = min(D, Ly - v - dlo);
+        const int n1 = m1hi - m1lo, n2 = m2hi - m2lo;
+        float acc = 0.f;
+        if (n1 > 0 && n2 > 0) {
+            const int items = N * N * n1;
+            for (int it = threadIdx.x; it < items; it += kWeakThreads) {
+                const int q = it / n1, m1 = m1lo + (it - q * n1);
+                const int bq = q / N, aq = q - bq * N;
+                const float* tp = taps + (blk0 + bq) * tbs + ((int64_t)aq * D + m1) * D + m2lo;
+                const float* xp = ip + ((int64_t)q * Ly + (v + m2lo + dlo)) * Lx + (u + m1 + dlo);
+                for (int j2 = 0; j2 < n2; ++j2) acc = fmaf(__ldg(tp + j2), __ldg(xp + (int64_t)j2 * Lx), acc);
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (lane == 0) red[warp] = acc;
+        __syncthreads();
+        if (warp == 0) {
+            acc = lane < kWeakThreads / 32 ? red[lane] : 0.f;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+            if (lane == 0) bp[i] = acc;
+        }
+        __syncthreads();
+    }
+}
+
+// Cover one plane's weak voxels (v, u), sorted by (v, u), with runs: each voxel
+// goes to the direction of its longer maximal run (ties: column), runs split
+// at kRunMax.
+void plane_runs(int plane, const std::vector<std::pair<int, int>>& vu, int Lx, int Ly, std::vector<WeakRun>& cols,
+                std::vector<WeakRun>& rows)
+{
+    std::vector<unsigned char> in((size_t)Lx * Ly, 0), as_row((size_t)Lx * Ly, 0);
+    for (auto& e : vu) in[(size_t)e.first * Lx + e.second] = 1;
+    auto at = [&](int v, int u) { return v >= 0 && v < Ly && u >= 0 && u < Lx && in[(size_t)v * Lx + u]; };
+    for (auto& e : vu) {
+        const int v = e.first, u = e.second;
+        int h = 1, c = 1;
+        for (int x = u - 1; at(v, x); --x) ++h;
+        for (int x = u + 1; at(v, x); ++x) ++h;
+        for (int y = v - 1; at(y, u); --y) ++c;
+        for (int y = v + 1; at(y, u); ++y) ++c;
+        as_row[(size_t)v * Lx + u] = h > c;
+    }
+    // row runs: consecutive u at fixed v among the voxels assigned to rows
+    for (int v = 0; v < Ly; ++v)
+        for (int u = 0; u < Lx;) {
+            if (!(in[(size_t)v * Lx + u] && as_row[(size_t)v * Lx + u])) { ++u; continue; }
+            int e = u;
+            while (e < Lx && e - u < kRunMax && in[(size_t)v * Lx + e] && as_row[(size_t)v * Lx + e]) ++e;
+            rows.push_back({plane, v, u, e - u});
+            u = e;
+        }
+    for (int u = 0; u < Lx; ++u)
+        for (int v = 0; v < Ly;) {
+            if (!(in[(size_t)v * Lx + u] && !as_row[(size_t)v * Lx + u])) { ++v; continue; }
+            int e = v;
+            while (e < Ly && e - v < kRunMax && in[(size_t)e * Lx + u] && !as_row[(size_t)e * Lx + u]) ++e;
+            cols.push_back({plane, u, v, e - v});
+            v = e;
+        }
+}
+
+}  // namespace
+
+// List the weakly observed voxels: s = A'1 through the plan's most accurate
+// spectral back projection (its error is far below the threshold), then the
+// in-frame voxels with s < p->weak_frac * max(s), grouped into runs.
+int weak_build(sid_plan* p)
+{
+    p->nweak = p->nweak_cols = p->nweak_rows = 0;
+    p->weak.release();
+    p->weak_pad.release();
+    if (p->weak_frac <= 0.0) return SID_OK;
+    const int64_t N = p->N, Lx = p->Lx, Ly = p->Ly, Z = p->Z;
+    const int64_t ni = N * N * Lx * Ly, n = ni * Z;
+    SID_REQUIRE(n < INT32_MAX, "spectral plan: volume too large for the weak-voxel list");
+    const int fmt = p->spec_f32 ? FMT_F32 : (p->spec_f24 ? FMT_F24 : FMT_I16);
+    DBuf ones, s;
+    SID_TRY(ones.alloc((size_t)ni * sizeof(float)));
+    SID_TRY(s.alloc((size_t)n * sizeof(float)));
+    k_fill_ones<<<1024, 256>>>(ones.as<float>(), ni);
+    SID_CHECK_LAUNCH();
+    SID_TRY(mask_vp(p, ones.as<float>(), 1, 0));
+    SID_TRY(spectral_adjoint(p, fmt, ones.as<float>(), s.as<float>(), 0));
+    std::vector<float> h((size_t)n);
+    SID_CUDA_TRY(cudaMemcpy(h.data(), s.p, (size_t)n * sizeof(float), cudaMemcpyDeviceToHost));
+    ones.release();
+    s.release();
+    const int64_t plane = Lx * Ly;
+    // in-frame test of polyphase index i: x = a + N u < X and y = b + N v < Y
+    auto in_frame = [&](int64_t i) {
+        const int64_t u = i % Lx, v = (i / Lx) % Ly, a = (i / plane) % N, b = (i / (plane * N)) % N;
+        return a + N * u < p->X && b + N * v < p->Y;
+    };
+    double smax = 0.0;
+    for (int64_t i = 0; i < n; ++i)
+        if (h[(size_t)i] > smax && in_frame(i)) smax = h[(size_t)i];
+    const double thr = p->weak_frac * smax;
+    std::vector<int> list;
+    for (int64_t i = 0; i < n; ++i)
+        if ((double)h[(size_t)i] < thr && in_frame(i)) list.push_back((int)i);
+    if (list.empty()) return SID_OK;
+    p->nweak = (int64_t)list.size();
+    if (p->g.D > kRunDMax) {  // per-voxel path
+        SID_TRY(p->weak.alloc(list.size() * sizeof(int)));
+        SID_CUDA_TRY(cudaMemcpy(p->weak.p, list.data(), list.size() * sizeof(int), cudaMemcpyHostToDevice));
+        return SID_OK;
+    }
+    std::vector<WeakRun> cols, rows;
+    for (size_t k = 0; k < list.size();) {
+        const int pl = (int)(list[k] / plane);
+        std::vector<std::pair<int, int>> vu;
+        for (; k < list.size() && list[k] / plane == pl; ++k)
+            vu.push_back({(int)((list[k] % plane) / Lx), (int)(list[k] % Lx)});
+        plane_runs(pl, vu, (int)Lx, (int)Ly, cols, rows);
+    }
+    std::vector<WeakRun> all(cols);
+    all.insert(all.end(), rows.begin(), rows.end());
+    SID_TRY(p->weak.alloc(all.size() * sizeof(WeakRun)));
+    SID_CUDA_TRY(cudaMemcpy(p->weak.p, all.data(), all.size() * sizeof(WeakRun), cudaMemcpyHostToDevice));
+    p->nweak_cols = (int64_t)cols.size();
+    p->nweak_rows = (int64_t)rows.size();
+    // padded lattice copies (plain and transposed)
+    const int64_t lo = std::max<int64_t>(0, -p->g.dlo), hi = std::max<int64_t>(0, p->g.D - 1 + p->g.dlo);
+    const int64_t Wp = Lx + lo + hi, Hp = Ly + lo + hi;
+    SID_TRY(p->weak_pad.alloc((size_t)(2 * N * N * Wp * Hp) * sizeof(float)));
+    return SID_OK;
+}
+
+// Overwrite the listed voxels of a spectral back projection bp = A' ip with
+// their exact values.
+int weak_fix(sid_plan* p, const float* ip, float* bp, cudaStream_t st)
+{
+    if (p->nweak == 0) return SID_OK;
+    SID_REQUIRE(p->taps_f.p, "spectral plan: lenslet taps missing for the weak-voxel back projection");
+    const int64_t tbs = cdiv(p->N * p->g.D * p->g.D, 32) * 32;
+    const int N = (int)p->N, Lx = (int)p->Lx, Ly = (int)p->Ly, D = (int)p->g.D, dlo = (int)p->g.dlo;
+    if (p->g.D > kRunDMax) {
+        const unsigned grid = (unsigned)std::min<int64_t>(p->nweak, 152 * 8);
+        k_adj_voxel<<<grid, kWeakThreads, 0, st>>>(p->taps_f.as<float>(), ip, bp, p->weak.as<int>(),
+                                                   (int)p->nweak, N, Lx, Ly, D, dlo, tbs);
+        SID_CHECK_LAUNCH();
+        return SID_OK;
+    }
+    const int lo = (int)std::max<int64_t>(0, -p->g.dlo), hi = (int)std::max<int64_t>(0, p->g.D - 1 + p->g.dlo);
+    const int Wp = Lx + lo + hi, Hp = Ly + lo + hi;
+    float* pad = p->weak_pad.as<float>();
+    float* padT = pad + (size_t)N * N * Wp * Hp;
+    k_pad_lattice<<<1024, 256, 0, st>>>(ip, pad, p->nweak_rows ? padT : nullptr, N * N, Lx, Ly, lo, Wp, Hp);
+    SID_CHECK_LAUNCH();
+    const WeakRun* runs = p->weak.as<WeakRun>();
+    if (p->nweak_cols) {
+        k_adj_runs<false><<<(unsigned)p->nweak_cols, kWeakThreads, 0, st>>>(
+            p->taps_f.as<float>(), pad, bp, runs, (int)p->nweak_cols, N, Lx, Ly, D, dlo, lo, Wp, Hp, tbs);
+        SID_CHECK_LAUNCH();
+    }
+    if (p->nweak_rows) {
+        k_adj_runs<true><<<(unsigned)p->nweak_rows, kWeakThreads, 0, st>>>(
+            p->taps_f.as<float>(), padT, bp, runs + p->nweak_cols, (int)p->nweak_rows, N, Lx, Ly, D, dlo, lo, Wp,
+            Hp, tbs);
+        SID_CHECK_LAUNCH();
+    }
+    return SID_OK;
+}
+
+}  // namespace sid
+
+using namespace sid;
+
+extern "C" int sid_plan_set_weak_fraction(sid_plan* p, double frac)
+{
+    SID_REQUIRE(p, "sid_plan_set_weak_fraction: NULL plan");
+    SID_REQUIRE(frac >= 0.0 && frac <= 1.0, "sid_plan_set_weak_fraction: fraction %g outside [0, 1]", frac);
+    SID_REQUIRE(p->spec_f32 || p->spec_f24 || p->spec_i16, "sid_plan_set_weak_fraction: plan has no spectral form");
+    p->weak_frac = frac;
+    return weak_build(p);
+}

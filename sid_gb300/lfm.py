@@ -124,10 +124,16 @@ class Projector:
 
     # -- info ---------------------------------------------------------------
     def info(self) -> dict:
-        buf = (ctypes.c_int64 * 12)()
+        buf = (ctypes.c_int64 * 14)()
         _lib.call("sid_plan_info", self._plan, ctypes.cast(buf, ctypes.c_void_p))
-        keys = ["M", "Nnum", "Z", "X", "Y", "Lx", "Ly", "D", "L", "device_bytes", "flags", "adj_separate"]
+        keys = ["M", "Nnum", "Z", "X", "Y", "Lx", "Ly", "D", "L", "device_bytes", "flags", "adj_separate",
+                "weak_voxels", "weak_launches"]
         return dict(zip(keys, list(buf)))
+
+    def set_weak_fraction(self, frac: float):
+        """Voxels with column mass A'1 below `frac` of the largest get exact back
+        projections in the spectral forms (default 1e-2; 0 turns it off)."""
+        _lib.call("sid_plan_set_weak_fraction", self._plan, float(frac))
 
     def close(self):
         self._finalizer()
@@ -180,6 +186,15 @@ class Projector:
         X = to_device(Xguess).clone()
         _lib.call("sid_deconv_isra", self._plan, self._method(method), Htf.data_ptr(), X.data_ptr(),
                   int(maxIter), float(lam), _stream_ptr())
+        return X
+
+    def rl_poisson(self, y, Xguess, maxIter, method=None) -> torch.Tensor:
+        """Poisson-likelihood Richardson-Lucy from the sensor image y:
+        X <- X .* A'(y ./ AX) ./ A'1 (the reference's deconvRL is the ISRA form)."""
+        y = to_device(y)
+        X = to_device(Xguess).clone()
+        _lib.call("sid_deconv_rl_poisson", self._plan, self._method(method), y.data_ptr(), X.data_ptr(),
+                  int(maxIter), _stream_ptr())
         return X
 
     def isra_host(self, Htf, Xguess, maxIter, lam=0.0, method=None) -> np.ndarray:

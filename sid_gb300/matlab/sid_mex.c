@@ -195,7 +195,7 @@ void mexFunction(int nlhs, mxArray* plhs[], int nrhs, const mxArray* prhs[])
     }
     if (!strcmp(cmd, "forward") || !strcmp(cmd, "adjoint")) {
         sid_plan* p = plan_arg(prhs[1]);
-        int64_t info[12];
+        int64_t info[14];
         sid_plan_info(p, info);
         const int fwd = !strcmp(cmd, "forward");
         mwSize dims[3] = {(mwSize)info[3], (mwSize)info[4], (mwSize)info[2]};
@@ -421,7 +421,7 @@ void mexFunction(int nlhs, mxArray* plhs[], int nrhs, const mxArray* prhs[])
             if (w && mxIsChar(w)) mxGetString(w, sv, sizeof(sv));
             ro.solver = !strcmp(sv, "ISRA") ? 1 : 0;
         }
-        int64_t info[12];
+        int64_t info[14];
         sid_plan_info(p, info);
         mwSize dv[3] = {(mwSize)info[3], (mwSize)info[4], (mwSize)info[2]};
         mxGPUArray* X = mxGPUCreateGPUArray(3, dv, mxSINGLE_CLASS, mxREAL, MX_GPU_DO_NOT_INITIALIZE);

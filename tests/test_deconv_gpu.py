@@ -54,6 +54,27 @@ def test_isra_cfg0_mixed_vs_fp64(gpu, oracle):
         assert rel_l2(out, ref) < tol, (m, rel_l2(out, ref))
 
 
+@pytest.mark.parametrize("method,tol", [("direct", 1e-5), ("spectral_f32", 1e-5), ("spectral_mixed", 1e-4)])
+def test_rl_poisson_matches_oracle(small, method, tol):
+    """Poisson-likelihood RL from the sensor image, 8 iterations, against FP64."""
+    from oracle import oracle as o
+    import sid_gb300 as s
+    H, y, P, fwd, bwd = small
+    X0 = np.asfortranarray(bwd(y).astype(np.float32))
+    ref = o.rl_poisson(fwd, bwd, y, 8, X0)
+    out = s.to_numpy(P.rl_poisson(y.astype(np.float32), X0, 8, method=method))
+    assert rel_l2(out, ref) < 10 * tol, rel_l2(out, ref)
+
+
+def test_rl_poisson_zero_rules(small):
+    """Zero image and zero start: every ratio is 0/0 and the result stays 0, finite."""
+    import sid_gb300 as s
+    H, y, P, fwd, bwd = small
+    out = s.to_numpy(P.rl_poisson(np.zeros_like(y, dtype=np.float32), np.zeros((y.shape[0], y.shape[1], H.shape[4]),
+                                                                               np.float32, order="F"), 2))
+    assert np.all(out == 0)
+
+
 def _pinned_fortran(a):
     """A Fortran-ordered float32 copy of `a` in page-locked host memory."""
     import torch
