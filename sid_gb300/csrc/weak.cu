@@ -18,7 +18,7 @@
 //
 // The weak voxels of a polyphase plane (c, b, a) lie on its border lines (the
 // column u = 0 or Lx-1, the row v = 0 or Ly-1), so they are grouped into runs
-// of <= 32 consecutive voxels along v (column runs) or u (row runs).  For a
+// of <= 24 consecutive voxels along v (column runs) or u (row runs).  For a
 // column run, lane m1 of a warp holds the D taps K(m1, :) and the lattice
 // column s = u + m1 + dlo over the run's rows plus D - 1 in registers and
 // accumulates all run outputs (run x D FMAs per D + run loads); the warps of
@@ -36,7 +36,7 @@ namespace sid {
 namespace {
 
 constexpr int kWeakThreads = 256;
-constexpr int kRunMax = 32;   // voxels per run
+constexpr int kRunMax = 24;   // voxels per run
 constexpr int kRunDMax = 32;  // largest tap extent the run kernel handles (else per voxel)
 
 struct WeakRun {
@@ -71,48 +71,57 @@ __global__ void k_pad_lattice(const float* __restrict__ ip, float* __restrict__ 
 
 // ROW = false: column runs (fixed u, v = start + j) on pad[q][t][s];
 // ROW = true:  row runs (fixed v, u = start + j) on padT[q][s][t].
-template <bool ROW>
+// Lanes take the cross-axis taps c (m1 of a column run, m2 of a row run) whose
+// lattice line lies on the sensor; when at most 16 do, each half-warp takes its
+// own tap array.  DM >= D bounds the tap loop, JR >= run length the outputs.
+template <bool ROW, int DM, int JR>
 __global__ void __launch_bounds__(kWeakThreads)
 k_adj_runs(const float* __restrict__ taps, const float* __restrict__ lat, float* __restrict__ bp,
            const WeakRun* __restrict__ runs, int nrun, int N, int Lx, int Ly, int D, int dlo, int lo, int Wp, int Hp,
            int64_t tbs)
 {
     constexpr int NW = kWeakThreads / 32;
-    constexpr int CM = kRunMax + kRunDMax - 1;
-    __shared__ float part[NW][kRunMax];
+    constexpr int CM = JR + DM - 1;
+    __shared__ float part[NW][JR];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    // lane = tap index along the cross axis (m1 for column runs, m2 for row runs)
-    const int W = ROW ? Hp : Wp;                 // row pitch of the lattice copy
+    const int W = ROW ? Hp : Wp;   // pitch of the lattice copy along the run axis
+    const int Lc = ROW ? Ly : Lx;  // lattice extent along the cross axis
     const int64_t plane = (int64_t)Wp * Hp;
     for (int rk = blockIdx.x; rk < nrun; rk += gridDim.x) {
         const WeakRun R = runs[rk];
         const int64_t blk0 = (int64_t)R.plane * N;
-        float acc[kRunMax];
+        const int clo = max(0, -R.fixed - dlo), chi = min(D, Lc - R.fixed - dlo);
+        const int G = (chi - clo) <= 16 ? 2 : 1;  // tap arrays per warp step
+        const int gw = 32 / G, g = lane / gw, c = clo + (lane - g * gw);
+        float acc[JR];
 #pragma unroll
-        for (int j = 0; j < kRunMax; ++j) acc[j] = 0.f;
-        if (lane < D) {
-            for (int q = warp; q < N * N; q += NW) {
+        for (int j = 0; j < JR; ++j) acc[j] = 0.f;
+        if (c < chi) {
+            for (int q = warp * G + g; q < N * N; q += NW * G) {
                 const int bq = q / N, aq = q - bq * N;
                 const float* kb = taps + (blk0 + bq) * tbs + (int64_t)aq * D * D;
-                // taps along the run axis: K(m1 = lane, m2) (column) or K(m1, m2 = lane) (row)
-                float k[kRunDMax];
+                // taps along the run axis: K(m1 = c, m2) (column) or K(m1, m2 = c) (row)
+                float k[DM];
 #pragma unroll
-                for (int m = 0; m < kRunDMax; ++m)
-                    k[m] = m < D ? __ldg(ROW ? kb + (int64_t)m * D + lane : kb + (int64_t)lane * D + m) : 0.f;
-                // lattice line along the run axis at cross position fixed + lane + dlo
-                const float* line = lat + q * plane + (int64_t)(R.fixed + lane + dlo + lo) +
+                for (int m = 0; m < DM; ++m)
+                    k[m] = m < D ? __ldg(ROW ? kb + (int64_t)m * D + c : kb + (int64_t)c * D + m) : 0.f;
+                // lattice line along the run axis at cross position fixed + c + dlo
+                const float* line = lat + q * plane + (int64_t)(R.fixed + c + dlo + lo) +
                                     (int64_t)(R.start + dlo + lo) * W;
                 float col[CM];
 #pragma unroll
                 for (int r = 0; r < CM; ++r) col[r] = (r < R.len + D - 1) ? __ldg(line + (int64_t)r * W) : 0.f;
 #pragma unroll
-                for (int j = 0; j < kRunMax; ++j)
+                for (int m = 0; m < DM; ++m) {
+                    if (m < D) {
 #pragma unroll
-                    for (int m = 0; m < kRunDMax; ++m) acc[j] = fmaf(k[m], col[j + m], acc[j]);
+                        for (int j = 0; j < JR; ++j) acc[j] = fmaf(k[m], col[j + m], acc[j]);
+                    }
+                }
             }
         }
 #pragma unroll
-        for (int j = 0; j < kRunMax; ++j) {
+        for (int j = 0; j < JR; ++j) {
             float a = acc[j];
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
@@ -172,9 +181,19 @@ k_adj_voxel(const float* __restrict__ taps, const float* __restrict__ ip, float*
     }
 }
 
+// A maximal run of `len` voxels as ceil(len / kRunMax) runs of near-equal length.
+void split_run(int plane, int fixed, int start, int len, std::vector<WeakRun>& out)
+{
+    const int pieces = (len + kRunMax - 1) / kRunMax;
+    for (int k = 0, s = start; k < pieces; ++k) {
+        const int l = len / pieces + (k < len % pieces ? 1 : 0);
+        out.push_back({plane, fixed, s, l});
+        s += l;
+    }
+}
+
 // Cover one plane's weak voxels (v, u), sorted by (v, u), with runs: each voxel
-// goes to the direction of its longer maximal run (ties: column), runs split
-// at kRunMax.
+// goes to the direction of its longer maximal run (ties: column).
 void plane_runs(int plane, const std::vector<std::pair<int, int>>& vu, int Lx, int Ly, std::vector<WeakRun>& cols,
                 std::vector<WeakRun>& rows)
 {
@@ -195,16 +214,16 @@ void plane_runs(int plane, const std::vector<std::pair<int, int>>& vu, int Lx, i
         for (int u = 0; u < Lx;) {
             if (!(in[(size_t)v * Lx + u] && as_row[(size_t)v * Lx + u])) { ++u; continue; }
             int e = u;
-            while (e < Lx && e - u < kRunMax && in[(size_t)v * Lx + e] && as_row[(size_t)v * Lx + e]) ++e;
-            rows.push_back({plane, v, u, e - u});
+            while (e < Lx && in[(size_t)v * Lx + e] && as_row[(size_t)v * Lx + e]) ++e;
+            split_run(plane, v, u, e - u, rows);
             u = e;
         }
     for (int u = 0; u < Lx; ++u)
         for (int v = 0; v < Ly;) {
             if (!(in[(size_t)v * Lx + u] && !as_row[(size_t)v * Lx + u])) { ++v; continue; }
             int e = v;
-            while (e < Ly && e - v < kRunMax && in[(size_t)e * Lx + u] && !as_row[(size_t)e * Lx + u]) ++e;
-            cols.push_back({plane, u, v, e - v});
+            while (e < Ly && in[(size_t)e * Lx + u] && !as_row[(size_t)e * Lx + u]) ++e;
+            split_run(plane, u, v, e - v, cols);
             v = e;
         }
 }
@@ -298,15 +317,24 @@ int weak_fix(sid_plan* p, const float* ip, float* bp, cudaStream_t st)
     k_pad_lattice<<<1024, 256, 0, st>>>(ip, pad, p->nweak_rows ? padT : nullptr, N * N, Lx, Ly, lo, Wp, Hp);
     SID_CHECK_LAUNCH();
     const WeakRun* runs = p->weak.as<WeakRun>();
-    if (p->nweak_cols) {
-        k_adj_runs<false><<<(unsigned)p->nweak_cols, kWeakThreads, 0, st>>>(
-            p->taps_f.as<float>(), pad, bp, runs, (int)p->nweak_cols, N, Lx, Ly, D, dlo, lo, Wp, Hp, tbs);
+    const float* taps = p->taps_f.as<float>();
+    const int nc = (int)p->nweak_cols, nr = (int)p->nweak_rows;
+    if (nc) {
+        if (D <= 16)
+            k_adj_runs<false, 16, kRunMax><<<nc, kWeakThreads, 0, st>>>(taps, pad, bp, runs, nc, N, Lx, Ly, D, dlo,
+                                                                        lo, Wp, Hp, tbs);
+        else
+            k_adj_runs<false, 32, kRunMax><<<nc, kWeakThreads, 0, st>>>(taps, pad, bp, runs, nc, N, Lx, Ly, D, dlo,
+                                                                        lo, Wp, Hp, tbs);
         SID_CHECK_LAUNCH();
     }
-    if (p->nweak_rows) {
-        k_adj_runs<true><<<(unsigned)p->nweak_rows, kWeakThreads, 0, st>>>(
-            p->taps_f.as<float>(), padT, bp, runs + p->nweak_cols, (int)p->nweak_rows, N, Lx, Ly, D, dlo, lo, Wp,
-            Hp, tbs);
+    if (nr) {
+        if (D <= 16)
+            k_adj_runs<true, 16, kRunMax><<<nr, kWeakThreads, 0, st>>>(taps, padT, bp, runs + nc, nr, N, Lx, Ly, D,
+                                                                       dlo, lo, Wp, Hp, tbs);
+        else
+            k_adj_runs<true, 32, kRunMax><<<nr, kWeakThreads, 0, st>>>(taps, padT, bp, runs + nc, nr, N, Lx, Ly, D,
+                                                                       dlo, lo, Wp, Hp, tbs);
         SID_CHECK_LAUNCH();
     }
     return SID_OK;
