@@ -11,6 +11,8 @@
  *   B        = sid_mex('adjoint', plan, I, method)
  *   X        = sid_mex('isra', plan, Htf, Xguess, maxIter, lambda, method)
  *   X        = sid_mex('ls_deconv', plan, df, max_iter, lamb_L1, lamb_L2, method)
+ *   X        = sid_mex('rl_poisson', plan, y, Xguess, maxIter, method)
+ *   sid_mex('weak_fraction', plan, frac)
  *   [X, G]   = sid_mex('ls_nnls', A, Y, opts)
  *   [X, Q]   = sid_mex('fast_nnls', A, Y, opts)
  *   [S, T]   = sid_mex('t_update', Y, T, S, opts)        opts.active, opts.Y optional
@@ -275,6 +277,33 @@ void mexFunction(int nlhs, mxArray* plhs[], int nrhs, const mxArray* prhs[])
         check(rc, cmd);
         plhs[0] = on_gpu ? mxGPUCreateMxArrayOnGPU(X) : mxGPUCreateMxArrayOnCPU(X);
         mxGPUDestroyGPUArray(X);
+        return;
+    }
+    if (!strcmp(cmd, "rl_poisson")) {
+        /* X = sid_mex('rl_poisson', plan, y, Xguess, maxIter, method): y (X x Y) and Xguess (X x Y x Z)
+         * single, host or gpuArray; the result lives where Xguess did */
+        sid_plan* p = plan_arg(prhs[1]);
+        const int method = method_arg(nrhs, prhs, 5);
+        const int on_gpu = mxIsGPUArray(prhs[3]);
+        const mxGPUArray* y = mxGPUCreateFromMxArray(prhs[2]);
+        const mxGPUArray* x0 = mxGPUCreateFromMxArray(prhs[3]);
+        if (mxGPUGetClassID(y) != mxSINGLE_CLASS || mxGPUGetClassID(x0) != mxSINGLE_CLASS)
+            mexErrMsgIdAndTxt("sid:type", "rl_poisson: y and Xguess must be single");
+        mxGPUArray* X = gpu_copy(x0);
+        mxGPUDestroyGPUArray(x0);
+        int rc = sid_deconv_rl_poisson(p, method, (const float*)mxGPUGetDataReadOnly(y), (float*)mxGPUGetData(X),
+                                       (int)mxGetScalar(prhs[4]), NULL);
+        if (rc == SID_OK) rc = sid_plan_sync(p, NULL);
+        mxGPUDestroyGPUArray(y);
+        if (rc != SID_OK) mxGPUDestroyGPUArray(X);
+        check(rc, cmd);
+        plhs[0] = on_gpu ? mxGPUCreateMxArrayOnGPU(X) : mxGPUCreateMxArrayOnCPU(X);
+        mxGPUDestroyGPUArray(X);
+        return;
+    }
+    if (!strcmp(cmd, "weak_fraction")) {
+        /* sid_mex('weak_fraction', plan, frac) */
+        check(sid_plan_set_weak_fraction(plan_arg(prhs[1]), mxGetScalar(prhs[2])), cmd);
         return;
     }
     if (!strcmp(cmd, "t_update") || !strcmp(cmd, "s_update")) {
