@@ -183,6 +183,22 @@ int sid_gram(sid_ctx* ctx, const float* A, int64_t P, int64_t K, float* G, int p
 int sid_cross(sid_ctx* ctx, const float* A, const void* Y, int ydtype, int64_t P, int64_t K, int64_t F,
               float* h, int prec, void* stream);
 
+/* ---- Movie scans -------------------------------------------------------------
+ * [bg_spatial, bg_temporal] = rank_1_factorization(Y, maxIter)   rank_1_factorization.m:1
+ * std_image = compute_std_image(Y, bg_spatial, bg_temporal)      compute_std_image.m:1
+ * (the two calls of sid_main.m:95,101).  Y: P x F movie (device, column-major,
+ * SID_DTYPE_F32 or SID_DTYPE_F16); bg_spatial: P floats, bg_temporal: F floats
+ * (device outputs); maxIter >= 1.  std_image (P floats, device) may be NULL;
+ * when given it is computed in the same pass over Y as the last spatial
+ * update.  Negative variances (rounding) give 0 rather than MATLAB's complex
+ * square root. */
+int sid_rank1_background(sid_ctx* ctx, const void* Y, int ydtype, int64_t P, int64_t F, int maxIter,
+                         float* bg_spatial, float* bg_temporal, float* std_image, void* stream);
+/* std_image = compute_std_image(Y, y_1, y_2)   compute_std_image.m:1.  y_1 (P) and
+ * y_2 (F) are device floats or NULL for zeros (compute_std_image.m:17-19). */
+int sid_std_image(sid_ctx* ctx, const void* Y, int ydtype, int64_t P, int64_t F, const float* y1,
+                  const float* y2, float* std_image, void* stream);
+
 /* ---- NNLS solvers -----------------------------------------------------------
  * Options mirror the reference's opts fields and defaults. */
 typedef struct {

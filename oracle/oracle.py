@@ -551,6 +551,37 @@ def fast_nnls(A, Y, opts=None, Q=None, df=None, h=None, return_iters=False):
 # ----------------------------------------------------------------------------
 # NMF steps: T_update.m:5-78 and S_update.m:4-80
 # ----------------------------------------------------------------------------
+def rank_1_factorization(Y, maxIter=1):
+    """[bg_spatial, bg_temporal] = rank_1_factorization(Y, maxIter)
+    (rank_1_factorization.m:30-39): alternate t = s'Y / ||.||, s = Y t', s
+    normalised except after the last iteration; s starts at ones/sqrt(P)."""
+    Y = np.asarray(Y, dtype=np.float64)
+    s = np.ones(Y.shape[0]) / np.sqrt(Y.shape[0])
+    t = None
+    for it in range(1, int(maxIter) + 1):
+        t = s @ Y
+        t = t / np.linalg.norm(t)
+        s = Y @ t
+        if it < maxIter:
+            s = s / np.linalg.norm(s)
+    return s, t
+
+
+def compute_std_image(Y, y_1=None, y_2=None):
+    """compute_std_image.m:17-26: sqrt((A - y1.^2)/F - B.^2 + 2 B.*y1*C -
+    y1.^2*C^2) with A = sum(Y.^2, 2), B = mean(Y, 2), C = mean(y2); a negative
+    value (rounding) gives 0 where MATLAB would return a complex root."""
+    Y = np.asarray(Y, dtype=np.float64)
+    P, F = Y.shape
+    y1 = np.zeros(P) if y_1 is None else np.asarray(y_1, dtype=np.float64).reshape(-1)
+    y2 = np.zeros(F) if y_2 is None else np.asarray(y_2, dtype=np.float64).reshape(-1)
+    A = np.sum(Y ** 2, axis=1)
+    B = Y.mean(axis=1)
+    C = y2.mean()
+    v = (A - y1 ** 2) / len(y2) - B ** 2 + 2 * B * y1 * C - y1 ** 2 * C ** 2
+    return np.sqrt(np.maximum(v, 0.0))
+
+
 def _matlab_zscore(T):
     """MATLAB zscore(T): along the first non-singleton dimension (columns of
     an R x F matrix with R > 1), N-1 normalisation, a zero standard deviation

@@ -63,6 +63,8 @@ SIGNATURES = {
     "sid_ctx_destroy": [P],
     "sid_ctx_sync": [P, P],
     "sid_gram": [P, P, I64, I64, P, I32, P],
+    "sid_rank1_background": [P, P, I32, I64, I64, I32, P, P, P, P],
+    "sid_std_image": [P, P, I32, I64, I64, P, P, P, P],
     "sid_cross": [P, P, P, I32, I64, I64, I64, P, I32, P],
     "sid_ls_nnls_defaults": [P],
     "sid_fast_nnls_defaults": [P],

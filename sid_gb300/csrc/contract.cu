@@ -134,6 +134,7 @@ extern "C" int sid_ctx_destroy(sid_ctx* c)
     for (DBuf* x : b) x->release();
     for (DBuf& x : c->nn) x.release();
     for (DBuf& x : c->mf) x.release();
+    for (DBuf& x : c->bg) x.release();
     delete c;
     return SID_OK;
 }

@@ -360,7 +360,7 @@ static int launch_gemm(const GemmMaps& maps, int npass, int m, int n, int nkb, i
 }
 
 // Tile width and split-K choice (the project's autotuner for this kernel).
-// For each tile width BN in {256, 128, 64} split K until there are >= 4 waves
+// For each tile width BN in {256, 192, 128, 64} split K until there are >= 4 waves
 // of CTAs on the 152 SMs (or a split would hold fewer than 8 K blocks), then
 // estimate the time as waves x K blocks per CTA x BN / efficiency(BN) and keep
 // the fastest.  The efficiencies model tcgen05's shared-memory operand traffic
@@ -370,11 +370,11 @@ static int launch_gemm(const GemmMaps& maps, int npass, int m, int n, int nkb, i
 void gemm_autotune(int m, int n, int nkb, int* bn, int* splitk)
 {
     const int sms = 152;
-    const int cands[3] = {256, 128, 64};
-    const double eff[3] = {1.0, 0.85, 0.45};
+    const int cands[4] = {256, 192, 128, 64};
+    const double eff[4] = {1.0, 0.95, 0.85, 0.45};
     double best = 1e300;
     int bbn = 256, bs = 1;
-    for (int i = 0; i < 3; ++i) {
+    for (int i = 0; i < 4; ++i) {
         const int c = cands[i];
         const int64_t tiles = cdiv(m, GEMM_BM) * cdiv(n, c);
         int s = 1;
@@ -422,6 +422,7 @@ int gemm_tn(const void* const* A, const void* const* B, int npass, int64_t m, in
     int rc;
     switch (bn) {
     case 256: rc = launch_gemm<256, 4>(maps, npass, (int)m, (int)n, nkb, splitk, bf16, out, ldo, sstride, err, st); break;
+    case 192: rc = launch_gemm<192, 5>(maps, npass, (int)m, (int)n, nkb, splitk, bf16, out, ldo, sstride, err, st); break;
     case 128: rc = launch_gemm<128, 6>(maps, npass, (int)m, (int)n, nkb, splitk, bf16, out, ldo, sstride, err, st); break;
     case 64: rc = launch_gemm<64, 8>(maps, npass, (int)m, (int)n, nkb, splitk, bf16, out, ldo, sstride, err, st); break;
     default: set_error("gemm: unsupported tile width %d", bn); return SID_EINVAL;

@@ -1,0 +1,304 @@
+// movie.cu -- whole-movie scans: the rank-1 background factorisation and the
+// standard-deviation image (rank_1_factorization.m, compute_std_image.m).
+//
+// The movie Y is P x F, column-major (frame j is the contiguous column
+// Y(:, j)), FP32 or FP16.  Both scans are HBM-bound:
+//   column pass  t_j = sum_i s_i Y(i, j)            one CTA per frame
+//   row pass     s_i = sum_j Y(i, j) t_j, and optionally A_i = sum_j Y(i,j)^2,
+//                B_i = sum_j Y(i, j)                 one thread per pixel, t staged
+//                                                    in shared memory by frame chunks
+// Each byte of Y is read once per pass; the standard-deviation image needs A
+// and B, which the last spatial update of the factorisation computes in the
+// same pass.  Sums are FP32 over blocks of kSub terms, the blocks added in FP64.
+#include <algorithm>
+#include <cuda_fp16.h>
+
+#include "sid_internal.cuh"
+
+namespace sid {
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kSub = 32;        // FP32 terms per FP64 addition
+constexpr int kTChunk = 2048;   // frames of t staged per shared-memory round
+
+__device__ __forceinline__ float ld(const float* p) { return __ldcs(p); }
+__device__ __forceinline__ float ld(const __half* p) { return __half2float(__ldcs(p)); }
+
+__device__ __forceinline__ double block_sum(double v, double* red)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) red[warp] = v;
+    __syncthreads();
+    v = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+    if (warp == 0) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    }
+    return v;  // valid in thread 0
+}
+
+// t_j = scale_s * sum_i s_i Y(i, j); s == nullptr means s_i = 1.
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+k_col_pass(const T* __restrict__ Y, int64_t P, int64_t F, const float* __restrict__ s, float scale_s,
+           double* __restrict__ t)
+{
+    constexpr int U = 8;  // independent loads in flight per thread
+    __shared__ double red[kThreads / 32];
+    for (int64_t j = blockIdx.x; j < F; j += gridDim.x) {
+        const T* col = Y + j * P;
+        double acc = 0.0;
+        int64_t i = threadIdx.x;
+        for (; i + (U - 1) * kThreads < P; i += U * kThreads) {
+            float y[U], w[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                y[u] = ld(col + i + u * kThreads);
+                w[u] = s ? s[i + u * kThreads] : 1.f;
+            }
+            float part = 0.f;
+#pragma unroll
+            for (int u = 0; u < U; ++u) part = fmaf(w[u], y[u], part);
+            acc += part;
+        }
+        float part = 0.f;
+        for (; i < P; i += kThreads) part = fmaf(s ? s[i] : 1.f, ld(col + i), part);
+        acc += part;
+        acc = block_sum(acc, red);
+        if (threadIdx.x == 0) t[j] = acc * (double)scale_s;
+    }
+}
+
+// Per pixel i: s_i = sum_j Y(i,j) t_j (t != nullptr), A_i = sum_j Y(i,j)^2 and
+// B_i = sum_j Y(i,j) (stats != 0).
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+k_row_pass(const T* __restrict__ Y, int64_t P, int64_t F, const float* __restrict__ t, double* __restrict__ s_out,
+           double* __restrict__ a_out, double* __restrict__ b_out, int stats)
+{
+    __shared__ float ts[kTChunk];
+    const int64_t i = blockIdx.x * (int64_t)kThreads + threadIdx.x;
+    const bool live = i < P;
+    double sd = 0.0, ad = 0.0, bd = 0.0;
+    for (int64_t j0 = 0; j0 < F; j0 += kTChunk) {
+        const int nj = (int)std::min<int64_t>(kTChunk, F - j0);
+        if (t) {
+            __syncthreads();
+            for (int k = threadIdx.x; k < nj; k += kThreads) ts[k] = t[j0 + k];
+            __syncthreads();
+        }
+        if (!live) continue;
+        const T* yp = Y + i + j0 * P;
+        for (int k0 = 0; k0 < nj; k0 += kSub) {
+            const int kn = min(kSub, nj - k0);
+            float sp = 0.f, ap = 0.f, bp = 0.f;
+            if (kn == kSub) {
+                float y[kSub];
+#pragma unroll
+                for (int k = 0; k < kSub; ++k) y[k] = ld(yp + (int64_t)(k0 + k) * P);
+#pragma unroll
+                for (int k = 0; k < kSub; ++k) {
+                    if (t) sp = fmaf(y[k], ts[k0 + k], sp);
+                    ap = fmaf(y[k], y[k], ap);
+                    bp += y[k];
+                }
+            } else {
+                for (int k = 0; k < kn; ++k) {
+                    const float y = ld(yp + (int64_t)(k0 + k) * P);
+                    if (t) sp = fmaf(y, ts[k0 + k], sp);
+                    ap = fmaf(y, y, ap);
+                    bp += y;
+                }
+            }
+            sd += sp;
+            ad += ap;
+            bd += bp;
+        }
+    }
+    if (!live) return;
+    if (s_out) s_out[i] = sd;
+    if (stats) {
+        a_out[i] = ad;
+        b_out[i] = bd;
+    }
+}
+
+// sum of squares of x (n doubles) -> *out (one CTA)
+__global__ void k_sumsq(const double* __restrict__ x, int64_t n, double* __restrict__ out)
+{
+    __shared__ double red[kThreads / 32];
+    double acc = 0.0;
+    for (int64_t i = threadIdx.x; i < n; i += kThreads) acc += x[i] * x[i];
+    acc = block_sum(acc, red);
+    if (threadIdx.x == 0) *out = acc;
+}
+
+// partial sums of squares per CTA; the last CTA adds them (deterministic order)
+__global__ void k_sumsq_big(const double* __restrict__ x, int64_t n, double* __restrict__ part,
+                            unsigned int* __restrict__ done, double* __restrict__ out)
+{
+    __shared__ double red[kThreads / 32];
+    __shared__ bool last;
+    double acc = 0.0;
+    for (int64_t i = blockIdx.x * (int64_t)kThreads + threadIdx.x; i < n; i += (int64_t)gridDim.x * kThreads)
+        acc += x[i] * x[i];
+    acc = block_sum(acc, red);
+    if (threadIdx.x == 0) {
+        part[blockIdx.x] = acc;
+        __threadfence();
+        last = atomicAdd(done, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (last && threadIdx.x == 0) {
+        __threadfence();
+        double s = 0.0;
+        for (unsigned b = 0; b < gridDim.x; ++b) s += part[b];
+        *out = s;
+        *done = 0;
+    }
+}
+
+// y = x / sqrt(*ss) (or x when ss == nullptr), FP64 -> FP32
+__global__ void k_scale_out(const double* __restrict__ x, int64_t n, const double* __restrict__ ss,
+                            float* __restrict__ y)
+{
+    const double inv = ss ? 1.0 / sqrt(*ss) : 1.0;
+    for (int64_t i = blockIdx.x * (int64_t)kThreads + threadIdx.x; i < n; i += (int64_t)gridDim.x * kThreads)
+        y[i] = (float)(x[i] * inv);
+}
+
+// mean of y2 (F floats; y2 == nullptr: 0) -> *c (one CTA)
+__global__ void k_mean(const float* __restrict__ y2, int64_t F, double* __restrict__ c)
+{
+    __shared__ double red[kThreads / 32];
+    double acc = 0.0;
+    if (y2)
+        for (int64_t i = threadIdx.x; i < F; i += kThreads) acc += y2[i];
+    acc = block_sum(acc, red);
+    if (threadIdx.x == 0) *c = acc / (double)F;
+}
+
+// std = sqrt((A - y1^2)/F - Bm^2 + 2 Bm y1 C - y1^2 C^2), Bm = B / F
+// (compute_std_image.m:22-26); negative rounding residue -> 0.
+__global__ void k_std(const double* __restrict__ A, const double* __restrict__ B, const float* __restrict__ y1,
+                      const double* __restrict__ c, int64_t P, int64_t F, float* __restrict__ out)
+{
+    const double C = *c, invF = 1.0 / (double)F;
+    for (int64_t i = blockIdx.x * (int64_t)kThreads + threadIdx.x; i < P; i += (int64_t)gridDim.x * kThreads) {
+        const double a = y1 ? (double)y1[i] : 0.0;
+        const double bm = B[i] * invF;
+        const double v = (A[i] - a * a) * invF - bm * bm + 2.0 * bm * a * C - a * a * C * C;
+        out[i] = (float)sqrt(v > 0.0 ? v : 0.0);
+    }
+}
+
+unsigned grid_for(int64_t n) { return (unsigned)std::min<int64_t>(cdiv(n, kThreads), 152 * 16); }
+
+template <typename T>
+int background(sid_ctx* c, const T* Y, int64_t P, int64_t F, int maxIter, float* bg_s, float* bg_t, float* std_img,
+               cudaStream_t st)
+{
+    SID_TRY(c->bg[0].alloc((size_t)P * sizeof(double)));                  // s (FP64)
+    SID_TRY(c->bg[1].alloc((size_t)(F + 4096) * sizeof(double)));         // t, scalars, partials
+    SID_TRY(c->bg[4].alloc(sizeof(unsigned int)));
+    double* sd = c->bg[0].as<double>();
+    double* td = c->bg[1].as<double>();
+    double* ss = td + F;       // sum of squares of t or s
+    double* cm = td + F + 1;   // mean of t
+    double* part = td + F + 8;
+    unsigned int* done = c->bg[4].as<unsigned int>();
+    SID_CUDA_TRY(cudaMemsetAsync(done, 0, sizeof(unsigned int), st));
+    const bool stats = std_img != nullptr;
+    if (stats) {
+        SID_TRY(c->bg[2].alloc((size_t)P * sizeof(double)));
+        SID_TRY(c->bg[3].alloc((size_t)P * sizeof(double)));
+    }
+    const unsigned gcol = (unsigned)std::min<int64_t>(F, 152 * 8), grow = (unsigned)cdiv(P, kThreads);
+    const unsigned gred = std::min<unsigned>(grid_for(P), 4000);
+    for (int it = 1; it <= maxIter; ++it) {
+        // bg_temporal = bg_spatial' * Y, normalised (rank_1_factorization.m:33-34); the
+        // first bg_spatial is ones / sqrt(P) (:30)
+        if (it == 1)
+            k_col_pass<T><<<gcol, kThreads, 0, st>>>(Y, P, F, nullptr, (float)(1.0 / sqrt((double)P)), td);
+        else
+            k_col_pass<T><<<gcol, kThreads, 0, st>>>(Y, P, F, bg_s, 1.f, td);
+        SID_CHECK_LAUNCH();
+        k_sumsq<<<1, kThreads, 0, st>>>(td, F, ss);
+        SID_CHECK_LAUNCH();
+        k_scale_out<<<grid_for(F), kThreads, 0, st>>>(td, F, ss, bg_t);
+        SID_CHECK_LAUNCH();
+        // bg_spatial = Y * bg_temporal' (:35), normalised except after the last iteration (:36-38)
+        const bool last = it == maxIter;
+        k_row_pass<T><<<grow, kThreads, 0, st>>>(Y, P, F, bg_t, sd, stats && last ? c->bg[2].as<double>() : nullptr,
+                                                 stats && last ? c->bg[3].as<double>() : nullptr,
+                                                 stats && last ? 1 : 0);
+        SID_CHECK_LAUNCH();
+        if (!last) {
+            k_sumsq_big<<<gred, kThreads, 0, st>>>(sd, P, part, done, ss);
+            SID_CHECK_LAUNCH();
+        }
+        k_scale_out<<<grid_for(P), kThreads, 0, st>>>(sd, P, last ? nullptr : ss, bg_s);
+        SID_CHECK_LAUNCH();
+    }
+    if (stats) {
+        k_mean<<<1, kThreads, 0, st>>>(bg_t, F, cm);
+        SID_CHECK_LAUNCH();
+        k_std<<<grid_for(P), kThreads, 0, st>>>(c->bg[2].as<double>(), c->bg[3].as<double>(), bg_s, cm, P, F,
+                                                  std_img);
+        SID_CHECK_LAUNCH();
+    }
+    return SID_OK;
+}
+
+template <typename T>
+int std_image(sid_ctx* c, const T* Y, int64_t P, int64_t F, const float* y1, const float* y2, float* out,
+              cudaStream_t st)
+{
+    SID_TRY(c->bg[1].alloc((size_t)(F + 4096) * sizeof(double)));
+    SID_TRY(c->bg[2].alloc((size_t)P * sizeof(double)));
+    SID_TRY(c->bg[3].alloc((size_t)P * sizeof(double)));
+    double* cm = c->bg[1].as<double>() + F + 1;
+    k_row_pass<T><<<(unsigned)cdiv(P, kThreads), kThreads, 0, st>>>(Y, P, F, nullptr, nullptr, c->bg[2].as<double>(),
+                                                                    c->bg[3].as<double>(), 1);
+    SID_CHECK_LAUNCH();
+    k_mean<<<1, kThreads, 0, st>>>(y2, F, cm);
+    SID_CHECK_LAUNCH();
+    k_std<<<grid_for(P), kThreads, 0, st>>>(c->bg[2].as<double>(), c->bg[3].as<double>(), y1, cm, P, F, out);
+    SID_CHECK_LAUNCH();
+    return SID_OK;
+}
+
+}  // namespace
+
+}  // namespace sid
+
+using namespace sid;
+
+extern "C" int sid_rank1_background(sid_ctx* c, const void* Y, int ydtype, int64_t P, int64_t F, int maxIter,
+                                    float* bg_spatial, float* bg_temporal, float* std_img, void* stream)
+{
+    SID_REQUIRE(c && Y && bg_spatial && bg_temporal, "sid_rank1_background: NULL argument");
+    SID_REQUIRE(P > 0 && F > 0, "sid_rank1_background: empty movie (P=%lld F=%lld)", (long long)P, (long long)F);
+    SID_REQUIRE(maxIter >= 1, "sid_rank1_background: maxIter must be >= 1 (rank_1_factorization.m:31)");
+    SID_REQUIRE(ydtype == SID_DTYPE_F32 || ydtype == SID_DTYPE_F16, "sid_rank1_background: unknown dtype %d", ydtype);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (ydtype == SID_DTYPE_F16)
+        return background(c, static_cast<const __half*>(Y), P, F, maxIter, bg_spatial, bg_temporal, std_img, st);
+    return background(c, static_cast<const float*>(Y), P, F, maxIter, bg_spatial, bg_temporal, std_img, st);
+}
+
+extern "C" int sid_std_image(sid_ctx* c, const void* Y, int ydtype, int64_t P, int64_t F, const float* y1,
+                             const float* y2, float* out, void* stream)
+{
+    SID_REQUIRE(c && Y && out, "sid_std_image: NULL argument");
+    SID_REQUIRE(P > 0 && F > 0, "sid_std_image: empty movie (P=%lld F=%lld)", (long long)P, (long long)F);
+    SID_REQUIRE(ydtype == SID_DTYPE_F32 || ydtype == SID_DTYPE_F16, "sid_std_image: unknown dtype %d", ydtype);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (ydtype == SID_DTYPE_F16) return std_image(c, static_cast<const __half*>(Y), P, F, y1, y2, out, st);
+    return std_image(c, static_cast<const float*>(Y), P, F, y1, y2, out, st);
+}
