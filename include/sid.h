@@ -115,6 +115,14 @@ int sid_plan_sync(sid_plan* plan, void* stream);
 int sid_plan_timing_enable(sid_plan* plan, int on);
 int sid_plan_timing_read(sid_plan* plan, double* total_ms, int64_t* launches);
 
+/* Neuron-kernel composition (reconstruct_S.m:110-114,126-127,188-189): with a
+ * kernel set, every projection of the plan is P(convn(X, kernel, 'same')) and
+ * every back projection convn(P'(y), kernel, 'same') -- one kernel both ways,
+ * as the reference composes them -- for the projector calls and all solvers.
+ * kernel: HOST kx x ky x kz single, column-major (e.g. generate_kernel.m:1);
+ * each size <= 64.  NULL or a zero size removes it. */
+int sid_plan_set_kernel(sid_plan* plan, const float* kernel, int64_t kx, int64_t ky, int64_t kz);
+
 /* ---- Deconvolution -------------------------------------------------------
  * Xguess = deconvRL(fwd, bwd, Htf, maxIter, Xguess, opts)   deconvRL.m:1
  * ISRA: X <- X .* Htf ./ (A'A X + lambda) with inf -> 0 and NaN -> 0

@@ -551,6 +551,18 @@ def fast_nnls(A, Y, opts=None, Q=None, df=None, h=None, return_iters=False):
 # ----------------------------------------------------------------------------
 # NMF steps: T_update.m:5-78 and S_update.m:4-80
 # ----------------------------------------------------------------------------
+def convn_same(V, k):
+    """MATLAB convn(V, k, 'same') in FP64: the central part of the full
+    convolution, starting at floor(size(k) / 2) along each axis."""
+    from scipy.signal import convolve
+    V = np.asarray(V, dtype=np.float64)
+    k = np.asarray(k, dtype=np.float64)
+    k = k.reshape(k.shape + (1,) * (V.ndim - k.ndim))
+    full = convolve(V, k, mode="full", method="direct")
+    sl = tuple(slice(kn // 2, kn // 2 + vn) for vn, kn in zip(V.shape, k.shape))
+    return np.asfortranarray(full[sl])
+
+
 def rank_1_factorization(Y, maxIter=1):
     """[bg_spatial, bg_temporal] = rank_1_factorization(Y, maxIter)
     (rank_1_factorization.m:30-39): alternate t = s'Y / ||.||, s = Y t', s

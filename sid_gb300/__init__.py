@@ -17,6 +17,7 @@ from .lfm import (  # noqa: F401
     deconvRL,
     forwardProjectACC,
     forwardProjectGPU,
+    generate_kernel,
     generate_LFM_library_GPU,
     library_boxes,
     reconstruct_S,

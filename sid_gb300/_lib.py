@@ -48,6 +48,7 @@ SIGNATURES = {
     "sid_plan_destroy": [P],
     "sid_plan_info": [P, P],
     "sid_plan_set_weak_fraction": [P, ctypes.c_double],
+    "sid_plan_set_kernel": [P, P, I64, I64, I64],
     "sid_forward": [P, I32, P, P, P],
     "sid_adjoint": [P, I32, P, P, P],
     "sid_forward_host": [P, I32, P, P],

@@ -12,8 +12,16 @@ namespace sid {
 
 static cudaStream_t as_stream(void* s) { return static_cast<cudaStream_t>(s); }
 
+// Projection in the polyphase layout; with a neuron kernel set, the volume is
+// convolved with it first (reconstruct_S.m:126) and back projections are
+// convolved after (:127).
 int fwd_poly(sid_plan* p, int method, const float* vp, float* ip, cudaStream_t st)
 {
+    if (p->kdims[0]) {
+        SID_TRY(p->kvol[2].alloc((size_t)(vol_plane_elems(p) * p->Z) * sizeof(float)));
+        SID_TRY(conv_poly(p, vp, p->kvol[2].as<float>(), st));
+        vp = p->kvol[2].as<float>();
+    }
     switch (method) {
     case SID_METHOD_DIRECT: return direct_forward(p, vp, ip, p->errflag.as<int>(), st);
     case SID_METHOD_SPECTRAL_F32: return spectral_forward(p, false, vp, ip, st);
@@ -25,8 +33,16 @@ int fwd_poly(sid_plan* p, int method, const float* vp, float* ip, cudaStream_t s
 }
 
 // Spectral back projections are followed by the exact recomputation of the
-// weakly observed voxels (weak.cu).
+// weakly observed voxels (weak.cu), then by the neuron kernel if one is set.
+static int adj_raw(sid_plan* p, int method, const float* ip, float* bp, cudaStream_t st);
+
 int adj_poly(sid_plan* p, int method, const float* ip, float* bp, cudaStream_t st)
+{
+    SID_TRY(adj_raw(p, method, ip, bp, st));
+    return p->kdims[0] ? conv_poly(p, bp, bp, st) : SID_OK;
+}
+
+static int adj_raw(sid_plan* p, int method, const float* ip, float* bp, cudaStream_t st)
 {
     int fmt = FMT_F32;
     switch (method) {

@@ -184,8 +184,8 @@ extern "C" int sid_plan_destroy(sid_plan* p)
 {
     if (!p) return SID_OK;
     DBuf* bufs[] = {&p->taps_f, &p->taps_b, &p->khat_f32, &p->khat_i16, &p->rstep, &p->khat_f24h, &p->khat_f24l,
-                    &p->twiddle, &p->weak, &p->weak_pad, &p->vp, &p->ip, &p->bp, &p->ipart, &p->vhat,
-                    &p->ihat, &p->bhat, &p->red, &p->errflag};
+                    &p->twiddle, &p->weak, &p->weak_pad, &p->kern, &p->kvol[0], &p->kvol[1], &p->kvol[2],
+                    &p->vp, &p->ip, &p->bp, &p->ipart, &p->vhat, &p->ihat, &p->bhat, &p->red, &p->errflag};
     for (DBuf* b : bufs) b->release();
     for (DBuf& b : p->ws) b.release();
     p->timer.release();
@@ -201,8 +201,9 @@ extern "C" int sid_plan_info(const sid_plan* p, int64_t* info)
 {
     SID_REQUIRE(p && info, "sid_plan_info: NULL argument");
     const DBuf* bufs[] = {&p->taps_f, &p->taps_b, &p->khat_f32, &p->khat_i16, &p->rstep, &p->khat_f24h,
-                          &p->khat_f24l, &p->twiddle, &p->weak, &p->weak_pad, &p->vp, &p->ip, &p->bp,
-                          &p->ipart, &p->vhat, &p->ihat, &p->bhat, &p->red};
+                          &p->khat_f24l, &p->twiddle, &p->weak, &p->weak_pad, &p->kern, &p->kvol[0],
+                          &p->kvol[1], &p->kvol[2], &p->vp, &p->ip, &p->bp, &p->ipart, &p->vhat, &p->ihat,
+                          &p->bhat, &p->red};
     int64_t bytes = 0;
     for (const DBuf* b : bufs) bytes += (int64_t)b->bytes;
     for (const DBuf& b : p->ws) bytes += (int64_t)b.bytes;

@@ -152,6 +152,10 @@ struct sid_plan {
     sid::DBuf errflag;          // device int: nonzero after a bounded wait expired
     sid::KTimer timer;          // dominant-kernel timing (sid_plan_timing_*)
     int zsplit;
+    // neuron-kernel composition (sid_plan_set_kernel): kernel kx x ky x kz, two volume
+    // scratch buffers and a polyphase one
+    sid::DBuf kern, kvol[3];
+    int64_t kdims[3] = {0, 0, 0};
     // host-array calls: [0] work stream, [1] side stream (copies, higher priority);
     // events: [0] input volume converted, [1] Htf converted, [2] caller's stream 0
     cudaStream_t hstream[2] = {nullptr, nullptr};
@@ -166,6 +170,7 @@ int spectral_forward(sid_plan* p, bool i16, const float* vp, float* ip, cudaStre
 // storage formats of the tap spectra
 enum SpecFmt { FMT_F32 = 0, FMT_I16 = 1, FMT_F24 = 2 };
 int spectral_adjoint(sid_plan* p, int fmt, const float* ip, float* bp, cudaStream_t st);
+int conv_poly(sid_plan* p, const float* in_vp, float* out_vp, cudaStream_t st);
 int weak_build(sid_plan* p);
 int weak_fix(sid_plan* p, const float* ip, float* bp, cudaStream_t st);
 int v_to_vp(const sid_plan* p, const float* V, float* vp, int64_t Z, cudaStream_t st);

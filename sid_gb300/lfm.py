@@ -130,6 +130,17 @@ class Projector:
                 "weak_voxels", "weak_launches"]
         return dict(zip(keys, list(buf)))
 
+    def set_kernel(self, kernel):
+        """Compose every projection of this plan with convn(., kernel, 'same')
+        (reconstruct_S.m:126-127): forward P(convn(X, k)), back projection
+        convn(P'(y), k).  kernel: 3-D array (kx, ky, kz <= 64); None removes it."""
+        if kernel is None:
+            _lib.call("sid_plan_set_kernel", self._plan, None, 0, 0, 0)
+            return
+        k = np.asfortranarray(np.asarray(kernel, dtype=np.float32))
+        k = k.reshape(k.shape + (1,) * (3 - k.ndim), order="F")
+        _lib.call("sid_plan_set_kernel", self._plan, k.ctypes.data, *k.shape)
+
     def set_weak_fraction(self, frac: float):
         """Voxels with column mass A'1 below `frac` of the largest get exact back
         projections in the spectral forms (default 1e-2; 0 turns it off)."""
@@ -351,16 +362,67 @@ def LS_deconv(forwardFUN, backwardFUN, df, opts=None):
                           float(opts.get("lamb_L2", 0.0)))
 
 
+def _colon(a, b, step=1.0):
+    """MATLAB a:step:b."""
+    n = int(np.floor((b - a) / step + 1e-9)) + 1
+    return a + step * np.arange(max(n, 0))
+
+
+def _meshgrid3(x, y, z):
+    """MATLAB [X, Y, Z] = meshgrid(x, y, z): arrays of size (numel(y), numel(x), numel(z))."""
+    Yg, Xg, Zg = np.meshgrid(y, x, z, indexing="ij")
+    return Xg, Yg, Zg
+
+
+def _fspecial_gaussian(hsize, sigma):
+    """The rotationally symmetric Gaussian of fspecial('gaussian', hsize, sigma):
+    exp(-(x^2 + y^2) / 2 sigma^2) on an hsize x hsize grid centred at 0, values
+    below eps * max set to 0, normalised to sum 1."""
+    r = _colon(-(hsize - 1) / 2, (hsize - 1) / 2)
+    Xg, Yg = np.meshgrid(r, r)
+    h = np.exp(-(Xg ** 2 + Yg ** 2) / (2 * sigma ** 2))
+    h[h < np.finfo(np.float64).eps * h.max()] = 0
+    return h / h.sum()
+
+
+def generate_kernel(ker_shape, ker_param):
+    """kernel = generate_kernel(ker_shape, ker_param) (generate_kernel.m:1):
+    'ball' (radii ker_param(1) laterally, ker_param(2) axially), 'gaussian',
+    'lorentz' or 'user' (ker_param is the kernel), normalised to unit L2 norm.
+    Returns a Fortran-ordered float64 array."""
+    if ker_shape == "ball":
+        r1, r2 = float(ker_param[0]), float(ker_param[1])
+        Xg, Yg, Zg = _meshgrid3(_colon(-r1, r1), _colon(-r1, r1), _colon(-r2, r2))
+        k = ((Xg ** 2 / r1 ** 2 + Yg ** 2 / r1 ** 2 + Zg ** 2 / r2 ** 2) <= 1).astype(np.float64)
+    elif ker_shape == "gaussian":
+        p1, p2 = float(ker_param[0]), float(ker_param[1])
+        n = int(np.ceil(10 * p1)) + 1
+        g = _fspecial_gaussian(n, p1)
+        zt = np.exp(-_colon(-3 * p2, 3 * p2) ** 2 / 4 / p2 ** 2)
+        k = np.reshape(np.outer(g.reshape(-1, order="F"), zt), (n, n, len(zt)), order="F")
+    elif ker_shape == "lorentz":
+        p1, p2 = float(ker_param[0]), float(ker_param[1])
+        a, c = np.ceil(5 * p1), np.ceil(5 * p2)
+        Xg, Yg, Zg = _meshgrid3(_colon(-a, a), _colon(-a, a), _colon(-c, c))
+        k = 1.0 / (1 + (p1 * (Xg ** 2 + Yg ** 2) + p2 * Zg ** 2))
+    elif ker_shape == "user":
+        k = np.array(ker_param, dtype=np.float64)
+    else:
+        raise ValueError(f"generate_kernel: unknown shape {ker_shape!r}")
+    k = np.asfortranarray(k.reshape(k.shape + (1,) * (3 - k.ndim)))
+    return k / np.linalg.norm(k.ravel())
+
+
 def reconstruct_S(S, psf_ballistic, opts=None):
     """recon_nnmf = reconstruct_S(S, psf_ballistic, opts) (reconstruct_S.m:1),
     the GPU branch (:158-211): every component S(ii, :, :) reconstructed on
     one resident plan.  S: (n, X, Y); psf_ballistic: dict or object with H;
     opts: q, lamb_L1, lamb_L2, whichSolver, max_iter, microlenses.  Returns a
-    list of X x Y x Z CUDA tensors.  The neuron-kernel composition
-    (opts.ker_param) does not run natively."""
+    list of X x Y x Z CUDA tensors.  With opts.ker_param (and opts.ker_shape,
+    default 'user'), the projector is composed with convn(., kernel, 'same')
+    both ways (:110-114, :188-189)."""
     opts = dict(opts or {})
-    if "ker_param" in opts:
-        raise NotImplementedError("reconstruct_S: opts.ker_param (kernel composition) does not run natively")
+    kernel = generate_kernel(opts.get("ker_shape", "user"), opts["ker_param"]) if "ker_param" in opts else None
     tv = np.asarray(opts.get("lamb_TV_L2", 0.0))
     if np.any(tv != 0) or opts.get("lamb_TV_L1", 0):
         raise NotImplementedError("reconstruct_S: TV regularisers do not run natively")
@@ -370,8 +432,12 @@ def reconstruct_S(S, psf_ballistic, opts=None):
     method = opts.get("method", _DEFAULT_METHOD)
     P = _plan_for(H, (X, Y), None, method)
     out = []
-    for ii in range(n):
-        out.append(P.reconstruct_component(S[ii], opts.get("microlenses"), opts, method=method))
+    P.set_kernel(kernel)
+    try:
+        for ii in range(n):
+            out.append(P.reconstruct_component(S[ii], opts.get("microlenses"), opts, method=method))
+    finally:
+        P.set_kernel(None)
     return out
 
 
