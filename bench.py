@@ -444,6 +444,27 @@ def main():
         others[m] = {"rl_iter_s": 1e3 / tm, "ms_per_iter": tm,
                      "fwd_rel_err_vs_fp64": float(np.linalg.norm(gm - ref_pix) / np.linalg.norm(ref_pix))}
 
+    # neuron-kernel composition (reconstruct_S.m:126-127): ISRA iterations with
+    # convn(., k, 'same') before every forward and after every back projection
+    composed = {}
+    for kname, ker in (("ball_3_1", s.generate_kernel("ball", [3, 1])),
+                       ("gaussian_17x17x5", s.generate_kernel("gaussian", [1.6, 0.8]))):
+        P.set_kernel(ker)
+        xk = X0.clone()
+        iterate(xk, args.method, 2)
+        torch.cuda.synchronize()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        iterate(xk, args.method, 5)
+        b.record(stream)
+        torch.cuda.synchronize()
+        tk = a.elapsed_time(b) / 5
+        composed[kname] = {"kernel": list(ker.shape), "rl_iter_s": 1e3 / tk, "ms_per_iter": tk,
+                           "overhead_ms_per_iter": tk - ms_per_step}
+        P.set_kernel(None)
+        del xk
+
     nnls = None
     if not args.no_nnls:
         nnls = nnls_workload(args, P)
@@ -484,6 +505,7 @@ def main():
             "clocks": clk.summary(),
             "accuracy": {"fwd_rel_l2_vs_fp64_256px": fwd_err},
             "compare": others,
+            "kernel_composition": composed,
             "mixed_vs_fp32_direct": (value / world) / others["direct"]["rl_iter_s"] if "direct" in others else None,
             "plan": {"L": info["L"], "D": info["D"], "device_gb": info["device_bytes"] / 1e9},
             "nnls": nnls,
