@@ -207,6 +207,26 @@ int sid_rank1_background(sid_ctx* ctx, const void* Y, int ydtype, int64_t P, int
 int sid_std_image(sid_ctx* ctx, const void* Y, int ydtype, int64_t P, int64_t F, const float* y1,
                   const float* y2, float* std_image, void* stream);
 
+/* ---- Post-processing of the demixing (merge_filters.m, SNR_order.m) --------
+ * merge_filters(forward_model, timeseries, template, indices_in_orig, opts)
+ *                                                   merge_filters.m:1
+ * Merges components whose templates overlap by more than a third of the
+ * smaller one and whose traces correlate above `limit` (opts.limit, default
+ * 0.9), with MATLAB's single arithmetic and its two bg_sub crops
+ * (merge_filters.m:19-29).  ts: K x F single traces (device, the background
+ * row last when bg_sub); templ: (K - bg_sub) x P single 0/1 templates
+ * (device, merged in place: absorbing rows OR-ed, absorbed rows zeroed,
+ * :33-36); keep: HOST int32[K] output, 1 for the rows of forward_model /
+ * timeseries / indices_in_orig (and template, first K - bg_sub) that survive
+ * (:38-50).  The overlap Gram runs exactly on the tensor cores. */
+int sid_merge_filters(sid_ctx* ctx, const float* ts, int64_t K, int64_t F, float* templ, int64_t P, double limit,
+                      int bg_sub, int32_t* keep, void* stream);
+/* n = SNR_order(traces, opts)   SNR_order.m:1.  traces: K x F single (device);
+ * order: HOST int32[K] output, 0-based row order by decreasing peak-to-noise
+ * ratio, the background row (K-1) last when bg_sub. */
+int sid_snr_order(sid_ctx* ctx, const float* traces, int64_t K, int64_t F, int bg_sub, int32_t* order,
+                  void* stream);
+
 /* ---- NNLS solvers -----------------------------------------------------------
  * Options mirror the reference's opts fields and defaults. */
 typedef struct {

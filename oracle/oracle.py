@@ -563,6 +563,68 @@ def convn_same(V, k):
     return np.asfortranarray(full[sl])
 
 
+def merge_filters(forward_model, timeseries, template, indices_in_orig, limit=0.9, bg_sub=True):
+    """merge_filters.m:19-50 with MATLAB's types: corrcoef and the overlap
+    normalisation in single, the comparisons with 1/3 and 1 + limit in double,
+    the two bg_sub crops, and the sequential merge loop."""
+    b = 1 if bg_sub else 0
+    ts = np.asarray(timeseries, dtype=np.float64)
+    K = ts.shape[0]
+    corr = (np.corrcoef(ts).astype(np.float32) - np.eye(K, dtype=np.float32))[:K - b, :K - b]
+    tp = np.array(template, dtype=np.float32)
+    ssum = tp.sum(axis=1, dtype=np.float64).astype(np.float32)
+    gram = (tp.astype(np.float64) @ tp.T.astype(np.float64)).astype(np.float32)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        ov = (np.float32(1) / np.minimum(ssum[:, None], ssum[None, :])) * gram - np.eye(K - b, dtype=np.float32)
+        v = (ov.astype(np.float64) > 1.0 / 3.0).astype(np.float32) + corr
+    v = v[:K - 2 * b, :K - 2 * b]
+    mat = np.tril(v.astype(np.float64) > 1.0 + limit)
+    for ii in np.flatnonzero(mat.sum(axis=0)):
+        src = np.flatnonzero(mat[:, ii])
+        tp[ii, :] = ((tp[ii, :] + tp[src, :].sum(axis=0)) > 0).astype(np.float32)
+        tp[src, :] = 0
+    nz = np.flatnonzero(tp.sum(axis=1) > 0)
+    rows = np.concatenate([nz, [K - 1]]) if b else nz
+    return (np.asarray(forward_model)[rows], ts[rows], tp[nz], np.asarray(indices_in_orig)[rows])
+
+
+def matlab_smooth(y, span=5):
+    """MATLAB smooth(y, span) (moving average): an even span is reduced by one;
+    the window shrinks symmetrically at the ends."""
+    y = np.asarray(y, dtype=np.float64)
+    if span % 2 == 0:
+        span -= 1
+    n = len(y)
+    out = np.empty(n)
+    for i in range(n):
+        h = min(i, n - 1 - i, span // 2)
+        out[i] = y[i - h:i + h + 1].mean()
+    return out
+
+
+def snr_order(traces, bg_sub=True):
+    """SNR_order.m:13-28 (0-based order): FFT of [trace flip(trace)], bins 1..6
+    and their mirrors zeroed, inverse (real part), first half, zscore; ratio of
+    the range of smooth(., 5) to std(smooth(., 8) - .); sorted by decreasing
+    ratio (stable), the background row last."""
+    tr = np.asarray(traces, dtype=np.float64)
+    K = tr.shape[0]
+    b = 1 if bg_sub else 0
+    pp = np.empty(K - b)
+    for k in range(K - b):
+        x = tr[k]
+        hh = np.fft.fft(np.concatenate([x, x[::-1]]))
+        hh[1:7] = 0
+        hh[-6:] = 0
+        t = np.real(np.fft.ifft(hh))[:len(x)]
+        t = (t - t.mean()) / t.std(ddof=1)
+        sn = np.std(matlab_smooth(t, 8) - t, ddof=1)
+        sm = matlab_smooth(t)
+        pp[k] = (sm.max() - sm.min()) / sn
+    order = np.argsort(-pp, kind="stable")
+    return (np.concatenate([order, [K - 1]]) if b else order), pp
+
+
 def rank_1_factorization(Y, maxIter=1):
     """[bg_spatial, bg_temporal] = rank_1_factorization(Y, maxIter)
     (rank_1_factorization.m:30-39): alternate t = s'Y / ||.||, s = Y t', s

@@ -8,6 +8,7 @@ from ._lib import SidError  # noqa: F401
 from .nnls import Context, LS_nnls, fast_nnls, quantile, update_spatial_component  # noqa: F401
 from .nmf import S_update, T_update  # noqa: F401
 from .background import compute_std_image, rank_1_factorization  # noqa: F401
+from .postproc import SNR_order, merge_filters  # noqa: F401
 from .extract import Extractor, incremental_temporal_update_gpu  # noqa: F401
 from .lfm import (  # noqa: F401
     LS_deconv,
