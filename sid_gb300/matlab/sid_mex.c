@@ -18,6 +18,10 @@
  *   [S, T]   = sid_mex('t_update', Y, T, S, opts)        opts.active, opts.Y optional
  *   [S, T]   = sid_mex('s_update', Y, S, T, opts)        opts.Y, opts.hilf optional
  *   q        = sid_mex('quantile', x, p)
+ *   [s, t, sd] = sid_mex('rank1_background', Y, maxIter)    rank_1_factorization + compute_std_image
+ *   sid_mex('set_kernel', plan, kernel)                      neuron-kernel composition ([] removes)
+ *   [keep, template] = sid_mex('merge_filters', timeseries, template, limit, bg_sub)
+ *   n        = sid_mex('snr_order', traces, bg_sub)
  *   h        = sid_mex('pinv_create', F)                  F: K x P forward model
  *   T        = sid_mex('pinv_apply', h, Y, baseline)      baseline may be []
  *   sid_mex('pinv_destroy', h)
@@ -361,6 +365,80 @@ void mexFunction(int nlhs, mxArray* plhs[], int nrhs, const mxArray* prhs[])
         if (nlhs > 1) plhs[1] = mxGPUCreateMxArrayOnGPU(T);
         mxGPUDestroyGPUArray(S);
         mxGPUDestroyGPUArray(T);
+        return;
+    }
+    if (!strcmp(cmd, "rank1_background")) {
+        /* [bg_spatial, bg_temporal, std_image] = sid_mex('rank1_background', Y, maxIter):
+         * Y P x F single or half gpuArray; std_image computed in the last pass */
+        const mxGPUArray* Y = gpu_arg(prhs[1], 1, cmd);
+        const mwSize* dy = mxGPUGetDimensions(Y);
+        const int64_t P = (int64_t)dy[0], F = (int64_t)dy[1];
+        mwSize ds[2] = {(mwSize)P, 1}, dt[2] = {1, (mwSize)F};
+        mxGPUArray* s_ = mxGPUCreateGPUArray(2, ds, mxSINGLE_CLASS, mxREAL, MX_GPU_DO_NOT_INITIALIZE);
+        mxGPUArray* t_ = mxGPUCreateGPUArray(2, dt, mxSINGLE_CLASS, mxREAL, MX_GPU_DO_NOT_INITIALIZE);
+        mxGPUArray* sd = nlhs > 2 ? mxGPUCreateGPUArray(2, ds, mxSINGLE_CLASS, mxREAL, MX_GPU_DO_NOT_INITIALIZE) : NULL;
+        int rc = sid_rank1_background(ctx(cmd), mxGPUGetDataReadOnly(Y), ydtype(Y), P, F, (int)mxGetScalar(prhs[2]),
+                                      (float*)mxGPUGetData(s_), (float*)mxGPUGetData(t_),
+                                      sd ? (float*)mxGPUGetData(sd) : NULL, NULL);
+        if (rc == SID_OK) rc = sid_ctx_sync(g_ctx, NULL);
+        mxGPUDestroyGPUArray(Y);
+        check(rc, cmd);
+        plhs[0] = mxGPUCreateMxArrayOnGPU(s_);
+        if (nlhs > 1) plhs[1] = mxGPUCreateMxArrayOnGPU(t_);
+        if (sd) plhs[2] = mxGPUCreateMxArrayOnGPU(sd);
+        mxGPUDestroyGPUArray(s_);
+        mxGPUDestroyGPUArray(t_);
+        if (sd) mxGPUDestroyGPUArray(sd);
+        return;
+    }
+    if (!strcmp(cmd, "set_kernel")) {
+        /* sid_mex('set_kernel', plan, kernel): kernel single (host) 3-D, [] removes it */
+        sid_plan* p = plan_arg(prhs[1]);
+        const mxArray* k = prhs[2];
+        if (mxIsEmpty(k)) {
+            check(sid_plan_set_kernel(p, NULL, 0, 0, 0), cmd);
+            return;
+        }
+        if (!mxIsSingle(k)) mexErrMsgIdAndTxt("sid:type", "set_kernel: single kernel expected");
+        const mwSize nd = mxGetNumberOfDimensions(k);
+        const mwSize* d = mxGetDimensions(k);
+        check(sid_plan_set_kernel(p, (const float*)mxGetData(k), (int64_t)d[0], nd > 1 ? (int64_t)d[1] : 1,
+                                  nd > 2 ? (int64_t)d[2] : 1), cmd);
+        return;
+    }
+    if (!strcmp(cmd, "merge_filters")) {
+        /* keep = sid_mex('merge_filters', timeseries, template, limit, bg_sub): K x F and
+         * (K - bg_sub) x P single gpuArrays; template merged in place (returned as the
+         * second output); keep: logical K x 1 of the surviving rows */
+        const mxGPUArray* ts = gpu_arg(prhs[1], 0, cmd);
+        const mxGPUArray* t0 = gpu_arg(prhs[2], 0, cmd);
+        mxGPUArray* tp = gpu_copy(t0);
+        mxGPUDestroyGPUArray(t0);
+        const mwSize* dt = mxGPUGetDimensions(ts);
+        const mwSize* dp = mxGPUGetDimensions(tp);
+        const int64_t K = (int64_t)dt[0], F = (int64_t)dt[1], P = (int64_t)dp[1];
+        plhs[0] = mxCreateNumericMatrix((mwSize)K, 1, mxINT32_CLASS, mxREAL);
+        const int rc = sid_merge_filters(ctx(cmd), (const float*)mxGPUGetDataReadOnly(ts), K, F, (float*)mxGPUGetData(tp),
+                                         P, mxGetScalar(prhs[3]), (int)mxGetScalar(prhs[4]), (int32_t*)mxGetData(plhs[0]),
+                                         NULL);
+        mxGPUDestroyGPUArray(ts);
+        if (rc != SID_OK) mxGPUDestroyGPUArray(tp);
+        check(rc, cmd);
+        if (nlhs > 1) plhs[1] = mxGPUCreateMxArrayOnGPU(tp);
+        mxGPUDestroyGPUArray(tp);
+        return;
+    }
+    if (!strcmp(cmd, "snr_order")) {
+        /* n = sid_mex('snr_order', traces, bg_sub): traces K x F single gpuArray; n 1-based */
+        const mxGPUArray* tr = gpu_arg(prhs[1], 0, cmd);
+        const mwSize* d = mxGPUGetDimensions(tr);
+        plhs[0] = mxCreateNumericMatrix(1, d[0], mxINT32_CLASS, mxREAL);
+        int32_t* o = (int32_t*)mxGetData(plhs[0]);
+        const int rc = sid_snr_order(ctx(cmd), (const float*)mxGPUGetDataReadOnly(tr), (int64_t)d[0], (int64_t)d[1],
+                                     (int)mxGetScalar(prhs[2]), o, NULL);
+        mxGPUDestroyGPUArray(tr);
+        check(rc, cmd);
+        for (mwSize i = 0; i < d[0]; ++i) o[i] += 1;
         return;
     }
     if (!strcmp(cmd, "quantile")) {
