@@ -182,6 +182,7 @@ int sid_ctx_sync(sid_ctx* ctx, void* stream);
 /* Element types of movie arrays. */
 #define SID_DTYPE_F32 0
 #define SID_DTYPE_F16 1
+#define SID_DTYPE_U16 2 /* camera frames (sid_image_rect) */
 
 /* G = A'*A (K x K, column-major)   LS_nnls.m:82, fast_nnls.m:54, T_update.m:24
  * A: P x K single (device, column-major). */
@@ -226,6 +227,22 @@ int sid_merge_filters(sid_ctx* ctx, const float* ts, int64_t K, int64_t F, float
  * ratio, the background row (K-1) last when bg_sub. */
 int sid_snr_order(sid_ctx* ctx, const float* traces, int64_t K, int64_t F, int bg_sub, int32_t* order,
                   void* stream);
+
+/* ---- Sensor frames: lenslet rectification (ImageRect.m) --------------------
+ * IMG_RESAMPLE = ImageRect(IMG_BW, xCenter, yCenter, dx, M, Crop, XcutLeft,
+ *                          XcutRight, YcutUp, YcutDown)          ImageRect.m:1
+ * frames: rows x cols x nframes (device, column-major), SID_DTYPE_U16 or
+ * SID_DTYPE_F32; mask: rows x cols single (device) or NULL, multiplied in
+ * first as read_sensor_movie.m:94-99 does; cuts: HOST int32[4] = XcutLeft,
+ * XcutRight, YcutUp, YcutDown (used when crop).  out: out_rows x out_cols x
+ * nframes single (device) -- the P x F movie of read_sensor_movie.m --
+ * bilinear as interp2, NaN outside the image.  sid_image_rect_size gives
+ * out_rows / out_cols (host only). */
+int sid_image_rect_size(int64_t rows, int64_t cols, double xCenter, double yCenter, double dx, int64_t M, int crop,
+                        const int32_t* cuts, int64_t* out_rows, int64_t* out_cols);
+int sid_image_rect(sid_ctx* ctx, const void* frames, int dtype, int64_t rows, int64_t cols, int64_t nframes,
+                   const float* mask, double xCenter, double yCenter, double dx, int64_t M, int crop,
+                   const int32_t* cuts, float* out, void* stream);
 
 /* ---- NNLS solvers -----------------------------------------------------------
  * Options mirror the reference's opts fields and defaults. */

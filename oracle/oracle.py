@@ -625,6 +625,57 @@ def snr_order(traces, bg_sub=True):
     return (np.concatenate([order, [K - 1]]) if b else order), pp
 
 
+def _colon(a, step, b):
+    """MATLAB a:step:b."""
+    if step == 0 or (step > 0 and a > b) or (step < 0 and a < b):
+        return np.zeros(0)
+    n = int(np.floor((b - a) / step + 1e-10)) + 1
+    return a + step * np.arange(n)
+
+
+def image_rect(img, xCenter, yCenter, dx, M, crop=True, cuts=(0, 0, 0, 0)):
+    """ImageRect.m:7-45 in FP64: the resample grid (MATLAB colon steps dx/M
+    around the centre, started on a lenslet boundary, trimmed to whole
+    lenslets, cropped by cuts = XcutLeft, XcutRight, YcutUp, YcutDown) and
+    interp2's bilinear rule, NaN outside the image."""
+    img = np.asarray(img, dtype=np.float64)
+    rows, cols = img.shape
+    s = dx / M
+
+    def axis(c, size):
+        lo = _colon(c + 1, -s, 1.0)
+        hi = _colon(c + 1 + s, s, float(size))
+        allv = np.concatenate([lo[::-1], hi])
+        centre = len(lo) - M // 2
+        init = centre - M * int(np.floor(centre / M)) + M
+        return allv[init - 1:], init
+
+    xq, xi = axis(xCenter, cols)
+    yq, yi = axis(yCenter, rows)
+    nr = M * int(np.floor((len(yq) - yi) / M))
+    nc = M * int(np.floor((len(xq) - xi) / M))
+    xq, yq = xq[:nc], yq[:nr]
+    if crop:
+        xs, ys = nc // M, nr // M
+        xq = xq[cuts[0] * M:(xs - cuts[1]) * M]
+        yq = yq[cuts[2] * M:(ys - cuts[3]) * M]
+    out = np.full((len(yq), len(xq)), np.nan)
+    for r, y in enumerate(yq):
+        if not (1 <= y <= rows):
+            continue
+        iy = min(int(np.floor(y)), rows - 1)
+        fy = y - iy
+        for c, x in enumerate(xq):
+            if not (1 <= x <= cols):
+                continue
+            ix = min(int(np.floor(x)), cols - 1)
+            fx = x - ix
+            v00, v10 = img[iy - 1, ix - 1], img[iy - 1, ix]
+            v01, v11 = img[iy, ix - 1], img[iy, ix]
+            out[r, c] = (1 - fy) * ((1 - fx) * v00 + fx * v10) + fy * ((1 - fx) * v01 + fx * v11)
+    return out
+
+
 def rank_1_factorization(Y, maxIter=1):
     """[bg_spatial, bg_temporal] = rank_1_factorization(Y, maxIter)
     (rank_1_factorization.m:30-39): alternate t = s'Y / ||.||, s = Y t', s

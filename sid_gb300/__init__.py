@@ -8,7 +8,8 @@ from ._lib import SidError  # noqa: F401
 from .nnls import Context, LS_nnls, fast_nnls, quantile, update_spatial_component  # noqa: F401
 from .nmf import S_update, T_update  # noqa: F401
 from .background import compute_std_image, rank_1_factorization  # noqa: F401
-from .postproc import SNR_order, merge_filters  # noqa: F401
+from .postproc import ImageRect, SNR_order, merge_filters, read_sensor_movie, rectify_frames  # noqa: F401
+from .tiff import read_tiff  # noqa: F401
 from .extract import Extractor, incremental_temporal_update_gpu  # noqa: F401
 from .lfm import (  # noqa: F401
     LS_deconv,

@@ -68,6 +68,9 @@ SIGNATURES = {
     "sid_std_image": [P, P, I32, I64, I64, P, P, P, P],
     "sid_merge_filters": [P, P, I64, I64, P, I64, ctypes.c_double, I32, P, P],
     "sid_snr_order": [P, P, I64, I64, I32, P, P],
+    "sid_image_rect_size": [I64, I64, ctypes.c_double, ctypes.c_double, ctypes.c_double, I64, I32, P, P, P],
+    "sid_image_rect": [P, P, I32, I64, I64, I64, P, ctypes.c_double, ctypes.c_double, ctypes.c_double, I64, I32, P,
+                       P, P],
     "sid_cross": [P, P, P, I32, I64, I64, I64, P, I32, P],
     "sid_ls_nnls_defaults": [P],
     "sid_fast_nnls_defaults": [P],
