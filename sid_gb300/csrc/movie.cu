@@ -42,33 +42,90 @@ __device__ __forceinline__ double block_sum(double v, double* red)
     return v;  // valid in thread 0
 }
 
-// t_j = scale_s * sum_i s_i Y(i, j); s == nullptr means s_i = 1.
+// 8 consecutive movie values from a 16-byte aligned address
+__device__ __forceinline__ void ld8(const __half* p, float (&v)[8])
+{
+    const uint4 w = __ldcs(reinterpret_cast<const uint4*>(p));
+    const __half2* h = reinterpret_cast<const __half2*>(&w);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const float2 f = __half22float2(h[q]);
+        v[2 * q] = f.x;
+        v[2 * q + 1] = f.y;
+    }
+}
+__device__ __forceinline__ void ld8(const float* p, float (&v)[8])
+{
+    const float4 a = __ldcs(reinterpret_cast<const float4*>(p)), b = __ldcs(reinterpret_cast<const float4*>(p) + 1);
+    v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+    v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+}
+
+// Four copies of s shifted by a = 0..3 elements: s4[a * ps + a + i] = s[i], so
+// that s4 + a * ps + a + head is 16-byte aligned whenever head + a = 0 (mod 4).
+__global__ void k_shift4(const float* __restrict__ s, int64_t P, int64_t ps, float* __restrict__ s4)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < P; i += (int64_t)gridDim.x * blockDim.x) {
+        const float v = s[i];
+#pragma unroll
+        for (int a = 0; a < 4; ++a) s4[a * ps + a + i] = v;
+    }
+}
+
+// t_j = scale_s * sum_i s_i Y(i, j); s == nullptr means s_i = 1 (s4: the
+// shifted copies of s).  Each frame column is read with 16-byte loads from its
+// first 16-byte aligned element (a scalar head and tail around it), four
+// vectors in flight per thread; the weights of the vectors come from the copy
+// of s in which they are 16-byte aligned.
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
-k_col_pass(const T* __restrict__ Y, int64_t P, int64_t F, const float* __restrict__ s, float scale_s,
-           double* __restrict__ t)
+k_col_pass(const T* __restrict__ Y, int64_t P, int64_t F, const float* __restrict__ s, const float* __restrict__ s4,
+           int64_t ps, float scale_s, double* __restrict__ t)
 {
-    constexpr int U = 8;  // independent loads in flight per thread
+    constexpr int U = 4;
     __shared__ double red[kThreads / 32];
     for (int64_t j = blockIdx.x; j < F; j += gridDim.x) {
         const T* col = Y + j * P;
+        const int64_t head = std::min<int64_t>(P, (int64_t)(((16 - ((uintptr_t)col & 15)) & 15) / sizeof(T)));
+        const int64_t nv = (P - head) / 8;
         double acc = 0.0;
-        int64_t i = threadIdx.x;
-        for (; i + (U - 1) * kThreads < P; i += U * kThreads) {
-            float y[U], w[U];
+        float part = 0.f;
+        for (int64_t i = threadIdx.x; i < head; i += kThreads) part = fmaf(s ? s[i] : 1.f, ld(col + i), part);
+        for (int64_t i = head + nv * 8 + threadIdx.x; i < P; i += kThreads) part = fmaf(s ? s[i] : 1.f, ld(col + i), part);
+        acc += part;
+        const T* body = col + head;
+        const int a = (int)((4 - head % 4) % 4);
+        const float* sb = s ? s4 + a * ps + a + head : nullptr;
+        for (int64_t v0 = threadIdx.x; v0 < nv; v0 += (int64_t)U * kThreads) {
+            float y[U][8];
 #pragma unroll
             for (int u = 0; u < U; ++u) {
-                y[u] = ld(col + i + u * kThreads);
-                w[u] = s ? s[i + u * kThreads] : 1.f;
-            }
-            float part = 0.f;
+                const int64_t v = v0 + (int64_t)u * kThreads;
+                if (v < nv) ld8(body + v * 8, y[u]);
+                else {
 #pragma unroll
-            for (int u = 0; u < U; ++u) part = fmaf(w[u], y[u], part);
-            acc += part;
+                    for (int q = 0; q < 8; ++q) y[u][q] = 0.f;
+                }
+            }
+            float p2 = 0.f;
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int64_t v = v0 + (int64_t)u * kThreads;
+                if (v >= nv) continue;
+                if (!sb) {
+#pragma unroll
+                    for (int q = 0; q < 8; ++q) p2 += y[u][q];
+                } else {
+                    const float4 a = reinterpret_cast<const float4*>(sb + v * 8)[0];
+                    const float4 b = reinterpret_cast<const float4*>(sb + v * 8)[1];
+                    p2 = fmaf(a.x, y[u][0], p2); p2 = fmaf(a.y, y[u][1], p2);
+                    p2 = fmaf(a.z, y[u][2], p2); p2 = fmaf(a.w, y[u][3], p2);
+                    p2 = fmaf(b.x, y[u][4], p2); p2 = fmaf(b.y, y[u][5], p2);
+                    p2 = fmaf(b.z, y[u][6], p2); p2 = fmaf(b.w, y[u][7], p2);
+                }
+            }
+            acc += p2;
         }
-        float part = 0.f;
-        for (; i < P; i += kThreads) part = fmaf(s ? s[i] : 1.f, ld(col + i), part);
-        acc += part;
         acc = block_sum(acc, red);
         if (threadIdx.x == 0) t[j] = acc * (double)scale_s;
     }
@@ -206,6 +263,9 @@ int background(sid_ctx* c, const T* Y, int64_t P, int64_t F, int maxIter, float*
     SID_TRY(c->bg[0].alloc((size_t)P * sizeof(double)));                  // s (FP64)
     SID_TRY(c->bg[1].alloc((size_t)(F + 4096) * sizeof(double)));         // t, scalars, partials
     SID_TRY(c->bg[4].alloc(sizeof(unsigned int)));
+    const int64_t ps = cdiv(P + 4, 4) * 4;  // pitch of the shifted weight copies
+    if (maxIter > 1) SID_TRY(c->bg[5].alloc((size_t)(4 * ps) * sizeof(float)));
+    float* s4 = maxIter > 1 ? c->bg[5].as<float>() : nullptr;
     double* sd = c->bg[0].as<double>();
     double* td = c->bg[1].as<double>();
     double* ss = td + F;       // sum of squares of t or s
@@ -223,10 +283,13 @@ int background(sid_ctx* c, const T* Y, int64_t P, int64_t F, int maxIter, float*
     for (int it = 1; it <= maxIter; ++it) {
         // bg_temporal = bg_spatial' * Y, normalised (rank_1_factorization.m:33-34); the
         // first bg_spatial is ones / sqrt(P) (:30)
-        if (it == 1)
-            k_col_pass<T><<<gcol, kThreads, 0, st>>>(Y, P, F, nullptr, (float)(1.0 / sqrt((double)P)), td);
-        else
-            k_col_pass<T><<<gcol, kThreads, 0, st>>>(Y, P, F, bg_s, 1.f, td);
+        if (it == 1) {
+            k_col_pass<T><<<gcol, kThreads, 0, st>>>(Y, P, F, nullptr, nullptr, 0, (float)(1.0 / sqrt((double)P)), td);
+        } else {
+            k_shift4<<<grid_for(P), kThreads, 0, st>>>(bg_s, P, ps, s4);
+            SID_CHECK_LAUNCH();
+            k_col_pass<T><<<gcol, kThreads, 0, st>>>(Y, P, F, bg_s, s4, ps, 1.f, td);
+        }
         SID_CHECK_LAUNCH();
         k_sumsq<<<1, kThreads, 0, st>>>(td, F, ss);
         SID_CHECK_LAUNCH();

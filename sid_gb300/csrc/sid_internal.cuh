@@ -185,5 +185,5 @@ struct sid_ctx {
     sid::DBuf a_hi, a_lo, b_hi, b_lo, ws, scal, errflag;
     sid::DBuf nn[16];  // NNLS iteration state
     sid::DBuf mf[8];   // NMF step workspaces (T_update / S_update)
-    sid::DBuf bg[5];   // movie scans (rank-1 background, standard-deviation image)
+    sid::DBuf bg[6];   // movie scans (rank-1 background, standard-deviation image)
 };
