@@ -59,7 +59,10 @@ def small(gpu, oracle):
     return H, Vt, P
 
 
-KERNELS = {"ball": ("ball", [2, 1]), "even_user": ("user", np.arange(1, 25, dtype=float).reshape(4, 3, 2))}
+KERNELS = {"ball": ("ball", [2, 1]), "even_user": ("user", np.arange(1, 25, dtype=float).reshape(4, 3, 2)),
+           "gaussian": ("gaussian", [1.6, 0.8]),
+           # wider than 32 along x: the generic kernel
+           "wide_user": ("user", np.random.default_rng(5).uniform(0, 1, (33, 3, 2)))}
 
 
 @pytest.mark.gpu
