@@ -7,14 +7,16 @@
 // contribute nothing, so the row equals the full-depth forward projection of
 // the boxed volume.  Here every neuron is one batch entry of one launch:
 //   1. k_lib_average: the boxed, averaged sub-volumes (packed, one per neuron);
-//   2. k_lib_project: one CTA per (neuron, output phase a'b'); threads own the
-//      output lenslets around the box; per box channel (a,b,c) the D x D tap
-//      array K[abc][b'a'] is staged in shared memory and applied to the box's
-//      lattice points of that phase (the same lenslet-tap algebra as
-//      direct.cu), so only the box's own channels are visited;
+//   2. k_lib_project: one CTA per (group of neurons sharing a depth window,
+//      output phase a'b'); threads own the output lenslets around each box; per
+//      box channel (a,b,c) the D x D tap array K[abc][b'a'] is staged in shared
+//      memory once for the whole group and applied to every box's lattice
+//      points of that phase (the same lenslet-tap algebra as direct.cu), so
+//      only the boxes' own channels are visited;
 //   3. the rest of each row is zero (one memset of the output).
 // Box and window arithmetic (MATLAB round, clipping at 1 and the volume size,
 // ceil(neur_rad/axial)) is done on the host, bit-exact with the reference.
+#include <algorithm>
 #include <cmath>
 #include <vector>
 
@@ -48,89 +50,107 @@ __global__ void k_lib_average(const float* const* __restrict__ recon, const uint
     }
 }
 
-// One CTA per (neuron, output phase a'b'); output written to
-// out[n * ldn + pixel * ldp] with pixel = x + X*y.  Each thread owns four
-// consecutive output lenslets (s, t..t+3) of the neuron's window.  Per depth c
-// and input row phase b the D x D tap arrays of all N input column phases a
-// are staged in shared memory inside a zero border of R taps (R = the box's
-// lattice span), so for every box lattice point (u, v) a thread's four taps
-// sit at one offset from its base: one address, four shared loads and four
-// FMAs per point, no range checks, two barriers per (c, b).  The lattice
-// ranges of every phase are computed once per CTA.
+// One CTA per (group of up to G neurons with the same depth window, output
+// phase a'b'); output written to out[n * ldn + pixel * ldp] with pixel = x + X*y.
+// Per depth c and input row phase b the D x D tap arrays of all N input column
+// phases a are staged in shared memory once, inside a zero border of R taps
+// (R = the boxes' lattice span), and applied to every neuron of the group: the
+// tap arrays are the whole of the kernel's memory traffic, so grouping divides
+// it by the group size.  Each thread owns four consecutive output lenslets
+// (s, t..t+3) at the same place in every neuron's output window, so for every
+// box lattice point (u, v) a neuron's four taps sit at one offset from the
+// thread's base: one address, four shared loads and four FMAs per point, no
+// range checks.  The lattice ranges of every neuron and phase are computed once
+// per CTA.
 constexpr int kLibT = 4;  // consecutive output lenslets per thread
+constexpr int kLibG = 8;  // neurons per CTA
 
+template <int G>
 __global__ void __launch_bounds__(256)
 k_lib_project(const float* __restrict__ taps, const float* __restrict__ packed, const LibBox* __restrict__ boxes,
-              int N, int D, int dlo, int R, int64_t tbs, int Lx, int Ly, int64_t X, int64_t Y,
-              float* __restrict__ out, int64_t ldn, int64_t ldp)
+              const int* __restrict__ groups, int N, int D, int dlo, int R, int ntgM, int64_t tbs, int Lx, int Ly,
+              int64_t X, int64_t Y, float* __restrict__ out, int64_t ldn, int64_t ldp)
 {
-    extern __shared__ float tile[];  // [N][Dp][Dp + 4], then DD ints (padded tap offsets), then 4N ints (ranges)
+    extern __shared__ float tile[];  // [N][Dp][Dp + 4], then DD ints (padded tap offsets), then G * 4N ints (ranges)
     const int Dp = D + 2 * R, Dq = Dp + kLibT, tsz = Dp * Dq, DD = D * D;
     int* padoff = reinterpret_cast<int*>(tile + N * tsz);
-    int* rng = padoff + DD;  // ulo[a], uhi[a], vlo[b], vhi[b]
-    const int n = blockIdx.x;
+    int* rng = padoff + DD;  // per neuron k: ulo[a], uhi[a], vlo[b], vhi[b] at rng + 4N k
+    const int* grp = groups + blockIdx.x * (G + 1);
+    const int cnt = grp[0];
     const int o = blockIdx.y;  // b'*N + a'
     const int bp = o / N, ap = o - (o / N) * N;
-    const LibBox b = boxes[n];
-    const int bw = b.x1 - b.x0, bh = b.y1 - b.y0;
-    const int ns = b.s1 - b.s0, nt = b.t1 - b.t0;
-    const int ntg = (nt + kLibT - 1) / kLibT;  // groups of kLibT along t
     for (int i = threadIdx.x; i < N * tsz; i += blockDim.x) tile[i] = 0.f;
     for (int r = threadIdx.x; r < DD; r += blockDim.x) padoff[r] = (r / D + R) * Dq + (r - (r / D) * D) + R;
-    for (int ph = threadIdx.x; ph < N; ph += blockDim.x) {
-        // lattice columns u of phase ph in the box: x = ph + N u in [x0, x1); rows likewise
-        rng[ph] = (b.x0 - ph) > 0 ? (b.x0 - ph + N - 1) / N : 0;
-        rng[N + ph] = (b.x1 - 1 - ph) >= 0 ? (b.x1 - 1 - ph) / N : -1;
-        rng[2 * N + ph] = (b.y0 - ph) > 0 ? (b.y0 - ph + N - 1) / N : 0;
-        rng[3 * N + ph] = (b.y1 - 1 - ph) >= 0 ? (b.y1 - 1 - ph) / N : -1;
+    for (int e = threadIdx.x; e < cnt * N; e += blockDim.x) {
+        // lattice columns u of phase ph in box k: x = ph + N u in [x0, x1); rows likewise
+        const int k = e / N, ph = e - k * N;
+        const LibBox b = boxes[grp[1 + k]];
+        int* rk = rng + 4 * N * k;
+        rk[ph] = (b.x0 - ph) > 0 ? (b.x0 - ph + N - 1) / N : 0;
+        rk[N + ph] = (b.x1 - 1 - ph) >= 0 ? (b.x1 - 1 - ph) / N : -1;
+        rk[2 * N + ph] = (b.y0 - ph) > 0 ? (b.y0 - ph + N - 1) / N : 0;
+        rk[3 * N + ph] = (b.y1 - 1 - ph) >= 0 ? (b.y1 - 1 - ph) / N : -1;
     }
     const int g = threadIdx.x;
-    const bool ok = g < ns * ntg;
-    const int ls = ok ? g / ntg : 0, lt = ok ? (g - (g / ntg) * ntg) * kLibT : 0;
+    const int ls = g / ntgM, lt = (g - (g / ntgM) * ntgM) * kLibT;
     const int base = (ls + R) * Dq + (lt + R);
-    float acc[kLibT];
+    float acc[G][kLibT];
 #pragma unroll
-    for (int q = 0; q < kLibT; ++q) acc[q] = 0.f;
+    for (int k = 0; k < G; ++k)
+#pragma unroll
+        for (int q = 0; q < kLibT; ++q) acc[k][q] = 0.f;
+    const LibBox b0 = boxes[grp[1]];  // every neuron of the group has this depth window
     __syncthreads();
-    for (int c = b.z0; c < b.z1; ++c) {
+    for (int c = b0.z0; c < b0.z1; ++c) {
         for (int bb = 0; bb < N; ++bb) {
-            const int vlo = rng[2 * N + bb], vhi = rng[3 * N + bb];
-            if (vhi < vlo) continue;
             __syncthreads();  // the previous row's taps are no longer read
             const int64_t rowblk = ((int64_t)c * N + bb) * N;
             for (int a = 0; a < N; ++a) {
-                if (rng[N + a] < rng[a]) continue;
                 const float* src = taps + ((rowblk + a) * N + bp) * tbs + (int64_t)ap * DD;
                 float* dst = tile + a * tsz;
                 for (int r = threadIdx.x; r < DD; r += blockDim.x) dst[padoff[r]] = src[r];
             }
             __syncthreads();
-            if (!ok) continue;
-            for (int a = 0; a < N; ++a) {
-                const int ulo = rng[a], uhi = rng[N + a];
-                if (uhi < ulo) continue;
-                const float* ta = tile + a * tsz + base;
-                for (int v = vlo; v <= vhi; ++v) {
-                    const int e2 = b.t0 - v - dlo;
-                    const float* prow = packed + b.off + bw * ((bb + N * v - b.y0) + bh * (c - b.z0)) - b.x0 + a;
-                    for (int u = ulo; u <= uhi; ++u) {
-                        const float val = prow[N * u];
-                        const float* tp = ta + (b.s0 - u - dlo) * Dq + e2;
 #pragma unroll
-                        for (int q = 0; q < kLibT; ++q) acc[q] = fmaf(val, tp[q], acc[q]);
+            for (int k = 0; k < G; ++k) {
+                if (k >= cnt) break;
+                const LibBox b = boxes[grp[1 + k]];
+                const int* rk = rng + 4 * N * k;
+                const int vlo = rk[2 * N + bb], vhi = rk[3 * N + bb];
+                if (vhi < vlo || ls >= b.s1 - b.s0 || lt >= b.t1 - b.t0) continue;
+                const int bw = b.x1 - b.x0, bh = b.y1 - b.y0;
+                for (int a = 0; a < N; ++a) {
+                    const int ulo = rk[a], uhi = rk[N + a];
+                    if (uhi < ulo) continue;
+                    const float* ta = tile + a * tsz + base;
+                    for (int v = vlo; v <= vhi; ++v) {
+                        const int e2 = b.t0 - v - dlo;
+                        const float* prow = packed + b.off + bw * ((bb + N * v - b.y0) + bh * (c - b.z0)) - b.x0 + a;
+                        for (int u = ulo; u <= uhi; ++u) {
+                            const float val = prow[N * u];
+                            const float* tp = ta + (b.s0 - u - dlo) * Dq + e2;
+#pragma unroll
+                            for (int q = 0; q < kLibT; ++q) acc[k][q] = fmaf(val, tp[q], acc[k][q]);
+                        }
                     }
                 }
             }
         }
     }
-    if (!ok) return;
-    const int s = b.s0 + ls;
 #pragma unroll
-    for (int q = 0; q < kLibT; ++q) {
-        const int t = b.t0 + lt + q;
-        if (lt + q >= nt) break;
-        const int64_t x = ap + (int64_t)N * s, y = bp + (int64_t)N * t;
-        if (s < Lx && t < Ly && x < X && y < Y) out[(int64_t)n * ldn + (x + X * y) * ldp] = acc[q];
+    for (int k = 0; k < G; ++k) {
+        if (k >= cnt) break;
+        const int n = grp[1 + k];
+        const LibBox b = boxes[n];
+        if (ls >= b.s1 - b.s0 || lt >= b.t1 - b.t0) continue;
+        const int s = b.s0 + ls;
+#pragma unroll
+        for (int q = 0; q < kLibT; ++q) {
+            const int t = b.t0 + lt + q;
+            if (lt + q >= b.t1 - b.t0) break;
+            const int64_t x = ap + (int64_t)N * s, y = bp + (int64_t)N * t;
+            if (s < Lx && t < Ly && x < X && y < Y) out[(int64_t)n * ldn + (x + X * y) * ldp] = acc[k][q];
+        }
     }
 }
 
@@ -177,7 +197,7 @@ extern "C" int sid_library(sid_plan* p, const float* const* recon, int64_t n_com
     const int64_t N = p->N, D = p->g.D;
     std::vector<LibBox> boxes(n_neur);
     int64_t off = 0;
-    int max_nl = 0, span = 0;
+    int max_ns = 0, ntgM = 0, span = 0;
     for (int64_t n = 0; n < n_neur; ++n) {
         int bx[6];
         neuron_box(centers, n_neur, n, neur_rad, axial, p->X, p->Y, p->Z, bx);
@@ -198,18 +218,41 @@ extern "C" int sid_library(sid_plan* p, const float* const* recon, int64_t n_com
         b.s1 = (int)std::min<int64_t>(p->Lx, umax + p->g.dhi + 1);
         b.t0 = (int)std::max<int64_t>(0, vmin + p->g.dlo);
         b.t1 = (int)std::min<int64_t>(p->Ly, vmax + p->g.dhi + 1);
-        max_nl = std::max(max_nl, (b.s1 - b.s0) * (int)cdiv(b.t1 - b.t0, kLibT));
+        max_ns = std::max(max_ns, b.s1 - b.s0);
+        ntgM = std::max(ntgM, (int)cdiv(b.t1 - b.t0, kLibT));
         span = std::max(span, std::max(umax - umin, vmax - vmin));
         boxes[n] = b;
     }
     SID_REQUIRE(off < INT32_MAX, "sid_library: boxes too large");
     const int Dp = (int)D + 2 * span;
-    const size_t tile_bytes = (size_t)N * Dp * (Dp + kLibT) * sizeof(float) + (size_t)(D * D + 4 * N) * sizeof(int);
+    const size_t tile_bytes =
+        (size_t)N * Dp * (Dp + kLibT) * sizeof(float) + (size_t)(D * D + 4 * N * kLibG) * sizeof(int);
     SID_REQUIRE(tile_bytes <= 200 * 1024, "sid_library: tap tiles (%zu bytes) exceed shared memory", tile_bytes);
-    SID_REQUIRE(max_nl <= 256, "sid_library: neuron radius too large for one CTA (%d output groups)", max_nl);
+    SID_REQUIRE(max_ns * ntgM <= 256, "sid_library: neuron radius too large for one CTA (%d output groups)",
+                max_ns * ntgM);
+    // groups of up to kLibG neurons with the same depth window, in window order
+    std::vector<int64_t> order(n_neur);
+    for (int64_t n = 0; n < n_neur; ++n) order[n] = n;
+    std::stable_sort(order.begin(), order.end(), [&](int64_t x, int64_t y) {
+        return boxes[x].z0 != boxes[y].z0 ? boxes[x].z0 < boxes[y].z0 : boxes[x].z1 < boxes[y].z1;
+    });
+    std::vector<int> groups;
+    for (size_t i = 0; i < order.size();) {
+        size_t e = i + 1;
+        while (e < order.size() && (int)(e - i) < kLibG && boxes[order[e]].z0 == boxes[order[i]].z0 &&
+               boxes[order[e]].z1 == boxes[order[i]].z1)
+            ++e;
+        groups.push_back((int)(e - i));
+        for (size_t k = i; k < i + kLibG; ++k) groups.push_back(k < e ? (int)order[k] : 0);
+        i = e;
+    }
+    const int64_t ngroups = (int64_t)groups.size() / (kLibG + 1);
     DBuf& dbox = p->ws[3];
     DBuf& dpack = p->ws[2];
     DBuf& dmeta = p->ws[1];
+    DBuf& dgrp = p->ws[0];
+    SID_TRY(dgrp.alloc(groups.size() * sizeof(int)));
+    SID_CUDA_TRY(cudaMemcpyAsync(dgrp.p, groups.data(), groups.size() * sizeof(int), cudaMemcpyHostToDevice, st));
     SID_TRY(dbox.alloc(boxes.size() * sizeof(LibBox)));
     SID_TRY(dpack.alloc((size_t)off * sizeof(float)));
     SID_TRY(dmeta.alloc((size_t)(n_comp * sizeof(float*) + n_neur * n_comp)));
@@ -224,11 +267,12 @@ extern "C" int sid_library(sid_plan* p, const float* const* recon, int64_t n_com
     SID_CUDA_TRY(cudaMemsetAsync(out, 0, (size_t)(P * n_neur) * sizeof(float), st));
     const int64_t tbs = cdiv(N * D * D, 32) * 32;
     const int64_t ldn = out_layout == 0 ? 1 : P, ldp = out_layout == 0 ? n_neur : 1;
-    dim3 grid((unsigned)n_neur, (unsigned)(N * N));
-    SID_CUDA_TRY(cudaFuncSetAttribute(k_lib_project, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tile_bytes));
-    k_lib_project<<<grid, 256, tile_bytes, st>>>(p->taps_f.as<float>(), dpack.as<float>(), dbox.as<LibBox>(), (int)N,
-                                                 (int)D, (int)p->g.dlo, span, tbs, (int)p->Lx, (int)p->Ly, p->X, p->Y,
-                                                 out, ldn, ldp);
+    dim3 grid((unsigned)ngroups, (unsigned)(N * N));
+    SID_CUDA_TRY(cudaFuncSetAttribute(k_lib_project<kLibG>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)tile_bytes));
+    k_lib_project<kLibG><<<grid, 256, tile_bytes, st>>>(p->taps_f.as<float>(), dpack.as<float>(), dbox.as<LibBox>(),
+                                                        dgrp.as<int>(), (int)N, (int)D, (int)p->g.dlo, span, ntgM,
+                                                        tbs, (int)p->Lx, (int)p->Ly, p->X, p->Y, out, ldn, ldp);
     SID_CHECK_LAUNCH();
     // the staging buffers are read by the kernels above: wait before the host
     // vectors go out of scope and before the workspaces can be reused
