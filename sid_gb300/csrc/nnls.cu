@@ -5,9 +5,11 @@
 //   mask:   passive = (x > 0) | (df < 0), d = df .* passive, s1 = sum d^2
 //   G d     (contraction: tcgen05 split precision, or FP32 SIMT)
 //   step:   alpha = s1 / sum(d .* G d), x_new = max(x - alpha d, 0),
-//           step = x_new - x, convergence statistic of the step
-//   G step  (contraction; the next iteration's mask kernel applies
-//            df = df + G step before it reads df)
+//           step = x_new - x, convergence statistic of the step, and
+//           G step = -alpha (G d) + G (clamp corrections), formed in place
+//           from the contraction's G d (the clamps touch few entries); the
+//           next iteration's mask kernel applies df = df + G step before it
+//           reads df.  (With use_std a second contraction forms G step.)
 //   retire: the reference's log-linear extrapolation test
 // The iterate x and the gradient df are double-float (about 44 significant
 // bits, FP32 arithmetic) and the gradient is updated incrementally
@@ -81,9 +83,13 @@ struct ColBufs {
     uint16_t *vhi, *vlo; // K x F BF16 split operand, K-blocked (tensor-core path)
     float* g;            // K x F contraction result
     double* test;        // sample x F window of step statistics
-    double *s1, *fit, *anyp, *xmax;  // per column
+    float2* s1;          // per column: sum d.^2, plain and scaled by 2^100
+    double* fit;         // 3 x F window-fit results
+    float *anyp, *xmax;  // per column: passive count, max x
     double* xi;          // 2 x sample fit matrix
     float *u, *gu;       // use_std: column-sum vector and G * it
+    const float* Gf;     // K x K FP32 (normalised) Gram: the clamp corrections of G * step
+    int sparse;          // G * step formed in the step kernel (no second contraction)
     int* active;
     NnlsCounters* cnt;
     int F;
@@ -106,17 +112,38 @@ __device__ __forceinline__ void put_operand(const ColBufs& b, int64_t o, int j, 
 
 __global__ void k_iter_inc(NnlsCounters* c) { c->iter += 1; }
 
-__device__ __forceinline__ double warp_sum_d(double v)
+// Reductions on the FP32 and integer pipes.  A sum is carried as an
+// unevaluated pair hi + lo (an error-free two-sum at every addition), so the
+// partials add up as accurately as an FP64 sum would.  The column kernels issue
+// no FP64 instruction at all: GB300's FP64 rate is about 1/64 of its FP32
+// rate, an FP64 warp instruction holds its SM sub-partition for tens of cycles
+// whatever number of lanes it has active, and a few of them per warp cost as
+// much as the column pass itself.
+__device__ __forceinline__ float2 ff_add(float2 a, float2 b)
 {
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
-    return v;
+    const float s = a.x + b.x;
+    const float bb = s - a.x;
+    const float e = (a.x - (s - bb)) + (b.x - bb);
+    const float l = (a.y + b.y) + e;
+    const float hi = s + l;
+    return make_float2(hi, l - (hi - s));
 }
 
-__device__ __forceinline__ double warp_max_d(double v)
+__device__ __forceinline__ float2 warp_sum_ff(float v)
+{
+    float2 a = make_float2(v, 0.f);
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        const float2 o = make_float2(__shfl_xor_sync(0xffffffffu, a.x, off), __shfl_xor_sync(0xffffffffu, a.y, off));
+        a = ff_add(a, o);
+    }
+    return a;
+}
+
+__device__ __forceinline__ float warp_max_f(float v)
 {
 #pragma unroll
-    for (int off = 16; off > 0; off >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, off));
+    for (int off = 16; off > 0; off >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, off));
     return v;
 }
 
@@ -142,16 +169,41 @@ __device__ __forceinline__ ColIdx col_idx()
     return c;
 }
 
+// Column sums of products for the line search, s1 = sum d.^2 and
+// den = sum d .* (G d) (LS_nnls.m:122, fast_nnls.m:119).  A converging column's
+// masked gradient shrinks geometrically, and below |d| ~ 1e-19 its FP32
+// products underflow: den reaches 0 while s1 is still a denormal, which would
+// make alpha infinite.  Each thread therefore keeps a second partial of the same
+// products with both factors scaled by 2^50 (exact).  alpha is the ratio of
+// the two scaled sums when both are finite (they overflow only for products
+// above ~1e8, where the plain sums are exact to FP32 rounding), else of the
+// two plain sums.
+constexpr float kWideUp = 0x1p50f;
+
+__device__ __forceinline__ void wide_fma(float a, float b, float& plain, float& wide)
+{
+    plain = fmaf(a, b, plain);
+    wide = fmaf(a * kWideUp, b * kWideUp, wide);
+}
+
+// num, den: {plain, scaled} column sums
+__device__ __forceinline__ float wide_ratio(float2 num, float2 den)
+{
+    return (isfinite(num.y) && isfinite(den.y)) ? num.y / den.y : num.x / den.x;
+}
+
 // The pending gradient update df += G step of the previous iteration
 // (fast_nnls.m:153; the incremental form of LS_nnls.m:119), then the passive
 // set and masked gradient (LS_nnls.m:120-121, fast_nnls.m:100,163).  g holds
 // G step (zero before the first iteration).
 __global__ void __launch_bounds__(256) k_nn_mask(ColBufs b, int K, int F, int use_std)
 {
-    __shared__ double red[kColsPerCta][kWarpsPerCol][3];
+    __shared__ float2 red[kColsPerCta][kWarpsPerCol][2];
+    __shared__ float redm[kColsPerCta][kWarpsPerCol];
+    __shared__ int redn[kColsPerCta][kWarpsPerCol];
     const ColIdx c = col_idx();
     const bool act = c.j < F && b.active[c.j];
-    float acc_f = 0.f, mx_f = -INFINITY;
+    float acc_f = 0.f, accw_f = 0.f, mx_f = -INFINITY;
     int np_i = 0;
     if (act) {
         const int64_t o = (int64_t)c.j * K;
@@ -165,30 +217,121 @@ __global__ void __launch_bounds__(256) k_nn_mask(ColBufs b, int K, int F, int us
             const bool p = xv.x > 0.f || dv.x < 0.f;
             const float dm = p ? dv.x + dv.y : 0.f;
             put_operand(b, o, c.j, k, dm);
-            acc_f = fmaf(dm, dm, acc_f);
+            wide_fma(dm, dm, acc_f, accw_f);
             np_i += p ? 1 : 0;
             mx_f = fmaxf(mx_f, xv.x);
         }
     }
-    const double acc = warp_sum_d((double)acc_f);
-    const double np = warp_sum_d((double)np_i);
-    const double mx = warp_max_d((double)mx_f);
+    const float2 acc = warp_sum_ff(acc_f);
+    const float2 accw = warp_sum_ff(accw_f);
+    const int np = __reduce_add_sync(0xffffffffu, np_i);
+    const float mx = warp_max_f(mx_f);
     if (c.lane == 0) {
         red[c.cl][c.wc][0] = acc;
-        red[c.cl][c.wc][1] = np;
-        red[c.cl][c.wc][2] = mx;
+        red[c.cl][c.wc][1] = accw;
+        redn[c.cl][c.wc] = np;
+        redm[c.cl][c.wc] = mx;
     }
     __syncthreads();
     if (act && c.wc == 0 && c.lane == 0) {
-        double s = 0.0, n = 0.0, m = -INFINITY;
-        for (int w = 0; w < kWarpsPerCol; ++w) {
-            s += red[c.cl][w][0];
-            n += red[c.cl][w][1];
-            m = fmax(m, red[c.cl][w][2]);
+        float2 s = red[c.cl][0][0], sw = red[c.cl][0][1];
+        int n = redn[c.cl][0];
+        float m = redm[c.cl][0];
+        for (int w = 1; w < kWarpsPerCol; ++w) {
+            s = ff_add(s, red[c.cl][w][0]);
+            sw = ff_add(sw, red[c.cl][w][1]);
+            n += redn[c.cl][w];
+            m = fmaxf(m, redm[c.cl][w]);
         }
-        b.s1[c.j] = s;
-        b.anyp[c.j] = n;
+        b.s1[c.j] = make_float2(s.x, sw.x);
+        b.anyp[c.j] = (float)n;
         b.xmax[c.j] = m;
+    }
+}
+
+// G step without a second contraction (sparse mode).  step = -alpha d + c with
+// d the masked gradient whose product G d the first contraction left in b.g,
+// and c nonzero only where the bound clamps (a small fraction of the entries),
+// so G step = -alpha (G d) + sum over the clamped k of G(:, k) c_k.  The clamped
+// entries of a column are compacted in thread order (deterministic), in rounds
+// of kClampList, and b.g is overwritten with G step for the next iteration's
+// mask kernel (fast_nnls.m:153).
+constexpr int kStepRows = 16;   // rows per thread: K <= 16 * 128 in sparse mode
+constexpr int kClampList = 256;
+
+__device__ __forceinline__ void gstep_sparse(const ColBufs& b, int K, const ColIdx& c, bool act, int64_t o,
+                                             float alpha_f, const float (&cc)[kStepRows], unsigned cmask)
+{
+    __shared__ int lk[kColsPerCta][kClampList];
+    __shared__ float lc[kColsPerCta][kClampList];
+    __shared__ int wtot[kColsPerCta][kWarpsPerCol];
+    __shared__ int rounds_s;
+    const int cnt = __popc(cmask);
+    int incl = cnt;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const int v = __shfl_up_sync(0xffffffffu, incl, d);
+        if (c.lane >= d) incl += v;
+    }
+    if (threadIdx.x == 0) rounds_s = 0;
+    __syncthreads();
+    if (c.lane == 31) wtot[c.cl][c.wc] = incl;
+    __syncthreads();
+    int base = 0, ntot = 0;
+    for (int w = 0; w < kWarpsPerCol; ++w) {
+        if (w < c.wc) base += wtot[c.cl][w];
+        ntot += wtot[c.cl][w];
+    }
+    if (c.wc == 0 && c.lane == 0) atomicMax(&rounds_s, (ntot + kClampList - 1) / kClampList);
+    __syncthreads();
+    const int rounds = rounds_s;
+    float corr[kStepRows];
+#pragma unroll
+    for (int t = 0; t < kStepRows; ++t) corr[t] = 0.f;
+    for (int r = 0; r < rounds; ++r) {
+        const int lo = r * kClampList;
+        int pos = base + incl - cnt;
+#pragma unroll
+        for (int t = 0; t < kStepRows; ++t)
+            if (cmask & (1u << t)) {
+                if (pos >= lo && pos < lo + kClampList) {
+                    lk[c.cl][pos - lo] = c.wc * 32 + c.lane + t * kColThreads;
+                    lc[c.cl][pos - lo] = cc[t];
+                }
+                ++pos;
+            }
+        __syncthreads();
+        const int n = min(kClampList, ntot - lo);
+        if (act) {
+            // four clamped columns of G per pass keep four L2 reads in flight per row
+            for (int m = 0; m < n; m += 4) {
+                const float* gc[4];
+                float cv[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const bool ok = m + u < n;
+                    gc[u] = b.Gf + (int64_t)(ok ? lk[c.cl][m + u] : 0) * K;
+                    cv[u] = ok ? lc[c.cl][m + u] : 0.f;
+                }
+#pragma unroll
+                for (int t = 0; t < kStepRows; ++t) {
+                    const int k = c.wc * 32 + c.lane + t * kColThreads;
+                    if (k < K) {
+                        float a = corr[t];
+#pragma unroll
+                        for (int u = 0; u < 4; ++u) a = fmaf(__ldg(gc[u] + k), cv[u], a);
+                        corr[t] = a;
+                    }
+                }
+            }
+        }
+        __syncthreads();
+    }
+    if (!act) return;
+#pragma unroll
+    for (int t = 0; t < kStepRows; ++t) {
+        const int k = c.wc * 32 + c.lane + t * kColThreads;
+        if (k < K) b.g[o + k] = fmaf(-alpha_f, b.g[o + k], corr[t]);
     }
 }
 
@@ -197,11 +340,11 @@ __global__ void __launch_bounds__(256) k_nn_mask(ColBufs b, int K, int F, int us
 __global__ void __launch_bounds__(256) k_nn_step(ColBufs b, int K, int F, int solver, int sample, int tol_p,
                                                  int use_std)
 {
-    __shared__ double red[kColsPerCta][kWarpsPerCol][2];
+    __shared__ float2 red[kColsPerCta][kWarpsPerCol][2];
     const ColIdx c = col_idx();
     const bool act = c.j < F && b.active[c.j];
     const int64_t o = (int64_t)c.j * K;
-    float s2_f = 0.f;
+    float s2_f = 0.f, s2w_f = 0.f;
     if (act) {
 #pragma unroll 2
         for (int k = c.wc * 32 + c.lane; k < K; k += kColThreads) {
@@ -209,21 +352,44 @@ __global__ void __launch_bounds__(256) k_nn_step(ColBufs b, int K, int F, int so
             const float dm = (xv.x > 0.f || dv.x < 0.f) ? dv.x + dv.y : 0.f;
             float g = b.g[o + k];
             if (use_std) g -= b.gu[k];
-            s2_f = fmaf(dm, g, s2_f);
+            wide_fma(dm, g, s2_f, s2w_f);
         }
     }
-    const double s2 = warp_sum_d((double)s2_f);
-    if (c.lane == 0) red[c.cl][c.wc][0] = s2;
+    const float2 s2 = warp_sum_ff(s2_f);
+    const float2 s2w = warp_sum_ff(s2w_f);
+    if (c.lane == 0) {
+        red[c.cl][c.wc][0] = s2;
+        red[c.cl][c.wc][1] = s2w;
+    }
     __syncthreads();
-    double den = 0.0;
-    for (int w = 0; w < kWarpsPerCol; ++w) den += red[c.cl][w][0];
+    // one thread per column forms alpha and shares it
+    __shared__ float alpha_s[kColsPerCta];
+    if (c.wc == 0 && c.lane == 0) {
+        float2 den = red[c.cl][0][0], denw = red[c.cl][0][1];
+        for (int w = 1; w < kWarpsPerCol; ++w) {
+            den = ff_add(den, red[c.cl][w][0]);
+            denw = ff_add(denw, red[c.cl][w][1]);
+        }
+        // NaN (no passive entry) gives no step (LS_nnls.m:123, fast_nnls.m:120);
+        // so does a step beyond the FP32 range, which only sums below the
+        // range of the products above can produce
+        float af = act ? wide_ratio(b.s1[c.j], make_float2(den.x, denw.x)) : 0.f;
+        if (!isfinite(af)) af = 0.f;
+        alpha_s[c.cl] = af;
+    }
+    __syncthreads();
     float a1_f = 0.f, a2_f = 0.f;
+    const float alpha_f = alpha_s[c.cl];
+    // sparse mode: this thread's clamp corrections c = step - (-alpha d), rows
+    // k = wc*32 + lane + 128 t (t < kStepRows)
+    float cc[kStepRows];
+    unsigned cmask = 0;
     if (act) {
-        double alpha = b.s1[c.j] / den;
-        if (isnan(alpha)) alpha = 0.0;
-        const float alpha_f = (float)alpha;
-#pragma unroll 2
-        for (int k = c.wc * 32 + c.lane; k < K; k += kColThreads) {
+#pragma unroll
+        for (int t = 0; t < kStepRows; ++t) {
+            const int k = c.wc * 32 + c.lane + t * kColThreads;
+            cc[t] = 0.f;
+            if (k >= K) continue;
             const float2 xv = b.x[o + k], dv = b.df[o + k];
             const float dm = (xv.x > 0.f || dv.x < 0.f) ? dv.x + dv.y : 0.f;
             const float pstep = dm * alpha_f;
@@ -233,43 +399,52 @@ __global__ void __launch_bounds__(256) k_nn_step(ColBufs b, int K, int F, int so
             if (xn.x < 0.f) {
                 xn = make_float2(0.f, 0.f);
                 stp = -(xv.x + xv.y);
+                cc[t] = stp + pstep;
+                cmask |= 1u << t;
             }
             b.x[o + k] = xn;
-            put_operand(b, o, c.j, k, stp);
+            if (!b.sparse) put_operand(b, o, c.j, k, stp);
+            // the convergence statistic takes the difference of the stored
+            // iterates, as the reference does: it reaches 0 once the step falls
+            // below the iterate's rounding, where the FP64 reference's does too
+            const float dx = (xn.x - xv.x) + (xn.y - xv.y);
             if (solver == SOLVER_LS) {
-                a1_f += stp;                     // sum(x - x_)
+                a1_f += dx;                      // sum(x - x_)
                 a2_f = fmaf(xv.x, xv.x, a2_f);   // sum(x_.^2)
             } else {
-                a1_f += (tol_p == 2) ? stp * stp : fabsf(stp);
+                a1_f += (tol_p == 2) ? dx * dx : fabsf(dx);
             }
         }
     }
-    const double a1 = warp_sum_d((double)a1_f);
-    const double a2 = warp_sum_d((double)a2_f);
+    const float2 a1p = warp_sum_ff(a1_f);
+    const float2 a2p = warp_sum_ff(a2_f);
     __syncthreads();  // everyone has read the first exchange
     if (c.lane == 0) {
-        red[c.cl][c.wc][0] = a1;
-        red[c.cl][c.wc][1] = a2;
+        red[c.cl][c.wc][0] = a1p;
+        red[c.cl][c.wc][1] = a2p;
     }
     __syncthreads();
     const int it = b.cnt->iter;
     if (act && c.wc == 0 && c.lane == 0 && (it & 1)) {
-        double t1 = 0.0, t2 = 0.0;
-        for (int w = 0; w < kWarpsPerCol; ++w) {
-            t1 += red[c.cl][w][0];
-            t2 += red[c.cl][w][1];
+        float2 t1 = red[c.cl][0][0], t2 = red[c.cl][0][1];
+        for (int w = 1; w < kWarpsPerCol; ++w) {
+            t1 = ff_add(t1, red[c.cl][w][0]);
+            t2 = ff_add(t2, red[c.cl][w][1]);
         }
-        double t;
+        // FP32 logarithms: the statistic feeds a linear fit with absolute
+        // tolerances (tol_ * sample), far above FP32 rounding of a logarithm
+        float t;
         int e;
         if (solver == SOLVER_LS) {
-            t = log(t1 * t1 / t2) / 2.0;  // LS_nnls.m:136
+            t = logf(fabsf(t1.x)) - 0.5f * logf(t2.x);  // log(t1^2 / t2) / 2, LS_nnls.m:136
             e = (it - 1) / 2;
         } else {
-            t = (tol_p == 2) ? log(sqrt(t1)) : log(t1);  // fast_nnls.m:138-141
+            t = (tol_p == 2) ? 0.5f * logf(t1.x) : logf(t1.x);  // fast_nnls.m:138-141
             e = (it - 3) / 2;
         }
-        if (e >= 0) b.test[(int64_t)(e % sample) * F + c.j] = t;
+        if (e >= 0) b.test[(int64_t)(e % sample) * F + c.j] = (double)t;
     }
+    if (b.sparse) gstep_sparse(b, K, c, act, o, alpha_f, cc, cmask);
 }
 
 // df = df + G x0 for a warm start with use_std (G x0 minus its column-sum term)
@@ -356,8 +531,8 @@ __global__ void k_nn_retire(ColBufs b, int32_t* __restrict__ iters, int K, int F
                 const bool c1 = exp(te) / (1.0 - exp(k1first)) < tol;
                 ids = (c1 && c2 && c3) || (te == -INFINITY);
             } else {
-                const bool c1 = hmax * exp(te) / (1.0 - exp(k1)) < tol * (double)K * b.xmax[j];
-                ids = (b.anyp[j] == 0.0) || (c1 && c2 && c3);
+                const bool c1 = hmax * exp(te) / (1.0 - exp(k1)) < tol * (double)K * (double)b.xmax[j];
+                ids = (b.anyp[j] == 0.f) || (c1 && c2 && c3);
             }
         }
         if (ids) {
@@ -518,10 +693,10 @@ static int alloc_work(sid_ctx* c, int64_t K, int64_t F, int sample, bool split, 
     b.g = nn[3].as<float>();
     b.test = nn[4].as<double>();
     double* sc = nn[5].as<double>();
-    b.s1 = sc;
+    b.s1 = reinterpret_cast<float2*>(sc);
     b.fit = sc + F;  // 3F
-    b.anyp = sc + 4 * F;
-    b.xmax = sc + 5 * F;
+    b.anyp = reinterpret_cast<float*>(sc + 4 * F);
+    b.xmax = reinterpret_cast<float*>(sc + 5 * F);
     b.xi = sc + 6 * F;
     b.active = nn[6].as<int>();
     b.cnt = reinterpret_cast<NnlsCounters*>(nn[6].as<uint8_t>() + cdiv(F * 4, 16) * 16);
@@ -657,6 +832,10 @@ static int iterate(sid_ctx* c, NnlsWork& w, int64_t K, int64_t F, int solver, co
     SID_CUDA_TRY(cudaStreamSynchronize(st));
     const int use_std = (solver == SOLVER_LS && o->use_std) ? 1 : 0;
     const int max_iter = (int)o->max_iter;
+    // G step from G d and the clamp corrections (one contraction per iteration),
+    // except with use_std, whose operand carries a column-mean term
+    b.sparse = (!use_std && K <= (int64_t)kStepRows * kColThreads) ? 1 : 0;
+    b.Gf = w.G;
     auto gmul_std = [&](cudaStream_t s) -> int {
         SID_TRY(gmul(c, w, K, F, s));
         if (use_std) {
@@ -677,7 +856,7 @@ static int iterate(sid_ctx* c, NnlsWork& w, int64_t K, int64_t F, int solver, co
         k_nn_step<<<(unsigned)cdiv(F, kColsPerCta), kColsPerCta * kColThreads, 0, s>>>(
             b, (int)K, (int)F, solver, sample, (int)o->tol_p, use_std);
         SID_CHECK_LAUNCH();
-        SID_TRY(gmul_std(s));  // G step: applied by the next iteration's mask kernel
+        if (!b.sparse) SID_TRY(gmul_std(s));  // G step: applied by the next iteration's mask kernel
         k_nn_fit<<<cdiv(F, 256), 256, 0, s>>>(b, (int)F, solver, sample, max_iter, use_std);
         SID_CHECK_LAUNCH();
         if (solver == SOLVER_LS) {

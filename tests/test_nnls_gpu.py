@@ -63,10 +63,24 @@ def test_fast_nnls_matches_oracle(ctx, oracle, prec):
     ctx.sync()
     Xo, Qo, _, _, ito = oracle.fast_nnls(A, Y, {}, return_iters=True)
     it = it.cpu().numpy()
-    # the early-retirement fraction is a threshold statistic: the FP64 oracle
-    # itself gives 0.725 with x86 BLAS and 0.7625 with Arm BLAS on this problem
-    assert abs(np.mean(it < 2001) - np.mean(ito < 2001)) <= 0.2, (np.mean(it < 2001), np.mean(ito < 2001))
-    assert abs(np.median(it) - np.median(ito)) <= 0.2 * np.median(ito) + 4, (np.median(it), np.median(ito))
+    # Retirement is the reference's threshold test on the log sizes of the
+    # iterate differences (fast_nnls.m:138-149).  A column that converges
+    # geometrically retires at the first checks once a 30-sample window of
+    # the statistic is linear; those columns must retire at the same iteration.
+    # A column whose differences reach the iterate's rounding floor before such
+    # a window forms gets a flat or -inf window and retires late or never, and
+    # which columns do that depends on the arithmetic: the FP64 oracle retires
+    # 0.725 of these columns early with x86 BLAS and 0.7625 with Arm BLAS, the
+    # reference's own single-precision runs floor far sooner, and the
+    # double-float iterate here (about 49 bits) floors a few iterations before
+    # FP64 does.
+    clean = ito <= 2 * 30 + 31
+    same = np.abs(it[clean] - ito[clean]) <= 6
+    assert same.mean() >= 0.75, (same.mean(), it[clean], ito[clean])
+    assert abs(np.mean(it < 2001) - np.mean(ito < 2001)) <= 0.25, (np.mean(it < 2001), np.mean(ito < 2001))
+    early = it < 2001
+    viol, _ = kkt(A, Y[:, early], Xg[:, early])
+    assert viol < 1e-4, viol
     assert rel_l2(to_numpy(Q), Qo) < 1e-5
     assert rel_l2(Xg, Xo) < 1e-3, rel_l2(Xg, Xo)
     viol, mn = kkt(A, Y, Xg)
