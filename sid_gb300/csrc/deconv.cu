@@ -83,24 +83,48 @@ int plan_sync(sid_plan* p, cudaStream_t st)
 // ------------------------------------------------------ elementwise + sums --
 constexpr int kRedBlocks = 1024;
 
-// partial[block] = sum over the block's grid-stride range of a[i]*b[i] (double)
-__global__ void k_dot_partial(const float* __restrict__ a, const float* __restrict__ b, int64_t n,
-                              double* __restrict__ partial)
+// Sums on the FP32 pipes: exact products (fmaf two-product) added as
+// unevaluated pairs hi + lo (two-sum), as accurate as FP64 accumulation.
+// GB300's FP64 rate is about 1/64 of its FP32 rate: an FP64 product and add
+// per voxel made the dot products of a 31-million-voxel volume FP64-bound at
+// about four times their memory time.
+__device__ __forceinline__ float2 ff_add(float2 a, float2 b)
 {
-    __shared__ double red[256];
-    double s = 0.0;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        s += (double)a[i] * (double)b[i];
-    red[threadIdx.x] = s;
-    __syncthreads();
-    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-        if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) partial[blockIdx.x] = red[0];
+    const float s = a.x + b.x;
+    const float bb = s - a.x;
+    const float e = (a.x - (s - bb)) + (b.x - bb);
+    const float l = (a.y + b.y) + e;
+    const float hi = s + l;
+    return make_float2(hi, l - (hi - s));
 }
 
-__global__ void k_sum_partials(const double* __restrict__ partial, int n, double* __restrict__ out)
+// partial[block] = sum over the block's grid-stride range of a[i]*b[i]
+__global__ void __launch_bounds__(256) k_dot_partial(const float* __restrict__ a, const float* __restrict__ b,
+                                                     int64_t n, double* __restrict__ partial)
+{
+    __shared__ float2 red[8];
+    float2 s = make_float2(0.f, 0.f);
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const float x = a[i], y = b[i];
+        const float p = x * y;
+        s = ff_add(s, make_float2(p, fmaf(x, y, -p)));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        s = ff_add(s, make_float2(__shfl_xor_sync(0xffffffffu, s.x, o), __shfl_xor_sync(0xffffffffu, s.y, o)));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float2 t = red[0];
+        for (int w = 1; w < 8; ++w) t = ff_add(t, red[w]);
+        partial[blockIdx.x] = (double)t.x + (double)t.y;
+    }
+}
+
+// *out = sum of the partials (one CTA); with `alpha`, also the LS step size
+// *num / *out as FP32, 0 where not finite (LS_deconv.m:86-88)
+__global__ void k_sum_partials(const double* __restrict__ partial, int n, double* __restrict__ out,
+                               const double* __restrict__ num, float* __restrict__ alpha)
 {
     __shared__ double red[256];
     double s = 0.0;
@@ -111,15 +135,22 @@ __global__ void k_sum_partials(const double* __restrict__ partial, int n, double
         if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
         __syncthreads();
     }
-    if (threadIdx.x == 0) *out = red[0];
+    if (threadIdx.x == 0) {
+        *out = red[0];
+        if (alpha) {
+            const float a = (float)(*num / red[0]);
+            *alpha = isfinite(a) ? a : 0.f;
+        }
+    }
 }
 
 // out = sum a.*b, deterministic two-stage reduction into `out` (device double)
-static int dot(const float* a, const float* b, int64_t n, double* scratch, double* out, cudaStream_t st)
+static int dot(const float* a, const float* b, int64_t n, double* scratch, double* out, cudaStream_t st,
+               const double* num = nullptr, float* alpha = nullptr)
 {
     k_dot_partial<<<kRedBlocks, 256, 0, st>>>(a, b, n, scratch);
     SID_CHECK_LAUNCH();
-    k_sum_partials<<<1, 256, 0, st>>>(scratch, kRedBlocks, out);
+    k_sum_partials<<<1, 256, 0, st>>>(scratch, kRedBlocks, out, num, alpha);
     SID_CHECK_LAUNCH();
     return SID_OK;
 }
@@ -173,14 +204,12 @@ __global__ void k_ls_passive(const float* __restrict__ x, const float* __restric
     }
 }
 
-// alpha = s1/s2 (nan/inf -> 0); xn = max(x - alpha*d_, 0); dm <- xn - x; x <- xn
-// (LS_deconv.m:86-91)
-__global__ void k_ls_step(float* __restrict__ x, float* __restrict__ dm, const double* __restrict__ s12,
+// xn = max(x - alpha*d_, 0); dm <- xn - x; x <- xn  (LS_deconv.m:89-91; alpha
+// = s1/s2 with nan/inf -> 0, formed once by the reduction)
+__global__ void k_ls_step(float* __restrict__ x, float* __restrict__ dm, const float* __restrict__ alpha_p,
                           int64_t n)
 {
-    double a = s12[0] / s12[1];
-    if (!isfinite(a)) a = 0.0;
-    const float alpha = (float)a;
+    const float alpha = *alpha_p;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const float xo = x[i];
         float xn = xo - alpha * dm[i];
@@ -382,7 +411,8 @@ extern "C" int sid_deconv_ls(sid_plan* p, int method, float* X, int max_iter, fl
     float* dp = p->ws[1].as<float>();
     float* tp = p->ws[2].as<float>();
     double* red = p->red.as<double>();
-    double* s12 = red + kRedBlocks;  // two scalars after the partials
+    double* s12 = red + kRedBlocks;  // two scalars after the partials, then alpha
+    float* alpha = reinterpret_cast<float*>(s12 + 2);
     SID_TRY(v_to_vp(p, X, xp, p->Z, st));
     // df = Q(x0) - x0 + lamb_L1 with x0 = df
     SID_TRY(fwd_poly(p, method, xp, p->ip.as<float>(), st));
@@ -395,8 +425,8 @@ extern "C" int sid_deconv_ls(sid_plan* p, int method, float* X, int max_iter, fl
         SID_CHECK_LAUNCH();
         SID_TRY(dot(tp, tp, n, red, s12, st));
         SID_TRY(fwd_poly(p, method, tp, p->ip.as<float>(), st));
-        SID_TRY(dot(p->ip.as<float>(), p->ip.as<float>(), ni, red, s12 + 1, st));
-        k_ls_step<<<2048, 256, 0, st>>>(xp, tp, s12, n);
+        SID_TRY(dot(p->ip.as<float>(), p->ip.as<float>(), ni, red, s12 + 1, st, s12, alpha));
+        k_ls_step<<<2048, 256, 0, st>>>(xp, tp, alpha, n);
         SID_CHECK_LAUNCH();
         SID_TRY(fwd_poly(p, method, tp, p->ip.as<float>(), st));
         SID_TRY(adj_poly(p, method, p->ip.as<float>(), p->bp.as<float>(), st));

@@ -9,7 +9,10 @@
 //                                                    in shared memory by frame chunks
 // Each byte of Y is read once per pass; the standard-deviation image needs A
 // and B, which the last spatial update of the factorisation computes in the
-// same pass.  Sums are FP32 over blocks of kSub terms, the blocks added in FP64.
+// same pass.  Sums are FP32 over blocks of kSub terms, the blocks added as
+// unevaluated FP32 pairs hi + lo (two-sum: FP64 accuracy on the FP32 pipes;
+// GB300's FP64 rate is about 1/64 of FP32, and an FP64 add per block held the
+// passes below the HBM rate).
 #include <algorithm>
 #include <cuda_fp16.h>
 
@@ -20,11 +23,48 @@ namespace sid {
 namespace {
 
 constexpr int kThreads = 256;
-constexpr int kSub = 32;        // FP32 terms per FP64 addition
+constexpr int kSub = 32;        // FP32 terms per pair addition
 constexpr int kTChunk = 2048;   // frames of t staged per shared-memory round
 
 __device__ __forceinline__ float ld(const float* p) { return __ldcs(p); }
 __device__ __forceinline__ float ld(const __half* p) { return __half2float(__ldcs(p)); }
+
+__device__ __forceinline__ float2 ff_add(float2 a, float2 b)
+{
+    const float s = a.x + b.x;
+    const float bb = s - a.x;
+    const float e = (a.x - (s - bb)) + (b.x - bb);
+    const float l = (a.y + b.y) + e;
+    const float hi = s + l;
+    return make_float2(hi, l - (hi - s));
+}
+
+__device__ __forceinline__ float2 ff_add(float2 a, float b) { return ff_add(a, make_float2(b, 0.f)); }
+
+__device__ __forceinline__ float2 warp_sum_ff(float2 v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        v = ff_add(v, make_float2(__shfl_xor_sync(0xffffffffu, v.x, o), __shfl_xor_sync(0xffffffffu, v.y, o)));
+    return v;
+}
+
+// block sum of pairs, as FP64 in thread 0
+__device__ __forceinline__ double block_sum_ff(float2 v, float2* red)
+{
+    v = warp_sum_ff(v);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) red[warp] = v;
+    __syncthreads();
+    double r = 0.0;
+    if (threadIdx.x == 0) {
+        float2 t = red[0];
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) t = ff_add(t, red[w]);
+        r = (double)t.x + (double)t.y;
+    }
+    return r;  // valid in thread 0
+}
 
 __device__ __forceinline__ double block_sum(double v, double* red)
 {
@@ -83,16 +123,16 @@ k_col_pass(const T* __restrict__ Y, int64_t P, int64_t F, const float* __restric
            int64_t ps, float scale_s, double* __restrict__ t)
 {
     constexpr int U = 4;
-    __shared__ double red[kThreads / 32];
+    __shared__ float2 red[kThreads / 32];
     for (int64_t j = blockIdx.x; j < F; j += gridDim.x) {
         const T* col = Y + j * P;
         const int64_t head = std::min<int64_t>(P, (int64_t)(((16 - ((uintptr_t)col & 15)) & 15) / sizeof(T)));
         const int64_t nv = (P - head) / 8;
-        double acc = 0.0;
+        float2 acc = make_float2(0.f, 0.f);
         float part = 0.f;
         for (int64_t i = threadIdx.x; i < head; i += kThreads) part = fmaf(s ? s[i] : 1.f, ld(col + i), part);
         for (int64_t i = head + nv * 8 + threadIdx.x; i < P; i += kThreads) part = fmaf(s ? s[i] : 1.f, ld(col + i), part);
-        acc += part;
+        acc = ff_add(acc, part);
         const T* body = col + head;
         const int a = (int)((4 - head % 4) % 4);
         const float* sb = s ? s4 + a * ps + a + head : nullptr;
@@ -124,10 +164,10 @@ k_col_pass(const T* __restrict__ Y, int64_t P, int64_t F, const float* __restric
                     p2 = fmaf(b.z, y[u][6], p2); p2 = fmaf(b.w, y[u][7], p2);
                 }
             }
-            acc += p2;
+            acc = ff_add(acc, p2);
         }
-        acc = block_sum(acc, red);
-        if (threadIdx.x == 0) t[j] = acc * (double)scale_s;
+        const double tot = block_sum_ff(acc, red);
+        if (threadIdx.x == 0) t[j] = tot * (double)scale_s;
     }
 }
 
@@ -141,7 +181,7 @@ k_row_pass(const T* __restrict__ Y, int64_t P, int64_t F, const float* __restric
     __shared__ float ts[kTChunk];
     const int64_t i = blockIdx.x * (int64_t)kThreads + threadIdx.x;
     const bool live = i < P;
-    double sd = 0.0, ad = 0.0, bd = 0.0;
+    float2 sd = make_float2(0.f, 0.f), ad = sd, bd = sd;
     for (int64_t j0 = 0; j0 < F; j0 += kTChunk) {
         const int nj = (int)std::min<int64_t>(kTChunk, F - j0);
         if (t) {
@@ -161,43 +201,52 @@ k_row_pass(const T* __restrict__ Y, int64_t P, int64_t F, const float* __restric
 #pragma unroll
                 for (int k = 0; k < kSub; ++k) {
                     if (t) sp = fmaf(y[k], ts[k0 + k], sp);
-                    ap = fmaf(y[k], y[k], ap);
-                    bp += y[k];
+                    if (stats) {
+                        ap = fmaf(y[k], y[k], ap);
+                        bp += y[k];
+                    }
                 }
             } else {
                 for (int k = 0; k < kn; ++k) {
                     const float y = ld(yp + (int64_t)(k0 + k) * P);
                     if (t) sp = fmaf(y, ts[k0 + k], sp);
-                    ap = fmaf(y, y, ap);
-                    bp += y;
+                    if (stats) {
+                        ap = fmaf(y, y, ap);
+                        bp += y;
+                    }
                 }
             }
-            sd += sp;
-            ad += ap;
-            bd += bp;
+            if (t) sd = ff_add(sd, sp);
+            if (stats) {
+                ad = ff_add(ad, ap);
+                bd = ff_add(bd, bp);
+            }
         }
     }
     if (!live) return;
-    if (s_out) s_out[i] = sd;
+    if (s_out) s_out[i] = (double)sd.x + (double)sd.y;
     if (stats) {
-        a_out[i] = ad;
-        b_out[i] = bd;
+        a_out[i] = (double)ad.x + (double)ad.y;
+        b_out[i] = (double)bd.x + (double)bd.y;
     }
 }
 
-// sum of squares of x (n doubles) -> *out (one CTA)
-__global__ void k_sumsq(const double* __restrict__ x, int64_t n, double* __restrict__ out)
+// sum of squares of x (n doubles) -> *out, and 1/sqrt of it -> *inv (one CTA)
+__global__ void k_sumsq(const double* __restrict__ x, int64_t n, double* __restrict__ out, double* __restrict__ inv)
 {
     __shared__ double red[kThreads / 32];
     double acc = 0.0;
     for (int64_t i = threadIdx.x; i < n; i += kThreads) acc += x[i] * x[i];
     acc = block_sum(acc, red);
-    if (threadIdx.x == 0) *out = acc;
+    if (threadIdx.x == 0) {
+        *out = acc;
+        *inv = 1.0 / sqrt(acc);
+    }
 }
 
 // partial sums of squares per CTA; the last CTA adds them (deterministic order)
 __global__ void k_sumsq_big(const double* __restrict__ x, int64_t n, double* __restrict__ part,
-                            unsigned int* __restrict__ done, double* __restrict__ out)
+                            unsigned int* __restrict__ done, double* __restrict__ out, double* __restrict__ inv)
 {
     __shared__ double red[kThreads / 32];
     __shared__ bool last;
@@ -211,22 +260,28 @@ __global__ void k_sumsq_big(const double* __restrict__ x, int64_t n, double* __r
         last = atomicAdd(done, 1u) == gridDim.x - 1;
     }
     __syncthreads();
-    if (last && threadIdx.x == 0) {
-        __threadfence();
-        double s = 0.0;
-        for (unsigned b = 0; b < gridDim.x; ++b) s += part[b];
+    if (!last) return;
+    // the last CTA adds the partials, all its threads in a fixed order (a
+    // single thread's chain of dependent FP64 adds is slow on GB300)
+    __threadfence();
+    double s = 0.0;
+    for (unsigned b = threadIdx.x; b < gridDim.x; b += kThreads) s += part[b];
+    s = block_sum(s, red);
+    if (threadIdx.x == 0) {
         *out = s;
+        *inv = 1.0 / sqrt(s);
         *done = 0;
     }
 }
 
-// y = x / sqrt(*ss) (or x when ss == nullptr), FP64 -> FP32
-__global__ void k_scale_out(const double* __restrict__ x, int64_t n, const double* __restrict__ ss,
+// y = x * (*inv) (or x when inv == nullptr; inv = 1/sqrt of the sum of squares,
+// formed once by the reduction, not per thread), FP64 -> FP32
+__global__ void k_scale_out(const double* __restrict__ x, int64_t n, const double* __restrict__ inv,
                             float* __restrict__ y)
 {
-    const double inv = ss ? 1.0 / sqrt(*ss) : 1.0;
+    const double v = inv ? *inv : 1.0;
     for (int64_t i = blockIdx.x * (int64_t)kThreads + threadIdx.x; i < n; i += (int64_t)gridDim.x * kThreads)
-        y[i] = (float)(x[i] * inv);
+        y[i] = (float)(x[i] * v);
 }
 
 // mean of y2 (F floats; y2 == nullptr: 0) -> *c (one CTA)
@@ -270,6 +325,7 @@ int background(sid_ctx* c, const T* Y, int64_t P, int64_t F, int maxIter, float*
     double* td = c->bg[1].as<double>();
     double* ss = td + F;       // sum of squares of t or s
     double* cm = td + F + 1;   // mean of t
+    double* inv = td + F + 2;  // 1/sqrt(*ss)
     double* part = td + F + 8;
     unsigned int* done = c->bg[4].as<unsigned int>();
     SID_CUDA_TRY(cudaMemsetAsync(done, 0, sizeof(unsigned int), st));
@@ -291,9 +347,9 @@ int background(sid_ctx* c, const T* Y, int64_t P, int64_t F, int maxIter, float*
             k_col_pass<T><<<gcol, kThreads, 0, st>>>(Y, P, F, bg_s, s4, ps, 1.f, td);
         }
         SID_CHECK_LAUNCH();
-        k_sumsq<<<1, kThreads, 0, st>>>(td, F, ss);
+        k_sumsq<<<1, kThreads, 0, st>>>(td, F, ss, inv);
         SID_CHECK_LAUNCH();
-        k_scale_out<<<grid_for(F), kThreads, 0, st>>>(td, F, ss, bg_t);
+        k_scale_out<<<grid_for(F), kThreads, 0, st>>>(td, F, inv, bg_t);
         SID_CHECK_LAUNCH();
         // bg_spatial = Y * bg_temporal' (:35), normalised except after the last iteration (:36-38)
         const bool last = it == maxIter;
@@ -302,10 +358,10 @@ int background(sid_ctx* c, const T* Y, int64_t P, int64_t F, int maxIter, float*
                                                  stats && last ? 1 : 0);
         SID_CHECK_LAUNCH();
         if (!last) {
-            k_sumsq_big<<<gred, kThreads, 0, st>>>(sd, P, part, done, ss);
+            k_sumsq_big<<<gred, kThreads, 0, st>>>(sd, P, part, done, ss, inv);
             SID_CHECK_LAUNCH();
         }
-        k_scale_out<<<grid_for(P), kThreads, 0, st>>>(sd, P, last ? nullptr : ss, bg_s);
+        k_scale_out<<<grid_for(P), kThreads, 0, st>>>(sd, P, last ? nullptr : inv, bg_s);
         SID_CHECK_LAUNCH();
     }
     if (stats) {

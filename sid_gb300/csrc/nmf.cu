@@ -34,6 +34,50 @@ __device__ __forceinline__ double warp_sum(double v)
 }
 
 __device__ __forceinline__ float finite_or_zero(double a) { return isfinite(a) ? (float)a : 0.f; }
+__device__ __forceinline__ float finite_or_zero_f(float a) { return isfinite(a) ? a : 0.f; }
+
+// FP32 pairs hi + lo for the pixel-long loops of S_update (P x R elements):
+// two-sum additions and fmaf two-products give FP64-grade sums on the FP32
+// pipes.  GB300's FP64 rate is about 1/64 of its FP32 rate, so FP64 arithmetic
+// per element (and a 64-bit integer division per element to find its column)
+// held these kernels far below the HBM rate.
+__device__ __forceinline__ float2 ff_add(float2 a, float2 b)
+{
+    const float s = a.x + b.x;
+    const float bb = s - a.x;
+    const float e = (a.x - (s - bb)) + (b.x - bb);
+    const float l = (a.y + b.y) + e;
+    const float hi = s + l;
+    return make_float2(hi, l - (hi - s));
+}
+__device__ __forceinline__ float2 two_prod(float a, float b)
+{
+    const float p = a * b;
+    return make_float2(p, fmaf(a, b, -p));
+}
+__device__ __forceinline__ float2 ff_from(double v)
+{
+    const float h = (float)v;
+    return make_float2(h, (float)(v - (double)h));
+}
+__device__ __forceinline__ float2 warp_sum_ff(float2 v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        v = ff_add(v, make_float2(__shfl_xor_sync(0xffffffffu, v.x, o), __shfl_xor_sync(0xffffffffu, v.y, o)));
+    return v;
+}
+// block sum of pairs (blockDim.x a multiple of 32, <= 1024), valid in thread 0
+__device__ __forceinline__ float2 block_sum_ff(float2 v)
+{
+    __shared__ float2 sh[32];
+    v = warp_sum_ff(v);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x == 0)
+        for (int i = 1; i < (int)(blockDim.x >> 5); ++i) v = ff_add(v, sh[i]);
+    return v;
+}
 
 __global__ void k_nan_zero(float* __restrict__ x, int64_t n)
 {
@@ -104,31 +148,37 @@ __global__ void k_row_std(const float* __restrict__ T, int R, int64_t F, double*
     if (lane == 0) sd[warp] = F > 1 ? sqrt(b / (double)(F - 1)) : 0.0;
 }
 
-// T(r, :) /= platz(r), S(:, r) *= platz(r) with platz = ||T(r, :)||  (T_update.m:14-19)
-__global__ void k_renorm_rows(float* __restrict__ T, int R, int64_t F, float* __restrict__ S, int64_t P,
-                              const double* __restrict__ sq)
+// platz = sqrt of the squared row norms, FP32 (once per row, not per element)
+__global__ void k_sqrt_f(const double* __restrict__ sq, int R, float* __restrict__ pl)
 {
-    const int64_t nT = (int64_t)R * F, nS = P * R;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nT + nS;
-         i += (int64_t)gridDim.x * blockDim.x) {
-        if (i < nT) {
-            const float pl = (float)sqrt(sq[i % R]);
-            T[i] = T[i] / pl;
-        } else {
-            const int64_t j = i - nT;
-            const float pl = (float)sqrt(sq[j / P]);
-            S[j] = S[j] * pl;
-        }
-    }
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < R; r += gridDim.x * blockDim.x) pl[r] = (float)sqrt(sq[r]);
 }
 
-// Sm(p, r) = active(p) ? S(p, r) : 0  (S(opts.active, :), T_update.m:24-25)
-__global__ void k_mask_rows(const float* __restrict__ S, const uint8_t* __restrict__ active, int64_t P, int64_t R,
+// T(r, :) /= platz(r)  (T_update.m:14-19)
+__global__ void k_renorm_rows_t(float* __restrict__ T, int R, int64_t F, const float* __restrict__ pl)
+{
+    const int64_t nT = (int64_t)R * F;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nT; i += (int64_t)gridDim.x * blockDim.x)
+        T[i] = T[i] / pl[i % R];
+}
+
+// S(:, r) *= platz(r)  (T_update.m:14-19); grid.y = component r
+__global__ void k_renorm_cols_s(float* __restrict__ S, int64_t P, const float* __restrict__ pl)
+{
+    const float m = pl[blockIdx.y];
+    float* col = S + P * blockIdx.y;
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < P; p += (int64_t)gridDim.x * blockDim.x)
+        col[p] = col[p] * m;
+}
+
+// Sm(p, r) = active(p) ? S(p, r) : 0  (S(opts.active, :), T_update.m:24-25);
+// grid.y = component r
+__global__ void k_mask_rows(const float* __restrict__ S, const uint8_t* __restrict__ active, int64_t P,
                             float* __restrict__ Sm)
 {
-    const int64_t n = P * R;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        Sm[i] = active[i % P] ? S[i] : 0.f;
+    const int64_t o = P * blockIdx.y;
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < P; p += (int64_t)gridDim.x * blockDim.x)
+        Sm[o + p] = active[p] ? S[o + p] : 0.f;
 }
 
 // out(r, f) = v(r, f) - rowsum(r) / F: the use_std centring inside Q(x)
@@ -320,15 +370,29 @@ __global__ void k_qt_adjust(float* __restrict__ QT, int R, const double* __restr
     }
 }
 
-// df_S = -q_S [+ opts.Y .* ts' / F] + S*Q_T + lamb_spat  (S_update.m:8-34), in place of SQ
-__global__ void k_s_grad(const float* __restrict__ qS, float* __restrict__ SQ, int64_t P, int R,
+// df_S = -q_S [+ opts.Y .* ts' / F] + S*Q_T + lamb_spat  (S_update.m:8-34), in place
+// of SQ; grid.y = component r, the pixels of its column grid-strided in x
+__global__ void k_s_grad(const float* __restrict__ qS, float* __restrict__ SQ, int64_t P,
                          const float* __restrict__ ymean, const double* __restrict__ ts, double invF, double lamb_spat)
 {
-    const int64_t n = P * R;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        double q = qS[i];
-        if (ymean) q -= (double)ymean[i % P] * ts[i / P] * invF;
-        SQ[i] = (float)(-q + (double)SQ[i] + lamb_spat);
+    const int r = blockIdx.y;
+    __shared__ float2 tsf, lam;
+    if (threadIdx.x == 0) {
+        tsf = ymean ? ff_from(ts[r] * invF) : make_float2(0.f, 0.f);
+        lam = ff_from(lamb_spat);
+    }
+    __syncthreads();
+    const float* q = qS + P * r;
+    float* sq = SQ + P * r;
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < P; p += (int64_t)gridDim.x * blockDim.x) {
+        float2 a = ff_add(make_float2(sq[p], 0.f), make_float2(-q[p], 0.f));
+        if (ymean) {
+            const float y = ymean[p];
+            const float2 t = two_prod(y, tsf.x);
+            a = ff_add(a, make_float2(t.x, fmaf(y, tsf.y, t.y)));
+        }
+        a = ff_add(a, lam);
+        sq[p] = a.x + a.y;
     }
 }
 
@@ -336,7 +400,7 @@ __global__ void k_s_grad(const float* __restrict__ qS, float* __restrict__ SQ, i
 // orth:  v = df [+ l2o * M2]; z = sum_r S.*v; v = v - S.*z; v = passive(S, v) .* v
 // else:  v = passive(S, df) .* df
 __global__ void k_s_dir(const float* __restrict__ S, const float* __restrict__ df, const float* __restrict__ M2,
-                        double l2o, int orth, int64_t P, int R, float* __restrict__ v)
+                        float l2o, int orth, int64_t P, int R, float* __restrict__ v)
 {
     for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < P; p += (int64_t)gridDim.x * blockDim.x) {
         if (!orth) {
@@ -347,17 +411,18 @@ __global__ void k_s_dir(const float* __restrict__ S, const float* __restrict__ d
             }
             continue;
         }
-        double z = 0.0;
+        float2 z = make_float2(0.f, 0.f);
         for (int r = 0; r < R; ++r) {
             const int64_t i = p + P * r;
-            const double vi = (double)df[i] + (M2 ? l2o * (double)M2[i] : 0.0);
-            z += (double)S[i] * (double)(float)vi;
+            const float vi = M2 ? fmaf(l2o, M2[i], df[i]) : df[i];
+            z = ff_add(z, two_prod(S[i], vi));
         }
         for (int r = 0; r < R; ++r) {
             const int64_t i = p + P * r;
-            const float vi = (float)((double)df[i] + (M2 ? l2o * (double)M2[i] : 0.0));
-            const float w = (float)((double)vi - (double)S[i] * z);
-            v[i] = (S[i] > 0.f || w < 0.f) ? w : 0.f;
+            const float vi = M2 ? fmaf(l2o, M2[i], df[i]) : df[i];
+            const float si = S[i];
+            const float w = fmaf(-si, z.y, fmaf(-si, z.x, vi));
+            v[i] = (si > 0.f || w < 0.f) ? w : 0.f;
         }
     }
 }
@@ -367,78 +432,81 @@ __global__ void k_s_dir(const float* __restrict__ S, const float* __restrict__ d
 __global__ void k_s_sums(const float* __restrict__ v, const float* __restrict__ df, const float* __restrict__ vQ,
                          int64_t P, int R, int pointwise, float* __restrict__ alpha, double* __restrict__ part)
 {
-    double bn = 0.0, bd = 0.0;
+    float2 bn = make_float2(0.f, 0.f), bd = bn;
     for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < P; p += (int64_t)gridDim.x * blockDim.x) {
-        double x = 0.0, y = 0.0;
+        float2 x = make_float2(0.f, 0.f), y = x;
         for (int r = 0; r < R; ++r) {
             const int64_t i = p + P * r;
-            x += (double)v[i] * (double)df[i];
-            y += (double)v[i] * (double)vQ[i];
+            const float vv = v[i];
+            x = ff_add(x, two_prod(vv, df[i]));
+            y = ff_add(y, two_prod(vv, vQ[i]));
         }
-        if (pointwise) alpha[p] = finite_or_zero(x / y);
-        bn += x;
-        bd += y;
+        if (pointwise) alpha[p] = finite_or_zero_f(x.x / y.x);
+        bn = ff_add(bn, x);
+        bd = ff_add(bd, y);
     }
     if (pointwise) return;
-    __shared__ double sn[32], sd[32];
-    bn = warp_sum(bn);
-    bd = warp_sum(bd);
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    if (lane == 0) {
-        sn[w] = bn;
-        sd[w] = bd;
-    }
+    bn = block_sum_ff(bn);
     __syncthreads();
+    bd = block_sum_ff(bd);
     if (threadIdx.x == 0) {
-        double a = 0.0, b = 0.0;
-        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) {
-            a += sn[i];
-            b += sd[i];
-        }
-        part[blockIdx.x] = a;
-        part[kRedBlocks + blockIdx.x] = b;
+        part[blockIdx.x] = (double)bn.x + (double)bn.y;
+        part[kRedBlocks + blockIdx.x] = (double)bd.x + (double)bd.y;
     }
 }
 
-// Column norms of S (P x R), one block per column
-__global__ void k_col_norm2(const float* __restrict__ S, int64_t P, double* __restrict__ out)
+// Column norms of S (P x R), one block per column: squared norm (FP64) and
+// the norm itself (FP32) for the rescaling
+__global__ void k_col_norm2(const float* __restrict__ S, int64_t P, double* __restrict__ out, float* __restrict__ pl)
 {
     const float* col = S + P * blockIdx.x;
-    double a = 0.0;
-    for (int64_t p = threadIdx.x; p < P; p += blockDim.x) {
-        const double v = col[p];
-        a += v * v;
-    }
-    __shared__ double sh[32];
-    a = warp_sum(a);
-    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = a;
-    __syncthreads();
+    float2 a = make_float2(0.f, 0.f);
+    for (int64_t p = threadIdx.x; p < P; p += blockDim.x) a = ff_add(a, two_prod(col[p], col[p]));
+    a = block_sum_ff(a);
     if (threadIdx.x == 0) {
-        double s = 0.0;
-        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) s += sh[i];
+        const double s = (double)a.x + (double)a.y;
         out[blockIdx.x] = s;
+        pl[blockIdx.x] = (float)sqrt(s);
     }
 }
 
-// T(r, :) *= platz(r), S(:, r) /= platz(r)   (S_update.m:75-79)
-__global__ void k_unit_cols(float* __restrict__ S, int64_t P, int R, float* __restrict__ T, int64_t F,
-                            const double* __restrict__ sq)
+// S(:, r) /= platz(r)   (S_update.m:75-79); grid.y = component r
+__global__ void k_unit_cols_s(float* __restrict__ S, int64_t P, const float* __restrict__ pl)
 {
-    const int64_t nS = P * R, nT = (int64_t)R * F;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nS + nT;
-         i += (int64_t)gridDim.x * blockDim.x) {
-        if (i < nS) {
-            const float pl = (float)sqrt(sq[i / P]);
-            S[i] = S[i] / pl;
-        } else {
-            const int64_t j = i - nS;
-            const float pl = (float)sqrt(sq[j % R]);
-            T[j] = pl * T[j];
-        }
+    const float d = pl[blockIdx.y];
+    float* col = S + P * blockIdx.y;
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < P; p += (int64_t)gridDim.x * blockDim.x)
+        col[p] = col[p] / d;
+}
+
+// T(r, :) *= platz(r)   (S_update.m:75-79)
+__global__ void k_unit_rows_t(float* __restrict__ T, int R, int64_t F, const float* __restrict__ pl)
+{
+    const int64_t n = (int64_t)R * F;
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x)
+        T[j] = pl[j % R] * T[j];
+}
+
+// x(:, r) = max(x(:, r) - alpha .* d(:, r), 0) for a P x R matrix with alpha
+// per pixel (per_row != 0) or one scalar; grid.y = column r
+__global__ void k_pg_step_cols(float* __restrict__ x, const float* __restrict__ d, int64_t P,
+                               const float* __restrict__ alpha, int per_row)
+{
+    const int64_t o = P * blockIdx.y;
+    const float a0 = alpha[0];
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < P; p += (int64_t)gridDim.x * blockDim.x) {
+        const float a = per_row ? alpha[p] : a0;
+        const float v = x[o + p] - d[o + p] * a;
+        x[o + p] = v < 0.f ? 0.f : v;
     }
 }
 
 inline unsigned grid_for(int64_t n, int per = 256) { return (unsigned)std::max<int64_t>(1, std::min<int64_t>(cdiv(n, per), 152 * 16)); }
+// P x R column kernels: grid.y = column, about 152 * 16 CTAs in all
+inline dim3 grid_cols(int64_t P, int64_t R)
+{
+    return dim3((unsigned)std::max<int64_t>(1, std::min<int64_t>(cdiv(P, 256), cdiv(152 * 16, R))), (unsigned)R);
+}
 
 // C (m x n) = A' B, FP32 SIMT (through the contraction entry, which owns the workspace)
 inline int tn32(sid_ctx* c, const float* A, const float* B, int64_t m, int64_t n, int64_t k, int64_t lda, int64_t ldb,
@@ -507,15 +575,20 @@ extern "C" int sid_t_update(sid_ctx* c, const void* Y, int ydtype, float* T, flo
     SID_CHECK_LAUNCH();
     // unit-norm rows of T, S rescaled (T_update.m:14-19)
     if (o->lamb_corr > 0) {
+        SID_REQUIRE(R <= 65535, "T_update: at most 65535 components");
+        float* pl = tmp;  // R floats, free until the use_std products below
         k_row_moments<<<(unsigned)cdiv(R * 32, 256), 256, 0, st>>>(T, (int)R, F, s1, s2);
-        k_renorm_rows<<<grid_for(RF + P * R), 256, 0, st>>>(T, (int)R, F, S, P, s2);
+        k_sqrt_f<<<(unsigned)cdiv(R, 256), 256, 0, st>>>(s2, (int)R, pl);
+        k_renorm_rows_t<<<grid_for(RF), 256, 0, st>>>(T, (int)R, F, pl);
+        k_renorm_cols_s<<<grid_cols(P, R), 256, 0, st>>>(S, P, pl);
         SID_CHECK_LAUNCH();
     }
     // Q_S = S_a' S_a, q_T = S_a' Y_a (T_update.m:24-25)
     const float* Sa = S;
     if (active) {
         SID_TRY(b[4].alloc((size_t)(P * R) * 4));
-        k_mask_rows<<<grid_for(P * R), 256, 0, st>>>(S, active, P, R, b[4].as<float>());
+        SID_REQUIRE(R <= 65535, "T_update: at most 65535 components");
+        k_mask_rows<<<grid_cols(P, R), 256, 0, st>>>(S, active, P, b[4].as<float>());
         SID_CHECK_LAUNCH();
         Sa = b[4].as<float>();
     }
@@ -608,7 +681,8 @@ extern "C" int sid_s_update(sid_ctx* c, const void* Y, int ydtype, float* S, flo
     DBuf* b = c->mf;
     SID_TRY(b[0].alloc((size_t)(R * R) * 4 * 4));  // Q_T, Q_T', S'S, M1'
     SID_TRY(b[1].alloc((size_t)RF * 4));           // T'
-    SID_TRY(b[2].alloc((size_t)(2 * R + 2 * kRedBlocks + 8) * 8));
+    SID_REQUIRE(R <= 65535, "S_update: at most 65535 components");
+    SID_TRY(b[2].alloc((size_t)(3 * R + 2 * kRedBlocks + 8) * 8));
     SID_TRY(b[3].alloc((size_t)(P + 1) * 4));      // alpha
     SID_TRY(b[4].alloc((size_t)PR * 4 * 3));       // q_S / vQ, df, v
     float* QT = b[0].as<float>();
@@ -619,6 +693,7 @@ extern "C" int sid_s_update(sid_ctx* c, const void* Y, int ydtype, float* S, flo
     double* ts = b[2].as<double>();
     double* sq = ts + R;
     double* part = sq + R;
+    float* pl = reinterpret_cast<float*>(part + 2 * kRedBlocks + 8);  // column norms
     float* alpha = b[3].as<float>();
     float* qS = b[4].as<float>();
     float* df = qS + PR;
@@ -645,7 +720,7 @@ extern "C" int sid_s_update(sid_ctx* c, const void* Y, int ydtype, float* S, flo
     SID_TRY(transpose(QT, R, R, QTt, st));
     // df_S = -q_S + S*Q_T + lamb_spat  (:32)
     SID_TRY(sgemm_nt(S, 0, QTt, P, R, R, P, R, df, P, st));
-    k_s_grad<<<grid_for(PR), 256, 0, st>>>(qS, df, P, (int)R, o->use_std ? ymean : nullptr, ts, invF, o->lamb_spat);
+    k_s_grad<<<grid_cols(P, R), 256, 0, st>>>(qS, df, P, o->use_std ? ymean : nullptr, ts, invF, o->lamb_spat);
     SID_CHECK_LAUNCH();
     // direction (:38-53); M2 = S*(hilf*(S'*S)) for the L2 orthogonality term, in the q_S buffer
     const float* M2 = nullptr;
@@ -660,7 +735,7 @@ extern "C" int sid_s_update(sid_ctx* c, const void* Y, int ydtype, float* S, flo
         SID_TRY(sgemm_nt(S, 0, M1t, P, R, R, P, R, qS, P, st));
         M2 = qS;
     }
-    k_s_dir<<<grid_for(P), 256, 0, st>>>(S, df, M2, o->lamb_orth_L2, orth ? 1 : 0, P, (int)R, v);
+    k_s_dir<<<grid_for(P), 256, 0, st>>>(S, df, M2, (float)o->lamb_orth_L2, orth ? 1 : 0, P, (int)R, v);
     SID_CHECK_LAUNCH();
     // exact line search (:57-68): vQ = v*Q_T into the q_S buffer
     SID_TRY(sgemm_nt(v, 0, QTt, P, R, R, P, R, qS, P, st));
@@ -671,12 +746,13 @@ extern "C" int sid_s_update(sid_ctx* c, const void* Y, int ydtype, float* S, flo
         k_alpha<<<1, 256, 0, st>>>(part, part + kRedBlocks, kRedBlocks, 0, o->lamb_orth_L2 != 0.0 ? 1e-6 : 0.0,
                                    alpha);
     }
-    k_pg_step<<<grid_for(PR), 256, 0, st>>>(S, v, P, R, alpha, o->pointwise ? 2 : 0);
+    k_pg_step_cols<<<grid_cols(P, R), 256, 0, st>>>(S, v, P, alpha, o->pointwise ? 1 : 0);
     SID_CHECK_LAUNCH();
     // unit-norm columns of S, T rescaled (:75-79)
     if (orth) {
-        k_col_norm2<<<(unsigned)R, 256, 0, st>>>(S, P, sq);
-        k_unit_cols<<<grid_for(PR + RF), 256, 0, st>>>(S, P, (int)R, T, F, sq);
+        k_col_norm2<<<(unsigned)R, 256, 0, st>>>(S, P, sq, pl);
+        k_unit_cols_s<<<grid_cols(P, R), 256, 0, st>>>(S, P, pl);
+        k_unit_rows_t<<<grid_for(RF), 256, 0, st>>>(T, (int)R, F, pl);
         SID_CHECK_LAUNCH();
     }
     return SID_OK;

@@ -77,23 +77,47 @@ template <typename T> __device__ __forceinline__ float px(const T* f, int64_t i)
 template <> __device__ __forceinline__ float px<float>(const float* f, int64_t i) { return f[i]; }
 template <> __device__ __forceinline__ float px<uint16_t>(const uint16_t* f, int64_t i) { return (float)f[i]; }
 
+// interp2's bilinear rule along one axis, evaluated on the host in FP64 for
+// each output column (or row): the 1-based base index (the last interval
+// serves the far edge) and the FP32 fraction, or index -1 outside [1, size].
+// The kernel then needs no FP64 arithmetic per output pixel (GB300's FP64 rate
+// is about 1/64 of its FP32 rate).
+struct AxisTap {
+    int32_t i;
+    float f;
+};
+
+std::vector<AxisTap> axis_taps(const std::vector<double>& q, int64_t size)
+{
+    std::vector<AxisTap> t(q.size());
+    for (size_t k = 0; k < q.size(); ++k) {
+        const double v = q[k];
+        if (!(v >= 1.0 && v <= (double)size)) {
+            t[k] = {-1, 0.f};
+            continue;
+        }
+        int64_t iv = (int64_t)std::floor(v);
+        if (iv == size) --iv;
+        t[k] = {(int32_t)iv, (float)(v - (double)iv)};
+    }
+    return t;
+}
+
 // out[(r + R c) + R C n] = interp2 at (xq[c], yq[r]) of frame n (times the mask).
 template <typename T>
 __global__ void k_rect(const T* __restrict__ in, const float* __restrict__ mask, int64_t rows, int64_t cols,
-                       int64_t nframes, const double* __restrict__ xq, const double* __restrict__ yq, int64_t R,
+                       int64_t nframes, const AxisTap* __restrict__ tx, const AxisTap* __restrict__ ty, int64_t R,
                        int64_t C, float* __restrict__ out)
 {
     const int64_t plane = R * C, total = plane * nframes;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
         const int64_t n = i / plane, rc = i - n * plane;
         const int64_t c = rc / R, r = rc - c * R;
-        const double x = xq[c], y = yq[r];
+        const AxisTap ax = tx[c], ay = ty[r];
         float v = __int_as_float(0x7fc00000);  // NaN outside the grid
-        if (x >= 1.0 && x <= (double)cols && y >= 1.0 && y <= (double)rows) {
-            int64_t ix = (int64_t)floor(x), iy = (int64_t)floor(y);
-            if (ix == cols) --ix;
-            if (iy == rows) --iy;
-            const float fx = (float)(x - (double)ix), fy = (float)(y - (double)iy);
+        if (ax.i >= 0 && ay.i >= 0) {
+            const int64_t ix = ax.i, iy = ay.i;
+            const float fx = ax.f, fy = ay.f;
             const T* f = in + n * rows * cols;
             const int64_t i00 = (iy - 1) + rows * (ix - 1);
             auto at = [&](int64_t k) { return mask ? px<T>(f, k) * mask[k] : px<T>(f, k); };
@@ -133,10 +157,11 @@ extern "C" int sid_image_rect(sid_ctx* c, const void* frames, int dtype, int64_t
     SID_TRY(rect_geometry(rows, cols, xCenter, yCenter, dx, M, crop, cuts, &g));
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const int64_t R = (int64_t)g.yq.size(), C = (int64_t)g.xq.size();
-    SID_TRY(c->mf[6].alloc((size_t)(R + C) * sizeof(double)));
-    double* dq = c->mf[6].as<double>();
-    SID_CUDA_TRY(cudaMemcpyAsync(dq, g.xq.data(), (size_t)C * 8, cudaMemcpyHostToDevice, st));
-    SID_CUDA_TRY(cudaMemcpyAsync(dq + C, g.yq.data(), (size_t)R * 8, cudaMemcpyHostToDevice, st));
+    const std::vector<AxisTap> tx = axis_taps(g.xq, cols), ty = axis_taps(g.yq, rows);
+    SID_TRY(c->mf[6].alloc((size_t)(R + C) * sizeof(AxisTap)));
+    AxisTap* dq = c->mf[6].as<AxisTap>();
+    SID_CUDA_TRY(cudaMemcpyAsync(dq, tx.data(), (size_t)C * sizeof(AxisTap), cudaMemcpyHostToDevice, st));
+    SID_CUDA_TRY(cudaMemcpyAsync(dq + C, ty.data(), (size_t)R * sizeof(AxisTap), cudaMemcpyHostToDevice, st));
     const unsigned grid = (unsigned)std::min<int64_t>(cdiv(R * C * nframes, 256), 152 * 32);
     if (dtype == SID_DTYPE_U16)
         k_rect<uint16_t><<<grid, 256, 0, st>>>(static_cast<const uint16_t*>(frames), mask, rows, cols, nframes, dq,
