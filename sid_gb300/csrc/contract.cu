@@ -135,6 +135,7 @@ extern "C" int sid_ctx_destroy(sid_ctx* c)
     for (DBuf& x : c->nn) x.release();
     for (DBuf& x : c->mf) x.release();
     for (DBuf& x : c->bg) x.release();
+    for (DBuf& x : c->pix) x.release();
     delete c;
     return SID_OK;
 }

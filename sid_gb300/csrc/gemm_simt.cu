@@ -223,6 +223,66 @@ __global__ void k_copy16_blk(const uint16_t* __restrict__ src, int64_t k, int64_
     }
 }
 
+// The same K-blocked layouts from a row-contiguous source: element (kk, r) at
+// src[r + ldr*kk] (a rows x k column-major matrix, e.g. a pixel-major P x R
+// factor).  One CTA per 64 x 64 tile: coalesced reads along r into shared
+// memory, then 128-byte block rows written along kk.  MODE 0: FP32 source,
+// BF16 hi/lo; MODE 1: FP32 source, FP16 hi/lo of src*scale; MODE 2: 16-bit
+// source copied (hi only).
+template <int MODE>
+__global__ void __launch_bounds__(256) k_blk16_t(const void* __restrict__ src_v, int64_t rows, int64_t k, int64_t ldr,
+                                                 uint16_t* __restrict__ hi, uint16_t* __restrict__ lo, float scale)
+{
+    __shared__ float tile[64][65];
+    __shared__ uint16_t tile16[64][66];
+    const int64_t nrt = (rows + 63) / 64, nkt = (k + 63) / 64;
+    for (int64_t t = blockIdx.x; t < nrt * nkt; t += gridDim.x) {
+        const int64_t r0 = (t % nrt) * 64, kb = t / nrt, k0 = kb * 64;
+        __syncthreads();
+        for (int e = threadIdx.x; e < 64 * 64; e += 256) {
+            const int kk = e >> 6, r = e & 63;
+            const bool in = r0 + r < rows && k0 + kk < k;
+            if (MODE == 2) {
+                const uint16_t* src = static_cast<const uint16_t*>(src_v);
+                tile16[kk][r] = in ? src[(r0 + r) + ldr * (k0 + kk)] : (uint16_t)0;
+            } else {
+                const float* src = static_cast<const float*>(src_v);
+                tile[kk][r] = in ? src[(r0 + r) + ldr * (k0 + kk)] : 0.f;
+            }
+        }
+        __syncthreads();
+        // 64 rows x 16 groups of 4 consecutive kk
+        for (int e = threadIdx.x; e < 64 * 16; e += 256) {
+            const int r = e >> 4, g = e & 15;
+            if (r0 + r >= rows) continue;
+            uint16_t h[4], l[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int kk = g * 4 + q;
+                if (MODE == 2) {
+                    h[q] = tile16[kk][r];
+                    l[q] = 0;
+                } else if (MODE == 0) {
+                    const float x = tile[kk][r];
+                    const __nv_bfloat16 bh = __float2bfloat16_rn(x);
+                    h[q] = __bfloat16_as_ushort(bh);
+                    l[q] = __bfloat16_as_ushort(__float2bfloat16_rn(x - __bfloat162float(bh)));
+                } else {
+                    const float x = tile[kk][r] * scale;
+                    const __half fh = __float2half_rn(x);
+                    h[q] = __half_as_ushort(fh);
+                    l[q] = __half_as_ushort(__float2half_rn(x - __half2float(fh)));
+                }
+            }
+            const int64_t o = (kb * rows + r0 + r) * 64 + g * 4;
+            *reinterpret_cast<uint2*>(hi + o) = make_uint2(h[0] | ((uint32_t)h[1] << 16), h[2] | ((uint32_t)h[3] << 16));
+            if (lo && MODE != 2)
+                *reinterpret_cast<uint2*>(lo + o) =
+                    make_uint2(l[0] | ((uint32_t)l[1] << 16), l[2] | ((uint32_t)l[3] << 16));
+        }
+    }
+}
+
 // max |x| over n floats -> out (float bits, atomicMax; out must start at 0)
 __global__ void k_absmax(const float* __restrict__ x, int64_t n, unsigned int* __restrict__ out)
 {
@@ -255,6 +315,29 @@ int copy16_blk(const uint16_t* src, int64_t k, int64_t rows, int64_t lds, uint16
     const int64_t total = cdiv(k, 64) * rows * 8;
     const unsigned grid = (unsigned)std::min<int64_t>(cdiv(total, 256), 152 * 32);
     k_copy16_blk<<<grid, 256, 0, st>>>(src, k, rows, lds, dst, vec8);
+    SID_CHECK_LAUNCH();
+    return SID_OK;
+}
+
+// K-blocked 16-bit operand (reduction index k) of a rows x k matrix stored
+// row-contiguous (src[r + ldr*kk]): FP32 split into BF16 hi/lo (bf16) or FP16
+// hi/lo of src*scale, or a 16-bit source copied (src16).
+int split16_t(const float* src, int64_t rows, int64_t k, int64_t ldr, uint16_t* hi, uint16_t* lo, bool bf16,
+              float scale, cudaStream_t st)
+{
+    const int64_t tiles = cdiv(rows, 64) * cdiv(k, 64);
+    const unsigned grid = (unsigned)std::min<int64_t>(tiles, 152 * 8);
+    if (bf16) k_blk16_t<0><<<grid, 256, 0, st>>>(src, rows, k, ldr, hi, lo, 1.f);
+    else k_blk16_t<1><<<grid, 256, 0, st>>>(src, rows, k, ldr, hi, lo, scale);
+    SID_CHECK_LAUNCH();
+    return SID_OK;
+}
+
+int copy16_t(const uint16_t* src, int64_t rows, int64_t k, int64_t ldr, uint16_t* dst, cudaStream_t st)
+{
+    const int64_t tiles = cdiv(rows, 64) * cdiv(k, 64);
+    const unsigned grid = (unsigned)std::min<int64_t>(tiles, 152 * 8);
+    k_blk16_t<2><<<grid, 256, 0, st>>>(src, rows, k, ldr, dst, nullptr, 1.f);
     SID_CHECK_LAUNCH();
     return SID_OK;
 }

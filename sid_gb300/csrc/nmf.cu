@@ -21,6 +21,17 @@ int contract(sid_ctx* c, const float* A, const void* B, bool b_f16, int64_t m, i
              int64_t ldb, float* C, int64_t ldc, float alpha, float beta, int prec, cudaStream_t st);
 int sgemm_nt(const void* A, int a_f16, const float* B, int64_t m, int64_t n, int64_t k, int64_t lda, int64_t ldb,
              float* C, int64_t ldc, cudaStream_t st);
+int gemm_tn(const void* const* A, const void* const* B, int npass, int64_t m, int64_t n, int64_t k, bool bf16,
+            float* C, int64_t ldc, float alpha, float beta, int bn, int splitk, float* ws, int64_t ws_elems, int* err,
+            cudaStream_t st);
+void gemm_autotune(int m, int n, int nkb, int* bn, int* splitk);
+int split16(const float* src, int64_t k, int64_t rows, int64_t lds, uint16_t* hi, uint16_t* lo, bool bf16,
+            float scale, cudaStream_t st);
+int split16_t(const float* src, int64_t rows, int64_t k, int64_t ldr, uint16_t* hi, uint16_t* lo, bool bf16,
+              float scale, cudaStream_t st);
+int copy16_t(const uint16_t* src, int64_t rows, int64_t k, int64_t ldr, uint16_t* dst, cudaStream_t st);
+int64_t blk16_elems(int64_t k, int64_t rows);
+int absmax(const float* x, int64_t n, unsigned int* out, cudaStream_t st);
 
 namespace {
 
@@ -664,6 +675,102 @@ extern "C" int sid_t_update(sid_ctx* c, const void* Y, int ydtype, float* T, flo
     return SID_OK;
 }
 
+namespace sid {
+namespace {
+
+// Products of a pixel-major P x k factor X (pixels contiguous: the movie, S,
+// the step direction) with a small k x n matrix W, on the tensor cores:
+// C (P x n) = X W.  X is brought once into the K-blocked 16-bit layout of the
+// tcgen05 GEMM by a transposing tile kernel.  Split precision: an FP16 movie
+// as it is, FP32 factors as FP16 hi/lo of X s (22 significant bits; a
+// power-of-two s brings max |X| to 2^14), W likewise, and the three products
+// hi*hi + hi*lo + lo*hi.  (BF16 hi/lo keeps 16 bits, which the cancellation in
+// S_update's use_std gradient amplifies past FP32-level agreement.)  BF16
+// precision: one BF16 pass.
+struct PixOperand {
+    const void* hi;
+    const void* lo;
+    bool f16;     // FP16 operands (else BF16)
+    float scale;  // X was multiplied by this power of two
+};
+
+// largest power of two s with max |x| s <= 2^14 (1 for an all-zero x)
+int pow2_scale(sid_ctx* c, const float* x, int64_t n, float* scale, cudaStream_t st)
+{
+    SID_TRY(c->scal.alloc(64));
+    SID_TRY(absmax(x, n, c->scal.as<unsigned int>(), st));
+    unsigned int bits = 0;
+    SID_CUDA_TRY(cudaMemcpyAsync(&bits, c->scal.p, sizeof(bits), cudaMemcpyDeviceToHost, st));
+    SID_CUDA_TRY(cudaStreamSynchronize(st));
+    float mx;
+    std::memcpy(&mx, &bits, sizeof(mx));
+    *scale = (mx > 0.f) ? std::ldexp(1.0f, (int)std::floor(std::log2(16384.0 / (double)mx))) : 1.f;
+    return SID_OK;
+}
+
+int pix_operand(sid_ctx* c, int slot, const void* X, bool x_f16, int64_t P, int64_t k, int prec, PixOperand* op,
+                cudaStream_t st)
+{
+    const size_t bytes = (size_t)blk16_elems(k, P) * 2;
+    DBuf* b = c->pix + 2 * slot;
+    SID_TRY(b[0].alloc(bytes));
+    if (x_f16) {
+        SID_TRY(copy16_t(static_cast<const uint16_t*>(X), P, k, P, b[0].as<uint16_t>(), st));
+        *op = {b[0].p, nullptr, true, 1.f};
+        return SID_OK;
+    }
+    const float* xf = static_cast<const float*>(X);
+    if (prec != SID_PREC_SPLIT) {
+        SID_TRY(split16_t(xf, P, k, P, b[0].as<uint16_t>(), nullptr, true, 1.f, st));
+        *op = {b[0].p, nullptr, false, 1.f};
+        return SID_OK;
+    }
+    float sx = 1.f;
+    SID_TRY(pow2_scale(c, xf, P * k, &sx, st));
+    SID_TRY(b[1].alloc(bytes));
+    SID_TRY(split16_t(xf, P, k, P, b[0].as<uint16_t>(), b[1].as<uint16_t>(), false, sx, st));
+    *op = {b[0].p, b[1].p, true, sx};
+    return SID_OK;
+}
+
+// C (P x n, leading dimension P) = X (P x k) * W (k x n, W(kk, j) at W[kk + ldw*j])
+int gemm_pix(sid_ctx* c, const PixOperand& x, int64_t P, int64_t k, const float* W, int64_t n, int64_t ldw,
+             float* C, int prec, cudaStream_t st)
+{
+    const bool split = prec == SID_PREC_SPLIT;
+    const size_t wbytes = (size_t)blk16_elems(k, n) * 2;
+    SID_TRY(c->pix[4].alloc(wbytes));
+    if (split) SID_TRY(c->pix[5].alloc(wbytes));
+    uint16_t* wh = c->pix[4].as<uint16_t>();
+    uint16_t* wl = split ? c->pix[5].as<uint16_t>() : nullptr;
+    int bn = 0, sk = 0;
+    gemm_autotune((int)P, (int)n, (int)cdiv(k, 64), &bn, &sk);
+    float alpha = 1.f;
+    const void *As[3], *Bs[3];
+    int npass = 1;
+    As[0] = As[1] = x.hi;
+    As[2] = x.lo;
+    Bs[0] = Bs[2] = wh;
+    Bs[1] = wl;
+    if (x.f16) {
+        float sw = 1.f;
+        SID_TRY(pow2_scale(c, W, ldw * (n - 1) + k, &sw, st));
+        SID_TRY(split16(W, k, n, ldw, wh, wl, false, sw, st));
+        npass = !split ? 1 : (x.lo ? 3 : 2);
+        alpha = 1.f / (x.scale * sw);
+    } else {
+        SID_TRY(split16(W, k, n, ldw, wh, nullptr, true, 1.f, st));
+    }
+    // the scaled (alpha != 1) or split-K epilogue goes through a P x n workspace
+    const int64_t ws_elems = (sk > 1 || alpha != 1.f) ? (int64_t)std::max(sk, 1) * P * n : 1;
+    SID_TRY(c->ws.alloc((size_t)ws_elems * sizeof(float)));
+    return gemm_tn(As, Bs, npass, P, n, k, !x.f16, C, P, alpha, 0.f, bn, sk, c->ws.as<float>(),
+                   (int64_t)(c->ws.bytes / sizeof(float)), c->errflag.as<int>(), st);
+}
+
+}  // namespace
+}  // namespace sid
+
 extern "C" int sid_s_update(sid_ctx* c, const void* Y, int ydtype, float* S, float* T, int64_t P, int64_t R,
                             int64_t F, const float* ymean, const float* hilf, const sid_nmf_opts* o, int prec,
                             void* stream)
@@ -705,7 +812,17 @@ extern "C" int sid_s_update(sid_ctx* c, const void* Y, int ydtype, float* S, flo
     // Q_T = T T', q_S = Y T'  (S_update.m:8-9)
     SID_TRY(transpose(T, R, F, Tt, st));
     SID_TRY(tn32(c, Tt, Tt, R, R, F, F, F, QT, st));
-    SID_TRY(sgemm_nt(Y, ydtype == SID_DTYPE_F16 ? 1 : 0, T, P, R, F, P, R, qS, P, st));
+    // pixel-long-by-rank products on the tensor cores except at FP32 precision
+    const bool tc = prec != SID_PREC_FP32;
+    PixOperand Sx{};
+    if (tc) {
+        PixOperand Yx{};
+        SID_TRY(pix_operand(c, 0, Y, ydtype == SID_DTYPE_F16, P, F, prec, &Yx, st));
+        SID_TRY(gemm_pix(c, Yx, P, F, Tt, R, F, qS, prec, st));
+        SID_TRY(pix_operand(c, 1, S, false, P, R, prec, &Sx, st));
+    } else {
+        SID_TRY(sgemm_nt(Y, ydtype == SID_DTYPE_F16 ? 1 : 0, T, P, R, F, P, R, qS, P, st));
+    }
     // use_std (S_update.m:11-15), orthogonality L1 (:19-21)
     const double invF = 1.0 / (double)F;
     if (o->use_std) {
@@ -719,7 +836,8 @@ extern "C" int sid_s_update(sid_ctx* c, const void* Y, int ydtype, float* S, flo
     }
     SID_TRY(transpose(QT, R, R, QTt, st));
     // df_S = -q_S + S*Q_T + lamb_spat  (:32)
-    SID_TRY(sgemm_nt(S, 0, QTt, P, R, R, P, R, df, P, st));
+    if (tc) SID_TRY(gemm_pix(c, Sx, P, R, QT, R, R, df, prec, st));
+    else SID_TRY(sgemm_nt(S, 0, QTt, P, R, R, P, R, df, P, st));
     k_s_grad<<<grid_cols(P, R), 256, 0, st>>>(qS, df, P, o->use_std ? ymean : nullptr, ts, invF, o->lamb_spat);
     SID_CHECK_LAUNCH();
     // direction (:38-53); M2 = S*(hilf*(S'*S)) for the L2 orthogonality term, in the q_S buffer
@@ -732,13 +850,20 @@ extern "C" int sid_s_update(sid_ctx* c, const void* Y, int ydtype, float* S, flo
         SID_TRY(transpose(hilf, R, R, hT, st));
         SID_TRY(tn32(c, hT, SS, R, R, R, R, R, M1, st));
         SID_TRY(transpose(M1, R, R, M1t, st));
-        SID_TRY(sgemm_nt(S, 0, M1t, P, R, R, P, R, qS, P, st));
+        if (tc) SID_TRY(gemm_pix(c, Sx, P, R, M1, R, R, qS, prec, st));
+        else SID_TRY(sgemm_nt(S, 0, M1t, P, R, R, P, R, qS, P, st));
         M2 = qS;
     }
     k_s_dir<<<grid_for(P), 256, 0, st>>>(S, df, M2, (float)o->lamb_orth_L2, orth ? 1 : 0, P, (int)R, v);
     SID_CHECK_LAUNCH();
     // exact line search (:57-68): vQ = v*Q_T into the q_S buffer
-    SID_TRY(sgemm_nt(v, 0, QTt, P, R, R, P, R, qS, P, st));
+    if (tc) {
+        PixOperand Vx{};
+        SID_TRY(pix_operand(c, 0, v, false, P, R, prec, &Vx, st));
+        SID_TRY(gemm_pix(c, Vx, P, R, QT, R, R, qS, prec, st));
+    } else {
+        SID_TRY(sgemm_nt(v, 0, QTt, P, R, R, P, R, qS, P, st));
+    }
     if (o->pointwise) {
         k_s_sums<<<grid_for(P), 256, 0, st>>>(v, df, qS, P, (int)R, 1, alpha, part);
     } else {
