@@ -141,7 +141,7 @@ constexpr int GEMM_THREADS = (GEMM_DRAIN_WARPS + 2) * 32;
 template <int BN, int STAGES>
 __global__ void __launch_bounds__(GEMM_THREADS, 1)
 k_gemm_tc(const __grid_constant__ GemmMaps maps, int npass, int m, int n, int nkb, int kb_per, int bf16,
-          float* __restrict__ out, int64_t ldc, int64_t split_stride, int* __restrict__ err)
+          float* __restrict__ out, int64_t ldc, int64_t split_stride, float alpha, int* __restrict__ err)
 {
     using SM = GemmSmem<BN, STAGES>;
     constexpr uint32_t ACC_COLS = BN <= 32 ? 32 : (BN <= 64 ? 64 : (BN <= 128 ? 128 : 256));
@@ -278,7 +278,7 @@ k_gemm_tc(const __grid_constant__ GemmMaps maps, int npass, int m, int n, int nk
 #pragma unroll
             for (int j = 0; j < HALF; ++j) {
                 const int col = n0 + ch0 + j;
-                if (col < n) dst[(int64_t)row + ldc * col] = accr[j];
+                if (col < n) dst[(int64_t)row + ldc * col] = accr[j] * alpha;
             }
         }
     }
@@ -343,7 +343,7 @@ static int make_map(CUtensorMap* map, const void* base, int64_t rows, int64_t nk
 
 template <int BN, int STAGES>
 static int launch_gemm(const GemmMaps& maps, int npass, int m, int n, int nkb, int splitk, bool bf16, float* out,
-                       int64_t ldc, int64_t split_stride, int* err, cudaStream_t st)
+                       int64_t ldc, int64_t split_stride, float alpha, int* err, cudaStream_t st)
 {
     using SM = GemmSmem<BN, STAGES>;
     static bool configured = false;
@@ -354,7 +354,7 @@ static int launch_gemm(const GemmMaps& maps, int npass, int m, int n, int nkb, i
     const int kb_per = (int)cdiv(nkb, splitk);
     dim3 grid((unsigned)cdiv(m, GEMM_BM), (unsigned)cdiv(n, BN), (unsigned)splitk);
     k_gemm_tc<BN, STAGES><<<grid, GEMM_THREADS, SM::TOTAL, st>>>(maps, npass, m, n, nkb, kb_per, bf16 ? 1 : 0, out, ldc,
-                                                         split_stride, err);
+                                                         split_stride, alpha, err);
     SID_CHECK_LAUNCH();
     return SID_OK;
 }
@@ -394,7 +394,8 @@ void gemm_autotune(int m, int n, int nkb, int* bn, int* splitk)
 }
 
 // out (m x n, ldc) = sum_p A_p^T B_p; A_p: k x m, B_p: k x n, 16-bit K-blocked.
-// ws: >= splitk * m * n floats when splitk > 1 or (alpha, beta) != (1, 0).
+// ws: >= splitk * m * n floats when splitk > 1 or beta != 0 (alpha alone is
+// applied as the tiles are stored).
 int gemm_tn(const void* const* A, const void* const* B, int npass, int64_t m, int64_t n, int64_t k, bool bf16,
             float* C, int64_t ldc, float alpha, float beta, int bn, int splitk, float* ws, int64_t ws_elems, int* err,
             cudaStream_t st)
@@ -410,7 +411,7 @@ int gemm_tn(const void* const* A, const void* const* B, int npass, int64_t m, in
         SID_TRY(make_map(&maps.a[p], A[p], m, nkb, GEMM_BM, bf16));
         SID_TRY(make_map(&maps.b[p], B[p], n, nkb, bn, bf16));
     }
-    const bool direct = (splitk == 1 && alpha == 1.f && beta == 0.f);
+    const bool direct = (splitk == 1 && beta == 0.f);
     float* out = C;
     int64_t ldo = ldc, sstride = 0;
     if (!direct) {
@@ -421,10 +422,10 @@ int gemm_tn(const void* const* A, const void* const* B, int npass, int64_t m, in
     }
     int rc;
     switch (bn) {
-    case 256: rc = launch_gemm<256, 4>(maps, npass, (int)m, (int)n, nkb, splitk, bf16, out, ldo, sstride, err, st); break;
-    case 192: rc = launch_gemm<192, 5>(maps, npass, (int)m, (int)n, nkb, splitk, bf16, out, ldo, sstride, err, st); break;
-    case 128: rc = launch_gemm<128, 6>(maps, npass, (int)m, (int)n, nkb, splitk, bf16, out, ldo, sstride, err, st); break;
-    case 64: rc = launch_gemm<64, 8>(maps, npass, (int)m, (int)n, nkb, splitk, bf16, out, ldo, sstride, err, st); break;
+    case 256: rc = launch_gemm<256, 4>(maps, npass, (int)m, (int)n, nkb, splitk, bf16, out, ldo, sstride, direct ? alpha : 1.f, err, st); break;
+    case 192: rc = launch_gemm<192, 5>(maps, npass, (int)m, (int)n, nkb, splitk, bf16, out, ldo, sstride, direct ? alpha : 1.f, err, st); break;
+    case 128: rc = launch_gemm<128, 6>(maps, npass, (int)m, (int)n, nkb, splitk, bf16, out, ldo, sstride, direct ? alpha : 1.f, err, st); break;
+    case 64: rc = launch_gemm<64, 8>(maps, npass, (int)m, (int)n, nkb, splitk, bf16, out, ldo, sstride, direct ? alpha : 1.f, err, st); break;
     default: set_error("gemm: unsupported tile width %d", bn); return SID_EINVAL;
     }
     SID_TRY(rc);

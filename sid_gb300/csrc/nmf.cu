@@ -761,8 +761,8 @@ int gemm_pix(sid_ctx* c, const PixOperand& x, int64_t P, int64_t k, const float*
     } else {
         SID_TRY(split16(W, k, n, ldw, wh, nullptr, true, 1.f, st));
     }
-    // the scaled (alpha != 1) or split-K epilogue goes through a P x n workspace
-    const int64_t ws_elems = (sk > 1 || alpha != 1.f) ? (int64_t)std::max(sk, 1) * P * n : 1;
+    // a split-K epilogue goes through a P x n workspace (the scale is applied as the tiles are stored)
+    const int64_t ws_elems = sk > 1 ? (int64_t)sk * P * n : 1;
     SID_TRY(c->ws.alloc((size_t)ws_elems * sizeof(float)));
     return gemm_tn(As, Bs, npass, P, n, k, !x.f16, C, P, alpha, 0.f, bn, sk, c->ws.as<float>(),
                    (int64_t)(c->ws.bytes / sizeof(float)), c->errflag.as<int>(), st);
