@@ -256,11 +256,12 @@ __global__ void __launch_bounds__(256) k_nn_mask(ColBufs b, int K, int F, int us
 // entries of a column are compacted in thread order (deterministic), in rounds
 // of kClampList, and b.g is overwritten with G step for the next iteration's
 // mask kernel (fast_nnls.m:153).
-constexpr int kStepRows = 16;   // rows per thread: K <= 16 * 128 in sparse mode
+constexpr int kStepRows = 16;   // most rows per thread: K <= 16 * 128 in sparse mode
 constexpr int kClampList = 256;
 
+template <int ROWS>
 __device__ __forceinline__ void gstep_sparse(const ColBufs& b, int K, const ColIdx& c, bool act, int64_t o,
-                                             float alpha_f, const float (&cc)[kStepRows], unsigned cmask)
+                                             float alpha_f, const float (&cc)[ROWS], unsigned cmask)
 {
     __shared__ int lk[kColsPerCta][kClampList];
     __shared__ float lc[kColsPerCta][kClampList];
@@ -285,14 +286,14 @@ __device__ __forceinline__ void gstep_sparse(const ColBufs& b, int K, const ColI
     if (c.wc == 0 && c.lane == 0) atomicMax(&rounds_s, (ntot + kClampList - 1) / kClampList);
     __syncthreads();
     const int rounds = rounds_s;
-    float corr[kStepRows];
+    float corr[ROWS];
 #pragma unroll
-    for (int t = 0; t < kStepRows; ++t) corr[t] = 0.f;
+    for (int t = 0; t < ROWS; ++t) corr[t] = 0.f;
     for (int r = 0; r < rounds; ++r) {
         const int lo = r * kClampList;
         int pos = base + incl - cnt;
 #pragma unroll
-        for (int t = 0; t < kStepRows; ++t)
+        for (int t = 0; t < ROWS; ++t)
             if (cmask & (1u << t)) {
                 if (pos >= lo && pos < lo + kClampList) {
                     lk[c.cl][pos - lo] = c.wc * 32 + c.lane + t * kColThreads;
@@ -314,7 +315,7 @@ __device__ __forceinline__ void gstep_sparse(const ColBufs& b, int K, const ColI
                     cv[u] = ok ? lc[c.cl][m + u] : 0.f;
                 }
 #pragma unroll
-                for (int t = 0; t < kStepRows; ++t) {
+                for (int t = 0; t < ROWS; ++t) {
                     const int k = c.wc * 32 + c.lane + t * kColThreads;
                     if (k < K) {
                         float a = corr[t];
@@ -329,7 +330,7 @@ __device__ __forceinline__ void gstep_sparse(const ColBufs& b, int K, const ColI
     }
     if (!act) return;
 #pragma unroll
-    for (int t = 0; t < kStepRows; ++t) {
+    for (int t = 0; t < ROWS; ++t) {
         const int k = c.wc * 32 + c.lane + t * kColThreads;
         if (k < K) b.g[o + k] = fmaf(-alpha_f, b.g[o + k], corr[t]);
     }
@@ -337,6 +338,7 @@ __device__ __forceinline__ void gstep_sparse(const ColBufs& b, int K, const ColI
 
 // exact line search, clamp, step statistic (LS_nnls.m:122-142, fast_nnls.m:119-145).
 // `gu` (use_std) holds G * (column sum of d) / F, subtracted from G d.
+template <int ROWS>
 __global__ void __launch_bounds__(256) k_nn_step(ColBufs b, int K, int F, int solver, int sample, int tol_p,
                                                  int use_std)
 {
@@ -381,40 +383,48 @@ __global__ void __launch_bounds__(256) k_nn_step(ColBufs b, int K, int F, int so
     float a1_f = 0.f, a2_f = 0.f;
     const float alpha_f = alpha_s[c.cl];
     // sparse mode: this thread's clamp corrections c = step - (-alpha d), rows
-    // k = wc*32 + lane + 128 t (t < kStepRows)
-    float cc[kStepRows];
+    // k = wc*32 + lane + 128 t (t < ROWS)
+    float cc[ROWS];
     unsigned cmask = 0;
+    // one row: clamp, store, operand (dense mode), statistic; returns the clamp
+    // correction (0 where the bound does not clamp)
+    auto row = [&](int k) -> float {
+        const float2 xv = b.x[o + k], dv = b.df[o + k];
+        const float dm = (xv.x > 0.f || dv.x < 0.f) ? dv.x + dv.y : 0.f;
+        const float pstep = dm * alpha_f;
+        float2 xn = dd_add(xv, -pstep);
+        // the step x_new - x exactly: -alpha d, or -x where the bound clamps
+        float stp = -pstep, corr = 0.f;
+        if (xn.x < 0.f) {
+            xn = make_float2(0.f, 0.f);
+            stp = -(xv.x + xv.y);
+            corr = stp + pstep;
+        }
+        b.x[o + k] = xn;
+        if (!b.sparse) put_operand(b, o, c.j, k, stp);
+        // the convergence statistic takes the difference of the stored
+        // iterates, as the reference does: it reaches 0 once the step falls
+        // below the iterate's rounding, where the FP64 reference's does too
+        const float dx = (xn.x - xv.x) + (xn.y - xv.y);
+        if (solver == SOLVER_LS) {
+            a1_f += dx;                      // sum(x - x_)
+            a2_f = fmaf(xv.x, xv.x, a2_f);   // sum(x_.^2)
+        } else {
+            a1_f += (tol_p == 2) ? dx * dx : fabsf(dx);
+        }
+        return corr;
+    };
     if (act) {
 #pragma unroll
-        for (int t = 0; t < kStepRows; ++t) {
+        for (int t = 0; t < ROWS; ++t) {
             const int k = c.wc * 32 + c.lane + t * kColThreads;
             cc[t] = 0.f;
             if (k >= K) continue;
-            const float2 xv = b.x[o + k], dv = b.df[o + k];
-            const float dm = (xv.x > 0.f || dv.x < 0.f) ? dv.x + dv.y : 0.f;
-            const float pstep = dm * alpha_f;
-            float2 xn = dd_add(xv, -pstep);
-            // the step x_new - x exactly: -alpha d, or -x where the bound clamps
-            float stp = -pstep;
-            if (xn.x < 0.f) {
-                xn = make_float2(0.f, 0.f);
-                stp = -(xv.x + xv.y);
-                cc[t] = stp + pstep;
-                cmask |= 1u << t;
-            }
-            b.x[o + k] = xn;
-            if (!b.sparse) put_operand(b, o, c.j, k, stp);
-            // the convergence statistic takes the difference of the stored
-            // iterates, as the reference does: it reaches 0 once the step falls
-            // below the iterate's rounding, where the FP64 reference's does too
-            const float dx = (xn.x - xv.x) + (xn.y - xv.y);
-            if (solver == SOLVER_LS) {
-                a1_f += dx;                      // sum(x - x_)
-                a2_f = fmaf(xv.x, xv.x, a2_f);   // sum(x_.^2)
-            } else {
-                a1_f += (tol_p == 2) ? dx * dx : fabsf(dx);
-            }
+            cc[t] = row(k);
+            if (cc[t] != 0.f) cmask |= 1u << t;
         }
+        // rows past ROWS * 128 (dense mode only: sparse mode needs K <= ROWS * 128)
+        for (int k = c.wc * 32 + c.lane + ROWS * kColThreads; k < K; k += kColThreads) row(k);
     }
     const float2 a1p = warp_sum_ff(a1_f);
     const float2 a2p = warp_sum_ff(a2_f);
@@ -853,7 +863,11 @@ static int iterate(sid_ctx* c, NnlsWork& w, int64_t K, int64_t F, int solver, co
         k_nn_mask<<<(unsigned)cdiv(F, kColsPerCta), kColsPerCta * kColThreads, 0, s>>>(b, (int)K, (int)F, use_std);
         SID_CHECK_LAUNCH();
         SID_TRY(gmul_std(s));
-        k_nn_step<<<(unsigned)cdiv(F, kColsPerCta), kColsPerCta * kColThreads, 0, s>>>(
+if (K <= 8 * kColThreads)
+            k_nn_step<8><<<(unsigned)cdiv(F, kColsPerCta), kColsPerCta * kColThreads, 0, s>>>(
+            b, (int)K, (int)F, solver, sample, (int)o->tol_p, use_std);
+        else
+            k_nn_step<kStepRows><<<(unsigned)cdiv(F, kColsPerCta), kColsPerCta * kColThreads, 0, s>>>(
             b, (int)K, (int)F, solver, sample, (int)o->tol_p, use_std);
         SID_CHECK_LAUNCH();
         if (!b.sparse) SID_TRY(gmul_std(s));  // G step: applied by the next iteration's mask kernel

@@ -87,6 +87,26 @@ def test_fast_nnls_matches_oracle(ctx, oracle, prec):
     assert mn >= 0 and viol < 1e-3, viol
 
 
+@pytest.mark.parametrize("prec", ["fp32", "split"])
+def test_fast_nnls_many_components(ctx, oracle, prec):
+    """K = 2100 components: past the rows a step-kernel thread keeps in
+    registers (16 x 128), so G step comes from the second contraction and the
+    update pass runs its general tail.  Sparse library rows (1 %) keep the
+    Gram well conditioned: both runs converge (about 100 iterations)."""
+    from sid_gb300 import to_numpy
+    rng = np.random.default_rng(7)
+    P, K, F = 6000, 2100, 6
+    A = np.asfortranarray((rng.random((P, K)) * (rng.random((P, K)) < 0.01)).astype(np.float32))
+    T = rng.random((K, F)) * (rng.random((K, F)) < 0.4)
+    Y = np.asfortranarray((A.astype(np.float64) @ T + 0.01 * rng.standard_normal((P, F))).astype(np.float32))
+    Xg, _ = ctx.fast_nnls(A, Y, {}, prec=prec)
+    Xg = to_numpy(Xg)
+    Xo, _, _, _ = oracle.fast_nnls(A, Y, {})
+    assert rel_l2(Xg, Xo) < 1e-4, rel_l2(Xg, Xo)
+    viol, mn = kkt(A, Y, Xg)
+    assert mn >= 0 and viol < 1e-4, viol
+
+
 def test_fast_nnls_warm_start(ctx, oracle):
     from sid_gb300 import to_numpy
     A, Y, T = problem(1200, 30, 64, 3)
