@@ -5,11 +5,14 @@
 // (spatial components), T R x F (timeseries).  Each step is one gradient
 // evaluation, a projection onto the non-negativity constraint, an exact line
 // search and a clamped update.  The pixel-long contractions (S'S, S'Y) run
-// through the tensor-core contraction at the requested precision; the frame-
-// and rank-long products (R x R and R x F, or P x R with an R-deep
-// reduction) run on the FP32 SIMT GEMMs; every reduction of the line search
-// accumulates in FP64.  Nothing is copied to the host: the step sizes stay in
-// device memory, so a step is stream-ordered and graph-capturable.
+// through the tensor-core contraction at the requested precision, and so do
+// S_update's pixel-by-rank products (Y T', S Q_T, v Q_T; P x R with an F- or
+// R-deep reduction) except at FP32 precision, where they and the frame- and
+// rank-long products (R x R, R x F) run on the FP32 SIMT GEMMs.  The line
+// search's reductions over R x F accumulate in FP64; those over the P x R
+// factors as FP32 two-sum pairs (FP64-grade).  The step sizes stay in device
+// memory; the split precision's power-of-two operand scales are read back to
+// the host once per product.
 #include <cmath>
 #include <cstring>
 
