@@ -286,6 +286,18 @@ int sid_spatial_update(sid_ctx* ctx, const float* T, const void* Y, int ydtype, 
                        int64_t F, int64_t P, double lamb_L1, double lamb_L2, double lamb_orth_L1, int use_std,
                        int bg_sub, float* forward_model, int32_t* status, void* stream);
 
+/* [x, w, info] = NQP(Q, b) for B independent problems of one size
+ *                                            NQP.m:42-178 (default options)
+ * argmin_{x >= 0} 0.5 x'Qx + q'x, Lawson-Hanson active set with an incremental
+ * Cholesky factor, FP64, one thread per problem; the solver reg_nnls.m:69 and
+ * the spatial update call.  Q: n x n x B (column-major, device), q: n x B;
+ * x: n x B; w (optional): n x B, NQP's final w; iters / status (optional, B
+ * int32): iterations taken, 0 ok or 2 at the iteration cap.  n <= 32.
+ * SID_ENOCONV if any problem hit the cap (NQP.m:116-119's error).
+ * Synchronises the stream. */
+int sid_nqp_batched(sid_ctx* ctx, const double* Q, const double* q, int n, int64_t B, double* x, double* w,
+                    int32_t* iters, int32_t* status, void* stream);
+
 /* ---- Quantiles and component reconstruction ---------------------------------
  * MATLAB quantile of a vector (sorted non-NaN data at probabilities
  * (k - 0.5)/n, linear interpolation, clamped to the extremes; NaN when no

@@ -5,7 +5,7 @@ The compute lives in ``libsid.so`` (hand-written CUDA behind the C ABI of
 top of it.  Import does not require a GPU; calling the operators does.
 """
 from ._lib import SidError  # noqa: F401
-from .nnls import Context, LS_nnls, fast_nnls, quantile, update_spatial_component  # noqa: F401
+from .nnls import Context, LS_nnls, NQP, fast_nnls, quantile, reg_nnls, update_spatial_component  # noqa: F401
 from .nmf import S_update, T_update  # noqa: F401
 from .background import compute_std_image, rank_1_factorization  # noqa: F401
 from .postproc import ImageRect, SNR_order, merge_filters, read_sensor_movie, rectify_frames  # noqa: F401

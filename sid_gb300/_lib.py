@@ -80,6 +80,7 @@ SIGNATURES = {
     "sid_library": [P, P, I64, P, P, I64, I64, F64, P, I32, P],
     "sid_library_boxes": [P, I64, I64, F64, I64, I64, I64, P],
     "sid_spatial_update": [P, P, P, I32, P, I64, I64, I64, F64, F64, F64, I32, I32, P, P, P],
+    "sid_nqp_batched": [P, P, P, I32, I64, P, P, P, P, P],
     "sid_nmf_defaults": [P],
     "sid_t_update": [P, P, I32, P, P, I64, I64, I64, P, P, P, I32, P],
     "sid_s_update": [P, P, I32, P, P, I64, I64, I64, P, P, P, I32, P],

@@ -149,64 +149,20 @@ struct SpatialOpts {
     int use_std, bg_sub;
 };
 
-// One thread per pixel: collect the covering components and solve the NQP in
-// FP64.  status[p]: 0 ok, 1 too many components, 2 iteration cap (NQP.m:116-119).
-__global__ void __launch_bounds__(128)
-k_pixel_nqp(const uint8_t* __restrict__ tmpl, int Rt, int64_t P, const float* __restrict__ G, int R,
-            const float* __restrict__ C, int64_t ldc, const float* __restrict__ pnrm, const float* __restrict__ psum,
-            const float* __restrict__ tsum, int F, SpatialOpts o, float* __restrict__ out, int* __restrict__ status,
-            int* __restrict__ nfail)
+// Lawson-Hanson active set with an incremental Cholesky factor of the passive
+// block (NQP.m:93-178, default options, FP64): argmin_{x >= 0} 0.5 x'Qx - b'x
+// for n <= kNqpMax.  Qij(i, j) returns Q(i, j); b is NQP's internal right-hand
+// side (minus the linear term); w receives the final w = b - Q x.  Returns 0,
+// or 2 at the iteration cap (NQP.m:116-119); *iters = iterations taken.
+template <class QF>
+__device__ int nqp_solve(int n, const QF& Qij, const double* b, double* x, double* w, int* iters)
 {
-    const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (p >= P) return;
-    int idx[kNqpMax];
-    int n = 0;
-    bool over = false;
-    for (int r = 0; r < Rt; ++r) {
-        if (tmpl[r + (int64_t)Rt * p]) {
-            if (n < kNqpMax) idx[n++] = r;
-            else over = true;
-        }
-    }
-    if (n == 0) {
-        // outside every template: background row, if any (update_spatial_component.m:128-131)
-        if (o.bg_sub) out[(R - 1) + (int64_t)R * p] = C[p + ldc * (R - 1)];
-        status[p] = 0;
-        return;
-    }
-    if (o.bg_sub) {
-        if (n < kNqpMax) idx[n++] = R - 1;
-        else over = true;
-    }
-    if (over) {
-        status[p] = 1;
-        atomicAdd(nfail, 1);
-        return;
-    }
-    const double yn = (double)pnrm[p];
-    if (!(yn > 0.0)) {
-        for (int i = 0; i < n; ++i) out[idx[i] + (int64_t)R * p] = 0.f;
-        status[p] = 0;
-        return;
-    }
-    // Q(i,j) and b = -q (NQP works with b = -q, NQP.m:145)
-    auto Qij = [&](int i, int j) -> double {
-        double v = (double)G[idx[i] + (int64_t)R * idx[j]];
-        if (i == j) v += o.l2;
-        else if (!(o.bg_sub && (i == n - 1 || j == n - 1))) v += o.lo;  // hilf = ones - eye, bg row/col zero
-        if (o.use_std) v -= (double)tsum[idx[i]] * (double)tsum[idx[j]] / (double)F;
-        return v;
-    };
-    double b[kNqpMax], x[kNqpMax], z[kNqpMax], w[kNqpMax], wsc[kNqpMax], t[kNqpMax];
+    double z[kNqpMax], wsc[kNqpMax], t[kNqpMax];
     double L[kNqpMax * (kNqpMax + 1) / 2];  // packed lower triangle, row-major
     int pn[kNqpMax];
     bool Pset[kNqpMax];
     for (int i = 0; i < n; ++i) {
-        double q = -(double)C[p + ldc * idx[i]] / yn;
-        if (o.use_std) q += (double)tsum[idx[i]] * (double)psum[p] / yn / (double)F;
-        q += o.l1;
-        b[i] = -q;
-        w[i] = -q;  // w = -b_input, NQP.m:122 (b_input = q)
+        w[i] = b[i];  // w = -b_input, NQP.m:122
         x[i] = 0.0;
         wsc[i] = 0.0;
         Pset[i] = false;
@@ -307,12 +263,98 @@ k_pixel_nqp(const uint8_t* __restrict__ tmpl, int Rt, int64_t P, const float* __
     }
 done:
 #undef LIJ
+    *iters = iter;
+    return st;
+}
+
+// One thread per pixel: collect the covering components and solve the NQP in
+// FP64.  status[p]: 0 ok, 1 too many components, 2 iteration cap (NQP.m:116-119).
+__global__ void __launch_bounds__(128)
+k_pixel_nqp(const uint8_t* __restrict__ tmpl, int Rt, int64_t P, const float* __restrict__ G, int R,
+            const float* __restrict__ C, int64_t ldc, const float* __restrict__ pnrm, const float* __restrict__ psum,
+            const float* __restrict__ tsum, int F, SpatialOpts o, float* __restrict__ out, int* __restrict__ status,
+            int* __restrict__ nfail)
+{
+    const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (p >= P) return;
+    int idx[kNqpMax];
+    int n = 0;
+    bool over = false;
+    for (int r = 0; r < Rt; ++r) {
+        if (tmpl[r + (int64_t)Rt * p]) {
+            if (n < kNqpMax) idx[n++] = r;
+            else over = true;
+        }
+    }
+    if (n == 0) {
+        // outside every template: background row, if any (update_spatial_component.m:128-131)
+        if (o.bg_sub) out[(R - 1) + (int64_t)R * p] = C[p + ldc * (R - 1)];
+        status[p] = 0;
+        return;
+    }
+    if (o.bg_sub) {
+        if (n < kNqpMax) idx[n++] = R - 1;
+        else over = true;
+    }
+    if (over) {
+        status[p] = 1;
+        atomicAdd(nfail, 1);
+        return;
+    }
+    const double yn = (double)pnrm[p];
+    if (!(yn > 0.0)) {
+        for (int i = 0; i < n; ++i) out[idx[i] + (int64_t)R * p] = 0.f;
+        status[p] = 0;
+        return;
+    }
+    // Q(i,j) and b = -q (NQP works with b = -q, NQP.m:145)
+    auto Qij = [&](int i, int j) -> double {
+        double v = (double)G[idx[i] + (int64_t)R * idx[j]];
+        if (i == j) v += o.l2;
+        else if (!(o.bg_sub && (i == n - 1 || j == n - 1))) v += o.lo;  // hilf = ones - eye, bg row/col zero
+        if (o.use_std) v -= (double)tsum[idx[i]] * (double)tsum[idx[j]] / (double)F;
+        return v;
+    };
+    double b[kNqpMax], x[kNqpMax], w[kNqpMax];
+    for (int i = 0; i < n; ++i) {
+        double q = -(double)C[p + ldc * idx[i]] / yn;
+        if (o.use_std) q += (double)tsum[idx[i]] * (double)psum[p] / yn / (double)F;
+        q += o.l1;
+        b[i] = -q;  // NQP works with b = -q (NQP.m:145)
+    }
+    int iters = 0;
+    const int st = nqp_solve(n, Qij, b, x, w, &iters);
     status[p] = st;
     if (st) {
         atomicAdd(nfail, 1);
         return;
     }
     for (int i = 0; i < n; ++i) out[idx[i] + (int64_t)R * p] = (float)(x[i] * yn);
+}
+
+// One thread per problem k: Q (n x n, column-major, FP64) at Q + n*n*k, the
+// linear term at q + n*k; x and w (optional) n x B; NQP's [x, w, info]
+// (NQP.m:42-178) for independent problems of one size.
+__global__ void __launch_bounds__(128) k_nqp_batched(const double* __restrict__ Q, const double* __restrict__ q,
+                                                     int n, int64_t B, double* __restrict__ x, double* __restrict__ w,
+                                                     int32_t* __restrict__ iters, int32_t* __restrict__ status,
+                                                     int* __restrict__ nfail)
+{
+    const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (k >= B) return;
+    const double* Qk = Q + (int64_t)n * n * k;
+    auto Qij = [&](int i, int j) -> double { return Qk[i + (int64_t)n * j]; };
+    double bb[kNqpMax], xx[kNqpMax], ww[kNqpMax];
+    for (int i = 0; i < n; ++i) bb[i] = -q[i + (int64_t)n * k];  // NQP works with b = -q (NQP.m:145)
+    int it = 0;
+    const int st = nqp_solve(n, Qij, bb, xx, ww, &it);
+    for (int i = 0; i < n; ++i) {
+        x[i + (int64_t)n * k] = xx[i];
+        if (w) w[i + (int64_t)n * k] = ww[i];
+    }
+    if (iters) iters[k] = it;
+    if (status) status[k] = st;
+    if (st) atomicAdd(nfail, 1);
 }
 
 }  // namespace sid
@@ -370,6 +412,29 @@ extern "C" int sid_spatial_update(sid_ctx* c, const float* T, const void* Y, int
         set_error("sid_spatial_update: %d pixel problems failed (more than %d covering components, or the "
                   "NQP iteration cap of NQP.m:116-119); see the status array",
                   hf, kNqpMax);
+        return SID_ENOCONV;
+    }
+    return SID_OK;
+}
+
+extern "C" int sid_nqp_batched(sid_ctx* c, const double* Q, const double* q, int n, int64_t B, double* x, double* w,
+                               int32_t* iters, int32_t* status, void* stream)
+{
+    SID_REQUIRE(c && Q && q && x, "sid_nqp_batched: NULL argument");
+    SID_REQUIRE(n >= 1 && n <= kNqpMax, "sid_nqp_batched: n = %d outside [1, %d]", n, kNqpMax);
+    SID_REQUIRE(B >= 1, "sid_nqp_batched: no problems");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    SID_TRY(c->scal.alloc(64));
+    int* nfail = c->scal.as<int>();
+    SID_CUDA_TRY(cudaMemsetAsync(nfail, 0, sizeof(int), st));
+    k_nqp_batched<<<(unsigned)cdiv(B, 128), 128, 0, st>>>(Q, q, n, B, x, w, iters, status, nfail);
+    SID_CHECK_LAUNCH();
+    int hf = 0;
+    SID_CUDA_TRY(cudaMemcpyAsync(&hf, nfail, sizeof(int), cudaMemcpyDeviceToHost, st));
+    SID_TRY(ctx_sync(c, st));
+    if (hf) {
+        set_error("nnls Failed to converge: %d of %lld problems hit the NQP iteration cap (NQP.m:116-119)", hf,
+                  (long long)B);
         return SID_ENOCONV;
     }
     return SID_OK;

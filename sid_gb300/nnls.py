@@ -229,3 +229,85 @@ Context.spatial_update = _spatial_update
 def update_spatial_component(timeseries, sensor_movie, template, opts=None):
     """forward_model = update_spatial_component(timeseries, sensor_movie, template, opts)."""
     return _ctx().spatial_update(timeseries, sensor_movie, template, opts)
+
+
+def _f64_fortran(a):
+    """1-D contiguous CUDA float64 tensor of a's elements in column-major order."""
+    if isinstance(a, torch.Tensor):
+        t = a.to(device="cuda", dtype=torch.float64)
+        return t.permute(*reversed(range(t.dim()))).contiguous().reshape(-1)
+    arr = np.asarray(a, dtype=np.float64)
+    return torch.from_numpy(np.ascontiguousarray(arr.ravel(order="F"))).to("cuda")
+
+
+def _nqp(self, Q, b, opts=None):
+    """[x, w, info] = NQP(Q, b, opts) (NQP.m:1, default options) on the GPU:
+    argmin_{x >= 0} 0.5 x'Qx + b'x in FP64 by the Lawson-Hanson active set.
+    Q is n x n, or n x n x B for B independent problems solved at once (b then
+    n x B); n <= 32.  x and w are CUDA float64 tensors shaped like b; info
+    carries ``iter`` (an int, or a B-vector).  A problem that reaches the
+    iteration cap raises SidError, as NQP.m:116-119 raises its error."""
+    if opts:
+        raise NotImplementedError("NQP: only the default options (NQP.m:42-76) are supported")
+    Qs = tuple(Q.shape) if isinstance(Q, torch.Tensor) else np.shape(Q)
+    bs = tuple(b.shape) if isinstance(b, torch.Tensor) else np.shape(b)
+    if len(Qs) not in (2, 3) or Qs[0] != Qs[1]:
+        raise ValueError(f"NQP: Q must be n x n or n x n x B, got {Qs}")
+    n = int(Qs[0])
+    B = int(Qs[2]) if len(Qs) == 3 else 1
+    if int(np.prod(bs)) != n * B:
+        raise ValueError(f"NQP: b must hold {n} x {B} values, got {bs}")
+    Qd, bd = _f64_fortran(Q), _f64_fortran(b)
+    x = torch.empty(B, n, dtype=torch.float64, device="cuda")
+    w = torch.empty(B, n, dtype=torch.float64, device="cuda")
+    it = torch.zeros(B, dtype=torch.int32, device="cuda")
+    _lib.call("sid_nqp_batched", self._ctx, Qd.data_ptr(), bd.data_ptr(), n, B, x.data_ptr(), w.data_ptr(),
+              it.data_ptr(), None, _stream_ptr())
+    if len(Qs) == 2:
+        return x[0], w[0], {"iter": int(it[0])}
+    return x.T, w.T, {"iter": it}
+
+
+Context.nqp = _nqp
+
+
+def NQP(Q, b, opts=None):
+    """[x, w, info] = NQP(Q, b, opts) (NQP.m:1)."""
+    return _ctx().nqp(Q, b, opts)
+
+
+def reg_nnls(A, d, opts=None):
+    """x = reg_nnls(A, d, opts) (reg_nnls.m:1): the regularised NNLS
+    min_{x >= 0} ||A x - d||^2 (+ L1, L2, orthogonality terms) as one NQP.  The
+    n x n system is formed in FP64 on the GPU (reg_nnls.m:40-66) and solved by
+    the batched NQP kernel."""
+    opts = dict(opts or {})
+    At = A.to(device="cuda", dtype=torch.float64) if isinstance(A, torch.Tensor) else \
+        torch.from_numpy(np.asarray(A, dtype=np.float64)).to("cuda")
+    dt = d.to(device="cuda", dtype=torch.float64) if isinstance(d, torch.Tensor) else \
+        torch.from_numpy(np.asarray(d, dtype=np.float64)).to("cuda")
+    dt = dt.reshape(At.shape[0], -1)
+    n = At.shape[1]
+    hilf = opts.get("hilf")
+    if hilf is None:
+        hilf = torch.ones(n, n, dtype=torch.float64, device="cuda") - torch.eye(n, dtype=torch.float64, device="cuda")
+        if opts.get("bg_sub", 0):
+            hilf[:, -1] = 0
+            hilf[-1, :] = 0
+    else:
+        hilf = hilf.to(device="cuda", dtype=torch.float64) if isinstance(hilf, torch.Tensor) else \
+            torch.from_numpy(np.asarray(hilf, dtype=np.float64)).to("cuda")
+    Q = At.T @ At
+    q = -(At.T @ dt)
+    if opts.get("use_std", False):
+        tt = At.sum(dim=0)
+        Q = Q - torch.outer(tt, tt) / At.shape[0]
+        q = q + tt[:, None] * dt.sum(dim=0)[None, :] / At.shape[0]
+    if opts.get("lamb_L1", 0):
+        q = q + float(opts["lamb_L1"])
+    if opts.get("lamb_L2", 0):
+        Q = Q + float(opts["lamb_L2"]) * torch.eye(n, dtype=torch.float64, device="cuda")
+    if opts.get("lamb_orth_L1", 0):
+        Q = Q + float(opts["lamb_orth_L1"]) * hilf
+    x, _, _ = NQP(Q, q[:, 0])
+    return x

@@ -49,3 +49,59 @@ def test_spatial_update_matches_oracle(gpu, oracle, opts):
     # FP32 products into an FP64 active-set solve: the support (which entries
     # are zero) must agree and the values within the FP32 path's bar
     assert rel_l2(got, ref) < 1e-4, rel_l2(got, ref)
+
+
+def _nqp_problems(rng, n, B):
+    Qs = np.empty((n, n, B))
+    bs = np.empty((n, B))
+    for k in range(B):
+        M = rng.standard_normal((n + 3, n))
+        Qs[:, :, k] = M.T @ M + 1e-3 * np.eye(n)
+        bs[:, k] = rng.standard_normal(n)
+    return np.asfortranarray(Qs), np.asfortranarray(bs)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n", [1, 5, 17, 32])
+def test_nqp_batched_matches_oracle(gpu, oracle, n):
+    """[x, w, info] = NQP(Q, b) (NQP.m:42-178) for a stack of independent
+    problems against the oracle's Lawson-Hanson restatement, both FP64."""
+    import sid_gb300 as s
+    rng = np.random.default_rng(11 + n)
+    Qs, bs = _nqp_problems(rng, n, 40)
+    x, w, info = s.NQP(Qs, bs)
+    x, w, its = x.cpu().numpy(), w.cpu().numpy(), info["iter"].cpu().numpy()
+    same_iters = 0
+    for k in range(bs.shape[1]):
+        xo, wo, ito = oracle.NQP(Qs[:, :, k], bs[:, k])
+        scale = np.abs(bs[:, k]).max()
+        np.testing.assert_allclose(x[:, k], xo, rtol=1e-9, atol=1e-12 * scale)
+        np.testing.assert_allclose(w[:, k], wo, rtol=1e-8, atol=1e-9 * scale)
+        same_iters += int(its[k] == ito)
+    # FMA contraction differs between the host and device compilers: an
+    # active-set tie could take another order, never a different optimum
+    assert same_iters >= 0.95 * bs.shape[1]
+    x1, w1, info1 = s.NQP(Qs[:, :, 0], bs[:, 0])
+    assert tuple(x1.shape) == (n,) and isinstance(info1["iter"], int)
+    np.testing.assert_array_equal(x1.cpu().numpy(), x[:, 0])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("opts", [{}, {"lamb_L1": 0.1, "lamb_L2": 0.05},
+                                  {"use_std": True, "lamb_orth_L1": 0.02, "bg_sub": 1}])
+def test_reg_nnls_matches_oracle(gpu, oracle, opts):
+    """x = reg_nnls(A, d, opts) (reg_nnls.m:40-69)."""
+    import sid_gb300 as s
+    rng = np.random.default_rng(12)
+    A = rng.random((200, 12))
+    d = A @ (rng.random(12) * (rng.random(12) < 0.6)) + 0.01 * rng.standard_normal(200)
+    x = s.reg_nnls(A, d, opts).cpu().numpy()
+    xo = oracle.reg_nnls(A, d, opts)
+    np.testing.assert_allclose(x, xo, rtol=1e-8, atol=1e-10 * np.abs(xo).max())
+
+
+@pytest.mark.gpu
+def test_nqp_rejects_oversized_problem(gpu):
+    import sid_gb300 as s
+    with pytest.raises(s.SidError):
+        s.NQP(np.eye(33), np.ones(33))
