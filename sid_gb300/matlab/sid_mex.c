@@ -18,6 +18,7 @@
  *   [S, T]   = sid_mex('t_update', Y, T, S, opts)        opts.active, opts.Y optional
  *   [S, T]   = sid_mex('s_update', Y, S, T, opts)        opts.Y, opts.hilf optional
  *   q        = sid_mex('quantile', x, p)
+ *   [x, w, it] = sid_mex('nqp', Q, b)     Q n x n x B, b n x B double gpuArrays (n <= 32)
  *   [s, t, sd] = sid_mex('rank1_background', Y, maxIter)    rank_1_factorization + compute_std_image
  *   sid_mex('set_kernel', plan, kernel)                      neuron-kernel composition ([] removes)
  *   [keep, template] = sid_mex('merge_filters', timeseries, template, limit, bg_sub)
@@ -439,6 +440,36 @@ void mexFunction(int nlhs, mxArray* plhs[], int nrhs, const mxArray* prhs[])
         mxGPUDestroyGPUArray(tr);
         check(rc, cmd);
         for (mwSize i = 0; i < d[0]; ++i) o[i] += 1;
+        return;
+    }
+    if (!strcmp(cmd, "nqp")) {
+        /* [x, w, it] = sid_mex('nqp', Q, b): B independent NQPs (NQP.m:42-178) */
+        if (!mxIsGPUArray(prhs[1]) || !mxIsGPUArray(prhs[2]))
+            mexErrMsgIdAndTxt("sid:type", "%s: gpuArray arguments expected", cmd);
+        const mxGPUArray* Q = mxGPUCreateFromMxArray(prhs[1]);
+        const mxGPUArray* b = mxGPUCreateFromMxArray(prhs[2]);
+        if (mxGPUGetClassID(Q) != mxDOUBLE_CLASS || mxGPUGetClassID(b) != mxDOUBLE_CLASS)
+            mexErrMsgIdAndTxt("sid:type", "%s: double gpuArrays expected", cmd);
+        const mwSize* dq = mxGPUGetDimensions(Q);
+        const mwSize n = dq[0];
+        const mwSize B = (mwSize)(mxGPUGetNumberOfElements(b) / (n ? n : 1));
+        const mwSize dx[2] = {n, B}, di[2] = {1, B};
+        mxGPUArray* x = mxGPUCreateGPUArray(2, dx, mxDOUBLE_CLASS, mxREAL, MX_GPU_DO_NOT_INITIALIZE);
+        mxGPUArray* w = mxGPUCreateGPUArray(2, dx, mxDOUBLE_CLASS, mxREAL, MX_GPU_DO_NOT_INITIALIZE);
+        mxGPUArray* it = mxGPUCreateGPUArray(2, di, mxINT32_CLASS, mxREAL, MX_GPU_DO_NOT_INITIALIZE);
+        const int rc = sid_nqp_batched(ctx(cmd), (const double*)mxGPUGetDataReadOnly(Q),
+                                       (const double*)mxGPUGetDataReadOnly(b), (int)n, (int64_t)B,
+                                       (double*)mxGPUGetData(x), (double*)mxGPUGetData(w), (int32_t*)mxGPUGetData(it),
+                                       NULL, NULL);
+        plhs[0] = mxGPUCreateMxArrayOnGPU(x);
+        if (nlhs > 1) plhs[1] = mxGPUCreateMxArrayOnGPU(w);
+        if (nlhs > 2) plhs[2] = mxGPUCreateMxArrayOnGPU(it);
+        mxGPUDestroyGPUArray(Q);
+        mxGPUDestroyGPUArray(b);
+        mxGPUDestroyGPUArray(x);
+        mxGPUDestroyGPUArray(w);
+        mxGPUDestroyGPUArray(it);
+        check(rc, cmd);
         return;
     }
     if (!strcmp(cmd, "quantile")) {

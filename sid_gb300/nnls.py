@@ -247,8 +247,10 @@ def _nqp(self, Q, b, opts=None):
     n x B); n <= 32.  x and w are CUDA float64 tensors shaped like b; info
     carries ``iter`` (an int, or a B-vector).  A problem that reaches the
     iteration cap raises SidError, as NQP.m:116-119 raises its error."""
-    if opts:
-        raise NotImplementedError("NQP: only the default options (NQP.m:42-76) are supported")
+    opts = dict(opts or {})
+    if opts.get("Accy", 1) != 1 or "Order" in opts or opts.get("Tol", 0) != 0 or "Iter" in opts:
+        raise NotImplementedError("NQP: only the default options (Accy 1, no Order, Tol 0, default Iter) "
+                                  "are supported")
     Qs = tuple(Q.shape) if isinstance(Q, torch.Tensor) else np.shape(Q)
     bs = tuple(b.shape) if isinstance(b, torch.Tensor) else np.shape(b)
     if len(Qs) not in (2, 3) or Qs[0] != Qs[1]:
