@@ -248,9 +248,9 @@ def _nqp(self, Q, b, opts=None):
     carries ``iter`` (an int, or a B-vector).  A problem that reaches the
     iteration cap raises SidError, as NQP.m:116-119 raises its error."""
     opts = dict(opts or {})
-    if opts.get("Accy", 1) != 1 or "Order" in opts or opts.get("Tol", 0) != 0 or "Iter" in opts:
-        raise NotImplementedError("NQP: only the default options (Accy 1, no Order, Tol 0, default Iter) "
-                                  "are supported")
+    # NQP.m reads Tol, Iter and Order (NQP.m:63-80); other fields are ignored
+    if "Order" in opts or opts.get("Tol", 0) != 0 or "Iter" in opts:
+        raise NotImplementedError("NQP: only the default options (no Order, Tol 0, default Iter) are supported")
     Qs = tuple(Q.shape) if isinstance(Q, torch.Tensor) else np.shape(Q)
     bs = tuple(b.shape) if isinstance(b, torch.Tensor) else np.shape(b)
     if len(Qs) not in (2, 3) or Qs[0] != Qs[1]:
