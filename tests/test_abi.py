@@ -58,3 +58,27 @@ def test_null_arguments_rejected(sidlib):
 
 def test_destroy_null_is_ok(sidlib):
     assert sidlib.sid_plan_destroy(None) == 0
+
+
+_NO_STATUS = {"sid_version", "sid_last_error", "sid_plan_destroy", "sid_ctx_destroy", "sid_pinv_destroy",
+              "sid_ls_nnls_defaults", "sid_fast_nnls_defaults", "sid_nmf_defaults", "sid_recon_defaults"}
+
+
+def test_every_entry_point_rejects_null_arguments(sidlib):
+    """Every computing entry point the header declares checks its pointers and
+    sizes first: all-NULL / zero arguments give SID_EINVAL and a message, with
+    no CUDA call (this machine has no GPU)."""
+    names = [n for n in _lib.header_functions() if n not in _NO_STATUS]
+    assert len(names) >= 30
+    for name in names:
+        args = []
+        for t in _lib.SIGNATURES[name]:
+            if t in (ctypes.c_double, ctypes.c_float):
+                args.append(0.0)
+            elif t in (ctypes.c_int, ctypes.c_int32, ctypes.c_int64, ctypes.c_long, ctypes.c_longlong):
+                args.append(0)
+            else:
+                args.append(None)
+        rc = getattr(sidlib, name)(*args)
+        assert rc == _lib.SID_EINVAL, (name, rc)
+        assert sidlib.sid_last_error(), name
