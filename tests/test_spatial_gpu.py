@@ -35,6 +35,33 @@ def test_oracle_nqp_is_nnls_optimum(oracle):
         np.testing.assert_allclose(x, xs, atol=1e-10)
 
 
+def test_oracle_reg_nnls_options_pinned(oracle):
+    """reg_nnls.m:40-66 against independent forms of the same problem: lamb_L2
+    is NNLS on [A; sqrt(l2) I] x ~ [d; 0]; use_std is NNLS on A and d with their
+    means over the rows removed; with lamb_L1 and lamb_orth_L1 the solution
+    meets the KKT conditions of 0.5 x'Qx + q'x over x >= 0."""
+    from scipy.optimize import nnls
+    rng = np.random.default_rng(4)
+    A = rng.random((60, 7))
+    d = A @ (rng.random(7) * (rng.random(7) < 0.6)) + 0.05 * rng.standard_normal(60)
+    l2 = 0.3
+    x = oracle.reg_nnls(A, d, {"lamb_L2": l2})
+    xs, _ = nnls(np.vstack([A, np.sqrt(l2) * np.eye(7)]), np.concatenate([d, np.zeros(7)]))
+    np.testing.assert_allclose(x, xs, atol=1e-10)
+    x = oracle.reg_nnls(A, d, {"use_std": True})
+    xs, _ = nnls(A - A.mean(axis=0), d - d.mean())
+    np.testing.assert_allclose(x, xs, atol=1e-10)
+    opts = {"lamb_L1": 0.2, "lamb_orth_L1": 0.05, "bg_sub": 1}
+    x = oracle.reg_nnls(A, d, opts)
+    hilf = np.ones((7, 7)) - np.eye(7)
+    hilf[:, -1] = 0
+    hilf[-1, :] = 0
+    g = (A.T @ A + 0.05 * hilf) @ x - A.T @ d + 0.2
+    assert x.min() >= 0
+    assert np.abs(g[x > 0]).max(initial=0.0) < 1e-9
+    assert g[x == 0].min(initial=0.0) > -1e-9
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("opts", [{"bg_sub": 1}, {"bg_sub": 1, "lamb_L1": 0.01, "lamb_L2": 0.05,
                                                    "lamb_orth_L1": 1e-3}, {"bg_sub": 0}, {"bg_sub": 1, "use_std": True}])
