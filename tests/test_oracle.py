@@ -97,3 +97,47 @@ def test_ls_deconv_decreases_objective(oracle):
         x = oracle.LS_deconv(fwd, bwd, Htf, {"max_iter": it})
         objs.append(np.sum((y - fwd(x)) ** 2))
     assert objs[2] < objs[1] < objs[0]
+
+
+def _sparse_nnls_problem(seed, P=600, K=40, F=8, dens=0.05):
+    rng = np.random.default_rng(seed)
+    A = rng.random((P, K)) * (rng.random((P, K)) < dens)
+    A[rng.integers(0, P, K), np.arange(K)] += 1.0  # no empty column
+    T = rng.random((K, F)) * (rng.random((K, F)) < 0.5)
+    Y = A @ T + 0.01 * rng.standard_normal((P, F))
+    return A, Y
+
+
+def _kkt(A, Y, X, lam=0.0):
+    g = A.T @ (A @ X - Y) + lam
+    scale = np.abs(A.T @ Y).max()
+    return float(np.abs(np.where(X > 0, g, np.minimum(g, 0))).max() / scale)
+
+
+@pytest.mark.parametrize("solver", ["fast_nnls", "LS_nnls"])
+def test_oracle_nnls_reaches_scipy_optimum(oracle, solver):
+    """fast_nnls.m / LS_nnls.m restated: on a well-conditioned problem the
+    retired columns sit at the NNLS optimum of an independent solver."""
+    from scipy.optimize import nnls
+    A, Y = _sparse_nnls_problem(1)
+    if solver == "fast_nnls":
+        X = oracle.fast_nnls(A, Y, {})[0]
+    else:
+        X = oracle.LS_nnls(A, Y, {})[0]
+    Xs = np.stack([nnls(A, Y[:, j])[0] for j in range(Y.shape[1])], axis=1)
+    assert np.linalg.norm(X - Xs) / np.linalg.norm(Xs) < 1e-4
+    assert X.min() >= 0 and _kkt(A, Y, X) < 1e-4
+
+
+@pytest.mark.parametrize("solver", ["fast_nnls", "LS_nnls"])
+def test_oracle_nnls_lambda_is_l1_weight(oracle, solver):
+    """opts.lambda enters as h = A'Y - lambda (LS_nnls.m:76) or
+    df = diag(h)(-A'Y + lambda) (fast_nnls.m:57): both minimise
+    0.5 ||A x - y||^2 + lambda * sum(x) over x >= 0."""
+    A, Y = _sparse_nnls_problem(2)
+    lam = 0.05
+    if solver == "fast_nnls":
+        X = oracle.fast_nnls(A, Y, {"lambda": lam})[0]
+    else:
+        X = oracle.LS_nnls(A, Y, {"lambda": lam})[0]
+    assert X.min() >= 0 and _kkt(A, Y, X, lam) < 1e-4
