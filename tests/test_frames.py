@@ -54,6 +54,36 @@ def test_tiff_roundtrip(tmp_path, dtype, comp, pred, bo):
     np.testing.assert_array_equal(read_tiff(p), img)
 
 
+@pytest.mark.parametrize("xc,yc,dx,M", [(100.3, 90.7, 15.2, 15), (57.0, 61.0, 15.0, 15), (99.5, 80.25, 11.7, 11)])
+def test_oracle_image_rect_pinned(oracle, xc, yc, dx, M):
+    """ImageRect.m:7-45 restated, against its definition: rectifying the images
+    x and y themselves (bilinear interpolation reproduces them exactly) recovers
+    the query grid, which steps dx/M, holds whole lenslets and puts the given
+    centre on the middle pixel of its lenslet; the interpolation of a random
+    image equals scipy's linear grid interpolator, NaN outside."""
+    from scipy.interpolate import RegularGridInterpolator
+    rows, cols = 181, 203
+    xs = np.tile(np.arange(1.0, cols + 1), (rows, 1))
+    ys = np.tile(np.arange(1.0, rows + 1)[:, None], (1, cols))
+    gx = oracle.image_rect(xs, xc, yc, dx, M, crop=False)
+    gy = oracle.image_rect(ys, xc, yc, dx, M, crop=False)
+    xq = gx[np.isfinite(gx).any(axis=1)][0]
+    yq = gy[:, np.isfinite(gy).any(axis=0)][:, 0]
+    for q, c in ((xq, xc), (yq, yc)):
+        assert q.size % M == 0
+        f = q[np.isfinite(q)]
+        np.testing.assert_allclose(np.diff(f), dx / M, rtol=1e-9)
+        i = int(np.argmin(np.abs(np.nan_to_num(q, nan=-1e9) - (c + 1))))
+        assert abs(q[i] - (c + 1)) < 1e-9 and i % M == M // 2
+    img = np.random.default_rng(0).random((rows, cols))
+    out = oracle.image_rect(img, xc, yc, dx, M, crop=False)
+    fin = np.isfinite(yq)[:, None] & np.isfinite(xq)[None, :]
+    assert np.array_equal(np.isfinite(out), fin)
+    Yq, Xq = np.meshgrid(yq, xq, indexing="ij")
+    ref = RegularGridInterpolator((np.arange(1.0, rows + 1), np.arange(1.0, cols + 1)), img)
+    np.testing.assert_allclose(out[fin], ref(np.stack([Yq[fin], Xq[fin]], axis=1)), rtol=1e-12, atol=1e-12)
+
+
 def test_rect_size_matches_oracle(sidlib, oracle):
     for rows, cols, xc, yc, dx, M, cuts in [(300, 310, 148.3, 151.7, 15.06, 15, (1, 2, 0, 1)),
                                             (200, 180, 90.0, 100.0, 14.8, 15, (0, 0, 0, 0)),
