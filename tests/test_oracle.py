@@ -141,3 +141,25 @@ def test_oracle_nnls_lambda_is_l1_weight(oracle, solver):
     else:
         X = oracle.LS_nnls(A, Y, {"lambda": lam})[0]
     assert X.min() >= 0 and _kkt(A, Y, X, lam) < 1e-4
+
+
+def test_rl_poisson_is_em(oracle):
+    """Richardson-Lucy is the EM algorithm of the Poisson likelihood: every
+    iteration keeps sum(A x) = sum(y) (x_new = x A'(y/Ax) / A'1) and does not
+    lower sum(y log(Ax) - Ax)."""
+    rng = np.random.default_rng(8)
+    M, N, Z, X = 9, 3, 2, 12
+    H = rng.random((M, M, N, N, Z)).astype(np.float32)
+    fwd = lambda v: oracle.forward_project(H, v)  # noqa: E731
+    bwd = lambda i: oracle.backward_project(H, i)  # noqa: E731
+    y = rng.poisson(50.0 * fwd(rng.random((X, X, Z)))).astype(np.float64)
+    x = np.full((X, X, Z), 0.5)
+    prev = None
+    for _ in range(6):
+        x = oracle.rl_poisson(fwd, bwd, y, 1, x)
+        ax = fwd(x)
+        assert abs(ax.sum() - y.sum()) <= 1e-9 * y.sum()
+        ll = float(np.sum(y * np.log(ax) - ax))
+        if prev is not None:
+            assert ll >= prev - 1e-9 * abs(prev)
+        prev = ll
