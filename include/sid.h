@@ -391,10 +391,22 @@ int sid_pinv_destroy(sid_pinv* q);
  * without a context: split-K partials live in a fixed 16 MiB device array
  * compiled into libsid, so K is limited to 2048 (SID_EINVAL beyond).  The
  * array is shared by every call and keeps the last call's contents; calls
- * whose kernels overlap on the GPU race on it.  The first call on a device
- * looks the array up (cudaGetSymbolAddress) and should precede any stream
- * capture.  A: P x K single, G: K x K single (device). */
+ * whose kernels overlap on the GPU race on it.  The first call in a CUDA
+ * context looks the array up (cudaGetSymbolAddress) and should precede any
+ * stream capture; the address is kept per context (driver context ID), so a
+ * device reset or a second context on the device looks it up again.
+ * A: P x K single, G: K x K single (device). */
 int sid_gram_noalloc(const float* A, int64_t P, int64_t K, float* G, void* stream);
+
+/* ---- Self-test of the bounded device waits --------------------------------------
+ * No counterpart in the reference (library diagnostics).  Runs one CTA shaped
+ * like a tensor-core pipeline at its abort point (TMEM held, one mbarrier, no
+ * copies or MMAs in flight) whose waiter polls the mbarrier at most `polls`
+ * times (1..2^20).  arrive = 0: nobody arrives, the wait runs out, the kernel
+ * frees TMEM and returns, and the call returns SID_ETIMEOUT (the mapping every
+ * pipelined entry point uses).  arrive = 1: the barrier completes and the call
+ * returns SID_OK.  Synchronises the device. */
+int sid_selftest_wait_timeout(uint32_t polls, int arrive);
 
 #ifdef __cplusplus
 }

@@ -24,8 +24,8 @@ k_sgemm_tn(const float* __restrict__ A, const float* __restrict__ B, float* __re
     __shared__ __align__(16) float Bs[2][SG_BK][SG_BN + 4];
     const int tid = threadIdx.x;
     const int m0 = blockIdx.x * SG_BM, n0 = blockIdx.y * SG_BN;
-    const int kbeg = blockIdx.z * kb_per * SG_BK;
-    const int kend = min(k, kbeg + kb_per * SG_BK);
+    const int64_t kbeg = (int64_t)blockIdx.z * kb_per * SG_BK;
+    const int64_t kend = min((int64_t)k, kbeg + (int64_t)kb_per * SG_BK);
     // loader mapping: 256 threads x 8 values = 128 rows x 16 k
     const int lr = tid >> 1;            // row (m or n) 0..127
     const int lk = (tid & 1) * 8;       // k offset 0 or 8
@@ -38,11 +38,11 @@ k_sgemm_tn(const float* __restrict__ A, const float* __restrict__ B, float* __re
         for (int j = 0; j < 8; ++j) acc[i][j] = 0.f;
 
     float ra[8], rb[8];
-    auto gload = [&](int k0) {
+    auto gload = [&](int64_t k0) {
         const int gm = m0 + lr, gn = n0 + lr;
 #pragma unroll
         for (int e = 0; e < 8; ++e) {
-            const int kk = k0 + lk + e;
+            const int64_t kk = k0 + lk + e;
             ra[e] = (gm < m && kk < kend) ? A[(int64_t)gm * lda + kk] : 0.f;
             rb[e] = (gn < n && kk < kend) ? B[(int64_t)gn * ldb + kk] : 0.f;
         }
@@ -60,7 +60,7 @@ k_sgemm_tn(const float* __restrict__ A, const float* __restrict__ B, float* __re
         sstore(0);
     }
     __syncthreads();
-    for (int k0 = kbeg; k0 < kend; k0 += SG_BK) {
+    for (int64_t k0 = kbeg; k0 < kend; k0 += SG_BK) {
         const bool more = k0 + SG_BK < kend;
         if (more) gload(k0 + SG_BK);
 #pragma unroll
@@ -118,7 +118,7 @@ int sgemm_tn(const float* A, const float* B, int64_t m, int64_t n, int64_t k, in
     const int64_t tiles = cdiv(m, SG_BM) * cdiv(n, SG_BN);
     const int64_t nkb = cdiv(k, SG_BK);
     int splitk = 1;
-    while (tiles * splitk < 4 * 152 && nkb / (splitk + 1) >= 16) ++splitk;
+    while (tiles * splitk < 4 * sm_count() && nkb / (splitk + 1) >= 16) ++splitk;
     const int kb_per = (int)cdiv(nkb, splitk);
     splitk = (int)cdiv(nkb, kb_per);
     const bool direct = splitk == 1 && alpha == 1.f && beta == 0.f;
@@ -145,7 +145,7 @@ int64_t sgemm_ws_elems(int64_t m, int64_t n, int64_t k)
     const int64_t tiles = cdiv(m, SG_BM) * cdiv(n, SG_BN);
     const int64_t nkb = cdiv(k, SG_BK);
     int splitk = 1;
-    while (tiles * splitk < 4 * 152 && nkb / (splitk + 1) >= 16) ++splitk;
+    while (tiles * splitk < 4 * sm_count() && nkb / (splitk + 1) >= 16) ++splitk;
     return (int64_t)splitk * m * n;
 }
 

@@ -19,11 +19,15 @@
 //     threads) race on it and must be serialised by the caller;
 //   * every call overwrites each partial it later reads, so nothing in the
 //     array has to start at zero;
-//   * the first call on a device looks the array's address up with
+//   * the first call in a CUDA context looks the array's address up with
 //     cudaGetSymbolAddress (host code cannot use the array's name as a device
-//     address); make that first call before any stream capture.
-#include <mutex>
+//     address) and keeps it for that context; make that first call before any
+//     stream capture.  The address is keyed by the driver's context ID, so a
+//     device reset (MATLAB's reset(gpuDevice)) or a second context on the same
+//     device looks it up again instead of reusing a stale address.
+#include <cuda.h>
 
+#include "ctx_cache.h"
 #include "sid_internal.cuh"
 
 namespace sid {
@@ -37,32 +41,76 @@ __global__ void k_splitk_reduce_simt(const float* __restrict__ part, int nsplit,
 constexpr int64_t kNoAllocScratchFloats = 4 * 1024 * 1024;  // 16 MiB
 constexpr int64_t kNoAllocMaxK = 2048;                      // 2048^2 floats = the whole array
 constexpr int kNaBM = 128, kNaBN = 128, kNaBK = 16;         // tile of k_sgemm_tn
-constexpr int kMaxDevices = 64;
 
 static __device__ __align__(256) float g_noalloc_scratch[kNoAllocScratchFloats];
 
-static std::mutex g_noalloc_mu;
-static float* g_noalloc_ptr[kMaxDevices] = {};
+static CtxCache<float*> g_noalloc_cache;
 
-// Device address of g_noalloc_scratch on the current device (looked up once).
-static int noalloc_scratch(float** out)
+using PfnCtxGetCurrent = CUresult (*)(CUcontext*);
+using PfnCtxGetId = CUresult (*)(CUcontext, unsigned long long*);
+
+// Unique ID of the context current on this thread (binding the device's primary
+// context first if the runtime has not yet done so on this thread).
+static int current_context_id(unsigned long long* id)
 {
-    int dev = -1;
-    SID_CUDA_TRY(cudaGetDevice(&dev));
-    SID_REQUIRE(dev >= 0 && dev < kMaxDevices, "sid_gram_noalloc: device ordinal %d out of range", dev);
-    std::lock_guard<std::mutex> lk(g_noalloc_mu);
-    if (!g_noalloc_ptr[dev]) {
+    static std::once_flag once;
+    static PfnCtxGetCurrent get_current = nullptr;
+    static PfnCtxGetId get_id = nullptr;
+    std::call_once(once, [] {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_current = reinterpret_cast<PfnCtxGetCurrent>(f);
+        f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = reinterpret_cast<PfnCtxGetId>(f);
+    });
+    if (!get_current || !get_id) {
+        set_error("sid_gram_noalloc: cuCtxGetCurrent/cuCtxGetId are not available from the driver");
+        return SID_ECUDA;
+    }
+    CUcontext ctx = nullptr;
+    if (get_current(&ctx) != CUDA_SUCCESS) {
+        set_error("sid_gram_noalloc: cuCtxGetCurrent failed");
+        return SID_ECUDA;
+    }
+    if (!ctx) {
+        // no context bound to this thread yet: a runtime call that needs one binds the primary context
         void* p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess || !p) {
-            set_error("sid_gram_noalloc: cudaGetSymbolAddress of the scratch array failed: %s",
-                      cudaGetErrorString(e));
+        SID_CUDA_TRY(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+        if (get_current(&ctx) != CUDA_SUCCESS || !ctx) {
+            set_error("sid_gram_noalloc: no CUDA context is current");
             return SID_ECUDA;
         }
-        g_noalloc_ptr[dev] = static_cast<float*>(p);
     }
-    *out = g_noalloc_ptr[dev];
+    if (get_id(ctx, id) != CUDA_SUCCESS) {
+        set_error("sid_gram_noalloc: cuCtxGetId failed");
+        return SID_ECUDA;
+    }
     return SID_OK;
+}
+
+// Device address of g_noalloc_scratch in the current context (looked up once per context).
+static int noalloc_scratch(float** out)
+{
+    unsigned long long id = 0;
+    SID_TRY(current_context_id(&id));
+    return g_noalloc_cache.get(
+        id,
+        [](float** v) -> int {
+            void* p = nullptr;
+            cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+            if (e != cudaSuccess || !p) {
+                set_error("sid_gram_noalloc: cudaGetSymbolAddress of the scratch array failed: %s",
+                          cudaGetErrorString(e));
+                return SID_ECUDA;
+            }
+            *v = static_cast<float*>(p);
+            return SID_OK;
+        },
+        out);
 }
 
 }  // namespace sid
@@ -86,7 +134,7 @@ extern "C" int sid_gram_noalloc(const float* A, int64_t P, int64_t K, float* G, 
     const int64_t nkb = cdiv(P, kNaBK);
     const int64_t cap = kNoAllocScratchFloats / (K * K);
     int64_t splitk = 1;
-    while (tiles * splitk < 4 * 152 && nkb / (splitk + 1) >= 16 && splitk + 1 <= cap) ++splitk;
+    while (tiles * splitk < 4 * sm_count() && nkb / (splitk + 1) >= 16 && splitk + 1 <= cap) ++splitk;
     const int64_t kb_per = cdiv(nkb, splitk);
     splitk = cdiv(nkb, kb_per);
     const int64_t sstride = K * K;

@@ -9,6 +9,7 @@
 #include <climits>
 #include <cstdarg>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 #include "sid_internal.cuh"
@@ -26,6 +27,21 @@ void set_error(const char* fmt, ...)
 }
 
 int build_spectra(sid_plan* p);  // spectral.cu
+
+int sm_count()
+{
+    static std::mutex mu;
+    static int cached[64] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 152;
+    std::lock_guard<std::mutex> lk(mu);
+    if (!cached[dev]) {
+        int n = 0;
+        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 152;
+        cached[dev] = n;
+    }
+    return cached[dev];
+}
 
 // Tap builder.  One thread per tap; `adj_layout` selects [c][b][b'][a'][a]
 // block order (adjoint kernels) instead of [c][b][a][b'][a'] (forward kernels).

@@ -53,6 +53,10 @@ void set_error(const char* fmt, ...);
     } while (0)
 
 inline int64_t cdiv(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+// Streaming multiprocessors of the current device (cudaDevAttrMultiProcessorCount,
+// looked up once per device ordinal; 152 on GB300).
+int sm_count();
 inline int64_t floordiv(int64_t a, int64_t b) { return (a >= 0) ? a / b : -((-a + b - 1) / b); }
 inline int64_t ceildiv_signed(int64_t a, int64_t b) { return -floordiv(-a, b); }
 
