@@ -54,13 +54,18 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity)
 }
 
 // Bounded wait on an mbarrier phase.  Returns false (and records the error)
-// if the phase did not complete within the budget.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err)
+// if the phase did not complete within `limit` polls.
+__device__ __forceinline__ bool mbar_wait_n(uint64_t* bar, uint32_t parity, int* err, uint32_t limit)
 {
-    for (uint32_t it = 0; it < kSpinLimit; ++it)
+    for (uint32_t it = 0; it < limit; ++it)
         if (mbar_try_wait(bar, parity)) return true;
     if (err) atomicExch(err, kErrTimeoutMbar);
     return false;
+}
+
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err)
+{
+    return mbar_wait_n(bar, parity, err, kSpinLimit);
 }
 
 // 1-D bulk copy global -> shared through the TMA engine, completion counted

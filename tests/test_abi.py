@@ -75,7 +75,8 @@ def test_every_entry_point_rejects_null_arguments(sidlib):
         for t in _lib.SIGNATURES[name]:
             if t in (ctypes.c_double, ctypes.c_float):
                 args.append(0.0)
-            elif t in (ctypes.c_int, ctypes.c_int32, ctypes.c_int64, ctypes.c_long, ctypes.c_longlong):
+            elif t in (ctypes.c_int, ctypes.c_int32, ctypes.c_int64, ctypes.c_long, ctypes.c_longlong,
+                       ctypes.c_uint32):
                 args.append(0)
             else:
                 args.append(None)
