@@ -50,6 +50,8 @@ def parse():
     ap.add_argument("--no-nnls", action="store_true", help="skip the library + temporal NNLS measurement")
     ap.add_argument("--nnls-frames", type=int, default=3000)
     ap.add_argument("--nnls-neurons", type=int, default=800)
+    ap.add_argument("--nnls-fp64-frames", type=int, default=192,
+                    help="frames of the temporal NNLS solved again in FP64 (oracle) for the accuracy fields")
     return ap.parse_args()
 
 
@@ -151,41 +153,24 @@ class Clocks:
                 "samples": len(sm)}
 
 
-def nnls_workload(args, P_proj):
-    """Library generation (800 anisotropic Gaussian neurons, sigma_xy U(2,4),
-    sigma_z U(1,2), uniform in the 1005^2 x 31 volume) followed by the temporal
-    NNLS of 3000 FP16 frames Y = S'T + b + noise (SNR 10), T sparse exponential
-    transients (0.5 Hz events at 20 Hz, tau 0.3 s).  Times fast_nnls (the SID
-    temporal update, temporal_SID_update.m:45) at split tensor-core precision
-    and at FP32, and the Gram / cross contractions on their own."""
+def nnls_inputs(P_proj, K, F):
+    """Library generation (K anisotropic Gaussian neurons in the projector's
+    volume, generate_LFM_library_GPU.m:63-109, through the plan's lenslet taps,
+    timed) and the temporal NNLS movie Y = S'T + b + noise from it (FP16 and
+    FP32 copies).  Returns (A (P x K, L2-normalised columns), Y16, Yf, T_true,
+    library ms)."""
+    import ctypes
+
     import numpy as np
     import torch
 
     import sid_gb300 as s
-    from sid_gb300 import synthetic
-    K, F = args.nnls_neurons, args.nnls_frames
+    from sid_gb300 import _lib, synthetic
     X, Y, Z = P_proj.X, P_proj.Y, P_proj.Z
     P = X * Y
-    rng = np.random.default_rng(5)
-    cx, cy, cz = rng.uniform(1, X, K), rng.uniform(1, Y, K), rng.uniform(1, Z, K)
-    sxy, sz = rng.uniform(2, 4, K), rng.uniform(1, 2, K)
-    vol = np.zeros((X, Y, Z), dtype=np.float32, order="F")
-    for k in range(K):
-        r, rz = int(np.ceil(3 * sxy[k])), int(np.ceil(3 * sz[k]))
-        x0, x1 = max(int(cx[k]) - 1 - r, 0), min(int(cx[k]) + r, X)
-        y0, y1 = max(int(cy[k]) - 1 - r, 0), min(int(cy[k]) + r, Y)
-        z0, z1 = max(int(cz[k]) - 1 - rz, 0), min(int(cz[k]) + rz, Z)
-        gx = np.exp(-0.5 * ((np.arange(x0, x1) + 1 - cx[k]) / sxy[k]) ** 2)
-        gy = np.exp(-0.5 * ((np.arange(y0, y1) + 1 - cy[k]) / sxy[k]) ** 2)
-        gz = np.exp(-0.5 * ((np.arange(z0, z1) + 1 - cz[k]) / sz[k]) ** 2)
-        vol[x0:x1, y0:y1, z0:z1] += (gx[:, None, None] * gy[None, :, None] * gz[None, None, :]).astype(np.float32)
-    centers = np.stack([cx, cy, cz], 1)
+    vol, centers = synthetic.neuron_volume(X, Y, Z, K)
     neur_id = np.ones((K, 1), dtype=bool)
-    opts = {"neur_rad": 12, "axial": 2.0}
     recon = [s.to_device(vol)]
-    # library through the bench's plan (direct taps)
-    import ctypes
-    from sid_gb300 import _lib
     A = s.lfm._fortran_tensor((P, K), "cuda")
     ptrs = (ctypes.c_void_p * 1)(recon[0].data_ptr())
     c = np.asfortranarray(centers)
@@ -201,23 +186,60 @@ def nnls_workload(args, P_proj):
     # L2-normalise library rows (temporal_SID_update.m:42)
     nrm = torch.linalg.vector_norm(A, dim=0)
     A.div_(nrm.clamp_min(1e-30))
-    # T_true: events at 0.5 Hz (p = 0.025 per 20 Hz frame), exponential kernel tau = 6 frames
-    g = torch.Generator(device="cuda").manual_seed(7)
-    ev = (torch.rand(K, F, generator=g, device="cuda") < 0.025).float() * (0.5 + torch.rand(K, F, generator=g,
-                                                                                              device="cuda"))
-    kern = torch.exp(-torch.arange(0, 40, device="cuda", dtype=torch.float32) / 6.0)
-    T = torch.nn.functional.conv1d(ev[:, None, :], kern.flip(0)[None, None, :], padding=39)[:, 0, :F]
-    sig = (A.T.contiguous().T @ T)  # synthetic movie (data generation, not the measured path)
-    rms = sig.pow(2).mean().sqrt()
-    Yf = sig + 0.1 * rms + 0.1 * rms * torch.randn(sig.shape, generator=g, device="cuda")
-    del sig
-    Y16 = Yf.half()
-    Yf = Yf.T.contiguous().T  # column-major P x F
-    Y16 = Y16.T.contiguous().T
+    Y16, Yf, T = synthetic.transient_movie(A, F)
+    return A, Y16, Yf, T, min(lib_ms)
+
+
+def nnls_fp64_reference(A, Y16, cols, opts=None):
+    """FP64 fast_nnls on the frames `cols` of the FP16 movie: the Gram A'A and
+    the cross product A'Y(:, cols) formed in FP64 (torch FP64 products on the
+    device, pixel chunks), the iterations by the oracle's FP64 restatement
+    (fast_nnls.m:53-199) on the host.  Columns are independent problems, so a
+    frame sample checks the whole solve."""
+    import numpy as np
+    import torch
+
+    from oracle import oracle
+    P, K = A.shape
+    Q = torch.zeros(K, K, dtype=torch.float64, device=A.device)
+    c = torch.zeros(K, len(cols), dtype=torch.float64, device=A.device)
+    idx = torch.as_tensor(np.asarray(cols), device=A.device)
+    step = 1 << 17
+    for p0 in range(0, P, step):
+        a = A[p0:p0 + step].double()
+        Q += a.T @ a
+        c += a.T @ Y16[p0:p0 + step].index_select(1, idx).double()
+    Q = Q.cpu().numpy()
+    c = c.cpu().numpy()
+    dq = np.sqrt(np.diag(Q))
+    h = 1.0 / dq
+    Qn = Q / np.outer(dq, dq)
+    lam = float((opts or {}).get("lambda", 0.0))
+    df = h[:, None] * (-c + lam)
+    xx, _, _, _, it = oracle.fast_nnls(np.zeros((0, K)), np.zeros((0, len(cols))), opts, Qn, df, h,
+                                       return_iters=True)
+    return xx, it
+
+
+def nnls_workload(args, P_proj):
+    """Library generation (800 anisotropic Gaussian neurons, sigma_xy U(2,4),
+    sigma_z U(1,2), uniform in the 1005^2 x 31 volume) followed by the temporal
+    NNLS of 3000 FP16 frames Y = S'T + b + noise (SNR 10), T sparse exponential
+    transients (0.5 Hz events at 20 Hz, tau 0.3 s).  Times fast_nnls (the SID
+    temporal update, temporal_SID_update.m:45) at split tensor-core precision
+    and at FP32, and the Gram / cross contractions on their own; checks both
+    solves against FP64 on a frame sample."""
+    import numpy as np
+    import torch
+
+    import sid_gb300 as s
+    K, F = args.nnls_neurons, args.nnls_frames
+    P = P_proj.X * P_proj.Y
+    A, Y16, Yf, T, lib_ms = nnls_inputs(P_proj, K, F)
     ctx = s.Context()
     out = {"workload": f"library {K} neurons (cfg2) + temporal NNLS {K} x {F} frames, P = {P} (cfg3), FP16 movie"}
-    out["library_ms"] = min(lib_ms)
-    out["library_neurons_per_s"] = K / (min(lib_ms) / 1e3)
+    out["library_ms"] = lib_ms
+    out["library_neurons_per_s"] = K / (lib_ms / 1e3)
 
     def timed(fn, reps=1):
         torch.cuda.synchronize()
@@ -275,6 +297,18 @@ def nnls_workload(args, P_proj):
     out["split_vs_fp32_speedup"] = t_fp32 / t_split
     out["rel_l2_split_vs_fp32"] = float(torch.linalg.norm(Xs - X32) / torch.linalg.norm(X32))
     out["rel_l2_vs_T_true"] = float(torch.linalg.norm(Xs - T) / torch.linalg.norm(T))
+    if args.nnls_fp64_frames > 0:
+        cols = np.sort(np.random.default_rng(11).choice(F, min(F, args.nnls_fp64_frames), replace=False))
+        t0 = time.perf_counter()
+        x64, it64 = nnls_fp64_reference(A, Y16, cols)
+        ci = torch.as_tensor(cols, device=A.device)
+
+        def err(Xg):
+            g = Xg.index_select(1, ci).double().cpu().numpy()
+            return float(np.linalg.norm(g - x64) / np.linalg.norm(x64))
+        out["fp64_check"] = {"frames": len(cols), "seconds": time.perf_counter() - t0,
+                             "iters_median": float(np.median(it64)), "iters_max": int(it64.max()),
+                             "rel_l2_split_vs_fp64": err(Xs), "rel_l2_fp32_vs_fp64": err(X32)}
     # one NMF refinement round on the same factors (fast_NMF.m:185-186): S = the
     # library rows (P x K), T = the temporal NNLS result (K x F), split precision
     ctx.t_update(Y16, Xs, A, {"lamb_temp": 0.01})

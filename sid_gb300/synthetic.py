@@ -83,3 +83,47 @@ def poisson_image(I: np.ndarray, scale=1000.0, seed=2) -> np.ndarray:
     """Poisson-noised sensor image (counts / scale)."""
     rng = np.random.default_rng(seed)
     return np.asfortranarray((rng.poisson(np.maximum(I, 0) * scale) / scale).astype(np.float32))
+
+
+def neuron_volume(X: int, Y: int, Z: int, K: int, seed=5):
+    """K anisotropic Gaussian neuron footprints (sigma_xy U(2,4), sigma_z U(1,2)
+    voxels, boxes of +-3 sigma) at uniform positions in an X x Y x Z volume,
+    summed into one float32 volume.  Returns (volume, centers (K x 3, 1-based
+    MATLAB coordinates))."""
+    rng = np.random.default_rng(seed)
+    cx, cy, cz = rng.uniform(1, X, K), rng.uniform(1, Y, K), rng.uniform(1, Z, K)
+    sxy, sz = rng.uniform(2, 4, K), rng.uniform(1, 2, K)
+    vol = np.zeros((X, Y, Z), dtype=np.float32, order="F")
+    for k in range(K):
+        r, rz = int(np.ceil(3 * sxy[k])), int(np.ceil(3 * sz[k]))
+        x0, x1 = max(int(cx[k]) - 1 - r, 0), min(int(cx[k]) + r, X)
+        y0, y1 = max(int(cy[k]) - 1 - r, 0), min(int(cy[k]) + r, Y)
+        z0, z1 = max(int(cz[k]) - 1 - rz, 0), min(int(cz[k]) + rz, Z)
+        gx = np.exp(-0.5 * ((np.arange(x0, x1) + 1 - cx[k]) / sxy[k]) ** 2)
+        gy = np.exp(-0.5 * ((np.arange(y0, y1) + 1 - cy[k]) / sxy[k]) ** 2)
+        gz = np.exp(-0.5 * ((np.arange(z0, z1) + 1 - cz[k]) / sz[k]) ** 2)
+        vol[x0:x1, y0:y1, z0:z1] += (gx[:, None, None] * gy[None, :, None] * gz[None, None, :]).astype(np.float32)
+    return vol, np.stack([cx, cy, cz], 1)
+
+
+def transient_movie(A, F: int, seed=7, event_rate=0.025, tau_frames=6.0, snr=10.0):
+    """Temporal NNLS inputs on the GPU from a library A (P x K, CUDA float32,
+    column-major): T_true (K x F) of sparse exponential transients (events with
+    probability `event_rate` per frame -- 0.5 Hz at 20 Hz --, amplitudes
+    U(0.5, 1.5), decay tau_frames = 0.3 s), and the movie Y = A T_true + b + noise
+    with a constant background b = rms/snr and Gaussian noise of deviation
+    rms/snr.  Returns (Y16 half, Yf float32, T_true), Y column-major P x F."""
+    import torch
+    K = A.shape[1]
+    g = torch.Generator(device=A.device).manual_seed(seed)
+    ev = (torch.rand(K, F, generator=g, device=A.device) < event_rate).float() * \
+        (0.5 + torch.rand(K, F, generator=g, device=A.device))
+    kern = torch.exp(-torch.arange(0, 40, device=A.device, dtype=torch.float32) / tau_frames)
+    T = torch.nn.functional.conv1d(ev[:, None, :], kern.flip(0)[None, None, :], padding=39)[:, 0, :F]
+    sig = A.T.contiguous().T @ T
+    rms = sig.pow(2).mean().sqrt()
+    Yf = sig + rms / snr + rms / snr * torch.randn(sig.shape, generator=g, device=A.device)
+    del sig
+    Y16 = Yf.half().T.contiguous().T
+    Yf = Yf.T.contiguous().T
+    return Y16, Yf, T
