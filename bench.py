@@ -195,7 +195,12 @@ def nnls_fp64_reference(A, Y16, cols, opts=None):
     the cross product A'Y(:, cols) formed in FP64 (torch FP64 products on the
     device, pixel chunks), the iterations by the oracle's FP64 restatement
     (fast_nnls.m:53-199) on the host.  Columns are independent problems, so a
-    frame sample checks the whole solve."""
+    frame sample checks the whole solve.  Also runs the FP64 solve a second
+    time with the normalised Gram formed as diag(h)*Q*diag(h) instead of
+    Q./sqrt(diag*diag') (the two differ only in the last bit of some entries):
+    the distance between the two FP64 results is the spread that rounding
+    alone causes on this problem.  Returns (x64, iterations, x64 of the second
+    form, unnormalised FP64 Gram, FP64 cross product)."""
     import numpy as np
     import torch
 
@@ -213,12 +218,27 @@ def nnls_fp64_reference(A, Y16, cols, opts=None):
     c = c.cpu().numpy()
     dq = np.sqrt(np.diag(Q))
     h = 1.0 / dq
-    Qn = Q / np.outer(dq, dq)
     lam = float((opts or {}).get("lambda", 0.0))
     df = h[:, None] * (-c + lam)
-    xx, _, _, _, it = oracle.fast_nnls(np.zeros((0, K)), np.zeros((0, len(cols))), opts, Qn, df, h,
-                                       return_iters=True)
-    return xx, it
+    empty_a, empty_y = np.zeros((0, K)), np.zeros((0, len(cols)))
+    xx, _, _, _, it = oracle.fast_nnls(empty_a, empty_y, opts, Q / np.outer(dq, dq), df, h, return_iters=True)
+    xx2, _, _, _ = oracle.fast_nnls(empty_a, empty_y, opts, (h[:, None] * Q) * h[None, :], df, h)
+    return xx, it, xx2, Q, c
+
+
+def nnls_accuracy(T, x64, Q, c):
+    """Distances of a solve T (K x n frames) from the FP64 solve x64 of the same
+    frames: in the iterate (rel-L2), in data space (||A(T - x64)|| / ||A x64||,
+    through the FP64 Gram Q = A'A) and in the objective the solve lowers,
+    f(t) = t'Qt/2 - c't (= ||y - At||^2/2 up to a constant; max and median
+    over frames of |f(T) - f(x64)| / |f(x64)|)."""
+    import numpy as np
+    D = T - x64
+    f = lambda X: 0.5 * np.einsum("kf,kl,lf->f", X, Q, X) - np.einsum("kf,kf->f", c, X)  # noqa: E731
+    obj = np.abs(f(T) - f(x64)) / np.abs(f(x64))
+    return {"iterate_rel_l2": float(np.linalg.norm(D) / np.linalg.norm(x64)),
+            "data_rel_l2": float(np.sqrt(np.einsum("kf,kl,lf->", D, Q, D) / np.einsum("kf,kl,lf->", x64, Q, x64))),
+            "objective_rel_max": float(obj.max()), "objective_rel_median": float(np.median(obj))}
 
 
 def nnls_workload(args, P_proj):
@@ -300,15 +320,17 @@ def nnls_workload(args, P_proj):
     if args.nnls_fp64_frames > 0:
         cols = np.sort(np.random.default_rng(11).choice(F, min(F, args.nnls_fp64_frames), replace=False))
         t0 = time.perf_counter()
-        x64, it64 = nnls_fp64_reference(A, Y16, cols)
+        x64, it64, x64b, Q64, c64 = nnls_fp64_reference(A, Y16, cols)
         ci = torch.as_tensor(cols, device=A.device)
-
-        def err(Xg):
-            g = Xg.index_select(1, ci).double().cpu().numpy()
-            return float(np.linalg.norm(g - x64) / np.linalg.norm(x64))
-        out["fp64_check"] = {"frames": len(cols), "seconds": time.perf_counter() - t0,
-                             "iters_median": float(np.median(it64)), "iters_max": int(it64.max()),
-                             "rel_l2_split_vs_fp64": err(Xs), "rel_l2_fp32_vs_fp64": err(X32)}
+        ev = np.linalg.eigvalsh(Q64 / np.sqrt(np.outer(np.diag(Q64), np.diag(Q64))))
+        sub = lambda Xg: Xg.index_select(1, ci).double().cpu().numpy()  # noqa: E731
+        out["fp64_check"] = {
+            "frames": len(cols), "seconds": time.perf_counter() - t0,
+            "iters_median": float(np.median(it64)), "iters_max": int(it64.max()),
+            "normalised_gram_eig_min_max": [float(ev[0]), float(ev[-1])],
+            "split": nnls_accuracy(sub(Xs), x64, Q64, c64),
+            "fp32": nnls_accuracy(sub(X32), x64, Q64, c64),
+            "fp64_second_rounding": nnls_accuracy(x64b, x64, Q64, c64)}
     # one NMF refinement round on the same factors (fast_NMF.m:185-186): S = the
     # library rows (P x K), T = the temporal NNLS result (K x F), split precision
     ctx.t_update(Y16, Xs, A, {"lamb_temp": 0.01})

@@ -130,6 +130,19 @@ int sid_plan_set_kernel(sid_plan* plan, const float* kernel, int64_t kx, int64_t
  * Htf, X: X x Y x Z single (device); X holds Xguess on entry. */
 int sid_deconv_isra(sid_plan* plan, int method, const float* Htf, float* X,
                     int maxIter, float lambda, void* stream);
+
+/* [Xguess, Xguess_history] = deconvRL(forwardFUN, backwardFUN, Htf, maxIter, Xguess, opts)
+ *                                            deconvRL.m:1 (every mode)
+ * mode 0 'basic': lambda3[0] is opts.lambda (p must be 1 when it is nonzero:
+ * p ~= 1 reads the reference's undefined Filter, deconvRL.m:57); mode 1
+ * 'TV': lambda3 is opts.lambda (1 x 3, one weight per axis), pnorm 1
+ * (sign of forward differences, deconvRL.m:67-74) or 2 (7-point filter,
+ * deconvRL.m:75-78); other pnorm values return X unchanged, as the
+ * reference's 'p>2 not supported' return does.  lambda3: 3 floats (host).
+ * history (optional, device): maxIter x X x Y x Z single, Xguess_history
+ * (deconvRL.m:10,90-92). */
+int sid_deconv_isra_ex(sid_plan* plan, int method, const float* Htf, float* X, int maxIter, int mode, int pnorm,
+                       const float* lambda3, float* history, void* stream);
 /* Host-array form of sid_deconv_isra (copies in, iterates, copies X out). */
 int sid_deconv_isra_host(sid_plan* plan, int method, const float* Htf, float* X,
                          int maxIter, float lambda);
@@ -148,6 +161,16 @@ int sid_deconv_rl_poisson(sid_plan* plan, int method, const float* y, float* X, 
  * X: X x Y x Z single (device); holds df = A'y on entry, the solution on exit. */
 int sid_deconv_ls(sid_plan* plan, int method, float* X, int max_iter,
                   float lamb_L1, float lamb_L2, void* stream);
+
+/* Xguess = LS_deconv(forwardFUN, backwardFUN, df, opts) with the TV terms
+ *                                            LS_deconv.m:1
+ * lamb_TV_L2: 3 floats (host), the per-axis weights of the 7-point
+ * Laplacian term convn(X, filter, 'same') in Q (LS_deconv.m:49-62,73);
+ * lamb_TV_L1 enters only the reference's step-length test: alpha comes from
+ * Q itself when lamb_TV_L1 * lamb_TV_L2 * lamb_L2 is nonzero in every
+ * component, else from ||A df_||^2 (LS_deconv.m:82-87). */
+int sid_deconv_ls_ex(sid_plan* plan, int method, float* X, int max_iter, float lamb_L1, float lamb_L2,
+                     const float* lamb_TV_L2, float lamb_TV_L1, void* stream);
 
 /* ---- Library generation -----------------------------------------------------
  * forward_model = generate_LFM_library_GPU(recon, centers, neur_id, psf, options)
@@ -274,14 +297,34 @@ int sid_fast_nnls(sid_ctx* ctx, const float* A, const void* Y, int ydtype, int64
                   const sid_nnls_opts* opts, const float* warm_start, float* X, float* Q_out, int prec,
                   int32_t* iters, void* stream);
 
+/* [xx, Q, df, h] = fast_nnls(A, Y, opts, Q, df, h) with every input and output
+ *                                            fast_nnls.m:1
+ * total: opts.total (one step length for all columns, fast_nnls.m:101-117;
+ * the reference's loop then ends at max_iter without copying x into xx, so X
+ * is diag(h) * ones, and df_out carries the iterations' result).
+ * warm_mode: 0 none; 1 opts.warm_start == 1 (x = inv(Q)(-df) clamped at 0,
+ * fast_nnls.m:66-69; Q singular is SID_EINVAL); 2 opts.warm_start = W (K x F).
+ * Q_in (K x K, normalised) and h_in (K) given together: the caller's Q and h
+ * (fast_nnls.m:58-62, nargin > 3); df_in (K x F): the caller's df.  A and Y
+ * are read only to form what is not given (they may be NULL when Q, h and df
+ * all are).  Outputs (optional except X): Q_out, h_out, and df_out (total
+ * mode; the reference's df has no columns left otherwise). */
+int sid_fast_nnls_ex(sid_ctx* ctx, const float* A, const void* Y, int ydtype, int64_t P, int64_t K, int64_t F,
+                     const sid_nnls_opts* opts, int total, int warm_mode, const float* W, const float* Q_in,
+                     const float* df_in, const float* h_in, float* X, float* Q_out, float* df_out, float* h_out,
+                     int prec, int32_t* iters, void* stream);
+
 /* forward_model = update_spatial_component(timeseries, sensor_movie, template, opts)
  *                                            update_spatial_component.m:1
  * Every template pixel's regularised NNLS (reg_nnls.m:40-69, NQP.m:42-178 with
  * default options, FP64 active set) in one launch.  T: R x F single (the
  * timeseries; with bg_sub the last row is the background); Y: P x F single or
  * half; tmpl: (R - bg_sub) x P uint8 template; forward_model: R x P single
- * (dense).  status (optional, P int32): 0 ok, 1 more than 32 components cover
- * the pixel, 2 NQP iteration cap; SID_ENOCONV if any pixel failed. */
+ * (dense).  Pixels covered by up to 32 components solve with their working
+ * arrays in registers and local memory; more crowded pixels (any number of
+ * components) are listed and solved by a second launch whose working arrays sit
+ * in device scratch.  status (optional, P int32): 0 ok, 2 NQP iteration cap;
+ * SID_ENOCONV if any pixel hit the cap. */
 int sid_spatial_update(sid_ctx* ctx, const float* T, const void* Y, int ydtype, const uint8_t* tmpl, int64_t R,
                        int64_t F, int64_t P, double lamb_L1, double lamb_L2, double lamb_orth_L1, int use_std,
                        int bg_sub, float* forward_model, int32_t* status, void* stream);
@@ -292,11 +335,22 @@ int sid_spatial_update(sid_ctx* ctx, const float* T, const void* Y, int ydtype, 
  * Cholesky factor, FP64, one thread per problem; the solver reg_nnls.m:69 and
  * the spatial update call.  Q: n x n x B (column-major, device), q: n x B;
  * x: n x B; w (optional): n x B, NQP's final w; iters / status (optional, B
- * int32): iterations taken, 0 ok or 2 at the iteration cap.  n <= 32.
+ * int32): iterations taken, 0 ok or 2 at the iteration cap.  n <= 4096 (above
+ * 32 the working arrays of each problem sit in device scratch).
  * SID_ENOCONV if any problem hit the cap (NQP.m:116-119's error).
  * Synchronises the stream. */
 int sid_nqp_batched(sid_ctx* ctx, const double* Q, const double* q, int n, int64_t B, double* x, double* w,
                     int32_t* iters, int32_t* status, void* stream);
+
+/* x = reg_nnls(A, d, opts) (reg_nnls.m:1): min_{x >= 0} ||A x - d||^2 with the
+ * reference's options, as one NQP whose system libsid forms in FP64
+ * (reg_nnls.m:40-66: Q = A'A [- t t'/m] + lamb_L2 I + lamb_orth_L1 hilf,
+ * q = -A'd [+ t sum(d)/m] + lamb_L1, t = column sums of A when use_std) and
+ * solves with the Lawson-Hanson kernel (NQP.m:42-178).  A: m x n double, d: m
+ * double, x: n double (device); hilf: n x n double or NULL (ones - eye, with
+ * the last row and column zero when bg_sub, reg_nnls.m:31-38).  n <= 4096. */
+int sid_reg_nnls(sid_ctx* c, const double* A, int64_t m, int n, const double* d, double lamb_L1, double lamb_L2,
+                 double lamb_orth_L1, int use_std, int bg_sub, const double* hilf, double* x, void* stream);
 
 /* ---- Quantiles and component reconstruction ---------------------------------
  * MATLAB quantile of a vector (sorted non-NaN data at probabilities

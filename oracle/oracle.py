@@ -207,7 +207,8 @@ def deconvRL(forward, backward, Htf, maxIter, Xguess, opts=None):
                     num = Htf + sum(lam3[d] * (_shift(X, d, -1) + _shift(X, d, +1)) for d in range(3))
                     err = num / den
                 else:
-                    raise ValueError("deconvRL: p > 2 not supported")
+                    # deconvRL.m:79-81 prints 'p>2 not supported' and returns Xguess
+                    return X
             else:
                 raise ValueError("deconvRL: unknown mode")
             err[np.isinf(err)] = 0.0
@@ -505,7 +506,8 @@ def fast_nnls(A, Y, opts=None, Q=None, df=None, h=None, return_iters=False):
                 x = x_
                 passive = (x > 0) | (df < 0)
                 if s > max_iter:
-                    xx[:, rds] = x
+                    # fast_nnls.m:112-116 breaks without copying x into xx, so
+                    # the reference returns diag(h) * ones in total mode
                     iters[rds] = s
                     break
                 continue

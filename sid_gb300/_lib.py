@@ -56,6 +56,8 @@ SIGNATURES = {
     "sid_plan_sync": [P, P],
     "sid_deconv_isra": [P, I32, P, P, I32, F32, P],
     "sid_deconv_ls": [P, I32, P, I32, F32, F32, P],
+    "sid_deconv_isra_ex": [P, I32, P, P, I32, I32, I32, P, P, P],
+    "sid_deconv_ls_ex": [P, I32, P, I32, F32, F32, P, F32, P],
     "sid_deconv_isra_host": [P, I32, P, P, I32, F32],
     "sid_deconv_rl_poisson": [P, I32, P, P, I32, P],
     "sid_plan_timing_enable": [P, I32],
@@ -76,12 +78,14 @@ SIGNATURES = {
     "sid_fast_nnls_defaults": [P],
     "sid_ls_nnls": [P, P, P, I32, I64, I64, I64, P, P, I32, P, I32, I32, P, P],
     "sid_fast_nnls": [P, P, P, I32, I64, I64, I64, P, P, P, P, I32, P, P],
+    "sid_fast_nnls_ex": [P, P, P, I32, I64, I64, I64, P, I32, I32, P, P, P, P, P, P, P, P, I32, P, P],
     "sid_gram_noalloc": [P, I64, I64, P, P],
     "sid_selftest_wait_timeout": [ctypes.c_uint32, I32],
     "sid_library": [P, P, I64, P, P, I64, I64, F64, P, I32, P],
     "sid_library_boxes": [P, I64, I64, F64, I64, I64, I64, P],
     "sid_spatial_update": [P, P, P, I32, P, I64, I64, I64, F64, F64, F64, I32, I32, P, P, P],
     "sid_nqp_batched": [P, P, P, I32, I64, P, P, P, P, P],
+    "sid_reg_nnls": [P, P, I64, I32, P, F64, F64, F64, I32, I32, P, P, P],
     "sid_nmf_defaults": [P],
     "sid_t_update": [P, P, I32, P, P, I64, I64, I64, P, P, P, I32, P],
     "sid_s_update": [P, P, I32, P, P, I64, I64, I64, P, P, P, I32, P],

@@ -18,6 +18,9 @@ int gemm_tn(const void* const* A, const void* const* B, int npass, int64_t m, in
             float* C, int64_t ldc, float alpha, float beta, int bn, int splitk, float* ws, int64_t ws_elems, int* err,
             cudaStream_t st);
 void gemm_autotune(int m, int n, int nkb, int* bn, int* splitk);
+void gemm_autotune_sym(int m, int nkb, int* bn, int* splitk);
+int gemm_tn_sym(const void* const* A, const void* const* B, int npass, int64_t m, int64_t k, bool bf16, float* C,
+                int64_t ldc, float alpha, int bn, int splitk, float* ws, int64_t ws_elems, int* err, cudaStream_t st);
 int sgemm_tn(const float* A, const float* B, int64_t m, int64_t n, int64_t k, int64_t lda, int64_t ldb, float* C,
              int64_t ldc, float alpha, float beta, float* ws, int64_t ws_elems, cudaStream_t st);
 int64_t sgemm_ws_elems(int64_t m, int64_t n, int64_t k);
@@ -71,7 +74,9 @@ int contract(sid_ctx* c, const float* A, const void* B, bool b_f16, int64_t m, i
     }
     SID_REQUIRE(prec == SID_PREC_SPLIT || prec == SID_PREC_BF16, "unknown precision %d", prec);
     int bn = 0, splitk = 0;
-    gemm_autotune((int)m, (int)n, (int)cdiv(k, 64), &bn, &splitk);
+    const bool same = (static_cast<const void*>(A) == B && lda == ldb && m == n && !b_f16);
+    if (same && beta == 0.f) gemm_autotune_sym((int)m, (int)cdiv(k, 64), &bn, &splitk);
+    else gemm_autotune((int)m, (int)n, (int)cdiv(k, 64), &bn, &splitk);
     SID_TRY(c->ws.alloc((size_t)(splitk * m * n) * sizeof(float)));
     const bool split = prec == SID_PREC_SPLIT;
     const size_t abytes = (size_t)blk16_elems(k, m) * 2, bbytes = (size_t)blk16_elems(k, n) * 2;
@@ -90,7 +95,6 @@ int contract(sid_ctx* c, const float* A, const void* B, bool b_f16, int64_t m, i
                        (int64_t)(c->ws.bytes / sizeof(float)), err, st);
     }
     // FP32 x FP32: BF16 hi/lo splits of both (no scaling needed: BF16 keeps the FP32 exponent range)
-    const bool same = (static_cast<const void*>(A) == B && lda == ldb && m == n);
     SID_TRY(c->a_hi.alloc(abytes));
     if (split) SID_TRY(c->a_lo.alloc(abytes));
     SID_TRY(split16(A, k, m, lda, c->a_hi.as<uint16_t>(), split ? c->a_lo.as<uint16_t>() : nullptr, true, 1.f, st));
@@ -105,6 +109,9 @@ int contract(sid_ctx* c, const float* A, const void* B, bool b_f16, int64_t m, i
     }
     const void* As[3] = {c->a_hi.p, c->a_hi.p, c->a_lo.p};
     const void* Bs[3] = {bh, bl, bh};
+    if (same && beta == 0.f)  // A'A: hi*hi + hi*lo + lo*hi is symmetric as a whole
+        return gemm_tn_sym(As, Bs, split ? 3 : 1, m, k, true, C, ldc, alpha, bn, splitk, c->ws.as<float>(),
+                           (int64_t)(c->ws.bytes / sizeof(float)), err, st);
     return gemm_tn(As, Bs, split ? 3 : 1, m, n, k, true, C, ldc, alpha, beta, bn, splitk, c->ws.as<float>(),
                    (int64_t)(c->ws.bytes / sizeof(float)), err, st);
 }

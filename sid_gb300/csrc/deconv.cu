@@ -6,6 +6,8 @@
 // entry and exit.
 #include <cmath>
 
+#include <utility>
+
 #include "sid_internal.cuh"
 
 namespace sid {
@@ -227,6 +229,150 @@ __global__ void k_ls_grad(float* __restrict__ d, const float* __restrict__ b, co
         d[i] += b[i] + l2 * step[i];
 }
 
+// ---------------------------------------------------------------- TV terms --
+// Neighbours along x, y and z of a polyphase volume entry: Vp index
+// i = u + Lx (v + Ly (a + N (b + N c))) holds V(a + N u, b + N v, c).  Entries
+// past the volume (x >= X, y >= Y, or off the lattice) read 0, as convn's
+// zero padding does (the polyphase padding itself holds zeros).
+struct PolyGeom {
+    int N, Lx, Ly, Z;
+    int X, Y;
+};
+
+struct PolyPos {
+    int u, v, a, b, c;
+};
+
+__device__ __forceinline__ float pv_at(const float* __restrict__ x, const PolyGeom& g, int u, int v, int a, int b,
+                                       int c)
+{
+    if (c < 0 || c >= g.Z) return 0.f;
+    if (a < 0) { a += g.N; --u; } else if (a >= g.N) { a -= g.N; ++u; }
+    if (b < 0) { b += g.N; --v; } else if (b >= g.N) { b -= g.N; ++v; }
+    if (u < 0 || u >= g.Lx || v < 0 || v >= g.Ly) return 0.f;
+    if (a + g.N * u >= g.X || b + g.N * v >= g.Y) return 0.f;
+    return x[u + (int64_t)g.Lx * (v + (int64_t)g.Ly * (a + g.N * (b + (int64_t)g.N * c)))];
+}
+
+// grid: x over the Lx*Ly lattice of one plane, y over the N*N*Z planes
+__device__ __forceinline__ bool poly_pos(const PolyGeom& g, PolyPos& p, int64_t& i)
+{
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= g.Lx * g.Ly) return false;
+    const int pl = blockIdx.y;  // a + N (b + N c)
+    p.u = e % g.Lx;
+    p.v = e / g.Lx;
+    p.a = pl % g.N;
+    p.b = (pl / g.N) % g.N;
+    p.c = pl / (g.N * g.N);
+    i = e + (int64_t)g.Lx * g.Ly * pl;
+    return true;
+}
+
+__device__ __forceinline__ float sgnf(float v) { return v > 0.f ? 1.f : (v < 0.f ? -1.f : 0.f); }
+
+// deconvRL.m:61-87 (mode 'TV'), out-of-place (the stencil reads the old X):
+//   p = 1: dx = sign(convn(X, center-left)) = sign(X(x) - X(x+1)) (y, z alike),
+//          den = A'AX + l1 dx + l2 dy + l3 dz + sum(l),
+//          num = Htf + l1 dx(x-1) + l2 dy(y-1) + l3 dz(z-1) + sum(l);
+//   p = 2: den = A'AX + 2 sum(l) X, num = Htf + convn(X, filt) = Htf + l1 (X(x+1) + X(x-1)) + ...;
+//   e = num ./ den, e(isinf(e)) = 0, X = X .* e, X(isnan(X)) = 0.
+__global__ void k_isra_tv(float* __restrict__ xn, const float* __restrict__ x, const float* __restrict__ htf,
+                          const float* __restrict__ b, PolyGeom g, int pnorm, float l1, float l2, float l3)
+{
+    PolyPos q;
+    int64_t i;
+    if (!poly_pos(g, q, i)) return;
+    const float xi = x[i];
+    const float lsum = (float)((double)l1 + (double)l2 + (double)l3);
+    float den, num;
+    if (pnorm == 1) {
+        const float dxp = sgnf(xi - pv_at(x, g, q.u, q.v, q.a + 1, q.b, q.c));
+        const float dyp = sgnf(xi - pv_at(x, g, q.u, q.v, q.a, q.b + 1, q.c));
+        const float dzp = sgnf(xi - pv_at(x, g, q.u, q.v, q.a, q.b, q.c + 1));
+        // dx at x - 1 (0 at the first plane: convn(dx, right) reads dx(0) = 0)
+        const bool hx = (q.a + g.N * q.u) > 0, hy = (q.b + g.N * q.v) > 0, hz = q.c > 0;
+        const float dxm = hx ? sgnf(pv_at(x, g, q.u, q.v, q.a - 1, q.b, q.c) - xi) : 0.f;
+        const float dym = hy ? sgnf(pv_at(x, g, q.u, q.v, q.a, q.b - 1, q.c) - xi) : 0.f;
+        const float dzm = hz ? sgnf(pv_at(x, g, q.u, q.v, q.a, q.b, q.c - 1) - xi) : 0.f;
+        den = (((b[i] + l1 * dxp) + l2 * dyp) + l3 * dzp) + lsum;
+        num = (((htf[i] + l1 * dxm) + l2 * dym) + l3 * dzm) + lsum;
+    } else {
+        den = b[i] + (2.f * lsum) * xi;
+        const float cx = pv_at(x, g, q.u, q.v, q.a + 1, q.b, q.c) + pv_at(x, g, q.u, q.v, q.a - 1, q.b, q.c);
+        const float cy = pv_at(x, g, q.u, q.v, q.a, q.b + 1, q.c) + pv_at(x, g, q.u, q.v, q.a, q.b - 1, q.c);
+        const float cz = pv_at(x, g, q.u, q.v, q.a, q.b, q.c + 1) + pv_at(x, g, q.u, q.v, q.a, q.b, q.c - 1);
+        num = htf[i] + (l1 * cx + l2 * cy + l3 * cz);
+    }
+    float e = __fdiv_rn(num, den);
+    if (isinf(e)) e = 0.f;
+    float v = xi * e;
+    if (isnan(v)) v = 0.f;
+    xn[i] = v;
+}
+
+// LS_deconv.m:53-59: lb_TV_L2(X) = convn(X, filter, 'same') with filter
+// l1 at (+-1,0,0), l2 at (0,+-1,0), l3 at (0,0,+-1) and -sum(l) at the centre.
+__device__ __forceinline__ float tv_l2_at(const float* __restrict__ x, const PolyGeom& g, const PolyPos& q, float xi,
+                                          float l1, float l2, float l3)
+{
+    const float cx = pv_at(x, g, q.u, q.v, q.a + 1, q.b, q.c) + pv_at(x, g, q.u, q.v, q.a - 1, q.b, q.c);
+    const float cy = pv_at(x, g, q.u, q.v, q.a, q.b + 1, q.c) + pv_at(x, g, q.u, q.v, q.a, q.b - 1, q.c);
+    const float cz = pv_at(x, g, q.u, q.v, q.a, q.b, q.c + 1) + pv_at(x, g, q.u, q.v, q.a, q.b, q.c - 1);
+    return (l1 * cx + l2 * cy + l3 * cz) - (float)((double)l1 + (double)l2 + (double)l3) * xi;
+}
+
+// d = B + lb_TV_L2(x) + l2 x - x + l1   (LS_deconv.m:73-75 with x = df)
+__global__ void k_ls_init_tv(float* __restrict__ d, const float* __restrict__ b, const float* __restrict__ x,
+                             PolyGeom g, float l1, float l2, float t1, float t2, float t3)
+{
+    PolyPos q;
+    int64_t i;
+    if (!poly_pos(g, q, i)) return;
+    const float xi = x[i];
+    d[i] = (((b[i] + tv_l2_at(x, g, q, xi, t1, t2, t3)) + l2 * xi) - xi) + l1;
+}
+
+// d += B + lb_TV_L2(step) + l2 step   (LS_deconv.m:92)
+__global__ void k_ls_grad_tv(float* __restrict__ d, const float* __restrict__ b, const float* __restrict__ step,
+                             PolyGeom g, float l2, float t1, float t2, float t3)
+{
+    PolyPos q;
+    int64_t i;
+    if (!poly_pos(g, q, i)) return;
+    const float si = step[i];
+    d[i] += (b[i] + tv_l2_at(step, g, q, si, t1, t2, t3)) + l2 * si;
+}
+
+// qd = B + lb_TV_L2(d) + l2 d   (Q(df_) of LS_deconv.m:83)
+__global__ void k_ls_qd(float* __restrict__ qd, const float* __restrict__ b, const float* __restrict__ d, PolyGeom g,
+                        float l2, float t1, float t2, float t3)
+{
+    PolyPos q;
+    int64_t i;
+    if (!poly_pos(g, q, i)) return;
+    const float di = d[i];
+    qd[i] = (b[i] + tv_l2_at(d, g, q, di, t1, t2, t3)) + l2 * di;
+}
+
+// Xguess_history(it, :, :, :) = X  (deconvRL.m:90-92): history is maxIter x X x Y x Z
+__global__ void k_history(float* __restrict__ hist, const float* __restrict__ xp, PolyGeom g, int it, int maxIter)
+{
+    PolyPos q;
+    int64_t i;
+    if (!poly_pos(g, q, i)) return;
+    const int xx = q.a + g.N * q.u, yy = q.b + g.N * q.v;
+    if (xx >= g.X || yy >= g.Y) return;
+    hist[it + (int64_t)maxIter * (xx + (int64_t)g.X * (yy + (int64_t)g.Y * q.c))] = xp[i];
+}
+
+static PolyGeom poly_geom(const sid_plan* p)
+{
+    return PolyGeom{(int)p->N, (int)p->Lx, (int)p->Ly, (int)p->Z, (int)p->X, (int)p->Y};
+}
+
+static dim3 poly_grid(const sid_plan* p) { return dim3((unsigned)cdiv(p->Lx * p->Ly, 256), (unsigned)(p->N * p->N * p->Z)); }
+
 static int isra_update(sid_plan* p, float* xp, const float* hp, float lambda, cudaStream_t st)
 {
     k_isra_update<<<2048, 256, 0, st>>>(xp, hp, p->bp.as<float>(), lambda, vol_plane_elems(p) * p->Z);
@@ -431,6 +577,110 @@ extern "C" int sid_deconv_ls(sid_plan* p, int method, float* X, int max_iter, fl
         SID_TRY(fwd_poly(p, method, tp, p->ip.as<float>(), st));
         SID_TRY(adj_poly(p, method, p->ip.as<float>(), p->bp.as<float>(), st));
         k_ls_grad<<<2048, 256, 0, st>>>(dp, p->bp.as<float>(), tp, lamb_L2, n);
+        SID_CHECK_LAUNCH();
+    }
+    SID_TRY(vp_to_v(p, xp, X, p->Z, st));
+    return SID_OK;
+}
+
+extern "C" int sid_deconv_isra_ex(sid_plan* p, int method, const float* Htf, float* X, int maxIter, int mode,
+                                  int pnorm, const float* lambda3, float* history, void* stream)
+{
+    SID_REQUIRE(p && Htf && X && lambda3, "sid_deconv_isra_ex: NULL argument");
+    SID_REQUIRE(maxIter >= 0, "sid_deconv_isra_ex: maxIter < 0");
+    SID_REQUIRE(mode == 0 || mode == 1, "sid_deconv_isra_ex: mode must be 0 ('basic') or 1 ('TV')");
+    const float l1 = lambda3[0], l2 = mode ? lambda3[1] : 0.f, l3 = mode ? lambda3[2] : 0.f;
+    const bool lam_on = mode ? (l1 != 0.f || l2 != 0.f || l3 != 0.f) : (l1 != 0.f);
+    SID_REQUIRE(mode == 1 || !lam_on || pnorm == 1,
+                "deconvRL: mode 'basic' with lambda ~= 0 and p ~= 1 uses the undefined Filter (deconvRL.m:57)");
+    SID_REQUIRE(!p->X || p->X * p->Y < INT32_MAX, "sid_deconv_isra_ex: volume too large");
+    cudaStream_t st = as_stream(stream);
+    SID_TRY(ensure_proj_ws(p));
+    const int64_t n = vol_plane_elems(p) * p->Z;
+    SID_TRY(p->ws[0].alloc((size_t)n * sizeof(float)));
+    SID_TRY(p->ws[1].alloc((size_t)n * sizeof(float)));
+    if (mode && lam_on) SID_TRY(p->ws[2].alloc((size_t)n * sizeof(float)));
+    float* xp = p->ws[0].as<float>();
+    float* hp = p->ws[1].as<float>();
+    SID_TRY(v_to_vp(p, Htf, hp, p->Z, st));
+    SID_TRY(v_to_vp(p, X, xp, p->Z, st));
+    const PolyGeom g = poly_geom(p);
+    // mode 'TV' with p > 2 prints 'p>2 not supported' and returns X (deconvRL.m:79-81)
+    const bool tv_stop = mode && lam_on && pnorm != 1 && pnorm != 2;
+    for (int it = 0; it < maxIter && !tv_stop; ++it) {
+        SID_TRY(fwd_poly(p, method, xp, p->ip.as<float>(), st));
+        SID_TRY(adj_poly(p, method, p->ip.as<float>(), p->bp.as<float>(), st));
+        if (mode && lam_on) {
+            float* xn = p->ws[2].as<float>();
+            k_isra_tv<<<poly_grid(p), 256, 0, st>>>(xn, xp, hp, p->bp.as<float>(), g, pnorm, l1, l2, l3);
+            SID_CHECK_LAUNCH();
+            std::swap(p->ws[0], p->ws[2]);
+            xp = p->ws[0].as<float>();
+        } else {
+            SID_TRY(isra_update(p, xp, hp, l1, st));
+        }
+        if (history) {
+            k_history<<<poly_grid(p), 256, 0, st>>>(history, xp, g, it, maxIter);
+            SID_CHECK_LAUNCH();
+        }
+    }
+    SID_TRY(vp_to_v(p, xp, X, p->Z, st));
+    return SID_OK;
+}
+
+extern "C" int sid_deconv_ls_ex(sid_plan* p, int method, float* X, int max_iter, float lamb_L1, float lamb_L2,
+                                const float* lamb_TV_L2, float lamb_TV_L1, void* stream)
+{
+    SID_REQUIRE(p && X && lamb_TV_L2, "sid_deconv_ls_ex: NULL argument");
+    SID_REQUIRE(max_iter >= 0, "sid_deconv_ls_ex: max_iter < 0");
+    const float t1 = lamb_TV_L2[0], t2 = lamb_TV_L2[1], t3 = lamb_TV_L2[2];
+    const bool tv = t1 != 0.f || t2 != 0.f || t3 != 0.f;  // max(opts.lamb_TV_L2) ~= 0 (LS_deconv.m:49)
+    // alpha from Q itself only when lamb_TV_L1 * lamb_TV_L2 * lamb_L2 is nonzero in every component (LS_deconv.m:82)
+    const bool qalpha = lamb_TV_L1 != 0.f && t1 != 0.f && t2 != 0.f && t3 != 0.f && lamb_L2 != 0.f;
+    if (!tv && !qalpha) return sid_deconv_ls(p, method, X, max_iter, lamb_L1, lamb_L2, stream);
+    SID_REQUIRE(p->X * p->Y < INT32_MAX, "sid_deconv_ls_ex: volume too large");
+    cudaStream_t st = as_stream(stream);
+    SID_TRY(ensure_proj_ws(p));
+    const int64_t n = vol_plane_elems(p) * p->Z;
+    const int64_t ni = vol_plane_elems(p);
+    for (int k = 0; k < 4; ++k) SID_TRY(p->ws[k].alloc((size_t)n * sizeof(float)));
+    float* xp = p->ws[0].as<float>();
+    float* dp = p->ws[1].as<float>();
+    float* tp = p->ws[2].as<float>();
+    float* qp = p->ws[3].as<float>();
+    double* red = p->red.as<double>();
+    double* s12 = red + kRedBlocks;
+    float* alpha = reinterpret_cast<float*>(s12 + 2);
+    const PolyGeom g = poly_geom(p);
+    const dim3 pg = poly_grid(p);
+    SID_TRY(v_to_vp(p, X, xp, p->Z, st));
+    // df = Q(x0) - x0 + lamb_L1 with x0 = df, Q = A'A + lb_TV_L2 + lamb_L2 I
+    SID_TRY(fwd_poly(p, method, xp, p->ip.as<float>(), st));
+    SID_TRY(adj_poly(p, method, p->ip.as<float>(), p->bp.as<float>(), st));
+    k_ls_init_tv<<<pg, 256, 0, st>>>(dp, p->bp.as<float>(), xp, g, lamb_L1, lamb_L2, t1, t2, t3);
+    SID_CHECK_LAUNCH();
+    SID_TRY(mask_vp(p, dp, p->Z, st));
+    for (int it = 0; it < max_iter; ++it) {
+        k_ls_passive<<<2048, 256, 0, st>>>(xp, dp, tp, n);
+        SID_CHECK_LAUNCH();
+        SID_TRY(dot(tp, tp, n, red, s12, st));
+        if (qalpha) {
+            // alpha = (df_' df_) / sum(df_ .* Q(df_))
+            SID_TRY(fwd_poly(p, method, tp, p->ip.as<float>(), st));
+            SID_TRY(adj_poly(p, method, p->ip.as<float>(), p->bp.as<float>(), st));
+            k_ls_qd<<<pg, 256, 0, st>>>(qp, p->bp.as<float>(), tp, g, lamb_L2, t1, t2, t3);
+            SID_CHECK_LAUNCH();
+            SID_TRY(dot(tp, qp, n, red, s12 + 1, st, s12, alpha));
+        } else {
+            // alpha = (df_' df_) / (v' v), v = A df_
+            SID_TRY(fwd_poly(p, method, tp, p->ip.as<float>(), st));
+            SID_TRY(dot(p->ip.as<float>(), p->ip.as<float>(), ni, red, s12 + 1, st, s12, alpha));
+        }
+        k_ls_step<<<2048, 256, 0, st>>>(xp, tp, alpha, n);
+        SID_CHECK_LAUNCH();
+        SID_TRY(fwd_poly(p, method, tp, p->ip.as<float>(), st));
+        SID_TRY(adj_poly(p, method, p->ip.as<float>(), p->bp.as<float>(), st));
+        k_ls_grad_tv<<<pg, 256, 0, st>>>(dp, p->bp.as<float>(), tp, g, lamb_L2, t1, t2, t3);
         SID_CHECK_LAUNCH();
     }
     SID_TRY(vp_to_v(p, xp, X, p->Z, st));

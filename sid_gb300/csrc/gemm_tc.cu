@@ -141,8 +141,10 @@ constexpr int GEMM_THREADS = (GEMM_DRAIN_WARPS + 2) * 32;
 template <int BN, int STAGES>
 __global__ void __launch_bounds__(GEMM_THREADS, 1)
 k_gemm_tc(const __grid_constant__ GemmMaps maps, int npass, int m, int n, int nkb, int kb_per, int bf16,
-          float* __restrict__ out, int64_t ldc, int64_t split_stride, float alpha, int* __restrict__ err)
+          float* __restrict__ out, int64_t ldc, int64_t split_stride, float alpha, int* __restrict__ err, int sym)
 {
+    // symmetric product (A'A): tiles wholly below the diagonal are mirrored afterwards
+    if (sym && (int)blockIdx.x * GEMM_BM >= (int)blockIdx.y * BN + BN) return;
     using SM = GemmSmem<BN, STAGES>;
     constexpr uint32_t ACC_COLS = BN <= 32 ? 32 : (BN <= 64 ? 64 : (BN <= 128 ? 128 : 256));
     constexpr uint32_t TMEM_COLS = 2 * ACC_COLS;  // two accumulators
@@ -343,7 +345,7 @@ static int make_map(CUtensorMap* map, const void* base, int64_t rows, int64_t nk
 
 template <int BN, int STAGES>
 static int launch_gemm(const GemmMaps& maps, int npass, int m, int n, int nkb, int splitk, bool bf16, float* out,
-                       int64_t ldc, int64_t split_stride, float alpha, int* err, cudaStream_t st)
+                       int64_t ldc, int64_t split_stride, float alpha, int* err, bool sym, cudaStream_t st)
 {
     using SM = GemmSmem<BN, STAGES>;
     static bool configured = false;
@@ -354,29 +356,40 @@ static int launch_gemm(const GemmMaps& maps, int npass, int m, int n, int nkb, i
     const int kb_per = (int)cdiv(nkb, splitk);
     dim3 grid((unsigned)cdiv(m, GEMM_BM), (unsigned)cdiv(n, BN), (unsigned)splitk);
     k_gemm_tc<BN, STAGES><<<grid, GEMM_THREADS, SM::TOTAL, st>>>(maps, npass, m, n, nkb, kb_per, bf16 ? 1 : 0, out, ldc,
-                                                         split_stride, alpha, err);
+                                                         split_stride, alpha, err, sym ? 1 : 0);
     SID_CHECK_LAUNCH();
     return SID_OK;
 }
 
+// Output tiles a launch computes: all of them, or for a symmetric product
+// (A'A, m == n) those reaching the diagonal or above it.
+static int64_t gemm_tiles(int m, int n, int bn, bool sym)
+{
+    const int64_t tm = cdiv(m, GEMM_BM), tn = cdiv(n, bn);
+    if (!sym) return tm * tn;
+    int64_t t = 0;
+    for (int64_t j = 0; j < tn; ++j) t += std::min<int64_t>(tm, cdiv(j * bn + bn, GEMM_BM));
+    return t;
+}
+
 // Tile width and split-K choice (the project's autotuner for this kernel).
 // For each tile width BN in {256, 192, 128, 64} split K until there are >= 4 waves
-// of CTAs on the 152 SMs (or a split would hold fewer than 8 K blocks), then
+// of CTAs on the SMs (or a split would hold fewer than 8 K blocks), then
 // estimate the time as waves x K blocks per CTA x BN / efficiency(BN) and keep
 // the fastest.  The efficiencies model tcgen05's shared-memory operand traffic
 // per MMA: A (128 x 16) plus B (BN x 16) must be read for 128*BN*16 MACs, so
 // BN = 64 is limited by shared-memory bandwidth (measured) and BN = 256
-// amortises A best.
-void gemm_autotune(int m, int n, int nkb, int* bn, int* splitk)
+// amortises A best.  A symmetric product counts only the tiles it computes.
+static void gemm_autotune_impl(int m, int n, int nkb, bool sym, int* bn, int* splitk)
 {
-    const int sms = 152;
+    const int sms = sm_count();
     const int cands[4] = {256, 192, 128, 64};
     const double eff[4] = {1.0, 0.95, 0.85, 0.45};
     double best = 1e300;
     int bbn = 256, bs = 1;
     for (int i = 0; i < 4; ++i) {
         const int c = cands[i];
-        const int64_t tiles = cdiv(m, GEMM_BM) * cdiv(n, c);
+        const int64_t tiles = gemm_tiles(m, n, c, sym);
         int s = 1;
         while (tiles * s < 4 * sms && nkb / (s + 1) >= 8) ++s;
         const int64_t kb_per = cdiv(nkb, s);
@@ -393,17 +406,31 @@ void gemm_autotune(int m, int n, int nkb, int* bn, int* splitk)
     *splitk = bs;
 }
 
+void gemm_autotune(int m, int n, int nkb, int* bn, int* splitk) { gemm_autotune_impl(m, n, nkb, false, bn, splitk); }
+void gemm_autotune_sym(int m, int nkb, int* bn, int* splitk) { gemm_autotune_impl(m, m, nkb, true, bn, splitk); }
+
+// C(r, c) = C(c, r) for r > c: completes a symmetric product computed on and above the diagonal
+__global__ void k_mirror_lower(float* __restrict__ C, int m, int64_t ldc)
+{
+    const int64_t total = (int64_t)m * m;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+        const int r = (int)(i % m), c = (int)(i / m);
+        if (r > c) C[r + ldc * c] = C[c + ldc * r];
+    }
+}
+
 // out (m x n, ldc) = sum_p A_p^T B_p; A_p: k x m, B_p: k x n, 16-bit K-blocked.
 // ws: >= splitk * m * n floats when splitk > 1 or beta != 0 (alpha alone is
 // applied as the tiles are stored).
-int gemm_tn(const void* const* A, const void* const* B, int npass, int64_t m, int64_t n, int64_t k, bool bf16,
-            float* C, int64_t ldc, float alpha, float beta, int bn, int splitk, float* ws, int64_t ws_elems, int* err,
-            cudaStream_t st)
+static int gemm_tn_impl(const void* const* A, const void* const* B, int npass, int64_t m, int64_t n, int64_t k,
+                        bool bf16, float* C, int64_t ldc, float alpha, float beta, int bn, int splitk, float* ws,
+                        int64_t ws_elems, int* err, bool sym, cudaStream_t st)
 {
     SID_REQUIRE(npass >= 1 && npass <= GEMM_MAXPASS, "gemm: npass %d outside [1,3]", npass);
     SID_REQUIRE(m > 0 && n > 0 && k > 0, "gemm: empty problem");
+    SID_REQUIRE(!sym || m == n, "gemm: a symmetric product needs m == n");
     const int nkb = (int)cdiv(k, GEMM_BK);
-    if (bn <= 0 || splitk <= 0) gemm_autotune((int)m, (int)n, nkb, &bn, &splitk);
+    if (bn <= 0 || splitk <= 0) gemm_autotune_impl((int)m, (int)n, nkb, sym, &bn, &splitk);
     splitk = std::max(1, std::min(splitk, nkb));
     GemmMaps maps;
     std::memset(&maps, 0, sizeof(maps));
@@ -422,10 +449,10 @@ int gemm_tn(const void* const* A, const void* const* B, int npass, int64_t m, in
     }
     int rc;
     switch (bn) {
-    case 256: rc = launch_gemm<256, 4>(maps, npass, (int)m, (int)n, nkb, splitk, bf16, out, ldo, sstride, direct ? alpha : 1.f, err, st); break;
-    case 192: rc = launch_gemm<192, 5>(maps, npass, (int)m, (int)n, nkb, splitk, bf16, out, ldo, sstride, direct ? alpha : 1.f, err, st); break;
-    case 128: rc = launch_gemm<128, 6>(maps, npass, (int)m, (int)n, nkb, splitk, bf16, out, ldo, sstride, direct ? alpha : 1.f, err, st); break;
-    case 64: rc = launch_gemm<64, 8>(maps, npass, (int)m, (int)n, nkb, splitk, bf16, out, ldo, sstride, direct ? alpha : 1.f, err, st); break;
+    case 256: rc = launch_gemm<256, 4>(maps, npass, (int)m, (int)n, nkb, splitk, bf16, out, ldo, sstride, direct ? alpha : 1.f, err, sym, st); break;
+    case 192: rc = launch_gemm<192, 5>(maps, npass, (int)m, (int)n, nkb, splitk, bf16, out, ldo, sstride, direct ? alpha : 1.f, err, sym, st); break;
+    case 128: rc = launch_gemm<128, 6>(maps, npass, (int)m, (int)n, nkb, splitk, bf16, out, ldo, sstride, direct ? alpha : 1.f, err, sym, st); break;
+    case 64: rc = launch_gemm<64, 8>(maps, npass, (int)m, (int)n, nkb, splitk, bf16, out, ldo, sstride, direct ? alpha : 1.f, err, sym, st); break;
     default: set_error("gemm: unsupported tile width %d", bn); return SID_EINVAL;
     }
     SID_TRY(rc);
@@ -433,7 +460,28 @@ int gemm_tn(const void* const* A, const void* const* B, int npass, int64_t m, in
         k_splitk_reduce<<<1024, 256, 0, st>>>(ws, splitk, sstride, (int)m, (int)n, m, C, ldc, alpha, beta);
         SID_CHECK_LAUNCH();
     }
+    if (sym) {
+        k_mirror_lower<<<1024, 256, 0, st>>>(C, (int)m, ldc);
+        SID_CHECK_LAUNCH();
+    }
     return SID_OK;
+}
+
+int gemm_tn(const void* const* A, const void* const* B, int npass, int64_t m, int64_t n, int64_t k, bool bf16,
+            float* C, int64_t ldc, float alpha, float beta, int bn, int splitk, float* ws, int64_t ws_elems, int* err,
+            cudaStream_t st)
+{
+    return gemm_tn_impl(A, B, npass, m, n, k, bf16, C, ldc, alpha, beta, bn, splitk, ws, ws_elems, err, false, st);
+}
+
+// Symmetric product C = sum_p A_p^T B_p with A_p^T B_p + A_q^T B_q symmetric
+// over the passes (A'A, or the split hi/lo passes of A'A): only the tiles on
+// and above the diagonal are computed, the rest mirrored (an exactly symmetric
+// result).  beta must be 0.
+int gemm_tn_sym(const void* const* A, const void* const* B, int npass, int64_t m, int64_t k, bool bf16, float* C,
+                int64_t ldc, float alpha, int bn, int splitk, float* ws, int64_t ws_elems, int* err, cudaStream_t st)
+{
+    return gemm_tn_impl(A, B, npass, m, m, k, bf16, C, ldc, alpha, 0.f, bn, splitk, ws, ws_elems, err, true, st);
 }
 
 }  // namespace sid

@@ -154,6 +154,208 @@ k_lib_project(const float* __restrict__ taps, const float* __restrict__ packed, 
     }
 }
 
+// Tiled form (the default).  One CTA per (group of up to G neurons with the
+// same depth window, output phase a'b').  Every neuron's output window has the
+// same shape, W rows (s) x NTB*TB columns (t) of output lenslets starting at
+// (umin + dlo, vmin + dlo) with (umin, vmin) the first lenslet its box touches,
+// so a box lattice point (u, v) lands at a relative offset (ru, rv) = (u -
+// umin, v - vmin) in [0, span]^2 and the tap it meets at relative output (ds,
+// dt) is K(ds - ru, dt - rv).  Per depth c and input row phase b the N tap
+// arrays K[abc][b'a'] of all input column phases a are copied (cp.async,
+// double-buffered: the next (c, b) row is in flight while this one is used)
+// into zero-bordered shared tiles with an odd row pitch.  Lane = output row ds,
+// so the 32 lanes of a warp read 32 different tile rows (distinct banks); each
+// warp owns (neuron, block of TB output columns) pairs.  For each lattice row
+// ru of a box phase, a lane loads TB + NRV - 1 consecutive taps of its tile row
+// into registers once and applies them to the NRV lattice columns rv of that
+// row: TB + NRV - 1 shared loads for NRV * TB FMAs, and only the boxes' own
+// lattice points are visited.  TB (the template's column count, >= the
+// window's width) is the whole row, so one (warp, neuron) pair covers a
+// neuron's window and the per-phase bookkeeping is paid once per row.
+
+__device__ __forceinline__ void cp_async4_lib(float* dst, const float* src)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)),
+                 "l"(src)
+                 : "memory");
+}
+
+struct LibTileArgs {
+    int N, D, dlo, span, W, Wt, rows, pitch, cb, tsz;
+    int64_t tbs;
+    int Lx, Ly;
+    int64_t X, Y, ldn, ldp;
+};
+
+template <int G, int TB, int NRV>
+__global__ void __launch_bounds__(256, 2)
+k_lib_tile(const float* __restrict__ taps, const float* __restrict__ packed, const LibBox* __restrict__ boxes,
+           const int* __restrict__ groups, const LibTileArgs a, float* __restrict__ out)
+{
+    constexpr int NTB = 1;
+    constexpr int PPW = (G * NTB + 7) / 8;  // (neuron, column block) pairs per warp
+    constexpr int NW = TB + NRV - 1;        // taps held per lattice row
+    extern __shared__ float sm[];           // 2 x N tiles of rows x pitch, then neuron tables
+    const int N = a.N, D = a.D, tsz = a.tsz;
+    int* tab = reinterpret_cast<int*>(sm + 2 * N * tsz);
+    // per neuron k: [0] x0 [1] y0 [2] z0 [3] bw [4] bh [5] off [6] umin [7] vmin, then ulo[N], nu[N], vlo[N], nv[N]
+    const int tstride = 8 + 4 * N;
+    const int* grp = groups + blockIdx.x * (G + 1);
+    const int cnt = grp[0];
+    const int o = blockIdx.y;
+    const int bp = o / N, ap = o - bp * N;
+    for (int i = threadIdx.x; i < 2 * N * tsz; i += blockDim.x) sm[i] = 0.f;
+    for (int e = threadIdx.x; e < cnt * N; e += blockDim.x) {
+        const int k = e / N, ph = e - k * N;
+        const LibBox b = boxes[grp[1 + k]];
+        int* t = tab + k * tstride;
+        if (ph == 0) {
+            t[0] = b.x0; t[1] = b.y0; t[2] = b.z0; t[3] = b.x1 - b.x0; t[4] = b.y1 - b.y0; t[5] = b.off;
+            t[6] = b.x0 / N; t[7] = b.y0 / N;
+        }
+        // lattice u of column phase ph inside [x0, x1): x = ph + N u
+        const int ulo = b.x0 > ph ? (b.x0 - ph + N - 1) / N : 0;
+        const int uhi = (b.x1 - 1 - ph) >= 0 ? (b.x1 - 1 - ph) / N : -1;
+        const int vlo = b.y0 > ph ? (b.y0 - ph + N - 1) / N : 0;
+        const int vhi = (b.y1 - 1 - ph) >= 0 ? (b.y1 - 1 - ph) / N : -1;
+        t[8 + ph] = ulo;
+        t[8 + N + ph] = uhi - ulo + 1;
+        t[8 + 2 * N + ph] = vlo;
+        t[8 + 3 * N + ph] = vhi - vlo + 1;
+    }
+    const int z0 = boxes[grp[1]].z0, z1 = boxes[grp[1]].z1;
+    const int nst = (z1 - z0) * N;
+    const int DD = D * D;
+    // this thread's tap copies: r = tid + 256 i, i < 3 covers D*D <= 768
+    int roff[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        const int r = threadIdx.x + 256 * i;
+        roff[i] = r < DD ? (r / D + a.span) * a.pitch + (r % D) + a.cb : -1;
+    }
+    auto issue = [&](int st, int buf) {
+        const int c = z0 + st / N, bb = st - (st / N) * N;
+        const int64_t rowblk = ((int64_t)c * N + bb) * N;
+        float* dst0 = sm + buf * N * tsz;
+        for (int aa = 0; aa < N; ++aa) {
+            const float* src = taps + ((rowblk + aa) * N + bp) * a.tbs + (int64_t)ap * DD;
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+                if (roff[i] >= 0) cp_async4_lib(dst0 + aa * tsz + roff[i], src + threadIdx.x + 256 * i);
+        }
+        asm volatile("cp.async.commit_group;" ::: "memory");
+    };
+    const int warp = threadIdx.x >> 5, ds = threadIdx.x & 31;
+    float acc[PPW][TB];
+#pragma unroll
+    for (int q = 0; q < PPW; ++q)
+#pragma unroll
+        for (int j = 0; j < TB; ++j) acc[q][j] = 0.f;
+    __syncthreads();  // zeroed tiles and tables before the first copies land
+    issue(0, 0);
+    for (int st = 0; st < nst; ++st) {
+        if (st + 1 < nst) {
+            issue(st + 1, (st + 1) & 1);
+            asm volatile("cp.async.wait_group 1;" ::: "memory");
+        } else {
+            asm volatile("cp.async.wait_group 0;" ::: "memory");
+        }
+        __syncthreads();
+        const int c = z0 + st / N, bb = st - (st / N) * N;
+        const float* tb0 = sm + (st & 1) * N * tsz;
+        if (ds < a.W) {
+#pragma unroll
+            for (int q = 0; q < PPW; ++q) {
+                const int pr = warp + 8 * q;
+                const int k = pr / NTB, tbk = pr - (pr / NTB) * NTB;
+                if (k >= cnt) continue;
+                const int* t = tab + k * tstride;
+                const int nv = t[8 + 3 * N + bb];
+                if (nv <= 0) continue;
+                const int vlo = t[8 + 2 * N + bb], rvlo = vlo - t[7];
+                const int bw = t[3];
+                // packed index of (x, y, c) = off + (x - x0) + bw * ((y - y0) + bh * (c - z0))
+                const int vrow = t[5] + bw * ((bb + N * vlo - t[1]) + t[4] * (c - t[2])) - t[0];
+                const int colb = tbk * TB - rvlo - (NRV - 1) + a.cb;
+                for (int aa = 0; aa < N; ++aa) {
+                    const int nu = t[8 + N + aa];
+                    if (nu <= 0) continue;
+                    const int ulo = t[8 + aa];
+                    const float* tile = tb0 + aa * tsz;
+                    for (int iu = 0; iu < nu; ++iu) {
+                        const int u = ulo + iu;
+                        const int row = ds - (u - t[6]) + a.span;
+                        const float* wp = tile + row * a.pitch + colb;
+                        float w[NW];
+#pragma unroll
+                        for (int i = 0; i < NW; ++i) w[i] = wp[i];
+                        const float* vp = packed + vrow + aa + N * u;
+#pragma unroll
+                        for (int e = 0; e < NRV; ++e) {
+                            if (e < nv) {
+                                const float val = __ldg(vp + (int64_t)bw * N * e);
+#pragma unroll
+                                for (int j = 0; j < TB; ++j) acc[q][j] = fmaf(val, w[j - e + NRV - 1], acc[q][j]);
+                            }
+                        }
+                    }
+                }
+            }
+        }
+        __syncthreads();  // this buffer is refilled by the next-but-one copy
+    }
+    if (ds < a.W) {
+#pragma unroll
+        for (int q = 0; q < PPW; ++q) {
+            const int pr = warp + 8 * q;
+            const int k = pr / NTB, tbk = pr - (pr / NTB) * NTB;
+            if (k >= cnt) continue;
+            const int n = grp[1 + k];
+            const int* t = tab + k * tstride;
+            const int s = t[6] + a.dlo + ds;
+            if (s < 0 || s >= a.Lx) continue;
+            const int64_t x = ap + (int64_t)N * s;
+            if (x >= a.X) continue;
+#pragma unroll
+            for (int j = 0; j < TB; ++j) {
+                const int dt = tbk * TB + j;
+                const int tt = t[7] + a.dlo + dt;
+                if (dt >= a.Wt || tt < 0 || tt >= a.Ly) continue;
+                const int64_t y = bp + (int64_t)N * tt;
+                if (y < a.Y) out[(int64_t)n * a.ldn + (x + a.X * y) * a.ldp] = acc[q][j];
+            }
+        }
+    }
+}
+
+template <int TB, int NRV>
+static int launch_lib_tile_t(dim3 grid, size_t smem, const float* taps, const float* packed, const LibBox* boxes,
+                             const int* groups, const LibTileArgs& a, float* out, cudaStream_t st)
+{
+    SID_CUDA_TRY(cudaFuncSetAttribute(k_lib_tile<kLibG, TB, NRV>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)smem));
+    k_lib_tile<kLibG, TB, NRV><<<grid, 256, smem, st>>>(taps, packed, boxes, groups, a, out);
+    SID_CHECK_LAUNCH();
+    return SID_OK;
+}
+
+// output window columns per lane row, as a template: the smallest of 16, 24, 28, 32 that holds Wt
+static int tile_tb(int Wt) { return Wt <= 16 ? 16 : (Wt <= 24 ? 24 : (Wt <= 28 ? 28 : 32)); }
+
+static int launch_lib_tile(int tb, int nrv, dim3 grid, size_t smem, const float* taps, const float* packed,
+                           const LibBox* boxes, const int* groups, const LibTileArgs& a, float* out, cudaStream_t st)
+{
+#define SID_LIB_CASE(T, R) \
+    if (tb == T && nrv == R) return launch_lib_tile_t<T, R>(grid, smem, taps, packed, boxes, groups, a, out, st);
+    SID_LIB_CASE(16, 1) SID_LIB_CASE(16, 2) SID_LIB_CASE(16, 3)
+    SID_LIB_CASE(24, 1) SID_LIB_CASE(24, 2) SID_LIB_CASE(24, 3)
+    SID_LIB_CASE(28, 1) SID_LIB_CASE(28, 2) SID_LIB_CASE(28, 3)
+    SID_LIB_CASE(32, 1) SID_LIB_CASE(32, 2) SID_LIB_CASE(32, 3)
+#undef SID_LIB_CASE
+    set_error("sid_library: no tiled kernel for %d columns x %d lattice points", tb, nrv);
+    return SID_EINVAL;
+}
+
 static int mround(double v) { return (int)(v < 0 ? -std::floor(-v + 0.5) : std::floor(v + 0.5)); }
 
 // Box of neuron n: x = round(centre), [max(x-r,1), min(x+r,size)] laterally,
@@ -197,7 +399,7 @@ extern "C" int sid_library(sid_plan* p, const float* const* recon, int64_t n_com
     const int64_t N = p->N, D = p->g.D;
     std::vector<LibBox> boxes(n_neur);
     int64_t off = 0;
-    int max_ns = 0, ntgM = 0, span = 0;
+    int max_ns = 0, ntgM = 0, span = 0, nrv = 0;
     for (int64_t n = 0; n < n_neur; ++n) {
         int bx[6];
         neuron_box(centers, n_neur, n, neur_rad, axial, p->X, p->Y, p->Z, bx);
@@ -221,15 +423,30 @@ extern "C" int sid_library(sid_plan* p, const float* const* recon, int64_t n_com
         max_ns = std::max(max_ns, b.s1 - b.s0);
         ntgM = std::max(ntgM, (int)cdiv(b.t1 - b.t0, kLibT));
         span = std::max(span, std::max(umax - umin, vmax - vmin));
+        nrv = std::max(nrv, (int)std::max(cdiv(b.x1 - b.x0, N), cdiv(b.y1 - b.y0, N)));
         boxes[n] = b;
     }
     SID_REQUIRE(off < INT32_MAX, "sid_library: boxes too large");
+    // tiled kernel: output windows of W x Wt lenslets, W <= 32 (one lane per row)
+    LibTileArgs ta;
+    ta.N = (int)N; ta.D = (int)D; ta.dlo = (int)p->g.dlo; ta.span = span;
+    ta.W = (int)D + span; ta.Wt = (int)D + span;
+    const int tb = tile_tb(ta.Wt);
+    ta.rows = ta.W + span;
+    ta.cb = span + nrv - 1;
+    ta.pitch = (tb + ta.cb) | 1;  // odd: the 32 lanes' rows fall in distinct banks
+    ta.tsz = ta.rows * ta.pitch;
+    const size_t tiled_bytes = (size_t)2 * N * ta.tsz * sizeof(float) + (size_t)kLibG * (8 + 4 * N) * sizeof(int);
+    const bool tiled = ta.W <= 32 && ta.Wt <= 32 && nrv >= 1 && nrv <= 3 && D * D <= 768 &&
+                       tiled_bytes <= 112 * 1024;
     const int Dp = (int)D + 2 * span;
     const size_t tile_bytes =
         (size_t)N * Dp * (Dp + kLibT) * sizeof(float) + (size_t)(D * D + 4 * N * kLibG) * sizeof(int);
-    SID_REQUIRE(tile_bytes <= 200 * 1024, "sid_library: tap tiles (%zu bytes) exceed shared memory", tile_bytes);
-    SID_REQUIRE(max_ns * ntgM <= 256, "sid_library: neuron radius too large for one CTA (%d output groups)",
-                max_ns * ntgM);
+    if (!tiled) {
+        SID_REQUIRE(tile_bytes <= 200 * 1024, "sid_library: tap tiles (%zu bytes) exceed shared memory", tile_bytes);
+        SID_REQUIRE(max_ns * ntgM <= 256, "sid_library: neuron radius too large for one CTA (%d output groups)",
+                    max_ns * ntgM);
+    }
     // groups of up to kLibG neurons with the same depth window, in window order
     std::vector<int64_t> order(n_neur);
     for (int64_t n = 0; n < n_neur; ++n) order[n] = n;
@@ -268,12 +485,19 @@ extern "C" int sid_library(sid_plan* p, const float* const* recon, int64_t n_com
     const int64_t tbs = cdiv(N * D * D, 32) * 32;
     const int64_t ldn = out_layout == 0 ? 1 : P, ldp = out_layout == 0 ? n_neur : 1;
     dim3 grid((unsigned)ngroups, (unsigned)(N * N));
-    SID_CUDA_TRY(cudaFuncSetAttribute(k_lib_project<kLibG>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)tile_bytes));
-    k_lib_project<kLibG><<<grid, 256, tile_bytes, st>>>(p->taps_f.as<float>(), dpack.as<float>(), dbox.as<LibBox>(),
-                                                        dgrp.as<int>(), (int)N, (int)D, (int)p->g.dlo, span, ntgM,
-                                                        tbs, (int)p->Lx, (int)p->Ly, p->X, p->Y, out, ldn, ldp);
-    SID_CHECK_LAUNCH();
+    if (tiled) {
+        ta.tbs = tbs; ta.Lx = (int)p->Lx; ta.Ly = (int)p->Ly; ta.X = p->X; ta.Y = p->Y; ta.ldn = ldn; ta.ldp = ldp;
+        SID_TRY(launch_lib_tile(tb, nrv, grid, tiled_bytes, p->taps_f.as<float>(), dpack.as<float>(),
+                                dbox.as<LibBox>(), dgrp.as<int>(), ta, out, st));
+    } else {
+        SID_CUDA_TRY(cudaFuncSetAttribute(k_lib_project<kLibG>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)tile_bytes));
+        k_lib_project<kLibG><<<grid, 256, tile_bytes, st>>>(p->taps_f.as<float>(), dpack.as<float>(),
+                                                            dbox.as<LibBox>(), dgrp.as<int>(), (int)N, (int)D,
+                                                            (int)p->g.dlo, span, ntgM, tbs, (int)p->Lx, (int)p->Ly,
+                                                            p->X, p->Y, out, ldn, ldp);
+        SID_CHECK_LAUNCH();
+    }
     // the staging buffers are read by the kernels above: wait before the host
     // vectors go out of scope and before the workspaces can be reused
     SID_CUDA_TRY(cudaStreamSynchronize(st));

@@ -679,7 +679,6 @@ extern "C" int sid_t_update(sid_ctx* c, const void* Y, int ydtype, float* T, flo
 }
 
 namespace sid {
-namespace {
 
 // Products of a pixel-major P x k factor X (pixels contiguous: the movie, S,
 // the step direction) with a small k x n matrix W, on the tensor cores:
@@ -690,13 +689,6 @@ namespace {
 // hi*hi + hi*lo + lo*hi.  (BF16 hi/lo keeps 16 bits, which the cancellation in
 // S_update's use_std gradient amplifies past FP32-level agreement.)  BF16
 // precision: one BF16 pass.
-struct PixOperand {
-    const void* hi;
-    const void* lo;
-    bool f16;     // FP16 operands (else BF16)
-    float scale;  // X was multiplied by this power of two
-};
-
 // largest power of two s with max |x| s <= 2^14 (1 for an all-zero x)
 int pow2_scale(sid_ctx* c, const float* x, int64_t n, float* scale, cudaStream_t st)
 {
@@ -771,7 +763,6 @@ int gemm_pix(sid_ctx* c, const PixOperand& x, int64_t P, int64_t k, const float*
                    (int64_t)(c->ws.bytes / sizeof(float)), c->errflag.as<int>(), st);
 }
 
-}  // namespace
 }  // namespace sid
 
 extern "C" int sid_s_update(sid_ctx* c, const void* Y, int ydtype, float* S, float* T, int64_t P, int64_t R,

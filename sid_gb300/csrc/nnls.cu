@@ -19,11 +19,20 @@
 // reference's FP64 arithmetic and its convergence test can fire.  With a
 // gradient recomputed from a 16- or 32-bit product every iteration the steps
 // stall at the product's noise floor and no column ever retires early.
+// What the incremental gradient does carry is the drift of every increment's
+// rounding, so the increments are formed close to FP32 accuracy: on the tensor
+// cores the Gram (|G| <= 1 after normalisation, scaled by 2^14) and each
+// column of d (scaled by its own power of two 2^e_j, found by the mask kernel)
+// enter as FP16 hi/lo pairs (22 significant bits each; hi*hi + hi*lo + lo*hi
+// with FP32 accumulation), and the step kernel multiplies G d by 2^-e_j.
+// BF16 hi/lo pairs (16 bits) let the gradient drift by about 1e-5 of |x|,
+// enough to move converged columns visibly away from the FP64 result.
 //
 // Every kernel reads the iteration number from device memory, so a chunk of
 // iterations is captured once in a CUDA graph and replayed.  A retired column
 // is frozen (never written again), which is what removing it from x does in
 // the reference (LS_nnls.m:158-168, fast_nnls.m:165-179).
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -46,6 +55,7 @@ int split16(const float* src, int64_t k, int64_t rows, int64_t lds, uint16_t* hi
             float scale, cudaStream_t st);
 int64_t blk16_elems(int64_t k, int64_t rows);
 int ctx_sync(sid_ctx* c, cudaStream_t st);
+int absmax(const float* x, int64_t n, unsigned int* out, cudaStream_t st);
 
 struct NnlsCounters {
     int iter;    // LS_nnls: iteration number; fast_nnls: the reference's s
@@ -90,6 +100,8 @@ struct ColBufs {
     float *u, *gu;       // use_std: column-sum vector and G * it
     const float* Gf;     // K x K FP32 (normalised) Gram: the clamp corrections of G * step
     int sparse;          // G * step formed in the step kernel (no second contraction)
+    int f16s;            // tensor-core operand as FP16 hi/lo of d * 2^e_j (per-column power of two)
+    float* dsc;          // per column: 2^-e_j, applied to the contraction result
     int* active;
     NnlsCounters* cnt;
     int F;
@@ -108,6 +120,26 @@ __device__ __forceinline__ void put_operand(const ColBufs& b, int64_t o, int j, 
     } else {
         b.v[o + k] = val;
     }
+}
+
+// FP16 hi/lo of v (|v| <= 2^14, a scaled operand), K-blocked like put_operand
+__device__ __forceinline__ void put_operand_f16(const ColBufs& b, int j, int k, float v)
+{
+    const int64_t i = (((int64_t)(k >> 6) * b.F + j) << 6) + (k & 63);
+    const __half h = __float2half_rn(v);
+    b.vhi[i] = __half_as_ushort(h);
+    b.vlo[i] = __half_as_ushort(__float2half_rn(v - __half2float(h)));
+}
+
+// Power of two 2^e with amax * 2^e in [2^13, 2^14) (1 for amax == 0): FP16
+// hi/lo of the scaled values then keep 22 significant bits of each entry
+// relative to its column's largest, in FP16's normal range.
+__device__ __forceinline__ float pow2_for(float amax)
+{
+    if (!(amax > 0.f) || !isfinite(amax)) return 1.f;
+    int ex;
+    frexpf(amax, &ex);  // amax in [2^(ex-1), 2^ex)
+    return ldexpf(1.f, max(-126, min(126, 14 - ex)));
 }
 
 __global__ void k_iter_inc(NnlsCounters* c) { c->iter += 1; }
@@ -201,9 +233,10 @@ __global__ void __launch_bounds__(256) k_nn_mask(ColBufs b, int K, int F, int us
     __shared__ float2 red[kColsPerCta][kWarpsPerCol][2];
     __shared__ float redm[kColsPerCta][kWarpsPerCol];
     __shared__ int redn[kColsPerCta][kWarpsPerCol];
+    __shared__ float reda[kColsPerCta][kWarpsPerCol];
     const ColIdx c = col_idx();
     const bool act = c.j < F && b.active[c.j];
-    float acc_f = 0.f, accw_f = 0.f, mx_f = -INFINITY;
+    float acc_f = 0.f, accw_f = 0.f, mx_f = -INFINITY, am_f = 0.f;
     int np_i = 0;
     if (act) {
         const int64_t o = (int64_t)c.j * K;
@@ -216,7 +249,8 @@ __global__ void __launch_bounds__(256) k_nn_mask(ColBufs b, int K, int F, int us
             b.df[o + k] = dv;
             const bool p = xv.x > 0.f || dv.x < 0.f;
             const float dm = p ? dv.x + dv.y : 0.f;
-            put_operand(b, o, c.j, k, dm);
+            if (b.f16s) am_f = fmaxf(am_f, fabsf(dm));
+            else put_operand(b, o, c.j, k, dm);
             wide_fma(dm, dm, acc_f, accw_f);
             np_i += p ? 1 : 0;
             mx_f = fmaxf(mx_f, xv.x);
@@ -226,13 +260,28 @@ __global__ void __launch_bounds__(256) k_nn_mask(ColBufs b, int K, int F, int us
     const float2 accw = warp_sum_ff(accw_f);
     const int np = __reduce_add_sync(0xffffffffu, np_i);
     const float mx = warp_max_f(mx_f);
+    const float am = warp_max_f(am_f);
     if (c.lane == 0) {
         red[c.cl][c.wc][0] = acc;
         red[c.cl][c.wc][1] = accw;
         redn[c.cl][c.wc] = np;
         redm[c.cl][c.wc] = mx;
+        reda[c.cl][c.wc] = am;
     }
     __syncthreads();
+    if (b.f16s && act) {
+        // second pass: the scaled FP16 hi/lo operand (d read back from the updated df)
+        float amax = reda[c.cl][0];
+        for (int w = 1; w < kWarpsPerCol; ++w) amax = fmaxf(amax, reda[c.cl][w]);
+        const float sc = pow2_for(amax);
+        const int64_t o = (int64_t)c.j * K;
+        for (int k = c.wc * 32 + c.lane; k < K; k += kColThreads) {
+            const float2 xv = b.x[o + k], dv = b.df[o + k];
+            const float dm = (xv.x > 0.f || dv.x < 0.f) ? dv.x + dv.y : 0.f;
+            put_operand_f16(b, c.j, k, dm * sc);
+        }
+        if (c.wc == 0 && c.lane == 0) b.dsc[c.j] = 1.f / sc;
+    }
     if (act && c.wc == 0 && c.lane == 0) {
         float2 s = red[c.cl][0][0], sw = red[c.cl][0][1];
         int n = redn[c.cl][0];
@@ -346,13 +395,14 @@ __global__ void __launch_bounds__(256) k_nn_step(ColBufs b, int K, int F, int so
     const ColIdx c = col_idx();
     const bool act = c.j < F && b.active[c.j];
     const int64_t o = (int64_t)c.j * K;
+    const float gsc = (b.f16s && act) ? b.dsc[c.j] : 1.f;  // undoes the operand's power-of-two scale
     float s2_f = 0.f, s2w_f = 0.f;
     if (act) {
 #pragma unroll 2
         for (int k = c.wc * 32 + c.lane; k < K; k += kColThreads) {
             const float2 xv = b.x[o + k], dv = b.df[o + k];
             const float dm = (xv.x > 0.f || dv.x < 0.f) ? dv.x + dv.y : 0.f;
-            float g = b.g[o + k];
+            float g = b.g[o + k] * gsc;
             if (use_std) g -= b.gu[k];
             wide_fma(dm, g, s2_f, s2w_f);
         }
@@ -454,7 +504,7 @@ __global__ void __launch_bounds__(256) k_nn_step(ColBufs b, int K, int F, int so
         }
         if (e >= 0) b.test[(int64_t)(e % sample) * F + c.j] = (double)t;
     }
-    if (b.sparse) gstep_sparse(b, K, c, act, o, alpha_f, cc, cmask);
+    if (b.sparse) gstep_sparse(b, K, c, act, o, alpha_f * gsc, cc, cmask);
 }
 
 // df = df + G x0 for a warm start with use_std (G x0 minus its column-sum term)
@@ -645,6 +695,188 @@ __global__ void k_fill_int(int* __restrict__ a, int n, int v)
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) a[i] = v;
 }
 
+// --------------------------------------------- warm_start == 1 (fast_nnls.m:66-69) --
+// x = inv(Q) (-df) by Gauss-Jordan elimination with partial pivoting on the
+// augmented FP64 matrix M = [Q | -df] (K x (K + F), column-major): after
+// step j column j is e_j, and at the end the right block holds inv(Q) (-df)
+// (MATLAB forms inv(Q) and multiplies; the solve is the same product without
+// the explicit inverse).  A zero pivot sets *err (MATLAB warns that Q is
+// singular and returns Inf/NaN).
+__global__ void __launch_bounds__(1024) k_gj_pivot(double* __restrict__ M, int K, int64_t ncols, int j,
+                                                   int* __restrict__ err)
+{
+    __shared__ double bv[32];
+    __shared__ int bi[32];
+    __shared__ int piv;
+    double best = -1.0;
+    int arg = j;
+    for (int i = j + threadIdx.x; i < K; i += blockDim.x) {
+        const double v = fabs(M[i + (int64_t)K * j]);
+        if (v > best) { best = v; arg = i; }
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        const double ov = __shfl_xor_sync(0xffffffffu, best, off);
+        const int oi = __shfl_xor_sync(0xffffffffu, arg, off);
+        if (ov > best || (ov == best && oi < arg)) { best = ov; arg = oi; }
+    }
+    if ((threadIdx.x & 31) == 0) { bv[threadIdx.x >> 5] = best; bi[threadIdx.x >> 5] = arg; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double b = -1.0;
+        int a = j;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w)
+            if (bv[w] > b || (bv[w] == b && bi[w] < a)) { b = bv[w]; a = bi[w]; }
+        piv = a;
+        if (!(b > 0.0)) atomicExch(err, 1);
+    }
+    __syncthreads();
+    const int p = piv;
+    // swap rows j and p, then scale row j by the pivot (columns j.., column j becomes 1)
+    for (int64_t c = j + threadIdx.x; c < ncols; c += blockDim.x) {
+        const double a = M[j + (int64_t)K * c], b = M[p + (int64_t)K * c];
+        M[j + (int64_t)K * c] = b;
+        M[p + (int64_t)K * c] = a;
+    }
+    __syncthreads();
+    const double inv = 1.0 / M[j + (int64_t)K * j];
+    __syncthreads();
+    for (int64_t c = j + threadIdx.x; c < ncols; c += blockDim.x) M[j + (int64_t)K * c] *= inv;
+}
+
+__global__ void k_gj_elim(double* __restrict__ M, int K, int64_t ncols, int j)
+{
+    const int64_t w = ncols - j - 1;  // columns after j
+    const int64_t n = (int64_t)K * w;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+        const int i = (int)(e % K);
+        const int64_t c = j + 1 + e / K;
+        if (i == j) continue;
+        M[i + (int64_t)K * c] -= M[i + (int64_t)K * j] * M[j + (int64_t)K * c];
+    }
+}
+
+// M = [Q | -df] in FP64
+__global__ void k_gj_load(const float* __restrict__ G, const float2* __restrict__ df, int K, int64_t F,
+                          double* __restrict__ M)
+{
+    const int64_t n = (int64_t)K * (K + F);
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t c = e / K;
+        M[e] = c < K ? (double)G[e] : -dd_to(df[e - (int64_t)K * K]);
+    }
+}
+
+// x = max(inv(Q)(-df), 0) as the double-float iterate and its FP32 copy
+__global__ void k_gj_store(const double* __restrict__ M, int K, int64_t F, float2* __restrict__ x,
+                           float* __restrict__ xf)
+{
+    const int64_t n = (int64_t)K * F;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+        double v = M[(int64_t)K * K + e];
+        if (v < 0.0) v = 0.0;  // x(x<0) = 0
+        x[e] = dd_from(v);
+        xf[e] = (float)v;
+    }
+}
+
+// -------------------------------------------- opts.total (fast_nnls.m:101-117) --
+// One step length for all columns: alpha = sum(df_.^2) / sum(df_ .* (Q df_))
+// over the whole K x F block.  Per-block partial sums (FP32 two-sum pairs)
+// are reduced by one block into the device scalar alpha.
+__global__ void __launch_bounds__(256) k_tot_mask(ColBufs b, int64_t n, float2* __restrict__ part)
+{
+    float2 acc = make_float2(0.f, 0.f);
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+        const float2 xv = b.x[e], dv = b.df[e];
+        const float dm = (xv.x > 0.f || dv.x < 0.f) ? dv.x + dv.y : 0.f;  // df .* passive
+        b.v[e] = dm;
+        acc = ff_add(acc, make_float2(dm * dm, fmaf(dm, dm, -dm * dm)));
+    }
+    __shared__ float2 red[8];
+    for (int off = 16; off > 0; off >>= 1)
+        acc = ff_add(acc, make_float2(__shfl_xor_sync(0xffffffffu, acc.x, off), __shfl_xor_sync(0xffffffffu, acc.y, off)));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float2 s = red[0];
+        for (int w = 1; w < 8; ++w) s = ff_add(s, red[w]);
+        part[blockIdx.x] = s;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_tot_den(const float* __restrict__ v, const float* __restrict__ g, int64_t n,
+                                                 float2* __restrict__ part)
+{
+    float2 acc = make_float2(0.f, 0.f);
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+        const float a = v[e], c = g[e];
+        acc = ff_add(acc, make_float2(a * c, fmaf(a, c, -a * c)));
+    }
+    __shared__ float2 red[8];
+    for (int off = 16; off > 0; off >>= 1)
+        acc = ff_add(acc, make_float2(__shfl_xor_sync(0xffffffffu, acc.x, off), __shfl_xor_sync(0xffffffffu, acc.y, off)));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float2 s = red[0];
+        for (int w = 1; w < 8; ++w) s = ff_add(s, red[w]);
+        part[blockIdx.x] = s;
+    }
+}
+
+// alpha = sum(num parts) / sum(den parts); NaN -> 0 (fast_nnls.m:103)
+__global__ void k_tot_alpha(const float2* __restrict__ num, const float2* __restrict__ den, int nb,
+                            float* __restrict__ alpha)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double a = 0.0, c = 0.0;
+    for (int i = 0; i < nb; ++i) {
+        a += (double)num[i].x + (double)num[i].y;
+        c += (double)den[i].x + (double)den[i].y;
+    }
+    double al = a / c;
+    if (al != al) al = 0.0;
+    *alpha = (float)al;
+}
+
+// x_ = max(x - alpha df_, 0); v = x_ - x (the operand of Q (x_ - x)); x = x_
+__global__ void k_tot_step(ColBufs b, int64_t n, const float* __restrict__ alpha)
+{
+    const float al = *alpha;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+        const float2 xv = b.x[e];
+        const float pstep = b.v[e] * al;
+        float2 xn = dd_add(xv, -pstep);
+        float stp = -pstep;
+        if (xn.x < 0.f) {
+            xn = make_float2(0.f, 0.f);
+            stp = -(xv.x + xv.y);
+        }
+        b.x[e] = xn;
+        b.v[e] = stp;
+    }
+}
+
+// X = diag(h) * ones: the reference leaves xx at its initial ones in total
+// mode (fast_nnls.m:87 and the break at :113-115 never assigns it)
+__global__ void k_fill_h(float* __restrict__ X, const float* __restrict__ hs, int K, int64_t n)
+{
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x)
+        X[e] = hs[e % K];
+}
+
+__global__ void k_df_out(const float2* __restrict__ df, int64_t n, float* __restrict__ out)
+{
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x)
+        out[e] = (float)dd_to(df[e]);
+}
+
+__global__ void k_df_from(const float* __restrict__ src, int64_t n, float2* __restrict__ df)
+{
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x)
+        df[e] = make_float2(src[e], 0.f);
+}
+
 // ------------------------------------------------------------ host driver --
 static std::vector<double> fit_matrix(int sample)
 {
@@ -672,6 +904,8 @@ struct NnlsWork {
     float* hs;     // K scaling (fast_nnls)
     uint16_t *Ghi, *Glo;
     bool split;
+    bool f16s;      // Gram and iteration operands as scaled FP16 hi/lo (else BF16 hi/lo)
+    float gscale;   // power of two applied to the Gram before its FP16 split (max|G| * gscale in [2^13, 2^14))
 };
 
 static int alloc_work(sid_ctx* c, int64_t K, int64_t F, int sample, bool split, NnlsWork* w, cudaStream_t st)
@@ -683,7 +917,7 @@ static int alloc_work(sid_ctx* c, int64_t K, int64_t F, int sample, bool split, 
     SID_TRY(nn[2].alloc(KF * 4));  // v / h
     SID_TRY(nn[3].alloc(KF * 4));  // g
     SID_TRY(nn[4].alloc((size_t)sample * F * 8));
-    SID_TRY(nn[5].alloc((size_t)(6 * F + 2 * sample + 8) * 8));
+    SID_TRY(nn[5].alloc((size_t)(7 * F + 2 * sample + 8) * 8));
     SID_TRY(nn[6].alloc((size_t)F * 4 + 64));
     SID_TRY(nn[7].alloc((size_t)(K * K + 3 * K + 16) * 4));
     SID_TRY(nn[10].alloc(KF * 4));  // h
@@ -708,6 +942,7 @@ static int alloc_work(sid_ctx* c, int64_t K, int64_t F, int sample, bool split, 
     b.anyp = reinterpret_cast<float*>(sc + 4 * F);
     b.xmax = reinterpret_cast<float*>(sc + 5 * F);
     b.xi = sc + 6 * F;
+    b.dsc = reinterpret_cast<float*>(sc + 6 * F + 2 * sample + 8);
     b.active = nn[6].as<int>();
     b.cnt = reinterpret_cast<NnlsCounters*>(nn[6].as<uint8_t>() + cdiv(F * 4, 16) * 16);
     float* fs = nn[7].as<float>();
@@ -722,7 +957,45 @@ static int alloc_work(sid_ctx* c, int64_t K, int64_t F, int sample, bool split, 
     w->Ghi = split ? nn[11].as<uint16_t>() : nullptr;
     w->Glo = split ? nn[12].as<uint16_t>() : nullptr;
     w->split = split;
+    w->f16s = false;
+    w->gscale = 1.f;
+    b.f16s = 0;
     return SID_OK;
+}
+
+// Operand format of the iterations: scaled FP16 hi/lo in sparse mode (one
+// contraction per iteration; the operand is d, whose column scale the mask
+// kernel finds), BF16 hi/lo otherwise (use_std's column sums and the dense
+// mode's second operand read BF16).
+static bool f16_operands(const NnlsWork& w, int64_t K, bool use_std)
+{
+    return w.split && !use_std && K <= (int64_t)kStepRows * kColThreads;
+}
+
+// 16-bit split of the (normalised) Gram in the format the iterations use.  The
+// FP16 split scales the Gram by the power of two that puts its largest entry
+// in [2^13, 2^14) (2^14 for fast_nnls's normalised Gram, whose diagonal is 1).
+static int split_gram(sid_ctx* c, NnlsWork& w, int64_t K, bool f16s, cudaStream_t st)
+{
+    w.f16s = f16s;
+    w.b.f16s = f16s ? 1 : 0;
+    w.gscale = 1.f;
+    if (!w.split) return SID_OK;
+    if (f16s) {
+        SID_TRY(c->scal.alloc(64));
+        SID_TRY(absmax(w.G, K * K, c->scal.as<unsigned int>(), st));
+        unsigned int bits = 0;
+        SID_CUDA_TRY(cudaMemcpyAsync(&bits, c->scal.p, sizeof(bits), cudaMemcpyDeviceToHost, st));
+        SID_CUDA_TRY(cudaStreamSynchronize(st));
+        float mx;
+        std::memcpy(&mx, &bits, sizeof(mx));
+        if (mx > 0.f && std::isfinite(mx)) {
+            int ex;
+            std::frexp(mx, &ex);
+            w.gscale = std::ldexp(1.f, std::max(-126, std::min(126, 14 - ex)));
+        }
+    }
+    return split16(w.G, K, K, K, w.Ghi, w.Glo, !f16s, w.gscale, st);
 }
 
 // g = G * operand (operand = b.v or its BF16 split)
@@ -735,7 +1008,8 @@ static int gmul(sid_ctx* c, const NnlsWork& w, int64_t K, int64_t F, cudaStream_
     const void* Bs[3] = {w.b.vhi, w.b.vlo, w.b.vhi};
     int bn = 0, sk = 0;
     gemm_autotune((int)K, (int)F, (int)cdiv(K, 64), &bn, &sk);
-    return gemm_tn(As, Bs, 3, K, F, K, true, w.b.g, K, 1.f, 0.f, bn, sk, c->ws.as<float>(), (int64_t)(c->ws.bytes / 4),
+    return gemm_tn(As, Bs, 3, K, F, K, !w.f16s, w.b.g, K, 1.f / w.gscale, 0.f, bn, sk,
+                   c->ws.as<float>(), (int64_t)(c->ws.bytes / 4),
                    c->errflag.as<int>(), st);
 }
 
@@ -947,7 +1221,7 @@ extern "C" int sid_ls_nnls(sid_ctx* c, const float* A, const void* Y, int ydtype
         SID_CUDA_TRY(cudaStreamSynchronize(st));
         ys.release();
     }
-    if (split) SID_TRY(split16(w.G, K, K, K, w.Ghi, w.Glo, true, 1.f, st));
+    SID_TRY(split_gram(c, w, K, f16_operands(w, K, o->use_std != 0), st));
     // df = -h + G x0  (x0 = 0 unless given)
     k_df_init<<<1024, 256, 0, st>>>(w.h, nullptr, b.df, (int)K, K * F, o->lambda, SOLVER_LS);
     SID_CHECK_LAUNCH();
@@ -955,9 +1229,16 @@ extern "C" int sid_ls_nnls(sid_ctx* c, const float* A, const void* Y, int ydtype
         k_x_from<<<1024, 256, 0, st>>>(b.x, X, nullptr, (int)K, K * F);
         SID_CHECK_LAUNCH();
         SID_TRY(ensure_gemm_ws(c, K, F, split));
-        if (split) SID_TRY(split16(X, K, F, K, b.vhi, b.vlo, true, 1.f, st));
-        else SID_CUDA_TRY(cudaMemcpyAsync(b.v, X, (size_t)(K * F) * 4, cudaMemcpyDeviceToDevice, st));
-        SID_TRY(gmul(c, w, K, F, st));
+        if (o->use_std) {
+            // G x0 through the iterations' own operand (the column-sum kernel reads it)
+            if (split) SID_TRY(split16(X, K, F, K, b.vhi, b.vlo, true, 1.f, st));
+            else SID_CUDA_TRY(cudaMemcpyAsync(b.v, X, (size_t)(K * F) * 4, cudaMemcpyDeviceToDevice, st));
+            SID_TRY(gmul(c, w, K, F, st));
+        } else {
+            // G x0 once, FP32
+            SID_TRY(sgemm_tn(w.G, X, K, F, K, K, K, b.g, K, 1.f, 0.f, c->ws.as<float>(), (int64_t)(c->ws.bytes / 4),
+                             st));
+        }
         if (o->use_std) {
             // the start gradient needs G(x0) - G sum(x0,2)/F
             k_fill_int<<<64, 256, 0, st>>>(b.active, (int)F, 1);
@@ -983,54 +1264,158 @@ extern "C" int sid_ls_nnls(sid_ctx* c, const float* A, const void* Y, int ydtype
     return ctx_sync(c, st);
 }
 
-extern "C" int sid_fast_nnls(sid_ctx* c, const float* A, const void* Y, int ydtype, int64_t P, int64_t K, int64_t F,
-                             const sid_nnls_opts* o, const float* warm_start, float* X, float* Q_out, int prec,
-                             int32_t* iters, void* stream)
+// x = inv(Q)(-df), clamped, as the start (fast_nnls.m:66-69); xf: FP32 copy
+static int warm_inverse(sid_ctx* c, NnlsWork& w, int64_t K, int64_t F, cudaStream_t st)
 {
-    SID_TRY(nnls_common_checks(c, A, Y, ydtype, P, K, F, o, prec));
-    SID_REQUIRE(X, "fast_nnls: X is NULL");
+    DBuf& m = c->nn[15];
+    SID_TRY(m.alloc((size_t)(K * (K + F)) * 8 + 16));
+    double* M = m.as<double>();
+    int* err = reinterpret_cast<int*>(m.as<uint8_t>() + (size_t)(K * (K + F)) * 8);
+    SID_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), st));
+    k_gj_load<<<2048, 256, 0, st>>>(w.G, w.b.df, (int)K, F, M);
+    SID_CHECK_LAUNCH();
+    const int64_t ncols = K + F;
+    for (int j = 0; j < (int)K; ++j) {
+        k_gj_pivot<<<1, 1024, 0, st>>>(M, (int)K, ncols, j, err);
+        const int64_t n = K * (ncols - j - 1);
+        if (n > 0) k_gj_elim<<<(unsigned)std::min<int64_t>(cdiv(n, 256), 4096), 256, 0, st>>>(M, (int)K, ncols, j);
+    }
+    SID_CHECK_LAUNCH();
+    int he = 0;
+    SID_CUDA_TRY(cudaMemcpyAsync(&he, err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    SID_CUDA_TRY(cudaStreamSynchronize(st));
+    SID_REQUIRE(!he, "fast_nnls: warm_start == 1 needs inv(Q), and Q is singular");
+    k_gj_store<<<1024, 256, 0, st>>>(M, (int)K, F, w.b.x, w.b.v);
+    SID_CHECK_LAUNCH();
+    return SID_OK;
+}
+
+// opts.total: max_iter iterations with one step length for all columns
+static int total_iterations(sid_ctx* c, NnlsWork& w, int64_t K, int64_t F, int max_iter, cudaStream_t st)
+{
+    ColBufs& b = w.b;
+    const int64_t n = K * F;
+    const int nb = 512;
+    DBuf& pb = c->nn[13];
+    SID_TRY(pb.alloc((size_t)(2 * nb) * sizeof(float2) + 16));
+    float2* pnum = pb.as<float2>();
+    float2* pden = pnum + nb;
+    float* alpha = reinterpret_cast<float*>(pden + nb);
+    SID_TRY(c->ws.alloc((size_t)std::max<int64_t>(sgemm_ws_elems(K, F, K), 1) * 4));
+    // the loop breaks once s > max_iter after an iteration (fast_nnls.m:112-116): max(max_iter, 1) iterations
+    for (int it = 0; it < std::max(max_iter, 1); ++it) {
+        k_tot_mask<<<nb, 256, 0, st>>>(b, n, pnum);
+        SID_TRY(sgemm_tn(w.G, b.v, K, F, K, K, K, b.g, K, 1.f, 0.f, c->ws.as<float>(), (int64_t)(c->ws.bytes / 4),
+                         st));
+        k_tot_den<<<nb, 256, 0, st>>>(b.v, b.g, n, pden);
+        k_tot_alpha<<<1, 32, 0, st>>>(pnum, pden, nb, alpha);
+        k_tot_step<<<1024, 256, 0, st>>>(b, n, alpha);
+        SID_CHECK_LAUNCH();
+        // df = df + Q (x_ - x)   fast_nnls.m:106
+        SID_TRY(sgemm_tn(w.G, b.v, K, F, K, K, K, b.g, K, 1.f, 0.f, c->ws.as<float>(), (int64_t)(c->ws.bytes / 4),
+                         st));
+        k_add_g<<<1024, 256, 0, st>>>(b.df, b.g, n);
+        SID_CHECK_LAUNCH();
+    }
+    return SID_OK;
+}
+
+extern "C" int sid_fast_nnls_ex(sid_ctx* c, const float* A, const void* Y, int ydtype, int64_t P, int64_t K, int64_t F,
+                                const sid_nnls_opts* o, int total, int warm_mode, const float* W, const float* Q_in,
+                                const float* df_in, const float* h_in, float* X, float* Q_out, float* df_out,
+                                float* h_out, int prec, int32_t* iters, void* stream)
+{
+    SID_REQUIRE(c && o && X, "fast_nnls: NULL argument");
+    SID_REQUIRE(K > 0 && F > 0, "fast_nnls: empty problem (K=%lld F=%lld)", (long long)K, (long long)F);
+    SID_REQUIRE(prec == SID_PREC_FP32 || prec == SID_PREC_SPLIT, "NNLS: precision must be FP32 or SPLIT");
+    SID_REQUIRE(o->sample >= 1 && o->max_iter >= 0, "NNLS: sample must be >= 1 and max_iter >= 0");
     SID_REQUIRE(o->tol_p == 1 || o->tol_p == 2, "fast_nnls: tol_p must be 1 or 2");
+    SID_REQUIRE(warm_mode >= 0 && warm_mode <= 2, "fast_nnls: warm_mode must be 0, 1 or 2");
+    SID_REQUIRE(warm_mode != 2 || W, "fast_nnls: warm_mode 2 needs the warm-start matrix");
+    SID_REQUIRE(!Q_in == !h_in, "fast_nnls: Q and h are given together (fast_nnls.m:58-62)");
+    const bool need_a = !Q_in || !df_in;
+    if (need_a) {
+        SID_REQUIRE(A && Y && P > 0, "fast_nnls: A and Y are needed to form %s", !Q_in ? "Q" : "df");
+        SID_REQUIRE(ydtype == SID_DTYPE_F32 || ydtype == SID_DTYPE_F16, "NNLS: unknown Y dtype %d", ydtype);
+    }
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const bool split = prec == SID_PREC_SPLIT;
     NnlsWork w;
     SID_TRY(alloc_work(c, K, F, (int)o->sample, split, &w, st));
     ColBufs& b = w.b;
     const bool f16 = ydtype == SID_DTYPE_F16;
-    // Q = A'A normalised, hs = 1./sqrt(diag), df = diag(hs)(-A'Y + lambda)   (fast_nnls.m:53-57)
-    SID_TRY(contract(c, A, A, false, K, K, P, P, P, w.G, K, 1.f, 0.f, prec, st));
-    k_diag_rsqrt<<<cdiv(K, 256), 256, 0, st>>>(w.G, w.hs, (int)K);
-    SID_CHECK_LAUNCH();
-    k_normalise_gram<<<1024, 256, 0, st>>>(w.G, w.hs, (int)K);
-    SID_CHECK_LAUNCH();
-    SID_TRY(contract(c, A, Y, f16, K, F, P, P, P, w.h, K, 1.f, 0.f, f16 ? SID_PREC_SPLIT : prec, st));
-    k_df_init<<<1024, 256, 0, st>>>(w.h, w.hs, b.df, (int)K, K * F, o->lambda, SOLVER_FAST);
-    SID_CHECK_LAUNCH();
-    if (split) SID_TRY(split16(w.G, K, K, K, w.Ghi, w.Glo, true, 1.f, st));
-    if (warm_start) {
-        // x = diag(1./hs) W; df = df + Q x   (fast_nnls.m:72-73)
-        k_x_from<<<1024, 256, 0, st>>>(b.x, warm_start, w.hs, (int)K, K * F);
+    if (Q_in) {
+        // the caller's normalised Gram and scaling (fast_nnls.m:58-62)
+        SID_CUDA_TRY(cudaMemcpyAsync(w.G, Q_in, (size_t)(K * K) * 4, cudaMemcpyDeviceToDevice, st));
+        SID_CUDA_TRY(cudaMemcpyAsync(w.hs, h_in, (size_t)K * 4, cudaMemcpyDeviceToDevice, st));
+    } else {
+        // Q = A'A normalised, hs = 1./sqrt(diag)   (fast_nnls.m:53-56)
+        SID_TRY(contract(c, A, A, false, K, K, P, P, P, w.G, K, 1.f, 0.f, prec, st));
+        k_diag_rsqrt<<<cdiv(K, 256), 256, 0, st>>>(w.G, w.hs, (int)K);
         SID_CHECK_LAUNCH();
-        // FP32 copy of x as the contraction operand
-        float* xf = w.h;  // h is no longer needed
-        k_x_out<<<1024, 256, 0, st>>>(xf, b.x, nullptr, (int)K, K * F);
+        k_normalise_gram<<<1024, 256, 0, st>>>(w.G, w.hs, (int)K);
         SID_CHECK_LAUNCH();
-        SID_TRY(ensure_gemm_ws(c, K, F, split));
-        if (split) SID_TRY(split16(xf, K, F, K, b.vhi, b.vlo, true, 1.f, st));
-        else SID_CUDA_TRY(cudaMemcpyAsync(b.v, xf, (size_t)(K * F) * 4, cudaMemcpyDeviceToDevice, st));
-        SID_TRY(gmul(c, w, K, F, st));
-        k_add_g<<<1024, 256, 0, st>>>(b.df, b.g, K * F);
+    }
+    if (df_in) {
+        k_df_from<<<1024, 256, 0, st>>>(df_in, K * F, b.df);
         SID_CHECK_LAUNCH();
+    } else {
+        // df = diag(hs)(-A'Y + lambda)   (fast_nnls.m:57,60)
+        SID_TRY(contract(c, A, Y, f16, K, F, P, P, P, w.h, K, 1.f, 0.f, f16 ? SID_PREC_SPLIT : prec, st));
+        k_df_init<<<1024, 256, 0, st>>>(w.h, w.hs, b.df, (int)K, K * F, o->lambda, SOLVER_FAST);
+        SID_CHECK_LAUNCH();
+    }
+    SID_TRY(split_gram(c, w, K, f16_operands(w, K, false), st));
+    SID_TRY(ensure_gemm_ws(c, K, F, split));
+    if (warm_mode == 2) {
+        // x = diag(1./hs) W   (fast_nnls.m:72)
+        k_x_from<<<1024, 256, 0, st>>>(b.x, W, w.hs, (int)K, K * F);
+        SID_CHECK_LAUNCH();
+        k_x_out<<<1024, 256, 0, st>>>(b.v, b.x, nullptr, (int)K, K * F);
+        SID_CHECK_LAUNCH();
+    } else if (warm_mode == 1) {
+        SID_TRY(warm_inverse(c, w, K, F, st));
     } else {
         SID_CUDA_TRY(cudaMemsetAsync(b.x, 0, (size_t)(K * F) * 8, st));
     }
-    std::vector<float> hs(K);
-    SID_CUDA_TRY(cudaMemcpyAsync(hs.data(), w.hs, (size_t)K * 4, cudaMemcpyDeviceToHost, st));
-    SID_CUDA_TRY(cudaStreamSynchronize(st));
-    double hmax = -INFINITY;
-    for (float v : hs) hmax = std::max(hmax, (double)v);
-    SID_TRY(iterate(c, w, K, F, SOLVER_FAST, o, hmax, iters, st));
-    k_x_out<<<1024, 256, 0, st>>>(X, b.x, w.hs, (int)K, K * F);
-    SID_CHECK_LAUNCH();
+    if (warm_mode) {
+        // df = df + Q x   (fast_nnls.m:69,73), once in FP32
+        SID_TRY(sgemm_tn(w.G, b.v, K, F, K, K, K, b.g, K, 1.f, 0.f, c->ws.as<float>(), (int64_t)(c->ws.bytes / 4), st));
+        k_add_g<<<1024, 256, 0, st>>>(b.df, b.g, K * F);
+        SID_CHECK_LAUNCH();
+    }
+    if (total) {
+        SID_TRY(total_iterations(c, w, K, F, (int)o->max_iter, st));
+        k_fill_h<<<1024, 256, 0, st>>>(X, w.hs, (int)K, K * F);
+        SID_CHECK_LAUNCH();
+        if (df_out) {
+            k_df_out<<<1024, 256, 0, st>>>(b.df, K * F, df_out);
+            SID_CHECK_LAUNCH();
+        }
+        if (iters) {
+            k_fill_int<<<64, 256, 0, st>>>(iters, (int)F, (int)o->max_iter + 1);
+            SID_CHECK_LAUNCH();
+        }
+    } else {
+        std::vector<float> hs(K);
+        SID_CUDA_TRY(cudaMemcpyAsync(hs.data(), w.hs, (size_t)K * 4, cudaMemcpyDeviceToHost, st));
+        SID_CUDA_TRY(cudaStreamSynchronize(st));
+        double hmax = -INFINITY;
+        for (float v : hs) hmax = std::max(hmax, (double)v);
+        SID_TRY(iterate(c, w, K, F, SOLVER_FAST, o, hmax, iters, st));
+        k_x_out<<<1024, 256, 0, st>>>(X, b.x, w.hs, (int)K, K * F);
+        SID_CHECK_LAUNCH();
+    }
     if (Q_out) SID_CUDA_TRY(cudaMemcpyAsync(Q_out, w.G, (size_t)(K * K) * 4, cudaMemcpyDeviceToDevice, st));
+    if (h_out) SID_CUDA_TRY(cudaMemcpyAsync(h_out, w.hs, (size_t)K * 4, cudaMemcpyDeviceToDevice, st));
     return ctx_sync(c, st);
+}
+
+extern "C" int sid_fast_nnls(sid_ctx* c, const float* A, const void* Y, int ydtype, int64_t P, int64_t K, int64_t F,
+                             const sid_nnls_opts* o, const float* warm_start, float* X, float* Q_out, int prec,
+                             int32_t* iters, void* stream)
+{
+    SID_TRY(nnls_common_checks(c, A, Y, ydtype, P, K, F, o, prec));
+    return sid_fast_nnls_ex(c, A, Y, ydtype, P, K, F, o, 0, warm_start ? 2 : 0, warm_start, nullptr, nullptr,
+                            nullptr, X, Q_out, nullptr, nullptr, prec, iters, stream);
 }

@@ -117,6 +117,15 @@ struct KTimer {
     }
 };
 
+// A pixel-major P x k factor in the K-blocked 16-bit layout of the tensor-core
+// GEMM (nmf.cu pix_operand / gemm_pix): hi (and lo for a split FP32 factor).
+struct PixOperand {
+    const void* hi;
+    const void* lo;
+    bool f16;     // FP16 operands (else BF16)
+    float scale;  // X was multiplied by this power of two
+};
+
 // Lenslet-tap geometry shared by the direct and spectral projectors.
 struct TapGeom {
     int64_t N, Z, X, Y, Lx, Ly;

@@ -8,7 +8,8 @@
 // on the original template (a pixel is solved once, by the first neuron that
 // reaches it, with every neuron covering it), so all pixel problems are
 // independent and run here in one launch:
-//   1. G = T T' (R x R) and C = Y T' (P x R)  -- contractions;
+//   1. G = T T' (R x R, FP32) and C = Y T' (P x R, tensor cores, FP16 hi/lo
+//      operands, FP32 accumulation)  -- contractions;
 //   2. per pixel: ||y||, sum(y), and the covering neurons in ascending order,
 //      background last (update_spatial_component.m:59-79);
 //   3. per pixel, FP64: Q = G(idx,idx) + l2*I + lo*hilf [- s s'/F],
@@ -17,6 +18,7 @@
 //      (NQP.m:93-178, default options), x * ||y|| into the forward model;
 //   4. pixels outside every template get the background row C(p, bg)
 //      (update_spatial_component.m:128-131).
+#include <algorithm>
 #include <cfloat>
 #include <vector>
 
@@ -27,8 +29,13 @@ namespace sid {
 int contract(sid_ctx* c, const float* A, const void* B, bool b_f16, int64_t m, int64_t n, int64_t k, int64_t lda,
              int64_t ldb, float* C, int64_t ldc, float alpha, float beta, int prec, cudaStream_t st);
 int ctx_sync(sid_ctx* c, cudaStream_t st);
+int pix_operand(sid_ctx* c, int slot, const void* X, bool x_f16, int64_t P, int64_t k, int prec, PixOperand* op,
+                cudaStream_t st);
+int gemm_pix(sid_ctx* c, const PixOperand& x, int64_t P, int64_t k, const float* W, int64_t n, int64_t ldw,
+             float* C, int prec, cudaStream_t st);
 
-constexpr int kNqpMax = 32;  // largest number of components covering one pixel
+constexpr int kNqpMax = 32;          // components per problem solved with local working arrays
+constexpr int kNqpLargeMax = 4096;   // sid_nqp_batched's largest n (scratch working arrays above kNqpMax)
 
 // --------------------------------------------- C = Y T' (FP32, NT layout) --
 // C (m x n, col-major) = A B' with A m x k (m contiguous) and B n x k (n
@@ -154,18 +161,51 @@ struct SpatialOpts {
 // for n <= kNqpMax.  Qij(i, j) returns Q(i, j); b is NQP's internal right-hand
 // side (minus the linear term); w receives the final w = b - Q x.  Returns 0,
 // or 2 at the iteration cap (NQP.m:116-119); *iters = iterations taken.
-template <class QF>
-__device__ int nqp_solve(int n, const QF& Qij, const double* b, double* x, double* w, int* iters)
+// Working arrays of one solve: z, wsc, t (n each), L (packed lower triangle,
+// row-major, n(n+1)/2), pn (n ints), Pset (n flags).  Problems with n <=
+// kNqpMax keep them in the thread's local arrays; larger ones in a slice of a
+// global scratch buffer.
+struct NqpWs {
+    double *z, *wsc, *t, *L;
+    int* pn;
+    uint8_t* Pset;
+};
+
+// Scratch of one large problem (n <= nm), in doubles: L, z, wsc, t, b, x, w,
+// then pn and idx (nm ints each) and Pset (nm bytes).
+__host__ __device__ inline int64_t nqp_scratch_doubles(int64_t nm) { return nm * (nm + 1) / 2 + 6 * nm + nm + nm / 8 + 2; }
+
+__device__ inline NqpWs nqp_ws_at(double* base, int nm, double** b, double** x, double** w, int** idx)
 {
-    double z[kNqpMax], wsc[kNqpMax], t[kNqpMax];
-    double L[kNqpMax * (kNqpMax + 1) / 2];  // packed lower triangle, row-major
-    int pn[kNqpMax];
-    bool Pset[kNqpMax];
+    NqpWs ws;
+    ws.L = base;
+    double* d = base + (int64_t)nm * (nm + 1) / 2;
+    ws.z = d;
+    ws.wsc = d + nm;
+    ws.t = d + 2 * nm;
+    *b = d + 3 * nm;
+    *x = d + 4 * nm;
+    *w = d + 5 * nm;
+    ws.pn = reinterpret_cast<int*>(d + 6 * nm);
+    *idx = ws.pn + nm;
+    ws.Pset = reinterpret_cast<uint8_t*>(*idx + nm);
+    return ws;
+}
+
+template <class QF>
+__device__ int nqp_solve(int n, const QF& Qij, const double* b, double* x, double* w, const NqpWs& ws, int* iters)
+{
+    double* z = ws.z;
+    double* wsc = ws.wsc;
+    double* t = ws.t;
+    double* L = ws.L;
+    int* pn = ws.pn;
+    uint8_t* Pset = ws.Pset;
     for (int i = 0; i < n; ++i) {
         w[i] = b[i];  // w = -b_input, NQP.m:122
         x[i] = 0.0;
         wsc[i] = 0.0;
-        Pset[i] = false;
+        Pset[i] = 0;
     }
     const double tol = 3.0 * DBL_EPSILON;
     double wsc0 = 0.0;
@@ -189,7 +229,7 @@ __device__ int nqp_solve(int n, const QF& Qij, const double* b, double* x, doubl
             const double v = w[i] - wsc[i];
             if (best < 0 || v > bv) { best = i; bv = v; }
         }
-        Pset[best] = true;
+        Pset[best] = 1;
         pn2 = pn1 + 1;
         pn[pn2 - 1] = best;
         for (;;) {
@@ -252,7 +292,7 @@ __device__ int nqp_solve(int n, const QF& Qij, const double* b, double* x, doubl
                 wsc[worst] = (fabs(acc) + wsc[worst]) * 2.0;
                 w[worst] = acc;
             }
-            Pset[worst] = false;
+            Pset[worst] = 0;
             for (int i = 0; i < n; ++i) x[i] = x[i] - alpha * (x[i] - z[i]);
             int pos = 0;
             while (pn[pos] != worst) ++pos;
@@ -267,87 +307,147 @@ done:
     return st;
 }
 
+struct PixelArgs {
+    const uint8_t* tmpl;
+    int Rt;
+    int64_t P;
+    const float* G;
+    int R;
+    const float* C;
+    int64_t ldc;
+    const float *pnrm, *psum, *tsum;
+    int F;
+    SpatialOpts o;
+    float* out;
+    int* status;
+    int* nfail;
+};
+
+// Solve pixel p's problem over the components idx[0..n) (background last when
+// bg_sub): Q(i,j) and b = -q (NQP works with b = -q, NQP.m:145), reg_nnls.m:48-67.
+__device__ void pixel_solve(const PixelArgs& a, int64_t p, const int* idx, int n, double* b, double* x, double* w,
+                            const NqpWs& ws)
+{
+    const SpatialOpts& o = a.o;
+    const double yn = (double)a.pnrm[p];
+    if (!(yn > 0.0)) {
+        for (int i = 0; i < n; ++i) a.out[idx[i] + (int64_t)a.R * p] = 0.f;
+        a.status[p] = 0;
+        return;
+    }
+    auto Qij = [&](int i, int j) -> double {
+        double v = (double)a.G[idx[i] + (int64_t)a.R * idx[j]];
+        if (i == j) v += o.l2;
+        else if (!(o.bg_sub && (i == n - 1 || j == n - 1))) v += o.lo;  // hilf = ones - eye, bg row/col zero
+        if (o.use_std) v -= (double)a.tsum[idx[i]] * (double)a.tsum[idx[j]] / (double)a.F;
+        return v;
+    };
+    for (int i = 0; i < n; ++i) {
+        double q = -(double)a.C[p + a.ldc * idx[i]] / yn;
+        if (o.use_std) q += (double)a.tsum[idx[i]] * (double)a.psum[p] / yn / (double)a.F;
+        q += o.l1;
+        b[i] = -q;
+    }
+    int iters = 0;
+    const int st = nqp_solve(n, Qij, b, x, w, ws, &iters);
+    a.status[p] = st;
+    if (st) {
+        atomicAdd(a.nfail, 1);
+        return;
+    }
+    for (int i = 0; i < n; ++i) a.out[idx[i] + (int64_t)a.R * p] = (float)(x[i] * yn);
+}
+
 // One thread per pixel: collect the covering components and solve the NQP in
-// FP64.  status[p]: 0 ok, 1 too many components, 2 iteration cap (NQP.m:116-119).
+// FP64 with the working arrays in registers / local memory.  A pixel covered by
+// more than kNqpMax components is put on the large-problem list (status 3
+// until k_pixel_nqp_large solves it); nlarge[0] counts them, nlarge[1] keeps
+// the largest n.  status[p]: 0 ok, 2 iteration cap (NQP.m:116-119).
 __global__ void __launch_bounds__(128)
-k_pixel_nqp(const uint8_t* __restrict__ tmpl, int Rt, int64_t P, const float* __restrict__ G, int R,
-            const float* __restrict__ C, int64_t ldc, const float* __restrict__ pnrm, const float* __restrict__ psum,
-            const float* __restrict__ tsum, int F, SpatialOpts o, float* __restrict__ out, int* __restrict__ status,
-            int* __restrict__ nfail)
+k_pixel_nqp(PixelArgs a, int* __restrict__ large, int* __restrict__ nlarge)
 {
     const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (p >= P) return;
+    if (p >= a.P) return;
     int idx[kNqpMax];
     int n = 0;
-    bool over = false;
-    for (int r = 0; r < Rt; ++r) {
-        if (tmpl[r + (int64_t)Rt * p]) {
-            if (n < kNqpMax) idx[n++] = r;
-            else over = true;
+    for (int r = 0; r < a.Rt; ++r) {
+        if (a.tmpl[r + (int64_t)a.Rt * p]) {
+            if (n < kNqpMax) idx[n] = r;
+            ++n;
         }
     }
     if (n == 0) {
         // outside every template: background row, if any (update_spatial_component.m:128-131)
-        if (o.bg_sub) out[(R - 1) + (int64_t)R * p] = C[p + ldc * (R - 1)];
-        status[p] = 0;
+        if (a.o.bg_sub) a.out[(a.R - 1) + (int64_t)a.R * p] = a.C[p + a.ldc * (a.R - 1)];
+        a.status[p] = 0;
         return;
     }
-    if (o.bg_sub) {
-        if (n < kNqpMax) idx[n++] = R - 1;
-        else over = true;
+    if (a.o.bg_sub) {
+        if (n < kNqpMax) idx[n] = a.R - 1;
+        ++n;
     }
-    if (over) {
-        status[p] = 1;
-        atomicAdd(nfail, 1);
+    if (n > kNqpMax) {
+        const int pos = atomicAdd(&nlarge[0], 1);
+        large[pos] = (int)p;
+        atomicMax(&nlarge[1], n);
+        a.status[p] = 3;
         return;
     }
-    const double yn = (double)pnrm[p];
-    if (!(yn > 0.0)) {
-        for (int i = 0; i < n; ++i) out[idx[i] + (int64_t)R * p] = 0.f;
-        status[p] = 0;
-        return;
-    }
-    // Q(i,j) and b = -q (NQP works with b = -q, NQP.m:145)
-    auto Qij = [&](int i, int j) -> double {
-        double v = (double)G[idx[i] + (int64_t)R * idx[j]];
-        if (i == j) v += o.l2;
-        else if (!(o.bg_sub && (i == n - 1 || j == n - 1))) v += o.lo;  // hilf = ones - eye, bg row/col zero
-        if (o.use_std) v -= (double)tsum[idx[i]] * (double)tsum[idx[j]] / (double)F;
-        return v;
-    };
+    double z[kNqpMax], wsc[kNqpMax], t[kNqpMax], L[kNqpMax * (kNqpMax + 1) / 2];
+    int pn[kNqpMax];
+    uint8_t Pset[kNqpMax];
+    const NqpWs ws{z, wsc, t, L, pn, Pset};
     double b[kNqpMax], x[kNqpMax], w[kNqpMax];
-    for (int i = 0; i < n; ++i) {
-        double q = -(double)C[p + ldc * idx[i]] / yn;
-        if (o.use_std) q += (double)tsum[idx[i]] * (double)psum[p] / yn / (double)F;
-        q += o.l1;
-        b[i] = -q;  // NQP works with b = -q (NQP.m:145)
-    }
-    int iters = 0;
-    const int st = nqp_solve(n, Qij, b, x, w, &iters);
-    status[p] = st;
-    if (st) {
-        atomicAdd(nfail, 1);
-        return;
-    }
-    for (int i = 0; i < n; ++i) out[idx[i] + (int64_t)R * p] = (float)(x[i] * yn);
+    pixel_solve(a, p, idx, n, b, x, w, ws);
+}
+
+// Pixels of the large-problem list large[off .. off+cnt): one thread each,
+// working arrays in a slice of `scratch` sized for nm components.
+__global__ void __launch_bounds__(128)
+k_pixel_nqp_large(PixelArgs a, const int* __restrict__ large, int off, int cnt, int nm, double* __restrict__ scratch)
+{
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= cnt) return;
+    const int64_t p = large[off + e];
+    double *b, *x, *w;
+    int* idx;
+    const NqpWs ws = nqp_ws_at(scratch + (int64_t)e * nqp_scratch_doubles(nm), nm, &b, &x, &w, &idx);
+    int n = 0;
+    for (int r = 0; r < a.Rt; ++r)
+        if (a.tmpl[r + (int64_t)a.Rt * p] && n < nm) idx[n++] = r;
+    if (a.o.bg_sub && n < nm) idx[n++] = a.R - 1;
+    pixel_solve(a, p, idx, n, b, x, w, ws);
 }
 
 // One thread per problem k: Q (n x n, column-major, FP64) at Q + n*n*k, the
 // linear term at q + n*k; x and w (optional) n x B; NQP's [x, w, info]
-// (NQP.m:42-178) for independent problems of one size.
+// (NQP.m:42-178) for independent problems of one size.  n <= kNqpMax keeps
+// the working arrays in local memory (scratch == nullptr); larger n uses a
+// slice of `scratch` per problem, for problems k0 .. k0+cnt.
 __global__ void __launch_bounds__(128) k_nqp_batched(const double* __restrict__ Q, const double* __restrict__ q,
-                                                     int n, int64_t B, double* __restrict__ x, double* __restrict__ w,
-                                                     int32_t* __restrict__ iters, int32_t* __restrict__ status,
-                                                     int* __restrict__ nfail)
+                                                     int n, int64_t k0, int64_t cnt, double* __restrict__ x,
+                                                     double* __restrict__ w, int32_t* __restrict__ iters,
+                                                     int32_t* __restrict__ status, int* __restrict__ nfail,
+                                                     double* __restrict__ scratch)
 {
-    const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (k >= B) return;
+    const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= cnt) return;
+    const int64_t k = k0 + e;
     const double* Qk = Q + (int64_t)n * n * k;
     auto Qij = [&](int i, int j) -> double { return Qk[i + (int64_t)n * j]; };
-    double bb[kNqpMax], xx[kNqpMax], ww[kNqpMax];
+    double zl[kNqpMax], wscl[kNqpMax], tl[kNqpMax], Ll[kNqpMax * (kNqpMax + 1) / 2];
+    int pnl[kNqpMax];
+    uint8_t Psl[kNqpMax];
+    double bl[kNqpMax], xl[kNqpMax], wl[kNqpMax];
+    double *bb = bl, *xx = xl, *ww = wl;
+    NqpWs ws{zl, wscl, tl, Ll, pnl, Psl};
+    if (scratch) {
+        int* idx;
+        ws = nqp_ws_at(scratch + e * nqp_scratch_doubles(n), n, &bb, &xx, &ww, &idx);
+    }
     for (int i = 0; i < n; ++i) bb[i] = -q[i + (int64_t)n * k];  // NQP works with b = -q (NQP.m:145)
     int it = 0;
-    const int st = nqp_solve(n, Qij, bb, xx, ww, &it);
+    const int st = nqp_solve(n, Qij, bb, xx, ww, ws, &it);
     for (int i = 0; i < n; ++i) {
         x[i + (int64_t)n * k] = xx[i];
         if (w) w[i + (int64_t)n * k] = ww[i];
@@ -355,6 +455,62 @@ __global__ void __launch_bounds__(128) k_nqp_batched(const double* __restrict__ 
     if (iters) iters[k] = it;
     if (status) status[k] = st;
     if (st) atomicAdd(nfail, 1);
+}
+
+// reg_nnls.m:40-66: Q = A'A [- t t'/m] + l2 I + lo hilf, q = -A'd [+ t sum(d)/m] + l1,
+// t = column sums of A (use_std); one CTA per entry of Q (and per entry of q,
+// row n of the grid), FP64 sums over the m rows.  Q n x n and q n, column-major.
+__global__ void __launch_bounds__(256) k_reg_form(const double* __restrict__ A, int64_t m, int n,
+                                                  const double* __restrict__ d, double l1, double l2, double lo,
+                                                  int use_std, int bg_sub, const double* __restrict__ hilf,
+                                                  double* __restrict__ Q, double* __restrict__ q)
+{
+    __shared__ double red[3][8];
+    const int i = blockIdx.x, j = blockIdx.y;  // j == n: the linear term of row i
+    const double* ai = A + (int64_t)i * m;
+    const double* bj = (j < n) ? A + (int64_t)j * m : d;
+    double s = 0.0, si = 0.0, sj = 0.0;
+    for (int64_t r = threadIdx.x; r < m; r += blockDim.x) {
+        const double a = ai[r], b = bj[r];
+        s = fma(a, b, s);
+        si += a;
+        sj += b;
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        s += __shfl_xor_sync(0xffffffffu, s, off);
+        si += __shfl_xor_sync(0xffffffffu, si, off);
+        sj += __shfl_xor_sync(0xffffffffu, sj, off);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        red[0][threadIdx.x >> 5] = s;
+        red[1][threadIdx.x >> 5] = si;
+        red[2][threadIdx.x >> 5] = sj;
+    }
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    s = si = sj = 0.0;
+    for (int w = 0; w < 8; ++w) {
+        s += red[0][w];
+        si += red[1][w];
+        sj += red[2][w];
+    }
+    if (use_std) s -= si * sj / (double)m;
+    if (j < n) {
+        if (i == j) s += l2;
+        const double h = hilf ? hilf[i + (int64_t)n * j]
+                              : ((i == j || (bg_sub && (i == n - 1 || j == n - 1))) ? 0.0 : 1.0);
+        s += lo * h;
+        Q[i + (int64_t)n * j] = s;
+    } else {
+        q[i] = -s + l1;
+    }
+}
+
+// problems of nm components whose scratch fits in the budget (at least one)
+inline int64_t nqp_chunk(int64_t total, int64_t nm)
+{
+    const int64_t budget = (int64_t)1 << 30;  // bytes of scratch per launch
+    return std::max<int64_t>(1, std::min<int64_t>(total, budget / (nqp_scratch_doubles(nm) * 8)));
 }
 
 }  // namespace sid
@@ -390,11 +546,12 @@ extern "C" int sid_spatial_update(sid_ctx* c, const float* T, const void* Y, int
     SID_CHECK_LAUNCH();
     // G = T T' (contraction over frames)
     SID_TRY(contract(c, Tt, Tt, false, R, R, F, F, F, G, R, 1.f, 0.f, SID_PREC_FP32, st));
-    // C = Y T' (P x R)
-    dim3 grid((unsigned)cdiv(P, 128), (unsigned)cdiv(R, 64));
-    k_sgemm_nt<<<grid, 256, 0, st>>>(static_cast<const float*>(Y), T, nullptr, (int)P, (int)R, (int)F, P, R, Cm, P,
-                                     ydtype == SID_DTYPE_F16 ? 1 : 0);
-    SID_CHECK_LAUNCH();
+    // C = Y T' (P x R) on the tensor cores: the pixel-major movie brought once into
+    // the GEMM's K-blocked layout (an FP16 movie as it is, an FP32 one as FP16
+    // hi/lo), T' as FP16 hi/lo with a power-of-two scale; FP32 accumulation
+    PixOperand yop;
+    SID_TRY(pix_operand(c, 0, Y, ydtype == SID_DTYPE_F16, P, F, SID_PREC_SPLIT, &yop, st));
+    SID_TRY(gemm_pix(c, yop, P, F, Tt, R, F, Cm, SID_PREC_SPLIT, st));
     k_pixel_stats<<<1024, 256, 0, st>>>(Y, ydtype == SID_DTYPE_F16 ? 1 : 0, P, F, pn, ps);
     SID_CHECK_LAUNCH();
     k_row_sums<<<cdiv(R, 256), 256, 0, st>>>(T, (int)R, (int)F, ts);
@@ -402,16 +559,35 @@ extern "C" int sid_spatial_update(sid_ctx* c, const float* T, const void* Y, int
     SID_CUDA_TRY(cudaMemsetAsync(forward_model, 0, (size_t)(R * P) * 4, st));
     SID_CUDA_TRY(cudaMemsetAsync(nfail, 0, sizeof(int), st));
     SpatialOpts o{lamb_L1, lamb_L2, lamb_orth_L1, use_std ? 1 : 0, bg_sub ? 1 : 0};
-    k_pixel_nqp<<<(unsigned)cdiv(P, 128), 128, 0, st>>>(tmpl, (int)Rt, P, G, (int)R, Cm, P, pn, ps, ts, (int)F, o,
-                                                        forward_model, stat, nfail);
+    PixelArgs pa{tmpl, (int)Rt, P, G, (int)R, Cm, P, pn, ps, ts, (int)F, o, forward_model, stat, nfail};
+    SID_TRY(nn[5].alloc((size_t)P * 4 + 16));  // large-problem list, then its count and largest n
+    int* large = nn[5].as<int>();
+    int* nlarge = reinterpret_cast<int*>(nn[5].as<uint8_t>() + (size_t)P * 4);
+    SID_CUDA_TRY(cudaMemsetAsync(nlarge, 0, 2 * sizeof(int), st));
+    k_pixel_nqp<<<(unsigned)cdiv(P, 128), 128, 0, st>>>(pa, large, nlarge);
     SID_CHECK_LAUNCH();
+    int hl[2] = {0, 0};
+    SID_CUDA_TRY(cudaMemcpyAsync(hl, nlarge, sizeof(hl), cudaMemcpyDeviceToHost, st));
+    SID_CUDA_TRY(cudaStreamSynchronize(st));
+    if (hl[0] > 0) {
+        // pixels covered by more than kNqpMax components: working arrays in global scratch
+        const int nm = hl[1];
+        const int64_t chunk = nqp_chunk(hl[0], nm);
+        SID_TRY(nn[6].alloc((size_t)(chunk * nqp_scratch_doubles(nm)) * 8));
+        for (int64_t off = 0; off < hl[0]; off += chunk) {
+            const int cnt = (int)std::min<int64_t>(chunk, hl[0] - off);
+            k_pixel_nqp_large<<<(unsigned)cdiv(cnt, 128), 128, 0, st>>>(pa, large, (int)off, cnt, nm,
+                                                                          nn[6].as<double>());
+            SID_CHECK_LAUNCH();
+        }
+    }
     int hf = 0;
     SID_CUDA_TRY(cudaMemcpyAsync(&hf, nfail, sizeof(int), cudaMemcpyDeviceToHost, st));
     SID_TRY(ctx_sync(c, st));
     if (hf) {
-        set_error("sid_spatial_update: %d pixel problems failed (more than %d covering components, or the "
-                  "NQP iteration cap of NQP.m:116-119); see the status array",
-                  hf, kNqpMax);
+        set_error("sid_spatial_update: %d pixel problems hit the NQP iteration cap of NQP.m:116-119; see the "
+                  "status array",
+                  hf);
         return SID_ENOCONV;
     }
     return SID_OK;
@@ -421,14 +597,25 @@ extern "C" int sid_nqp_batched(sid_ctx* c, const double* Q, const double* q, int
                                int32_t* iters, int32_t* status, void* stream)
 {
     SID_REQUIRE(c && Q && q && x, "sid_nqp_batched: NULL argument");
-    SID_REQUIRE(n >= 1 && n <= kNqpMax, "sid_nqp_batched: n = %d outside [1, %d]", n, kNqpMax);
+    SID_REQUIRE(n >= 1 && n <= kNqpLargeMax, "sid_nqp_batched: n = %d outside [1, %d]", n, kNqpLargeMax);
     SID_REQUIRE(B >= 1, "sid_nqp_batched: no problems");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     SID_TRY(c->scal.alloc(64));
     int* nfail = c->scal.as<int>();
     SID_CUDA_TRY(cudaMemsetAsync(nfail, 0, sizeof(int), st));
-    k_nqp_batched<<<(unsigned)cdiv(B, 128), 128, 0, st>>>(Q, q, n, B, x, w, iters, status, nfail);
-    SID_CHECK_LAUNCH();
+    if (n <= kNqpMax) {
+        k_nqp_batched<<<(unsigned)cdiv(B, 128), 128, 0, st>>>(Q, q, n, 0, B, x, w, iters, status, nfail, nullptr);
+        SID_CHECK_LAUNCH();
+    } else {
+        const int64_t chunk = nqp_chunk(B, n);
+        SID_TRY(c->nn[13].alloc((size_t)(chunk * nqp_scratch_doubles(n)) * 8));
+        for (int64_t k0 = 0; k0 < B; k0 += chunk) {
+            const int64_t cnt = std::min<int64_t>(chunk, B - k0);
+            k_nqp_batched<<<(unsigned)cdiv(cnt, 128), 128, 0, st>>>(Q, q, n, k0, cnt, x, w, iters, status, nfail,
+                                                                     c->nn[13].as<double>());
+            SID_CHECK_LAUNCH();
+        }
+    }
     int hf = 0;
     SID_CUDA_TRY(cudaMemcpyAsync(&hf, nfail, sizeof(int), cudaMemcpyDeviceToHost, st));
     SID_TRY(ctx_sync(c, st));
@@ -438,4 +625,20 @@ extern "C" int sid_nqp_batched(sid_ctx* c, const double* Q, const double* q, int
         return SID_ENOCONV;
     }
     return SID_OK;
+}
+
+extern "C" int sid_reg_nnls(sid_ctx* c, const double* A, int64_t m, int n, const double* d, double lamb_L1,
+                            double lamb_L2, double lamb_orth_L1, int use_std, int bg_sub, const double* hilf,
+                            double* x, void* stream)
+{
+    SID_REQUIRE(c && A && d && x, "sid_reg_nnls: NULL argument");
+    SID_REQUIRE(m >= 1 && n >= 1 && n <= kNqpLargeMax, "sid_reg_nnls: need m >= 1 and 1 <= n <= %d", kNqpLargeMax);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    SID_TRY(c->nn[14].alloc((size_t)((int64_t)n * n + n) * 8));
+    double* Q = c->nn[14].as<double>();
+    double* q = Q + (int64_t)n * n;
+    k_reg_form<<<dim3((unsigned)n, (unsigned)n + 1), 256, 0, st>>>(A, m, n, d, lamb_L1, lamb_L2, lamb_orth_L1,
+                                                                  use_std ? 1 : 0, bg_sub ? 1 : 0, hilf, Q, q);
+    SID_CHECK_LAUNCH();
+    return sid_nqp_batched(c, Q, q, n, 1, x, nullptr, nullptr, nullptr, stream);
 }

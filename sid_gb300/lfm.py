@@ -199,6 +199,27 @@ class Projector:
                   int(maxIter), float(lam), _stream_ptr())
         return X
 
+    def isra_ex(self, Htf, Xguess, maxIter, mode="basic", p=1, lam=0.0, history=False, method=None):
+        """deconvRL in every mode (deconvRL.m:1): mode 'basic' (lam a scalar)
+        or 'TV' (lam one weight per axis, p = 1 or 2).  history=True also
+        returns Xguess_history (maxIter x X x Y x Z, deconvRL.m:10,90-92)."""
+        Htf = to_device(Htf)
+        X = to_device(Xguess).clone()
+        lam3 = np.zeros(3, dtype=np.float32)
+        lv = np.asarray(lam, dtype=np.float64).ravel()
+        if mode == "TV":
+            lam3[:] = np.broadcast_to(lv, (3,)) if lv.size in (1, 3) else lv[:3]
+        else:
+            lam3[0] = lv[0] if lv.size else 0.0
+        H = None
+        if history:
+            H = torch.zeros((Htf.shape[2], Htf.shape[1], Htf.shape[0], int(maxIter)), dtype=torch.float32,
+                            device=Htf.device).permute(3, 2, 1, 0)
+        _lib.call("sid_deconv_isra_ex", self._plan, self._method(method), Htf.data_ptr(), X.data_ptr(),
+                  int(maxIter), 1 if mode == "TV" else 0, int(p), lam3.ctypes.data,
+                  H.data_ptr() if H is not None else None, _stream_ptr())
+        return (X, H) if history else X
+
     def rl_poisson(self, y, Xguess, maxIter, method=None) -> torch.Tensor:
         """Poisson-likelihood Richardson-Lucy from the sensor image y:
         X <- X .* A'(y ./ AX) ./ A'1 (the reference's deconvRL is the ISRA form)."""
@@ -272,10 +293,13 @@ class Projector:
                   _stream_ptr())
         return (X, lam.value) if return_lambda else X
 
-    def ls_deconv(self, df, max_iter=8, lamb_L1=0.0, lamb_L2=0.0, method=None) -> torch.Tensor:
+    def ls_deconv(self, df, max_iter=8, lamb_L1=0.0, lamb_L2=0.0, method=None, lamb_TV_L2=(0.0, 0.0, 0.0),
+                  lamb_TV_L1=0.0) -> torch.Tensor:
         X = to_device(df).clone()
-        _lib.call("sid_deconv_ls", self._plan, self._method(method), X.data_ptr(), int(max_iter),
-                  float(lamb_L1), float(lamb_L2), _stream_ptr())
+        tv = np.zeros(3, dtype=np.float32)
+        tv[:] = np.asarray(lamb_TV_L2, dtype=np.float32).ravel()[:3]
+        _lib.call("sid_deconv_ls_ex", self._plan, self._method(method), X.data_ptr(), int(max_iter),
+                  float(lamb_L1), float(lamb_L2), tv.ctypes.data, float(lamb_TV_L1), _stream_ptr())
         return X
 
 
@@ -333,33 +357,46 @@ def _native_pair(forwardFUN, backwardFUN):
     return None
 
 
-def deconvRL(forwardFUN, backwardFUN, Htf, maxIter, Xguess, opts=None):
-    """Xguess = deconvRL(forwardFUN, backwardFUN, Htf, maxIter, Xguess, opts)
-    (deconvRL.m:1): ISRA, mode 'basic' with p = 1.  The projector handles must
-    be a Projector's ``forward`` / ``adjoint``."""
-    opts = dict(opts or {"lambda": 0, "p": 1, "mode": "basic"})
-    if opts.get("mode", "basic") != "basic":
-        raise NotImplementedError("deconvRL: only mode 'basic' runs natively")
-    lam = float(np.asarray(opts.get("lambda", 0.0)).ravel()[0])
-    if lam != 0 and opts.get("p", 1) != 1:
+def deconvRL(forwardFUN, backwardFUN, Htf, maxIter, Xguess, opts=None, nargout=1):
+    """[Xguess, Xguess_history] = deconvRL(forwardFUN, backwardFUN, Htf, maxIter,
+    Xguess, opts) (deconvRL.m:1): ISRA in mode 'basic' (opts.lambda a scalar,
+    p = 1) or 'TV' (opts.lambda one weight per axis, p = 1 or 2).  The
+    projector handles must be a Projector's ``forward`` / ``adjoint``.
+    nargout=2 also returns Xguess_history (maxIter x size(Xguess))."""
+    opts = dict(opts if opts is not None else {"lambda": 0, "p": 1, "mode": "basic"})
+    mode = opts.get("mode", "basic")
+    if mode not in ("basic", "TV"):
+        raise ValueError(f"deconvRL: unknown mode {mode!r}")
+    lam = np.asarray(opts.get("lambda", 0.0), dtype=np.float64).ravel()
+    p = int(opts.get("p", 1))
+    if mode == "basic" and np.any(lam != 0) and p != 1:
         raise ValueError("deconvRL: mode 'basic' with p != 1 is undefined in the reference")
+    if mode == "TV" and np.any(lam != 0) and lam.size != 3:
+        raise ValueError("deconvRL: mode 'TV' needs opts.lambda with one weight per axis (1 x 3)")
     proj = _native_pair(forwardFUN, backwardFUN)
     if proj is None:
         raise TypeError("deconvRL: forwardFUN/backwardFUN must be a Projector's forward/adjoint")
-    return proj.isra(Htf, Xguess, maxIter, lam)
+    if mode == "basic" and nargout < 2:
+        return proj.isra(Htf, Xguess, maxIter, float(lam[0]) if lam.size else 0.0)
+    return proj.isra_ex(Htf, Xguess, maxIter, mode=mode, p=p, lam=lam if lam.size else 0.0, history=nargout > 1)
 
 
 def LS_deconv(forwardFUN, backwardFUN, df, opts=None):
-    """Xguess = LS_deconv(forwardFUN, backwardFUN, df, opts) (LS_deconv.m:1)."""
+    """Xguess = LS_deconv(forwardFUN, backwardFUN, df, opts) (LS_deconv.m:1),
+    with the TV Laplacian term lamb_TV_L2 (1 x 3) and lamb_TV_L1's role in the
+    step-length test."""
     opts = dict(opts or {})
-    tv = np.asarray(opts.get("lamb_TV_L2", 0.0))
-    if np.any(tv != 0) or opts.get("lamb_TV_L1", 0):
-        raise NotImplementedError("LS_deconv: TV regularisers do not run natively")
+    tv = np.asarray(opts.get("lamb_TV_L2", [0.0, 0.0, 0.0]), dtype=np.float64).ravel()
+    if tv.size != 3:
+        if np.any(tv != 0):
+            # LS_deconv.m:50-55 broadcasts a scalar into opts.p, then reads lamb_TV_L2(3)
+            raise ValueError("LS_deconv: lamb_TV_L2 must have 3 entries")
+        tv = np.zeros(3)
     proj = _native_pair(forwardFUN, backwardFUN)
     if proj is None:
         raise TypeError("LS_deconv: forwardFUN/backwardFUN must be a Projector's forward/adjoint")
     return proj.ls_deconv(df, int(opts.get("max_iter", 8)), float(opts.get("lamb_L1", 0.0)),
-                          float(opts.get("lamb_L2", 0.0)))
+                          float(opts.get("lamb_L2", 0.0)), lamb_TV_L2=tv, lamb_TV_L1=float(opts.get("lamb_TV_L1", 0.0)))
 
 
 def _colon(a, b, step=1.0):

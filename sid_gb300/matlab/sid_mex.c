@@ -27,6 +27,12 @@
  *   T        = sid_mex('pinv_apply', h, Y, baseline)      baseline may be []
  *   sid_mex('pinv_destroy', h)
  *   [X, lam] = sid_mex('reconstruct', plan, img, microlenses, opts, method)
+ *   [X, hist] = sid_mex('isra_ex', plan, Htf, Xguess, maxIter, mode, p, lambda, method)   mode 0 basic, 1 TV
+ *   X        = sid_mex('ls_deconv_ex', plan, df, max_iter, lamb_L1, lamb_L2, lamb_TV_L2, lamb_TV_L1, method)
+ *   F        = sid_mex('library', plan, recon, centers, neur_id, neur_rad, axial)   recon: cell of volumes
+ *   Fm       = sid_mex('spatial_update', T, Y, template, opts)     template: logical (R - bg_sub) x P
+ *   [xx, Q, df, h] = sid_mex('fast_nnls_ex', A, Y, opts, Q, df, h)  every fast_nnls input and output
+ *   x        = sid_mex('reg_nnls', A, d, opts)                      A m x n, d m double gpuArrays
  *   sid_mex('destroy', plan)
  * Matrix arguments of the NNLS / NMF / extraction commands are single
  * gpuArrays (the movie Y may be half); results are gpuArrays.
@@ -35,6 +41,7 @@
  * MATLAB error with identifier 'sid:<command>' and sid_last_error() as text.
  */
 #include <stdint.h>
+#include <stdio.h>
 #include <string.h>
 
 #include "gpu/mxGPUArray.h"
@@ -576,6 +583,224 @@ void mexFunction(int nlhs, mxArray* plhs[], int nrhs, const mxArray* prhs[])
         plhs[0] = mxGPUCreateMxArrayOnGPU(X);
         if (nlhs > 1) plhs[1] = mxCreateDoubleScalar(lam);
         mxGPUDestroyGPUArray(X);
+        return;
+    }
+    if (!strcmp(cmd, "isra_ex")) {
+        /* [X, hist] = sid_mex('isra_ex', plan, Htf, Xguess, maxIter, mode, p, lambda, method): Htf, Xguess single
+         * gpuArrays; lambda a scalar ('basic') or 1 x 3 ('TV') */
+        sid_plan* p = plan_arg(prhs[1]);
+        const mxGPUArray* htf = gpu_arg(prhs[2], 0, cmd);
+        const mxGPUArray* x0 = gpu_arg(prhs[3], 0, cmd);
+        const int maxIter = (int)mxGetScalar(prhs[4]);
+        const int mode = (int)mxGetScalar(prhs[5]);
+        const int pn = (int)mxGetScalar(prhs[6]);
+        float lam3[3] = {0.f, 0.f, 0.f};
+        const mwSize nl = mxGetNumberOfElements(prhs[7]);
+        for (mwSize i = 0; i < nl && i < 3; ++i) lam3[i] = (float)mxGetPr(prhs[7])[i];
+        mxGPUArray* X = gpu_copy(x0);
+        mxGPUArray* hist = NULL;
+        if (nlhs > 1) {
+            int64_t info[14];
+            sid_plan_info(p, info);
+            mwSize dh[4] = {(mwSize)maxIter, (mwSize)info[3], (mwSize)info[4], (mwSize)info[2]};
+            hist = mxGPUCreateGPUArray(4, dh, mxSINGLE_CLASS, mxREAL, MX_GPU_INITIALIZE_VALUES);
+        }
+        int rc = sid_deconv_isra_ex(p, method_arg(nrhs, prhs, 8), (const float*)mxGPUGetDataReadOnly(htf),
+                                    (float*)mxGPUGetData(X), maxIter, mode, pn, lam3,
+                                    hist ? (float*)mxGPUGetData(hist) : NULL, NULL);
+        if (rc == SID_OK) rc = sid_plan_sync(p, NULL);
+        mxGPUDestroyGPUArray(htf);
+        mxGPUDestroyGPUArray(x0);
+        if (rc != SID_OK) {
+            mxGPUDestroyGPUArray(X);
+            if (hist) mxGPUDestroyGPUArray(hist);
+            check(rc, cmd);
+        }
+        plhs[0] = mxGPUCreateMxArrayOnGPU(X);
+        mxGPUDestroyGPUArray(X);
+        if (hist) {
+            plhs[1] = mxGPUCreateMxArrayOnGPU(hist);
+            mxGPUDestroyGPUArray(hist);
+        }
+        return;
+    }
+    if (!strcmp(cmd, "ls_deconv_ex")) {
+        /* X = sid_mex('ls_deconv_ex', plan, df, max_iter, lamb_L1, lamb_L2, lamb_TV_L2, lamb_TV_L1, method) */
+        sid_plan* p = plan_arg(prhs[1]);
+        const mxGPUArray* df = gpu_arg(prhs[2], 0, cmd);
+        float tv[3] = {0.f, 0.f, 0.f};
+        const mwSize nt = mxGetNumberOfElements(prhs[6]);
+        for (mwSize i = 0; i < nt && i < 3; ++i) tv[i] = (float)mxGetPr(prhs[6])[i];
+        mxGPUArray* X = gpu_copy(df);
+        int rc = sid_deconv_ls_ex(p, method_arg(nrhs, prhs, 8), (float*)mxGPUGetData(X), (int)mxGetScalar(prhs[3]),
+                                  (float)mxGetScalar(prhs[4]), (float)mxGetScalar(prhs[5]), tv,
+                                  (float)mxGetScalar(prhs[7]), NULL);
+        if (rc == SID_OK) rc = sid_plan_sync(p, NULL);
+        mxGPUDestroyGPUArray(df);
+        if (rc != SID_OK) mxGPUDestroyGPUArray(X);
+        check(rc, cmd);
+        plhs[0] = mxGPUCreateMxArrayOnGPU(X);
+        mxGPUDestroyGPUArray(X);
+        return;
+    }
+    if (!strcmp(cmd, "library")) {
+        /* F = sid_mex('library', plan, recon, centers, neur_id, neur_rad, axial): recon a cell of X x Y x Z
+         * single gpuArrays, centers n x 3 double, neur_id n x numel(recon) logical; F n x P single gpuArray */
+        sid_plan* p = plan_arg(prhs[1]);
+        const mxArray* rc_cell = prhs[2];
+        const mwSize nc = mxGetNumberOfElements(rc_cell);
+        if (nc < 1 || nc > 4096) mexErrMsgIdAndTxt("sid:library", "recon must be a cell of 1..4096 volumes");
+        const mxGPUArray* vols[4096];
+        const float* ptrs[4096];
+        for (mwSize k = 0; k < nc; ++k) {
+            vols[k] = gpu_arg(mxGetCell(rc_cell, k), 0, cmd);
+            ptrs[k] = (const float*)mxGPUGetDataReadOnly(vols[k]);
+        }
+        const mwSize n = mxGetDimensions(prhs[3])[0];
+        mxArray* ids = mxCreateNumericMatrix(n, nc, mxUINT8_CLASS, mxREAL);
+        const mxLogical* nid = mxGetLogicals(prhs[4]);
+        uint8_t* idp = (uint8_t*)mxGetData(ids);
+        for (mwSize i = 0; i < n * nc; ++i) idp[i] = nid[i] ? 1 : 0;
+        int64_t info[14];
+        sid_plan_info(p, info);
+        mwSize df[2] = {n, (mwSize)(info[3] * info[4])};
+        mxGPUArray* F = mxGPUCreateGPUArray(2, df, mxSINGLE_CLASS, mxREAL, MX_GPU_DO_NOT_INITIALIZE);
+        int rc = sid_library(p, ptrs, (int64_t)nc, mxGetPr(prhs[3]), idp, (int64_t)n, (int64_t)mxGetScalar(prhs[5]),
+                             mxGetScalar(prhs[6]), (float*)mxGPUGetData(F), 0, NULL);
+        for (mwSize k = 0; k < nc; ++k) mxGPUDestroyGPUArray(vols[k]);
+        mxDestroyArray(ids);
+        if (rc != SID_OK) mxGPUDestroyGPUArray(F);
+        check(rc, cmd);
+        plhs[0] = mxGPUCreateMxArrayOnGPU(F);
+        mxGPUDestroyGPUArray(F);
+        return;
+    }
+    if (!strcmp(cmd, "spatial_update")) {
+        /* Fm = sid_mex('spatial_update', T, Y, template, opts): T R x F single gpuArray, Y P x F single or half
+         * gpuArray, template (R - bg_sub) x P logical (host); Fm R x P single gpuArray */
+        const mxGPUArray* T = gpu_arg(prhs[1], 0, cmd);
+        const mxGPUArray* Y = gpu_arg(prhs[2], 1, cmd);
+        const mwSize* dt = mxGPUGetDimensions(T);
+        const mwSize* dy = mxGPUGetDimensions(Y);
+        const mxArray* o = nrhs > 4 ? prhs[4] : NULL;
+        const int bg = (int)field_or(o, "bg_sub", 1.0);
+        const mwSize R = dt[0], F = dt[1], P = dy[0];
+        if (mxGetNumberOfElements(prhs[3]) != (R - (mwSize)bg) * P)
+            mexErrMsgIdAndTxt("sid:spatial_update", "template must be (R - bg_sub) x P");
+        mxArray* tm = mxCreateNumericMatrix(R - (mwSize)bg, P, mxUINT8_CLASS, mxREAL);
+        const mxLogical* tl = mxGetLogicals(prhs[3]);
+        uint8_t* tp = (uint8_t*)mxGetData(tm);
+        for (mwSize i = 0; i < (R - (mwSize)bg) * P; ++i) tp[i] = tl[i] ? 1 : 0;
+        const mxGPUArray* tg = mxGPUCreateFromMxArray(tm);
+        mwSize dfm[2] = {R, P};
+        mxGPUArray* Fm = mxGPUCreateGPUArray(2, dfm, mxSINGLE_CLASS, mxREAL, MX_GPU_DO_NOT_INITIALIZE);
+        int rc = sid_spatial_update(ctx(cmd), (const float*)mxGPUGetDataReadOnly(T), mxGPUGetDataReadOnly(Y), ydtype(Y),
+                                    (const uint8_t*)mxGPUGetDataReadOnly(tg), (int64_t)R, (int64_t)F, (int64_t)P,
+                                    field_or(o, "lamb_L1", 0.0), field_or(o, "lamb_L2", 0.0),
+                                    field_or(o, "lamb_orth_L1", 0.0), (int)field_or(o, "use_std", 0.0), bg,
+                                    (float*)mxGPUGetData(Fm), NULL, NULL);
+        mxGPUDestroyGPUArray(T);
+        mxGPUDestroyGPUArray(Y);
+        mxGPUDestroyGPUArray(tg);
+        mxDestroyArray(tm);
+        if (rc != SID_OK) mxGPUDestroyGPUArray(Fm);
+        check(rc, cmd);
+        plhs[0] = mxGPUCreateMxArrayOnGPU(Fm);
+        mxGPUDestroyGPUArray(Fm);
+        return;
+    }
+    if (!strcmp(cmd, "fast_nnls_ex")) {
+        /* [xx, Q, df, h] = sid_mex('fast_nnls_ex', A, Y, opts, Q, df, h): A P x K and Y P x F single (Y may be
+         * half) gpuArrays, or [] when Q, h and df are all given; opts.warm_start a K x F single gpuArray or 1;
+         * opts.total; Q K x K, df K x F, h K single gpuArrays or [] */
+        const int hasA = !mxIsEmpty(prhs[1]);
+        const mxGPUArray* A = hasA ? gpu_arg(prhs[1], 0, cmd) : NULL;
+        const mxGPUArray* Y = hasA ? gpu_arg(prhs[2], 1, cmd) : NULL;
+        const mxArray* o = nrhs > 3 ? prhs[3] : NULL;
+        const mxGPUArray* Qi = (nrhs > 4 && !mxIsEmpty(prhs[4])) ? gpu_arg(prhs[4], 0, cmd) : NULL;
+        const mxGPUArray* dfi = (nrhs > 5 && !mxIsEmpty(prhs[5])) ? gpu_arg(prhs[5], 0, cmd) : NULL;
+        const mxGPUArray* hi = (nrhs > 6 && !mxIsEmpty(prhs[6])) ? gpu_arg(prhs[6], 0, cmd) : NULL;
+        int64_t P = 0, K = 0, F = 0;
+        if (A) {
+            P = (int64_t)mxGPUGetDimensions(A)[0];
+            K = (int64_t)mxGPUGetDimensions(A)[1];
+            F = (int64_t)mxGPUGetDimensions(Y)[1];
+        } else if (Qi && dfi) {
+            K = (int64_t)mxGPUGetDimensions(Qi)[0];
+            F = (int64_t)mxGPUGetDimensions(dfi)[1];
+        } else {
+            mexErrMsgIdAndTxt("sid:fast_nnls_ex", "A and Y, or Q, df and h, are needed");
+        }
+        sid_nnls_opts opts;
+        sid_fast_nnls_defaults(&opts);
+        if (nrhs < 4) opts.tol = 1e-12; /* two-argument call, fast_nnls.m:12-15 */
+        opts.lambda = field_or(o, "lambda", opts.lambda);
+        opts.sample = (int64_t)field_or(o, "sample", (double)opts.sample);
+        opts.tol = field_or(o, "tol", opts.tol);
+        opts.tol_ = field_or(o, "tol_", opts.tol_);
+        opts.max_iter = (int64_t)field_or(o, "max_iter", (double)opts.max_iter);
+        opts.tol_p = (int)field_or(o, "tol_p", 1);
+        const int total = (int)field_or(o, "total", 0.0) != 0;
+        int warm_mode = 0;
+        const mxGPUArray* W = NULL;
+        const mxArray* wf = (o && mxIsStruct(o)) ? mxGetField(o, 0, "warm_start") : NULL;
+        if (wf && !mxIsEmpty(wf)) {
+            if (mxGetNumberOfElements(wf) == 1 && !mxIsGPUArray(wf)) warm_mode = 1;
+            else { W = gpu_arg(wf, 0, cmd); warm_mode = 2; }
+        }
+        mwSize dx[2] = {(mwSize)K, (mwSize)F}, dq[2] = {(mwSize)K, (mwSize)K}, dh[2] = {(mwSize)K, 1};
+        mwSize ddf[2] = {(mwSize)K, total ? (mwSize)F : 0};
+        mxGPUArray* X = mxGPUCreateGPUArray(2, dx, mxSINGLE_CLASS, mxREAL, MX_GPU_DO_NOT_INITIALIZE);
+        mxGPUArray* Qo = mxGPUCreateGPUArray(2, dq, mxSINGLE_CLASS, mxREAL, MX_GPU_DO_NOT_INITIALIZE);
+        mxGPUArray* dfo = mxGPUCreateGPUArray(2, ddf, mxSINGLE_CLASS, mxREAL, MX_GPU_DO_NOT_INITIALIZE);
+        mxGPUArray* ho = mxGPUCreateGPUArray(2, dh, mxSINGLE_CLASS, mxREAL, MX_GPU_DO_NOT_INITIALIZE);
+        int rc = sid_fast_nnls_ex(ctx(cmd), A ? (const float*)mxGPUGetDataReadOnly(A) : NULL,
+                                  Y ? mxGPUGetDataReadOnly(Y) : NULL, Y ? ydtype(Y) : SID_DTYPE_F32, P, K, F, &opts,
+                                  total, warm_mode, W ? (const float*)mxGPUGetDataReadOnly(W) : NULL,
+                                  Qi ? (const float*)mxGPUGetDataReadOnly(Qi) : NULL,
+                                  dfi ? (const float*)mxGPUGetDataReadOnly(dfi) : NULL,
+                                  hi ? (const float*)mxGPUGetDataReadOnly(hi) : NULL, (float*)mxGPUGetData(X),
+                                  (float*)mxGPUGetData(Qo), total ? (float*)mxGPUGetData(dfo) : NULL,
+                                  (float*)mxGPUGetData(ho), SID_PREC_SPLIT, NULL, NULL);
+        const mxGPUArray* ins[6] = {A, Y, Qi, dfi, hi, W};
+        for (int i = 0; i < 6; ++i)
+            if (ins[i]) mxGPUDestroyGPUArray(ins[i]);
+        mxGPUArray* outs[4] = {X, Qo, dfo, ho};
+        if (rc != SID_OK)
+            for (int i = 0; i < 4; ++i) mxGPUDestroyGPUArray(outs[i]);
+        check(rc, cmd);
+        for (int i = 0; i < 4; ++i) {
+            if (i < (nlhs > 0 ? nlhs : 1)) plhs[i] = mxGPUCreateMxArrayOnGPU(outs[i]);
+            mxGPUDestroyGPUArray(outs[i]);
+        }
+        return;
+    }
+    if (!strcmp(cmd, "reg_nnls")) {
+        /* x = sid_mex('reg_nnls', A, d, opts): A m x n, d m double gpuArrays; x n double gpuArray */
+        if (!mxIsGPUArray(prhs[1]) || !mxIsGPUArray(prhs[2]))
+            mexErrMsgIdAndTxt("sid:type", "%s: gpuArray arguments expected", cmd);
+        const mxGPUArray* A = mxGPUCreateFromMxArray(prhs[1]);
+        const mxGPUArray* d = mxGPUCreateFromMxArray(prhs[2]);
+        if (mxGPUGetClassID(A) != mxDOUBLE_CLASS || mxGPUGetClassID(d) != mxDOUBLE_CLASS)
+            mexErrMsgIdAndTxt("sid:type", "%s: double gpuArrays expected", cmd);
+        const mwSize* da = mxGPUGetDimensions(A);
+        const mxArray* o = nrhs > 3 ? prhs[3] : NULL;
+        const mxArray* hf = (o && mxIsStruct(o)) ? mxGetField(o, 0, "hilf") : NULL;
+        const mxGPUArray* hg = (hf && !mxIsEmpty(hf)) ? mxGPUCreateFromMxArray(hf) : NULL;
+        mwSize dxx[2] = {da[1], 1};
+        mxGPUArray* x = mxGPUCreateGPUArray(2, dxx, mxDOUBLE_CLASS, mxREAL, MX_GPU_DO_NOT_INITIALIZE);
+        int rc = sid_reg_nnls(ctx(cmd), (const double*)mxGPUGetDataReadOnly(A), (int64_t)da[0], (int)da[1],
+                              (const double*)mxGPUGetDataReadOnly(d), field_or(o, "lamb_L1", 0.0),
+                              field_or(o, "lamb_L2", 0.0), field_or(o, "lamb_orth_L1", 0.0),
+                              (int)field_or(o, "use_std", 0.0), (int)field_or(o, "bg_sub", 0.0),
+                              hg ? (const double*)mxGPUGetDataReadOnly(hg) : NULL, (double*)mxGPUGetData(x), NULL);
+        mxGPUDestroyGPUArray(A);
+        mxGPUDestroyGPUArray(d);
+        if (hg) mxGPUDestroyGPUArray(hg);
+        if (rc != SID_OK) mxGPUDestroyGPUArray(x);
+        check(rc, cmd);
+        plhs[0] = mxGPUCreateMxArrayOnGPU(x);
+        mxGPUDestroyGPUArray(x);
         return;
     }
     mexErrMsgIdAndTxt("sid:usage", "unknown command '%s'", cmd);

@@ -1,14 +1,27 @@
 function plan = sid_plan_for(H, CAindex, X, Y)
 % SID_PLAN_FOR  Resident libsid projector plan for the PSF H (created on first
-% use, reused while H keeps its size and contents).  CAindex = [] selects the
-% uncropped PSF (forwardProjectGPU semantics).
+% use and reused).  CAindex = [] selects the uncropped PSF (forwardProjectGPU
+% semantics) and the storage the current sid_method() needs; a CAindex gives
+% the cropped direct form (forwardProjectACC semantics).
+% Plans are keyed on the PSF's size, the crop, the sensor size, the storage
+% and a fingerprint of 4096 entries of H at fixed strided positions (a full
+% pass over the 3.3 GB PSF of the 1005^2 x 31 configuration per call would
+% cost more than the projection).  Two PSFs that agree at every sampled
+% entry share a plan: pass distinct PSFs through sid_mex('plan', ...) directly
+% when that can happen.
 persistent keys plans
 if isempty(keys), keys = {}; plans = []; end
-key = sprintf('%s|%s|%d|%d|%.17g', mat2str(size(H)), mat2str(CAindex), X, Y, double(sum(H(:))));
+flags_for = [1, 2, 4, 4 + 8, 4 + 2];   % direct, spectral_f32, _i16, _mixed, _mixed_f32
+if isempty(CAindex), flags = flags_for(sid_method() + 1); else, flags = 1; end
+n = numel(H);
+idx = unique(round(linspace(1, n, min(n, 4096))));
+smp = double(gather(H(idx)));
+w = (1:numel(smp))';
+fp = sprintf('%.17g|%.17g|%.17g', sum(smp(:) .* w), sum(smp(:) .^ 2), smp(end));
+key = sprintf('%s|%s|%d|%d|%d|%s', mat2str(size(H)), mat2str(CAindex), X, Y, flags, fp);
 hit = find(strcmp(keys, key), 1);
 if isempty(hit)
-    if isempty(CAindex), flags = 4 + 8 + 1; else, flags = 1; end   % spectral 16-bit + 24-bit + direct / direct
-    plan = sid_mex('plan', single(H), CAindex, X, Y, flags);
+    plan = sid_mex('plan', single(gather(H)), CAindex, X, Y, flags);
     keys{end+1} = key; plans(end+1) = plan;
 else
     plan = plans(hit);

@@ -89,8 +89,7 @@ def _opts(kind: str, opts: dict | None) -> NnlsOpts:
         elif k in ("use_std", "tol_p"):
             setattr(o, k, int(bool(v)) if k == "use_std" else int(v))
         elif k in ("warm_start", "gpu", "gpu_id", "gpu_ids", "display", "total"):
-            if k == "total" and v:
-                raise NotImplementedError("fast_nnls: opts.total (one line search for all columns) is not supported")
+            pass
         else:
             raise ValueError(f"unknown NNLS option {k!r}")
     return o
@@ -118,26 +117,62 @@ def _ls_nnls(self, A, Y, opts=None, G=None, x=None, prec="split", return_iters=F
     return (X, Gd, it) if return_iters else (X, Gd)
 
 
-def _fast_nnls(self, A, Y, opts=None, prec="split", return_iters=False):
-    """[xx, Q] = fast_nnls(A, Y, opts) (fast_nnls.m:1) on the GPU; opts may
-    carry warm_start (K x F)."""
-    A = to_device(A)
-    Yd, half = _movie(Y)
-    P, K = A.shape
-    F = Yd.shape[1]
+def _fast_nnls(self, A, Y, opts=None, Q=None, df=None, h=None, prec="split", return_iters=False, full=False):
+    """[xx, Q] = fast_nnls(A, Y, opts, Q, df, h) (fast_nnls.m:1) on the GPU.
+
+    opts may carry warm_start (a K x F matrix, or the scalar 1 for the
+    inverse-Gram start of fast_nnls.m:66-69) and total (one step length for
+    all columns, fast_nnls.m:101-117).  Q and h (the normalised Gram and the
+    scaling of a previous call) are passed together; df is optional
+    (fast_nnls.m:58-62).  ``opts=None`` is the reference's two-argument call,
+    whose tolerance is 1e-12 (fast_nnls.m:12-15).  full=True returns
+    (xx, Q, df, h) like the reference's four outputs (df has no columns unless
+    total mode, as the reference removes every retired column from it)."""
+    two_args = opts is None
     opts = dict(opts or {})
+    if two_args:
+        opts["tol"] = 1e-12
     warm = opts.get("warm_start", None)
+    total = 1 if opts.get("total", 0) else 0
+    warm_mode, W = 0, None
     if warm is not None and np.ndim(warm) == 0:
-        raise NotImplementedError("fast_nnls: warm_start == 1 (inverse-Gram start) is not supported")
-    W = to_device(warm) if warm is not None and np.size(warm) else None
+        if float(warm) != 1:
+            raise ValueError("fast_nnls: a scalar warm_start must be 1 (the inverse-Gram start)")
+        warm_mode = 1
+    elif warm is not None and np.size(warm):
+        warm_mode, W = 2, to_device(warm)
     o = _opts("fast_nnls", opts)
-    X = _fortran_tensor((K, F), A.device)
-    Q = _fortran_tensor((K, K), A.device)
-    it = torch.zeros(F, dtype=torch.int32, device=A.device)
-    _lib.call("sid_fast_nnls", self._ctx, A.data_ptr(), Yd.data_ptr(), _lib.DTYPE_F16 if half else _lib.DTYPE_F32,
-              P, K, F, ctypes.byref(o), W.data_ptr() if W is not None else None, X.data_ptr(), Q.data_ptr(),
-              _lib.PREC[prec], it.data_ptr(), _stream_ptr())
-    return (X, Q, it) if return_iters else (X, Q)
+    if (Q is None) != (h is None):
+        raise ValueError("fast_nnls: Q and h are passed together (fast_nnls.m:58-62)")
+    Qd = to_device(Q) if Q is not None else None
+    hd = to_device(np.reshape(h, -1) if not isinstance(h, torch.Tensor) else h.reshape(-1)) if h is not None else None
+    dfd = to_device(df) if df is not None and np.size(df) else None
+    Ad = to_device(A) if A is not None else None
+    K = Ad.shape[1] if Ad is not None else Qd.shape[0]
+    if Y is not None:
+        Yd, half = _movie(Y)
+        F = Yd.shape[1]
+    else:
+        Yd, half = None, False
+        F = dfd.shape[1]
+    P = Ad.shape[0] if Ad is not None else 0
+    X = _fortran_tensor((K, F), "cuda")
+    Qo = _fortran_tensor((K, K), "cuda")
+    ho = torch.empty(K, dtype=torch.float32, device="cuda")
+    dfo = _fortran_tensor((K, F), "cuda") if total else None
+    it = torch.zeros(F, dtype=torch.int32, device="cuda")
+    _lib.call("sid_fast_nnls_ex", self._ctx, Ad.data_ptr() if Ad is not None else None,
+              Yd.data_ptr() if Yd is not None else None, _lib.DTYPE_F16 if half else _lib.DTYPE_F32, P, K, F,
+              ctypes.byref(o), total, warm_mode, W.data_ptr() if W is not None else None,
+              Qd.data_ptr() if Qd is not None else None, dfd.data_ptr() if dfd is not None else None,
+              hd.data_ptr() if hd is not None else None, X.data_ptr(), Qo.data_ptr(),
+              dfo.data_ptr() if dfo is not None else None, ho.data_ptr(), _lib.PREC[prec], it.data_ptr(),
+              _stream_ptr())
+    if full:
+        dfr = dfo if dfo is not None else _fortran_tensor((K, 0), "cuda")
+        out = (X, Qo, dfr, ho)
+        return out + (it,) if return_iters else out
+    return (X, Qo, it) if return_iters else (X, Qo)
 
 
 def _flat_f(a, dtype):
@@ -190,9 +225,9 @@ def LS_nnls(A, Y, opts=None, G=None, x=None):
     return _ctx().ls_nnls(A, Y, opts, G, x)
 
 
-def fast_nnls(A, Y, opts=None):
-    """[xx, Q] = fast_nnls(A, Y, opts) (fast_nnls.m:1)."""
-    return _ctx().fast_nnls(A, Y, opts)
+def fast_nnls(A, Y, opts=None, Q=None, df=None, h=None):
+    """[xx, Q, df, h] = fast_nnls(A, Y, opts, Q, df, h) (fast_nnls.m:1)."""
+    return _ctx().fast_nnls(A, Y, opts, Q, df, h, full=True)
 
 
 def _spatial_update(self, timeseries, sensor_movie, template, opts=None):
@@ -244,7 +279,8 @@ def _nqp(self, Q, b, opts=None):
     """[x, w, info] = NQP(Q, b, opts) (NQP.m:1, default options) on the GPU:
     argmin_{x >= 0} 0.5 x'Qx + b'x in FP64 by the Lawson-Hanson active set.
     Q is n x n, or n x n x B for B independent problems solved at once (b then
-    n x B); n <= 32.  x and w are CUDA float64 tensors shaped like b; info
+    n x B); n <= 4096 (problems above 32 components keep their working
+    arrays in device scratch).  x and w are CUDA float64 tensors shaped like b; info
     carries ``iter`` (an int, or a B-vector).  A problem that reaches the
     iteration cap raises SidError, as NQP.m:116-119 raises its error."""
     opts = dict(opts or {})
@@ -281,35 +317,28 @@ def NQP(Q, b, opts=None):
 def reg_nnls(A, d, opts=None):
     """x = reg_nnls(A, d, opts) (reg_nnls.m:1): the regularised NNLS
     min_{x >= 0} ||A x - d||^2 (+ L1, L2, orthogonality terms) as one NQP.  The
-    n x n system is formed in FP64 on the GPU (reg_nnls.m:40-66) and solved by
-    the batched NQP kernel."""
+    n x n system is formed in FP64 by libsid (reg_nnls.m:40-66) and solved by
+    its Lawson-Hanson kernel (sid_reg_nnls)."""
+    return _ctx().reg_nnls(A, d, opts)
+
+
+def _reg_nnls(self, A, d, opts=None):
     opts = dict(opts or {})
-    At = A.to(device="cuda", dtype=torch.float64) if isinstance(A, torch.Tensor) else \
-        torch.from_numpy(np.asarray(A, dtype=np.float64)).to("cuda")
-    dt = d.to(device="cuda", dtype=torch.float64) if isinstance(d, torch.Tensor) else \
-        torch.from_numpy(np.asarray(d, dtype=np.float64)).to("cuda")
-    dt = dt.reshape(At.shape[0], -1)
-    n = At.shape[1]
+    At = _f64_fortran(A)
+    m, n = (tuple(A.shape) if isinstance(A, torch.Tensor) else np.shape(A))[:2]
+    dt = _f64_fortran(d)
+    if dt.numel() != m:
+        raise ValueError(f"reg_nnls: d must hold {m} values, got {dt.numel()}")
     hilf = opts.get("hilf")
-    if hilf is None:
-        hilf = torch.ones(n, n, dtype=torch.float64, device="cuda") - torch.eye(n, dtype=torch.float64, device="cuda")
-        if opts.get("bg_sub", 0):
-            hilf[:, -1] = 0
-            hilf[-1, :] = 0
-    else:
-        hilf = hilf.to(device="cuda", dtype=torch.float64) if isinstance(hilf, torch.Tensor) else \
-            torch.from_numpy(np.asarray(hilf, dtype=np.float64)).to("cuda")
-    Q = At.T @ At
-    q = -(At.T @ dt)
-    if opts.get("use_std", False):
-        tt = At.sum(dim=0)
-        Q = Q - torch.outer(tt, tt) / At.shape[0]
-        q = q + tt[:, None] * dt.sum(dim=0)[None, :] / At.shape[0]
-    if opts.get("lamb_L1", 0):
-        q = q + float(opts["lamb_L1"])
-    if opts.get("lamb_L2", 0):
-        Q = Q + float(opts["lamb_L2"]) * torch.eye(n, dtype=torch.float64, device="cuda")
-    if opts.get("lamb_orth_L1", 0):
-        Q = Q + float(opts["lamb_orth_L1"]) * hilf
-    x, _, _ = NQP(Q, q[:, 0])
+    hd = _f64_fortran(hilf) if hilf is not None else None
+    if hd is not None and hd.numel() != n * n:
+        raise ValueError(f"reg_nnls: hilf must be {n} x {n}")
+    x = torch.empty(n, dtype=torch.float64, device="cuda")
+    _lib.call("sid_reg_nnls", self._ctx, At.data_ptr(), m, n, dt.data_ptr(), float(opts.get("lamb_L1", 0.0)),
+              float(opts.get("lamb_L2", 0.0)), float(opts.get("lamb_orth_L1", 0.0)),
+              1 if opts.get("use_std", False) else 0, 1 if opts.get("bg_sub", 0) else 0,
+              hd.data_ptr() if hd is not None else None, x.data_ptr(), _stream_ptr())
     return x
+
+
+Context.reg_nnls = _reg_nnls

@@ -144,3 +144,48 @@ def test_cfg1_rl_poisson_30_iterations(cfg1):
     for m in ("spectral_f32", "spectral_mixed"):
         out = s.to_numpy(P.rl_poisson(y, X0, 30, method=m))
         assert rel_l2(out, ref) < 1e-4, (m, rel_l2(out, ref))
+
+
+def test_cfg2_library_sampled_pixels(cfg1):
+    """Library generation at the 800-neuron size (generate_LFM_library_GPU.m:
+    63-109: neur_rad 12, axial 2, one component): 20 neurons' rows against an
+    FP64 restatement at 500 sampled pixels each inside their sensor footprints,
+    summing every voxel of the neuron's box through the PSF
+    (forwardProjectACC.m:21-25 with the full PSF)."""
+    import ctypes
+
+    import torch
+    import sid_gb300 as s
+    from sid_gb300 import _lib, synthetic
+    H, V, y, P = cfg1
+    X, Y, Z = V.shape
+    M, N = H.shape[0], H.shape[2]
+    cf = M // 2
+    K = 800
+    vol, centers = synthetic.neuron_volume(X, Y, Z, K)
+    dv = s.to_device(vol)
+    out = torch.zeros((K, X * Y), dtype=torch.float32, device="cuda")  # column layout: out[n, pixel]
+    ptrs = (ctypes.c_void_p * 1)(dv.data_ptr())
+    c = np.asfortranarray(centers)
+    ids = np.ones((K, 1), dtype=np.uint8, order="F")
+    _lib.call("sid_library", P._plan, ctypes.cast(ptrs, ctypes.c_void_p), 1, c.ctypes.data, ids.ctypes.data, K, 12,
+              2.0, out.data_ptr(), 1, s.lfm._stream_ptr())
+    torch.cuda.synchronize()
+    boxes = s.library_boxes(centers, 12, 2.0, (X, Y, Z))  # 0-based half-open
+    rng = np.random.default_rng(17)
+    worst = 0.0
+    for n in rng.choice(K, 20, replace=False):
+        x0, x1, y0, y1, z0, z1 = (int(v) for v in boxes[n])
+        p, q, cc = np.meshgrid(np.arange(x0, x1), np.arange(y0, y1), np.arange(z0, z1), indexing="ij")
+        p, q, cc = p.ravel(), q.ravel(), cc.ravel()
+        val = vol[p, q, cc].astype(np.float64)
+        px = rng.integers(max(0, x0 - cf), min(X, x1 + cf), 500)
+        py = rng.integers(max(0, y0 - cf), min(Y, y1 + cf), 500)
+        i = px[:, None] - p[None, :] + cf
+        j = py[:, None] - q[None, :] + cf
+        ok = (i >= 0) & (i < M) & (j >= 0) & (j < M)
+        hv = H[np.clip(i, 0, M - 1), np.clip(j, 0, M - 1), (p % N)[None, :], (q % N)[None, :], cc[None, :]]
+        ref = np.sum(np.where(ok, hv.astype(np.float64), 0.0) * val[None, :], axis=1)
+        got = out[int(n)].cpu().numpy()[px + X * py]
+        worst = max(worst, rel_l2(got, ref))
+    assert worst < 1e-5, worst

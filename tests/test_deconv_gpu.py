@@ -128,3 +128,53 @@ def test_isra_zero_rules(gpu):
     out = s.to_numpy(P.isra(Htf, X0, 2))
     assert np.all(np.isfinite(out))
     assert out[0, 0, 1] == 0.0
+
+
+@pytest.mark.parametrize("p,lam", [(1, [0.02, 0.01, 0.005]), (2, [0.05, 0.03, 0.01])])
+def test_isra_tv_matches_oracle(small, p, lam):
+    """deconvRL mode 'TV' (deconvRL.m:61-83): p = 1 (sign of forward
+    differences) and p = 2 (7-point filter), with the iteration history."""
+    import sid_gb300 as s
+    from oracle import oracle as o
+    H, y, P, fwd, bwd = small
+    Htf = bwd(y).astype(np.float32)
+    opts = {"lambda": lam, "p": p, "mode": "TV"}
+    ref = o.deconvRL(fwd, bwd, Htf, 6, Htf, opts)
+    P.default_method = "direct"
+    out, hist = s.deconvRL(P.forward, P.adjoint, Htf, 6, Htf, opts, nargout=2)
+    assert rel_l2(s.to_numpy(out), ref) < 1e-4, rel_l2(s.to_numpy(out), ref)
+    h = hist.cpu().numpy()
+    assert h.shape == (6,) + Htf.shape
+    np.testing.assert_array_equal(h[5], s.to_numpy(out))
+    ref3 = o.deconvRL(fwd, bwd, Htf, 3, Htf, opts)
+    assert rel_l2(h[2], ref3) < 1e-4
+
+
+def test_isra_basic_history(small):
+    """Xguess_history of mode 'basic' (deconvRL.m:10,90-92): one volume per iteration."""
+    import sid_gb300 as s
+    from oracle import oracle as o
+    H, y, P, fwd, bwd = small
+    Htf = bwd(y).astype(np.float32)
+    P.default_method = "direct"
+    out, hist = s.deconvRL(P.forward, P.adjoint, Htf, 4, Htf, None, nargout=2)
+    h = hist.cpu().numpy()
+    for k in range(4):
+        assert rel_l2(h[k], o.deconvRL(fwd, bwd, Htf, k + 1, Htf)) < 1e-5
+
+
+@pytest.mark.parametrize("opts", [{"lamb_TV_L2": [0.01, 0.02, 0.005], "max_iter": 6},
+                                  {"lamb_TV_L2": [0.01, 0.02, 0.005], "lamb_TV_L1": 0.1, "lamb_L2": 0.05,
+                                   "lamb_L1": 1e-3, "max_iter": 6}])
+def test_ls_deconv_tv_matches_oracle(small, opts):
+    """LS_deconv's lamb_TV_L2 Laplacian term in Q (LS_deconv.m:49-73), and the
+    step length from Q itself when lamb_TV_L1 * lamb_TV_L2 * lamb_L2 is nonzero
+    in every component (LS_deconv.m:82-83)."""
+    import sid_gb300 as s
+    from oracle import oracle as o
+    H, y, P, fwd, bwd = small
+    Htf = bwd(y).astype(np.float32)
+    ref = o.LS_deconv(fwd, bwd, Htf, opts)
+    P.default_method = "direct"
+    out = s.to_numpy(s.LS_deconv(P.forward, P.adjoint, Htf, opts))
+    assert rel_l2(out, ref) < 1e-4, rel_l2(out, ref)

@@ -82,9 +82,9 @@ def test_fast_nnls_matches_oracle(ctx, oracle, prec):
     viol, _ = kkt(A, Y[:, early], Xg[:, early])
     assert viol < 1e-4, viol
     assert rel_l2(to_numpy(Q), Qo) < 1e-5
-    assert rel_l2(Xg, Xo) < 1e-3, rel_l2(Xg, Xo)
+    assert rel_l2(Xg, Xo) < 1e-4, rel_l2(Xg, Xo)
     viol, mn = kkt(A, Y, Xg)
-    assert mn >= 0 and viol < 1e-3, viol
+    assert mn >= 0 and viol < 1e-4, viol
 
 
 @pytest.mark.parametrize("prec", ["fp32", "split"])
@@ -113,7 +113,7 @@ def test_fast_nnls_warm_start(ctx, oracle):
     W = np.asfortranarray(T.astype(np.float32))
     Xg, _ = ctx.fast_nnls(A, Y, {"warm_start": W}, prec="split")
     Xo, _, _, _ = oracle.fast_nnls(A, Y, {"warm_start": W.astype(np.float64)})
-    assert rel_l2(to_numpy(Xg), Xo) < 1e-3
+    assert rel_l2(to_numpy(Xg), Xo) < 1e-4
 
 
 def test_ls_nnls_half_movie_and_lambda(ctx, oracle):
@@ -152,3 +152,46 @@ def test_ls_nnls_warm_start_and_given_gram(ctx, oracle):
     Xg, _ = ctx.ls_nnls(A, Y, {}, G=G, x=x0, prec="split")
     Xo, _ = oracle.LS_nnls(A, Y, {}, G=G.astype(np.float64), x=x0.astype(np.float64))
     assert rel_l2(to_numpy(Xg), Xo) < 1e-4
+
+
+def test_fast_nnls_inverse_gram_warm_start(ctx, oracle):
+    """opts.warm_start == 1: x = inv(Q)(-df) clamped at zero (fast_nnls.m:66-69)."""
+    from sid_gb300 import to_numpy
+    A, Y, _ = problem(1200, 30, 48, 9)
+    Xg, _ = ctx.fast_nnls(A, Y, {"warm_start": 1}, prec="fp32")
+    Xo, _, _, _ = oracle.fast_nnls(A, Y, {"warm_start": 1})
+    assert rel_l2(to_numpy(Xg), Xo) < 1e-4, rel_l2(to_numpy(Xg), Xo)
+
+
+@pytest.mark.parametrize("prec", ["fp32", "split"])
+def test_fast_nnls_total_mode(ctx, oracle, prec):
+    """opts.total: one step length for all columns (fast_nnls.m:101-117).  The
+    reference's loop ends at max_iter without copying x into xx, so xx is
+    diag(h) * ones; its df holds the iterations' result."""
+    from sid_gb300 import to_numpy
+    A, Y, _ = problem(900, 20, 32, 10)
+    X, Q, df, h = ctx.fast_nnls(A, Y, {"total": 1, "max_iter": 300}, prec=prec, full=True)
+    Xo, Qo, dfo, ho = oracle.fast_nnls(A, Y, {"total": 1, "max_iter": 300})
+    # h = 1 ./ sqrt(diag(A'A)): FP32 rounding, or the split products' 1e-5 bar
+    rt = 2e-6 if prec == "fp32" else 1e-5
+    np.testing.assert_allclose(to_numpy(X), Xo, rtol=rt)
+    np.testing.assert_allclose(h.cpu().numpy(), ho, rtol=rt)
+    assert rel_l2(to_numpy(df), dfo) < 1e-4, rel_l2(to_numpy(df), dfo)
+
+
+def test_fast_nnls_caller_q_df_h_and_two_argument_tol(ctx, oracle):
+    """fast_nnls(A, Y, opts, Q, df, h) reuses the caller's normalised Gram,
+    scaling and gradient (fast_nnls.m:58-62); the two-argument call uses
+    tol = 1e-12 (fast_nnls.m:12-15)."""
+    from sid_gb300 import to_numpy
+    A, Y, _ = problem(1000, 24, 40, 11)
+    X1, Q1, _, h1 = ctx.fast_nnls(A, Y, {}, prec="fp32", full=True)
+    Q64 = to_numpy(Q1).astype(np.float64)
+    h64 = h1.cpu().numpy().astype(np.float64)
+    df0 = h64[:, None] * (-(A.astype(np.float64).T @ Y.astype(np.float64)))
+    X2, _ = ctx.fast_nnls(None, None, {}, Q=Q1, df=np.asfortranarray(df0.astype(np.float32)), h=h1, prec="fp32")
+    Xo, _, _, _ = oracle.fast_nnls(A, Y, {}, Q64, df0, h64)
+    assert rel_l2(to_numpy(X2), Xo) < 1e-4, rel_l2(to_numpy(X2), Xo)
+    X3, _ = ctx.fast_nnls(A, Y, None, prec="fp32")
+    Xo3, _, _, _ = oracle.fast_nnls(A, Y, {"tol": 1e-12})
+    assert rel_l2(to_numpy(X3), Xo3) < 1e-4, rel_l2(to_numpy(X3), Xo3)

@@ -89,7 +89,7 @@ def _nqp_problems(rng, n, B):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("n", [1, 5, 17, 32])
+@pytest.mark.parametrize("n", [1, 5, 17, 32, 33, 64, 128])
 def test_nqp_batched_matches_oracle(gpu, oracle, n):
     """[x, w, info] = NQP(Q, b) (NQP.m:42-178) for a stack of independent
     problems against the oracle's Lawson-Hanson restatement, both FP64."""
@@ -131,4 +131,44 @@ def test_reg_nnls_matches_oracle(gpu, oracle, opts):
 def test_nqp_rejects_oversized_problem(gpu):
     import sid_gb300 as s
     with pytest.raises(s.SidError):
-        s.NQP(np.eye(33), np.ones(33))
+        s.NQP(np.eye(4097), np.ones(4097))
+
+
+def crowded_problem(seed, R=60, F=400, side=16):
+    """R templates that all cover the centre of a small field: the centre
+    pixels have up to R + 1 covering components (with the background), far
+    more than the 32 a thread keeps in registers."""
+    rng = np.random.default_rng(seed)
+    P = side * side
+    yy, xx = np.meshgrid(np.arange(side), np.arange(side), indexing="ij")
+    tmpl = np.zeros((R, P), dtype=bool)
+    S = np.zeros((R + 1, P))
+    for r in range(R):
+        cx, cy = side / 2 + rng.uniform(-2, 2), side / 2 + rng.uniform(-2, 2)
+        rad = rng.uniform(4, 8)
+        m = ((xx - cx) ** 2 + (yy - cy) ** 2 < rad ** 2).ravel()
+        tmpl[r] = m
+        S[r, m] = rng.random(m.sum())
+    S[R] = 0.05
+    # sparse transients keep the 61 x 61 pixel Grams well conditioned (about 75),
+    # so FP32 products into the FP64 solve stay within the 1e-4 bar
+    T = rng.random((R + 1, F)) * (rng.random((R + 1, F)) < 0.2)
+    T[R] = 1.0
+    Y = S.T @ T + 0.01 * rng.standard_normal((P, F))
+    return np.asfortranarray(T.astype(np.float32)), np.asfortranarray(Y.astype(np.float32)), tmpl
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("opts", [{"bg_sub": 1}, {"bg_sub": 1, "lamb_L2": 0.05, "lamb_orth_L1": 1e-3}])
+def test_spatial_update_crowded_pixels(gpu, oracle, opts):
+    """update_spatial_component.m:86-97 solves every pixel whatever the number
+    of neurons covering it: pixels with 33 to 61 components against the oracle."""
+    import sid_gb300 as s
+    T, Y, tmpl = crowded_problem(8)
+    counts = tmpl.sum(axis=0) + 1
+    assert counts.max() > 40 and (counts > 32).sum() >= 20
+    ref = oracle.update_spatial_component(T, Y, tmpl, opts)
+    got = s.to_numpy(s.update_spatial_component(T, Y, tmpl, opts))
+    big = counts > 32
+    assert rel_l2(got[:, big], ref[:, big]) < 1e-4, rel_l2(got[:, big], ref[:, big])
+    assert rel_l2(got, ref) < 1e-4, rel_l2(got, ref)
