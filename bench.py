@@ -50,6 +50,10 @@ def parse():
     ap.add_argument("--no-nnls", action="store_true", help="skip the library + temporal NNLS measurement")
     ap.add_argument("--nnls-frames", type=int, default=3000)
     ap.add_argument("--nnls-neurons", type=int, default=800)
+    ap.add_argument("--no-demix", action="store_true", help="skip the demixing-loop measurement")
+    ap.add_argument("--demix-neurons", type=int, default=1500)
+    ap.add_argument("--demix-frames", type=int, default=5000)
+    ap.add_argument("--demix-iters", type=int, default=5)
     ap.add_argument("--nnls-fp64-frames", type=int, default=192,
                     help="frames of the temporal NNLS solved again in FP64 (oracle) for the accuracy fields")
     return ap.parse_args()
@@ -343,6 +347,170 @@ def nnls_workload(args, P_proj):
     return out
 
 
+def demix_workload(args, P_proj):
+    """The alternating SID demixing loop (sid_main.m:470-511) on the
+    1500-neuron, 5000-frame configuration at 1005^2: neurons and their
+    library rows from the projector (generate_LFM_library_GPU.m), square
+    support templates of 20-200 lenslets (log-uniform), an FP16 movie
+    Y = S'T + b + noise, then per outer iteration the spatial update
+    (spatial_SID_update.m:32-33: rows of T normalised, update_spatial_component),
+    the temporal update (temporal_SID_update.m:42-47: rows of the forward model
+    normalised, fast_nnls warm-started at the previous traces) and merge_filters.
+    Times each stage; after the last iteration checks the spatial update at 256
+    pixels and the temporal update at 64 frames against FP64 (oracle), and the
+    gradient of ||Y - S'T||^2 / 2 from the contractions against central
+    differences at 32 entries."""
+    import ctypes
+
+    import numpy as np
+    import torch
+
+    import sid_gb300 as s
+    from oracle import oracle
+    from sid_gb300 import _lib, synthetic
+    K, F, iters = args.demix_neurons, args.demix_frames, args.demix_iters
+    X, Y, Z, N = P_proj.X, P_proj.Y, P_proj.Z, P_proj.Nnum
+    P = X * Y
+    dev = "cuda"
+    vol, centers = synthetic.neuron_volume(X, Y, Z, K, seed=9)
+    lib = s.lfm._fortran_tensor((P, K), dev)
+    ptrs = (ctypes.c_void_p * 1)(s.to_device(vol).data_ptr())
+    c = np.asfortranarray(centers)
+    ids = np.ones((K, 1), dtype=np.uint8, order="F")
+    _lib.call("sid_library", P_proj._plan, ctypes.cast(ptrs, ctypes.c_void_p), 1, c.ctypes.data, ids.ctypes.data, K, 12,
+              2.0, lib.data_ptr(), 1, s.lfm._stream_ptr())
+    lib.div_(torch.linalg.vector_norm(lib, dim=0).clamp_min(1e-30))
+    # templates: square crops of 20..200 lenslets around each centre
+    rng = np.random.default_rng(13)
+    area = np.exp(rng.uniform(np.log(20), np.log(200), K))
+    half = np.sqrt(area) * N / 2
+    tmpl = torch.zeros((P, K), dtype=torch.uint8, device=dev).T  # K x P, column-major (template(k, p))
+    tv = tmpl.T.reshape(Y, X, K)  # [y][x][k] view of the same memory
+    for k in range(K):
+        x0, x1 = max(0, int(centers[k, 0] - half[k])), min(X, int(centers[k, 0] + half[k]) + 1)
+        y0, y1 = max(0, int(centers[k, 1] - half[k])), min(Y, int(centers[k, 1] + half[k]) + 1)
+        tv[y0:y1, x0:x1, k] = 1
+    # movie: S'T (the library restricted to its templates) + background + noise, FP16, pixel chunks
+    g = torch.Generator(device=dev).manual_seed(17)
+    ev = (torch.rand(K, F, generator=g, device=dev) < 0.025).float() * (0.5 + torch.rand(K, F, generator=g,
+                                                                                        device=dev))
+    kern = torch.exp(-torch.arange(0, 40, device=dev, dtype=torch.float32) / 6.0)
+    T_true = torch.nn.functional.conv1d(ev[:, None, :], kern.flip(0)[None, None, :], padding=39)[:, 0, :F]
+    Y16 = torch.empty((F, P), dtype=torch.float16, device=dev).T  # P x F column-major
+    S_true = lib * tmpl.T.float()  # P x K, zero outside the templates
+    step = 1 << 15
+    rms = None
+    for p0 in range(0, P, step):
+        sig = S_true[p0:p0 + step] @ T_true
+        if rms is None:
+            rms = float(sig.pow(2).mean().sqrt())
+        Y16[p0:p0 + step] = (sig + rms / 10 + rms / 10 * torch.randn(sig.shape, generator=g, device=dev)).half()
+    del S_true, sig
+    # initial state: the library as forward model, traces from an unregularised first temporal pass
+    ctx = s.Context()
+    Tk = torch.cat([T_true * 0 + 0.1, torch.ones(1, F, device=dev)], 0)  # R x F, background last
+    fm = torch.cat([lib.T, torch.full((1, P), 1.0 / np.sqrt(P), device=dev)], 0)  # R x P
+    fm = s.to_device(fm)
+    R = K + 1
+
+    def ev_t():
+        e = torch.cuda.Event(enable_timing=True)
+        e.record()
+        return e
+
+    stage = {"spatial_ms": [], "temporal_ms": [], "merge_ms": []}
+    kept = R
+    for it in range(iters):
+        e0 = ev_t()
+        # spatial_SID_update.m:32-33
+        Tn = Tk / torch.linalg.vector_norm(Tk, dim=1, keepdim=True).clamp_min(1e-30)
+        fm = ctx.spatial_update(Tn, Y16, tmpl[:kept - 1], {"bg_sub": 1})
+        e1 = ev_t()
+        # temporal_SID_update.m:42-47
+        fmn = fm / torch.linalg.vector_norm(fm, dim=1, keepdim=True).clamp_min(1e-30)
+        A = s.to_device(fmn.T)  # P x R, column-major
+        Tk, _ = ctx.fast_nnls(A, Y16, {"warm_start": s.to_device(Tk)}, prec="split")
+        e2 = ev_t()
+        fm, Tk, tm2, _ = s.merge_filters(fmn, Tk, tmpl[:kept - 1], np.arange(kept), {"limit": 0.9, "bg_sub": 1})
+        tmpl = tm2.to(torch.uint8)
+        kept = Tk.shape[0]
+        e3 = ev_t()
+        torch.cuda.synchronize()
+        stage["spatial_ms"].append(e0.elapsed_time(e1))
+        stage["temporal_ms"].append(e1.elapsed_time(e2))
+        stage["merge_ms"].append(e2.elapsed_time(e3))
+        del A
+    out = {"workload": f"demixing loop {K} neurons x {F} frames at {X}x{Y} (FP16 movie), {iters} outer iterations, "
+                       f"templates of 20-200 lenslets",
+           "components_after": int(kept),
+           "seconds_per_outer_iteration": float(np.mean([a + b + c_ for a, b, c_ in zip(
+               stage["spatial_ms"], stage["temporal_ms"], stage["merge_ms"])]) / 1e3)}
+    out.update({k: [round(v, 2) for v in vals] for k, vals in stage.items()})
+    # FP64 checks after the last iteration
+    Tn = Tk / torch.linalg.vector_norm(Tk, dim=1, keepdim=True).clamp_min(1e-30)
+    fm_last = ctx.spatial_update(Tn, Y16, tmpl[:kept - 1], {"bg_sub": 1})
+    torch.cuda.synchronize()
+    tm_np = tmpl[:kept - 1]
+    cover = torch.nonzero(tm_np.sum(dim=0) > 0).flatten().cpu().numpy()
+    pix = np.sort(rng.choice(cover, 256, replace=False))
+    Tn64 = Tn.double().cpu().numpy()
+    errs_num, errs_den = 0.0, 0.0
+    ncomp = []
+    for p in pix:
+        idx = np.append(np.flatnonzero(tm_np[:, int(p)].cpu().numpy()), kept - 1)
+        ncomp.append(len(idx))
+        yv = Y16[int(p)].double().cpu().numpy()
+        nrm = np.linalg.norm(yv)
+        ref = oracle.reg_nnls(Tn64[idx].T, yv / nrm, {"bg_sub": 1}) * nrm
+        got = fm_last[torch.as_tensor(idx, device=dev), int(p)].double().cpu().numpy()
+        errs_num += float(np.sum((got - ref) ** 2))
+        errs_den += float(np.sum(ref ** 2))
+    out["spatial_vs_fp64_256px"] = {"rel_l2": float(np.sqrt(errs_num / max(errs_den, 1e-300))),
+                                     "components_per_pixel_max": int(max(ncomp)),
+                                     "components_per_pixel_median": float(np.median(ncomp))}
+    # temporal update at 64 frames: the same warm-started solve in FP64
+    fmn = fm_last / torch.linalg.vector_norm(fm_last, dim=1, keepdim=True).clamp_min(1e-30)
+    A = s.to_device(fmn.T)
+    W = Tk.clone()
+    Tg, _ = ctx.fast_nnls(A, Y16, {"warm_start": s.to_device(W)}, prec="split")
+    cols = np.sort(rng.choice(F, 64, replace=False))
+    ci = torch.as_tensor(cols, device=dev)
+    Q = torch.zeros(kept, kept, dtype=torch.float64, device=dev)
+    cr = torch.zeros(kept, len(cols), dtype=torch.float64, device=dev)
+    for p0 in range(0, P, 1 << 16):
+        a = A[p0:p0 + (1 << 16)].double()
+        Q += a.T @ a
+        cr += a.T @ Y16[p0:p0 + (1 << 16)].index_select(1, ci).double()
+    Q, cr = Q.cpu().numpy(), cr.cpu().numpy()
+    dq = np.sqrt(np.diag(Q))
+    h = 1.0 / dq
+    Wc = W.index_select(1, ci).double().cpu().numpy()
+    x64, *_ = oracle.fast_nnls(np.zeros((0, kept)), np.zeros((0, len(cols))), {"warm_start": Wc},
+                               Q / np.outer(dq, dq), h[:, None] * (-cr), h)
+    out["temporal_vs_fp64_64frames"] = nnls_accuracy(Tg.index_select(1, ci).double().cpu().numpy(), x64, Q, cr)
+    # gradient of ||Y - A T||^2 / 2 wrt T from the contractions vs central differences (FP64)
+    G = ctx.gram(A, "split").double()
+    C = ctx.cross(A, Y16, "split").double()
+    grad = G @ Tg.double() - C
+    ent = np.stack([rng.integers(0, kept, 32), rng.integers(0, F, 32)], 1)
+    fd, gv = [], []
+    for k, f in ent:
+        yv = Y16[:, int(f)].double()
+        t = Tg[:, int(f)].double()
+        r = yv.clone()
+        for p0 in range(0, P, 1 << 17):
+            r[p0:p0 + (1 << 17)] -= A[p0:p0 + (1 << 17)].double() @ t
+        a = A[:, int(k)].double()
+        hh = 1e-3 * max(abs(float(t[int(k)])), 1e-3)
+        fp = 0.5 * torch.sum((r - hh * a) ** 2)
+        fm_ = 0.5 * torch.sum((r + hh * a) ** 2)
+        fd.append(float((fp - fm_) / (2 * hh)))
+        gv.append(float(grad[int(k), int(f)]))
+    fd, gv = np.array(fd), np.array(gv)
+    out["gradient_vs_central_differences_32"] = float(np.linalg.norm(gv - fd) / np.linalg.norm(fd))
+    return out
+
+
 def peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -532,6 +700,11 @@ def main():
     nnls = None
     if not args.no_nnls:
         nnls = nnls_workload(args, P)
+        torch.cuda.empty_cache()
+    demix = None
+    if not args.no_demix and not args.no_nnls:
+        demix = demix_workload(args, P)
+        torch.cuda.empty_cache()
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -573,6 +746,7 @@ def main():
             "mixed_vs_fp32_direct": (value / world) / others["direct"]["rl_iter_s"] if "direct" in others else None,
             "plan": {"L": info["L"], "D": info["D"], "device_gb": info["device_bytes"] / 1e9},
             "nnls": nnls,
+            "demix": demix,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
