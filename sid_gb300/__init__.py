@@ -10,6 +10,7 @@ from .nmf import S_update, T_update  # noqa: F401
 from .background import compute_std_image, rank_1_factorization  # noqa: F401
 from .postproc import ImageRect, SNR_order, merge_filters, read_sensor_movie, rectify_frames  # noqa: F401
 from .tiff import read_tiff  # noqa: F401
+from .matfile import load_psf, matfile_read  # noqa: F401
 from .extract import Extractor, incremental_temporal_update_gpu  # noqa: F401
 from .lfm import (  # noqa: F401
     LS_deconv,

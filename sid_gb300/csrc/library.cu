@@ -63,7 +63,7 @@ __global__ void k_lib_average(const float* const* __restrict__ recon, const uint
 // range checks.  The lattice ranges of every neuron and phase are computed once
 // per CTA.
 constexpr int kLibT = 4;  // consecutive output lenslets per thread
-constexpr int kLibG = 8;  // neurons per CTA
+constexpr int kLibG = 16;  // neurons per CTA
 
 template <int G>
 __global__ void __launch_bounds__(256)
@@ -182,29 +182,35 @@ __device__ __forceinline__ void cp_async4_lib(float* dst, const float* src)
 
 struct LibTileArgs {
     int N, D, dlo, span, W, Wt, rows, pitch, cb, tsz;
+    int bwm;  // widest box (x extent) of any neuron: the staged lattice rows hold bwm floats
     int64_t tbs;
     int Lx, Ly;
     int64_t X, Y, ldn, ldp;
 };
 
 template <int G, int TB, int NRV>
-__global__ void __launch_bounds__(256, 2)
+__global__ void __launch_bounds__(32 * G, 16 / G)
 k_lib_tile(const float* __restrict__ taps, const float* __restrict__ packed, const LibBox* __restrict__ boxes,
            const int* __restrict__ groups, const LibTileArgs a, float* __restrict__ out)
 {
     constexpr int NTB = 1;
-    constexpr int PPW = (G * NTB + 7) / 8;  // (neuron, column block) pairs per warp
+    constexpr int NWARP = G;                // one warp per neuron of the group
+    constexpr int NT = 32 * NWARP;
+    constexpr int PPW = (G * NTB + NWARP - 1) / NWARP;  // (neuron, column block) pairs per warp
+    constexpr int RI = (768 + NT - 1) / NT;             // tap copies per thread and tile (D*D <= 768)
     constexpr int NW = TB + NRV - 1;        // taps held per lattice row
-    extern __shared__ float sm[];           // 2 x N tiles of rows x pitch, then neuron tables
+    extern __shared__ float sm[];           // 2 x N tiles of rows x pitch, 2 x G x NRV box rows, neuron tables
     const int N = a.N, D = a.D, tsz = a.tsz;
-    int* tab = reinterpret_cast<int*>(sm + 2 * N * tsz);
+    float* vrows = sm + 2 * N * tsz;        // [buf][k][e][x - x0]: the box rows of lattice row vlo + e at (c, b)
+    const int vstride = NRV * a.bwm;
+    int* tab = reinterpret_cast<int*>(vrows + 2 * G * vstride);
     // per neuron k: [0] x0 [1] y0 [2] z0 [3] bw [4] bh [5] off [6] umin [7] vmin, then ulo[N], nu[N], vlo[N], nv[N]
     const int tstride = 8 + 4 * N;
     const int* grp = groups + blockIdx.x * (G + 1);
     const int cnt = grp[0];
     const int o = blockIdx.y;
     const int bp = o / N, ap = o - bp * N;
-    for (int i = threadIdx.x; i < 2 * N * tsz; i += blockDim.x) sm[i] = 0.f;
+    for (int i = threadIdx.x; i < 2 * N * tsz + 2 * G * vstride; i += blockDim.x) sm[i] = 0.f;
     for (int e = threadIdx.x; e < cnt * N; e += blockDim.x) {
         const int k = e / N, ph = e - k * N;
         const LibBox b = boxes[grp[1 + k]];
@@ -226,11 +232,11 @@ k_lib_tile(const float* __restrict__ taps, const float* __restrict__ packed, con
     const int z0 = boxes[grp[1]].z0, z1 = boxes[grp[1]].z1;
     const int nst = (z1 - z0) * N;
     const int DD = D * D;
-    // this thread's tap copies: r = tid + 256 i, i < 3 covers D*D <= 768
-    int roff[3];
+    // this thread's tap copies: r = tid + NT i, i < RI covers D*D <= 768
+    int roff[RI];
 #pragma unroll
-    for (int i = 0; i < 3; ++i) {
-        const int r = threadIdx.x + 256 * i;
+    for (int i = 0; i < RI; ++i) {
+        const int r = threadIdx.x + NT * i;
         roff[i] = r < DD ? (r / D + a.span) * a.pitch + (r % D) + a.cb : -1;
     }
     auto issue = [&](int st, int buf) {
@@ -240,8 +246,19 @@ k_lib_tile(const float* __restrict__ taps, const float* __restrict__ packed, con
         for (int aa = 0; aa < N; ++aa) {
             const float* src = taps + ((rowblk + aa) * N + bp) * a.tbs + (int64_t)ap * DD;
 #pragma unroll
-            for (int i = 0; i < 3; ++i)
-                if (roff[i] >= 0) cp_async4_lib(dst0 + aa * tsz + roff[i], src + threadIdx.x + 256 * i);
+            for (int i = 0; i < RI; ++i)
+                if (roff[i] >= 0) cp_async4_lib(dst0 + aa * tsz + roff[i], src + threadIdx.x + NT * i);
+        }
+        // each neuron's box rows y = bb + N (vlo + e), e < nv, at depth c (bw contiguous floats each)
+        float* vdst = vrows + buf * G * vstride;
+        for (int e2 = threadIdx.x; e2 < cnt * vstride; e2 += blockDim.x) {
+            const int k = e2 / vstride, r = e2 - k * vstride;
+            const int e = r / a.bwm, x = r - e * a.bwm;
+            const int* t = tab + k * tstride;
+            if (e < t[8 + 3 * N + bb] && x < t[3]) {
+                const int y = bb + N * (t[8 + 2 * N + bb] + e);
+                cp_async4_lib(vdst + e2, packed + t[5] + t[3] * ((y - t[1]) + t[4] * (c - t[2])) + x);
+            }
         }
         asm volatile("cp.async.commit_group;" ::: "memory");
     };
@@ -266,16 +283,15 @@ k_lib_tile(const float* __restrict__ taps, const float* __restrict__ packed, con
         if (ds < a.W) {
 #pragma unroll
             for (int q = 0; q < PPW; ++q) {
-                const int pr = warp + 8 * q;
+                const int pr = warp + NWARP * q;
                 const int k = pr / NTB, tbk = pr - (pr / NTB) * NTB;
                 if (k >= cnt) continue;
                 const int* t = tab + k * tstride;
                 const int nv = t[8 + 3 * N + bb];
                 if (nv <= 0) continue;
                 const int vlo = t[8 + 2 * N + bb], rvlo = vlo - t[7];
-                const int bw = t[3];
-                // packed index of (x, y, c) = off + (x - x0) + bw * ((y - y0) + bh * (c - z0))
-                const int vrow = t[5] + bw * ((bb + N * vlo - t[1]) + t[4] * (c - t[2])) - t[0];
+                // the staged box rows of this neuron: V(x, bb + N (vlo + e), c) at vk[e * bwm + x - x0]
+                const float* vk = vrows + ((st & 1) * G + k) * vstride - t[0];
                 const int colb = tbk * TB - rvlo - (NRV - 1) + a.cb;
                 for (int aa = 0; aa < N; ++aa) {
                     const int nu = t[8 + N + aa];
@@ -289,11 +305,11 @@ k_lib_tile(const float* __restrict__ taps, const float* __restrict__ packed, con
                         float w[NW];
 #pragma unroll
                         for (int i = 0; i < NW; ++i) w[i] = wp[i];
-                        const float* vp = packed + vrow + aa + N * u;
+                        const float* vp = vk + aa + N * u;
 #pragma unroll
                         for (int e = 0; e < NRV; ++e) {
                             if (e < nv) {
-                                const float val = __ldg(vp + (int64_t)bw * N * e);
+                                const float val = vp[e * a.bwm];
 #pragma unroll
                                 for (int j = 0; j < TB; ++j) acc[q][j] = fmaf(val, w[j - e + NRV - 1], acc[q][j]);
                             }
@@ -307,7 +323,7 @@ k_lib_tile(const float* __restrict__ taps, const float* __restrict__ packed, con
     if (ds < a.W) {
 #pragma unroll
         for (int q = 0; q < PPW; ++q) {
-            const int pr = warp + 8 * q;
+            const int pr = warp + NWARP * q;
             const int k = pr / NTB, tbk = pr - (pr / NTB) * NTB;
             if (k >= cnt) continue;
             const int n = grp[1 + k];
@@ -334,7 +350,7 @@ static int launch_lib_tile_t(dim3 grid, size_t smem, const float* taps, const fl
 {
     SID_CUDA_TRY(cudaFuncSetAttribute(k_lib_tile<kLibG, TB, NRV>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)smem));
-    k_lib_tile<kLibG, TB, NRV><<<grid, 256, smem, st>>>(taps, packed, boxes, groups, a, out);
+    k_lib_tile<kLibG, TB, NRV><<<grid, 32 * kLibG, smem, st>>>(taps, packed, boxes, groups, a, out);
     SID_CHECK_LAUNCH();
     return SID_OK;
 }
@@ -399,7 +415,7 @@ extern "C" int sid_library(sid_plan* p, const float* const* recon, int64_t n_com
     const int64_t N = p->N, D = p->g.D;
     std::vector<LibBox> boxes(n_neur);
     int64_t off = 0;
-    int max_ns = 0, ntgM = 0, span = 0, nrv = 0;
+    int max_ns = 0, ntgM = 0, span = 0, nrv = 0, bwm = 0;
     for (int64_t n = 0; n < n_neur; ++n) {
         int bx[6];
         neuron_box(centers, n_neur, n, neur_rad, axial, p->X, p->Y, p->Z, bx);
@@ -424,6 +440,7 @@ extern "C" int sid_library(sid_plan* p, const float* const* recon, int64_t n_com
         ntgM = std::max(ntgM, (int)cdiv(b.t1 - b.t0, kLibT));
         span = std::max(span, std::max(umax - umin, vmax - vmin));
         nrv = std::max(nrv, (int)std::max(cdiv(b.x1 - b.x0, N), cdiv(b.y1 - b.y0, N)));
+        bwm = std::max(bwm, b.x1 - b.x0);
         boxes[n] = b;
     }
     SID_REQUIRE(off < INT32_MAX, "sid_library: boxes too large");
@@ -436,9 +453,11 @@ extern "C" int sid_library(sid_plan* p, const float* const* recon, int64_t n_com
     ta.cb = span + nrv - 1;
     ta.pitch = (tb + ta.cb) | 1;  // odd: the 32 lanes' rows fall in distinct banks
     ta.tsz = ta.rows * ta.pitch;
-    const size_t tiled_bytes = (size_t)2 * N * ta.tsz * sizeof(float) + (size_t)kLibG * (8 + 4 * N) * sizeof(int);
+    ta.bwm = bwm;
+    const size_t tiled_bytes = (size_t)(2 * N * ta.tsz + 2 * kLibG * std::max(nrv, 1) * bwm) * sizeof(float) +
+                               (size_t)kLibG * (8 + 4 * N) * sizeof(int);
     const bool tiled = ta.W <= 32 && ta.Wt <= 32 && nrv >= 1 && nrv <= 3 && D * D <= 768 &&
-                       tiled_bytes <= 112 * 1024;
+                       tiled_bytes <= 200 * 1024;
     const int Dp = (int)D + 2 * span;
     const size_t tile_bytes =
         (size_t)N * Dp * (Dp + kLibT) * sizeof(float) + (size_t)(D * D + 4 * N * kLibG) * sizeof(int);

@@ -55,6 +55,28 @@ def SNR_order(traces, opts=None):
     return order
 
 
+def _sensor_movie_means(files, idx, x_offset, y_offset, dx, Nnum, do_rectify, cuts, nfiles):
+    """frames.mean (read_sensor_movie.m:65-90): column j of the movie is the
+    mean of the rectified frames idx[j] .. idx[j+1] (both ends included, the
+    mask not applied, as the reference's branch does), j < len(idx) - 1."""
+    from .tiff import read_tiff
+    if not do_rectify:
+        raise NotImplementedError("read_sensor_movie: frames.mean without rectification (the reference's crop "
+                                  "subscript there selects a single column, read_sensor_movie.m:77-79)")
+    cols, size = [], None
+    for j in range(len(idx) - 1):
+        grp = list(range(idx[j], idx[j + 1] + 1))
+        imgs = np.stack([read_tiff(files[i - 1]) for i in grp], axis=2)
+        mov, (R, C) = rectify_frames(imgs if imgs.dtype == np.uint16 else imgs.astype(np.float32), x_offset, y_offset,
+                                     dx, Nnum, True, cuts, None)
+        cols.append(mov.mean(dim=1, keepdim=True))
+        size = (R, C)
+    if not cols:
+        raise ValueError("read_sensor_movie: frames.mean needs at least two frame indices")
+    movie = to_device(torch.cat(cols, dim=1))
+    return movie, (size[0], size[1], nfiles)
+
+
 def _rect_size(rows, cols, xCenter, yCenter, dx, M, crop, cuts):
     c = np.asarray(cuts, dtype=np.int32)
     r_ = np.zeros(1, dtype=np.int64)
@@ -112,13 +134,13 @@ def read_sensor_movie(in_folder, x_offset, y_offset, dx, Nnum, do_rectify=True, 
     files = sorted(glob.glob(os.path.join(in_folder, "*.tif*")), key=os.path.basename)
     nfiles = len(files)
     fr = dict(frames or {})
-    if fr.get("mean", 0):
-        raise NotImplementedError("read_sensor_movie: frames.mean (moving average) does not run natively")
     if fr.get("list") is not None and len(fr["list"]):
         idx = [int(i) for i in fr["list"] if int(i) <= nfiles]
     else:
         idx = list(range(int(fr.get("start", 1)), min(int(fr.get("end", nfiles)), nfiles) + 1, int(fr.get("step", 1))))
     cuts = tuple(int(c) for c in crop_border_microlenses)
+    if fr.get("mean", 0):
+        return _sensor_movie_means(files, idx, x_offset, y_offset, dx, Nnum, do_rectify, cuts, nfiles)
     cols_out = []
     size = None
     for b0 in range(0, len(idx), batch):

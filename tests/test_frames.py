@@ -140,3 +140,28 @@ def test_read_sensor_movie_pipeline(gpu, oracle, tmp_path):
         g = got[:, j].reshape(size[0], size[1], order="F")
         ok = ~np.isnan(ref)
         assert rel_l2(g[ok], ref[ok]) < 1e-6
+
+
+@pytest.mark.gpu
+def test_read_sensor_movie_frame_means(gpu, oracle, tmp_path):
+    """frames.mean (read_sensor_movie.m:65-90): column j is the mean of the
+    rectified frames list(j) .. list(j+1), both ends included."""
+    import sid_gb300 as s
+    rng = np.random.default_rng(4)
+    rows, cols = 160, 150
+    imgs = [rng.uniform(0, 60000, (rows, cols)).astype(np.uint16) for _ in range(8)]
+    for i, im in enumerate(imgs):
+        write_tiff(tmp_path / f"frame_{i:03d}.tif", im, 8, 2)
+    xc, yc, dx, N = 75.0, 80.0, 14.8, 15
+    movie, size = s.read_sensor_movie(str(tmp_path), xc, yc, dx, N, True, {"start": 1, "step": 3, "end": 8,
+                                                                           "mean": 1})
+    got = movie.cpu().numpy()
+    starts = [1, 4, 7]
+    assert got.shape[1] == len(starts) - 1
+    for j in range(len(starts) - 1):
+        refs = [oracle.image_rect(imgs[k - 1].astype(np.float64), xc, yc, dx, N, True, (0, 0, 0, 0))
+                for k in range(starts[j], starts[j + 1] + 1)]
+        ref = np.mean(refs, axis=0)
+        g = got[:, j].reshape(size[0], size[1], order="F")
+        ok = ~np.isnan(ref)
+        assert rel_l2(g[ok], ref[ok]) < 1e-6
