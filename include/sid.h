@@ -143,6 +143,21 @@ int sid_deconv_isra(sid_plan* plan, int method, const float* Htf, float* X,
  * (deconvRL.m:10,90-92). */
 int sid_deconv_isra_ex(sid_plan* plan, int method, const float* Htf, float* X, int maxIter, int mode, int pnorm,
                        const float* lambda3, float* history, void* stream);
+
+/* Several volumes at once (reconstruct_S.m:162-212 reconstructs components
+ * side by side): nb volumes / images given as host arrays of device pointers
+ * (each X x Y x Z or X x Y single).  The spectral forms contract up to four
+ * volumes per pass over the tap spectra, so the spectra stream once per four
+ * volumes; the direct form runs volume by volume.  Results equal nb single
+ * calls up to FP32 rounding.
+ *   sid_forward_batched:     I[b] = forwardProjectGPU(H, V[b])      forwardProjectGPU.m:1
+ *   sid_adjoint_batched:     V[b] = backwardProjectGPU_new(H, I[b]) backwardProjectGPU_new.m:1
+ *   sid_deconv_isra_batched: X[b] = deconvRL(fwd, bwd, Htf[b], maxIter, X[b], opts) in mode
+ *                            'basic' with opts.lambda = lambda     deconvRL.m:1 */
+int sid_forward_batched(sid_plan* plan, int method, int64_t nb, const float* const* V, float* const* I, void* stream);
+int sid_adjoint_batched(sid_plan* plan, int method, int64_t nb, const float* const* I, float* const* V, void* stream);
+int sid_deconv_isra_batched(sid_plan* plan, int method, int64_t nb, const float* const* Htf, float* const* X,
+                            int maxIter, float lambda, void* stream);
 /* Host-array form of sid_deconv_isra (copies in, iterates, copies X out). */
 int sid_deconv_isra_host(sid_plan* plan, int method, const float* Htf, float* X,
                          int maxIter, float lambda);

@@ -4,6 +4,7 @@
 // (Vp[c][b][a][v][u]), so an iteration is: forward (polyphase in/out),
 // adjoint, and one fused elementwise pass; the V <-> Vp transposes run only at
 // entry and exit.
+#include <algorithm>
 #include <cmath>
 
 #include <utility>
@@ -684,6 +685,136 @@ extern "C" int sid_deconv_ls_ex(sid_plan* p, int method, float* X, int max_iter,
         SID_CHECK_LAUNCH();
     }
     SID_TRY(vp_to_v(p, xp, X, p->Z, st));
+    return SID_OK;
+}
+
+// --------------------------------------------------- several volumes at once --
+// Projections of nb volumes (polyphase, back to back): the spectral forms run
+// up to four volumes per tap-spectrum pass (spectral_forward_batch); the
+// direct form and the per-volume steps (neuron kernel, weak-voxel
+// recomputation) go volume by volume.
+static int spectral_fmt_fwd(int method, bool* i16)
+{
+    switch (method) {
+    case SID_METHOD_SPECTRAL_F32: *i16 = false; return 1;
+    case SID_METHOD_SPECTRAL_I16:
+    case SID_METHOD_SPECTRAL_MIXED:
+    case SID_METHOD_SPECTRAL_MIXED_F32: *i16 = true; return 1;
+    default: return 0;
+    }
+}
+
+static int spectral_fmt_adj(int method)
+{
+    switch (method) {
+    case SID_METHOD_SPECTRAL_F32: return FMT_F32;
+    case SID_METHOD_SPECTRAL_I16: return FMT_I16;
+    case SID_METHOD_SPECTRAL_MIXED: return FMT_F24;
+    case SID_METHOD_SPECTRAL_MIXED_F32: return FMT_F32;
+    default: return -1;
+    }
+}
+
+int fwd_poly_batch(sid_plan* p, int method, const float* vp, float* ip, int nb, cudaStream_t st)
+{
+    const int64_t nv = vol_plane_elems(p) * p->Z, ni = vol_plane_elems(p);
+    bool i16 = false;
+    if (nb == 1 || p->kdims[0] || !spectral_fmt_fwd(method, &i16)) {
+        for (int b = 0; b < nb; ++b) SID_TRY(fwd_poly(p, method, vp + b * nv, ip + b * ni, st));
+        return SID_OK;
+    }
+    return spectral_forward_batch(p, i16, vp, ip, nb, st);
+}
+
+int adj_poly_batch(sid_plan* p, int method, const float* ip, float* bp, int nb, cudaStream_t st)
+{
+    const int64_t nv = vol_plane_elems(p) * p->Z, ni = vol_plane_elems(p);
+    const int fmt = spectral_fmt_adj(method);
+    if (nb == 1 || fmt < 0) {
+        for (int b = 0; b < nb; ++b) SID_TRY(adj_poly(p, method, ip + b * ni, bp + b * nv, st));
+        return SID_OK;
+    }
+    SID_TRY(spectral_adjoint_batch(p, fmt, ip, bp, nb, st));
+    for (int b = 0; b < nb; ++b) {
+        SID_TRY(weak_fix(p, ip + b * ni, bp + b * nv, st));
+        if (p->kdims[0]) SID_TRY(conv_poly(p, bp + b * nv, bp + b * nv, st));
+    }
+    return SID_OK;
+}
+
+constexpr int kVolBatch = 4;  // volumes per spectral pass
+
+extern "C" int sid_deconv_isra_batched(sid_plan* p, int method, int64_t nb, const float* const* Htf, float* const* X,
+                                       int maxIter, float lambda, void* stream)
+{
+    SID_REQUIRE(p && Htf && X, "sid_deconv_isra_batched: NULL argument");
+    SID_REQUIRE(nb >= 1 && maxIter >= 0, "sid_deconv_isra_batched: need nb >= 1 and maxIter >= 0");
+    for (int64_t b = 0; b < nb; ++b)
+        SID_REQUIRE(Htf[b] && X[b], "sid_deconv_isra_batched: volume %lld is NULL", (long long)b);
+    cudaStream_t st = as_stream(stream);
+    SID_TRY(ensure_proj_ws(p));
+    const int64_t nv = vol_plane_elems(p) * p->Z, ni = vol_plane_elems(p);
+    const int g = (int)std::min<int64_t>(nb, kVolBatch);
+    SID_TRY(p->ws[0].alloc((size_t)(g * nv) * sizeof(float)));  // iterates
+    SID_TRY(p->ws[1].alloc((size_t)(g * nv) * sizeof(float)));  // Htf
+    SID_TRY(p->ws[4].alloc((size_t)(g * nv) * sizeof(float)));  // back projections
+    SID_TRY(p->ws[5].alloc((size_t)(g * ni) * sizeof(float)));  // images
+    float* xp = p->ws[0].as<float>();
+    float* hp = p->ws[1].as<float>();
+    float* bp = p->ws[4].as<float>();
+    float* ip = p->ws[5].as<float>();
+    for (int64_t b0 = 0; b0 < nb; b0 += kVolBatch) {
+        const int n = (int)std::min<int64_t>(kVolBatch, nb - b0);
+        for (int b = 0; b < n; ++b) {
+            SID_TRY(v_to_vp(p, Htf[b0 + b], hp + b * nv, p->Z, st));
+            SID_TRY(v_to_vp(p, X[b0 + b], xp + b * nv, p->Z, st));
+        }
+        for (int it = 0; it < maxIter; ++it) {
+            SID_TRY(fwd_poly_batch(p, method, xp, ip, n, st));
+            SID_TRY(adj_poly_batch(p, method, ip, bp, n, st));
+            k_isra_update<<<2048, 256, 0, st>>>(xp, hp, bp, lambda, n * nv);
+            SID_CHECK_LAUNCH();
+        }
+        for (int b = 0; b < n; ++b) SID_TRY(vp_to_v(p, xp + b * nv, X[b0 + b], p->Z, st));
+    }
+    return SID_OK;
+}
+
+extern "C" int sid_forward_batched(sid_plan* p, int method, int64_t nb, const float* const* V, float* const* I,
+                                   void* stream)
+{
+    SID_REQUIRE(p && V && I && nb >= 1, "sid_forward_batched: NULL argument or empty batch");
+    cudaStream_t st = as_stream(stream);
+    SID_TRY(ensure_proj_ws(p));
+    const int64_t nv = vol_plane_elems(p) * p->Z, ni = vol_plane_elems(p);
+    const int g = (int)std::min<int64_t>(nb, kVolBatch);
+    SID_TRY(p->ws[0].alloc((size_t)(g * nv) * sizeof(float)));
+    SID_TRY(p->ws[5].alloc((size_t)(g * ni) * sizeof(float)));
+    for (int64_t b0 = 0; b0 < nb; b0 += kVolBatch) {
+        const int n = (int)std::min<int64_t>(kVolBatch, nb - b0);
+        for (int b = 0; b < n; ++b) SID_TRY(v_to_vp(p, V[b0 + b], p->ws[0].as<float>() + b * nv, p->Z, st));
+        SID_TRY(fwd_poly_batch(p, method, p->ws[0].as<float>(), p->ws[5].as<float>(), n, st));
+        for (int b = 0; b < n; ++b) SID_TRY(vp_to_v(p, p->ws[5].as<float>() + b * ni, I[b0 + b], 1, st));
+    }
+    return SID_OK;
+}
+
+extern "C" int sid_adjoint_batched(sid_plan* p, int method, int64_t nb, const float* const* I, float* const* V,
+                                   void* stream)
+{
+    SID_REQUIRE(p && V && I && nb >= 1, "sid_adjoint_batched: NULL argument or empty batch");
+    cudaStream_t st = as_stream(stream);
+    SID_TRY(ensure_proj_ws(p));
+    const int64_t nv = vol_plane_elems(p) * p->Z, ni = vol_plane_elems(p);
+    const int g = (int)std::min<int64_t>(nb, kVolBatch);
+    SID_TRY(p->ws[4].alloc((size_t)(g * nv) * sizeof(float)));
+    SID_TRY(p->ws[5].alloc((size_t)(g * ni) * sizeof(float)));
+    for (int64_t b0 = 0; b0 < nb; b0 += kVolBatch) {
+        const int n = (int)std::min<int64_t>(kVolBatch, nb - b0);
+        for (int b = 0; b < n; ++b) SID_TRY(v_to_vp(p, I[b0 + b], p->ws[5].as<float>() + b * ni, 1, st));
+        SID_TRY(adj_poly_batch(p, method, p->ws[5].as<float>(), p->ws[4].as<float>(), n, st));
+        for (int b = 0; b < n; ++b) SID_TRY(vp_to_v(p, p->ws[4].as<float>() + b * nv, V[b0 + b], p->Z, st));
+    }
     return SID_OK;
 }
 

@@ -183,6 +183,9 @@ int spectral_forward(sid_plan* p, bool i16, const float* vp, float* ip, cudaStre
 // storage formats of the tap spectra
 enum SpecFmt { FMT_F32 = 0, FMT_I16 = 1, FMT_F24 = 2 };
 int spectral_adjoint(sid_plan* p, int fmt, const float* ip, float* bp, cudaStream_t st);
+// nb (<= 4) polyphase volumes / images back to back
+int spectral_forward_batch(sid_plan* p, bool i16, const float* vp, float* ip, int nb, cudaStream_t st);
+int spectral_adjoint_batch(sid_plan* p, int fmt, const float* ip, float* bp, int nb, cudaStream_t st);
 int conv_poly(sid_plan* p, const float* in_vp, float* out_vp, cudaStream_t st);
 int weak_build(sid_plan* p);
 int weak_fix(sid_plan* p, const float* ip, float* bp, cudaStream_t st);

@@ -650,6 +650,141 @@ k_spec_adj(const uint4* __restrict__ khat, const uint4* __restrict__ klo, const 
     }
 }
 
+// ------------------------------------------------ several volumes at once --
+// The same contractions for NB volumes per launch (reconstruct_S.m:162-212
+// reconstructs components side by side): each tap-spectrum entry read from
+// HBM is applied to NB volume spectra, so the spectra stream once per NB
+// volumes and the contraction turns from memory- to FMA-bound.  Layouts:
+// vhat [b][k][f], ihat [b][o][f] (NB consecutive single-volume blocks).
+template <bool I16, int NB>
+__global__ void __launch_bounds__(512)
+k_spec_fwd_b(const uint4* __restrict__ khat, const float* __restrict__ rstep, const float2* __restrict__ vhat,
+             float2* __restrict__ ihat, int n_in, int64_t n_in_pad, int n_out, int nf)
+{
+    using KL = KLoad<I16>;
+    constexpr int EPL = KL::EPL;
+    constexpr int RBB = 2;  // rows per warp pass (NB x RBB complex accumulators per lane)
+    extern __shared__ float2 xv[];  // [NB][n_in_pad]
+    const int f = blockIdx.x;
+    for (int b = 0; b < NB; ++b)
+        for (int k = threadIdx.x; k < n_in_pad; k += blockDim.x)
+            xv[b * n_in_pad + k] = (k < n_in) ? vhat[((int64_t)b * n_in + k) * nf + f] : make_float2(0.f, 0.f);
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int nvec = (int)(n_in_pad / EPL);
+    const int64_t rowvec = n_in_pad / EPL;
+    for (int o0 = warp * RBB; o0 < n_out; o0 += nw * RBB) {
+        float ar[RBB][NB], ai[RBB][NB];
+        const uint4* kr[RBB];
+#pragma unroll
+        for (int r = 0; r < RBB; ++r) {
+#pragma unroll
+            for (int b = 0; b < NB; ++b) ar[r][b] = ai[r][b] = 0.f;
+            kr[r] = khat + ((int64_t)f * n_out + min(o0 + r, n_out - 1)) * rowvec;
+        }
+#pragma unroll 2
+        for (int j = lane; j < nvec; j += 32) {
+            uint4 q[RBB];
+#pragma unroll
+            for (int r = 0; r < RBB; ++r) q[r] = __ldcs(kr[r] + j);
+            float2 kk[RBB][EPL];
+#pragma unroll
+            for (int r = 0; r < RBB; ++r) KL::unpack(q[r], kk[r]);
+#pragma unroll
+            for (int b = 0; b < NB; ++b) {
+                float2 x[EPL];
+#pragma unroll
+                for (int e = 0; e < EPL; ++e) x[e] = xv[b * n_in_pad + EPL * j + e];
+#pragma unroll
+                for (int r = 0; r < RBB; ++r)
+#pragma unroll
+                    for (int e = 0; e < EPL; ++e) {
+                        ar[r][b] = fmaf(kk[r][e].x, x[e].x, ar[r][b]);
+                        ar[r][b] = fmaf(-kk[r][e].y, x[e].y, ar[r][b]);
+                        ai[r][b] = fmaf(kk[r][e].x, x[e].y, ai[r][b]);
+                        ai[r][b] = fmaf(kk[r][e].y, x[e].x, ai[r][b]);
+                    }
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < RBB; ++r)
+#pragma unroll
+            for (int b = 0; b < NB; ++b)
+#pragma unroll
+                for (int off = 16; off > 0; off >>= 1) {
+                    ar[r][b] += __shfl_xor_sync(0xffffffffu, ar[r][b], off);
+                    ai[r][b] += __shfl_xor_sync(0xffffffffu, ai[r][b], off);
+                }
+        // lane r * NB + b writes row o0 + r of volume b
+#pragma unroll
+        for (int r = 0; r < RBB; ++r)
+#pragma unroll
+            for (int b = 0; b < NB; ++b)
+                if (lane == r * NB + b && o0 + r < n_out) {
+                    const int o = o0 + r;
+                    const float st = I16 ? rstep[(int64_t)f * n_out + o] : 1.f;
+                    ihat[((int64_t)b * n_out + o) * nf + f] = make_float2(ar[r][b] * st, ai[r][b] * st);
+                }
+    }
+}
+
+template <int FMT, int NB>
+__global__ void __launch_bounds__(512)
+k_spec_adj_b(const uint4* __restrict__ khat, const uint4* __restrict__ klo, const float* __restrict__ rstep,
+             const float2* __restrict__ ihat, float2* __restrict__ bhat, int n_in, int64_t n_in_pad, int n_out, int nf)
+{
+    constexpr int V = FMT == FMT_F32 ? 2 : (FMT == FMT_I16 ? 4 : 8);
+    extern __shared__ float2 yv[];  // [NB][n_out], pre-multiplied by the row steps
+    const int f = blockIdx.x;
+    for (int i = threadIdx.x; i < NB * n_out; i += blockDim.x) {
+        const int b = i / n_out, o = i - b * n_out;
+        const float2 y = ihat[((int64_t)b * n_out + o) * nf + f];
+        const float st = FMT == FMT_I16 ? rstep[(int64_t)f * n_out + o] : 1.f;
+        yv[i] = make_float2(y.x * st, y.y * st);
+    }
+    __syncthreads();
+    const int nvec = (int)(n_in_pad / V);
+    const int64_t rowvec = FMT == FMT_F24 ? n_in_pad / 4 : n_in_pad / V;
+    const int64_t rowlo = n_in_pad / 8;
+    const uint4* base = khat + (int64_t)f * n_out * rowvec;
+    const uint4* lbase = FMT == FMT_F24 ? klo + (int64_t)f * n_out * rowlo : nullptr;
+    for (int j = threadIdx.x; j < nvec; j += blockDim.x) {
+        float ar[NB][V], ai[NB][V];
+#pragma unroll
+        for (int b = 0; b < NB; ++b)
+#pragma unroll
+            for (int e = 0; e < V; ++e) ar[b][e] = ai[b][e] = 0.f;
+        const uint4* col = base + (FMT == FMT_F24 ? 2 * j : j);
+        const uint4* lcol = FMT == FMT_F24 ? lbase + j : nullptr;
+#pragma unroll 2
+        for (int o = 0; o < n_out; ++o) {
+            float2 kk[V];
+            if constexpr (FMT == FMT_F24) {
+                unpack_f24(__ldcs(col + (int64_t)o * rowvec), __ldcs(col + (int64_t)o * rowvec + 1),
+                           __ldcs(lcol + (int64_t)o * rowlo), kk);
+            } else {
+                KLoad<FMT == FMT_I16>::unpack(__ldcs(col + (int64_t)o * rowvec), kk);
+            }
+#pragma unroll
+            for (int b = 0; b < NB; ++b) {
+                const float2 y = yv[b * n_out + o];
+#pragma unroll
+                for (int e = 0; e < V; ++e) {
+                    ar[b][e] = fmaf(kk[e].x, y.x, ar[b][e]); ar[b][e] = fmaf(kk[e].y, y.y, ar[b][e]);
+                    ai[b][e] = fmaf(kk[e].x, y.y, ai[b][e]); ai[b][e] = fmaf(-kk[e].y, y.x, ai[b][e]);
+                }
+            }
+        }
+#pragma unroll
+        for (int b = 0; b < NB; ++b)
+#pragma unroll
+            for (int e = 0; e < V; ++e) {
+                const int k = V * j + e;
+                if (k < n_in) bhat[((int64_t)b * n_in + k) * nf + f] = make_float2(ar[b][e], ai[b][e]);
+            }
+    }
+}
+
 // ------------------------------------------------------------- launchers --
 static int ensure_spec_ws(sid_plan* p)
 {
@@ -766,6 +901,93 @@ int spectral_adjoint(sid_plan* p, int fmt, const float* ip, float* bp, cudaStrea
     SID_CHECK_LAUNCH();
     SID_TRY(dft_c2r(p, p->vhat.as<float2>(), bp, n_in, st));
     return SID_OK;
+}
+
+// nb (2..4) volumes per call: vp holds nb polyphase volumes, ip nb polyphase images
+constexpr int kSpecBatchMax = 4;
+
+static int ensure_spec_ws_b(sid_plan* p, int nb)
+{
+    const int64_t n_in = p->N * p->N * p->Z, n_out = p->N * p->N;
+    SID_TRY(p->vhat.alloc((size_t)(nb * n_in * p->nf) * sizeof(float2)));
+    SID_TRY(p->ihat.alloc((size_t)(nb * n_out * p->nf) * sizeof(float2)));
+    return SID_OK;
+}
+
+template <bool I16, int NB>
+static int launch_fwd_b(sid_plan* p, int64_t n_in, int64_t n_in_pad, int64_t n_out, cudaStream_t st)
+{
+    const size_t sm = (size_t)NB * n_in_pad * sizeof(float2);
+    SID_REQUIRE(sm <= 227 * 1024, "spectral projector: %d volumes of %lld channels exceed shared memory", NB,
+                (long long)n_in);
+    SID_CUDA_TRY(cudaFuncSetAttribute(k_spec_fwd_b<I16, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    k_spec_fwd_b<I16, NB><<<(unsigned)p->nf, 512, sm, st>>>(I16 ? p->khat_i16.as<uint4>() : p->khat_f32.as<uint4>(),
+                                                           I16 ? p->rstep.as<float>() : nullptr, p->vhat.as<float2>(),
+                                                           p->ihat.as<float2>(), (int)n_in, n_in_pad, (int)n_out,
+                                                           (int)p->nf);
+    SID_CHECK_LAUNCH();
+    return SID_OK;
+}
+
+template <int FMT, int NB>
+static int launch_adj_b(sid_plan* p, int64_t n_in, int64_t n_in_pad, int64_t n_out, cudaStream_t st)
+{
+    const size_t sm = (size_t)NB * n_out * sizeof(float2);
+    const uint4* kh = FMT == FMT_I16 ? p->khat_i16.as<uint4>() : (FMT == FMT_F24 ? p->khat_f24h.as<uint4>()
+                                                                                  : p->khat_f32.as<uint4>());
+    k_spec_adj_b<FMT, NB><<<(unsigned)p->nf, 512, sm, st>>>(kh, FMT == FMT_F24 ? p->khat_f24l.as<uint4>() : nullptr,
+                                                           FMT == FMT_I16 ? p->rstep.as<float>() : nullptr,
+                                                           p->ihat.as<float2>(), p->vhat.as<float2>(), (int)n_in,
+                                                           n_in_pad, (int)n_out, (int)p->nf);
+    SID_CHECK_LAUNCH();
+    return SID_OK;
+}
+
+int spectral_forward_batch(sid_plan* p, bool i16, const float* vp, float* ip, int nb, cudaStream_t st)
+{
+    if (nb == 1) return spectral_forward(p, i16, vp, ip, st);
+    SID_REQUIRE(nb >= 2 && nb <= kSpecBatchMax, "spectral projector: batch of %d volumes outside [1, %d]", nb,
+                kSpecBatchMax);
+    SID_TRY(spec_check(p, i16 ? FMT_I16 : FMT_F32));
+    SID_TRY(ensure_spec_ws_b(p, nb));
+    SID_TRY(configure_dft(p));
+    const int64_t n_in = p->N * p->N * p->Z, n_out = p->N * p->N, n_in_pad = spec_nin_pad(p);
+    SID_TRY(dft_r2c(p, vp, p->vhat.as<float2>(), nb * n_in, st));
+    p->timer.begin(st);
+    int rc;
+    if (i16) rc = nb == 2 ? launch_fwd_b<true, 2>(p, n_in, n_in_pad, n_out, st)
+                          : (nb == 3 ? launch_fwd_b<true, 3>(p, n_in, n_in_pad, n_out, st)
+                                     : launch_fwd_b<true, 4>(p, n_in, n_in_pad, n_out, st));
+    else rc = nb == 2 ? launch_fwd_b<false, 2>(p, n_in, n_in_pad, n_out, st)
+                      : (nb == 3 ? launch_fwd_b<false, 3>(p, n_in, n_in_pad, n_out, st)
+                                 : launch_fwd_b<false, 4>(p, n_in, n_in_pad, n_out, st));
+    p->timer.finish(st);
+    SID_TRY(rc);
+    return dft_c2r(p, p->ihat.as<float2>(), ip, nb * n_out, st);
+}
+
+int spectral_adjoint_batch(sid_plan* p, int fmt, const float* ip, float* bp, int nb, cudaStream_t st)
+{
+    if (nb == 1) return spectral_adjoint(p, fmt, ip, bp, st);
+    SID_REQUIRE(nb >= 2 && nb <= kSpecBatchMax, "spectral projector: batch of %d volumes outside [1, %d]", nb,
+                kSpecBatchMax);
+    SID_TRY(spec_check(p, fmt));
+    SID_TRY(ensure_spec_ws_b(p, nb));
+    SID_TRY(configure_dft(p));
+    const int64_t n_in = p->N * p->N * p->Z, n_out = p->N * p->N, n_in_pad = spec_nin_pad(p);
+    SID_TRY(dft_r2c(p, ip, p->ihat.as<float2>(), nb * n_out, st));
+    p->timer.begin(st);
+    int rc;
+#define SID_ADJ_B(F)                                                                                        \
+    (nb == 2 ? launch_adj_b<F, 2>(p, n_in, n_in_pad, n_out, st)                                             \
+             : (nb == 3 ? launch_adj_b<F, 3>(p, n_in, n_in_pad, n_out, st) : launch_adj_b<F, 4>(p, n_in, n_in_pad, n_out, st)))
+    if (fmt == FMT_I16) rc = SID_ADJ_B(FMT_I16);
+    else if (fmt == FMT_F24) rc = SID_ADJ_B(FMT_F24);
+    else rc = SID_ADJ_B(FMT_F32);
+#undef SID_ADJ_B
+    p->timer.finish(st);
+    SID_TRY(rc);
+    return dft_c2r(p, p->vhat.as<float2>(), bp, nb * n_in, st);
 }
 
 }  // namespace sid

@@ -220,6 +220,40 @@ class Projector:
                   H.data_ptr() if H is not None else None, _stream_ptr())
         return (X, H) if history else X
 
+    def _ptr_array(self, ts):
+        return (ctypes.c_void_p * len(ts))(*[t.data_ptr() for t in ts])
+
+    def forward_batched(self, volumes, method=None):
+        """[forwardProjectGPU(H, V) for V in volumes], up to four volumes per
+        pass over the tap spectra."""
+        vs = [to_device(v) for v in volumes]
+        outs = [_fortran_tensor((self.X, self.Y), vs[0].device) for _ in vs]
+        _lib.call("sid_forward_batched", self._plan, self._method(method), len(vs),
+                  ctypes.cast(self._ptr_array(vs), ctypes.c_void_p), ctypes.cast(self._ptr_array(outs), ctypes.c_void_p),
+                  _stream_ptr())
+        return outs
+
+    def adjoint_batched(self, images, method=None):
+        """[backwardProjectGPU_new(H, I) for I in images]."""
+        ims = [to_device(i) for i in images]
+        outs = [_fortran_tensor((self.X, self.Y, self.Z), ims[0].device) for _ in ims]
+        _lib.call("sid_adjoint_batched", self._plan, self._method(method), len(ims),
+                  ctypes.cast(self._ptr_array(ims), ctypes.c_void_p), ctypes.cast(self._ptr_array(outs), ctypes.c_void_p),
+                  _stream_ptr())
+        return outs
+
+    def isra_batched(self, Htfs, Xguesses, maxIter, lam=0.0, method=None):
+        """deconvRL (mode 'basic') for several components at once: one list of
+        volumes in, one out (the inputs are not modified)."""
+        hs = [to_device(h) for h in Htfs]
+        xs = [to_device(x).clone() for x in Xguesses]
+        if len(hs) != len(xs):
+            raise ValueError("isra_batched: Htf and Xguess lists differ in length")
+        _lib.call("sid_deconv_isra_batched", self._plan, self._method(method), len(hs),
+                  ctypes.cast(self._ptr_array(hs), ctypes.c_void_p), ctypes.cast(self._ptr_array(xs), ctypes.c_void_p),
+                  int(maxIter), float(lam), _stream_ptr())
+        return xs
+
     def rl_poisson(self, y, Xguess, maxIter, method=None) -> torch.Tensor:
         """Poisson-likelihood Richardson-Lucy from the sensor image y:
         X <- X .* A'(y ./ AX) ./ A'1 (the reference's deconvRL is the ISRA form)."""
