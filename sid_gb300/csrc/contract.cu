@@ -28,7 +28,6 @@ int split16(const float* src, int64_t k, int64_t rows, int64_t lds, uint16_t* hi
             float scale, cudaStream_t st);
 int copy16_blk(const uint16_t* src, int64_t k, int64_t rows, int64_t lds, uint16_t* dst, cudaStream_t st);
 int64_t blk16_elems(int64_t k, int64_t rows);
-int absmax(const float* x, int64_t n, unsigned int* out, cudaStream_t st);
 }  // namespace sid
 
 namespace sid {
@@ -43,20 +42,6 @@ int ctx_sync(sid_ctx* c, cudaStream_t st)
         set_error("a device-side wait exceeded its budget (code %d)", flag);
         return SID_ETIMEOUT;
     }
-    return SID_OK;
-}
-
-// Largest power of two s with max|x| * s <= 2^14 (FP16 operand scaling).
-static int pow2_scale(sid_ctx* c, const float* x, int64_t n, float* scale, cudaStream_t st)
-{
-    SID_TRY(c->scal.alloc(64));
-    SID_TRY(absmax(x, n, c->scal.as<unsigned int>(), st));
-    unsigned int bits = 0;
-    SID_CUDA_TRY(cudaMemcpyAsync(&bits, c->scal.p, sizeof(bits), cudaMemcpyDeviceToHost, st));
-    SID_CUDA_TRY(cudaStreamSynchronize(st));
-    float mx;
-    std::memcpy(&mx, &bits, sizeof(mx));
-    *scale = (mx > 0.f) ? std::ldexp(1.0f, (int)std::floor(std::log2(16384.0 / (double)mx))) : 1.f;
     return SID_OK;
 }
 
@@ -81,18 +66,23 @@ int contract(sid_ctx* c, const float* A, const void* B, bool b_f16, int64_t m, i
     const bool split = prec == SID_PREC_SPLIT;
     const size_t abytes = (size_t)blk16_elems(k, m) * 2, bbytes = (size_t)blk16_elems(k, n) * 2;
     if (b_f16) {
-        // FP16 right operand used unsplit; A split into FP16 hi/lo with a power-of-two scale
-        float sa = 1.f;
-        SID_TRY(pow2_scale(c, A, m * lda, &sa, st));  // over the whole stored matrix
+        // FP16 right operand used unsplit; A split into FP16 hi/lo with a
+        // power-of-two scale sa found and applied on the device (alpha / sa
+        // goes to the GEMM epilogue), so nothing waits on the host
+        float* sw = c->scales.as<float>();
+        unsigned int* amax = reinterpret_cast<unsigned int*>(sw + 12);
+        SID_TRY(pow2_scale_dev(A, m * lda, amax, sw + 13, st));  // over the whole stored matrix
+        SID_TRY(scale_ratio_dev(sw + 13, nullptr, 1.f, sw + 14, st));
         SID_TRY(c->a_hi.alloc(abytes));
         if (split) SID_TRY(c->a_lo.alloc(abytes));
-        SID_TRY(split16(A, k, m, lda, c->a_hi.as<uint16_t>(), split ? c->a_lo.as<uint16_t>() : nullptr, false, sa, st));
+        SID_TRY(split16_ds(A, k, m, lda, c->a_hi.as<uint16_t>(), split ? c->a_lo.as<uint16_t>() : nullptr, false, 1.f,
+                           sw + 13, st));
         SID_TRY(c->b_hi.alloc(bbytes));
         SID_TRY(copy16_blk(static_cast<const uint16_t*>(B), k, n, ldb, c->b_hi.as<uint16_t>(), st));
         const void* As[2] = {c->a_hi.p, c->a_lo.p};
         const void* Bs[2] = {c->b_hi.p, c->b_hi.p};
-        return gemm_tn(As, Bs, split ? 2 : 1, m, n, k, false, C, ldc, alpha / sa, beta, bn, splitk, c->ws.as<float>(),
-                       (int64_t)(c->ws.bytes / sizeof(float)), err, st);
+        return gemm_tn_ds(As, Bs, split ? 2 : 1, m, n, k, false, C, ldc, alpha, sw + 14, beta, bn, splitk,
+                          c->ws.as<float>(), (int64_t)(c->ws.bytes / sizeof(float)), err, st);
     }
     // FP32 x FP32: BF16 hi/lo splits of both (no scaling needed: BF16 keeps the FP32 exponent range)
     SID_TRY(c->a_hi.alloc(abytes));
@@ -125,7 +115,11 @@ extern "C" int sid_ctx_create(sid_ctx** out)
     SID_REQUIRE(out, "sid_ctx_create: NULL output");
     sid_ctx* c = new sid_ctx();
     cudaGetDevice(&c->device);
-    if (c->errflag.alloc(sizeof(int)) != SID_OK || cudaMemset(c->errflag.p, 0, sizeof(int)) != cudaSuccess) {
+    if (c->errflag.alloc(sizeof(int)) != SID_OK || cudaMemset(c->errflag.p, 0, sizeof(int)) != cudaSuccess ||
+        c->scales.alloc(kScaleWords * 4) != SID_OK ||
+        cudaMemset(c->scales.p, 0, kScaleWords * 4) != cudaSuccess) {
+        c->errflag.release();
+        c->scales.release();
         delete c;
         *out = nullptr;
         return SID_ENOMEM;
@@ -137,7 +131,7 @@ extern "C" int sid_ctx_create(sid_ctx** out)
 extern "C" int sid_ctx_destroy(sid_ctx* c)
 {
     if (!c) return SID_OK;
-    DBuf* b[] = {&c->a_hi, &c->a_lo, &c->b_hi, &c->b_lo, &c->ws, &c->scal, &c->errflag};
+    DBuf* b[] = {&c->a_hi, &c->a_lo, &c->b_hi, &c->b_lo, &c->ws, &c->scal, &c->errflag, &c->scales};
     for (DBuf* x : b) x->release();
     for (DBuf& x : c->nn) x.release();
     for (DBuf& x : c->mf) x.release();

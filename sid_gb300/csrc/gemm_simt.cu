@@ -158,8 +158,10 @@ int64_t sgemm_ws_elems(int64_t m, int64_t n, int64_t k)
 // source allows them, 8-byte writes; a warp covers two 128-byte block rows.
 template <bool BF16>
 __global__ void k_split16_blk(const float* __restrict__ src, int64_t k, int64_t rows, int64_t lds,
-                              uint16_t* __restrict__ hi, uint16_t* __restrict__ lo, float scale, int vec4)
+                              uint16_t* __restrict__ hi, uint16_t* __restrict__ lo, float scale, int vec4,
+                              const float* __restrict__ dscale)
 {
+    if (dscale) scale = *dscale;
     const int64_t nkb = (k + 63) / 64;
     const int64_t total = nkb * rows * 16;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
@@ -231,8 +233,10 @@ __global__ void k_copy16_blk(const uint16_t* __restrict__ src, int64_t k, int64_
 // source copied (hi only).
 template <int MODE>
 __global__ void __launch_bounds__(256) k_blk16_t(const void* __restrict__ src_v, int64_t rows, int64_t k, int64_t ldr,
-                                                 uint16_t* __restrict__ hi, uint16_t* __restrict__ lo, float scale)
+                                                 uint16_t* __restrict__ hi, uint16_t* __restrict__ lo, float scale,
+                                                 const float* __restrict__ dscale)
 {
+    if (dscale) scale = *dscale;
     __shared__ float tile[64][65];
     __shared__ uint16_t tile16[64][66];
     const int64_t nrt = (rows + 63) / 64, nkt = (k + 63) / 64;
@@ -296,17 +300,25 @@ __global__ void k_absmax(const float* __restrict__ x, int64_t n, unsigned int* _
 
 int64_t blk16_elems(int64_t k, int64_t rows) { return cdiv(k, 64) * 64 * rows; }
 
-// K-blocked 16-bit split of a k x rows FP32 matrix (see k_split16_blk)
-int split16(const float* src, int64_t k, int64_t rows, int64_t lds, uint16_t* hi, uint16_t* lo, bool bf16,
-            float scale, cudaStream_t st)
+// K-blocked 16-bit split of a k x rows FP32 matrix (see k_split16_blk).  An
+// FP16 split multiplies by dscale[0] (device memory) when dscale is given,
+// else by scale.
+int split16_ds(const float* src, int64_t k, int64_t rows, int64_t lds, uint16_t* hi, uint16_t* lo, bool bf16,
+               float scale, const float* dscale, cudaStream_t st)
 {
     const int vec4 = ((lds & 3) == 0 && ((uintptr_t)src & 15) == 0) ? 1 : 0;
     const int64_t total = cdiv(k, 64) * rows * 16;
     const unsigned grid = (unsigned)std::min<int64_t>(cdiv(total, 256), 152 * 32);
-    if (bf16) k_split16_blk<true><<<grid, 256, 0, st>>>(src, k, rows, lds, hi, lo, scale, vec4);
-    else k_split16_blk<false><<<grid, 256, 0, st>>>(src, k, rows, lds, hi, lo, scale, vec4);
+    if (bf16) k_split16_blk<true><<<grid, 256, 0, st>>>(src, k, rows, lds, hi, lo, scale, vec4, nullptr);
+    else k_split16_blk<false><<<grid, 256, 0, st>>>(src, k, rows, lds, hi, lo, scale, vec4, dscale);
     SID_CHECK_LAUNCH();
     return SID_OK;
+}
+
+int split16(const float* src, int64_t k, int64_t rows, int64_t lds, uint16_t* hi, uint16_t* lo, bool bf16,
+            float scale, cudaStream_t st)
+{
+    return split16_ds(src, k, rows, lds, hi, lo, bf16, scale, nullptr, st);
 }
 
 int copy16_blk(const uint16_t* src, int64_t k, int64_t rows, int64_t lds, uint16_t* dst, cudaStream_t st)
@@ -322,22 +334,28 @@ int copy16_blk(const uint16_t* src, int64_t k, int64_t rows, int64_t lds, uint16
 // K-blocked 16-bit operand (reduction index k) of a rows x k matrix stored
 // row-contiguous (src[r + ldr*kk]): FP32 split into BF16 hi/lo (bf16) or FP16
 // hi/lo of src*scale, or a 16-bit source copied (src16).
-int split16_t(const float* src, int64_t rows, int64_t k, int64_t ldr, uint16_t* hi, uint16_t* lo, bool bf16,
-              float scale, cudaStream_t st)
+int split16_t_ds(const float* src, int64_t rows, int64_t k, int64_t ldr, uint16_t* hi, uint16_t* lo, bool bf16,
+                 float scale, const float* dscale, cudaStream_t st)
 {
     const int64_t tiles = cdiv(rows, 64) * cdiv(k, 64);
     const unsigned grid = (unsigned)std::min<int64_t>(tiles, 152 * 8);
-    if (bf16) k_blk16_t<0><<<grid, 256, 0, st>>>(src, rows, k, ldr, hi, lo, 1.f);
-    else k_blk16_t<1><<<grid, 256, 0, st>>>(src, rows, k, ldr, hi, lo, scale);
+    if (bf16) k_blk16_t<0><<<grid, 256, 0, st>>>(src, rows, k, ldr, hi, lo, 1.f, nullptr);
+    else k_blk16_t<1><<<grid, 256, 0, st>>>(src, rows, k, ldr, hi, lo, scale, dscale);
     SID_CHECK_LAUNCH();
     return SID_OK;
+}
+
+int split16_t(const float* src, int64_t rows, int64_t k, int64_t ldr, uint16_t* hi, uint16_t* lo, bool bf16,
+              float scale, cudaStream_t st)
+{
+    return split16_t_ds(src, rows, k, ldr, hi, lo, bf16, scale, nullptr, st);
 }
 
 int copy16_t(const uint16_t* src, int64_t rows, int64_t k, int64_t ldr, uint16_t* dst, cudaStream_t st)
 {
     const int64_t tiles = cdiv(rows, 64) * cdiv(k, 64);
     const unsigned grid = (unsigned)std::min<int64_t>(tiles, 152 * 8);
-    k_blk16_t<2><<<grid, 256, 0, st>>>(src, rows, k, ldr, dst, nullptr, 1.f);
+    k_blk16_t<2><<<grid, 256, 0, st>>>(src, rows, k, ldr, dst, nullptr, 1.f, nullptr);
     SID_CHECK_LAUNCH();
     return SID_OK;
 }
@@ -346,6 +364,37 @@ int absmax(const float* x, int64_t n, unsigned int* out, cudaStream_t st)
 {
     SID_CUDA_TRY(cudaMemsetAsync(out, 0, sizeof(unsigned int), st));
     k_absmax<<<1024, 256, 0, st>>>(x, n, out);
+    SID_CHECK_LAUNCH();
+    return SID_OK;
+}
+
+__global__ void k_amax_pow2(const unsigned int* __restrict__ amax, float* __restrict__ scale)
+{
+    scale[0] = pow2_for(__uint_as_float(amax[0]));
+}
+
+__global__ void k_scale_ratio(const float* __restrict__ a, const float* __restrict__ b, float num,
+                              float* __restrict__ out)
+{
+    out[0] = num / (a[0] * (b ? b[0] : 1.f));
+}
+
+// Device-resident power-of-two scale of x (n floats): dscale[0] brings max |x|
+// into [2^13, 2^14) (1 for an all-zero or non-finite x); amax is scratch for
+// one word.  Nothing is read back, so the stream never waits on the host.
+int pow2_scale_dev(const float* x, int64_t n, unsigned int* amax, float* dscale, cudaStream_t st)
+{
+    SID_TRY(absmax(x, n, amax, st));
+    k_amax_pow2<<<1, 1, 0, st>>>(amax, dscale);
+    SID_CHECK_LAUNCH();
+    return SID_OK;
+}
+
+// out[0] = num / (a[0] * b[0]) (b may be null), on the device: the alpha that
+// undoes two power-of-two operand scales (exact).
+int scale_ratio_dev(const float* a, const float* b, float num, float* out, cudaStream_t st)
+{
+    k_scale_ratio<<<1, 1, 0, st>>>(a, b, num, out);
     SID_CHECK_LAUNCH();
     return SID_OK;
 }

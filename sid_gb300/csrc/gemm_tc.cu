@@ -141,7 +141,8 @@ constexpr int GEMM_THREADS = (GEMM_DRAIN_WARPS + 2) * 32;
 template <int BN, int STAGES>
 __global__ void __launch_bounds__(GEMM_THREADS, 1)
 k_gemm_tc(const __grid_constant__ GemmMaps maps, int npass, int m, int n, int nkb, int kb_per, int bf16,
-          float* __restrict__ out, int64_t ldc, int64_t split_stride, float alpha, int* __restrict__ err, int sym)
+          float* __restrict__ out, int64_t ldc, int64_t split_stride, float alpha, int* __restrict__ err, int sym,
+          const float* __restrict__ dalpha)
 {
     // symmetric product (A'A): tiles wholly below the diagonal are mirrored afterwards
     if (sym && (int)blockIdx.x * GEMM_BM >= (int)blockIdx.y * BN + BN) return;
@@ -277,10 +278,11 @@ k_gemm_tc(const __grid_constant__ GemmMaps maps, int npass, int m, int n, int nk
             mbar_arrive(&tempty[b]);
         }
         if (ok && row < m) {
+            const float al = dalpha ? alpha * *dalpha : alpha;
 #pragma unroll
             for (int j = 0; j < HALF; ++j) {
                 const int col = n0 + ch0 + j;
-                if (col < n) dst[(int64_t)row + ldc * col] = accr[j] * alpha;
+                if (col < n) dst[(int64_t)row + ldc * col] = accr[j] * al;
             }
         }
     }
@@ -295,8 +297,10 @@ k_gemm_tc(const __grid_constant__ GemmMaps maps, int npass, int m, int n, int nk
 
 // Sum split-K partials: C = alpha * sum_z P[z] + beta * C (beta == 0 ignores C).
 __global__ void k_splitk_reduce(const float* __restrict__ part, int nsplit, int64_t split_stride, int m, int n,
-                                int64_t ldp, float* __restrict__ C, int64_t ldc, float alpha, float beta)
+                                int64_t ldp, float* __restrict__ C, int64_t ldc, float alpha, float beta,
+                                const float* __restrict__ dalpha)
 {
+    if (dalpha) alpha *= *dalpha;
     const int64_t total = (int64_t)m * n;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
         const int r = (int)(i % m);
@@ -345,7 +349,8 @@ static int make_map(CUtensorMap* map, const void* base, int64_t rows, int64_t nk
 
 template <int BN, int STAGES>
 static int launch_gemm(const GemmMaps& maps, int npass, int m, int n, int nkb, int splitk, bool bf16, float* out,
-                       int64_t ldc, int64_t split_stride, float alpha, int* err, bool sym, cudaStream_t st)
+                       int64_t ldc, int64_t split_stride, float alpha, const float* dalpha, int* err, bool sym,
+                       cudaStream_t st)
 {
     using SM = GemmSmem<BN, STAGES>;
     static bool configured = false;
@@ -356,7 +361,7 @@ static int launch_gemm(const GemmMaps& maps, int npass, int m, int n, int nkb, i
     const int kb_per = (int)cdiv(nkb, splitk);
     dim3 grid((unsigned)cdiv(m, GEMM_BM), (unsigned)cdiv(n, BN), (unsigned)splitk);
     k_gemm_tc<BN, STAGES><<<grid, GEMM_THREADS, SM::TOTAL, st>>>(maps, npass, m, n, nkb, kb_per, bf16 ? 1 : 0, out, ldc,
-                                                         split_stride, alpha, err, sym ? 1 : 0);
+                                                         split_stride, alpha, err, sym ? 1 : 0, dalpha);
     SID_CHECK_LAUNCH();
     return SID_OK;
 }
@@ -423,8 +428,8 @@ __global__ void k_mirror_lower(float* __restrict__ C, int m, int64_t ldc)
 // ws: >= splitk * m * n floats when splitk > 1 or beta != 0 (alpha alone is
 // applied as the tiles are stored).
 static int gemm_tn_impl(const void* const* A, const void* const* B, int npass, int64_t m, int64_t n, int64_t k,
-                        bool bf16, float* C, int64_t ldc, float alpha, float beta, int bn, int splitk, float* ws,
-                        int64_t ws_elems, int* err, bool sym, cudaStream_t st)
+                        bool bf16, float* C, int64_t ldc, float alpha, const float* dalpha, float beta, int bn,
+                        int splitk, float* ws, int64_t ws_elems, int* err, bool sym, cudaStream_t st)
 {
     SID_REQUIRE(npass >= 1 && npass <= GEMM_MAXPASS, "gemm: npass %d outside [1,3]", npass);
     SID_REQUIRE(m > 0 && n > 0 && k > 0, "gemm: empty problem");
@@ -449,15 +454,15 @@ static int gemm_tn_impl(const void* const* A, const void* const* B, int npass, i
     }
     int rc;
     switch (bn) {
-    case 256: rc = launch_gemm<256, 4>(maps, npass, (int)m, (int)n, nkb, splitk, bf16, out, ldo, sstride, direct ? alpha : 1.f, err, sym, st); break;
-    case 192: rc = launch_gemm<192, 5>(maps, npass, (int)m, (int)n, nkb, splitk, bf16, out, ldo, sstride, direct ? alpha : 1.f, err, sym, st); break;
-    case 128: rc = launch_gemm<128, 6>(maps, npass, (int)m, (int)n, nkb, splitk, bf16, out, ldo, sstride, direct ? alpha : 1.f, err, sym, st); break;
-    case 64: rc = launch_gemm<64, 8>(maps, npass, (int)m, (int)n, nkb, splitk, bf16, out, ldo, sstride, direct ? alpha : 1.f, err, sym, st); break;
+    case 256: rc = launch_gemm<256, 4>(maps, npass, (int)m, (int)n, nkb, splitk, bf16, out, ldo, sstride, direct ? alpha : 1.f, direct ? dalpha : nullptr, err, sym, st); break;
+    case 192: rc = launch_gemm<192, 5>(maps, npass, (int)m, (int)n, nkb, splitk, bf16, out, ldo, sstride, direct ? alpha : 1.f, direct ? dalpha : nullptr, err, sym, st); break;
+    case 128: rc = launch_gemm<128, 6>(maps, npass, (int)m, (int)n, nkb, splitk, bf16, out, ldo, sstride, direct ? alpha : 1.f, direct ? dalpha : nullptr, err, sym, st); break;
+    case 64: rc = launch_gemm<64, 8>(maps, npass, (int)m, (int)n, nkb, splitk, bf16, out, ldo, sstride, direct ? alpha : 1.f, direct ? dalpha : nullptr, err, sym, st); break;
     default: set_error("gemm: unsupported tile width %d", bn); return SID_EINVAL;
     }
     SID_TRY(rc);
     if (!direct) {
-        k_splitk_reduce<<<1024, 256, 0, st>>>(ws, splitk, sstride, (int)m, (int)n, m, C, ldc, alpha, beta);
+        k_splitk_reduce<<<1024, 256, 0, st>>>(ws, splitk, sstride, (int)m, (int)n, m, C, ldc, alpha, beta, dalpha);
         SID_CHECK_LAUNCH();
     }
     if (sym) {
@@ -471,7 +476,16 @@ int gemm_tn(const void* const* A, const void* const* B, int npass, int64_t m, in
             float* C, int64_t ldc, float alpha, float beta, int bn, int splitk, float* ws, int64_t ws_elems, int* err,
             cudaStream_t st)
 {
-    return gemm_tn_impl(A, B, npass, m, n, k, bf16, C, ldc, alpha, beta, bn, splitk, ws, ws_elems, err, false, st);
+    return gemm_tn_impl(A, B, npass, m, n, k, bf16, C, ldc, alpha, nullptr, beta, bn, splitk, ws, ws_elems, err, false,
+                        st);
+}
+
+int gemm_tn_ds(const void* const* A, const void* const* B, int npass, int64_t m, int64_t n, int64_t k, bool bf16,
+               float* C, int64_t ldc, float alpha, const float* dalpha, float beta, int bn, int splitk, float* ws,
+               int64_t ws_elems, int* err, cudaStream_t st)
+{
+    return gemm_tn_impl(A, B, npass, m, n, k, bf16, C, ldc, alpha, dalpha, beta, bn, splitk, ws, ws_elems, err, false,
+                        st);
 }
 
 // Symmetric product C = sum_p A_p^T B_p with A_p^T B_p + A_q^T B_q symmetric
@@ -481,7 +495,8 @@ int gemm_tn(const void* const* A, const void* const* B, int npass, int64_t m, in
 int gemm_tn_sym(const void* const* A, const void* const* B, int npass, int64_t m, int64_t k, bool bf16, float* C,
                 int64_t ldc, float alpha, int bn, int splitk, float* ws, int64_t ws_elems, int* err, cudaStream_t st)
 {
-    return gemm_tn_impl(A, B, npass, m, m, k, bf16, C, ldc, alpha, 0.f, bn, splitk, ws, ws_elems, err, true, st);
+    return gemm_tn_impl(A, B, npass, m, m, k, bf16, C, ldc, alpha, nullptr, 0.f, bn, splitk, ws, ws_elems, err, true,
+                        st);
 }
 
 }  // namespace sid

@@ -10,9 +10,10 @@
 // R-deep reduction) except at FP32 precision, where they and the frame- and
 // rank-long products (R x R, R x F) run on the FP32 SIMT GEMMs.  The line
 // search's reductions over R x F accumulate in FP64; those over the P x R
-// factors as FP32 two-sum pairs (FP64-grade).  The step sizes stay in device
-// memory; the split precision's power-of-two operand scales are read back to
-// the host once per product.
+// factors as FP32 two-sum pairs (FP64-grade).  The step sizes and the split
+// precision's power-of-two operand scales stay in device memory: neither step
+// makes its stream wait on the host, so both can be captured in a CUDA graph
+// once their workspaces have been sized by an ordinary call.
 #include <cmath>
 #include <cstring>
 
@@ -685,24 +686,12 @@ namespace sid {
 // C (P x n) = X W.  X is brought once into the K-blocked 16-bit layout of the
 // tcgen05 GEMM by a transposing tile kernel.  Split precision: an FP16 movie
 // as it is, FP32 factors as FP16 hi/lo of X s (22 significant bits; a
-// power-of-two s brings max |X| to 2^14), W likewise, and the three products
-// hi*hi + hi*lo + lo*hi.  (BF16 hi/lo keeps 16 bits, which the cancellation in
-// S_update's use_std gradient amplifies past FP32-level agreement.)  BF16
-// precision: one BF16 pass.
-// largest power of two s with max |x| s <= 2^14 (1 for an all-zero x)
-int pow2_scale(sid_ctx* c, const float* x, int64_t n, float* scale, cudaStream_t st)
-{
-    SID_TRY(c->scal.alloc(64));
-    SID_TRY(absmax(x, n, c->scal.as<unsigned int>(), st));
-    unsigned int bits = 0;
-    SID_CUDA_TRY(cudaMemcpyAsync(&bits, c->scal.p, sizeof(bits), cudaMemcpyDeviceToHost, st));
-    SID_CUDA_TRY(cudaStreamSynchronize(st));
-    float mx;
-    std::memcpy(&mx, &bits, sizeof(mx));
-    *scale = (mx > 0.f) ? std::ldexp(1.0f, (int)std::floor(std::log2(16384.0 / (double)mx))) : 1.f;
-    return SID_OK;
-}
-
+// power-of-two s brings max |X| into [2^13, 2^14)), W likewise, and the three
+// products hi*hi + hi*lo + lo*hi.  (BF16 hi/lo keeps 16 bits, which the
+// cancellation in S_update's use_std gradient amplifies past FP32-level
+// agreement.)  BF16 precision: one BF16 pass.  The scales are found, applied
+// and undone on the device (the context's scale words), so these products
+// never make the stream wait on the host.
 int pix_operand(sid_ctx* c, int slot, const void* X, bool x_f16, int64_t P, int64_t k, int prec, PixOperand* op,
                 cudaStream_t st)
 {
@@ -711,20 +700,20 @@ int pix_operand(sid_ctx* c, int slot, const void* X, bool x_f16, int64_t P, int6
     SID_TRY(b[0].alloc(bytes));
     if (x_f16) {
         SID_TRY(copy16_t(static_cast<const uint16_t*>(X), P, k, P, b[0].as<uint16_t>(), st));
-        *op = {b[0].p, nullptr, true, 1.f};
+        *op = {b[0].p, nullptr, true, nullptr};
         return SID_OK;
     }
     const float* xf = static_cast<const float*>(X);
     if (prec != SID_PREC_SPLIT) {
         SID_TRY(split16_t(xf, P, k, P, b[0].as<uint16_t>(), nullptr, true, 1.f, st));
-        *op = {b[0].p, nullptr, false, 1.f};
+        *op = {b[0].p, nullptr, false, nullptr};
         return SID_OK;
     }
-    float sx = 1.f;
-    SID_TRY(pow2_scale(c, xf, P * k, &sx, st));
+    float* sw = c->scales.as<float>() + 4 * slot;
+    SID_TRY(pow2_scale_dev(xf, P * k, reinterpret_cast<unsigned int*>(sw), sw + 1, st));
     SID_TRY(b[1].alloc(bytes));
-    SID_TRY(split16_t(xf, P, k, P, b[0].as<uint16_t>(), b[1].as<uint16_t>(), false, sx, st));
-    *op = {b[0].p, b[1].p, true, sx};
+    SID_TRY(split16_t_ds(xf, P, k, P, b[0].as<uint16_t>(), b[1].as<uint16_t>(), false, 1.f, sw + 1, st));
+    *op = {b[0].p, b[1].p, true, sw + 1};
     return SID_OK;
 }
 
@@ -740,7 +729,7 @@ int gemm_pix(sid_ctx* c, const PixOperand& x, int64_t P, int64_t k, const float*
     uint16_t* wl = split ? c->pix[5].as<uint16_t>() : nullptr;
     int bn = 0, sk = 0;
     gemm_autotune((int)P, (int)n, (int)cdiv(k, 64), &bn, &sk);
-    float alpha = 1.f;
+    const float* dalpha = nullptr;
     const void *As[3], *Bs[3];
     int npass = 1;
     As[0] = As[1] = x.hi;
@@ -748,19 +737,21 @@ int gemm_pix(sid_ctx* c, const PixOperand& x, int64_t P, int64_t k, const float*
     Bs[0] = Bs[2] = wh;
     Bs[1] = wl;
     if (x.f16) {
-        float sw = 1.f;
-        SID_TRY(pow2_scale(c, W, ldw * (n - 1) + k, &sw, st));
-        SID_TRY(split16(W, k, n, ldw, wh, wl, false, sw, st));
+        // W s_w in FP16 hi/lo; alpha = 1 / (s_x s_w) in the epilogue
+        float* sw = c->scales.as<float>() + 8;
+        SID_TRY(pow2_scale_dev(W, ldw * (n - 1) + k, reinterpret_cast<unsigned int*>(sw), sw + 1, st));
+        SID_TRY(split16_ds(W, k, n, ldw, wh, wl, false, 1.f, sw + 1, st));
+        SID_TRY(scale_ratio_dev(sw + 1, x.dscale, 1.f, sw + 2, st));
         npass = !split ? 1 : (x.lo ? 3 : 2);
-        alpha = 1.f / (x.scale * sw);
+        dalpha = sw + 2;
     } else {
         SID_TRY(split16(W, k, n, ldw, wh, nullptr, true, 1.f, st));
     }
     // a split-K epilogue goes through a P x n workspace (the scale is applied as the tiles are stored)
     const int64_t ws_elems = sk > 1 ? (int64_t)sk * P * n : 1;
     SID_TRY(c->ws.alloc((size_t)ws_elems * sizeof(float)));
-    return gemm_tn(As, Bs, npass, P, n, k, !x.f16, C, P, alpha, 0.f, bn, sk, c->ws.as<float>(),
-                   (int64_t)(c->ws.bytes / sizeof(float)), c->errflag.as<int>(), st);
+    return gemm_tn_ds(As, Bs, npass, P, n, k, !x.f16, C, P, 1.f, dalpha, 0.f, bn, sk, c->ws.as<float>(),
+                      (int64_t)(c->ws.bytes / sizeof(float)), c->errflag.as<int>(), st);
 }
 
 }  // namespace sid

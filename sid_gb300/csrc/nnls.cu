@@ -131,16 +131,9 @@ __device__ __forceinline__ void put_operand_f16(const ColBufs& b, int j, int k, 
     b.vlo[i] = __half_as_ushort(__float2half_rn(v - __half2float(h)));
 }
 
-// Power of two 2^e with amax * 2^e in [2^13, 2^14) (1 for amax == 0): FP16
-// hi/lo of the scaled values then keep 22 significant bits of each entry
-// relative to its column's largest, in FP16's normal range.
-__device__ __forceinline__ float pow2_for(float amax)
-{
-    if (!(amax > 0.f) || !isfinite(amax)) return 1.f;
-    int ex;
-    frexpf(amax, &ex);  // amax in [2^(ex-1), 2^ex)
-    return ldexpf(1.f, max(-126, min(126, 14 - ex)));
-}
+// (pow2_for, sid_internal.cuh: FP16 hi/lo of values scaled into [2^13, 2^14)
+// keep 22 significant bits of each entry relative to its column's largest, in
+// FP16's normal range.)
 
 __global__ void k_iter_inc(NnlsCounters* c) { c->iter += 1; }
 

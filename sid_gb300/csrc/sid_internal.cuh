@@ -57,6 +57,28 @@ inline int64_t cdiv(int64_t a, int64_t b) { return (a + b - 1) / b; }
 // Streaming multiprocessors of the current device (cudaDevAttrMultiProcessorCount,
 // looked up once per device ordinal; 152 on GB300).
 int sm_count();
+// The power of two that brings a largest magnitude amax into [2^13, 2^14)
+// (1 for a zero or non-finite amax): the scale of an FP16 hi/lo split.
+__device__ __forceinline__ float pow2_for(float amax)
+{
+    if (!(amax > 0.f) || !isfinite(amax)) return 1.f;
+    int ex;
+    frexpf(amax, &ex);  // amax in [2^(ex-1), 2^ex)
+    return ldexpf(1.f, max(-126, min(126, 14 - ex)));
+}
+
+// Device-resident operand scales (gemm_simt.cu): pow2_scale_dev writes
+// pow2_for(max |x|) to dscale[0]; scale_ratio_dev writes num / (a[0] b[0]).
+int pow2_scale_dev(const float* x, int64_t n, unsigned int* amax, float* dscale, cudaStream_t st);
+int scale_ratio_dev(const float* a, const float* b, float num, float* out, cudaStream_t st);
+int split16_ds(const float* src, int64_t k, int64_t rows, int64_t lds, uint16_t* hi, uint16_t* lo, bool bf16,
+               float scale, const float* dscale, cudaStream_t st);
+int split16_t_ds(const float* src, int64_t rows, int64_t k, int64_t ldr, uint16_t* hi, uint16_t* lo, bool bf16,
+                 float scale, const float* dscale, cudaStream_t st);
+// tensor-core GEMM (gemm_tc.cu) whose alpha is multiplied by dalpha[0] (device memory) when dalpha is given
+int gemm_tn_ds(const void* const* A, const void* const* B, int npass, int64_t m, int64_t n, int64_t k, bool bf16,
+               float* C, int64_t ldc, float alpha, const float* dalpha, float beta, int bn, int splitk, float* ws,
+               int64_t ws_elems, int* err, cudaStream_t st);
 inline int64_t floordiv(int64_t a, int64_t b) { return (a >= 0) ? a / b : -((-a + b - 1) / b); }
 inline int64_t ceildiv_signed(int64_t a, int64_t b) { return -floordiv(-a, b); }
 
@@ -122,9 +144,11 @@ struct KTimer {
 struct PixOperand {
     const void* hi;
     const void* lo;
-    bool f16;     // FP16 operands (else BF16)
-    float scale;  // X was multiplied by this power of two
+    bool f16;             // FP16 operands (else BF16)
+    const float* dscale;  // X was multiplied by the power of two dscale[0] (device memory; null: 1)
 };
+
+constexpr int kScaleWords = 16;
 
 // Lenslet-tap geometry shared by the direct and spectral projectors.
 struct TapGeom {
@@ -199,6 +223,12 @@ inline int64_t vol_plane_elems(const sid_plan* p) { return p->N * p->N * p->Lx *
 struct sid_ctx {
     int device;
     sid::DBuf a_hi, a_lo, b_hi, b_lo, ws, scal, errflag;
+    // Power-of-two operand scales that stay on the device (kScaleWords words,
+    // allocated with the context so its address never changes): words 4s and
+    // 4s+1 hold the absmax bits and scale of pixel-operand slot s (s = 0, 1),
+    // 8..10 the right operand's absmax, scale and the product's alpha, 12..14
+    // the same for the FP16-movie contraction.
+    sid::DBuf scales;
     sid::DBuf nn[16];  // NNLS iteration state
     sid::DBuf mf[8];   // NMF step workspaces (T_update / S_update)
     sid::DBuf bg[6];   // movie scans (rank-1 background, standard-deviation image)
