@@ -43,6 +43,11 @@ enum {
                                      exponent, 15-bit mantissa: 16 significant bits),
                                      FP32 arithmetic: the back projection of
                                      SID_METHOD_SPECTRAL_MIXED */
+#define SID_PLAN_SPECTRAL_TC  0x10 /* with SPECTRAL_F24: a transposed copy of the 24-bit
+                                     spectra, so that the batched calls
+                                     (sid_*_batched) of SID_METHOD_SPECTRAL_MIXED
+                                     contract up to 32 volumes per pass on the tensor
+                                     cores, forward and back with the 24-bit spectra */
 
 /* Projection methods. */
 #define SID_METHOD_DIRECT       0
@@ -78,6 +83,10 @@ int sid_version(void);
 int sid_plan_create(const float* H, int64_t M, int64_t Nnum, int64_t Z,
                     const int32_t* CAindex, int64_t X, int64_t Y, int flags,
                     sid_plan** plan);
+/* Frees the plan's solver and projection workspaces (they are allocated again
+ * on demand), keeping the operator data (taps, spectra, weak-voxel lists).
+ * No reference counterpart: the MATLAB functions allocate per call. */
+int sid_plan_release_workspaces(sid_plan* plan);
 int sid_plan_destroy(sid_plan* plan);
 /* info[0..13] = M, Nnum, Z, X, Y, Lx, Ly, D (taps per axis), L (DFT length),
  * device bytes held, flags, adjoint-taps-separate, weakly observed voxels (column
@@ -147,9 +156,13 @@ int sid_deconv_isra_ex(sid_plan* plan, int method, const float* Htf, float* X, i
 /* Several volumes at once (reconstruct_S.m:162-212 reconstructs components
  * side by side): nb volumes / images given as host arrays of device pointers
  * (each X x Y x Z or X x Y single).  The spectral forms contract up to four
- * volumes per pass over the tap spectra, so the spectra stream once per four
- * volumes; the direct form runs volume by volume.  Results equal nb single
- * calls up to FP32 rounding.
+ * volumes per pass over the tap spectra on the FP32 pipes, so the spectra
+ * stream once per four volumes, and the results equal nb single calls up to
+ * FP32 rounding; on a plan built with SID_PLAN_SPECTRAL_TC the mixed form
+ * contracts up to 32 volumes per pass on the tensor cores with the 24-bit
+ * spectra both ways (BF16 operand splits that carry them exactly, FP32
+ * accumulation), within the mixed form's accuracy of the FP64 projections.
+ * The direct form runs volume by volume.
  *   sid_forward_batched:     I[b] = forwardProjectGPU(H, V[b])      forwardProjectGPU.m:1
  *   sid_adjoint_batched:     V[b] = backwardProjectGPU_new(H, I[b]) backwardProjectGPU_new.m:1
  *   sid_deconv_isra_batched: X[b] = deconvRL(fwd, bwd, Htf[b], maxIter, X[b], opts) in mode

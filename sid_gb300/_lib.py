@@ -15,7 +15,7 @@ LIB_PATH = os.path.join(_HERE, "_build", "libsid.so")
 HEADER = os.path.join(os.path.dirname(_HERE), "include", "sid.h")
 
 SID_OK, SID_EINVAL, SID_ENOMEM, SID_ECUDA, SID_ETIMEOUT, SID_ENOCONV, SID_ENOTSUP = 0, -1, -2, -3, -4, -5, -6
-PLAN_DIRECT, PLAN_SPECTRAL_F32, PLAN_SPECTRAL_I16, PLAN_SPECTRAL_F24 = 0x1, 0x2, 0x4, 0x8
+PLAN_DIRECT, PLAN_SPECTRAL_F32, PLAN_SPECTRAL_I16, PLAN_SPECTRAL_F24, PLAN_SPECTRAL_TC = 0x1, 0x2, 0x4, 0x8, 0x10
 METHODS = {"direct": 0, "spectral_f32": 1, "spectral_i16": 2, "spectral_mixed": 3, "spectral_mixed_f32": 4}
 PLAN_FLAG_FOR_METHOD = {"direct": PLAN_DIRECT, "spectral_f32": PLAN_SPECTRAL_F32, "spectral_i16": PLAN_SPECTRAL_I16,
                         "spectral_mixed": PLAN_SPECTRAL_I16 | PLAN_SPECTRAL_F24,
@@ -47,6 +47,7 @@ SIGNATURES = {
     "sid_plan_create": [P, I64, I64, I64, P, I64, I64, I32, PP],
     "sid_plan_destroy": [P],
     "sid_plan_info": [P, P],
+    "sid_plan_release_workspaces": [P],
     "sid_plan_set_weak_fraction": [P, ctypes.c_double],
     "sid_plan_set_kernel": [P, P, I64, I64, I64],
     "sid_forward": [P, I32, P, P, P],

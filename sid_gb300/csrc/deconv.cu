@@ -689,10 +689,16 @@ extern "C" int sid_deconv_ls_ex(sid_plan* p, int method, float* X, int max_iter,
 }
 
 // --------------------------------------------------- several volumes at once --
-// Projections of nb volumes (polyphase, back to back): the spectral forms run
-// up to four volumes per tap-spectrum pass (spectral_forward_batch); the
-// direct form and the per-volume steps (neuron kernel, weak-voxel
-// recomputation) go volume by volume.
+// Projections of nb volumes (polyphase, back to back): on a plan built with
+// SID_PLAN_SPECTRAL_TC the mixed form contracts up to 32 volumes per pass on
+// the tensor cores (spec_tc.cu, the 24-bit spectra both ways); otherwise the
+// spectral forms run up to four volumes per tap-spectrum pass on the FP32
+// pipes (spectral_forward_batch).  The direct form and the per-volume steps
+// (neuron kernel, weak-voxel recomputation) go volume by volume.
+static bool use_tc(const sid_plan* p, int method, int nb)
+{
+    return p->spec_tc && method == SID_METHOD_SPECTRAL_MIXED && nb >= 2;
+}
 static int spectral_fmt_fwd(int method, bool* i16)
 {
     switch (method) {
@@ -723,6 +729,7 @@ int fwd_poly_batch(sid_plan* p, int method, const float* vp, float* ip, int nb, 
         for (int b = 0; b < nb; ++b) SID_TRY(fwd_poly(p, method, vp + b * nv, ip + b * ni, st));
         return SID_OK;
     }
+    if (use_tc(p, method, nb)) return spectral_forward_tc(p, vp, ip, nb, st);
     return spectral_forward_batch(p, i16, vp, ip, nb, st);
 }
 
@@ -734,7 +741,8 @@ int adj_poly_batch(sid_plan* p, int method, const float* ip, float* bp, int nb, 
         for (int b = 0; b < nb; ++b) SID_TRY(adj_poly(p, method, ip + b * ni, bp + b * nv, st));
         return SID_OK;
     }
-    SID_TRY(spectral_adjoint_batch(p, fmt, ip, bp, nb, st));
+    if (use_tc(p, method, nb)) SID_TRY(spectral_adjoint_tc(p, ip, bp, nb, st));
+    else SID_TRY(spectral_adjoint_batch(p, fmt, ip, bp, nb, st));
     for (int b = 0; b < nb; ++b) {
         SID_TRY(weak_fix(p, ip + b * ni, bp + b * nv, st));
         if (p->kdims[0]) SID_TRY(conv_poly(p, bp + b * nv, bp + b * nv, st));
@@ -742,7 +750,12 @@ int adj_poly_batch(sid_plan* p, int method, const float* ip, float* bp, int nb, 
     return SID_OK;
 }
 
-constexpr int kVolBatch = 4;  // volumes per spectral pass
+// volumes per pass over the tap spectra
+static int64_t vol_group(const sid_plan* p, int method, int64_t nb)
+{
+    const int64_t g = (p->spec_tc && method == SID_METHOD_SPECTRAL_MIXED) ? 32 : 4;
+    return std::min<int64_t>(nb, g);
+}
 
 extern "C" int sid_deconv_isra_batched(sid_plan* p, int method, int64_t nb, const float* const* Htf, float* const* X,
                                        int maxIter, float lambda, void* stream)
@@ -754,7 +767,7 @@ extern "C" int sid_deconv_isra_batched(sid_plan* p, int method, int64_t nb, cons
     cudaStream_t st = as_stream(stream);
     SID_TRY(ensure_proj_ws(p));
     const int64_t nv = vol_plane_elems(p) * p->Z, ni = vol_plane_elems(p);
-    const int g = (int)std::min<int64_t>(nb, kVolBatch);
+    const int64_t g = vol_group(p, method, nb);
     SID_TRY(p->ws[0].alloc((size_t)(g * nv) * sizeof(float)));  // iterates
     SID_TRY(p->ws[1].alloc((size_t)(g * nv) * sizeof(float)));  // Htf
     SID_TRY(p->ws[4].alloc((size_t)(g * nv) * sizeof(float)));  // back projections
@@ -763,8 +776,8 @@ extern "C" int sid_deconv_isra_batched(sid_plan* p, int method, int64_t nb, cons
     float* hp = p->ws[1].as<float>();
     float* bp = p->ws[4].as<float>();
     float* ip = p->ws[5].as<float>();
-    for (int64_t b0 = 0; b0 < nb; b0 += kVolBatch) {
-        const int n = (int)std::min<int64_t>(kVolBatch, nb - b0);
+    for (int64_t b0 = 0; b0 < nb; b0 += g) {
+        const int n = (int)std::min<int64_t>(g, nb - b0);
         for (int b = 0; b < n; ++b) {
             SID_TRY(v_to_vp(p, Htf[b0 + b], hp + b * nv, p->Z, st));
             SID_TRY(v_to_vp(p, X[b0 + b], xp + b * nv, p->Z, st));
@@ -787,11 +800,11 @@ extern "C" int sid_forward_batched(sid_plan* p, int method, int64_t nb, const fl
     cudaStream_t st = as_stream(stream);
     SID_TRY(ensure_proj_ws(p));
     const int64_t nv = vol_plane_elems(p) * p->Z, ni = vol_plane_elems(p);
-    const int g = (int)std::min<int64_t>(nb, kVolBatch);
+    const int64_t g = vol_group(p, method, nb);
     SID_TRY(p->ws[0].alloc((size_t)(g * nv) * sizeof(float)));
     SID_TRY(p->ws[5].alloc((size_t)(g * ni) * sizeof(float)));
-    for (int64_t b0 = 0; b0 < nb; b0 += kVolBatch) {
-        const int n = (int)std::min<int64_t>(kVolBatch, nb - b0);
+    for (int64_t b0 = 0; b0 < nb; b0 += g) {
+        const int n = (int)std::min<int64_t>(g, nb - b0);
         for (int b = 0; b < n; ++b) SID_TRY(v_to_vp(p, V[b0 + b], p->ws[0].as<float>() + b * nv, p->Z, st));
         SID_TRY(fwd_poly_batch(p, method, p->ws[0].as<float>(), p->ws[5].as<float>(), n, st));
         for (int b = 0; b < n; ++b) SID_TRY(vp_to_v(p, p->ws[5].as<float>() + b * ni, I[b0 + b], 1, st));
@@ -806,11 +819,11 @@ extern "C" int sid_adjoint_batched(sid_plan* p, int method, int64_t nb, const fl
     cudaStream_t st = as_stream(stream);
     SID_TRY(ensure_proj_ws(p));
     const int64_t nv = vol_plane_elems(p) * p->Z, ni = vol_plane_elems(p);
-    const int g = (int)std::min<int64_t>(nb, kVolBatch);
+    const int64_t g = vol_group(p, method, nb);
     SID_TRY(p->ws[4].alloc((size_t)(g * nv) * sizeof(float)));
     SID_TRY(p->ws[5].alloc((size_t)(g * ni) * sizeof(float)));
-    for (int64_t b0 = 0; b0 < nb; b0 += kVolBatch) {
-        const int n = (int)std::min<int64_t>(kVolBatch, nb - b0);
+    for (int64_t b0 = 0; b0 < nb; b0 += g) {
+        const int n = (int)std::min<int64_t>(g, nb - b0);
         for (int b = 0; b < n; ++b) SID_TRY(v_to_vp(p, I[b0 + b], p->ws[5].as<float>() + b * ni, 1, st));
         SID_TRY(adj_poly_batch(p, method, p->ws[5].as<float>(), p->ws[4].as<float>(), n, st));
         for (int b = 0; b < n; ++b) SID_TRY(vp_to_v(p, p->ws[4].as<float>() + b * nv, V[b0 + b], p->Z, st));

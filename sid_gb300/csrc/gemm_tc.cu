@@ -33,6 +33,7 @@
 
 #include "ptx.cuh"
 #include "sid_internal.cuh"
+#include "tc.cuh"
 
 namespace sid {
 
@@ -46,74 +47,7 @@ struct GemmMaps {
     CUtensorMap b[GEMM_MAXPASS];
 };
 
-__device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t saddr)
-{
-    // tcgen05 shared-memory descriptor, K-major operand, 128-byte swizzle:
-    // start address >> 4 (bits 0-13), leading byte offset 16 B (ignored for
-    // swizzled K-major), stride byte offset 1024 B = 8 rows x 128 B (bits 32-45),
-    // fixed 0b001 at bits 46-48, swizzle mode 2 = 128B at bits 61-63.
-    uint64_t d = 0;
-    d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
-    d |= (uint64_t)(16u >> 4) << 16;
-    d |= (uint64_t)(1024u >> 4) << 32;
-    d |= (uint64_t)1 << 46;
-    d |= (uint64_t)2 << 61;
-    return d;
-}
-
-__device__ __forceinline__ uint32_t instr_desc(int n, bool bf16)
-{
-    // kind::f16 instruction descriptor: D = F32 (bits 4-5 = 1), A/B format
-    // (bits 7-9, 10-12: 0 = F16, 1 = BF16), both K-major, N>>3 at bits 17-22,
-    // M>>4 at bits 24-28.
-    const uint32_t fmt = bf16 ? 1u : 0u;
-    return (1u << 4) | (fmt << 7) | (fmt << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(GEMM_BM >> 4) << 24);
-}
-
-__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int x, int y, int z, uint64_t* bar)
-{
-    asm volatile(
-        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(
-            smem_u32(dst)),
-        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
-        : "memory");
-}
-
-__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc, int acc)
-{
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "setp.ne.b32 p, %4, 0;\n\t"
-        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
-        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc)
-        : "memory");
-}
-
-__device__ __forceinline__ void mma_commit(uint64_t* bar)
-{
-    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
-                 : "memory");
-}
-
-__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32])
-{
-    uint32_t r[32];
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
-        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
-          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
-          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-        : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-    for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
-}
+__device__ __forceinline__ uint32_t instr_desc(int n, bool bf16) { return instr_desc_m(GEMM_BM, n, bf16); }
 
 template <int BN, int STAGES>
 struct GemmSmem {
@@ -313,15 +247,10 @@ __global__ void k_splitk_reduce(const float* __restrict__ part, int nsplit, int6
 }
 
 // ----------------------------------------------------------- host side ----
-static int make_map(CUtensorMap* map, const void* base, int64_t rows, int64_t nkb, int box_rows, bool bf16)
+int encode_tmap_3d(CUtensorMap* map, CUtensorMapDataType dtype, const void* base, const uint64_t dims[3],
+                   const uint64_t strides[2], const uint32_t box[3], CUtensorMapSwizzle swizzle)
 {
-    // K-blocked operand: dims {64, rows, nkb}, byte strides {128, rows*128}
-    SID_REQUIRE(((uintptr_t)base & 15) == 0, "gemm: operand base address not 16-byte aligned");
-    cuuint64_t dims[3] = {(cuuint64_t)GEMM_BK, (cuuint64_t)rows, (cuuint64_t)nkb};
-    cuuint64_t strides[2] = {(cuuint64_t)(GEMM_BK * 2), (cuuint64_t)(rows * GEMM_BK * 2)};
-    cuuint32_t box[3] = {GEMM_BK, (cuuint32_t)box_rows, 1};
-    cuuint32_t estr[3] = {1, 1, 1};
-    // resolved through the runtime so libsid does not link libcuda directly
+    SID_REQUIRE(((uintptr_t)base & 15) == 0, "tensor map: base address not 16-byte aligned");
     using EncodeFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
@@ -336,15 +265,27 @@ static int make_map(CUtensorMap* map, const void* base, int64_t rows, int64_t nk
         }
         encode = reinterpret_cast<EncodeFn>(fn);
     }
-    CUresult r = encode(map, bf16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 3,
-                        const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                        CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    cuuint64_t d[3] = {dims[0], dims[1], dims[2]};
+    cuuint64_t str[2] = {strides[0], strides[1]};
+    cuuint32_t bx[3] = {box[0], box[1], box[2]};
+    cuuint32_t estr[3] = {1, 1, 1};
+    CUresult r = encode(map, dtype, 3, const_cast<void*>(base), d, str, bx, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                        swizzle, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) {
         set_error("cuTensorMapEncodeTiled failed (CUresult %d)", (int)r);
         return SID_ECUDA;
     }
     return SID_OK;
+}
+
+static int make_map(CUtensorMap* map, const void* base, int64_t rows, int64_t nkb, int box_rows, bool bf16)
+{
+    // K-blocked operand: dims {64, rows, nkb}, byte strides {128, rows*128}
+    const uint64_t dims[3] = {(uint64_t)GEMM_BK, (uint64_t)rows, (uint64_t)nkb};
+    const uint64_t strides[2] = {(uint64_t)(GEMM_BK * 2), (uint64_t)(rows * GEMM_BK * 2)};
+    const uint32_t box[3] = {GEMM_BK, (uint32_t)box_rows, 1};
+    return encode_tmap_3d(map, bf16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16, base, dims,
+                          strides, box, CU_TENSOR_MAP_SWIZZLE_128B);
 }
 
 template <int BN, int STAGES>

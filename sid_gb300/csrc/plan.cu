@@ -191,6 +191,14 @@ extern "C" int sid_plan_create(const float* H, int64_t M, int64_t Nnum, int64_t 
             st = build_spectra(p);
         }
     }
+    if (st == SID_OK && (flags & SID_PLAN_SPECTRAL_TC)) {
+        if (!(flags & SID_PLAN_SPECTRAL_F24)) {
+            set_error("sid_plan_create: SID_PLAN_SPECTRAL_TC needs SID_PLAN_SPECTRAL_F24");
+            st = SID_EINVAL;
+        } else {
+            st = build_spectra_tc(p);
+        }
+    }
     if (st != SID_OK) { sid_plan_destroy(p); return st; }
     *out = p;
     return SID_OK;
@@ -200,7 +208,8 @@ extern "C" int sid_plan_destroy(sid_plan* p)
 {
     if (!p) return SID_OK;
     DBuf* bufs[] = {&p->taps_f, &p->taps_b, &p->khat_f32, &p->khat_i16, &p->rstep, &p->khat_f24h, &p->khat_f24l,
-                    &p->twiddle, &p->weak, &p->weak_pad, &p->kern, &p->kvol[0], &p->kvol[1], &p->kvol[2],
+                    &p->khat_f24th, &p->khat_f24tl, &p->tcb, &p->tco, &p->twiddle, &p->weak, &p->weak_pad,
+                    &p->kern, &p->kvol[0], &p->kvol[1], &p->kvol[2],
                     &p->vp, &p->ip, &p->bp, &p->ipart, &p->vhat, &p->ihat, &p->bhat, &p->red, &p->errflag};
     for (DBuf* b : bufs) b->release();
     for (DBuf& b : p->ws) b.release();
@@ -213,11 +222,23 @@ extern "C" int sid_plan_destroy(sid_plan* p)
     return SID_OK;
 }
 
+extern "C" int sid_plan_release_workspaces(sid_plan* p)
+{
+    SID_REQUIRE(p, "sid_plan_release_workspaces: NULL plan");
+    SID_CUDA_TRY(cudaDeviceSynchronize());
+    DBuf* bufs[] = {&p->vp, &p->ip, &p->bp, &p->ipart, &p->vhat, &p->ihat, &p->bhat, &p->red, &p->tcb, &p->tco,
+                    &p->kvol[0], &p->kvol[1], &p->kvol[2]};
+    for (DBuf* b : bufs) b->release();
+    for (DBuf& b : p->ws) b.release();
+    return SID_OK;
+}
+
 extern "C" int sid_plan_info(const sid_plan* p, int64_t* info)
 {
     SID_REQUIRE(p && info, "sid_plan_info: NULL argument");
     const DBuf* bufs[] = {&p->taps_f, &p->taps_b, &p->khat_f32, &p->khat_i16, &p->rstep, &p->khat_f24h,
-                          &p->khat_f24l, &p->twiddle, &p->weak, &p->weak_pad, &p->kern, &p->kvol[0],
+                          &p->khat_f24l, &p->khat_f24th, &p->khat_f24tl, &p->tcb, &p->tco, &p->twiddle,
+                          &p->weak, &p->weak_pad, &p->kern, &p->kvol[0],
                           &p->kvol[1], &p->kvol[2], &p->vp, &p->ip, &p->bp, &p->ipart, &p->vhat, &p->ihat,
                           &p->bhat, &p->red};
     int64_t bytes = 0;

@@ -177,6 +177,10 @@ struct sid_plan {
     sid::DBuf khat_f24h;        // [f][b'a'][abc] 24-bit floats: high 16 bits of re, im
     sid::DBuf khat_f24l;        // [f][b'a'][abc] 24-bit floats: low 8 bits of re, im
     bool spec_f24;
+    sid::DBuf khat_f24th;       // [f][abc][b'a' padded to 8] the 24-bit planes transposed (tensor-core adjoint)
+    sid::DBuf khat_f24tl;
+    bool spec_tc = false;
+    sid::DBuf tcb, tco;         // tensor-core projections: B operand planes, contraction output
     sid::DBuf twiddle;          // L float2: exp(+2 pi i k / L)
     sid::DBuf weak;             // runs (column runs, then row runs) of the weakly observed voxels
     sid::DBuf weak_pad;         //   (recomputed exactly after each spectral back projection) and the
@@ -210,6 +214,14 @@ int spectral_adjoint(sid_plan* p, int fmt, const float* ip, float* bp, cudaStrea
 // nb (<= 4) polyphase volumes / images back to back
 int spectral_forward_batch(sid_plan* p, bool i16, const float* vp, float* ip, int nb, cudaStream_t st);
 int spectral_adjoint_batch(sid_plan* p, int fmt, const float* ip, float* bp, int nb, cudaStream_t st);
+// many volumes per pass on the tensor cores (spec_tc.cu; plan flag SID_PLAN_SPECTRAL_TC)
+int build_spectra_tc(sid_plan* p);
+int spectral_tc_max_volumes();
+int spectral_forward_tc(sid_plan* p, const float* vp, float* ip, int nb, cudaStream_t st);
+int spectral_adjoint_tc(sid_plan* p, const float* ip, float* bp, int nb, cudaStream_t st);
+// lenslet-grid real DFTs of nch channels (spectral.cu): planes [ch][Ly][Lx] <-> half spectra [ch][nf]
+int spec_r2c(sid_plan* p, const float* in, float2* out, int64_t nch, cudaStream_t st);
+int spec_c2r(sid_plan* p, const float2* in, float* out, int64_t nch, cudaStream_t st);
 int conv_poly(sid_plan* p, const float* in_vp, float* out_vp, cudaStream_t st);
 int weak_build(sid_plan* p);
 int weak_fix(sid_plan* p, const float* ip, float* bp, cudaStream_t st);

@@ -833,6 +833,18 @@ static int dft_c2r(const sid_plan* p, const float2* in, float* out, int64_t nch,
     return SID_OK;
 }
 
+int spec_r2c(sid_plan* p, const float* in, float2* out, int64_t nch, cudaStream_t st)
+{
+    SID_TRY(configure_dft(p));
+    return dft_r2c(p, in, out, nch, st);
+}
+
+int spec_c2r(sid_plan* p, const float2* in, float* out, int64_t nch, cudaStream_t st)
+{
+    SID_TRY(configure_dft(p));
+    return dft_c2r(p, in, out, nch, st);
+}
+
 static int spec_check(const sid_plan* p, int fmt)
 {
     if (fmt == FMT_I16 && !p->spec_i16) {

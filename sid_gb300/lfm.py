@@ -96,9 +96,12 @@ class Projector:
     CAindex : optional (Z, 2) 1-based per-depth crop (``psf_ballistic.CAindex``);
         None reproduces forwardProjectGPU / backwardProjectGPU_new.
     methods : operator forms to build ('direct', 'spectral_f32', 'spectral_i16').
+    batched : also build the transposed 24-bit spectra (SID_PLAN_SPECTRAL_TC) so
+        that the batched calls of 'spectral_mixed' contract up to 32 volumes per
+        pass on the tensor cores.
     """
 
-    def __init__(self, H, image_size, CAindex=None, methods=("direct",)):
+    def __init__(self, H, image_size, CAindex=None, methods=("direct",), batched=False):
         _require_cuda()
         Hn = np.asfortranarray(np.asarray(H, dtype=np.float32))
         if Hn.ndim == 4:
@@ -113,6 +116,8 @@ class Projector:
         flags = 0
         for m in methods:
             flags |= _lib.PLAN_FLAG_FOR_METHOD[m]
+        if batched:
+            flags |= _lib.PLAN_SPECTRAL_F24 | _lib.PLAN_SPECTRAL_TC
         self.methods = tuple(methods)
         self.default_method = self.methods[0]
         plan = ctypes.c_void_p()
@@ -148,6 +153,10 @@ class Projector:
 
     def close(self):
         self._finalizer()
+
+    def release_workspaces(self):
+        """Free the plan's solver and projection workspaces (sid_plan_release_workspaces)."""
+        _lib.call("sid_plan_release_workspaces", self._plan)
 
     def _method(self, method):
         m = method or self.default_method
