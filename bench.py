@@ -51,7 +51,7 @@ def parse():
     ap.add_argument("--nnls-frames", type=int, default=3000)
     ap.add_argument("--nnls-neurons", type=int, default=800)
     ap.add_argument("--no-demix", action="store_true", help="skip the demixing-loop measurement")
-    ap.add_argument("--batch-volumes", type=int, default=8,
+    ap.add_argument("--batch-volumes", type=int, default=32,
                     help="components deconvolved side by side in the batched measurement (0 skips it)")
     ap.add_argument("--demix-neurons", type=int, default=1500)
     ap.add_argument("--demix-frames", type=int, default=5000)
@@ -604,7 +604,9 @@ def main():
     plan_methods = list(methods)
     if not args.no_nnls and "direct" not in plan_methods:
         plan_methods.append("direct")  # the library generation reads the lenslet taps
-    P = s.Projector(H, (X, Y), None, methods=tuple(plan_methods))
+    # the tensor-core batched projections need the transposed 24-bit spectra
+    tc = args.method == "spectral_mixed" and args.batch_volumes > 1
+    P = s.Projector(H, (X, Y), None, methods=tuple(plan_methods), batched=tc)
     info = P.info()
     # RL input: Htf = A^T y with y = A V_true (the reference starts ISRA at Xguess = Htf)
     y = P.forward(Vt, method=args.method)
@@ -732,14 +734,15 @@ def main():
         P.set_kernel(None)
         del xk
 
-    # several components per pass over the tap spectra (reconstruct_S.m:162-212): 8 volumes, 3 ISRA
-    # iterations each, against the same iterations one volume at a time
+    # several components per pass over the tap spectra (reconstruct_S.m:162-212): nbv volumes, 3 ISRA
+    # iterations each, against the same iterations one volume at a time.  With the tensor-core plan the
+    # mixed form contracts up to 32 volumes per pass (spec_tc.cu); other methods 4 per pass on the FP32 pipes.
     batched = None
     if args.method.startswith("spectral") and args.batch_volumes > 1:
         nbv = args.batch_volumes
         hs = [Htf.clone() for _ in range(nbv)]
         xs = [X0.clone() for _ in range(nbv)]
-        P.isra_batched(hs[:2], xs[:2], 1, method=args.method)
+        P.isra_batched(hs, xs, 1, method=args.method)  # sizes the workspaces
         torch.cuda.synchronize()
         a = torch.cuda.Event(enable_timing=True)
         b = torch.cuda.Event(enable_timing=True)
@@ -755,20 +758,52 @@ def main():
         dev_b = float(np.linalg.norm(s.to_numpy(outs[-1]) - single) / np.linalg.norm(single))
         nf_ = (info["L"] // 2 + 1) * info["L"]
         n_in_, n_out_ = info["Nnum"] ** 2 * info["Z"], info["Nnum"] ** 2
-        # contraction work per launch: 4 volumes x (forward or adjoint) complex MACs = 8 FLOP each
-        flop_launch = 8.0 * nf_ * n_in_ * n_out_ * min(4, nbv)
-        fp32_peak = 152 * 128 * 2 * 2.07e9 / 1e12
+        per_vi = tb / (nbv * 3)
         batched = {"volumes": nbv, "iterations": 3, "ms": tb,
-                   "volume_iterations_per_s": nbv * 3 / (tb / 1e3),
-                   "ms_per_volume_iteration": tb / (nbv * 3),
+                   "volume_iterations_per_s": 1e3 / per_vi,
+                   "components_per_s": 1e3 / per_vi / 8,
+                   "components_per_s_note": "components deconvolved per second at reconstruct_S's 8 ISRA "
+                                            "iterations per component (reconstruct_S.m:87-89)",
+                   "ms_per_volume_iteration": per_vi,
                    "single_volume_ms_per_iteration": ms_per_step,
-                   "speedup_per_volume": ms_per_step / (tb / (nbv * 3)),
-                   "rel_l2_last_volume_vs_single_calls": dev_b,
-                   "contraction": {"launches": kb_n, "avg_launch_ms": kb_ms / max(kb_n, 1),
-                                   "fp32_tflops": flop_launch / (kb_ms / max(kb_n, 1)) / 1e9,
-                                   "frac_of_fp32_fma_peak": flop_launch / (kb_ms / max(kb_n, 1)) / 1e9 / fp32_peak,
-                                   "fp32_peak_note": "152 SMs x 128 lanes x 2 FLOP x 2.07 GHz (nominal)"}}
+                   "speedup_per_volume": ms_per_step / per_vi,
+                   "rel_l2_last_volume_vs_single_calls": dev_b}
+        avg = kb_ms / max(kb_n, 1)
+        if tc:
+            # tensor-core contraction: launches alternate forward (rows 225, reduction 2 x 6976) and
+            # back projection (rows 6976, reduction 2 x 232); 4 BF16 passes per MMA tile
+            g = min(nbv, 32)
+            bn = 64 if g <= 32 else 128
+            nip = -(-n_in_ // 8) * 8
+            op = -(-n_out_ // 8) * 8
+            kf, ka = 2 * nip, 2 * op
+            cd = lambda a_, b_: -(-a_ // b_) * b_  # noqa: E731
+            mma_f = 2 * 4 * cd(n_out_, 128) * bn * cd(kf, 64) * nf_
+            mma_a = 2 * 4 * cd(nip, 128) * bn * cd(ka, 64) * nf_
+            bytes_f = nf_ * n_out_ * kf * 3 + nf_ * bn * kf * 4 + nf_ * g * n_out_ * 8
+            bytes_a = nf_ * nip * ka * 3 + nf_ * bn * ka * 4 + nf_ * g * nip * 8
+            bf16_peak = float(json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["bf16_tflops"]) \
+                if os.path.exists(os.path.join(ROOT, "MEASURED_PEAKS.json")) else 1900.0
+            batched["contraction"] = {
+                "kernel": "k_spec_tc (tcgen05, 24-bit spectra as exact BF16 hi+lo, B split BF16 hi/lo, 4 passes)",
+                "volumes_per_pass": g, "launches": kb_n, "avg_launch_ms": avg,
+                "tensor_tflops": (mma_f + mma_a) / 2 / (avg / 1e3) / 1e12,
+                "tensor_frac_of_bf16_peak": (mma_f + mma_a) / 2 / (avg / 1e3) / 1e12 / bf16_peak,
+                "algorithmic_bytes_per_launch": (bytes_f + bytes_a) / 2,
+                "hbm_gbs": (bytes_f + bytes_a) / 2 / (avg / 1e3) / 1e9,
+                "hbm_frac": (bytes_f + bytes_a) / 2 / (avg / 1e3) / 1e9 / hbm,
+                "bound": "hbm", "peaks": "measured bf16_tflops / hbm_gbs (MEASURED_PEAKS.json)"}
+        else:
+            flop_launch = 8.0 * nf_ * n_in_ * n_out_ * min(4, nbv)
+            fp32_peak = 152 * 128 * 2 * 2.07e9 / 1e12
+            batched["contraction"] = {"kernel": "k_spec_fwd_b/k_spec_adj_b (FP32 pipes, 4 volumes per pass)",
+                                      "launches": kb_n, "avg_launch_ms": avg,
+                                      "fp32_tflops": flop_launch / avg / 1e9,
+                                      "frac_of_fp32_fma_peak": flop_launch / avg / 1e9 / fp32_peak,
+                                      "fp32_peak_note": "152 SMs x 128 lanes x 2 FLOP x 2.07 GHz (nominal)"}
         del hs, xs, outs
+        P.release_workspaces()
+        torch.cuda.empty_cache()
 
     nnls = None
     if not args.no_nnls:
