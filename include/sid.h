@@ -171,6 +171,11 @@ int sid_forward_batched(sid_plan* plan, int method, int64_t nb, const float* con
 int sid_adjoint_batched(sid_plan* plan, int method, int64_t nb, const float* const* I, float* const* V, void* stream);
 int sid_deconv_isra_batched(sid_plan* plan, int method, int64_t nb, const float* const* Htf, float* const* X,
                             int maxIter, float lambda, void* stream);
+/* X[b] = LS_deconv(fwd, bwd, X[b], max_iter, opts) in the plain mode (no TV
+ * terms) for nb volumes, X[b] holding df = Htf on entry (LS_deconv.m:1);
+ * lamb_L1: nb values (host), one per volume; lamb_L2 shared. */
+int sid_deconv_ls_batched(sid_plan* plan, int method, int64_t nb, float* const* X, int max_iter,
+                          const float* lamb_L1, float lamb_L2, void* stream);
 /* Host-array form of sid_deconv_isra (copies in, iterates, copies X out). */
 int sid_deconv_isra_host(sid_plan* plan, int method, const float* Htf, float* X,
                          int maxIter, float lambda);
@@ -405,6 +410,15 @@ void sid_recon_defaults(sid_recon_opts* opts); /* reconstruct_S.m:47-95 */
  * Reads the capped weight back to the host (one stream synchronisation). */
 int sid_reconstruct_component(sid_plan* plan, int method, const float* img, const uint8_t* microlenses,
                               const sid_recon_opts* opts, float* X, double* lamb_used, void* stream);
+/* The same for nc components (the components reconstruct_S.m:162-212 runs side
+ * by side): imgs / X are host arrays of nc device pointers, lamb_used (optional,
+ * host) nc values.  The back projections and the solver run on groups of up to
+ * 32 components through sid_adjoint_batched and sid_deconv_ls_batched /
+ * sid_deconv_isra_batched (on the tensor cores with a SID_PLAN_SPECTRAL_TC plan
+ * and SID_METHOD_SPECTRAL_MIXED).  One stream synchronisation per group. */
+int sid_reconstruct_components(sid_plan* plan, int method, int64_t nc, const float* const* imgs,
+                               const uint8_t* microlenses, const sid_recon_opts* opts, float* const* X,
+                               double* lamb_used, void* stream);
 
 /* ---- NMF steps (fast_NMF.m:185-186) ------------------------------------------
  * One projected-gradient step with exact line search on T or on S for

@@ -61,6 +61,8 @@ SIGNATURES = {
     "sid_forward_batched": [P, I32, I64, P, P, P],
     "sid_adjoint_batched": [P, I32, I64, P, P, P],
     "sid_deconv_isra_batched": [P, I32, I64, P, P, I32, F32, P],
+    "sid_deconv_ls_batched": [P, I32, I64, P, I32, P, F32, P],
+    "sid_reconstruct_components": [P, I32, I64, P, P, P, P, P, P],
     "sid_deconv_ls_ex": [P, I32, P, I32, F32, F32, P, F32, P],
     "sid_deconv_isra_host": [P, I32, P, P, I32, F32],
     "sid_deconv_rl_poisson": [P, I32, P, P, I32, P],

@@ -743,10 +743,9 @@ int adj_poly_batch(sid_plan* p, int method, const float* ip, float* bp, int nb, 
     }
     if (use_tc(p, method, nb)) SID_TRY(spectral_adjoint_tc(p, ip, bp, nb, st));
     else SID_TRY(spectral_adjoint_batch(p, fmt, ip, bp, nb, st));
-    for (int b = 0; b < nb; ++b) {
-        SID_TRY(weak_fix(p, ip + b * ni, bp + b * nv, st));
-        if (p->kdims[0]) SID_TRY(conv_poly(p, bp + b * nv, bp + b * nv, st));
-    }
+    SID_TRY(weak_fix_n(p, ip, bp, nb, st));
+    if (p->kdims[0])
+        for (int b = 0; b < nb; ++b) SID_TRY(conv_poly(p, bp + b * nv, bp + b * nv, st));
     return SID_OK;
 }
 
@@ -789,6 +788,60 @@ extern "C" int sid_deconv_isra_batched(sid_plan* p, int method, int64_t nb, cons
             SID_CHECK_LAUNCH();
         }
         for (int b = 0; b < n; ++b) SID_TRY(vp_to_v(p, xp + b * nv, X[b0 + b], p->Z, st));
+    }
+    return SID_OK;
+}
+
+// LS_deconv (plain mode, LS_deconv.m:72-93) for nb volumes: the projections
+// go through the batched forms, the per-volume scalars (step sizes) through
+// one reduction per volume.  lamb_L1: nb values (host), one per volume.
+extern "C" int sid_deconv_ls_batched(sid_plan* p, int method, int64_t nb, float* const* X, int max_iter,
+                                     const float* lamb_L1, float lamb_L2, void* stream)
+{
+    SID_REQUIRE(p && X && lamb_L1, "sid_deconv_ls_batched: NULL argument");
+    SID_REQUIRE(nb >= 1 && max_iter >= 0, "sid_deconv_ls_batched: need nb >= 1 and max_iter >= 0");
+    for (int64_t b = 0; b < nb; ++b) SID_REQUIRE(X[b], "sid_deconv_ls_batched: volume %lld is NULL", (long long)b);
+    cudaStream_t st = as_stream(stream);
+    SID_TRY(ensure_proj_ws(p));
+    const int64_t n = vol_plane_elems(p) * p->Z, ni = vol_plane_elems(p);
+    const int64_t g = vol_group(p, method, nb);
+    for (int k = 0; k < 3; ++k) SID_TRY(p->ws[k].alloc((size_t)(g * n) * sizeof(float)));
+    SID_TRY(p->ws[4].alloc((size_t)(g * n) * sizeof(float)));   // back projections
+    SID_TRY(p->ws[5].alloc((size_t)(g * ni) * sizeof(float)));  // images
+    SID_TRY(p->red.alloc((size_t)(kRedBlocks + 4 * g + 8) * sizeof(double)));
+    float* xp = p->ws[0].as<float>();
+    float* dp = p->ws[1].as<float>();
+    float* tp = p->ws[2].as<float>();
+    float* bp = p->ws[4].as<float>();
+    float* ip = p->ws[5].as<float>();
+    double* red = p->red.as<double>();
+    double* s12 = red + kRedBlocks;                            // two scalars per volume
+    float* alpha = reinterpret_cast<float*>(s12 + 2 * g);      // one step size per volume
+    for (int64_t b0 = 0; b0 < nb; b0 += g) {
+        const int m = (int)std::min<int64_t>(g, nb - b0);
+        for (int b = 0; b < m; ++b) SID_TRY(v_to_vp(p, X[b0 + b], xp + b * n, p->Z, st));
+        // df = Q(x0) - x0 + lamb_L1 with x0 = df
+        SID_TRY(fwd_poly_batch(p, method, xp, ip, m, st));
+        SID_TRY(adj_poly_batch(p, method, ip, bp, m, st));
+        for (int b = 0; b < m; ++b)
+            k_ls_init<<<2048, 256, 0, st>>>(dp + b * n, bp + b * n, xp + b * n, lamb_L1[b0 + b], lamb_L2, n);
+        SID_CHECK_LAUNCH();
+        SID_TRY(mask_vp(p, dp, m * p->Z, st));
+        for (int it = 0; it < max_iter; ++it) {
+            k_ls_passive<<<2048, 256, 0, st>>>(xp, dp, tp, m * n);
+            SID_CHECK_LAUNCH();
+            for (int b = 0; b < m; ++b) SID_TRY(dot(tp + b * n, tp + b * n, n, red, s12 + 2 * b, st));
+            SID_TRY(fwd_poly_batch(p, method, tp, ip, m, st));
+            for (int b = 0; b < m; ++b)
+                SID_TRY(dot(ip + b * ni, ip + b * ni, ni, red, s12 + 2 * b + 1, st, s12 + 2 * b, alpha + b));
+            for (int b = 0; b < m; ++b) k_ls_step<<<2048, 256, 0, st>>>(xp + b * n, tp + b * n, alpha + b, n);
+            SID_CHECK_LAUNCH();
+            SID_TRY(fwd_poly_batch(p, method, tp, ip, m, st));
+            SID_TRY(adj_poly_batch(p, method, ip, bp, m, st));
+            k_ls_grad<<<2048, 256, 0, st>>>(dp, bp, tp, lamb_L2, m * n);
+            SID_CHECK_LAUNCH();
+        }
+        for (int b = 0; b < m; ++b) SID_TRY(vp_to_v(p, xp + b * n, X[b0 + b], p->Z, st));
     }
     return SID_OK;
 }

@@ -17,6 +17,7 @@
 //   X = nrm * LS_deconv(A, A', Htf)   or   nrm * deconvRL(A, A', Htf, maxIter, Htf)
 #include <cmath>
 #include <cstring>
+#include <vector>
 
 #include "sid_internal.cuh"
 
@@ -307,5 +308,86 @@ extern "C" int sid_reconstruct_component(sid_plan* p, int method, const float* i
     // X = nrm * X  (:205)
     k_scale_norm<<<(unsigned)std::min<int64_t>(cdiv(nV, 256), 152 * 8), 256, 0, st>>>(X, nV, dsc + 1, 1);
     SID_CHECK_LAUNCH();
+    return SID_OK;
+}
+
+// Several components (reconstruct_S.m:162-212 reconstructs them side by side):
+// the background clip, normalisation and lamb_L1 quantile per component, the
+// back projection Htf and the solver for all components of a group together
+// (sid_adjoint_batched, sid_deconv_ls_batched / sid_deconv_isra_batched), so
+// the tap spectra stream once per group.
+extern "C" int sid_reconstruct_components(sid_plan* p, int method, int64_t nc, const float* const* imgs,
+                                          const uint8_t* microlenses, const sid_recon_opts* o, float* const* X,
+                                          double* lamb_used, void* stream)
+{
+    SID_REQUIRE(p && imgs && o && X, "sid_reconstruct_components: NULL argument");
+    SID_REQUIRE(nc >= 1, "sid_reconstruct_components: no components");
+    for (int64_t c = 0; c < nc; ++c)
+        SID_REQUIRE(imgs[c] && X[c], "sid_reconstruct_components: component %lld is NULL", (long long)c);
+    SID_REQUIRE(o->q >= 0.0 && o->q <= 1.0, "sid_reconstruct_components: q outside [0, 1]");
+    SID_REQUIRE(o->solver == 0 || o->solver == 1,
+                "sid_reconstruct_components: solver must be 0 ('fast_nnls') or 1 ('ISRA'); 'fast_ls' is not "
+                "supported");
+    SID_REQUIRE(o->max_iter >= 0, "sid_reconstruct_components: negative max_iter");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const int64_t nI = p->X * p->Y, nV = nI * p->Z;
+    const int64_t g = std::min<int64_t>(nc, 32);
+    SID_TRY(p->ws[6].alloc((size_t)(g * nI) * sizeof(float)));
+    SID_TRY(p->ws[8].alloc(quantile_work_bytes() + (size_t)(4 * g + 8) * sizeof(double)));
+    if (o->solver == 1) SID_TRY(p->ws[7].alloc((size_t)(g * nV) * sizeof(float)));
+    void* qw = p->ws[8].p;
+    double* dscs = reinterpret_cast<double*>(static_cast<char*>(p->ws[8].p) + quantile_work_bytes());
+    std::vector<const float*> ims(g), hs(g);
+    std::vector<float*> xs(g);
+    std::vector<float> lamb(g);
+    for (int64_t c0 = 0; c0 < nc; c0 += g) {
+        const int m = (int)std::min<int64_t>(g, nc - c0);
+        for (int b = 0; b < m; ++b) {
+            // per component: dsc[0] background quantile, dsc[1] sum of squares, dsc[2] Htf quantile, dsc[3] max
+            double* dsc = dscs + 4 * b;
+            unsigned* dmax = reinterpret_cast<unsigned*>(dsc + 3);
+            float* im = p->ws[6].as<float>() + b * nI;
+            SID_CUDA_TRY(cudaMemsetAsync(dsc + 1, 0, sizeof(double), st));
+            SID_CUDA_TRY(cudaMemsetAsync(dmax, 0, sizeof(unsigned), st));
+            SID_TRY(quantile_dev(imgs[c0 + b], nI, microlenses, o->q, dsc, qw, st));
+            const unsigned gr = (unsigned)std::min<int64_t>(cdiv(nI, 256), 152 * 8);
+            k_clip_max<<<gr, 256, 0, st>>>(imgs[c0 + b], nI, dsc, im, dmax);
+            k_div_sumsq<<<gr, 256, 0, st>>>(im, nI, dmax, dsc + 1);
+            k_scale_norm<<<gr, 256, 0, st>>>(im, nI, dsc + 1, 0);
+            SID_CHECK_LAUNCH();
+            ims[b] = im;
+            xs[b] = X[c0 + b];
+        }
+        // Htf = A'(img / nrm) for the group
+        SID_TRY(sid_adjoint_batched(p, method, m, ims.data(), xs.data(), stream));
+        for (int b = 0; b < m; ++b) {
+            double* dsc = dscs + 4 * b;
+            SID_TRY(quantile_dev(X[c0 + b], nV, nullptr, 1.0 - 1e-4, dsc + 2, qw, st));
+        }
+        std::vector<double> hq(4 * m);
+        SID_CUDA_TRY(cudaMemcpyAsync(hq.data(), dscs, (size_t)(4 * m) * sizeof(double), cudaMemcpyDeviceToHost, st));
+        SID_CUDA_TRY(cudaStreamSynchronize(st));
+        for (int b = 0; b < m; ++b) {
+            const double l = std::fmin(hq[4 * b + 2], o->lamb_L1);
+            lamb[b] = (float)l;
+            if (lamb_used) lamb_used[c0 + b] = l;
+        }
+        if (o->solver == 0) {
+            SID_TRY(sid_deconv_ls_batched(p, method, m, xs.data(), o->max_iter, lamb.data(), (float)o->lamb_L2,
+                                          stream));
+        } else {
+            for (int b = 0; b < m; ++b) {
+                float* h = p->ws[7].as<float>() + b * nV;
+                SID_CUDA_TRY(cudaMemcpyAsync(h, X[c0 + b], (size_t)nV * sizeof(float), cudaMemcpyDeviceToDevice, st));
+                hs[b] = h;
+            }
+            SID_TRY(sid_deconv_isra_batched(p, method, m, hs.data(), xs.data(), o->max_iter, 0.f, stream));
+        }
+        for (int b = 0; b < m; ++b) {
+            k_scale_norm<<<(unsigned)std::min<int64_t>(cdiv(nV, 256), 152 * 8), 256, 0, st>>>(X[c0 + b], nV,
+                                                                                           dscs + 4 * b + 1, 1);
+            SID_CHECK_LAUNCH();
+        }
+    }
     return SID_OK;
 }

@@ -225,6 +225,7 @@ int spec_c2r(sid_plan* p, const float2* in, float* out, int64_t nch, cudaStream_
 int conv_poly(sid_plan* p, const float* in_vp, float* out_vp, cudaStream_t st);
 int weak_build(sid_plan* p);
 int weak_fix(sid_plan* p, const float* ip, float* bp, cudaStream_t st);
+int weak_fix_n(sid_plan* p, const float* ip, float* bp, int nb, cudaStream_t st);  // nb back to back
 int v_to_vp(const sid_plan* p, const float* V, float* vp, int64_t Z, cudaStream_t st);
 int vp_to_v(const sid_plan* p, const float* vp, float* V, int64_t Z, cudaStream_t st);
 int mask_vp(const sid_plan* p, float* vp, int64_t Z, cudaStream_t st);

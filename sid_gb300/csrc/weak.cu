@@ -78,9 +78,12 @@ template <bool ROW, int DM, int JR>
 __global__ void __launch_bounds__(kWeakThreads)
 k_adj_runs(const float* __restrict__ taps, const float* __restrict__ lat, float* __restrict__ bp,
            const WeakRun* __restrict__ runs, int nrun, int N, int Lx, int Ly, int D, int dlo, int lo, int Wp, int Hp,
-           int64_t tbs)
+           int64_t tbs, int64_t lat_vol, int64_t bp_vol)
 {
     constexpr int NW = kWeakThreads / 32;
+    // blockIdx.y: the volume of a batch (lattice copies and back projections back to back)
+    lat += blockIdx.y * lat_vol;
+    bp += blockIdx.y * bp_vol;
     constexpr int CM = JR + DM - 1;
     __shared__ float part[NW][JR];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -295,50 +298,59 @@ int weak_build(sid_plan* p)
     return SID_OK;
 }
 
-// Overwrite the listed voxels of a spectral back projection bp = A' ip with
-// their exact values.
-int weak_fix(sid_plan* p, const float* ip, float* bp, cudaStream_t st)
+// Overwrite the listed voxels of nb spectral back projections bp[b] = A' ip[b]
+// (polyphase volumes and images back to back) with their exact values.
+int weak_fix_n(sid_plan* p, const float* ip, float* bp, int nb, cudaStream_t st)
 {
     if (p->nweak == 0) return SID_OK;
     SID_REQUIRE(p->taps_f.p, "spectral plan: lenslet taps missing for the weak-voxel back projection");
     const int64_t tbs = cdiv(p->N * p->g.D * p->g.D, 32) * 32;
     const int N = (int)p->N, Lx = (int)p->Lx, Ly = (int)p->Ly, D = (int)p->g.D, dlo = (int)p->g.dlo;
+    const int64_t ni = (int64_t)N * N * Lx * Ly, nv = ni * p->Z;
     if (p->g.D > kRunDMax) {
         const unsigned grid = (unsigned)std::min<int64_t>(p->nweak, 152 * 8);
-        k_adj_voxel<<<grid, kWeakThreads, 0, st>>>(p->taps_f.as<float>(), ip, bp, p->weak.as<int>(),
-                                                   (int)p->nweak, N, Lx, Ly, D, dlo, tbs);
-        SID_CHECK_LAUNCH();
+        for (int b = 0; b < nb; ++b) {
+            k_adj_voxel<<<grid, kWeakThreads, 0, st>>>(p->taps_f.as<float>(), ip + b * ni, bp + b * nv,
+                                                       p->weak.as<int>(), (int)p->nweak, N, Lx, Ly, D, dlo, tbs);
+            SID_CHECK_LAUNCH();
+        }
         return SID_OK;
     }
     const int lo = (int)std::max<int64_t>(0, -p->g.dlo), hi = (int)std::max<int64_t>(0, p->g.D - 1 + p->g.dlo);
     const int Wp = Lx + lo + hi, Hp = Ly + lo + hi;
+    const int64_t pv = (int64_t)N * N * Wp * Hp;  // one volume's padded lattice copy
+    SID_TRY(p->weak_pad.alloc((size_t)(2 * nb * pv) * sizeof(float)));
     float* pad = p->weak_pad.as<float>();
-    float* padT = pad + (size_t)N * N * Wp * Hp;
-    k_pad_lattice<<<1024, 256, 0, st>>>(ip, pad, p->nweak_rows ? padT : nullptr, N * N, Lx, Ly, lo, Wp, Hp);
+    float* padT = pad + nb * pv;
+    k_pad_lattice<<<1024, 256, 0, st>>>(ip, pad, p->nweak_rows ? padT : nullptr, nb * N * N, Lx, Ly, lo, Wp, Hp);
     SID_CHECK_LAUNCH();
     const WeakRun* runs = p->weak.as<WeakRun>();
     const float* taps = p->taps_f.as<float>();
     const int nc = (int)p->nweak_cols, nr = (int)p->nweak_rows;
     if (nc) {
+        const dim3 grid((unsigned)nc, (unsigned)nb);
         if (D <= 16)
-            k_adj_runs<false, 16, kRunMax><<<nc, kWeakThreads, 0, st>>>(taps, pad, bp, runs, nc, N, Lx, Ly, D, dlo,
-                                                                        lo, Wp, Hp, tbs);
+            k_adj_runs<false, 16, kRunMax><<<grid, kWeakThreads, 0, st>>>(taps, pad, bp, runs, nc, N, Lx, Ly, D, dlo,
+                                                                          lo, Wp, Hp, tbs, pv, nv);
         else
-            k_adj_runs<false, 32, kRunMax><<<nc, kWeakThreads, 0, st>>>(taps, pad, bp, runs, nc, N, Lx, Ly, D, dlo,
-                                                                        lo, Wp, Hp, tbs);
+            k_adj_runs<false, 32, kRunMax><<<grid, kWeakThreads, 0, st>>>(taps, pad, bp, runs, nc, N, Lx, Ly, D, dlo,
+                                                                          lo, Wp, Hp, tbs, pv, nv);
         SID_CHECK_LAUNCH();
     }
     if (nr) {
+        const dim3 grid((unsigned)nr, (unsigned)nb);
         if (D <= 16)
-            k_adj_runs<true, 16, kRunMax><<<nr, kWeakThreads, 0, st>>>(taps, padT, bp, runs + nc, nr, N, Lx, Ly, D,
-                                                                       dlo, lo, Wp, Hp, tbs);
+            k_adj_runs<true, 16, kRunMax><<<grid, kWeakThreads, 0, st>>>(taps, padT, bp, runs + nc, nr, N, Lx, Ly, D,
+                                                                         dlo, lo, Wp, Hp, tbs, pv, nv);
         else
-            k_adj_runs<true, 32, kRunMax><<<nr, kWeakThreads, 0, st>>>(taps, padT, bp, runs + nc, nr, N, Lx, Ly, D,
-                                                                       dlo, lo, Wp, Hp, tbs);
+            k_adj_runs<true, 32, kRunMax><<<grid, kWeakThreads, 0, st>>>(taps, padT, bp, runs + nc, nr, N, Lx, Ly, D,
+                                                                         dlo, lo, Wp, Hp, tbs, pv, nv);
         SID_CHECK_LAUNCH();
     }
     return SID_OK;
 }
+
+int weak_fix(sid_plan* p, const float* ip, float* bp, cudaStream_t st) { return weak_fix_n(p, ip, bp, 1, st); }
 
 }  // namespace sid
 

@@ -302,10 +302,7 @@ class Projector:
         _lib.call("sid_plan_timing_read", self._plan, ctypes.byref(ms), ctypes.byref(n))
         return ms.value, n.value
 
-    def reconstruct_component(self, img, microlenses=None, opts=None, method=None, return_lambda=False):
-        """nrm * solve(A'(img / nrm)) for one component image after the
-        background clip of reconstruct_S (reconstruct_S.m:168-205); opts:
-        q, lamb_L1, lamb_L2, whichSolver ('fast_nnls' or 'ISRA'), max_iter."""
+    def _recon_opts(self, opts):
         opts = dict(opts or {})
         o = ReconOpts()
         _lib.load().sid_recon_defaults(ctypes.byref(o))
@@ -317,24 +314,62 @@ class Projector:
         if solver not in ("fast_nnls", "ISRA"):
             raise NotImplementedError(f"reconstruct_S: solver {solver!r} does not run natively")
         o.solver = 0 if solver == "fast_nnls" else 1
+        return o
+
+    def _microlens_mask(self, microlenses):
+        if microlenses is None:
+            return None
+        if isinstance(microlenses, torch.Tensor):  # X x Y mask, flattened column-major
+            ml = microlenses.to(device="cuda", dtype=torch.uint8).permute(1, 0).contiguous().reshape(-1)
+        else:
+            m = np.asarray(microlenses) != 0
+            ml = torch.from_numpy(np.ascontiguousarray(m.astype(np.uint8).ravel(order="F"))).to("cuda")
+        if ml.numel() != self.X * self.Y:
+            raise ValueError("microlenses must be X x Y")
+        return ml
+
+    def reconstruct_component(self, img, microlenses=None, opts=None, method=None, return_lambda=False):
+        """nrm * solve(A'(img / nrm)) for one component image after the
+        background clip of reconstruct_S (reconstruct_S.m:168-205); opts:
+        q, lamb_L1, lamb_L2, whichSolver ('fast_nnls' or 'ISRA'), max_iter."""
+        o = self._recon_opts(opts)
         im = to_device(img)
         if tuple(im.shape) != (self.X, self.Y):
             raise ValueError(f"component image must be {(self.X, self.Y)}, got {tuple(im.shape)}")
-        ml = None
-        if microlenses is not None:  # X x Y mask, flattened column-major
-            if isinstance(microlenses, torch.Tensor):
-                ml = microlenses.to(device="cuda", dtype=torch.uint8).permute(1, 0).contiguous().reshape(-1)
-            else:
-                m = np.asarray(microlenses) != 0
-                ml = torch.from_numpy(np.ascontiguousarray(m.astype(np.uint8).ravel(order="F"))).to("cuda")
-            if ml.numel() != self.X * self.Y:
-                raise ValueError("microlenses must be X x Y")
+        ml = self._microlens_mask(microlenses)
         X = _fortran_tensor((self.X, self.Y, self.Z), im.device)
         lam = ctypes.c_double()
         _lib.call("sid_reconstruct_component", self._plan, self._method(method), im.data_ptr(),
                   ml.data_ptr() if ml is not None else None, ctypes.byref(o), X.data_ptr(), ctypes.byref(lam),
                   _stream_ptr())
         return (X, lam.value) if return_lambda else X
+
+    def reconstruct_components(self, imgs, microlenses=None, opts=None, method=None, return_lambda=False):
+        """reconstruct_component for several component images at once
+        (reconstruct_S.m:162-212): back projections and solver iterations run
+        on groups of up to 32 components (sid_reconstruct_components)."""
+        o = self._recon_opts(opts)
+        ims = [to_device(i) for i in imgs]
+        for im in ims:
+            if tuple(im.shape) != (self.X, self.Y):
+                raise ValueError(f"component image must be {(self.X, self.Y)}, got {tuple(im.shape)}")
+        ml = self._microlens_mask(microlenses)
+        outs = [_fortran_tensor((self.X, self.Y, self.Z), ims[0].device) for _ in ims]
+        lam = (ctypes.c_double * len(ims))()
+        _lib.call("sid_reconstruct_components", self._plan, self._method(method), len(ims),
+                  ctypes.cast(self._ptr_array(ims), ctypes.c_void_p), ml.data_ptr() if ml is not None else None,
+                  ctypes.byref(o), ctypes.cast(self._ptr_array(outs), ctypes.c_void_p),
+                  ctypes.cast(lam, ctypes.c_void_p), _stream_ptr())
+        return (outs, list(lam)) if return_lambda else outs
+
+    def ls_deconv_batched(self, dfs, max_iter=8, lamb_L1=0.0, lamb_L2=0.0, method=None):
+        """LS_deconv (plain mode) for several volumes; lamb_L1: one value or one per volume."""
+        xs = [to_device(d).clone() for d in dfs]
+        l1 = np.broadcast_to(np.asarray(lamb_L1, dtype=np.float32), (len(xs),)).copy()
+        _lib.call("sid_deconv_ls_batched", self._plan, self._method(method), len(xs),
+                  ctypes.cast(self._ptr_array(xs), ctypes.c_void_p), int(max_iter), l1.ctypes.data,
+                  float(lamb_L2), _stream_ptr())
+        return xs
 
     def ls_deconv(self, df, max_iter=8, lamb_L1=0.0, lamb_L2=0.0, method=None, lamb_TV_L2=(0.0, 0.0, 0.0),
                   lamb_TV_L1=0.0) -> torch.Tensor:
@@ -353,16 +388,16 @@ class Projector:
 _PLANS: dict = {}
 
 
-def _plan_for(H, image_size, CAindex, method):
+def _plan_for(H, image_size, CAindex, method, batched=False):
     key = (id(H), tuple(np.shape(H)), tuple(image_size), None if CAindex is None else
-           tuple(np.asarray(CAindex).ravel().tolist()), method)
+           tuple(np.asarray(CAindex).ravel().tolist()), method, batched)
     pr = _PLANS.get(key)
     if pr is None or pr[0]() is not H:
         try:
             ref = weakref.ref(H)
         except TypeError:
             ref = (lambda h=H: h)
-        _PLANS[key] = (ref, Projector(H, image_size, CAindex, methods=(method,)))
+        _PLANS[key] = (ref, Projector(H, image_size, CAindex, methods=(method,), batched=batched))
         pr = _PLANS[key]
     return pr[1]
 
@@ -495,8 +530,8 @@ def generate_kernel(ker_shape, ker_param):
 
 def reconstruct_S(S, psf_ballistic, opts=None):
     """recon_nnmf = reconstruct_S(S, psf_ballistic, opts) (reconstruct_S.m:1),
-    the GPU branch (:158-211): every component S(ii, :, :) reconstructed on
-    one resident plan.  S: (n, X, Y); psf_ballistic: dict or object with H;
+    the GPU branch (:158-211): the components S(ii, :, :) reconstructed on
+    one resident plan, in groups of up to 32 (sid_reconstruct_components).  S: (n, X, Y); psf_ballistic: dict or object with H;
     opts: q, lamb_L1, lamb_L2, whichSolver, max_iter, microlenses.  Returns a
     list of X x Y x Z CUDA tensors.  With opts.ker_param (and opts.ker_shape,
     default 'user'), the projector is composed with convn(., kernel, 'same')
@@ -510,12 +545,11 @@ def reconstruct_S(S, psf_ballistic, opts=None):
     S = S if isinstance(S, torch.Tensor) else np.asarray(S)
     n, X, Y = S.shape
     method = opts.get("method", _DEFAULT_METHOD)
-    P = _plan_for(H, (X, Y), None, method)
-    out = []
+    # many components: the mixed form's tensor-core batched projections
+    P = _plan_for(H, (X, Y), None, method, batched=(method == "spectral_mixed" and n > 1))
     P.set_kernel(kernel)
     try:
-        for ii in range(n):
-            out.append(P.reconstruct_component(S[ii], opts.get("microlenses"), opts, method=method))
+        out = P.reconstruct_components([S[ii] for ii in range(n)], opts.get("microlenses"), opts, method=method)
     finally:
         P.set_kernel(None)
     return out

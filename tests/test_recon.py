@@ -164,3 +164,60 @@ def test_reconstruct_S_function_api(small, oracle):
     for k in range(2):
         ref = oracle.reconstruct_S_one(S[k], fwd, bwd, {})
         assert rel_l2(s.to_numpy(recon[k]), ref) < 1e-4
+
+
+# --------------------------------------------- several components at once --
+def _component_images(img, n):
+    imgs = [img, np.asfortranarray(img[::-1, :]), np.asfortranarray(img[:, ::-1]),
+            np.asfortranarray(img.T), np.asfortranarray(img[::-1, ::-1])]
+    return [np.asfortranarray(imgs[k % 5] * (1.0 + 0.1 * k)).astype(np.float32) for k in range(n)]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("opts", [{}, {"whichSolver": "ISRA", "max_iter": 6}, {"lamb_L1": 1e6, "lamb_L2": 1e-2}])
+def test_reconstruct_components_equal_single_calls(small, opts):
+    """The batched driver (groups of components through the batched back
+    projection and solvers) gives what one call per component gives, with the
+    same capped lamb_L1 per component; 35 components span two groups."""
+    import sid_gb300 as s
+    H, img, P, fwd, bwd = small
+    imgs = _component_images(img, 35)
+    outs, lams = P.reconstruct_components(imgs, None, opts, method="direct", return_lambda=True)
+    for k in (0, 1, 17, 31, 32, 34):
+        one, lam = P.reconstruct_component(imgs[k], None, opts, method="direct", return_lambda=True)
+        assert rel_l2(s.to_numpy(outs[k]), s.to_numpy(one)) < 1e-6, k
+        assert lams[k] == pytest.approx(lam, rel=1e-12)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("opts,tol", [({}, 1e-4), ({"whichSolver": "ISRA", "max_iter": 6}, 1e-4)])
+def test_reconstruct_components_tensor_core_plan(gpu, oracle, opts, tol):
+    """The tensor-core batched projections (SID_PLAN_SPECTRAL_TC, mixed form)
+    inside the component driver, stage by stage as for the single spectral
+    calls: the back projections against the oracle's, then each solve against
+    the oracle's solve from the same back projection."""
+    import sid_gb300 as s
+    from sid_gb300 import Projector, synthetic
+    N, Z, M, L = 5, 3, 31, 9
+    X = N * L
+    H = synthetic.gaussian_psf(M, N, Z, sigma_min=1.0, sigma_max=3.0)
+    Vt = synthetic.blob_volume(X, X, Z, 6, sigma=(1.5, 1.5), seed=4)
+    rng = np.random.default_rng(9)
+    img = np.asfortranarray((oracle.forward_project(H, Vt) + 0.02 * rng.random((X, X))).astype(np.float32))
+    fwd = lambda v: oracle.forward_project(H, v)  # noqa: E731
+    bwd = lambda i: oracle.backward_project(H, i)  # noqa: E731
+    P = Projector(H, (X, X), None, methods=("spectral_mixed",), batched=True)
+    imgs = _component_images(img, 6)
+    o0 = dict(opts, max_iter=0)
+    o0.pop("whichSolver", None)
+    hg = P.reconstruct_components(imgs, None, o0, method="spectral_mixed")
+    outs = P.reconstruct_components(imgs, None, opts, method="spectral_mixed")
+    for k in range(6):
+        im = np.maximum(imgs[k].astype(np.float64) - oracle.matlab_quantile(imgs[k], 0.8), 0.0)
+        im = im / im.max()
+        nrm = np.sqrt(np.sum(im * im))
+        Hg = s.to_numpy(hg[k]).astype(np.float64) / nrm
+        assert rel_l2(Hg, bwd(im / nrm)) < 2e-5, (k, rel_l2(Hg, bwd(im / nrm)))
+        ref = _oracle_solve_from(oracle, Hg, nrm, fwd, bwd, opts)
+        assert rel_l2(s.to_numpy(outs[k]), ref) < tol, (k, rel_l2(s.to_numpy(outs[k]), ref))
+    P.close()
