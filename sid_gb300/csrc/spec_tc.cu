@@ -71,6 +71,7 @@ struct SpecTcSmem {
     static constexpr int TMA_BYTES = AHI + 2 * B + LO8;
     static constexpr int TOTAL = STAGES * STAGE + 1024;
     static_assert(B % 1024 == 0 && STAGE % 1024 == 0, "stage tiles must stay 1024-byte aligned");
+    static_assert(TOTAL <= 227 * 1024, "stages exceed the shared memory of one CTA");
 };
 
 // Remainders of one 8-element chunk: hi = 8 BF16 high halves, lo = their low bytes.
@@ -462,7 +463,8 @@ static int tc_contract(sid_plan* p, bool adj, const float2* src, int nb, int64_t
     SID_TRY(tc_maps(&maps, ah, al, bh, bl, rows, kp, nf, bn));
     const int nkb = (int)cdiv(kp, TC_BK);
     p->timer.begin(st);
-    int rc = bn == 64 ? launch_spec_tc<64, 3>(maps, (int)rows, nkb, nf, nb, p->tco.as<float2>(), p->errflag.as<int>(), st)
+    // stages: 4 x 56 KB (BN = 64) or 3 x 72 KB (BN = 128) of the 227 KB of shared memory
+    int rc = bn == 64 ? launch_spec_tc<64, 4>(maps, (int)rows, nkb, nf, nb, p->tco.as<float2>(), p->errflag.as<int>(), st)
                       : launch_spec_tc<128, 3>(maps, (int)rows, nkb, nf, nb, p->tco.as<float2>(),
                                                p->errflag.as<int>(), st);
     p->timer.finish(st);
