@@ -22,7 +22,10 @@ def test_boxes_bit_exact(sidlib, oracle):
 
 
 @pytest.mark.gpu
-def test_library_matches_oracle(gpu, oracle):
+# neur_rad 4 and 2: the tap-row kernel (boxes spanning 2 or 3 lattice points
+# per phase); 9: the generic kernel (boxes spanning 4-5)
+@pytest.mark.parametrize("rad", [4, 2, 9])
+def test_library_matches_oracle(gpu, oracle, rad):
     import sid_gb300 as s
     from sid_gb300 import synthetic
     N, Z, M, L = 5, 7, 41, 12
@@ -35,9 +38,9 @@ def test_library_matches_oracle(gpu, oracle):
     centers[1] = [X - 0.2, X / 2, Z]      # far edge
     neur_id = rng.random((12, 3)) < 0.6
     neur_id[:, 0] = True
-    opts = {"neur_rad": 4, "axial": 2.0}
+    opts = {"neur_rad": rad, "axial": 2.0}
     got = s.to_numpy(s.generate_LFM_library_GPU(recon, centers, neur_id, {"H": H}, opts))
-    ref = oracle.generate_library(recon, centers, neur_id, H, 4, 2.0)
+    ref = oracle.generate_library(recon, centers, neur_id, H, rad, 2.0)
     assert got.shape == ref.shape
     assert rel_l2(got, ref) < 1e-5, rel_l2(got, ref)
     for n in range(12):
