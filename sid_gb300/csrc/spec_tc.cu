@@ -18,11 +18,14 @@
 // Precision.  A 24-bit float (sign, 8-bit exponent, 15 stored mantissa bits,
 // spectral.cu f24_split) is exactly the sum of two BF16 numbers: its high 16
 // bits, and the remainder below them (at most 8 significant bits).  B is split
-// into BF16 hi + lo (about 17 significant bits).  Four BF16 MMA passes
-// (hi*hi + hi*lo + lo*hi + lo*lo) give K * (B_hi + B_lo) with FP32
-// accumulation in TMEM; the accumulator is drained into registers every 1024
-// reduction elements and added there with round-to-nearest (the tensor-core
-// accumulator truncates, gemm_tc.cu).
+// into three BF16 parts hi + mid + lo (24 significant bits, FP32's precision:
+// with two parts, 16-17 bits, ISRA from background-clipped components -- which
+// divides by near-zero back projections -- landed several times further from
+// FP64 than the single-volume mixed form).  Five BF16 MMA passes
+// (A_hi (B_hi + B_mid + B_lo) + A_lo (B_hi + B_mid); A_lo B_lo is below 2^-24)
+// with FP32 accumulation in TMEM; the accumulator is drained into registers
+// every 1024 reduction elements and added there with round-to-nearest (the
+// tensor-core accumulator truncates, gemm_tc.cu).
 //
 // Kernel: persistent, one CTA per SM, over work items (128-row tile, f).  Warp
 // 0 lane 0 drives a TMA ring (A high halves 128B-swizzled, A low bytes
@@ -54,7 +57,7 @@ constexpr int TC_THREADS = (2 + TC_CONV_WARPS + TC_DRAIN_WARPS) * 32;
 constexpr int kErrTimeoutSpecTc = 3;
 
 struct SpecTcMaps {
-    CUtensorMap ahi, alo, bhi, blo;
+    CUtensorMap ahi, alo, bhi, bmi, blo;
 };
 
 template <int BN, int STAGES>
@@ -65,10 +68,11 @@ struct SpecTcSmem {
     static constexpr int LO8 = TC_BM * TC_BK;      // 8 KB: low bytes, row-major
     static constexpr int OFF_ALO = AHI;
     static constexpr int OFF_BHI = AHI + ALO;
-    static constexpr int OFF_BLO = OFF_BHI + B;
+    static constexpr int OFF_BMI = OFF_BHI + B;
+    static constexpr int OFF_BLO = OFF_BMI + B;
     static constexpr int OFF_LO8 = OFF_BLO + B;
     static constexpr int STAGE = OFF_LO8 + LO8;
-    static constexpr int TMA_BYTES = AHI + 2 * B + LO8;
+    static constexpr int TMA_BYTES = AHI + 3 * B + LO8;
     static constexpr int TOTAL = STAGES * STAGE + 1024;
     static_assert(B % 1024 == 0 && STAGE % 1024 == 0, "stage tiles must stay 1024-byte aligned");
     static_assert(TOTAL <= 227 * 1024, "stages exceed the shared memory of one CTA");
@@ -159,6 +163,7 @@ k_spec_tc(const __grid_constant__ SpecTcMaps maps, int rows, int nkb, int nmt, i
                     tma_load_3d(st, &maps.ahi, kb * TC_BK, mt * TC_BM, f, &full[s]);
                     tma_load_3d(st + SM::OFF_LO8, &maps.alo, kb * TC_BK, mt * TC_BM, f, &full[s]);
                     tma_load_3d(st + SM::OFF_BHI, &maps.bhi, kb * TC_BK, 0, f, &full[s]);
+                    tma_load_3d(st + SM::OFF_BMI, &maps.bmi, kb * TC_BK, 0, f, &full[s]);
                     tma_load_3d(st + SM::OFF_BLO, &maps.blo, kb * TC_BK, 0, f, &full[s]);
                 }
                 if (*(volatile int*)&abort_flag) break;
@@ -184,15 +189,17 @@ k_spec_tc(const __grid_constant__ SpecTcMaps maps, int rows, int nkb, int nmt, i
                         if (!mbar_wait(&full[s], par, err) || !mbar_wait(&conv[s], par, err)) { ok = false; break; }
                         tc_fence_after();
                         const uint32_t ahi = smem_u32(tsm + s * SM::STAGE);
-                        const uint32_t alo = ahi + SM::OFF_ALO, bhi = ahi + SM::OFF_BHI, blo = ahi + SM::OFF_BLO;
+                        const uint32_t alo = ahi + SM::OFF_ALO, bhi = ahi + SM::OFF_BHI;
+                        const uint32_t bmi = ahi + SM::OFF_BMI, blo = ahi + SM::OFF_BLO;
 #pragma unroll
                         for (int kk = 0; kk < TC_BK / 16; ++kk) {
                             const uint32_t o = kk * 32;  // 16 elements inside the 128-byte swizzle row
                             mma_bf16(acc, smem_desc_sw128(ahi + o), smem_desc_sw128(bhi + o), idesc, first ? 0 : 1);
                             first = false;
+                            mma_bf16(acc, smem_desc_sw128(ahi + o), smem_desc_sw128(bmi + o), idesc, 1);
                             mma_bf16(acc, smem_desc_sw128(ahi + o), smem_desc_sw128(blo + o), idesc, 1);
                             mma_bf16(acc, smem_desc_sw128(alo + o), smem_desc_sw128(bhi + o), idesc, 1);
-                            mma_bf16(acc, smem_desc_sw128(alo + o), smem_desc_sw128(blo + o), idesc, 1);
+                            mma_bf16(acc, smem_desc_sw128(alo + o), smem_desc_sw128(bmi + o), idesc, 1);
                         }
                         mma_commit(&empty[s]);
                     }
@@ -312,12 +319,12 @@ __global__ void k_f24_transpose(const ushort2* __restrict__ h, const uchar2* __r
     }
 }
 
-// B operand planes [f][BN][2 * nch_pad] (BF16 hi and lo) from nb channel
+// B operand planes [f][BN][2 * nch_pad] (BF16 hi, mid and lo) from nb channel
 // spectra src[b][c][f] (c < nch); columns of volumes b >= nb and channels
 // c >= nch are zero.  ADJ selects the adjoint's column pattern.
 template <bool ADJ>
 __global__ void k_tc_pack(const float2* __restrict__ src, int nb, int nch, int nch_pad, int nf, int BN,
-                          uint32_t* __restrict__ bhi, uint32_t* __restrict__ blo)
+                          uint32_t* __restrict__ bhi, uint32_t* __restrict__ bmi, uint32_t* __restrict__ blo)
 {
     __shared__ float2 t[32][33];
     const int b = blockIdx.z;  // volume, < BN / 2
@@ -343,11 +350,16 @@ __global__ void k_tc_pack(const float2* __restrict__ src, int nb, int nch, int n
             x0 = col ? v.y : v.x;
             x1 = col ? -v.x : v.y;
         }
+        // x = hi + mid + lo: each remainder is exact in FP32
         const __nv_bfloat162 hi = __floats2bfloat162_rn(x0, x1);
         const float2 hf = __bfloat1622float2(hi);
-        const __nv_bfloat162 lo = __floats2bfloat162_rn(x0 - hf.x, x1 - hf.y);
+        const float r0 = x0 - hf.x, r1 = x1 - hf.y;
+        const __nv_bfloat162 mi = __floats2bfloat162_rn(r0, r1);
+        const float2 mf = __bfloat1622float2(mi);
+        const __nv_bfloat162 lo = __floats2bfloat162_rn(r0 - mf.x, r1 - mf.y);
         const int64_t o = ((int64_t)f * BN + 2 * b + col) * kp2 + c;
         bhi[o] = *reinterpret_cast<const uint32_t*>(&hi);
+        bmi[o] = *reinterpret_cast<const uint32_t*>(&mi);
         blo[o] = *reinterpret_cast<const uint32_t*>(&lo);
     }
 }
@@ -398,8 +410,8 @@ int spectral_tc_max_volumes() { return kTcMaxVolumes; }
 
 // A maps: 24-bit planes (high halves as BF16, low bytes) of rows x kp elements
 // per frequency; B maps: BN x kp BF16 per frequency.
-static int tc_maps(SpecTcMaps* m, const void* ah, const void* al, const void* bh, const void* bl, int64_t rows,
-                   int64_t kp, int64_t nf, int bn)
+static int tc_maps(SpecTcMaps* m, const void* ah, const void* al, const void* bh, const void* bm, const void* bl,
+                   int64_t rows, int64_t kp, int64_t nf, int bn)
 {
     std::memset(m, 0, sizeof(*m));
     const uint64_t da[3] = {(uint64_t)kp, (uint64_t)rows, (uint64_t)nf};
@@ -412,6 +424,7 @@ static int tc_maps(SpecTcMaps* m, const void* ah, const void* al, const void* bh
     const uint64_t sb[2] = {(uint64_t)(kp * 2), (uint64_t)(bn * kp * 2)};
     const uint32_t boxb[3] = {TC_BK, (uint32_t)bn, 1};
     SID_TRY(encode_tmap_3d(&m->bhi, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, bh, db, sb, boxb, CU_TENSOR_MAP_SWIZZLE_128B));
+    SID_TRY(encode_tmap_3d(&m->bmi, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, bm, db, sb, boxb, CU_TENSOR_MAP_SWIZZLE_128B));
     SID_TRY(encode_tmap_3d(&m->blo, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, bl, db, sb, boxb, CU_TENSOR_MAP_SWIZZLE_128B));
     return SID_OK;
 }
@@ -445,27 +458,26 @@ static int tc_contract(sid_plan* p, bool adj, const float2* src, int nb, int64_t
     const int bn = nb <= 32 ? 64 : 128;
     const int64_t kp = 2 * nch_pad, nf = p->nf;
     const size_t plane = (size_t)(nf * bn * kp);  // BF16 elements of one B plane
-    SID_TRY(p->tcb.alloc(2 * plane * sizeof(uint16_t)));
+    SID_TRY(p->tcb.alloc(3 * plane * sizeof(uint16_t)));
     SID_TRY(p->tco.alloc((size_t)(nf * nb * rows) * sizeof(float2)));
     uint16_t* bh = p->tcb.as<uint16_t>();
-    uint16_t* bl = bh + plane;
+    uint16_t* bm = bh + plane;
+    uint16_t* bl = bm + plane;
     {
         dim3 grid((unsigned)cdiv(nch_pad, 32), (unsigned)cdiv(nf, 32), (unsigned)(bn / 2));
-        if (adj)
-            k_tc_pack<true><<<grid, 256, 0, st>>>(src, nb, (int)nch, (int)nch_pad, (int)nf, bn,
-                                                   reinterpret_cast<uint32_t*>(bh), reinterpret_cast<uint32_t*>(bl));
-        else
-            k_tc_pack<false><<<grid, 256, 0, st>>>(src, nb, (int)nch, (int)nch_pad, (int)nf, bn,
-                                                    reinterpret_cast<uint32_t*>(bh), reinterpret_cast<uint32_t*>(bl));
+        uint32_t *h = reinterpret_cast<uint32_t*>(bh), *m = reinterpret_cast<uint32_t*>(bm),
+                 *l = reinterpret_cast<uint32_t*>(bl);
+        if (adj) k_tc_pack<true><<<grid, 256, 0, st>>>(src, nb, (int)nch, (int)nch_pad, (int)nf, bn, h, m, l);
+        else k_tc_pack<false><<<grid, 256, 0, st>>>(src, nb, (int)nch, (int)nch_pad, (int)nf, bn, h, m, l);
         SID_CHECK_LAUNCH();
     }
     SpecTcMaps maps;
-    SID_TRY(tc_maps(&maps, ah, al, bh, bl, rows, kp, nf, bn));
+    SID_TRY(tc_maps(&maps, ah, al, bh, bm, bl, rows, kp, nf, bn));
     const int nkb = (int)cdiv(kp, TC_BK);
     p->timer.begin(st);
-    // stages: 4 x 56 KB (BN = 64) or 3 x 72 KB (BN = 128) of the 227 KB of shared memory
-    int rc = bn == 64 ? launch_spec_tc<64, 4>(maps, (int)rows, nkb, nf, nb, p->tco.as<float2>(), p->errflag.as<int>(), st)
-                      : launch_spec_tc<128, 3>(maps, (int)rows, nkb, nf, nb, p->tco.as<float2>(),
+    // stages: 3 x 64 KB (BN = 64) or 2 x 88 KB (BN = 128) of the 227 KB of shared memory
+    int rc = bn == 64 ? launch_spec_tc<64, 3>(maps, (int)rows, nkb, nf, nb, p->tco.as<float2>(), p->errflag.as<int>(), st)
+                      : launch_spec_tc<128, 2>(maps, (int)rows, nkb, nf, nb, p->tco.as<float2>(),
                                                p->errflag.as<int>(), st);
     p->timer.finish(st);
     SID_TRY(rc);
