@@ -20,6 +20,7 @@
 #include <cmath>
 #include <vector>
 
+#include "ptx.cuh"
 #include "sid_internal.cuh"
 
 namespace sid {
@@ -170,40 +171,48 @@ struct LibTileArgs {
 };
 
 // Tap-row form (the default; k_lib_project when the boxes span more than 3
-// lattice points per phase or the output window exceeds 32 lenslets).  One CTA per (group of up to G
-// neurons with the same depth window, output phase a'b'), one warp per neuron.
-// Lane = tap row m1 (the first D lanes), so a lane reads its own row of the
-// staged tap array K[abc][b'a'](m1, .) once per (c, b, a) -- DM/4 aligned
-// 16-byte loads into registers -- and applies it to every lattice point (u, v)
-// of the box at that phase: the point at relative offset (du, dv) = (u - umin,
-// v - vmin) adds V(u, v) K(m1, m2) to the output at relative row m1 + du and
-// column m2 + dv, which the lane keeps in registers acc[du][m2 + dv].  A tap
-// load serves up to R x R lattice points, and lattice points outside the box
-// (or zero) cost nothing.  At the end the rows are
-// summed across lanes (row r = sum over du of lane r - du's acc[du]).
-template <int G, int DM, int R>
-__global__ void __launch_bounds__(32 * G, 1)
+// lattice points per phase or the output window exceeds 32 lenslets).  One
+// CTA per (group of up to G neurons with the same depth window, output phase
+// a'b'), two warps per neuron, each taking one half (WH columns) of the tap
+// array.  Lane = tap row m1 (the first D lanes), so a lane reads its half row
+// of K[abc][b'a'](m1, .) once per (c, b, a) -- WH/4 aligned 16-byte loads into
+// registers -- and applies it to every lattice point (u, v) of the box at that
+// phase: the point at relative offset (du, dv) = (u - umin, v - vmin) adds
+// V(u, v) K(m1, m2) to the output at relative row m1 + du and column m2 + dv,
+// kept in registers acc[du][m2 - half start + dv].  The box values of each
+// phase are staged as an R x R grid (zero outside the box), so a lattice point
+// costs one broadcast load and WH FMAs, and a zero costs a skipped branch.
+// At the end the rows are summed across lanes (row r = sum over du of lane
+// r - du's acc[du]) and the two halves, which overlap in R - 1 columns, are
+// added in shared memory before the output is written.
+template <int G, int WH, int R>
+__global__ void __launch_bounds__(64 * G, 1)
 k_lib_row(const float* __restrict__ taps, const float* __restrict__ packed, const LibBox* __restrict__ boxes,
           const int* __restrict__ groups, const LibTileArgs a, float* __restrict__ out)
 {
-    constexpr int NT = 32 * G;
+    constexpr int NT = 64 * G;
+    constexpr int DM = 2 * WH;                   // tap columns held (>= D)
     constexpr int RI = (32 * DM + NT - 1) / NT;  // tap copies per thread and tile (D * D <= 32 * DM)
-    constexpr int WC = DM + R - 1;               // output columns per lane
-    // tile row pitch: an odd multiple of 4 floats, so the 16-byte row loads of
+    constexpr int WC = WH + R - 1;               // output columns per lane
+    constexpr int VG = (R * R + 3) / 4 * 4;      // lattice grid values per (neuron, phase), padded to 16 bytes
+    // tile row pitch: an odd multiple of 4 floats, so the 16-byte loads of
     // eight consecutive lanes fall in distinct banks
     constexpr int TP = (DM / 4) % 2 ? DM : DM + 4;
-    extern __shared__ __align__(16) float sm[];  // 2 x N tiles of D x TP, 2 x G x R box rows, neuron tables
+    constexpr int OW = DM + R - 1;               // output tile width
+    extern __shared__ __align__(16) float sm[];  // 2 x N tiles of D x TP, 2 x G x N lattice grids, neuron tables
     const int N = a.N, D = a.D;
     const int tsz = D * TP;
-    float* vrows = sm + 2 * N * tsz;             // [buf][k][e][x - x0]: box rows of lattice row vlo + e at (c, b)
-    const int vstride = R * a.bwm;
-    int* tab = reinterpret_cast<int*>(vrows + 2 * G * vstride);
+    const int gstride = N * VG;                  // one neuron's grids for one (c, b)
+    // the tap tiles, later reused for the G output tiles of 32 x OW
+    const int tiles_sz = max(2 * N * tsz, G * 32 * OW);
+    float* vgrid = sm + tiles_sz;                // [buf][k][aa][du * R + dv]
+    int* tab = reinterpret_cast<int*>(vgrid + 2 * G * gstride);
     const int tstride = 8 + 4 * N;
     const int* grp = groups + blockIdx.x * (G + 1);
     const int cnt = grp[0];
     const int o = blockIdx.y;
     const int bp = o / N, ap = o - bp * N;
-    for (int i = threadIdx.x; i < 2 * N * tsz + 2 * G * vstride; i += blockDim.x) sm[i] = 0.f;
+    for (int i = threadIdx.x; i < 2 * N * tsz; i += blockDim.x) sm[i] = 0.f;
     for (int e = threadIdx.x; e < cnt * N; e += blockDim.x) {
         const int k = e / N, ph = e - k * N;
         const LibBox b = boxes[grp[1 + k]];
@@ -230,6 +239,7 @@ k_lib_row(const float* __restrict__ taps, const float* __restrict__ packed, cons
         const int r = threadIdx.x + NT * i;
         roff[i] = r < DD ? (r / D) * TP + (r % D) : -1;
     }
+    __syncthreads();  // tables before the first grid copies
     auto issue = [&](int st, int buf) {
         const int c = z0 + st / N, bb = st - (st / N) * N;
         const int64_t rowblk = ((int64_t)c * N + bb) * N;
@@ -240,25 +250,28 @@ k_lib_row(const float* __restrict__ taps, const float* __restrict__ packed, cons
             for (int i = 0; i < RI; ++i)
                 if (roff[i] >= 0) cp_async4_lib(dst0 + aa * tsz + roff[i], src + threadIdx.x + NT * i);
         }
-        float* vdst = vrows + buf * G * vstride;
-        for (int e2 = threadIdx.x; e2 < cnt * vstride; e2 += blockDim.x) {
-            const int k = e2 / vstride, r = e2 - k * vstride;
-            const int e = r / a.bwm, x = r - e * a.bwm;
+        // lattice grids: V(aa + N (umin + du), bb + N (vmin + dv), c) inside the box, else 0
+        float* gdst = vgrid + buf * G * gstride;
+        for (int e2 = threadIdx.x; e2 < cnt * gstride; e2 += blockDim.x) {
+            const int k = e2 / gstride, r = e2 - k * gstride;
+            const int aa = r / VG, q = r - aa * VG;
+            const int du = q / R, dv = q - (q / R) * R;
             const int* t = tab + k * tstride;
-            if (e < t[8 + 3 * N + bb] && x < t[3]) {
-                const int y = bb + N * (t[8 + 2 * N + bb] + e);
-                cp_async4_lib(vdst + e2, packed + t[5] + t[3] * ((y - t[1]) + t[4] * (c - t[2])) + x);
-            }
+            const int x = aa + N * (t[6] + du), y = bb + N * (t[7] + dv);
+            const int dx = x - t[0], dy = y - t[1];
+            const bool in = q < R * R && dx >= 0 && dx < t[3] && dy >= 0 && dy < t[4];
+            const float* src = packed + (in ? t[5] + dx + t[3] * (dy + t[4] * (c - t[2])) : 0);
+            cp_async4(gdst + e2, src, in);
         }
         asm volatile("cp.async.commit_group;" ::: "memory");
     };
-    const int k = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int k = warp >> 1, half = warp & 1;
     float acc[R][WC];
 #pragma unroll
     for (int du = 0; du < R; ++du)
 #pragma unroll
         for (int j = 0; j < WC; ++j) acc[du][j] = 0.f;
-    __syncthreads();  // zeroed tiles and tables before the first copies land
     issue(0, 0);
     for (int st = 0; st < nst; ++st) {
         if (st + 1 < nst) {
@@ -268,53 +281,42 @@ k_lib_row(const float* __restrict__ taps, const float* __restrict__ packed, cons
             asm volatile("cp.async.wait_group 0;" ::: "memory");
         }
         __syncthreads();
-        const int bb = st - (st / N) * N;
         if (k < cnt && lane < D) {
-            const int* t = tab + k * tstride;
-            const int nv = t[8 + 3 * N + bb];
-            if (nv > 0) {
-                const int dv0 = t[8 + 2 * N + bb] - t[7];
-                const float* vk = vrows + ((st & 1) * G + k) * vstride - t[0];
-                const float* trow = sm + (st & 1) * N * tsz + lane * TP;
-                for (int aa = 0; aa < N; ++aa) {
-                    const int nu = t[8 + N + aa];
-                    if (nu <= 0) continue;
-                    const int ulo = t[8 + aa], du0 = ulo - t[6];
-                    // lattice values of this phase at (du, dv), 0 outside the box
-                    float val[R][R];
+            const float* trow = sm + (st & 1) * N * tsz + lane * TP + half * WH;
+            const float* vg = vgrid + ((st & 1) * G + k) * gstride;
+            for (int aa = 0; aa < N; ++aa) {
+                float val[VG];
 #pragma unroll
-                    for (int du = 0; du < R; ++du)
-#pragma unroll
-                        for (int dv = 0; dv < R; ++dv) {
-                            const int iu = du - du0, iv = dv - dv0;
-                            val[du][dv] = (iu >= 0 && iu < nu && iv >= 0 && iv < nv)
-                                              ? vk[iv * a.bwm + aa + N * (ulo + iu)] : 0.f;
-                        }
-                    // this lane's tap row, DM/4 aligned 16-byte loads
-                    const float4* w4 = reinterpret_cast<const float4*>(trow + aa * tsz);
-                    float w[DM];
-#pragma unroll
-                    for (int q = 0; q < DM / 4; ++q) {
-                        const float4 t4 = w4[q];
-                        w[4 * q] = t4.x; w[4 * q + 1] = t4.y; w[4 * q + 2] = t4.z; w[4 * q + 3] = t4.w;
-                    }
-#pragma unroll
-                    for (int du = 0; du < R; ++du)
-#pragma unroll
-                        for (int dv = 0; dv < R; ++dv) {
-                            const float vv = val[du][dv];
-                            if (vv != 0.f) {  // warp-uniform: one neuron and phase per warp
-#pragma unroll
-                                for (int m = 0; m < DM; ++m) acc[du][m + dv] = fmaf(w[m], vv, acc[du][m + dv]);
-                            }
-                        }
+                for (int q = 0; q < VG / 4; ++q) {
+                    const float4 v4 = reinterpret_cast<const float4*>(vg + aa * VG)[q];
+                    val[4 * q] = v4.x; val[4 * q + 1] = v4.y; val[4 * q + 2] = v4.z; val[4 * q + 3] = v4.w;
                 }
+                bool any = false;
+#pragma unroll
+                for (int q = 0; q < R * R; ++q) any |= val[q] != 0.f;
+                if (!any) continue;  // warp-uniform: one neuron per warp
+                float w[WH];
+                const float4* w4 = reinterpret_cast<const float4*>(trow + aa * tsz);
+#pragma unroll
+                for (int q = 0; q < WH / 4; ++q) {
+                    const float4 t4 = w4[q];
+                    w[4 * q] = t4.x; w[4 * q + 1] = t4.y; w[4 * q + 2] = t4.z; w[4 * q + 3] = t4.w;
+                }
+#pragma unroll
+                for (int du = 0; du < R; ++du)
+#pragma unroll
+                    for (int dv = 0; dv < R; ++dv) {
+                        const float vv = val[du * R + dv];
+                        if (vv != 0.f) {
+#pragma unroll
+                            for (int m = 0; m < WH; ++m) acc[du][m + dv] = fmaf(w[m], vv, acc[du][m + dv]);
+                        }
+                    }
             }
         }
         __syncthreads();  // this buffer is refilled by the next-but-one copy
     }
-    if (k >= cnt) return;
-    // output row r (relative) = sum over du of lane r - du's acc[du]
+    // rows summed across lanes, then the two halves added in shared memory
     float res[WC];
 #pragma unroll
     for (int j = 0; j < WC; ++j) res[j] = acc[0][j];
@@ -325,50 +327,53 @@ k_lib_row(const float* __restrict__ taps, const float* __restrict__ packed, cons
             const float v = __shfl_up_sync(0xffffffffu, acc[du][j], du);
             if (lane >= du) res[j] += v;
         }
-    const int n = grp[1 + k];
-    const int* t = tab + k * tstride;
-    if (lane >= D + R - 1) return;
-    const int s = t[6] + a.dlo + lane;
-    if (s < 0 || s >= a.Lx) return;
-    const int64_t x = ap + (int64_t)N * s;
-    if (x >= a.X) return;
+    float* otile = sm + k * 32 * OW;  // [row][OW] per neuron (the tap tiles are no longer read)
+    for (int i = threadIdx.x; i < G * 32 * OW; i += blockDim.x) sm[i] = 0.f;
+    __syncthreads();
+    if (k < cnt) {
 #pragma unroll
-    for (int j = 0; j < WC; ++j) {
-        const int tt = t[7] + a.dlo + j;
-        if (j >= a.Wt || tt < 0 || tt >= a.Ly) continue;
-        const int64_t y = bp + (int64_t)N * tt;
-        if (y < a.Y) out[(int64_t)n * a.ldn + (x + a.X * y) * a.ldp] = res[j];
+        for (int j = 0; j < WC; ++j) atomicAdd(otile + lane * OW + half * WH + j, res[j]);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < cnt * 32 * OW; i += blockDim.x) {
+        const int kk = i / (32 * OW), r = i - kk * 32 * OW;
+        const int row = r / OW, col = r - row * OW;
+        if (row >= D + R - 1 || col >= a.Wt) continue;
+        const int* t = tab + kk * tstride;
+        const int s = t[6] + a.dlo + row, tt = t[7] + a.dlo + col;
+        if (s < 0 || s >= a.Lx || tt < 0 || tt >= a.Ly) continue;
+        const int64_t x = ap + (int64_t)N * s, y = bp + (int64_t)N * tt;
+        if (x < a.X && y < a.Y) out[(int64_t)grp[1 + kk] * a.ldn + (x + a.X * y) * a.ldp] = sm[i];
     }
 }
 
-constexpr int kLibRowG = 8;  // neurons (warps) per CTA of the tap-row form
+constexpr int kLibRowG = 8;  // neurons per CTA of the tap-row form (two warps each)
 
-// tap columns held per lane (the tap extent rounded up to 4) and its tile pitch
-static int lib_row_dm(int D) { return D <= 16 ? 16 : (D <= 24 ? 24 : (D <= 28 ? 28 : 32)); }
+// half of the tap columns held per lane (the tap extent rounded up to 8, halved) and the tile pitch
+static int lib_row_wh(int D) { return D <= 16 ? 8 : (D <= 24 ? 12 : 16); }
 static int lib_row_pitch(int dm) { return (dm / 4) % 2 ? dm : dm + 4; }
 
-template <int DM, int R>
+template <int WH, int R>
 static int launch_lib_row_t(dim3 grid, size_t smem, const float* taps, const float* packed, const LibBox* boxes,
                             const int* groups, const LibTileArgs& a, float* out, cudaStream_t st)
 {
-    SID_CUDA_TRY(cudaFuncSetAttribute(k_lib_row<kLibRowG, DM, R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    SID_CUDA_TRY(cudaFuncSetAttribute(k_lib_row<kLibRowG, WH, R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)smem));
-    k_lib_row<kLibRowG, DM, R><<<grid, 32 * kLibRowG, smem, st>>>(taps, packed, boxes, groups, a, out);
+    k_lib_row<kLibRowG, WH, R><<<grid, 64 * kLibRowG, smem, st>>>(taps, packed, boxes, groups, a, out);
     SID_CHECK_LAUNCH();
     return SID_OK;
 }
 
-static int launch_lib_row(int dm, int r, dim3 grid, size_t smem, const float* taps, const float* packed,
+static int launch_lib_row(int wh, int r, dim3 grid, size_t smem, const float* taps, const float* packed,
                           const LibBox* boxes, const int* groups, const LibTileArgs& a, float* out, cudaStream_t st)
 {
-#define SID_LIB_ROW(D_, R_) \
-    if (dm == D_ && r == R_) return launch_lib_row_t<D_, R_>(grid, smem, taps, packed, boxes, groups, a, out, st);
+#define SID_LIB_ROW(W_, R_) \
+    if (wh == W_ && r == R_) return launch_lib_row_t<W_, R_>(grid, smem, taps, packed, boxes, groups, a, out, st);
+    SID_LIB_ROW(8, 1) SID_LIB_ROW(8, 2) SID_LIB_ROW(8, 3)
+    SID_LIB_ROW(12, 1) SID_LIB_ROW(12, 2) SID_LIB_ROW(12, 3)
     SID_LIB_ROW(16, 1) SID_LIB_ROW(16, 2) SID_LIB_ROW(16, 3)
-    SID_LIB_ROW(24, 1) SID_LIB_ROW(24, 2) SID_LIB_ROW(24, 3)
-    SID_LIB_ROW(28, 1) SID_LIB_ROW(28, 2) SID_LIB_ROW(28, 3)
-    SID_LIB_ROW(32, 1) SID_LIB_ROW(32, 2) SID_LIB_ROW(32, 3)
 #undef SID_LIB_ROW
-    set_error("sid_library: no tap-row kernel for %d tap columns x %d lattice offsets", dm, r);
+    set_error("sid_library: no tap-row kernel for %d tap columns x %d lattice offsets", 2 * wh, r);
     return SID_EINVAL;
 }
 
@@ -450,9 +455,10 @@ extern "C" int sid_library(sid_plan* p, const float* const* recon, int64_t n_com
     ta.W = (int)D + span; ta.Wt = (int)D + span;
     ta.bwm = bwm;
     // tap-row kernel: lanes = tap rows, output window rows D + span <= 32, lattice offsets span + 1 <= 3
-    const int rdm = lib_row_dm((int)D), rtp = lib_row_pitch(rdm);
-    const size_t row_bytes = (size_t)(2 * N * D * rtp + 2 * kLibRowG * (span + 1) * bwm) * sizeof(float) +
-                             (size_t)kLibRowG * (8 + 4 * N) * sizeof(int);
+    const int rwh = lib_row_wh((int)D), rtp = lib_row_pitch(2 * rwh), rvg = ((span + 1) * (span + 1) + 3) / 4 * 4;
+    const size_t row_bytes =
+        (size_t)std::max<int64_t>(2 * N * D * rtp, (int64_t)kLibRowG * 32 * (2 * rwh + span)) * sizeof(float) +
+        (size_t)(2 * kLibRowG * N * rvg) * sizeof(float) + (size_t)kLibRowG * (8 + 4 * N) * sizeof(int);
     const bool rowk = D <= 32 && D + span <= 32 && span + 1 <= 3 && nrv >= 1 && row_bytes <= 200 * 1024;
     const int gsz = rowk ? kLibRowG : kLibG;
     const int Dp = (int)D + 2 * span;
@@ -503,7 +509,7 @@ extern "C" int sid_library(sid_plan* p, const float* const* recon, int64_t n_com
     dim3 grid((unsigned)ngroups, (unsigned)(N * N));
     if (rowk) {
         ta.tbs = tbs; ta.Lx = (int)p->Lx; ta.Ly = (int)p->Ly; ta.X = p->X; ta.Y = p->Y; ta.ldn = ldn; ta.ldp = ldp;
-        SID_TRY(launch_lib_row(rdm, span + 1, grid, row_bytes, p->taps_f.as<float>(), dpack.as<float>(),
+        SID_TRY(launch_lib_row(rwh, span + 1, grid, row_bytes, p->taps_f.as<float>(), dpack.as<float>(),
                                dbox.as<LibBox>(), dgrp.as<int>(), ta, out, st));
     } else {
         SID_CUDA_TRY(cudaFuncSetAttribute(k_lib_project<kLibG>, cudaFuncAttributeMaxDynamicSharedMemorySize,
