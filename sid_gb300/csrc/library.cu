@@ -7,12 +7,12 @@
 // contribute nothing, so the row equals the full-depth forward projection of
 // the boxed volume.  Here every neuron is one batch entry of one launch:
 //   1. k_lib_average: the boxed, averaged sub-volumes (packed, one per neuron);
-//   2. k_lib_row (k_lib_project for very wide boxes): one CTA per (group of
-//      neurons sharing a depth window, output phase a'b'); per box channel
-//      (a,b,c) the D x D tap array K[abc][b'a'] is staged in shared memory once
-//      for the whole group and applied to every box's lattice points of that
-//      phase (the same lenslet-tap algebra as direct.cu), so only the boxes'
-//      own channels are visited;
+//   2. k_lib_project: one CTA per (group of neurons sharing a depth window,
+//      output phase a'b'); threads own the output lenslets around each box; per
+//      box channel (a,b,c) the D x D tap array K[abc][b'a'] is staged in shared
+//      memory once for the whole group and applied to every box's lattice
+//      points of that phase (the same lenslet-tap algebra as direct.cu), so
+//      only the boxes' own channels are visited;
 //   3. the rest of each row is zero (one memset of the output).
 // Box and window arithmetic (MATLAB round, clipping at 1 and the volume size,
 // ceil(neur_rad/axial)) is done on the host, bit-exact with the reference.
@@ -20,7 +20,6 @@
 #include <cmath>
 #include <vector>
 
-#include "ptx.cuh"
 #include "sid_internal.cuh"
 
 namespace sid {
@@ -155,6 +154,25 @@ k_lib_project(const float* __restrict__ taps, const float* __restrict__ packed, 
     }
 }
 
+// Tiled form (the default).  One CTA per (group of up to G neurons with the
+// same depth window, output phase a'b').  Every neuron's output window has the
+// same shape, W rows (s) x NTB*TB columns (t) of output lenslets starting at
+// (umin + dlo, vmin + dlo) with (umin, vmin) the first lenslet its box touches,
+// so a box lattice point (u, v) lands at a relative offset (ru, rv) = (u -
+// umin, v - vmin) in [0, span]^2 and the tap it meets at relative output (ds,
+// dt) is K(ds - ru, dt - rv).  Per depth c and input row phase b the N tap
+// arrays K[abc][b'a'] of all input column phases a are copied (cp.async,
+// double-buffered: the next (c, b) row is in flight while this one is used)
+// into zero-bordered shared tiles with an odd row pitch.  Lane = output row ds,
+// so the 32 lanes of a warp read 32 different tile rows (distinct banks); each
+// warp owns (neuron, block of TB output columns) pairs.  For each lattice row
+// ru of a box phase, a lane loads TB + NRV - 1 consecutive taps of its tile row
+// into registers once and applies them to the NRV lattice columns rv of that
+// row: TB + NRV - 1 shared loads for NRV * TB FMAs, and only the boxes' own
+// lattice points are visited.  TB (the template's column count, >= the
+// window's width) is the whole row, so one (warp, neuron) pair covers a
+// neuron's window and the per-phase bookkeeping is paid once per row.
+
 __device__ __forceinline__ void cp_async4_lib(float* dst, const float* src)
 {
     asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)),
@@ -163,56 +181,36 @@ __device__ __forceinline__ void cp_async4_lib(float* dst, const float* src)
 }
 
 struct LibTileArgs {
-    int N, D, dlo, span, W, Wt;  // output windows of W x Wt lenslets (D + span)
+    int N, D, dlo, span, W, Wt, rows, pitch, cb, tsz;
     int bwm;  // widest box (x extent) of any neuron: the staged lattice rows hold bwm floats
     int64_t tbs;
     int Lx, Ly;
     int64_t X, Y, ldn, ldp;
 };
 
-// Tap-row form (the default; k_lib_project when the boxes span more than 3
-// lattice points per phase or the output window exceeds 32 lenslets).  One
-// CTA per (group of up to G neurons with the same depth window, output phase
-// a'b'), two warps per neuron, each taking one half (WH columns) of the tap
-// array.  Lane = tap row m1 (the first D lanes), so a lane reads its half row
-// of K[abc][b'a'](m1, .) once per (c, b, a) -- WH/4 aligned 16-byte loads into
-// registers -- and applies it to every lattice point (u, v) of the box at that
-// phase: the point at relative offset (du, dv) = (u - umin, v - vmin) adds
-// V(u, v) K(m1, m2) to the output at relative row m1 + du and column m2 + dv,
-// kept in registers acc[du][m2 - half start + dv].  The box values of each
-// phase are staged as an R x R grid (zero outside the box), so a lattice point
-// costs one broadcast load and WH FMAs, and a zero costs a skipped branch.
-// At the end the rows are summed across lanes (row r = sum over du of lane
-// r - du's acc[du]) and the two halves, which overlap in R - 1 columns, are
-// added in shared memory before the output is written.
-template <int G, int WH, int R>
-__global__ void __launch_bounds__(64 * G, 1)
-k_lib_row(const float* __restrict__ taps, const float* __restrict__ packed, const LibBox* __restrict__ boxes,
-          const int* __restrict__ groups, const LibTileArgs a, float* __restrict__ out)
+template <int G, int TB, int NRV>
+__global__ void __launch_bounds__(32 * G, 16 / G)
+k_lib_tile(const float* __restrict__ taps, const float* __restrict__ packed, const LibBox* __restrict__ boxes,
+           const int* __restrict__ groups, const LibTileArgs a, float* __restrict__ out)
 {
-    constexpr int NT = 64 * G;
-    constexpr int DM = 2 * WH;                   // tap columns held (>= D)
-    constexpr int RI = (32 * DM + NT - 1) / NT;  // tap copies per thread and tile (D * D <= 32 * DM)
-    constexpr int WC = WH + R - 1;               // output columns per lane
-    constexpr int VG = (R * R + 3) / 4 * 4;      // lattice grid values per (neuron, phase), padded to 16 bytes
-    // tile row pitch: an odd multiple of 4 floats, so the 16-byte loads of
-    // eight consecutive lanes fall in distinct banks
-    constexpr int TP = (DM / 4) % 2 ? DM : DM + 4;
-    constexpr int OW = DM + R - 1;               // output tile width
-    extern __shared__ __align__(16) float sm[];  // 2 x N tiles of D x TP, 2 x G x N lattice grids, neuron tables
-    const int N = a.N, D = a.D;
-    const int tsz = D * TP;
-    const int gstride = N * VG;                  // one neuron's grids for one (c, b)
-    // the tap tiles, later reused for the G output tiles of 32 x OW
-    const int tiles_sz = max(2 * N * tsz, G * 32 * OW);
-    float* vgrid = sm + tiles_sz;                // [buf][k][aa][du * R + dv]
-    int* tab = reinterpret_cast<int*>(vgrid + 2 * G * gstride);
+    constexpr int NTB = 1;
+    constexpr int NWARP = G;                // one warp per neuron of the group
+    constexpr int NT = 32 * NWARP;
+    constexpr int PPW = (G * NTB + NWARP - 1) / NWARP;  // (neuron, column block) pairs per warp
+    constexpr int RI = (768 + NT - 1) / NT;             // tap copies per thread and tile (D*D <= 768)
+    constexpr int NW = TB + NRV - 1;        // taps held per lattice row
+    extern __shared__ float sm[];           // 2 x N tiles of rows x pitch, 2 x G x NRV box rows, neuron tables
+    const int N = a.N, D = a.D, tsz = a.tsz;
+    float* vrows = sm + 2 * N * tsz;        // [buf][k][e][x - x0]: the box rows of lattice row vlo + e at (c, b)
+    const int vstride = NRV * a.bwm;
+    int* tab = reinterpret_cast<int*>(vrows + 2 * G * vstride);
+    // per neuron k: [0] x0 [1] y0 [2] z0 [3] bw [4] bh [5] off [6] umin [7] vmin, then ulo[N], nu[N], vlo[N], nv[N]
     const int tstride = 8 + 4 * N;
     const int* grp = groups + blockIdx.x * (G + 1);
     const int cnt = grp[0];
     const int o = blockIdx.y;
     const int bp = o / N, ap = o - bp * N;
-    for (int i = threadIdx.x; i < 2 * N * tsz; i += blockDim.x) sm[i] = 0.f;
+    for (int i = threadIdx.x; i < 2 * N * tsz + 2 * G * vstride; i += blockDim.x) sm[i] = 0.f;
     for (int e = threadIdx.x; e < cnt * N; e += blockDim.x) {
         const int k = e / N, ph = e - k * N;
         const LibBox b = boxes[grp[1 + k]];
@@ -221,6 +219,7 @@ k_lib_row(const float* __restrict__ taps, const float* __restrict__ packed, cons
             t[0] = b.x0; t[1] = b.y0; t[2] = b.z0; t[3] = b.x1 - b.x0; t[4] = b.y1 - b.y0; t[5] = b.off;
             t[6] = b.x0 / N; t[7] = b.y0 / N;
         }
+        // lattice u of column phase ph inside [x0, x1): x = ph + N u
         const int ulo = b.x0 > ph ? (b.x0 - ph + N - 1) / N : 0;
         const int uhi = (b.x1 - 1 - ph) >= 0 ? (b.x1 - 1 - ph) / N : -1;
         const int vlo = b.y0 > ph ? (b.y0 - ph + N - 1) / N : 0;
@@ -233,13 +232,13 @@ k_lib_row(const float* __restrict__ taps, const float* __restrict__ packed, cons
     const int z0 = boxes[grp[1]].z0, z1 = boxes[grp[1]].z1;
     const int nst = (z1 - z0) * N;
     const int DD = D * D;
+    // this thread's tap copies: r = tid + NT i, i < RI covers D*D <= 768
     int roff[RI];
 #pragma unroll
     for (int i = 0; i < RI; ++i) {
         const int r = threadIdx.x + NT * i;
-        roff[i] = r < DD ? (r / D) * TP + (r % D) : -1;
+        roff[i] = r < DD ? (r / D + a.span) * a.pitch + (r % D) + a.cb : -1;
     }
-    __syncthreads();  // tables before the first grid copies
     auto issue = [&](int st, int buf) {
         const int c = z0 + st / N, bb = st - (st / N) * N;
         const int64_t rowblk = ((int64_t)c * N + bb) * N;
@@ -250,28 +249,26 @@ k_lib_row(const float* __restrict__ taps, const float* __restrict__ packed, cons
             for (int i = 0; i < RI; ++i)
                 if (roff[i] >= 0) cp_async4_lib(dst0 + aa * tsz + roff[i], src + threadIdx.x + NT * i);
         }
-        // lattice grids: V(aa + N (umin + du), bb + N (vmin + dv), c) inside the box, else 0
-        float* gdst = vgrid + buf * G * gstride;
-        for (int e2 = threadIdx.x; e2 < cnt * gstride; e2 += blockDim.x) {
-            const int k = e2 / gstride, r = e2 - k * gstride;
-            const int aa = r / VG, q = r - aa * VG;
-            const int du = q / R, dv = q - (q / R) * R;
+        // each neuron's box rows y = bb + N (vlo + e), e < nv, at depth c (bw contiguous floats each)
+        float* vdst = vrows + buf * G * vstride;
+        for (int e2 = threadIdx.x; e2 < cnt * vstride; e2 += blockDim.x) {
+            const int k = e2 / vstride, r = e2 - k * vstride;
+            const int e = r / a.bwm, x = r - e * a.bwm;
             const int* t = tab + k * tstride;
-            const int x = aa + N * (t[6] + du), y = bb + N * (t[7] + dv);
-            const int dx = x - t[0], dy = y - t[1];
-            const bool in = q < R * R && dx >= 0 && dx < t[3] && dy >= 0 && dy < t[4];
-            const float* src = packed + (in ? t[5] + dx + t[3] * (dy + t[4] * (c - t[2])) : 0);
-            cp_async4(gdst + e2, src, in);
+            if (e < t[8 + 3 * N + bb] && x < t[3]) {
+                const int y = bb + N * (t[8 + 2 * N + bb] + e);
+                cp_async4_lib(vdst + e2, packed + t[5] + t[3] * ((y - t[1]) + t[4] * (c - t[2])) + x);
+            }
         }
         asm volatile("cp.async.commit_group;" ::: "memory");
     };
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int k = warp >> 1, half = warp & 1;
-    float acc[R][WC];
+    const int warp = threadIdx.x >> 5, ds = threadIdx.x & 31;
+    float acc[PPW][TB];
 #pragma unroll
-    for (int du = 0; du < R; ++du)
+    for (int q = 0; q < PPW; ++q)
 #pragma unroll
-        for (int j = 0; j < WC; ++j) acc[du][j] = 0.f;
+        for (int j = 0; j < TB; ++j) acc[q][j] = 0.f;
+    __syncthreads();  // zeroed tiles and tables before the first copies land
     issue(0, 0);
     for (int st = 0; st < nst; ++st) {
         if (st + 1 < nst) {
@@ -281,99 +278,97 @@ k_lib_row(const float* __restrict__ taps, const float* __restrict__ packed, cons
             asm volatile("cp.async.wait_group 0;" ::: "memory");
         }
         __syncthreads();
-        if (k < cnt && lane < D) {
-            const float* trow = sm + (st & 1) * N * tsz + lane * TP + half * WH;
-            const float* vg = vgrid + ((st & 1) * G + k) * gstride;
-            for (int aa = 0; aa < N; ++aa) {
-                float val[VG];
+        const int c = z0 + st / N, bb = st - (st / N) * N;
+        const float* tb0 = sm + (st & 1) * N * tsz;
+        if (ds < a.W) {
 #pragma unroll
-                for (int q = 0; q < VG / 4; ++q) {
-                    const float4 v4 = reinterpret_cast<const float4*>(vg + aa * VG)[q];
-                    val[4 * q] = v4.x; val[4 * q + 1] = v4.y; val[4 * q + 2] = v4.z; val[4 * q + 3] = v4.w;
-                }
-                bool any = false;
+            for (int q = 0; q < PPW; ++q) {
+                const int pr = warp + NWARP * q;
+                const int k = pr / NTB, tbk = pr - (pr / NTB) * NTB;
+                if (k >= cnt) continue;
+                const int* t = tab + k * tstride;
+                const int nv = t[8 + 3 * N + bb];
+                if (nv <= 0) continue;
+                const int vlo = t[8 + 2 * N + bb], rvlo = vlo - t[7];
+                // the staged box rows of this neuron: V(x, bb + N (vlo + e), c) at vk[e * bwm + x - x0]
+                const float* vk = vrows + ((st & 1) * G + k) * vstride - t[0];
+                const int colb = tbk * TB - rvlo - (NRV - 1) + a.cb;
+                for (int aa = 0; aa < N; ++aa) {
+                    const int nu = t[8 + N + aa];
+                    if (nu <= 0) continue;
+                    const int ulo = t[8 + aa];
+                    const float* tile = tb0 + aa * tsz;
+                    for (int iu = 0; iu < nu; ++iu) {
+                        const int u = ulo + iu;
+                        const int row = ds - (u - t[6]) + a.span;
+                        const float* wp = tile + row * a.pitch + colb;
+                        float w[NW];
 #pragma unroll
-                for (int q = 0; q < R * R; ++q) any |= val[q] != 0.f;
-                if (!any) continue;  // warp-uniform: one neuron per warp
-                float w[WH];
-                const float4* w4 = reinterpret_cast<const float4*>(trow + aa * tsz);
+                        for (int i = 0; i < NW; ++i) w[i] = wp[i];
+                        const float* vp = vk + aa + N * u;
 #pragma unroll
-                for (int q = 0; q < WH / 4; ++q) {
-                    const float4 t4 = w4[q];
-                    w[4 * q] = t4.x; w[4 * q + 1] = t4.y; w[4 * q + 2] = t4.z; w[4 * q + 3] = t4.w;
-                }
+                        for (int e = 0; e < NRV; ++e) {
+                            if (e < nv) {
+                                const float val = vp[e * a.bwm];
 #pragma unroll
-                for (int du = 0; du < R; ++du)
-#pragma unroll
-                    for (int dv = 0; dv < R; ++dv) {
-                        const float vv = val[du * R + dv];
-                        if (vv != 0.f) {
-#pragma unroll
-                            for (int m = 0; m < WH; ++m) acc[du][m + dv] = fmaf(w[m], vv, acc[du][m + dv]);
+                                for (int j = 0; j < TB; ++j) acc[q][j] = fmaf(val, w[j - e + NRV - 1], acc[q][j]);
+                            }
                         }
                     }
+                }
             }
         }
         __syncthreads();  // this buffer is refilled by the next-but-one copy
     }
-    // rows summed across lanes, then the two halves added in shared memory
-    float res[WC];
+    if (ds < a.W) {
 #pragma unroll
-    for (int j = 0; j < WC; ++j) res[j] = acc[0][j];
+        for (int q = 0; q < PPW; ++q) {
+            const int pr = warp + NWARP * q;
+            const int k = pr / NTB, tbk = pr - (pr / NTB) * NTB;
+            if (k >= cnt) continue;
+            const int n = grp[1 + k];
+            const int* t = tab + k * tstride;
+            const int s = t[6] + a.dlo + ds;
+            if (s < 0 || s >= a.Lx) continue;
+            const int64_t x = ap + (int64_t)N * s;
+            if (x >= a.X) continue;
 #pragma unroll
-    for (int du = 1; du < R; ++du)
-#pragma unroll
-        for (int j = 0; j < WC; ++j) {
-            const float v = __shfl_up_sync(0xffffffffu, acc[du][j], du);
-            if (lane >= du) res[j] += v;
+            for (int j = 0; j < TB; ++j) {
+                const int dt = tbk * TB + j;
+                const int tt = t[7] + a.dlo + dt;
+                if (dt >= a.Wt || tt < 0 || tt >= a.Ly) continue;
+                const int64_t y = bp + (int64_t)N * tt;
+                if (y < a.Y) out[(int64_t)n * a.ldn + (x + a.X * y) * a.ldp] = acc[q][j];
+            }
         }
-    float* otile = sm + k * 32 * OW;  // [row][OW] per neuron (the tap tiles are no longer read)
-    for (int i = threadIdx.x; i < G * 32 * OW; i += blockDim.x) sm[i] = 0.f;
-    __syncthreads();
-    if (k < cnt) {
-#pragma unroll
-        for (int j = 0; j < WC; ++j) atomicAdd(otile + lane * OW + half * WH + j, res[j]);
-    }
-    __syncthreads();
-    for (int i = threadIdx.x; i < cnt * 32 * OW; i += blockDim.x) {
-        const int kk = i / (32 * OW), r = i - kk * 32 * OW;
-        const int row = r / OW, col = r - row * OW;
-        if (row >= D + R - 1 || col >= a.Wt) continue;
-        const int* t = tab + kk * tstride;
-        const int s = t[6] + a.dlo + row, tt = t[7] + a.dlo + col;
-        if (s < 0 || s >= a.Lx || tt < 0 || tt >= a.Ly) continue;
-        const int64_t x = ap + (int64_t)N * s, y = bp + (int64_t)N * tt;
-        if (x < a.X && y < a.Y) out[(int64_t)grp[1 + kk] * a.ldn + (x + a.X * y) * a.ldp] = sm[i];
     }
 }
 
-constexpr int kLibRowG = 8;  // neurons per CTA of the tap-row form (two warps each)
-
-// half of the tap columns held per lane (the tap extent rounded up to 8, halved) and the tile pitch
-static int lib_row_wh(int D) { return D <= 16 ? 8 : (D <= 24 ? 12 : 16); }
-static int lib_row_pitch(int dm) { return (dm / 4) % 2 ? dm : dm + 4; }
-
-template <int WH, int R>
-static int launch_lib_row_t(dim3 grid, size_t smem, const float* taps, const float* packed, const LibBox* boxes,
-                            const int* groups, const LibTileArgs& a, float* out, cudaStream_t st)
+template <int TB, int NRV>
+static int launch_lib_tile_t(dim3 grid, size_t smem, const float* taps, const float* packed, const LibBox* boxes,
+                             const int* groups, const LibTileArgs& a, float* out, cudaStream_t st)
 {
-    SID_CUDA_TRY(cudaFuncSetAttribute(k_lib_row<kLibRowG, WH, R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    SID_CUDA_TRY(cudaFuncSetAttribute(k_lib_tile<kLibG, TB, NRV>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)smem));
-    k_lib_row<kLibRowG, WH, R><<<grid, 64 * kLibRowG, smem, st>>>(taps, packed, boxes, groups, a, out);
+    k_lib_tile<kLibG, TB, NRV><<<grid, 32 * kLibG, smem, st>>>(taps, packed, boxes, groups, a, out);
     SID_CHECK_LAUNCH();
     return SID_OK;
 }
 
-static int launch_lib_row(int wh, int r, dim3 grid, size_t smem, const float* taps, const float* packed,
-                          const LibBox* boxes, const int* groups, const LibTileArgs& a, float* out, cudaStream_t st)
+// output window columns per lane row, as a template: the smallest of 16, 24, 28, 32 that holds Wt
+static int tile_tb(int Wt) { return Wt <= 16 ? 16 : (Wt <= 24 ? 24 : (Wt <= 28 ? 28 : 32)); }
+
+static int launch_lib_tile(int tb, int nrv, dim3 grid, size_t smem, const float* taps, const float* packed,
+                           const LibBox* boxes, const int* groups, const LibTileArgs& a, float* out, cudaStream_t st)
 {
-#define SID_LIB_ROW(W_, R_) \
-    if (wh == W_ && r == R_) return launch_lib_row_t<W_, R_>(grid, smem, taps, packed, boxes, groups, a, out, st);
-    SID_LIB_ROW(8, 1) SID_LIB_ROW(8, 2) SID_LIB_ROW(8, 3)
-    SID_LIB_ROW(12, 1) SID_LIB_ROW(12, 2) SID_LIB_ROW(12, 3)
-    SID_LIB_ROW(16, 1) SID_LIB_ROW(16, 2) SID_LIB_ROW(16, 3)
-#undef SID_LIB_ROW
-    set_error("sid_library: no tap-row kernel for %d tap columns x %d lattice offsets", 2 * wh, r);
+#define SID_LIB_CASE(T, R) \
+    if (tb == T && nrv == R) return launch_lib_tile_t<T, R>(grid, smem, taps, packed, boxes, groups, a, out, st);
+    SID_LIB_CASE(16, 1) SID_LIB_CASE(16, 2) SID_LIB_CASE(16, 3)
+    SID_LIB_CASE(24, 1) SID_LIB_CASE(24, 2) SID_LIB_CASE(24, 3)
+    SID_LIB_CASE(28, 1) SID_LIB_CASE(28, 2) SID_LIB_CASE(28, 3)
+    SID_LIB_CASE(32, 1) SID_LIB_CASE(32, 2) SID_LIB_CASE(32, 3)
+#undef SID_LIB_CASE
+    set_error("sid_library: no tiled kernel for %d columns x %d lattice points", tb, nrv);
     return SID_EINVAL;
 }
 
@@ -449,22 +444,24 @@ extern "C" int sid_library(sid_plan* p, const float* const* recon, int64_t n_com
         boxes[n] = b;
     }
     SID_REQUIRE(off < INT32_MAX, "sid_library: boxes too large");
-    // output window of every neuron: (D + span) x (D + span) lenslets from (umin + dlo, vmin + dlo)
+    // tiled kernel: output windows of W x Wt lenslets, W <= 32 (one lane per row)
     LibTileArgs ta;
     ta.N = (int)N; ta.D = (int)D; ta.dlo = (int)p->g.dlo; ta.span = span;
     ta.W = (int)D + span; ta.Wt = (int)D + span;
+    const int tb = tile_tb(ta.Wt);
+    ta.rows = ta.W + span;
+    ta.cb = span + nrv - 1;
+    ta.pitch = (tb + ta.cb) | 1;  // odd: the 32 lanes' rows fall in distinct banks
+    ta.tsz = ta.rows * ta.pitch;
     ta.bwm = bwm;
-    // tap-row kernel: lanes = tap rows, output window rows D + span <= 32, lattice offsets span + 1 <= 3
-    const int rwh = lib_row_wh((int)D), rtp = lib_row_pitch(2 * rwh), rvg = ((span + 1) * (span + 1) + 3) / 4 * 4;
-    const size_t row_bytes =
-        (size_t)std::max<int64_t>(2 * N * D * rtp, (int64_t)kLibRowG * 32 * (2 * rwh + span)) * sizeof(float) +
-        (size_t)(2 * kLibRowG * N * rvg) * sizeof(float) + (size_t)kLibRowG * (8 + 4 * N) * sizeof(int);
-    const bool rowk = D <= 32 && D + span <= 32 && span + 1 <= 3 && nrv >= 1 && row_bytes <= 200 * 1024;
-    const int gsz = rowk ? kLibRowG : kLibG;
+    const size_t tiled_bytes = (size_t)(2 * N * ta.tsz + 2 * kLibG * std::max(nrv, 1) * bwm) * sizeof(float) +
+                               (size_t)kLibG * (8 + 4 * N) * sizeof(int);
+    const bool tiled = ta.W <= 32 && ta.Wt <= 32 && nrv >= 1 && nrv <= 3 && D * D <= 768 &&
+                       tiled_bytes <= 200 * 1024;
     const int Dp = (int)D + 2 * span;
     const size_t tile_bytes =
         (size_t)N * Dp * (Dp + kLibT) * sizeof(float) + (size_t)(D * D + 4 * N * kLibG) * sizeof(int);
-    if (!rowk) {
+    if (!tiled) {
         SID_REQUIRE(tile_bytes <= 200 * 1024, "sid_library: tap tiles (%zu bytes) exceed shared memory", tile_bytes);
         SID_REQUIRE(max_ns * ntgM <= 256, "sid_library: neuron radius too large for one CTA (%d output groups)",
                     max_ns * ntgM);
@@ -478,14 +475,14 @@ extern "C" int sid_library(sid_plan* p, const float* const* recon, int64_t n_com
     std::vector<int> groups;
     for (size_t i = 0; i < order.size();) {
         size_t e = i + 1;
-        while (e < order.size() && (int)(e - i) < gsz && boxes[order[e]].z0 == boxes[order[i]].z0 &&
+        while (e < order.size() && (int)(e - i) < kLibG && boxes[order[e]].z0 == boxes[order[i]].z0 &&
                boxes[order[e]].z1 == boxes[order[i]].z1)
             ++e;
         groups.push_back((int)(e - i));
-        for (size_t k = i; k < i + gsz; ++k) groups.push_back(k < e ? (int)order[k] : 0);
+        for (size_t k = i; k < i + kLibG; ++k) groups.push_back(k < e ? (int)order[k] : 0);
         i = e;
     }
-    const int64_t ngroups = (int64_t)groups.size() / (gsz + 1);
+    const int64_t ngroups = (int64_t)groups.size() / (kLibG + 1);
     DBuf& dbox = p->ws[3];
     DBuf& dpack = p->ws[2];
     DBuf& dmeta = p->ws[1];
@@ -507,10 +504,10 @@ extern "C" int sid_library(sid_plan* p, const float* const* recon, int64_t n_com
     const int64_t tbs = cdiv(N * D * D, 32) * 32;
     const int64_t ldn = out_layout == 0 ? 1 : P, ldp = out_layout == 0 ? n_neur : 1;
     dim3 grid((unsigned)ngroups, (unsigned)(N * N));
-    if (rowk) {
+    if (tiled) {
         ta.tbs = tbs; ta.Lx = (int)p->Lx; ta.Ly = (int)p->Ly; ta.X = p->X; ta.Y = p->Y; ta.ldn = ldn; ta.ldp = ldp;
-        SID_TRY(launch_lib_row(rwh, span + 1, grid, row_bytes, p->taps_f.as<float>(), dpack.as<float>(),
-                               dbox.as<LibBox>(), dgrp.as<int>(), ta, out, st));
+        SID_TRY(launch_lib_tile(tb, nrv, grid, tiled_bytes, p->taps_f.as<float>(), dpack.as<float>(),
+                                dbox.as<LibBox>(), dgrp.as<int>(), ta, out, st));
     } else {
         SID_CUDA_TRY(cudaFuncSetAttribute(k_lib_project<kLibG>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           (int)tile_bytes));

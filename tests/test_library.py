@@ -22,8 +22,8 @@ def test_boxes_bit_exact(sidlib, oracle):
 
 
 @pytest.mark.gpu
-# neur_rad 4 and 2: the tap-row kernel (boxes spanning 2 or 3 lattice points
-# per phase); 9: the generic kernel (boxes spanning 4-5)
+# neur_rad 4 and 2: the tiled kernel (boxes spanning 2 or 3 lattice points per
+# phase); 9: the generic kernel (boxes spanning 4-5)
 @pytest.mark.parametrize("rad", [4, 2, 9])
 def test_library_matches_oracle(gpu, oracle, rad):
     import sid_gb300 as s
