@@ -442,8 +442,9 @@ void sid_nmf_defaults(sid_nmf_opts* opts);
  * active: P uint8 (opts.active; NULL = every pixel); ymean: P single (opts.Y,
  * read with use_std).  S is written too: NaNs zeroed and, with lamb_corr > 0,
  * its columns rescaled by the norms of T's rows.  prec: precision of S'S and
- * S'Y (an FP16 movie always uses SID_PREC_SPLIT, whose power-of-two operand
- * scale is read back to the host: the call then waits for its stream). */
+ * S'Y (an FP16 movie always uses SID_PREC_SPLIT, with a power-of-two operand
+ * scale kept on the device).  No host round trip: the call can be captured in
+ * a CUDA graph once an ordinary call has sized its workspaces. */
 int sid_t_update(sid_ctx* ctx, const void* Y, int ydtype, float* T, float* S, int64_t P, int64_t R, int64_t F,
                  const uint8_t* active, const float* ymean, const sid_nmf_opts* opts, int prec, void* stream);
 /* [S, T] = S_update(Y, S, T, opts)   S_update.m:1
@@ -453,8 +454,9 @@ int sid_t_update(sid_ctx* ctx, const void* Y, int ydtype, float* T, float* S, in
  * prec: precision of the pixel-long products -- S'S (L2 orthogonality) and
  * the pixel-by-rank products Y*T', S*Q_T, v*Q_T, which at SID_PREC_SPLIT and
  * SID_PREC_BF16 run on the tensor cores (split: FP16 hi/lo of power-of-two
- * scaled operands, the scales read back to the host, so the call waits for
- * its stream) and at SID_PREC_FP32 on the FP32 SIMT GEMM. */
+ * scaled operands, the scales found, applied and undone on the device) and at
+ * SID_PREC_FP32 on the FP32 SIMT GEMM.  No host round trip: the call can be
+ * captured in a CUDA graph once an ordinary call has sized its workspaces. */
 int sid_s_update(sid_ctx* ctx, const void* Y, int ydtype, float* S, float* T, int64_t P, int64_t R, int64_t F,
                  const float* ymean, const float* hilf, const sid_nmf_opts* opts, int prec, void* stream);
 
