@@ -51,7 +51,7 @@ def parse():
     ap.add_argument("--nnls-frames", type=int, default=3000)
     ap.add_argument("--nnls-neurons", type=int, default=800)
     ap.add_argument("--no-demix", action="store_true", help="skip the demixing-loop measurement")
-    ap.add_argument("--batch-volumes", type=int, default=32,
+    ap.add_argument("--batch-volumes", type=int, default=64,
                     help="components deconvolved side by side in the batched measurement (0 skips it)")
     ap.add_argument("--demix-neurons", type=int, default=1500)
     ap.add_argument("--demix-frames", type=int, default=5000)
@@ -736,7 +736,8 @@ def main():
 
     # several components per pass over the tap spectra (reconstruct_S.m:162-212): nbv volumes, 3 ISRA
     # iterations each, against the same iterations one volume at a time.  With the tensor-core plan the
-    # mixed form contracts up to 32 volumes per pass (spec_tc.cu); other methods 4 per pass on the FP32 pipes.
+    # mixed form contracts up to 64 volumes per pass (spec_tc.cu, as many as the free device memory holds
+    # workspaces for); other methods 4 per pass on the FP32 pipes.
     batched = None
     if args.method.startswith("spectral") and args.batch_volumes > 1:
         nbv = args.batch_volumes
@@ -772,7 +773,9 @@ def main():
         if tc:
             # tensor-core contraction: launches alternate forward (rows 225, reduction 2 x 6976) and
             # back projection (rows 6976, reduction 2 x 232); 5 BF16 passes per MMA tile
-            g = min(nbv, 32)
+            # volumes per pass, from the launch count (two contractions per iteration and group)
+            groups = max(1, kb_n // 6)
+            g = -(-nbv // groups)
             bn = 64 if g <= 32 else 128
             nip = -(-n_in_ // 8) * 8
             op = -(-n_out_ // 8) * 8

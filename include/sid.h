@@ -46,7 +46,7 @@ enum {
 #define SID_PLAN_SPECTRAL_TC  0x10 /* with SPECTRAL_F24: a transposed copy of the 24-bit
                                      spectra, so that the batched calls
                                      (sid_*_batched) of SID_METHOD_SPECTRAL_MIXED
-                                     contract up to 32 volumes per pass on the tensor
+                                     contract up to 64 volumes per pass on the tensor
                                      cores, forward and back with the 24-bit spectra */
 
 /* Projection methods. */
@@ -159,7 +159,8 @@ int sid_deconv_isra_ex(sid_plan* plan, int method, const float* Htf, float* X, i
  * volumes per pass over the tap spectra on the FP32 pipes, so the spectra
  * stream once per four volumes, and the results equal nb single calls up to
  * FP32 rounding; on a plan built with SID_PLAN_SPECTRAL_TC the mixed form
- * contracts up to 32 volumes per pass on the tensor cores with the 24-bit
+ * contracts up to 64 volumes per pass (as many as the device memory holds
+ * workspaces for: 64, 32, 16 or 8) on the tensor cores with the 24-bit
  * spectra both ways (BF16 operand splits that carry them exactly, FP32
  * accumulation), within the mixed form's accuracy of the FP64 projections.
  * The direct form runs volume by volume.
@@ -412,8 +413,8 @@ int sid_reconstruct_component(sid_plan* plan, int method, const float* img, cons
                               const sid_recon_opts* opts, float* X, double* lamb_used, void* stream);
 /* The same for nc components (the components reconstruct_S.m:162-212 runs side
  * by side): imgs / X are host arrays of nc device pointers, lamb_used (optional,
- * host) nc values.  The back projections and the solver run on groups of up to
- * 32 components through sid_adjoint_batched and sid_deconv_ls_batched /
+ * host) nc values.  The back projections and the solver run on groups of
+ * components (up to 64 on the tensor cores, else 32) through sid_adjoint_batched and sid_deconv_ls_batched /
  * sid_deconv_isra_batched (on the tensor cores with a SID_PLAN_SPECTRAL_TC plan
  * and SID_METHOD_SPECTRAL_MIXED).  One stream synchronisation per group. */
 int sid_reconstruct_components(sid_plan* plan, int method, int64_t nc, const float* const* imgs,

@@ -331,7 +331,8 @@ extern "C" int sid_reconstruct_components(sid_plan* p, int method, int64_t nc, c
     SID_REQUIRE(o->max_iter >= 0, "sid_reconstruct_components: negative max_iter");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const int64_t nI = p->X * p->Y, nV = nI * p->Z;
-    const int64_t g = std::min<int64_t>(nc, 32);
+    const int64_t g = (p->spec_tc && method == SID_METHOD_SPECTRAL_MIXED) ? vol_group(p, method, nc)
+                                                                          : std::min<int64_t>(nc, 32);
     SID_TRY(p->ws[6].alloc((size_t)(g * nI) * sizeof(float)));
     SID_TRY(p->ws[8].alloc(quantile_work_bytes() + (size_t)(4 * g + 8) * sizeof(double)));
     if (o->solver == 1) SID_TRY(p->ws[7].alloc((size_t)(g * nV) * sizeof(float)));

@@ -217,6 +217,8 @@ int spectral_adjoint_batch(sid_plan* p, int fmt, const float* ip, float* bp, int
 // many volumes per pass on the tensor cores (spec_tc.cu; plan flag SID_PLAN_SPECTRAL_TC)
 int build_spectra_tc(sid_plan* p);
 int spectral_tc_max_volumes();
+int spectral_tc_group(const sid_plan* p, int64_t nb);  // volumes per pass that fit the device memory
+int64_t vol_group(const sid_plan* p, int method, int64_t nb);  // deconv.cu: volumes per batched pass
 int spectral_forward_tc(sid_plan* p, const float* vp, float* ip, int nb, cudaStream_t st);
 int spectral_adjoint_tc(sid_plan* p, const float* ip, float* bp, int nb, cudaStream_t st);
 // lenslet-grid real DFTs of nch channels (spectral.cu): planes [ch][Ly][Lx] <-> half spectra [ch][nf]

@@ -408,6 +408,40 @@ constexpr int kTcMaxVolumes = 64;
 
 int spectral_tc_max_volumes() { return kTcMaxVolumes; }
 
+// Device bytes a group of g volumes needs beyond the plan's operator data: the
+// solver's polyphase volumes (iterate, Htf, back projection) and images, the
+// channel spectra, the B operand planes and the contraction output.
+static int64_t tc_group_bytes(const sid_plan* p, int64_t g)
+{
+    const int64_t n_in = p->N * p->N * p->Z, n_out = p->N * p->N, n_in_pad = cdiv(n_in, 8) * 8;
+    const int64_t nv = n_out * p->Lx * p->Ly * p->Z, ni = n_out * p->Lx * p->Ly;
+    const int64_t bn = g <= 32 ? 64 : 128;
+    const int64_t per_vol = (3 * nv + ni) * 4 + (n_in + n_out) * p->nf * 8;
+    const int64_t bplanes = 3 * p->nf * bn * 2 * n_in_pad * 2;
+    const int64_t out = p->nf * g * n_in_pad * 8;
+    return g * per_vol + bplanes + out;
+}
+
+// Volumes per tensor-core pass: 64 where the free device memory (plus what
+// the plan's workspaces already hold) fits that group with a 10 % margin,
+// else 32, 16 or 8.
+int spectral_tc_group(const sid_plan* p, int64_t nb)
+{
+    size_t fr = 0, tot = 0;
+    if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) {
+        cudaGetLastError();
+        return 32;
+    }
+    int64_t held = 0;
+    const sid::DBuf* bufs[] = {&p->ws[0], &p->ws[1], &p->ws[4], &p->ws[5], &p->vhat, &p->ihat, &p->tcb, &p->tco};
+    for (const sid::DBuf* b : bufs) held += (int64_t)b->bytes;
+    const int64_t avail = (int64_t)fr + held;
+    for (int64_t g : {64, 32, 16, 8})
+        if (g <= 32 || nb > 32)
+            if (tc_group_bytes(p, g) * 11 / 10 <= avail) return (int)g;
+    return 8;
+}
+
 // A maps: 24-bit planes (high halves as BF16, low bytes) of rows x kp elements
 // per frequency; B maps: BN x kp BF16 per frequency.
 static int tc_maps(SpecTcMaps* m, const void* ah, const void* al, const void* bh, const void* bm, const void* bl,

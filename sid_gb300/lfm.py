@@ -97,7 +97,7 @@ class Projector:
         None reproduces forwardProjectGPU / backwardProjectGPU_new.
     methods : operator forms to build ('direct', 'spectral_f32', 'spectral_i16').
     batched : also build the transposed 24-bit spectra (SID_PLAN_SPECTRAL_TC) so
-        that the batched calls of 'spectral_mixed' contract up to 32 volumes per
+        that the batched calls of 'spectral_mixed' contract up to 64 volumes per
         pass on the tensor cores.
     """
 
@@ -347,7 +347,7 @@ class Projector:
     def reconstruct_components(self, imgs, microlenses=None, opts=None, method=None, return_lambda=False):
         """reconstruct_component for several component images at once
         (reconstruct_S.m:162-212): back projections and solver iterations run
-        on groups of up to 32 components (sid_reconstruct_components)."""
+        on groups of up to 64 components (sid_reconstruct_components)."""
         o = self._recon_opts(opts)
         ims = [to_device(i) for i in imgs]
         for im in ims:
@@ -531,7 +531,7 @@ def generate_kernel(ker_shape, ker_param):
 def reconstruct_S(S, psf_ballistic, opts=None):
     """recon_nnmf = reconstruct_S(S, psf_ballistic, opts) (reconstruct_S.m:1),
     the GPU branch (:158-211): the components S(ii, :, :) reconstructed on
-    one resident plan, in groups of up to 32 (sid_reconstruct_components).  S: (n, X, Y); psf_ballistic: dict or object with H;
+    one resident plan, in groups of up to 64 (sid_reconstruct_components).  S: (n, X, Y); psf_ballistic: dict or object with H;
     opts: q, lamb_L1, lamb_L2, whichSolver, max_iter, microlenses.  Returns a
     list of X x Y x Z CUDA tensors.  With opts.ker_param (and opts.ker_shape,
     default 'user'), the projector is composed with convn(., kernel, 'same')
