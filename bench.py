@@ -796,7 +796,8 @@ def main():
                 "algorithmic_bytes_per_launch": (bytes_f + bytes_a) / 2,
                 "hbm_gbs": (bytes_f + bytes_a) / 2 / (avg / 1e3) / 1e9,
                 "hbm_frac": (bytes_f + bytes_a) / 2 / (avg / 1e3) / 1e9 / hbm,
-                "bound": "hbm", "peaks": "measured bf16_tflops / hbm_gbs (MEASURED_PEAKS.json)"}
+                "limit": "shared-memory operand reads of the MMAs (neither DRAM nor the tensor pipe saturated)",
+                "peaks": "measured bf16_tflops / hbm_gbs (MEASURED_PEAKS.json)"}
         else:
             flop_launch = 8.0 * nf_ * n_in_ * n_out_ * min(4, nbv)
             fp32_peak = 152 * 128 * 2 * 2.07e9 / 1e12
