@@ -1130,12 +1130,12 @@ static int iterate(sid_ctx* c, NnlsWork& w, int64_t K, int64_t F, int solver, co
         k_nn_mask<<<(unsigned)cdiv(F, kColsPerCta), kColsPerCta * kColThreads, 0, s>>>(b, (int)K, (int)F, use_std);
         SID_CHECK_LAUNCH();
         SID_TRY(gmul_std(s));
-if (K <= 8 * kColThreads)
+        if (K <= 8 * kColThreads)
             k_nn_step<8><<<(unsigned)cdiv(F, kColsPerCta), kColsPerCta * kColThreads, 0, s>>>(
-            b, (int)K, (int)F, solver, sample, (int)o->tol_p, use_std);
+                b, (int)K, (int)F, solver, sample, (int)o->tol_p, use_std);
         else
             k_nn_step<kStepRows><<<(unsigned)cdiv(F, kColsPerCta), kColsPerCta * kColThreads, 0, s>>>(
-            b, (int)K, (int)F, solver, sample, (int)o->tol_p, use_std);
+                b, (int)K, (int)F, solver, sample, (int)o->tol_p, use_std);
         SID_CHECK_LAUNCH();
         if (!b.sparse) SID_TRY(gmul_std(s));  // G step: applied by the next iteration's mask kernel
         k_nn_fit<<<cdiv(F, 256), 256, 0, s>>>(b, (int)F, solver, sample, max_iter, use_std);
