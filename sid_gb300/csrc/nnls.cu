@@ -135,8 +135,6 @@ __device__ __forceinline__ void put_operand_f16(const ColBufs& b, int j, int k, 
 // keep 22 significant bits of each entry relative to its column's largest, in
 // FP16's normal range.)
 
-__global__ void k_iter_inc(NnlsCounters* c) { c->iter += 1; }
-
 // Reductions on the FP32 and integer pipes.  A sum is carried as an
 // unevaluated pair hi + lo (an error-free two-sum at every addition), so the
 // partials add up as accurately as an FP64 sum would.  The column kernels issue
@@ -221,8 +219,16 @@ __device__ __forceinline__ float wide_ratio(float2 num, float2 den)
 // (fast_nnls.m:153; the incremental form of LS_nnls.m:119), then the passive
 // set and masked gradient (LS_nnls.m:120-121, fast_nnls.m:100,163).  g holds
 // G step (zero before the first iteration).
-__global__ void __launch_bounds__(256) k_nn_mask(ColBufs b, int K, int F, int use_std)
+// (inc_iter: the first thread also advances the iteration counter, which no
+// thread of this kernel reads and the step kernel after it does.)  ROWS > 0:
+// every row of the column is one of this thread's ROWS register rows (K <=
+// ROWS * kColThreads), loaded together before any is used (more loads in
+// flight), and the masked gradient stays in registers for the FP16 operand
+// pass; ROWS = 0: any K, rows streamed.
+template <int ROWS>
+__global__ void __launch_bounds__(256) k_nn_mask(ColBufs b, int K, int F, int use_std, int inc_iter)
 {
+    if (inc_iter && blockIdx.x == 0 && threadIdx.x == 0) b.cnt->iter += 1;
     __shared__ float2 red[kColsPerCta][kWarpsPerCol][2];
     __shared__ float redm[kColsPerCta][kWarpsPerCol];
     __shared__ int redn[kColsPerCta][kWarpsPerCol];
@@ -231,22 +237,44 @@ __global__ void __launch_bounds__(256) k_nn_mask(ColBufs b, int K, int F, int us
     const bool act = c.j < F && b.active[c.j];
     float acc_f = 0.f, accw_f = 0.f, mx_f = -INFINITY, am_f = 0.f;
     int np_i = 0;
+    constexpr int RR = ROWS > 0 ? ROWS : 1;
+    float dmr[RR];
+    // one row: pending gradient update, passive set, operand, statistics
+    auto row = [&](int64_t o, int k, float g, float2 xv, float2 dold) -> float {
+        if (use_std) g -= b.gu[k];
+        const float2 dv = dd_add(dold, g);
+        b.df[o + k] = dv;
+        const bool p = xv.x > 0.f || dv.x < 0.f;
+        const float dm = p ? dv.x + dv.y : 0.f;
+        if (b.f16s) am_f = fmaxf(am_f, fabsf(dm));
+        else put_operand(b, o, c.j, k, dm);
+        wide_fma(dm, dm, acc_f, accw_f);
+        np_i += p ? 1 : 0;
+        mx_f = fmaxf(mx_f, xv.x);
+        return dm;
+    };
     if (act) {
         const int64_t o = (int64_t)c.j * K;
+        if (ROWS > 0) {
+            float gv[RR];
+            float2 xr[RR], dr[RR];
+#pragma unroll
+            for (int t = 0; t < RR; ++t) {
+                const int k = c.wc * 32 + c.lane + t * kColThreads;
+                if (k < K) {
+                    gv[t] = b.g[o + k];
+                    xr[t] = b.x[o + k];
+                    dr[t] = b.df[o + k];
+                }
+            }
+#pragma unroll
+            for (int t = 0; t < RR; ++t) {
+                const int k = c.wc * 32 + c.lane + t * kColThreads;
+                dmr[t] = k < K ? row(o, k, gv[t], xr[t], dr[t]) : 0.f;
+            }
+        } else {
 #pragma unroll 2
-        for (int k = c.wc * 32 + c.lane; k < K; k += kColThreads) {
-            float g = b.g[o + k];
-            if (use_std) g -= b.gu[k];
-            const float2 xv = b.x[o + k];
-            const float2 dv = dd_add(b.df[o + k], g);
-            b.df[o + k] = dv;
-            const bool p = xv.x > 0.f || dv.x < 0.f;
-            const float dm = p ? dv.x + dv.y : 0.f;
-            if (b.f16s) am_f = fmaxf(am_f, fabsf(dm));
-            else put_operand(b, o, c.j, k, dm);
-            wide_fma(dm, dm, acc_f, accw_f);
-            np_i += p ? 1 : 0;
-            mx_f = fmaxf(mx_f, xv.x);
+            for (int k = c.wc * 32 + c.lane; k < K; k += kColThreads) row(o, k, b.g[o + k], b.x[o + k], b.df[o + k]);
         }
     }
     const float2 acc = warp_sum_ff(acc_f);
@@ -267,11 +295,19 @@ __global__ void __launch_bounds__(256) k_nn_mask(ColBufs b, int K, int F, int us
         float amax = reda[c.cl][0];
         for (int w = 1; w < kWarpsPerCol; ++w) amax = fmaxf(amax, reda[c.cl][w]);
         const float sc = pow2_for(amax);
-        const int64_t o = (int64_t)c.j * K;
-        for (int k = c.wc * 32 + c.lane; k < K; k += kColThreads) {
-            const float2 xv = b.x[o + k], dv = b.df[o + k];
-            const float dm = (xv.x > 0.f || dv.x < 0.f) ? dv.x + dv.y : 0.f;
-            put_operand_f16(b, c.j, k, dm * sc);
+        if (ROWS > 0) {
+#pragma unroll
+            for (int t = 0; t < RR; ++t) {
+                const int k = c.wc * 32 + c.lane + t * kColThreads;
+                if (k < K) put_operand_f16(b, c.j, k, dmr[t] * sc);
+            }
+        } else {
+            const int64_t o = (int64_t)c.j * K;
+            for (int k = c.wc * 32 + c.lane; k < K; k += kColThreads) {
+                const float2 xv = b.x[o + k], dv = b.df[o + k];
+                const float dm = (xv.x > 0.f || dv.x < 0.f) ? dv.x + dv.y : 0.f;
+                put_operand_f16(b, c.j, k, dm * sc);
+            }
         }
         if (c.wc == 0 && c.lane == 0) b.dsc[c.j] = 1.f / sc;
     }
@@ -587,6 +623,35 @@ __global__ void k_nn_retire(ColBufs b, int32_t* __restrict__ iters, int K, int F
                 const bool c1 = hmax * exp(te) / (1.0 - exp(k1)) < tol * (double)K * (double)b.xmax[j];
                 ids = (b.anyp[j] == 0.f) || (c1 && c2 && c3);
             }
+        }
+        if (ids) {
+            b.active[j] = 0;
+            if (iters) iters[j] = it;
+            atomicSub(&b.cnt->active, 1);
+        }
+    }
+}
+
+// fast_nnls's test and retirement in one pass: its retirement reads only the
+// column's own fit (unlike LS_nnls, which reads the first active column's).
+__global__ void k_nn_fit_retire_fast(ColBufs b, int32_t* __restrict__ iters, int K, int F, int sample, double tol,
+                                     double tol_, int max_iter, double hmax)
+{
+    const int it = b.cnt->iter;
+    const bool all = it > max_iter;
+    if (!all && (!(it & 1) || it <= 2 * sample)) return;
+    const int e_last = (it - 3) / 2;
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < F; j += gridDim.x * blockDim.x) {
+        if (!b.active[j]) continue;
+        bool ids = all;
+        if (!all) {
+            double k1, r, te;
+            window_fit(b.test, sample, F, j, e_last, b.xi, &k1, &r, &te);
+            b.fit[j] = k1;
+            b.fit[F + j] = r;
+            b.fit[2 * F + j] = te;
+            const bool c1 = hmax * exp(te) / (1.0 - exp(k1)) < tol * (double)K * (double)b.xmax[j];
+            ids = (b.anyp[j] == 0.f) || (c1 && r < tol_ * (double)sample && exp(k1) < 1.0);
         }
         if (ids) {
             b.active[j] = 0;
@@ -1124,10 +1189,15 @@ static int iterate(sid_ctx* c, NnlsWork& w, int64_t K, int64_t F, int solver, co
         }
         return SID_OK;
     };
+    const bool fast_fused = solver == SOLVER_FAST && !use_std;
     auto body = [&](cudaStream_t s) -> int {
-        k_iter_inc<<<1, 1, 0, s>>>(b.cnt);
-        SID_CHECK_LAUNCH();
-        k_nn_mask<<<(unsigned)cdiv(F, kColsPerCta), kColsPerCta * kColThreads, 0, s>>>(b, (int)K, (int)F, use_std);
+        // the mask kernel advances the iteration counter (one launch fewer per iteration)
+        if (K <= 8 * kColThreads)
+            k_nn_mask<8><<<(unsigned)cdiv(F, kColsPerCta), kColsPerCta * kColThreads, 0, s>>>(b, (int)K, (int)F,
+                                                                                             use_std, 1);
+        else
+            k_nn_mask<0><<<(unsigned)cdiv(F, kColsPerCta), kColsPerCta * kColThreads, 0, s>>>(b, (int)K, (int)F,
+                                                                                             use_std, 1);
         SID_CHECK_LAUNCH();
         SID_TRY(gmul_std(s));
         if (K <= 8 * kColThreads)
@@ -1138,6 +1208,12 @@ static int iterate(sid_ctx* c, NnlsWork& w, int64_t K, int64_t F, int solver, co
                 b, (int)K, (int)F, solver, sample, (int)o->tol_p, use_std);
         SID_CHECK_LAUNCH();
         if (!b.sparse) SID_TRY(gmul_std(s));  // G step: applied by the next iteration's mask kernel
+        if (fast_fused) {
+            k_nn_fit_retire_fast<<<cdiv(F, 256), 256, 0, s>>>(b, iters, (int)K, (int)F, sample, o->tol, o->tol_,
+                                                              max_iter, hmax);
+            SID_CHECK_LAUNCH();
+            return SID_OK;
+        }
         k_nn_fit<<<cdiv(F, 256), 256, 0, s>>>(b, (int)F, solver, sample, max_iter, use_std);
         SID_CHECK_LAUNCH();
         if (solver == SOLVER_LS) {
