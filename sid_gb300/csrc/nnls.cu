@@ -426,7 +426,35 @@ __global__ void __launch_bounds__(256) k_nn_step(ColBufs b, int K, int F, int so
     const int64_t o = (int64_t)c.j * K;
     const float gsc = (b.f16s && act) ? b.dsc[c.j] : 1.f;  // undoes the operand's power-of-two scale
     float s2_f = 0.f, s2w_f = 0.f;
-    if (act) {
+    // when the ROWS register rows cover the column, the iterate and the masked
+    // gradient are loaded once (all rows together) and kept for the update
+    const bool regs = K <= ROWS * kColThreads;
+    float2 xr[ROWS];
+    float dmr[ROWS];
+    if (act && regs) {
+        float2 dr[ROWS];
+        float gr[ROWS];
+#pragma unroll
+        for (int t = 0; t < ROWS; ++t) {
+            const int k = c.wc * 32 + c.lane + t * kColThreads;
+            if (k < K) {
+                xr[t] = b.x[o + k];
+                dr[t] = b.df[o + k];
+                gr[t] = b.g[o + k];
+            }
+        }
+#pragma unroll
+        for (int t = 0; t < ROWS; ++t) {
+            const int k = c.wc * 32 + c.lane + t * kColThreads;
+            dmr[t] = 0.f;
+            if (k < K) {
+                dmr[t] = (xr[t].x > 0.f || dr[t].x < 0.f) ? dr[t].x + dr[t].y : 0.f;
+                float g = gr[t] * gsc;
+                if (use_std) g -= b.gu[k];
+                wide_fma(dmr[t], g, s2_f, s2w_f);
+            }
+        }
+    } else if (act) {
 #pragma unroll 2
         for (int k = c.wc * 32 + c.lane; k < K; k += kColThreads) {
             const float2 xv = b.x[o + k], dv = b.df[o + k];
@@ -467,9 +495,7 @@ __global__ void __launch_bounds__(256) k_nn_step(ColBufs b, int K, int F, int so
     unsigned cmask = 0;
     // one row: clamp, store, operand (dense mode), statistic; returns the clamp
     // correction (0 where the bound does not clamp)
-    auto row = [&](int k) -> float {
-        const float2 xv = b.x[o + k], dv = b.df[o + k];
-        const float dm = (xv.x > 0.f || dv.x < 0.f) ? dv.x + dv.y : 0.f;
+    auto row_with = [&](int k, float2 xv, float dm) -> float {
         const float pstep = dm * alpha_f;
         float2 xn = dd_add(xv, -pstep);
         // the step x_new - x exactly: -alpha d, or -x where the bound clamps
@@ -493,13 +519,17 @@ __global__ void __launch_bounds__(256) k_nn_step(ColBufs b, int K, int F, int so
         }
         return corr;
     };
+    auto row = [&](int k) -> float {
+        const float2 xv = b.x[o + k], dv = b.df[o + k];
+        return row_with(k, xv, (xv.x > 0.f || dv.x < 0.f) ? dv.x + dv.y : 0.f);
+    };
     if (act) {
 #pragma unroll
         for (int t = 0; t < ROWS; ++t) {
             const int k = c.wc * 32 + c.lane + t * kColThreads;
             cc[t] = 0.f;
             if (k >= K) continue;
-            cc[t] = row(k);
+            cc[t] = regs ? row_with(k, xr[t], dmr[t]) : row(k);
             if (cc[t] != 0.f) cmask |= 1u << t;
         }
         // rows past ROWS * 128 (dense mode only: sparse mode needs K <= ROWS * 128)
