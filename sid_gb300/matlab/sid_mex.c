@@ -27,6 +27,8 @@
  *   T        = sid_mex('pinv_apply', h, Y, baseline)      baseline may be []
  *   sid_mex('pinv_destroy', h)
  *   [X, lam] = sid_mex('reconstruct', plan, img, microlenses, opts, method)
+ *   [X, lam] = sid_mex('reconstruct_batch', plan, imgs, microlenses, opts, method)
+ *              imgs X x Y x n, X X x Y x Z x n (groups of components per pass)
  *   [X, hist] = sid_mex('isra_ex', plan, Htf, Xguess, maxIter, mode, p, lambda, method)   mode 0 basic, 1 TV
  *   X        = sid_mex('ls_deconv_ex', plan, df, max_iter, lamb_L1, lamb_L2, lamb_TV_L2, lamb_TV_L1, method)
  *   F        = sid_mex('library', plan, recon, centers, neur_id, neur_rad, axial)   recon: cell of volumes
@@ -538,6 +540,72 @@ void mexFunction(int nlhs, mxArray* plhs[], int nrhs, const mxArray* prhs[])
             sid_pinv_destroy(g_pinv[h]);
             g_pinv[h] = NULL;
         }
+        return;
+    }
+    if (!strcmp(cmd, "reconstruct_batch")) {
+        /* [X, lam] = sid_mex('reconstruct_batch', plan, imgs, microlenses, opts, method): imgs X x Y x n single
+         * gpuArray (one component image per slice); X: X x Y x Z x n, lam: n x 1 */
+        sid_plan* p = plan_arg(prhs[1]);
+        const mxGPUArray* imgs = gpu_arg(prhs[2], 0, cmd);
+        const mxGPUArray* ml = NULL;
+        mxArray* tmp_ml = NULL;
+        if (nrhs > 3 && !mxIsEmpty(prhs[3])) {
+            const mwSize nm = mxGetNumberOfElements(prhs[3]);
+            tmp_ml = mxCreateNumericMatrix(nm, 1, mxUINT8_CLASS, mxREAL);
+            uint8_t* dst = (uint8_t*)mxGetData(tmp_ml);
+            for (mwSize i = 0; i < nm; ++i) dst[i] = mxGetPr(prhs[3])[i] != 0.0;
+            ml = mxGPUCreateFromMxArray(tmp_ml);
+        }
+        const mxArray* o = nrhs > 4 ? prhs[4] : NULL;
+        sid_recon_opts ro;
+        sid_recon_defaults(&ro);
+        ro.q = field_or(o, "q", ro.q);
+        ro.lamb_L1 = field_or(o, "lamb_L1", ro.lamb_L1);
+        ro.lamb_L2 = field_or(o, "lamb_L2", ro.lamb_L2);
+        ro.max_iter = (int)field_or(o, "max_iter", ro.max_iter);
+        if (o && mxIsStruct(o)) {
+            const mxArray* w = mxGetField(o, 0, "whichSolver");
+            char sv[16] = "fast_nnls";
+            if (w && mxIsChar(w)) mxGetString(w, sv, sizeof(sv));
+            ro.solver = !strcmp(sv, "ISRA") ? 1 : 0;
+        }
+        int64_t info[14];
+        sid_plan_info(p, info);
+        const int64_t nI = info[3] * info[4], nV = nI * info[2];
+        const mwSize ne = mxGPUGetNumberOfElements(imgs);
+        if (ne % (mwSize)nI != 0) mexErrMsgIdAndTxt("sid:reconstruct_batch", "imgs must be X x Y x n");
+        const int64_t nc = (int64_t)(ne / (mwSize)nI);
+        mwSize dv[4] = {(mwSize)info[3], (mwSize)info[4], (mwSize)info[2], (mwSize)nc};
+        mxGPUArray* X = mxGPUCreateGPUArray(4, dv, mxSINGLE_CLASS, mxREAL, MX_GPU_DO_NOT_INITIALIZE);
+        const float** ip = (const float**)mxMalloc((size_t)nc * sizeof(float*));
+        float** xp = (float**)mxMalloc((size_t)nc * sizeof(float*));
+        double* lam = (double*)mxMalloc((size_t)nc * sizeof(double));
+        const float* ib = (const float*)mxGPUGetDataReadOnly(imgs);
+        float* xb = (float*)mxGPUGetData(X);
+        for (int64_t c = 0; c < nc; ++c) {
+            ip[c] = ib + c * nI;
+            xp[c] = xb + c * nV;
+        }
+        int rc = sid_reconstruct_components(p, method_arg(nrhs, prhs, 5), nc, ip,
+                                            ml ? (const uint8_t*)mxGPUGetDataReadOnly(ml) : NULL, &ro, xp, lam, NULL);
+        if (rc == SID_OK) rc = sid_plan_sync(p, NULL);
+        mxGPUDestroyGPUArray(imgs);
+        if (ml) mxGPUDestroyGPUArray(ml);
+        if (tmp_ml) mxDestroyArray(tmp_ml);
+        mxFree(ip);
+        mxFree(xp);
+        if (rc != SID_OK) {
+            mxFree(lam);
+            mxGPUDestroyGPUArray(X);
+        }
+        check(rc, cmd);
+        plhs[0] = mxGPUCreateMxArrayOnGPU(X);
+        if (nlhs > 1) {
+            plhs[1] = mxCreateDoubleMatrix((mwSize)nc, 1, mxREAL);
+            for (int64_t c = 0; c < nc; ++c) mxGetPr(plhs[1])[c] = lam[c];
+        }
+        mxFree(lam);
+        mxGPUDestroyGPUArray(X);
         return;
     }
     if (!strcmp(cmd, "reconstruct")) {

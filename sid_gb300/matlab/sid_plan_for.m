@@ -1,8 +1,10 @@
-function plan = sid_plan_for(H, CAindex, X, Y)
+function plan = sid_plan_for(H, CAindex, X, Y, batched)
 % SID_PLAN_FOR  Resident libsid projector plan for the PSF H (created on first
 % use and reused).  CAindex = [] selects the uncropped PSF (forwardProjectGPU
 % semantics) and the storage the current sid_method() needs; a CAindex gives
-% the cropped direct form (forwardProjectACC semantics).
+% the cropped direct form (forwardProjectACC semantics).  batched = true adds
+% the transposed 24-bit spectra of the tensor-core batched projections
+% (SID_PLAN_SPECTRAL_TC) to the spectral forms.
 % Plans are keyed on the PSF's size, the crop, the sensor size, the storage
 % and a fingerprint of 4096 entries of H at fixed strided positions (a full
 % pass over the 3.3 GB PSF of the 1005^2 x 31 configuration per call would
@@ -13,6 +15,7 @@ persistent keys plans
 if isempty(keys), keys = {}; plans = []; end
 flags_for = [1, 2, 4, 4 + 8, 4 + 2];   % direct, spectral_f32, _i16, _mixed, _mixed_f32
 if isempty(CAindex), flags = flags_for(sid_method() + 1); else, flags = 1; end
+if nargin > 4 && batched && flags ~= 1, flags = bitor(flags, 8 + 16); end
 n = numel(H);
 idx = unique(round(linspace(1, n, min(n, 4096))));
 smp = double(gather(H(idx)));

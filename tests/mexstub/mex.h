@@ -39,6 +39,8 @@ mxArray* mxCreateNumericMatrix(mwSize m, mwSize n, mxClassID cls, mxComplexity c
 mxArray* mxCreateNumericArray(mwSize nd, const mwSize* dims, mxClassID cls, mxComplexity c);
 mxArray* mxDuplicateArray(const mxArray* a);
 void mxDestroyArray(mxArray* a);
+void* mxMalloc(size_t n);
+void mxFree(void* p);
 
 void mexFunction(int nlhs, mxArray* plhs[], int nrhs, const mxArray* prhs[]);
 #endif
