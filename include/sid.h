@@ -218,6 +218,16 @@ int sid_deconv_ls_ex(sid_plan* plan, int method, float* X, int max_iter, float l
 int sid_library(sid_plan* plan, const float* const* recon, int64_t n_comp, const double* centers,
                 const uint8_t* neur_id, int64_t n_neur, int64_t neur_rad, double axial, float* out,
                 int out_layout, void* stream);
+/* The same library through the tensor-core spectral projector on lenslet
+ * windows around each neuron's box (tap spectra on a small lenslet grid, built
+ * at the first call and kept on the plan; up to 64 neurons per contraction
+ * pass, each pass reducing only over its neurons' depths).  Arguments and
+ * layouts as sid_library; the spectra carry 16 significant bits (about 1e-5
+ * relative per row against 1e-7 for sid_library's FP32 taps).  Any plan
+ * (odd PSF crop widths); boxes of at most 6 lattice points per phase. */
+int sid_library_spectral(sid_plan* plan, const float* const* recon, int64_t n_comp, const double* centers,
+                         const uint8_t* neur_id, int64_t n_neur, int64_t neur_rad, double axial, float* out,
+                         int out_layout, void* stream);
 /* The crop boxes the call above uses (host only): boxes[6n..6n+5] = 0-based
  * half-open x0 x1 y0 y1 z0 z1 of neuron n (generate_LFM_library_GPU.m:68-88). */
 int sid_library_boxes(const double* centers, int64_t n_neur, int64_t neur_rad, double axial, int64_t X,

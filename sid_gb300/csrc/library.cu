@@ -20,16 +20,10 @@
 #include <cmath>
 #include <vector>
 
-#include "sid_internal.cuh"
+#include "library.cuh"
 
 namespace sid {
 
-struct LibBox {
-    int x0, x1, y0, y1, z0, z1;  // 0-based half-open box
-    int off;                     // offset of the packed sub-volume
-    int ncomp;                   // components averaged
-    int s0, s1, t0, t1;          // output lenslet window (half-open)
-};
 
 // packed[b.off + (x-x0) + bw*((y-y0) + bh*(z-z0))] = mean_k recon_k(x, y, z)
 __global__ void k_lib_average(const float* const* __restrict__ recon, const uint8_t* __restrict__ neur_id,
@@ -390,6 +384,52 @@ static void neuron_box(const double* centers, int64_t n_neur, int64_t n, int64_t
     box6[5] = (int)std::min<int64_t>(z + zr, Z);
 }
 
+int lib_stage(sid_plan* p, const char* who, const float* const* recon, int64_t n_comp, const double* centers,
+              const uint8_t* neur_id, int64_t n_neur, int64_t neur_rad, double axial, std::vector<LibBox>& boxes,
+              cudaStream_t st)
+{
+    const int64_t N = p->N;
+    boxes.resize((size_t)n_neur);
+    int64_t off = 0;
+    for (int64_t n = 0; n < n_neur; ++n) {
+        int bx[6];
+        neuron_box(centers, n_neur, n, neur_rad, axial, p->X, p->Y, p->Z, bx);
+        LibBox b;
+        b.x0 = bx[0]; b.x1 = bx[1]; b.y0 = bx[2]; b.y1 = bx[3]; b.z0 = bx[4]; b.z1 = bx[5];
+        int nc = 0;
+        for (int64_t k = 0; k < n_comp; ++k) nc += neur_id[n + n_neur * k] ? 1 : 0;
+        SID_REQUIRE(nc > 0, "%s: neuron %lld is in no component (neur_id row is empty)", who, (long long)(n + 1));
+        SID_REQUIRE(b.x1 > b.x0 && b.y1 > b.y0 && b.z1 > b.z0,
+                    "%s: neuron %lld has an empty box (centre outside the volume)", who, (long long)(n + 1));
+        b.ncomp = nc;
+        b.off = (int)off;
+        off += (int64_t)(b.x1 - b.x0) * (b.y1 - b.y0) * (b.z1 - b.z0);
+        // output lenslets reached from the box: s = u + m + dlo
+        const int umin = b.x0 / (int)N, umax = (b.x1 - 1) / (int)N;
+        const int vmin = b.y0 / (int)N, vmax = (b.y1 - 1) / (int)N;
+        b.s0 = (int)std::max<int64_t>(0, umin + p->g.dlo);
+        b.s1 = (int)std::min<int64_t>(p->Lx, umax + p->g.dhi + 1);
+        b.t0 = (int)std::max<int64_t>(0, vmin + p->g.dlo);
+        b.t1 = (int)std::min<int64_t>(p->Ly, vmax + p->g.dhi + 1);
+        boxes[(size_t)n] = b;
+        SID_REQUIRE(off < INT32_MAX, "%s: boxes too large", who);
+    }
+    DBuf& dbox = p->ws[3];
+    DBuf& dpack = p->ws[2];
+    DBuf& dmeta = p->ws[1];
+    SID_TRY(dbox.alloc(boxes.size() * sizeof(LibBox)));
+    SID_TRY(dpack.alloc((size_t)off * sizeof(float)));
+    SID_TRY(dmeta.alloc((size_t)(n_comp * sizeof(float*) + n_neur * n_comp)));
+    SID_CUDA_TRY(cudaMemcpyAsync(dbox.p, boxes.data(), boxes.size() * sizeof(LibBox), cudaMemcpyHostToDevice, st));
+    SID_CUDA_TRY(cudaMemcpyAsync(dmeta.p, recon, (size_t)n_comp * sizeof(float*), cudaMemcpyHostToDevice, st));
+    uint8_t* did = dmeta.as<uint8_t>() + n_comp * sizeof(float*);
+    SID_CUDA_TRY(cudaMemcpyAsync(did, neur_id, (size_t)(n_neur * n_comp), cudaMemcpyHostToDevice, st));
+    k_lib_average<<<(unsigned)n_neur, 256, 0, st>>>(dmeta.as<const float*>(), did, n_neur, dbox.as<LibBox>(),
+                                                    (int)n_comp, p->X, p->Y, dpack.as<float>());
+    SID_CHECK_LAUNCH();
+    return SID_OK;
+}
+
 }  // namespace sid
 
 using namespace sid;
@@ -413,37 +453,18 @@ extern "C" int sid_library(sid_plan* p, const float* const* recon, int64_t n_com
     SID_REQUIRE(p->taps_f.p, "sid_library: the plan needs SID_PLAN_DIRECT (lenslet taps)");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const int64_t N = p->N, D = p->g.D;
-    std::vector<LibBox> boxes(n_neur);
-    int64_t off = 0;
+    std::vector<LibBox> boxes;
+    SID_TRY(lib_stage(p, "sid_library", recon, n_comp, centers, neur_id, n_neur, neur_rad, axial, boxes, st));
     int max_ns = 0, ntgM = 0, span = 0, nrv = 0, bwm = 0;
-    for (int64_t n = 0; n < n_neur; ++n) {
-        int bx[6];
-        neuron_box(centers, n_neur, n, neur_rad, axial, p->X, p->Y, p->Z, bx);
-        LibBox b;
-        b.x0 = bx[0]; b.x1 = bx[1]; b.y0 = bx[2]; b.y1 = bx[3]; b.z0 = bx[4]; b.z1 = bx[5];
-        int nc = 0;
-        for (int64_t k = 0; k < n_comp; ++k) nc += neur_id[n + n_neur * k] ? 1 : 0;
-        SID_REQUIRE(nc > 0, "sid_library: neuron %lld is in no component (neur_id row is empty)", (long long)(n + 1));
-        SID_REQUIRE(b.x1 > b.x0 && b.y1 > b.y0 && b.z1 > b.z0,
-                    "sid_library: neuron %lld has an empty box (centre outside the volume)", (long long)(n + 1));
-        b.ncomp = nc;
-        b.off = (int)off;
-        off += (int64_t)(b.x1 - b.x0) * (b.y1 - b.y0) * (b.z1 - b.z0);
-        // output lenslets reached from the box: s = u + m + dlo
+    for (const LibBox& b : boxes) {
         const int umin = b.x0 / (int)N, umax = (b.x1 - 1) / (int)N;
         const int vmin = b.y0 / (int)N, vmax = (b.y1 - 1) / (int)N;
-        b.s0 = (int)std::max<int64_t>(0, umin + p->g.dlo);
-        b.s1 = (int)std::min<int64_t>(p->Lx, umax + p->g.dhi + 1);
-        b.t0 = (int)std::max<int64_t>(0, vmin + p->g.dlo);
-        b.t1 = (int)std::min<int64_t>(p->Ly, vmax + p->g.dhi + 1);
         max_ns = std::max(max_ns, b.s1 - b.s0);
         ntgM = std::max(ntgM, (int)cdiv(b.t1 - b.t0, kLibT));
         span = std::max(span, std::max(umax - umin, vmax - vmin));
         nrv = std::max(nrv, (int)std::max(cdiv(b.x1 - b.x0, N), cdiv(b.y1 - b.y0, N)));
         bwm = std::max(bwm, b.x1 - b.x0);
-        boxes[n] = b;
     }
-    SID_REQUIRE(off < INT32_MAX, "sid_library: boxes too large");
     // tiled kernel: output windows of W x Wt lenslets, W <= 32 (one lane per row)
     LibTileArgs ta;
     ta.N = (int)N; ta.D = (int)D; ta.dlo = (int)p->g.dlo; ta.span = span;
@@ -483,22 +504,11 @@ extern "C" int sid_library(sid_plan* p, const float* const* recon, int64_t n_com
         i = e;
     }
     const int64_t ngroups = (int64_t)groups.size() / (kLibG + 1);
-    DBuf& dbox = p->ws[3];
-    DBuf& dpack = p->ws[2];
-    DBuf& dmeta = p->ws[1];
     DBuf& dgrp = p->ws[0];
     SID_TRY(dgrp.alloc(groups.size() * sizeof(int)));
     SID_CUDA_TRY(cudaMemcpyAsync(dgrp.p, groups.data(), groups.size() * sizeof(int), cudaMemcpyHostToDevice, st));
-    SID_TRY(dbox.alloc(boxes.size() * sizeof(LibBox)));
-    SID_TRY(dpack.alloc((size_t)off * sizeof(float)));
-    SID_TRY(dmeta.alloc((size_t)(n_comp * sizeof(float*) + n_neur * n_comp)));
-    SID_CUDA_TRY(cudaMemcpyAsync(dbox.p, boxes.data(), boxes.size() * sizeof(LibBox), cudaMemcpyHostToDevice, st));
-    SID_CUDA_TRY(cudaMemcpyAsync(dmeta.p, recon, (size_t)n_comp * sizeof(float*), cudaMemcpyHostToDevice, st));
-    uint8_t* did = dmeta.as<uint8_t>() + n_comp * sizeof(float*);
-    SID_CUDA_TRY(cudaMemcpyAsync(did, neur_id, (size_t)(n_neur * n_comp), cudaMemcpyHostToDevice, st));
-    k_lib_average<<<(unsigned)n_neur, 256, 0, st>>>(dmeta.as<const float*>(), did, n_neur, dbox.as<LibBox>(),
-                                                    (int)n_comp, p->X, p->Y, dpack.as<float>());
-    SID_CHECK_LAUNCH();
+    const LibBox* dbox = p->ws[3].as<LibBox>();
+    const float* dpack = p->ws[2].as<float>();
     const int64_t P = p->X * p->Y;
     SID_CUDA_TRY(cudaMemsetAsync(out, 0, (size_t)(P * n_neur) * sizeof(float), st));
     const int64_t tbs = cdiv(N * D * D, 32) * 32;
@@ -506,13 +516,13 @@ extern "C" int sid_library(sid_plan* p, const float* const* recon, int64_t n_com
     dim3 grid((unsigned)ngroups, (unsigned)(N * N));
     if (tiled) {
         ta.tbs = tbs; ta.Lx = (int)p->Lx; ta.Ly = (int)p->Ly; ta.X = p->X; ta.Y = p->Y; ta.ldn = ldn; ta.ldp = ldp;
-        SID_TRY(launch_lib_tile(tb, nrv, grid, tiled_bytes, p->taps_f.as<float>(), dpack.as<float>(),
-                                dbox.as<LibBox>(), dgrp.as<int>(), ta, out, st));
+        SID_TRY(launch_lib_tile(tb, nrv, grid, tiled_bytes, p->taps_f.as<float>(), dpack,
+                                dbox, dgrp.as<int>(), ta, out, st));
     } else {
         SID_CUDA_TRY(cudaFuncSetAttribute(k_lib_project<kLibG>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           (int)tile_bytes));
-        k_lib_project<kLibG><<<grid, 256, tile_bytes, st>>>(p->taps_f.as<float>(), dpack.as<float>(),
-                                                            dbox.as<LibBox>(), dgrp.as<int>(), (int)N, (int)D,
+        k_lib_project<kLibG><<<grid, 256, tile_bytes, st>>>(p->taps_f.as<float>(), dpack,
+                                                            dbox, dgrp.as<int>(), (int)N, (int)D,
                                                             (int)p->g.dlo, span, ntgM, tbs, (int)p->Lx, (int)p->Ly,
                                                             p->X, p->Y, out, ldn, ldp);
         SID_CHECK_LAUNCH();

@@ -1,0 +1,331 @@
+// libtc.cu -- library generation (generate_LFM_library_GPU.m:63-109) through
+// the tensor-core spectral projector on per-neuron lenslet windows.
+//
+// A neuron's boxed volume covers at most `span` lattice points per axis and
+// phase (3 for a 25-pixel box at Nnum 15), so its forward projection lives on
+// Wo = span + D - 1 output lenslets per axis around the box.  In window
+// coordinates (origin at the first output lenslet, umin + dlo) the box sits at
+// lattice positions [-dlo, -dlo + span) and the output at [0, Wo); on a lenslet
+// grid of L >= Wo points the circular convolution with the tap arrays never
+// wraps, so one set of tap spectra on that small grid (nf = (L/2+1) L
+// frequencies, 420 for L = 28 instead of 3280 for the 1005-pixel frame) serves
+// every neuron:
+//   Ihat_n[b'a'](f) = sum_abc Kw[f][b'a'][abc] Vhat_n[abc](f)
+// which for up to 64 neurons at once is the batched tensor-core contraction of
+// spec_tc.cu.  Per pass (neurons sorted by depth window, so a pass reduces only
+// over the input channels of its depths):
+//   1. k_lib_pack: each box channel's spectrum, a direct DFT of its <= span^2
+//      lattice points, written straight into the contraction's B operand
+//      (three BF16 parts, columns (Vr, -Vi) and (Vi, Vr) per neuron);
+//   2. k_spec_tc over the window spectra (24-bit planes), the pass's K range;
+//   3. the output spectra unpacked and inverse-transformed on the window grid;
+//   4. k_lib_scatter: window lenslets into the library rows (pixels outside
+//      the frame dropped; the rest of each row is zero).
+// Precision is the tensor-core forward projection's (24-bit spectra, B split
+// to FP32's 24 bits, FP32 accumulation): about 1e-5 relative per row, against
+// FP32 rounding for the tap kernels of library.cu.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include <cuda_bf16.h>
+
+#include "library.cuh"
+
+namespace sid {
+
+bool fft_factor(int64_t L, int* P, int* Q);
+int build_khat_f24(const sid_plan* p, int64_t L, const float2* tw, ushort2* h, uchar2* l);
+
+struct LibWin {
+    int64_t Wo = 0;  // window lenslets per axis
+    sid_plan geo;    // window geometry for the inverse DFTs: Lx = Ly = Wo, X = Y = Wo N, L, nf, twiddles
+    DBuf kh, kl;     // window tap spectra, 24-bit planes [f][b'a'][abc]
+    DBuf bpl;        // B operand planes of one pass
+    DBuf tco, ihat, img, cols;
+};
+
+namespace {
+
+constexpr int kLibPackThreads = 128;
+constexpr int kLibMaxL = 64;  // window grid lengths handled by the pack kernel
+
+__device__ __forceinline__ void split3(float x0, float x1, uint32_t& h, uint32_t& m, uint32_t& l)
+{
+    // x = hi + mid + lo, each remainder exact in FP32 (24 significant bits in all)
+    const __nv_bfloat162 hi = __floats2bfloat162_rn(x0, x1);
+    const float2 hf = __bfloat1622float2(hi);
+    const float r0 = x0 - hf.x, r1 = x1 - hf.y;
+    const __nv_bfloat162 mi = __floats2bfloat162_rn(r0, r1);
+    const float2 mf = __bfloat1622float2(mi);
+    const __nv_bfloat162 lo = __floats2bfloat162_rn(r0 - mf.x, r1 - mf.y);
+    h = *reinterpret_cast<const uint32_t*>(&hi);
+    m = *reinterpret_cast<const uint32_t*>(&mi);
+    l = *reinterpret_cast<const uint32_t*>(&lo);
+}
+
+// B planes [f][BN][kpb] for one pass: thread (channel cbase + cc, neuron slot j)
+// evaluates the channel's spectrum at the H1 frequencies f1 of row f2 =
+// blockIdx.y, Vhat(f1, f2) = sum_{u,v} V(u, v) exp(-2 pi i (f1 pu + f2 pv) / L)
+// over the box's lattice points (pu, pv: window coordinates mod L), and writes
+// the two columns of slot j (zeros for empty slots and channels).  MU bounds the
+// lattice points per axis and phase.
+template <int MU>
+__global__ void __launch_bounds__(kLibPackThreads)
+k_lib_pack(const float* __restrict__ packed, const LibBox* __restrict__ boxes, const int* __restrict__ cols, int nb,
+           int cbase, int nchb, int n_in, int N, int dlo, int L, int BN, const float2* __restrict__ tw,
+           uint32_t* __restrict__ bhi, uint32_t* __restrict__ bmi, uint32_t* __restrict__ blo)
+{
+    __shared__ float2 stw[kLibMaxL];
+    for (int i = threadIdx.x; i < L; i += blockDim.x) stw[i] = tw[i];
+    __syncthreads();
+    const int cc = blockIdx.x * blockDim.x + threadIdx.x;
+    if (cc >= nchb) return;
+    const int j = blockIdx.z, f2 = blockIdx.y, H1 = L / 2 + 1;
+    const int c = cbase + cc;
+    // empty slots and channels keep zero values at phase 0
+    float val[MU * MU];
+    int ph[MU * MU], du[MU * MU];
+#pragma unroll
+    for (int q = 0; q < MU * MU; ++q) {
+        val[q] = 0.f;
+        ph[q] = 0;
+        du[q] = 0;
+    }
+    if (j < nb && c < n_in) {
+        const LibBox b = boxes[cols[j]];
+        const int a = c % N, bb = (c / N) % N, z = c / (N * N);
+        if (z >= b.z0 && z < b.z1) {
+            const int bw = b.x1 - b.x0, bh = b.y1 - b.y0;
+            const int w0x = b.x0 / N + dlo, w0y = b.y0 / N + dlo;  // window origin (lattice)
+            // lattice points of phase (a, bb) inside the box: x = a + N u in [x0, x1)
+            const int ulo = (b.x0 - a + N - 1 + N) / N - 1, uhi = (b.x1 - 1 - a + N) / N - 1;
+            const int vlo = (b.y0 - bb + N - 1 + N) / N - 1, vhi = (b.y1 - 1 - bb + N) / N - 1;
+            const float* src = packed + b.off + (int64_t)bw * bh * (z - b.z0);
+#pragma unroll
+            for (int iv = 0; iv < MU; ++iv)
+#pragma unroll
+                for (int iu = 0; iu < MU; ++iu) {
+                    const int u = ulo + iu, v = vlo + iv, q = iv * MU + iu;
+                    if (u <= uhi && v <= vhi) {
+                        val[q] = src[(a + N * u - b.x0) + bw * (bb + N * v - b.y0)];
+                        const int pu = ((u - w0x) % L + L) % L, pv = ((v - w0y) % L + L) % L;
+                        ph[q] = (int)(((int64_t)f2 * pv) % L);  // phase at f1 = 0
+                        du[q] = pu;
+                    }
+                }
+        }
+    }
+    const int64_t kw = nchb;  // 32-bit words (complex parts as a BF16 pair) per B row
+    for (int f1 = 0; f1 < H1; ++f1) {
+        float re = 0.f, im = 0.f;
+#pragma unroll
+        for (int q = 0; q < MU * MU; ++q) {
+            const float2 w = stw[ph[q]];
+            re = fmaf(val[q], w.x, re);
+            im = fmaf(-val[q], w.y, im);
+            const int nx = ph[q] + du[q];
+            ph[q] = nx >= L ? nx - L : nx;
+        }
+        const int64_t f = (int64_t)f2 * H1 + f1;
+        uint32_t h, m, l;
+        // column 2j: (Vr, -Vi); column 2j + 1: (Vi, Vr)
+        const int64_t o0 = (f * BN + 2 * j) * kw + cc, o1 = o0 + kw;
+        split3(re, -im, h, m, l);
+        bhi[o0] = h; bmi[o0] = m; blo[o0] = l;
+        split3(im, re, h, m, l);
+        bhi[o1] = h; bmi[o1] = m; blo[o1] = l;
+    }
+}
+
+// img[j][b'a'][t][s] (window lenslets) -> library rows of the pass's neurons
+__global__ void k_lib_scatter(const float* __restrict__ img, const LibBox* __restrict__ boxes,
+                              const int* __restrict__ cols, int nb, int N, int Wo, int dlo, int64_t X, int64_t Y,
+                              float* __restrict__ out, int64_t ldn, int64_t ldp)
+{
+    const int64_t per = (int64_t)N * N * Wo * Wo, total = per * nb;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int j = (int)(i / per);
+        const int64_t r = i - j * per;
+        const int o = (int)(r / ((int64_t)Wo * Wo));
+        const int q = (int)(r - (int64_t)o * Wo * Wo);
+        const int t = q / Wo, s = q - t * Wo;
+        const int n = cols[j];
+        const LibBox b = boxes[n];
+        const int64_t x = (o % N) + (int64_t)N * (b.x0 / N + dlo + s);
+        const int64_t y = (o / N) + (int64_t)N * (b.y0 / N + dlo + t);
+        if (x >= 0 && x < X && y >= 0 && y < Y) out[(int64_t)n * ldn + (x + X * y) * ldp] = img[i];
+    }
+}
+
+}  // namespace
+
+void libwin_release_workspaces(sid_plan* p)
+{
+    if (!p->libwin) return;
+    LibWin* w = p->libwin;
+    for (DBuf* b : {&w->bpl, &w->tco, &w->ihat, &w->img, &w->cols}) b->release();
+}
+
+void libwin_free(sid_plan* p)
+{
+    if (!p->libwin) return;
+    libwin_release_workspaces(p);
+    LibWin* w = p->libwin;
+    w->kh.release();
+    w->kl.release();
+    w->geo.twiddle.release();
+    delete w;
+    p->libwin = nullptr;
+}
+
+// Window spectra for windows of at least Wo lenslets (kept on the plan; a
+// larger window serves smaller boxes too).
+static int libwin_ensure(sid_plan* p, int64_t Wo)
+{
+    if (p->libwin && p->libwin->Wo >= Wo) return SID_OK;
+    libwin_free(p);
+    int64_t L = Wo;
+    int P = 0, Q = 0;
+    while (!fft_factor(L, &P, &Q)) ++L;
+    SID_REQUIRE(L <= kLibMaxL, "sid_library_spectral: window of %lld lenslets exceeds the window grid limit",
+                (long long)Wo);
+    LibWin* w = new LibWin();
+    p->libwin = w;
+    w->Wo = Wo;
+    sid_plan& g = w->geo;
+    g.M = p->M; g.N = p->N; g.Z = p->Z;
+    g.Lx = g.Ly = Wo;
+    g.X = g.Y = Wo * p->N;
+    g.flags = 0;
+    g.device = p->device;
+    g.adj_separate = false;
+    g.g = p->g;
+    g.g.Lx = g.g.Ly = Wo;
+    g.g.X = g.g.Y = Wo * p->N;
+    g.zsplit = 1;
+    g.L = L;
+    g.nf = (L / 2 + 1) * L;
+    g.spec_f32 = g.spec_i16 = g.spec_f24 = false;
+    std::vector<float2> tw((size_t)L);
+    for (int64_t k = 0; k < L; ++k) {
+        const double a = 2.0 * M_PI * (double)k / (double)L;
+        tw[(size_t)k] = make_float2((float)std::cos(a), (float)std::sin(a));
+    }
+    SID_TRY(g.twiddle.alloc((size_t)L * sizeof(float2)));
+    SID_CUDA_TRY(cudaMemcpy(g.twiddle.p, tw.data(), (size_t)L * sizeof(float2), cudaMemcpyHostToDevice));
+    const int64_t n_out = p->N * p->N, n_in_pad = cdiv(p->N * p->N * p->Z, 8) * 8;
+    const size_t nent = (size_t)(g.nf * n_out * n_in_pad);
+    SID_TRY(w->kh.alloc(nent * sizeof(ushort2)));
+    SID_TRY(w->kl.alloc(nent * sizeof(uchar2)));
+    return build_khat_f24(p, L, g.twiddle.as<float2>(), w->kh.as<ushort2>(), w->kl.as<uchar2>());
+}
+
+template <int MU>
+static int launch_pack(dim3 grid, const float* packed, const LibBox* boxes, const int* cols, int nb, int cbase,
+                       int nchb, int n_in, int N, int dlo, int L, int BN, const float2* tw, uint32_t* h, uint32_t* m,
+                       uint32_t* l, cudaStream_t st)
+{
+    k_lib_pack<MU><<<grid, kLibPackThreads, 0, st>>>(packed, boxes, cols, nb, cbase, nchb, n_in, N, dlo, L, BN, tw,
+                                                      h, m, l);
+    SID_CHECK_LAUNCH();
+    return SID_OK;
+}
+
+}  // namespace sid
+
+using namespace sid;
+
+extern "C" int sid_library_spectral(sid_plan* p, const float* const* recon, int64_t n_comp, const double* centers,
+                                    const uint8_t* neur_id, int64_t n_neur, int64_t neur_rad, double axial,
+                                    float* out, int out_layout, void* stream)
+{
+    SID_REQUIRE(p && recon && centers && neur_id && out, "sid_library_spectral: NULL argument");
+    SID_REQUIRE(n_comp >= 1 && n_neur >= 1 && neur_rad >= 0 && axial > 0,
+                "sid_library_spectral: need n_comp >= 1, n_neur >= 1, neur_rad >= 0, axial > 0");
+    SID_REQUIRE(out_layout == 0 || out_layout == 1,
+                "sid_library_spectral: out_layout must be 0 (n x P) or 1 (P x n)");
+    SID_REQUIRE(!p->adj_separate, "sid_library_spectral: the spectral form needs odd PSF crop widths");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const int64_t N = p->N, D = p->g.D, n_out = N * N, n_in = N * N * p->Z, n_in_pad = cdiv(n_in, 8) * 8;
+    std::vector<LibBox> boxes;
+    SID_TRY(lib_stage(p, "sid_library_spectral", recon, n_comp, centers, neur_id, n_neur, neur_rad, axial, boxes,
+                      st));
+    int span = 1, mu = 1;
+    for (const LibBox& b : boxes) {
+        span = std::max(span, std::max((b.x1 - 1) / (int)N - b.x0 / (int)N, (b.y1 - 1) / (int)N - b.y0 / (int)N) + 1);
+        mu = std::max(mu, (int)std::max(cdiv(b.x1 - b.x0, N), cdiv(b.y1 - b.y0, N)));
+    }
+    SID_REQUIRE(mu <= 6, "sid_library_spectral: boxes of more than 6 lattice points per phase (use sid_library)");
+    SID_TRY(libwin_ensure(p, span + D - 1));
+    LibWin* w = p->libwin;
+    const int64_t L = w->geo.L, nf = w->geo.nf, Wo = w->Wo;
+    // passes: up to 64 neurons in depth-window order
+    std::vector<int> order((size_t)n_neur);
+    for (int64_t n = 0; n < n_neur; ++n) order[(size_t)n] = (int)n;
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+        return boxes[x].z0 != boxes[y].z0 ? boxes[x].z0 < boxes[y].z0 : boxes[x].z1 < boxes[y].z1;
+    });
+    const int G = spectral_tc_max_volumes();
+    struct Pass { int first, nb, akb0, nkb; };
+    std::vector<Pass> passes;
+    int64_t max_kpb = 0;
+    for (int i = 0; i < (int)n_neur; i += G) {
+        Pass ps;
+        ps.first = i;
+        ps.nb = (int)std::min<int64_t>(G, n_neur - i);
+        int zlo = INT32_MAX, zhi = 0;
+        for (int k = i; k < i + ps.nb; ++k) {
+            zlo = std::min(zlo, boxes[order[k]].z0);
+            zhi = std::max(zhi, boxes[order[k]].z1);
+        }
+        // K elements (complex parts interleaved) of the depths [zlo, zhi), in 64-element blocks
+        ps.akb0 = (int)((2 * n_out * zlo) / 64);
+        ps.nkb = (int)(cdiv(2 * n_out * zhi, 64) - ps.akb0);
+        max_kpb = std::max<int64_t>(max_kpb, 64 * ps.nkb);
+        passes.push_back(ps);
+    }
+    const int64_t bn_max = n_neur > 32 ? 128 : 64;
+    SID_TRY(w->bpl.alloc((size_t)(3 * nf * bn_max * max_kpb) * sizeof(uint16_t)));
+    const int gmax = (int)std::min<int64_t>(n_neur, G);
+    SID_TRY(w->tco.alloc((size_t)(nf * gmax * n_out) * sizeof(float2)));
+    SID_TRY(w->ihat.alloc((size_t)(nf * gmax * n_out) * sizeof(float2)));
+    SID_TRY(w->img.alloc((size_t)(gmax * n_out * Wo * Wo) * sizeof(float)));
+    SID_TRY(w->cols.alloc((size_t)n_neur * sizeof(int)));
+    SID_CUDA_TRY(cudaMemcpyAsync(w->cols.p, order.data(), order.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+    const int64_t P = p->X * p->Y;
+    SID_CUDA_TRY(cudaMemsetAsync(out, 0, (size_t)(P * n_neur) * sizeof(float), st));
+    const int64_t ldn = out_layout == 0 ? 1 : P, ldp = out_layout == 0 ? n_neur : 1;
+    const LibBox* dbox = p->ws[3].as<LibBox>();
+    const float* dpack = p->ws[2].as<float>();
+    for (const Pass& ps : passes) {
+        const int bn = ps.nb <= 32 ? 64 : 128;
+        const int64_t kpb = 64 * (int64_t)ps.nkb, nchb = kpb / 2;
+        const size_t plane = (size_t)(nf * bn * kpb);
+        uint16_t* bh = w->bpl.as<uint16_t>();
+        const int* cols = w->cols.as<int>() + ps.first;
+        dim3 grid((unsigned)cdiv(nchb, kLibPackThreads), (unsigned)L, (unsigned)(bn / 2));
+        uint32_t* h32 = reinterpret_cast<uint32_t*>(bh);
+        uint32_t* m32 = reinterpret_cast<uint32_t*>(bh + plane);
+        uint32_t* l32 = reinterpret_cast<uint32_t*>(bh + 2 * plane);
+        const int cbase = 32 * ps.akb0;
+        if (mu <= 3)
+            SID_TRY(launch_pack<3>(grid, dpack, dbox, cols, ps.nb, cbase, (int)nchb, (int)n_in, (int)N, (int)p->g.dlo,
+                                   (int)L, bn, w->geo.twiddle.as<float2>(), h32, m32, l32, st));
+        else
+            SID_TRY(launch_pack<6>(grid, dpack, dbox, cols, ps.nb, cbase, (int)nchb, (int)n_in, (int)N, (int)p->g.dlo,
+                                   (int)L, bn, w->geo.twiddle.as<float2>(), h32, m32, l32, st));
+        SID_TRY(spec_tc_forward_raw(w->kh.p, w->kl.p, n_out, 2 * n_in_pad, ps.akb0, bh, kpb, nf, ps.nb,
+                                    w->tco.as<float2>(), p->errflag.as<int>(), st));
+        SID_TRY(spec_tc_unpack(w->tco.as<float2>(), ps.nb, (int)n_out, (int)n_out, nf, w->ihat.as<float2>(), st));
+        SID_TRY(spec_c2r(&w->geo, w->ihat.as<float2>(), w->img.as<float>(), ps.nb * n_out, st));
+        const int64_t tot = (int64_t)ps.nb * n_out * Wo * Wo;
+        k_lib_scatter<<<(unsigned)std::min<int64_t>(cdiv(tot, 256), 152 * 16), 256, 0, st>>>(
+            w->img.as<float>(), dbox, cols, ps.nb, (int)N, (int)Wo, (int)p->g.dlo, p->X, p->Y, out, ldn, ldp);
+        SID_CHECK_LAUNCH();
+    }
+    // the staging buffers are read by the kernels above: wait before the host
+    // vectors go out of scope and before the workspaces can be reused
+    return plan_sync(p, st);
+}

@@ -207,6 +207,7 @@ extern "C" int sid_plan_create(const float* H, int64_t M, int64_t Nnum, int64_t 
 extern "C" int sid_plan_destroy(sid_plan* p)
 {
     if (!p) return SID_OK;
+    libwin_free(p);
     DBuf* bufs[] = {&p->taps_f, &p->taps_b, &p->khat_f32, &p->khat_i16, &p->rstep, &p->khat_f24h, &p->khat_f24l,
                     &p->khat_f24th, &p->khat_f24tl, &p->tcb, &p->tco, &p->twiddle, &p->weak, &p->weak_pad,
                     &p->kern, &p->kvol[0], &p->kvol[1], &p->kvol[2],
@@ -230,6 +231,7 @@ extern "C" int sid_plan_release_workspaces(sid_plan* p)
                     &p->kvol[0], &p->kvol[1], &p->kvol[2]};
     for (DBuf* b : bufs) b->release();
     for (DBuf& b : p->ws) b.release();
+    libwin_release_workspaces(p);
     return SID_OK;
 }
 

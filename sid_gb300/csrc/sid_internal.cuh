@@ -158,6 +158,10 @@ struct TapGeom {
 
 }  // namespace sid
 
+namespace sid {
+struct LibWin;  // library windows (libtc.cu)
+}
+
 // The opaque plan (declared in sid.h as struct sid_plan).
 struct sid_plan {
     int64_t M, N, Z, X, Y, Lx, Ly;
@@ -201,6 +205,9 @@ struct sid_plan {
     // events: [0] input volume converted, [1] Htf converted, [2] caller's stream 0
     cudaStream_t hstream[2] = {nullptr, nullptr};
     cudaEvent_t hevent[3] = {nullptr, nullptr, nullptr};
+    // library generation on the tensor cores: tap spectra on a small lenslet
+    // window and the per-pass workspaces (libtc.cu)
+    sid::LibWin* libwin = nullptr;
 };
 
 namespace sid {
@@ -221,6 +228,15 @@ int spectral_tc_group(const sid_plan* p, int64_t nb);  // volumes per pass that 
 int64_t vol_group(const sid_plan* p, int method, int64_t nb);  // deconv.cu: volumes per batched pass
 int spectral_forward_tc(sid_plan* p, const float* vp, float* ip, int nb, cudaStream_t st);
 int spectral_adjoint_tc(sid_plan* p, const float* ip, float* bp, int nb, cudaStream_t st);
+// the contraction alone: A = 24-bit planes (rows x kp per frequency, reduction
+// from element 64 akb0), B = three BF16 planes [f][BN][kpb], out [f][nb][rows]
+int spec_tc_forward_raw(const void* ah, const void* al, int64_t rows, int64_t kp, int akb0, const uint16_t* bplanes,
+                        int64_t kpb, int64_t nf, int nb, float2* out, int* err, cudaStream_t st);
+// dst[b][c][f] = src[f][b][c] for c < nch (rows >= nch per frequency and volume)
+int spec_tc_unpack(const float2* src, int nb, int rows, int nch, int64_t nf, float2* dst, cudaStream_t st);
+int plan_sync(sid_plan* p, cudaStream_t st);  // synchronise; an expired device wait -> SID_ETIMEOUT
+void libwin_free(sid_plan* p);
+void libwin_release_workspaces(sid_plan* p);
 // lenslet-grid real DFTs of nch channels (spectral.cu): planes [ch][Ly][Lx] <-> half spectra [ch][nf]
 int spec_r2c(sid_plan* p, const float* in, float2* out, int64_t nch, cudaStream_t st);
 int spec_c2r(sid_plan* p, const float2* in, float* out, int64_t nch, cudaStream_t st);

@@ -104,7 +104,7 @@ __device__ __forceinline__ uint4 f24_remainders(uint4 hi, uint2 lo)
 // out[(f * nb + b) * rows + r] (float2) = (D[r][2b], D[r][2b+1]) for r < rows, b < nb.
 template <int BN, int STAGES>
 __global__ void __launch_bounds__(TC_THREADS, 1)
-k_spec_tc(const __grid_constant__ SpecTcMaps maps, int rows, int nkb, int nmt, int64_t nitems, int nb,
+k_spec_tc(const __grid_constant__ SpecTcMaps maps, int rows, int nkb, int akb0, int nmt, int64_t nitems, int nb,
           float2* __restrict__ out, int* __restrict__ err)
 {
     using SM = SpecTcSmem<BN, STAGES>;
@@ -160,8 +160,8 @@ k_spec_tc(const __grid_constant__ SpecTcMaps maps, int rows, int nkb, int nmt, i
                     }
                     uint8_t* st = tsm + s * SM::STAGE;
                     mbar_arrive_expect_tx(&full[s], SM::TMA_BYTES);
-                    tma_load_3d(st, &maps.ahi, kb * TC_BK, mt * TC_BM, f, &full[s]);
-                    tma_load_3d(st + SM::OFF_LO8, &maps.alo, kb * TC_BK, mt * TC_BM, f, &full[s]);
+                    tma_load_3d(st, &maps.ahi, (akb0 + kb) * TC_BK, mt * TC_BM, f, &full[s]);
+                    tma_load_3d(st + SM::OFF_LO8, &maps.alo, (akb0 + kb) * TC_BK, mt * TC_BM, f, &full[s]);
                     tma_load_3d(st + SM::OFF_BHI, &maps.bhi, kb * TC_BK, 0, f, &full[s]);
                     tma_load_3d(st + SM::OFF_BMI, &maps.bmi, kb * TC_BK, 0, f, &full[s]);
                     tma_load_3d(st + SM::OFF_BLO, &maps.blo, kb * TC_BK, 0, f, &full[s]);
@@ -443,9 +443,9 @@ int spectral_tc_group(const sid_plan* p, int64_t nb)
 }
 
 // A maps: 24-bit planes (high halves as BF16, low bytes) of rows x kp elements
-// per frequency; B maps: BN x kp BF16 per frequency.
+// per frequency; B maps: BN x kpb BF16 per frequency.
 static int tc_maps(SpecTcMaps* m, const void* ah, const void* al, const void* bh, const void* bm, const void* bl,
-                   int64_t rows, int64_t kp, int64_t nf, int bn)
+                   int64_t rows, int64_t kp, int64_t kpb, int64_t nf, int bn)
 {
     std::memset(m, 0, sizeof(*m));
     const uint64_t da[3] = {(uint64_t)kp, (uint64_t)rows, (uint64_t)nf};
@@ -454,8 +454,8 @@ static int tc_maps(SpecTcMaps* m, const void* ah, const void* al, const void* bh
     const uint32_t boxa[3] = {TC_BK, TC_BM, 1};
     SID_TRY(encode_tmap_3d(&m->ahi, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, ah, da, sa16, boxa, CU_TENSOR_MAP_SWIZZLE_128B));
     SID_TRY(encode_tmap_3d(&m->alo, CU_TENSOR_MAP_DATA_TYPE_UINT8, al, da, sa8, boxa, CU_TENSOR_MAP_SWIZZLE_NONE));
-    const uint64_t db[3] = {(uint64_t)kp, (uint64_t)bn, (uint64_t)nf};
-    const uint64_t sb[2] = {(uint64_t)(kp * 2), (uint64_t)(bn * kp * 2)};
+    const uint64_t db[3] = {(uint64_t)kpb, (uint64_t)bn, (uint64_t)nf};
+    const uint64_t sb[2] = {(uint64_t)(kpb * 2), (uint64_t)(bn * kpb * 2)};
     const uint32_t boxb[3] = {TC_BK, (uint32_t)bn, 1};
     SID_TRY(encode_tmap_3d(&m->bhi, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, bh, db, sb, boxb, CU_TENSOR_MAP_SWIZZLE_128B));
     SID_TRY(encode_tmap_3d(&m->bmi, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, bm, db, sb, boxb, CU_TENSOR_MAP_SWIZZLE_128B));
@@ -464,8 +464,8 @@ static int tc_maps(SpecTcMaps* m, const void* ah, const void* al, const void* bh
 }
 
 template <int BN, int STAGES>
-static int launch_spec_tc(const SpecTcMaps& maps, int rows, int nkb, int64_t nf, int nb, float2* out, int* err,
-                          cudaStream_t st)
+static int launch_spec_tc(const SpecTcMaps& maps, int rows, int nkb, int akb0, int64_t nf, int nb, float2* out,
+                          int* err, cudaStream_t st)
 {
     using SM = SpecTcSmem<BN, STAGES>;
     static bool configured = false;
@@ -477,9 +477,31 @@ static int launch_spec_tc(const SpecTcMaps& maps, int rows, int nkb, int64_t nf,
     const int nmt = (int)cdiv(rows, TC_BM);
     const int64_t nitems = (int64_t)nmt * nf;
     const unsigned grid = (unsigned)std::min<int64_t>(nitems, sm_count());
-    k_spec_tc<BN, STAGES><<<grid, TC_THREADS, SM::TOTAL, st>>>(maps, rows, nkb, nmt, nitems, nb, out, err);
+    k_spec_tc<BN, STAGES><<<grid, TC_THREADS, SM::TOTAL, st>>>(maps, rows, nkb, akb0, nmt, nitems, nb, out, err);
     SID_CHECK_LAUNCH();
     return SID_OK;
+}
+
+// stages: 3 x 64 KB (BN = 64) or 2 x 88 KB (BN = 128) of the 227 KB of shared memory
+static int spec_tc_run(const SpecTcMaps& maps, int bn, int rows, int nkb, int akb0, int64_t nf, int nb, float2* out,
+                       int* err, cudaStream_t st)
+{
+    return bn == 64 ? launch_spec_tc<64, 3>(maps, rows, nkb, akb0, nf, nb, out, err, st)
+                    : launch_spec_tc<128, 2>(maps, rows, nkb, akb0, nf, nb, out, err, st);
+}
+
+int spec_tc_forward_raw(const void* ah, const void* al, int64_t rows, int64_t kp, int akb0, const uint16_t* bplanes,
+                        int64_t kpb, int64_t nf, int nb, float2* out, int* err, cudaStream_t st)
+{
+    SID_REQUIRE(nb >= 1 && nb <= kTcMaxVolumes, "tensor-core projection: %d volumes outside [1, %d]", nb,
+                kTcMaxVolumes);
+    SID_REQUIRE(kpb % TC_BK == 0 && akb0 >= 0 && (int64_t)akb0 * TC_BK + kpb <= cdiv(kp, TC_BK) * TC_BK,
+                "tensor-core projection: reduction range outside the operator");
+    const int bn = nb <= 32 ? 64 : 128;
+    const size_t plane = (size_t)(nf * bn * kpb);
+    SpecTcMaps maps;
+    SID_TRY(tc_maps(&maps, ah, al, bplanes, bplanes + plane, bplanes + 2 * plane, rows, kp, kpb, nf, bn));
+    return spec_tc_run(maps, bn, (int)rows, (int)(kpb / TC_BK), akb0, nf, nb, out, err, st);
 }
 
 // One contraction: A (rows x kp per frequency), B from nb channel spectra
@@ -506,17 +528,19 @@ static int tc_contract(sid_plan* p, bool adj, const float2* src, int nb, int64_t
         SID_CHECK_LAUNCH();
     }
     SpecTcMaps maps;
-    SID_TRY(tc_maps(&maps, ah, al, bh, bm, bl, rows, kp, nf, bn));
+    SID_TRY(tc_maps(&maps, ah, al, bh, bm, bl, rows, kp, kp, nf, bn));
     const int nkb = (int)cdiv(kp, TC_BK);
     p->timer.begin(st);
-    // stages: 3 x 64 KB (BN = 64) or 2 x 88 KB (BN = 128) of the 227 KB of shared memory
-    int rc = bn == 64 ? launch_spec_tc<64, 3>(maps, (int)rows, nkb, nf, nb, p->tco.as<float2>(), p->errflag.as<int>(), st)
-                      : launch_spec_tc<128, 2>(maps, (int)rows, nkb, nf, nb, p->tco.as<float2>(),
-                                               p->errflag.as<int>(), st);
+    int rc = spec_tc_run(maps, bn, (int)rows, nkb, 0, nf, nb, p->tco.as<float2>(), p->errflag.as<int>(), st);
     p->timer.finish(st);
     SID_TRY(rc);
-    dim3 grid((unsigned)cdiv(nch_out, 32), (unsigned)cdiv(nf, 32), (unsigned)nb);
-    k_tc_unpack<<<grid, 256, 0, st>>>(p->tco.as<float2>(), nb, (int)rows, (int)nch_out, (int)nf, dst);
+    return spec_tc_unpack(p->tco.as<float2>(), nb, (int)rows, (int)nch_out, nf, dst, st);
+}
+
+int spec_tc_unpack(const float2* src, int nb, int rows, int nch, int64_t nf, float2* dst, cudaStream_t st)
+{
+    dim3 grid((unsigned)cdiv(nch, 32), (unsigned)cdiv(nf, 32), (unsigned)nb);
+    k_tc_unpack<<<grid, 256, 0, st>>>(src, nb, rows, nch, (int)nf, dst);
     SID_CHECK_LAUNCH();
     return SID_OK;
 }

@@ -225,6 +225,33 @@ int build_spectra(sid_plan* p)
     return weak_build(p);
 }
 
+// 24-bit tap spectra [f][b'a'][abc] of the plan's forward taps on an L x L
+// lenslet grid other than the plan's own (the library's neuron windows):
+// twiddles tw[k] = exp(2 pi i k / L), planes h / l of nf = (L/2+1) L rows.
+int build_khat_f24(const sid_plan* p, int64_t L, const float2* tw, ushort2* h, uchar2* l)
+{
+    const int64_t N = p->N, Z = p->Z, D = p->g.D;
+    const int64_t H1 = L / 2 + 1, nf = H1 * L;
+    const int64_t n_out = N * N, n_in = N * N * Z, n_in_pad = spec_nin_pad(p);
+    const int64_t tbs = cdiv(N * D * D, 32) * 32;
+    const size_t nent = (size_t)(nf * n_out * n_in_pad);
+    SID_CUDA_TRY(cudaMemset(h, 0, nent * sizeof(ushort2)));
+    SID_CUDA_TRY(cudaMemset(l, 0, nent * sizeof(uchar2)));
+    const size_t smem = (size_t)(KB_CH * D * H1 + L) * sizeof(float2) + (size_t)(KB_CH * D * D) * sizeof(float);
+    SID_REQUIRE(smem <= 200 * 1024, "spectral plan: tap arrays too large for the spectra builder (D=%lld, L=%lld)",
+                (long long)D, (long long)L);
+    SID_CUDA_TRY(cudaFuncSetAttribute(k_build_khat, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    DBuf rowmax;  // written by the builder, not needed here
+    SID_TRY(rowmax.alloc((size_t)(nf * n_out) * sizeof(unsigned)));
+    dim3 grid((unsigned)n_out, (unsigned)cdiv(n_in, KB_CH));
+    k_build_khat<<<grid, 256, smem>>>(p->taps_f.as<float>(), tw, nullptr, nullptr, h, l, rowmax.as<unsigned int>(),
+                                      nullptr, 0, (int)N, (int)n_in, n_in_pad, (int)D, (int)p->g.dlo, (int)L, tbs);
+    SID_CHECK_LAUNCH();
+    SID_CUDA_TRY(cudaDeviceSynchronize());
+    rowmax.release();
+    return SID_OK;
+}
+
 // -------------------------------------------------------------- real DFTs --
 // Both transforms are small complex matrix products per channel, computed as
 // register-blocked GEMMs against twiddle tables held in shared memory (built

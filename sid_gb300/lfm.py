@@ -566,13 +566,18 @@ def library_boxes(centers, neur_rad, axial, size):
     return out
 
 
-def generate_LFM_library_GPU(recon, centers, neur_id, psf, options, layout="rows"):
+def generate_LFM_library_GPU(recon, centers, neur_id, psf, options, layout="rows", method="direct"):
     """forward_model = generate_LFM_library_GPU(recon, centers, neur_id, psf, options)
     (generate_LFM_library_GPU.m:1).  recon: list of (X, Y, Z) volumes; centers:
     (n, 3) 1-based; neur_id: (n, n_comp) logical; psf: dict with 'H';
     options: dict with 'neur_rad', 'axial'.  Returns the (n, X*Y) library on
     the GPU ('rows', the reference's layout) or its transpose (X*Y, n)
-    ('columns', the layout the NNLS solvers take)."""
+    ('columns', the layout the NNLS solvers take).  method 'direct': FP32
+    lenslet taps (sid_library); 'spectral': the tensor-core spectral
+    projector on lenslet windows around the boxes (sid_library_spectral,
+    about 1e-5 relative per row)."""
+    if method not in ("direct", "spectral"):
+        raise ValueError(f"method must be 'direct' or 'spectral', not {method!r}")
     H = psf["H"] if isinstance(psf, dict) else psf
     vols = [to_device(r) for r in recon]
     X, Y, Z = vols[0].shape
@@ -585,7 +590,8 @@ def generate_LFM_library_GPU(recon, centers, neur_id, psf, options, layout="rows
         out = _fortran_tensor((n, X * Y), vols[0].device)
     else:
         out = _fortran_tensor((X * Y, n), vols[0].device)
-    _lib.call("sid_library", proj._plan, ctypes.cast(ptrs, ctypes.c_void_p), len(vols), c.ctypes.data,
+    fn = "sid_library" if method == "direct" else "sid_library_spectral"
+    _lib.call(fn, proj._plan, ctypes.cast(ptrs, ctypes.c_void_p), len(vols), c.ctypes.data,
               ids.ctypes.data, n, int(options["neur_rad"]), float(options["axial"]), out.data_ptr(),
               0 if layout == "rows" else 1, _stream_ptr())
     return out

@@ -31,7 +31,8 @@
  *              imgs X x Y x n, X X x Y x Z x n (groups of components per pass)
  *   [X, hist] = sid_mex('isra_ex', plan, Htf, Xguess, maxIter, mode, p, lambda, method)   mode 0 basic, 1 TV
  *   X        = sid_mex('ls_deconv_ex', plan, df, max_iter, lamb_L1, lamb_L2, lamb_TV_L2, lamb_TV_L1, method)
- *   F        = sid_mex('library', plan, recon, centers, neur_id, neur_rad, axial)   recon: cell of volumes
+ *   F        = sid_mex('library', plan, recon, centers, neur_id, neur_rad, axial[, method])   recon: cell of
+ *              volumes; method 'direct' (default, FP32 lenslet taps) or 'spectral' (tensor-core windows)
  *   Fm       = sid_mex('spatial_update', T, Y, template, opts)     template: logical (R - bg_sub) x P
  *   [xx, Q, df, h] = sid_mex('fast_nnls_ex', A, Y, opts, Q, df, h)  every fast_nnls input and output
  *   x        = sid_mex('reg_nnls', A, d, opts)                      A m x n, d m double gpuArrays
@@ -712,9 +713,17 @@ void mexFunction(int nlhs, mxArray* plhs[], int nrhs, const mxArray* prhs[])
         return;
     }
     if (!strcmp(cmd, "library")) {
-        /* F = sid_mex('library', plan, recon, centers, neur_id, neur_rad, axial): recon a cell of X x Y x Z
-         * single gpuArrays, centers n x 3 double, neur_id n x numel(recon) logical; F n x P single gpuArray */
+        /* F = sid_mex('library', plan, recon, centers, neur_id, neur_rad, axial[, method]): recon a cell of
+         * X x Y x Z single gpuArrays, centers n x 3 double, neur_id n x numel(recon) logical; method 'direct'
+         * or 'spectral'; F n x P single gpuArray */
         sid_plan* p = plan_arg(prhs[1]);
+        int spectral = 0;
+        if (nrhs > 7) {
+            char m[16];
+            if (mxGetString(prhs[7], m, sizeof(m)) != 0 || (strcmp(m, "direct") && strcmp(m, "spectral")))
+                mexErrMsgIdAndTxt("sid:library", "method must be 'direct' or 'spectral'");
+            spectral = !strcmp(m, "spectral");
+        }
         const mxArray* rc_cell = prhs[2];
         const mwSize nc = mxGetNumberOfElements(rc_cell);
         if (nc < 1 || nc > 4096) mexErrMsgIdAndTxt("sid:library", "recon must be a cell of 1..4096 volumes");
@@ -733,8 +742,10 @@ void mexFunction(int nlhs, mxArray* plhs[], int nrhs, const mxArray* prhs[])
         sid_plan_info(p, info);
         mwSize df[2] = {n, (mwSize)(info[3] * info[4])};
         mxGPUArray* F = mxGPUCreateGPUArray(2, df, mxSINGLE_CLASS, mxREAL, MX_GPU_DO_NOT_INITIALIZE);
-        int rc = sid_library(p, ptrs, (int64_t)nc, mxGetPr(prhs[3]), idp, (int64_t)n, (int64_t)mxGetScalar(prhs[5]),
-                             mxGetScalar(prhs[6]), (float*)mxGPUGetData(F), 0, NULL);
+        int rc = (spectral ? sid_library_spectral : sid_library)(p, ptrs, (int64_t)nc, mxGetPr(prhs[3]), idp,
+                                                                 (int64_t)n, (int64_t)mxGetScalar(prhs[5]),
+                                                                 mxGetScalar(prhs[6]), (float*)mxGPUGetData(F), 0,
+                                                                 NULL);
         for (mwSize k = 0; k < nc; ++k) mxGPUDestroyGPUArray(vols[k]);
         mxDestroyArray(ids);
         if (rc != SID_OK) mxGPUDestroyGPUArray(F);

@@ -47,3 +47,55 @@ def test_library_matches_oracle(gpu, oracle, rad):
         assert rel_l2(got[n], ref[n]) < 1e-5, n
     cols = s.to_numpy(s.generate_LFM_library_GPU(recon, centers, neur_id, {"H": H}, opts, layout="columns"))
     np.testing.assert_array_equal(cols, got.T)
+
+
+def _library_problem(N, Z, M, L, n, rad, seed, sig=(1.5, 6.0), axial=2.0):
+    from sid_gb300 import synthetic
+    X = N * L
+    H = synthetic.gaussian_psf(M, N, Z, sigma_min=sig[0], sigma_max=sig[1])
+    rng = np.random.default_rng(seed)
+    recon = [synthetic.blob_volume(X, X, Z, 30, sigma=(1.5, 3.0), seed=seed + k) for k in range(2)]
+    centers = np.stack([rng.uniform(1, X, n), rng.uniform(1, X, n), rng.uniform(1, Z, n)], 1)
+    centers[0] = [1.0, 1.0, 1.0]          # corner: most of the footprint outside the frame
+    centers[1] = [X - 0.2, X / 2, Z]      # far edge, last depth
+    neur_id = rng.random((n, 2)) < 0.6
+    neur_id[:, 0] = True
+    return H, recon, centers, neur_id, {"neur_rad": rad, "axial": axial}
+
+
+@pytest.mark.gpu
+# boxes of 1, 2 and 4 lattice points per phase (the 3- and 6-point pack kernels)
+@pytest.mark.parametrize("rad", [4, 2, 9])
+def test_spectral_library_matches_oracle(gpu, oracle, rad):
+    """sid_library_spectral (tensor-core windows) against the FP64 oracle: the
+    24-bit tap spectra give ~1e-5 per row."""
+    import sid_gb300 as s
+    H, recon, centers, neur_id, opts = _library_problem(5, 7, 41, 12, 12, rad, 3)
+    got = s.to_numpy(s.generate_LFM_library_GPU(recon, centers, neur_id, {"H": H}, opts, method="spectral"))
+    ref = oracle.generate_library(recon, centers, neur_id, H, rad, 2.0)
+    assert got.shape == ref.shape
+    assert rel_l2(got, ref) < 2e-5, rel_l2(got, ref)
+    worst = max(rel_l2(got[n], ref[n]) for n in range(12))
+    assert worst < 5e-5, worst
+    cols = s.to_numpy(s.generate_LFM_library_GPU(recon, centers, neur_id, {"H": H}, opts, layout="columns",
+                                                 method="spectral"))
+    np.testing.assert_array_equal(cols, got.T)
+
+
+@pytest.mark.gpu
+def test_spectral_library_many_passes(gpu, oracle):
+    """150 neurons: three contraction passes (64, 64 and 22 neurons: both tile
+    widths), each over its own depth range (5-depth windows of 9), at Nnum 15
+    with the 25-pixel boxes of neur_rad 12 (two row tiles of output phases);
+    against the FP32 tap kernel, and 6 rows against the oracle."""
+    import sid_gb300 as s
+    H, recon, centers, neur_id, opts = _library_problem(15, 9, 75, 9, 150, 12, 11, sig=(2.0, 9.0), axial=6.0)
+    spec = s.to_numpy(s.generate_LFM_library_GPU(recon, centers, neur_id, {"H": H}, opts, method="spectral"))
+    direct = s.to_numpy(s.generate_LFM_library_GPU(recon, centers, neur_id, {"H": H}, opts))
+    assert rel_l2(spec, direct) < 2e-5, rel_l2(spec, direct)
+    worst = max(rel_l2(spec[n], direct[n]) for n in range(150))
+    assert worst < 5e-5, worst
+    pick = [0, 1, 40, 77, 128, 149]
+    ref = oracle.generate_library(recon, centers[pick], neur_id[pick], H, 12, 6.0)
+    for k, n in enumerate(pick):
+        assert rel_l2(spec[n], ref[k]) < 5e-5, n
