@@ -48,6 +48,8 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="budget of the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-nnls", action="store_true", help="skip the library + temporal NNLS measurement")
+    ap.add_argument("--library-only", action="store_true",
+                    help="time only the library generation (--nnls-neurons neurons) and print its numbers")
     ap.add_argument("--nnls-frames", type=int, default=3000)
     ap.add_argument("--nnls-neurons", type=int, default=800)
     ap.add_argument("--no-demix", action="store_true", help="skip the demixing-loop measurement")
@@ -164,12 +166,11 @@ class Clocks:
                 "samples": len(sm)}
 
 
-def nnls_inputs(P_proj, K, F):
-    """Library generation (K anisotropic Gaussian neurons in the projector's
-    volume, generate_LFM_library_GPU.m:63-109, through the plan's lenslet taps,
-    timed) and the temporal NNLS movie Y = S'T + b + noise from it (FP16 and
-    FP32 copies).  Returns (A (P x K, L2-normalised columns), Y16, Yf, T_true,
-    library ms)."""
+def library_timing(P_proj, K):
+    """Library generation for K anisotropic Gaussian neurons in the projector's
+    volume (generate_LFM_library_GPU.m:63-109), timed through the FP32 lenslet
+    taps (sid_library) and the tensor-core windows (sid_library_spectral).
+    Returns (A (P x K, the FP32 taps' rows, unnormalised), timings)."""
     import ctypes
 
     import numpy as np
@@ -206,6 +207,17 @@ def nnls_inputs(P_proj, K, F):
             lib_ms[fn]["rel_l2_vs_direct_worst_row"] = float(d.max())
             del dst
     P_proj.release_workspaces()
+    return A, lib_ms
+
+
+def nnls_inputs(P_proj, K, F):
+    """Library generation (library_timing) and the temporal NNLS movie
+    Y = S'T + b + noise from it (FP16 and FP32 copies).  Returns (A (P x K,
+    L2-normalised columns), Y16, Yf, T_true, library timings)."""
+    import torch
+
+    from sid_gb300 import synthetic
+    A, lib_ms = library_timing(P_proj, K)
     # L2-normalise library rows (temporal_SID_update.m:42)
     nrm = torch.linalg.vector_norm(A, dim=0)
     A.div_(nrm.clamp_min(1e-30))
@@ -623,9 +635,17 @@ def main():
     if not args.no_nnls and "direct" not in plan_methods:
         plan_methods.append("direct")  # the library generation reads the lenslet taps
     # the tensor-core batched projections need the transposed 24-bit spectra
-    tc = args.method == "spectral_mixed" and args.batch_volumes > 1
+    tc = args.method == "spectral_mixed" and args.batch_volumes > 1 and not args.library_only
+    if args.library_only:
+        plan_methods = ["direct"]  # both library forms read only the lenslet taps
     P = s.Projector(H, (X, Y), None, methods=tuple(plan_methods), batched=tc)
     info = P.info()
+    if args.library_only:
+        _, lib = library_timing(P, args.nnls_neurons)
+        if rank == 0:
+            print(json.dumps({"workload": f"library {args.nnls_neurons} neurons (neur_rad 12, axial 2) at "
+                                          f"{X}x{Y}x{Z}", "library": lib}))
+        return 0
     # RL input: Htf = A^T y with y = A V_true (the reference starts ISRA at Xguess = Htf)
     y = P.forward(Vt, method=args.method)
     Htf = P.adjoint(y, method=args.method)

@@ -18,9 +18,10 @@
 //      lattice points, written straight into the contraction's B operand
 //      (three BF16 parts, columns (Vr, -Vi) and (Vi, Vr) per neuron);
 //   2. k_spec_tc over the window spectra (24-bit planes), the pass's K range;
-//   3. the output spectra unpacked and inverse-transformed on the window grid;
-//   4. k_lib_scatter: window lenslets into the library rows (pixels outside
-//      the frame dropped; the rest of each row is zero).
+//   3. k_lib_synth: per neuron and output phase, the inverse real DFT of the
+//      window spectrum straight from the contraction's output, written into
+//      the library row (pixels outside the frame dropped; the rest of each row
+//      is zero).
 // Precision is the tensor-core forward projection's (24-bit spectra, B split
 // to FP32's 24 bits, FP32 accumulation): about 1e-5 relative per row, against
 // FP32 rounding for the tap kernels of library.cu.
@@ -38,17 +39,19 @@ bool fft_factor(int64_t L, int* P, int* Q);
 int build_khat_f24(const sid_plan* p, int64_t L, const float2* tw, ushort2* h, uchar2* l);
 
 struct LibWin {
-    int64_t Wo = 0;  // window lenslets per axis
-    sid_plan geo;    // window geometry for the inverse DFTs: Lx = Ly = Wo, X = Y = Wo N, L, nf, twiddles
-    DBuf kh, kl;     // window tap spectra, 24-bit planes [f][b'a'][abc]
-    DBuf bpl;        // B operand planes of one pass
-    DBuf tco, ihat, img, cols;
+    int64_t Wo = 0;      // window lenslets per axis
+    int64_t L = 0, nf = 0;  // window grid length, frequencies (L/2+1) L
+    DBuf tw;             // L float2: exp(2 pi i k / L)
+    DBuf kh, kl;         // window tap spectra, 24-bit planes [f][b'a'][abc]
+    DBuf bpl;            // B operand planes of one pass
+    DBuf tco, cols;      // contraction output [f][neuron][b'a'], neurons in pass order
 };
 
 namespace {
 
 constexpr int kLibPackThreads = 128;
-constexpr int kLibMaxL = 64;  // window grid lengths handled by the pack kernel
+constexpr int kLibMaxL = 64;  // window grid lengths handled by the pack and synthesis kernels
+constexpr int kLibSynthThreads = 256;
 
 __device__ __forceinline__ void split3(float x0, float x1, uint32_t& h, uint32_t& m, uint32_t& l)
 {
@@ -66,10 +69,11 @@ __device__ __forceinline__ void split3(float x0, float x1, uint32_t& h, uint32_t
 
 // B planes [f][BN][kpb] for one pass: thread (channel cbase + cc, neuron slot j)
 // evaluates the channel's spectrum at the H1 frequencies f1 of row f2 =
-// blockIdx.y, Vhat(f1, f2) = sum_{u,v} V(u, v) exp(-2 pi i (f1 pu + f2 pv) / L)
-// over the box's lattice points (pu, pv: window coordinates mod L), and writes
-// the two columns of slot j (zeros for empty slots and channels).  MU bounds the
-// lattice points per axis and phase.
+// blockIdx.y, separably over the box's lattice points (pu, pv: window
+// coordinates mod L):
+//   R(u) = sum_v V(u, v) exp(-2 pi i f2 pv / L),  Vhat(f1) = sum_u R(u) exp(-2 pi i f1 pu / L)
+// and writes the two columns of slot j (zeros for empty slots and channels).
+// MU bounds the lattice points per axis and phase.
 template <int MU>
 __global__ void __launch_bounds__(kLibPackThreads)
 k_lib_pack(const float* __restrict__ packed, const LibBox* __restrict__ boxes, const int* __restrict__ cols, int nb,
@@ -83,12 +87,12 @@ k_lib_pack(const float* __restrict__ packed, const LibBox* __restrict__ boxes, c
     if (cc >= nchb) return;
     const int j = blockIdx.z, f2 = blockIdx.y, H1 = L / 2 + 1;
     const int c = cbase + cc;
-    // empty slots and channels keep zero values at phase 0
-    float val[MU * MU];
-    int ph[MU * MU], du[MU * MU];
+    // empty slots and channels keep zero rows at phase 0
+    float2 R[MU];
+    int ph[MU], du[MU];
 #pragma unroll
-    for (int q = 0; q < MU * MU; ++q) {
-        val[q] = 0.f;
+    for (int q = 0; q < MU; ++q) {
+        R[q] = make_float2(0.f, 0.f);
         ph[q] = 0;
         du[q] = 0;
     }
@@ -103,27 +107,34 @@ k_lib_pack(const float* __restrict__ packed, const LibBox* __restrict__ boxes, c
             const int vlo = (b.y0 - bb + N - 1 + N) / N - 1, vhi = (b.y1 - 1 - bb + N) / N - 1;
             const float* src = packed + b.off + (int64_t)bw * bh * (z - b.z0);
 #pragma unroll
-            for (int iv = 0; iv < MU; ++iv)
+            for (int iv = 0; iv < MU; ++iv) {
+                const int v = vlo + iv;
+                if (v > vhi) break;
+                const int pv = ((v - w0y) % L + L) % L;
+                const float2 w = stw[(int)(((int64_t)f2 * pv) % L)];
 #pragma unroll
                 for (int iu = 0; iu < MU; ++iu) {
-                    const int u = ulo + iu, v = vlo + iv, q = iv * MU + iu;
-                    if (u <= uhi && v <= vhi) {
-                        val[q] = src[(a + N * u - b.x0) + bw * (bb + N * v - b.y0)];
-                        const int pu = ((u - w0x) % L + L) % L, pv = ((v - w0y) % L + L) % L;
-                        ph[q] = (int)(((int64_t)f2 * pv) % L);  // phase at f1 = 0
-                        du[q] = pu;
+                    const int u = ulo + iu;
+                    if (u <= uhi) {
+                        const float val = src[(a + N * u - b.x0) + bw * (bb + N * v - b.y0)];
+                        R[iu].x = fmaf(val, w.x, R[iu].x);  // val exp(-i theta)
+                        R[iu].y = fmaf(-val, w.y, R[iu].y);
                     }
                 }
+            }
+#pragma unroll
+            for (int iu = 0; iu < MU; ++iu) du[iu] = ((ulo + iu - w0x) % L + L) % L;
         }
     }
     const int64_t kw = nchb;  // 32-bit words (complex parts as a BF16 pair) per B row
     for (int f1 = 0; f1 < H1; ++f1) {
         float re = 0.f, im = 0.f;
 #pragma unroll
-        for (int q = 0; q < MU * MU; ++q) {
+        for (int q = 0; q < MU; ++q) {
+            // R exp(-i theta) = (Rx cos + Ry sin) + i (Ry cos - Rx sin)
             const float2 w = stw[ph[q]];
-            re = fmaf(val[q], w.x, re);
-            im = fmaf(-val[q], w.y, im);
+            re = fmaf(R[q].x, w.x, fmaf(R[q].y, w.y, re));
+            im = fmaf(R[q].y, w.x, fmaf(-R[q].x, w.y, im));
             const int nx = ph[q] + du[q];
             ph[q] = nx >= L ? nx - L : nx;
         }
@@ -138,24 +149,60 @@ k_lib_pack(const float* __restrict__ packed, const LibBox* __restrict__ boxes, c
     }
 }
 
-// img[j][b'a'][t][s] (window lenslets) -> library rows of the pass's neurons
-__global__ void k_lib_scatter(const float* __restrict__ img, const LibBox* __restrict__ boxes,
-                              const int* __restrict__ cols, int nb, int N, int Wo, int dlo, int64_t X, int64_t Y,
-                              float* __restrict__ out, int64_t ldn, int64_t ldp)
+// Inverse real DFT of one window spectrum per CTA (neuron slot j = blockIdx.y,
+// output phase o = blockIdx.x), from the contraction output S = tco[f][j][o]
+// (f = f1 + H1 f2), into the library row of the slot's neuron:
+//   G(f1, t)   = sum_f2 S(f1, f2) w^(t f2)                            t < Wo
+//   img(t, s)  = 1/L^2 sum_f1 c(f1) Re(G(f1, t) w^(s f1))            s < Wo
+// with w = exp(2 pi i / L), c = 1 at f1 = 0 and at L/2 (even L), else 2;
+// window lenslet (s, t) is pixel (a' + N (w0x + s), b' + N (w0y + t)).
+__global__ void __launch_bounds__(kLibSynthThreads)
+k_lib_synth(const float2* __restrict__ tco, const LibBox* __restrict__ boxes, const int* __restrict__ cols, int nb,
+            int rows, int N, int L, int Wo, int dlo, int64_t X, int64_t Y, const float2* __restrict__ tw,
+            float* __restrict__ out, int64_t ldn, int64_t ldp)
 {
-    const int64_t per = (int64_t)N * N * Wo * Wo, total = per * nb;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
-         i += (int64_t)gridDim.x * blockDim.x) {
-        const int j = (int)(i / per);
-        const int64_t r = i - j * per;
-        const int o = (int)(r / ((int64_t)Wo * Wo));
-        const int q = (int)(r - (int64_t)o * Wo * Wo);
-        const int t = q / Wo, s = q - t * Wo;
-        const int n = cols[j];
-        const LibBox b = boxes[n];
-        const int64_t x = (o % N) + (int64_t)N * (b.x0 / N + dlo + s);
-        const int64_t y = (o / N) + (int64_t)N * (b.y0 / N + dlo + t);
-        if (x >= 0 && x < X && y >= 0 && y < Y) out[(int64_t)n * ldn + (x + X * y) * ldp] = img[i];
+    __shared__ float2 stw[kLibMaxL];
+    __shared__ float2 S[kLibMaxL / 2 + 1][kLibMaxL];  // [f1][f2]
+    __shared__ float2 G[kLibMaxL / 2 + 1][kLibMaxL];  // [f1][t]
+    const int o = blockIdx.x, j = blockIdx.y, H1 = L / 2 + 1, nf = H1 * L;
+    for (int i = threadIdx.x; i < L; i += blockDim.x) stw[i] = tw[i];
+    for (int f = threadIdx.x; f < nf; f += blockDim.x) {
+        const int f2 = f / H1;
+        S[f - f2 * H1][f2] = tco[((int64_t)f * nb + j) * rows + o];
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < H1 * Wo; i += blockDim.x) {
+        const int f1 = i / Wo, t = i - f1 * Wo;
+        float gr = 0.f, gi = 0.f;
+        int ph = 0;
+        for (int f2 = 0; f2 < L; ++f2) {
+            const float2 sv = S[f1][f2], w = stw[ph];
+            gr = fmaf(sv.x, w.x, fmaf(-sv.y, w.y, gr));
+            gi = fmaf(sv.x, w.y, fmaf(sv.y, w.x, gi));
+            ph += t;
+            ph = ph >= L ? ph - L : ph;
+        }
+        G[f1][t] = make_float2(gr, gi);
+    }
+    __syncthreads();
+    const LibBox b = boxes[cols[j]];
+    const int n = cols[j];
+    const int64_t x0 = (o % N) + (int64_t)N * (b.x0 / N + dlo), y0 = (o / N) + (int64_t)N * (b.y0 / N + dlo);
+    const float inv = 1.0f / ((float)L * (float)L);
+    for (int i = threadIdx.x; i < Wo * Wo; i += blockDim.x) {
+        const int t = i / Wo, s = i - t * Wo;
+        const int64_t x = x0 + (int64_t)N * s, y = y0 + (int64_t)N * t;
+        if (x < 0 || x >= X || y < 0 || y >= Y) continue;
+        float acc = 0.f;
+        int ph = 0;
+        for (int f1 = 0; f1 < H1; ++f1) {
+            const float2 g = G[f1][t], w = stw[ph];
+            const float cf = (f1 == 0 || 2 * f1 == L) ? 1.f : 2.f;
+            acc = fmaf(cf, fmaf(g.x, w.x, -g.y * w.y), acc);
+            ph += s;
+            ph = ph >= L ? ph - L : ph;
+        }
+        out[(int64_t)n * ldn + (x + X * y) * ldp] = acc * inv;
     }
 }
 
@@ -165,7 +212,7 @@ void libwin_release_workspaces(sid_plan* p)
 {
     if (!p->libwin) return;
     LibWin* w = p->libwin;
-    for (DBuf* b : {&w->bpl, &w->tco, &w->ihat, &w->img, &w->cols}) b->release();
+    for (DBuf* b : {&w->bpl, &w->tco, &w->cols}) b->release();
 }
 
 void libwin_free(sid_plan* p)
@@ -175,7 +222,7 @@ void libwin_free(sid_plan* p)
     LibWin* w = p->libwin;
     w->kh.release();
     w->kl.release();
-    w->geo.twiddle.release();
+    w->tw.release();
     delete w;
     p->libwin = nullptr;
 }
@@ -194,32 +241,20 @@ static int libwin_ensure(sid_plan* p, int64_t Wo)
     LibWin* w = new LibWin();
     p->libwin = w;
     w->Wo = Wo;
-    sid_plan& g = w->geo;
-    g.M = p->M; g.N = p->N; g.Z = p->Z;
-    g.Lx = g.Ly = Wo;
-    g.X = g.Y = Wo * p->N;
-    g.flags = 0;
-    g.device = p->device;
-    g.adj_separate = false;
-    g.g = p->g;
-    g.g.Lx = g.g.Ly = Wo;
-    g.g.X = g.g.Y = Wo * p->N;
-    g.zsplit = 1;
-    g.L = L;
-    g.nf = (L / 2 + 1) * L;
-    g.spec_f32 = g.spec_i16 = g.spec_f24 = false;
+    w->L = L;
+    w->nf = (L / 2 + 1) * L;
     std::vector<float2> tw((size_t)L);
     for (int64_t k = 0; k < L; ++k) {
         const double a = 2.0 * M_PI * (double)k / (double)L;
         tw[(size_t)k] = make_float2((float)std::cos(a), (float)std::sin(a));
     }
-    SID_TRY(g.twiddle.alloc((size_t)L * sizeof(float2)));
-    SID_CUDA_TRY(cudaMemcpy(g.twiddle.p, tw.data(), (size_t)L * sizeof(float2), cudaMemcpyHostToDevice));
+    SID_TRY(w->tw.alloc((size_t)L * sizeof(float2)));
+    SID_CUDA_TRY(cudaMemcpy(w->tw.p, tw.data(), (size_t)L * sizeof(float2), cudaMemcpyHostToDevice));
     const int64_t n_out = p->N * p->N, n_in_pad = cdiv(p->N * p->N * p->Z, 8) * 8;
-    const size_t nent = (size_t)(g.nf * n_out * n_in_pad);
+    const size_t nent = (size_t)(w->nf * n_out * n_in_pad);
     SID_TRY(w->kh.alloc(nent * sizeof(ushort2)));
     SID_TRY(w->kl.alloc(nent * sizeof(uchar2)));
-    return build_khat_f24(p, L, g.twiddle.as<float2>(), w->kh.as<ushort2>(), w->kl.as<uchar2>());
+    return build_khat_f24(p, L, w->tw.as<float2>(), w->kh.as<ushort2>(), w->kl.as<uchar2>());
 }
 
 template <int MU>
@@ -260,7 +295,7 @@ extern "C" int sid_library_spectral(sid_plan* p, const float* const* recon, int6
     SID_REQUIRE(mu <= 6, "sid_library_spectral: boxes of more than 6 lattice points per phase (use sid_library)");
     SID_TRY(libwin_ensure(p, span + D - 1));
     LibWin* w = p->libwin;
-    const int64_t L = w->geo.L, nf = w->geo.nf, Wo = w->Wo;
+    const int64_t L = w->L, nf = w->nf, Wo = w->Wo;
     // passes: up to 64 neurons in depth-window order
     std::vector<int> order((size_t)n_neur);
     for (int64_t n = 0; n < n_neur; ++n) order[(size_t)n] = (int)n;
@@ -290,8 +325,6 @@ extern "C" int sid_library_spectral(sid_plan* p, const float* const* recon, int6
     SID_TRY(w->bpl.alloc((size_t)(3 * nf * bn_max * max_kpb) * sizeof(uint16_t)));
     const int gmax = (int)std::min<int64_t>(n_neur, G);
     SID_TRY(w->tco.alloc((size_t)(nf * gmax * n_out) * sizeof(float2)));
-    SID_TRY(w->ihat.alloc((size_t)(nf * gmax * n_out) * sizeof(float2)));
-    SID_TRY(w->img.alloc((size_t)(gmax * n_out * Wo * Wo) * sizeof(float)));
     SID_TRY(w->cols.alloc((size_t)n_neur * sizeof(int)));
     SID_CUDA_TRY(cudaMemcpyAsync(w->cols.p, order.data(), order.size() * sizeof(int), cudaMemcpyHostToDevice, st));
     const int64_t P = p->X * p->Y;
@@ -312,17 +345,15 @@ extern "C" int sid_library_spectral(sid_plan* p, const float* const* recon, int6
         const int cbase = 32 * ps.akb0;
         if (mu <= 3)
             SID_TRY(launch_pack<3>(grid, dpack, dbox, cols, ps.nb, cbase, (int)nchb, (int)n_in, (int)N, (int)p->g.dlo,
-                                   (int)L, bn, w->geo.twiddle.as<float2>(), h32, m32, l32, st));
+                                   (int)L, bn, w->tw.as<float2>(), h32, m32, l32, st));
         else
             SID_TRY(launch_pack<6>(grid, dpack, dbox, cols, ps.nb, cbase, (int)nchb, (int)n_in, (int)N, (int)p->g.dlo,
-                                   (int)L, bn, w->geo.twiddle.as<float2>(), h32, m32, l32, st));
+                                   (int)L, bn, w->tw.as<float2>(), h32, m32, l32, st));
         SID_TRY(spec_tc_forward_raw(w->kh.p, w->kl.p, n_out, 2 * n_in_pad, ps.akb0, bh, kpb, nf, ps.nb,
                                     w->tco.as<float2>(), p->errflag.as<int>(), st));
-        SID_TRY(spec_tc_unpack(w->tco.as<float2>(), ps.nb, (int)n_out, (int)n_out, nf, w->ihat.as<float2>(), st));
-        SID_TRY(spec_c2r(&w->geo, w->ihat.as<float2>(), w->img.as<float>(), ps.nb * n_out, st));
-        const int64_t tot = (int64_t)ps.nb * n_out * Wo * Wo;
-        k_lib_scatter<<<(unsigned)std::min<int64_t>(cdiv(tot, 256), 152 * 16), 256, 0, st>>>(
-            w->img.as<float>(), dbox, cols, ps.nb, (int)N, (int)Wo, (int)p->g.dlo, p->X, p->Y, out, ldn, ldp);
+        k_lib_synth<<<dim3((unsigned)n_out, (unsigned)ps.nb), kLibSynthThreads, 0, st>>>(
+            w->tco.as<float2>(), dbox, cols, ps.nb, (int)n_out, (int)N, (int)L, (int)Wo, (int)p->g.dlo, p->X, p->Y,
+            w->tw.as<float2>(), out, ldn, ldp);
         SID_CHECK_LAUNCH();
     }
     // the staging buffers are read by the kernels above: wait before the host
