@@ -22,9 +22,9 @@
 //      window spectrum straight from the contraction's output, written into
 //      the library row (pixels outside the frame dropped; the rest of each row
 //      is zero).
-// Precision is the tensor-core forward projection's (24-bit spectra, B split
-// to FP32's 24 bits, FP32 accumulation): about 1e-5 relative per row, against
-// FP32 rounding for the tap kernels of library.cu.
+// Precision: 24-bit window spectra, box spectra split into two BF16 parts
+// (16-17 bits), three MMA passes with FP32 accumulation -- about 1e-5 relative
+// per row, against FP32 rounding for the tap kernels of library.cu.
 #include <algorithm>
 #include <cmath>
 #include <vector>
@@ -52,6 +52,20 @@ namespace {
 constexpr int kLibPackThreads = 128;
 constexpr int kLibMaxL = 64;  // window grid lengths handled by the pack and synthesis kernels
 constexpr int kLibSynthThreads = 256;
+// B planes of the library contraction: two (hi, lo) and three MMA passes.  The
+// window spectra carry 16 significant bits; B to 16-17 bits and the dropped
+// A_lo B_lo product (below 2^-16 of each term) keep the rows within ~1e-5.
+constexpr int kLibBPlanes = 2;
+
+// x = hi + lo to 16-17 significant bits (hi: x rounded to BF16; lo: the remainder rounded)
+__device__ __forceinline__ void split2(float x0, float x1, uint32_t& h, uint32_t& l)
+{
+    const __nv_bfloat162 hi = __floats2bfloat162_rn(x0, x1);
+    const float2 hf = __bfloat1622float2(hi);
+    const __nv_bfloat162 lo = __floats2bfloat162_rn(x0 - hf.x, x1 - hf.y);
+    h = *reinterpret_cast<const uint32_t*>(&hi);
+    l = *reinterpret_cast<const uint32_t*>(&lo);
+}
 
 __device__ __forceinline__ void split3(float x0, float x1, uint32_t& h, uint32_t& m, uint32_t& l)
 {
@@ -72,9 +86,10 @@ __device__ __forceinline__ void split3(float x0, float x1, uint32_t& h, uint32_t
 // blockIdx.y, separably over the box's lattice points (pu, pv: window
 // coordinates mod L):
 //   R(u) = sum_v V(u, v) exp(-2 pi i f2 pv / L),  Vhat(f1) = sum_u R(u) exp(-2 pi i f1 pu / L)
-// and writes the two columns of slot j (zeros for empty slots and channels).
-// MU bounds the lattice points per axis and phase.
-template <int MU>
+// and writes the two columns of slot j (zeros for empty slots and channels)
+// as NBP BF16 planes (bmi unused for two).  MU bounds the lattice points per
+// axis and phase.
+template <int MU, int NBP>
 __global__ void __launch_bounds__(kLibPackThreads)
 k_lib_pack(const float* __restrict__ packed, const LibBox* __restrict__ boxes, const int* __restrict__ cols, int nb,
            int cbase, int nchb, int n_in, int N, int dlo, int L, int BN, const float2* __restrict__ tw,
@@ -142,10 +157,17 @@ k_lib_pack(const float* __restrict__ packed, const LibBox* __restrict__ boxes, c
         uint32_t h, m, l;
         // column 2j: (Vr, -Vi); column 2j + 1: (Vi, Vr)
         const int64_t o0 = (f * BN + 2 * j) * kw + cc, o1 = o0 + kw;
-        split3(re, -im, h, m, l);
-        bhi[o0] = h; bmi[o0] = m; blo[o0] = l;
-        split3(im, re, h, m, l);
-        bhi[o1] = h; bmi[o1] = m; blo[o1] = l;
+        if (NBP == 3) {
+            split3(re, -im, h, m, l);
+            bhi[o0] = h; bmi[o0] = m; blo[o0] = l;
+            split3(im, re, h, m, l);
+            bhi[o1] = h; bmi[o1] = m; blo[o1] = l;
+        } else {
+            split2(re, -im, h, l);
+            bhi[o0] = h; blo[o0] = l;
+            split2(im, re, h, l);
+            bhi[o1] = h; blo[o1] = l;
+        }
     }
 }
 
@@ -262,8 +284,8 @@ static int launch_pack(dim3 grid, const float* packed, const LibBox* boxes, cons
                        int nchb, int n_in, int N, int dlo, int L, int BN, const float2* tw, uint32_t* h, uint32_t* m,
                        uint32_t* l, cudaStream_t st)
 {
-    k_lib_pack<MU><<<grid, kLibPackThreads, 0, st>>>(packed, boxes, cols, nb, cbase, nchb, n_in, N, dlo, L, BN, tw,
-                                                      h, m, l);
+    k_lib_pack<MU, kLibBPlanes><<<grid, kLibPackThreads, 0, st>>>(packed, boxes, cols, nb, cbase, nchb, n_in, N, dlo,
+                                                                   L, BN, tw, h, m, l);
     SID_CHECK_LAUNCH();
     return SID_OK;
 }
@@ -322,7 +344,7 @@ extern "C" int sid_library_spectral(sid_plan* p, const float* const* recon, int6
         passes.push_back(ps);
     }
     const int64_t bn_max = n_neur > 32 ? 128 : 64;
-    SID_TRY(w->bpl.alloc((size_t)(3 * nf * bn_max * max_kpb) * sizeof(uint16_t)));
+    SID_TRY(w->bpl.alloc((size_t)(kLibBPlanes * nf * bn_max * max_kpb) * sizeof(uint16_t)));
     const int gmax = (int)std::min<int64_t>(n_neur, G);
     SID_TRY(w->tco.alloc((size_t)(nf * gmax * n_out) * sizeof(float2)));
     SID_TRY(w->cols.alloc((size_t)n_neur * sizeof(int)));
@@ -341,7 +363,7 @@ extern "C" int sid_library_spectral(sid_plan* p, const float* const* recon, int6
         dim3 grid((unsigned)cdiv(nchb, kLibPackThreads), (unsigned)L, (unsigned)(bn / 2));
         uint32_t* h32 = reinterpret_cast<uint32_t*>(bh);
         uint32_t* m32 = reinterpret_cast<uint32_t*>(bh + plane);
-        uint32_t* l32 = reinterpret_cast<uint32_t*>(bh + 2 * plane);
+        uint32_t* l32 = reinterpret_cast<uint32_t*>(bh + (kLibBPlanes - 1) * plane);
         const int cbase = 32 * ps.akb0;
         if (mu <= 3)
             SID_TRY(launch_pack<3>(grid, dpack, dbox, cols, ps.nb, cbase, (int)nchb, (int)n_in, (int)N, (int)p->g.dlo,
@@ -349,7 +371,7 @@ extern "C" int sid_library_spectral(sid_plan* p, const float* const* recon, int6
         else
             SID_TRY(launch_pack<6>(grid, dpack, dbox, cols, ps.nb, cbase, (int)nchb, (int)n_in, (int)N, (int)p->g.dlo,
                                    (int)L, bn, w->tw.as<float2>(), h32, m32, l32, st));
-        SID_TRY(spec_tc_forward_raw(w->kh.p, w->kl.p, n_out, 2 * n_in_pad, ps.akb0, bh, kpb, nf, ps.nb,
+        SID_TRY(spec_tc_forward_raw(w->kh.p, w->kl.p, n_out, 2 * n_in_pad, ps.akb0, bh, kLibBPlanes, kpb, nf, ps.nb,
                                     w->tco.as<float2>(), p->errflag.as<int>(), st));
         k_lib_synth<<<dim3((unsigned)n_out, (unsigned)ps.nb), kLibSynthThreads, 0, st>>>(
             w->tco.as<float2>(), dbox, cols, ps.nb, (int)n_out, (int)N, (int)L, (int)Wo, (int)p->g.dlo, p->X, p->Y,

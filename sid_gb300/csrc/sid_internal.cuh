@@ -229,9 +229,10 @@ int64_t vol_group(const sid_plan* p, int method, int64_t nb);  // deconv.cu: vol
 int spectral_forward_tc(sid_plan* p, const float* vp, float* ip, int nb, cudaStream_t st);
 int spectral_adjoint_tc(sid_plan* p, const float* ip, float* bp, int nb, cudaStream_t st);
 // the contraction alone: A = 24-bit planes (rows x kp per frequency, reduction
-// from element 64 akb0), B = three BF16 planes [f][BN][kpb], out [f][nb][rows]
+// from element 64 akb0), B = nbp (3: hi, mid, lo; 2: hi, lo) BF16 planes
+// [f][BN][kpb] back to back, out [f][nb][rows]
 int spec_tc_forward_raw(const void* ah, const void* al, int64_t rows, int64_t kp, int akb0, const uint16_t* bplanes,
-                        int64_t kpb, int64_t nf, int nb, float2* out, int* err, cudaStream_t st);
+                        int nbp, int64_t kpb, int64_t nf, int nb, float2* out, int* err, cudaStream_t st);
 // dst[b][c][f] = src[f][b][c] for c < nch (rows >= nch per frequency and volume)
 int spec_tc_unpack(const float2* src, int nb, int rows, int nch, int64_t nf, float2* dst, cudaStream_t st);
 int plan_sync(sid_plan* p, cudaStream_t st);  // synchronise; an expired device wait -> SID_ETIMEOUT

@@ -60,19 +60,21 @@ struct SpecTcMaps {
     CUtensorMap ahi, alo, bhi, bmi, blo;
 };
 
-template <int BN, int STAGES>
+// NBP: B planes, 3 (hi, mid, lo) or 2 (hi, lo: 16-17 significant bits)
+template <int BN, int STAGES, int NBP>
 struct SpecTcSmem {
+    static_assert(NBP == 2 || NBP == 3, "B is split into two or three BF16 planes");
     static constexpr int AHI = TC_BM * TC_BK * 2;  // 16 KB: high halves (BF16), swizzled
     static constexpr int ALO = AHI;                // remainders (BF16), same layout
     static constexpr int B = BN * TC_BK * 2;       // one B plane
     static constexpr int LO8 = TC_BM * TC_BK;      // 8 KB: low bytes, row-major
     static constexpr int OFF_ALO = AHI;
     static constexpr int OFF_BHI = AHI + ALO;
-    static constexpr int OFF_BMI = OFF_BHI + B;
-    static constexpr int OFF_BLO = OFF_BMI + B;
+    static constexpr int OFF_BMI = OFF_BHI + B;    // (three planes)
+    static constexpr int OFF_BLO = OFF_BHI + (NBP - 1) * B;
     static constexpr int OFF_LO8 = OFF_BLO + B;
     static constexpr int STAGE = OFF_LO8 + LO8;
-    static constexpr int TMA_BYTES = AHI + 3 * B + LO8;
+    static constexpr int TMA_BYTES = AHI + NBP * B + LO8;
     static constexpr int TOTAL = STAGES * STAGE + 1024;
     static_assert(B % 1024 == 0 && STAGE % 1024 == 0, "stage tiles must stay 1024-byte aligned");
     static_assert(TOTAL <= 227 * 1024, "stages exceed the shared memory of one CTA");
@@ -102,12 +104,14 @@ __device__ __forceinline__ uint4 f24_remainders(uint4 hi, uint2 lo)
 }
 
 // out[(f * nb + b) * rows + r] (float2) = (D[r][2b], D[r][2b+1]) for r < rows, b < nb.
-template <int BN, int STAGES>
+// NBP = 3: five MMA passes A_hi (B_hi + B_mid + B_lo) + A_lo (B_hi + B_mid);
+// NBP = 2: three, A_hi (B_hi + B_lo) + A_lo B_hi.
+template <int BN, int STAGES, int NBP>
 __global__ void __launch_bounds__(TC_THREADS, 1)
 k_spec_tc(const __grid_constant__ SpecTcMaps maps, int rows, int nkb, int akb0, int nmt, int64_t nitems, int nb,
           float2* __restrict__ out, int* __restrict__ err)
 {
-    using SM = SpecTcSmem<BN, STAGES>;
+    using SM = SpecTcSmem<BN, STAGES, NBP>;
     constexpr uint32_t TMEM_COLS = 2 * BN;  // two accumulators
     constexpr int HALF = BN / 2;            // columns per drain warp
     static_assert(HALF % 32 == 0, "BN must be a multiple of 64");
@@ -163,7 +167,7 @@ k_spec_tc(const __grid_constant__ SpecTcMaps maps, int rows, int nkb, int akb0, 
                     tma_load_3d(st, &maps.ahi, (akb0 + kb) * TC_BK, mt * TC_BM, f, &full[s]);
                     tma_load_3d(st + SM::OFF_LO8, &maps.alo, (akb0 + kb) * TC_BK, mt * TC_BM, f, &full[s]);
                     tma_load_3d(st + SM::OFF_BHI, &maps.bhi, kb * TC_BK, 0, f, &full[s]);
-                    tma_load_3d(st + SM::OFF_BMI, &maps.bmi, kb * TC_BK, 0, f, &full[s]);
+                    if (NBP == 3) tma_load_3d(st + SM::OFF_BMI, &maps.bmi, kb * TC_BK, 0, f, &full[s]);
                     tma_load_3d(st + SM::OFF_BLO, &maps.blo, kb * TC_BK, 0, f, &full[s]);
                 }
                 if (*(volatile int*)&abort_flag) break;
@@ -196,10 +200,10 @@ k_spec_tc(const __grid_constant__ SpecTcMaps maps, int rows, int nkb, int akb0, 
                             const uint32_t o = kk * 32;  // 16 elements inside the 128-byte swizzle row
                             mma_bf16(acc, smem_desc_sw128(ahi + o), smem_desc_sw128(bhi + o), idesc, first ? 0 : 1);
                             first = false;
-                            mma_bf16(acc, smem_desc_sw128(ahi + o), smem_desc_sw128(bmi + o), idesc, 1);
+                            if (NBP == 3) mma_bf16(acc, smem_desc_sw128(ahi + o), smem_desc_sw128(bmi + o), idesc, 1);
                             mma_bf16(acc, smem_desc_sw128(ahi + o), smem_desc_sw128(blo + o), idesc, 1);
                             mma_bf16(acc, smem_desc_sw128(alo + o), smem_desc_sw128(bhi + o), idesc, 1);
-                            mma_bf16(acc, smem_desc_sw128(alo + o), smem_desc_sw128(bmi + o), idesc, 1);
+                            if (NBP == 3) mma_bf16(acc, smem_desc_sw128(alo + o), smem_desc_sw128(bmi + o), idesc, 1);
                         }
                         mma_commit(&empty[s]);
                     }
@@ -463,36 +467,42 @@ static int tc_maps(SpecTcMaps* m, const void* ah, const void* al, const void* bh
     return SID_OK;
 }
 
-template <int BN, int STAGES>
+template <int BN, int STAGES, int NBP>
 static int launch_spec_tc(const SpecTcMaps& maps, int rows, int nkb, int akb0, int64_t nf, int nb, float2* out,
                           int* err, cudaStream_t st)
 {
-    using SM = SpecTcSmem<BN, STAGES>;
+    using SM = SpecTcSmem<BN, STAGES, NBP>;
     static bool configured = false;
     if (!configured) {
-        SID_CUDA_TRY(cudaFuncSetAttribute(k_spec_tc<BN, STAGES>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        SID_CUDA_TRY(cudaFuncSetAttribute(k_spec_tc<BN, STAGES, NBP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           SM::TOTAL));
         configured = true;
     }
     const int nmt = (int)cdiv(rows, TC_BM);
     const int64_t nitems = (int64_t)nmt * nf;
     const unsigned grid = (unsigned)std::min<int64_t>(nitems, sm_count());
-    k_spec_tc<BN, STAGES><<<grid, TC_THREADS, SM::TOTAL, st>>>(maps, rows, nkb, akb0, nmt, nitems, nb, out, err);
+    k_spec_tc<BN, STAGES, NBP><<<grid, TC_THREADS, SM::TOTAL, st>>>(maps, rows, nkb, akb0, nmt, nitems, nb, out,
+                                                                     err);
     SID_CHECK_LAUNCH();
     return SID_OK;
 }
 
-// stages: 3 x 64 KB (BN = 64) or 2 x 88 KB (BN = 128) of the 227 KB of shared memory
-static int spec_tc_run(const SpecTcMaps& maps, int bn, int rows, int nkb, int akb0, int64_t nf, int nb, float2* out,
-                       int* err, cudaStream_t st)
+// stages of the 227 KB of shared memory: three B planes 3 x 64 KB (BN = 64) or
+// 2 x 88 KB (BN = 128); two B planes 4 x 56 KB or 3 x 72 KB
+static int spec_tc_run(const SpecTcMaps& maps, int bn, int nbp, int rows, int nkb, int akb0, int64_t nf, int nb,
+                       float2* out, int* err, cudaStream_t st)
 {
-    return bn == 64 ? launch_spec_tc<64, 3>(maps, rows, nkb, akb0, nf, nb, out, err, st)
-                    : launch_spec_tc<128, 2>(maps, rows, nkb, akb0, nf, nb, out, err, st);
+    if (nbp == 2)
+        return bn == 64 ? launch_spec_tc<64, 4, 2>(maps, rows, nkb, akb0, nf, nb, out, err, st)
+                        : launch_spec_tc<128, 3, 2>(maps, rows, nkb, akb0, nf, nb, out, err, st);
+    return bn == 64 ? launch_spec_tc<64, 3, 3>(maps, rows, nkb, akb0, nf, nb, out, err, st)
+                    : launch_spec_tc<128, 2, 3>(maps, rows, nkb, akb0, nf, nb, out, err, st);
 }
 
 int spec_tc_forward_raw(const void* ah, const void* al, int64_t rows, int64_t kp, int akb0, const uint16_t* bplanes,
-                        int64_t kpb, int64_t nf, int nb, float2* out, int* err, cudaStream_t st)
+                        int nbp, int64_t kpb, int64_t nf, int nb, float2* out, int* err, cudaStream_t st)
 {
+    SID_REQUIRE(nbp == 2 || nbp == 3, "tensor-core projection: B in %d planes", nbp);
     SID_REQUIRE(nb >= 1 && nb <= kTcMaxVolumes, "tensor-core projection: %d volumes outside [1, %d]", nb,
                 kTcMaxVolumes);
     SID_REQUIRE(kpb % TC_BK == 0 && akb0 >= 0 && (int64_t)akb0 * TC_BK + kpb <= cdiv(kp, TC_BK) * TC_BK,
@@ -500,8 +510,8 @@ int spec_tc_forward_raw(const void* ah, const void* al, int64_t rows, int64_t kp
     const int bn = nb <= 32 ? 64 : 128;
     const size_t plane = (size_t)(nf * bn * kpb);
     SpecTcMaps maps;
-    SID_TRY(tc_maps(&maps, ah, al, bplanes, bplanes + plane, bplanes + 2 * plane, rows, kp, kpb, nf, bn));
-    return spec_tc_run(maps, bn, (int)rows, (int)(kpb / TC_BK), akb0, nf, nb, out, err, st);
+    SID_TRY(tc_maps(&maps, ah, al, bplanes, bplanes + plane, bplanes + (nbp - 1) * plane, rows, kp, kpb, nf, bn));
+    return spec_tc_run(maps, bn, nbp, (int)rows, (int)(kpb / TC_BK), akb0, nf, nb, out, err, st);
 }
 
 // One contraction: A (rows x kp per frequency), B from nb channel spectra
@@ -531,7 +541,7 @@ static int tc_contract(sid_plan* p, bool adj, const float2* src, int nb, int64_t
     SID_TRY(tc_maps(&maps, ah, al, bh, bm, bl, rows, kp, kp, nf, bn));
     const int nkb = (int)cdiv(kp, TC_BK);
     p->timer.begin(st);
-    int rc = spec_tc_run(maps, bn, (int)rows, nkb, 0, nf, nb, p->tco.as<float2>(), p->errflag.as<int>(), st);
+    int rc = spec_tc_run(maps, bn, 3, (int)rows, nkb, 0, nf, nb, p->tco.as<float2>(), p->errflag.as<int>(), st);
     p->timer.finish(st);
     SID_TRY(rc);
     return spec_tc_unpack(p->tco.as<float2>(), nb, (int)rows, (int)nch_out, nf, dst, st);
