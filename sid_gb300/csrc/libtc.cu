@@ -51,7 +51,7 @@ namespace {
 
 constexpr int kLibPackThreads = 128;
 constexpr int kLibMaxL = 64;  // window grid lengths handled by the pack and synthesis kernels
-constexpr int kLibSynthThreads = 256;
+constexpr int kLibSynthWarps = 4;  // output phases per synthesis CTA
 // B planes of the library contraction: two (hi, lo) and three MMA passes.  The
 // window spectra carry 16 significant bits; B to 16-17 bits and the dropped
 // A_lo B_lo product (below 2^-16 of each term) keep the rows within ~1e-5.
@@ -171,54 +171,65 @@ k_lib_pack(const float* __restrict__ packed, const LibBox* __restrict__ boxes, c
     }
 }
 
-// Inverse real DFT of one window spectrum per CTA (neuron slot j = blockIdx.y,
-// output phase o = blockIdx.x), from the contraction output S = tco[f][j][o]
-// (f = f1 + H1 f2), into the library row of the slot's neuron:
+// Inverse real DFT of the window spectra, one warp per (neuron slot j =
+// blockIdx.y, output phase o = kLibSynthWarps blockIdx.x + warp), from the
+// contraction output S = tco[f][j][o] (f = f1 + H1 f2) into the library row of
+// the slot's neuron:
 //   G(f1, t)   = sum_f2 S(f1, f2) w^(t f2)                            t < Wo
 //   img(t, s)  = 1/L^2 sum_f1 c(f1) Re(G(f1, t) w^(s f1))            s < Wo
 // with w = exp(2 pi i / L), c = 1 at f1 = 0 and at L/2 (even L), else 2;
-// window lenslet (s, t) is pixel (a' + N (w0x + s), b' + N (w0y + t)).
-__global__ void __launch_bounds__(kLibSynthThreads)
+// window lenslet (s, t) is pixel (a' + N (w0x + s), b' + N (w0y + t)).  The
+// CTA's warps take consecutive output phases, so the spectra arrive in
+// 32-byte pieces; shared memory: twiddles, then per warp S [H1][L], G [H1][Wo].
+__global__ void __launch_bounds__(kLibSynthWarps * 32)
 k_lib_synth(const float2* __restrict__ tco, const LibBox* __restrict__ boxes, const int* __restrict__ cols, int nb,
             int rows, int N, int L, int Wo, int dlo, int64_t X, int64_t Y, const float2* __restrict__ tw,
             float* __restrict__ out, int64_t ldn, int64_t ldp)
 {
-    __shared__ float2 stw[kLibMaxL];
-    __shared__ float2 S[kLibMaxL / 2 + 1][kLibMaxL];  // [f1][f2]
-    __shared__ float2 G[kLibMaxL / 2 + 1][kLibMaxL];  // [f1][t]
-    const int o = blockIdx.x, j = blockIdx.y, H1 = L / 2 + 1, nf = H1 * L;
+    extern __shared__ float2 syn_sm[];
+    const int H1 = L / 2 + 1, nf = H1 * L, per = H1 * L + H1 * Wo;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int j = blockIdx.y, o0 = blockIdx.x * kLibSynthWarps;
+    float2* stw = syn_sm;
     for (int i = threadIdx.x; i < L; i += blockDim.x) stw[i] = tw[i];
-    for (int f = threadIdx.x; f < nf; f += blockDim.x) {
-        const int f2 = f / H1;
-        S[f - f2 * H1][f2] = tco[((int64_t)f * nb + j) * rows + o];
+    for (int i = threadIdx.x; i < nf * kLibSynthWarps; i += blockDim.x) {
+        const int f = i / kLibSynthWarps, q = i - f * kLibSynthWarps;
+        if (o0 + q < rows) {
+            const int f2 = f / H1;
+            syn_sm[L + q * per + (f - f2 * H1) * L + f2] = tco[((int64_t)f * nb + j) * rows + o0 + q];
+        }
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < H1 * Wo; i += blockDim.x) {
+    const int o = o0 + warp;
+    if (o >= rows) return;
+    const float2* S = syn_sm + L + warp * per;
+    float2* G = syn_sm + L + warp * per + H1 * L;
+    for (int i = lane; i < H1 * Wo; i += 32) {
         const int f1 = i / Wo, t = i - f1 * Wo;
         float gr = 0.f, gi = 0.f;
         int ph = 0;
         for (int f2 = 0; f2 < L; ++f2) {
-            const float2 sv = S[f1][f2], w = stw[ph];
+            const float2 sv = S[f1 * L + f2], w = stw[ph];
             gr = fmaf(sv.x, w.x, fmaf(-sv.y, w.y, gr));
             gi = fmaf(sv.x, w.y, fmaf(sv.y, w.x, gi));
             ph += t;
             ph = ph >= L ? ph - L : ph;
         }
-        G[f1][t] = make_float2(gr, gi);
+        G[f1 * Wo + t] = make_float2(gr, gi);
     }
-    __syncthreads();
-    const LibBox b = boxes[cols[j]];
+    __syncwarp();
     const int n = cols[j];
+    const LibBox b = boxes[n];
     const int64_t x0 = (o % N) + (int64_t)N * (b.x0 / N + dlo), y0 = (o / N) + (int64_t)N * (b.y0 / N + dlo);
     const float inv = 1.0f / ((float)L * (float)L);
-    for (int i = threadIdx.x; i < Wo * Wo; i += blockDim.x) {
+    for (int i = lane; i < Wo * Wo; i += 32) {
         const int t = i / Wo, s = i - t * Wo;
         const int64_t x = x0 + (int64_t)N * s, y = y0 + (int64_t)N * t;
         if (x < 0 || x >= X || y < 0 || y >= Y) continue;
         float acc = 0.f;
         int ph = 0;
         for (int f1 = 0; f1 < H1; ++f1) {
-            const float2 g = G[f1][t], w = stw[ph];
+            const float2 g = G[f1 * Wo + t], w = stw[ph];
             const float cf = (f1 == 0 || 2 * f1 == L) ? 1.f : 2.f;
             acc = fmaf(cf, fmaf(g.x, w.x, -g.y * w.y), acc);
             ph += s;
@@ -354,6 +365,9 @@ extern "C" int sid_library_spectral(sid_plan* p, const float* const* recon, int6
     const int64_t ldn = out_layout == 0 ? 1 : P, ldp = out_layout == 0 ? n_neur : 1;
     const LibBox* dbox = p->ws[3].as<LibBox>();
     const float* dpack = p->ws[2].as<float>();
+    const int64_t H1 = L / 2 + 1;
+    const size_t synth_smem = (size_t)(L + kLibSynthWarps * (H1 * L + H1 * Wo)) * sizeof(float2);
+    SID_CUDA_TRY(cudaFuncSetAttribute(k_lib_synth, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)synth_smem));
     for (const Pass& ps : passes) {
         const int bn = ps.nb <= 32 ? 64 : 128;
         const int64_t kpb = 64 * (int64_t)ps.nkb, nchb = kpb / 2;
@@ -373,9 +387,9 @@ extern "C" int sid_library_spectral(sid_plan* p, const float* const* recon, int6
                                    (int)L, bn, w->tw.as<float2>(), h32, m32, l32, st));
         SID_TRY(spec_tc_forward_raw(w->kh.p, w->kl.p, n_out, 2 * n_in_pad, ps.akb0, bh, kLibBPlanes, kpb, nf, ps.nb,
                                     w->tco.as<float2>(), p->errflag.as<int>(), st));
-        k_lib_synth<<<dim3((unsigned)n_out, (unsigned)ps.nb), kLibSynthThreads, 0, st>>>(
-            w->tco.as<float2>(), dbox, cols, ps.nb, (int)n_out, (int)N, (int)L, (int)Wo, (int)p->g.dlo, p->X, p->Y,
-            w->tw.as<float2>(), out, ldn, ldp);
+        k_lib_synth<<<dim3((unsigned)cdiv(n_out, kLibSynthWarps), (unsigned)ps.nb), kLibSynthWarps * 32, synth_smem,
+                      st>>>(w->tco.as<float2>(), dbox, cols, ps.nb, (int)n_out, (int)N, (int)L, (int)Wo, (int)p->g.dlo,
+                            p->X, p->Y, w->tw.as<float2>(), out, ldn, ldp);
         SID_CHECK_LAUNCH();
     }
     // the staging buffers are read by the kernels above: wait before the host
