@@ -899,6 +899,10 @@ def main():
                                        if "spectral_f32" in others else None),
             "plan": {"L": info["L"], "D": info["D"], "device_gb": info["device_bytes"] / 1e9},
             "batched_components": batched,
+            # the mixed-precision batched form per volume-iteration against the FP32 paths one volume at a time
+            "batched_mixed_vs_fp32": ({m: (1e3 / batched["ms_per_volume_iteration"]) / others[m]["rl_iter_s"]
+                                       for m in ("spectral_f32", "direct") if m in others}
+                                      if batched else None),
             "nnls": nnls,
             "demix": demix,
         }
