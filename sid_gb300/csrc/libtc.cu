@@ -241,6 +241,15 @@ k_lib_synth(const float2* __restrict__ tco, const LibBox* __restrict__ boxes, co
 
 }  // namespace
 
+int64_t libwin_bytes(const sid_plan* p)
+{
+    if (!p->libwin) return 0;
+    const LibWin* w = p->libwin;
+    int64_t b = 0;
+    for (const DBuf* d : {&w->tw, &w->kh, &w->kl, &w->bpl, &w->tco, &w->cols}) b += (int64_t)d->bytes;
+    return b;
+}
+
 void libwin_release_workspaces(sid_plan* p)
 {
     if (!p->libwin) return;

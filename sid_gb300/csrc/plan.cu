@@ -209,7 +209,7 @@ extern "C" int sid_plan_destroy(sid_plan* p)
     if (!p) return SID_OK;
     libwin_free(p);
     DBuf* bufs[] = {&p->taps_f, &p->taps_b, &p->khat_f32, &p->khat_i16, &p->rstep, &p->khat_f24h, &p->khat_f24l,
-                    &p->khat_f24th, &p->khat_f24tl, &p->tcb, &p->tco, &p->twiddle, &p->weak, &p->weak_pad,
+                    &p->khat_f24th, &p->khat_f24tl, &p->tcb, &p->tco, &p->twiddle, &p->weak, &p->weak_pad, &p->weak_part,
                     &p->kern, &p->kvol[0], &p->kvol[1], &p->kvol[2],
                     &p->vp, &p->ip, &p->bp, &p->ipart, &p->vhat, &p->ihat, &p->bhat, &p->red, &p->errflag};
     for (DBuf* b : bufs) b->release();
@@ -228,7 +228,7 @@ extern "C" int sid_plan_release_workspaces(sid_plan* p)
     SID_REQUIRE(p, "sid_plan_release_workspaces: NULL plan");
     SID_CUDA_TRY(cudaDeviceSynchronize());
     DBuf* bufs[] = {&p->vp, &p->ip, &p->bp, &p->ipart, &p->vhat, &p->ihat, &p->bhat, &p->red, &p->tcb, &p->tco,
-                    &p->kvol[0], &p->kvol[1], &p->kvol[2]};
+                    &p->kvol[0], &p->kvol[1], &p->kvol[2], &p->weak_part};
     for (DBuf* b : bufs) b->release();
     for (DBuf& b : p->ws) b.release();
     libwin_release_workspaces(p);
@@ -242,12 +242,14 @@ extern "C" int sid_plan_info(const sid_plan* p, int64_t* info)
                           &p->khat_f24l, &p->khat_f24th, &p->khat_f24tl, &p->tcb, &p->tco, &p->twiddle,
                           &p->weak, &p->weak_pad, &p->kern, &p->kvol[0],
                           &p->kvol[1], &p->kvol[2], &p->vp, &p->ip, &p->bp, &p->ipart, &p->vhat, &p->ihat,
-                          &p->bhat, &p->red};
-    int64_t bytes = 0;
+                          &p->bhat, &p->red, &p->weak_part};
+    int64_t bytes = libwin_bytes(p);
     for (const DBuf* b : bufs) bytes += (int64_t)b->bytes;
     for (const DBuf& b : p->ws) bytes += (int64_t)b.bytes;
+    // launches of one volume's weak-voxel fix: lattice copy, column and row runs, the split's sum
     const int64_t weak_launches =
-        p->nweak == 0 ? 0 : (p->weak_pad.p ? 1 + (p->nweak_cols > 0) + (p->nweak_rows > 0) : 1);
+        p->nweak == 0 ? 0
+                      : (p->weak_pad.p ? 1 + (p->nweak_cols > 0) + (p->nweak_rows > 0) + (weak_qsplit(p, 1) > 1) : 1);
     int64_t v[14] = {p->M, p->N, p->Z, p->X, p->Y, p->Lx, p->Ly, p->g.D, p->L, bytes,
                      p->flags, p->adj_separate ? 1 : 0, p->nweak, weak_launches};
     std::memcpy(info, v, sizeof(v));

@@ -189,6 +189,7 @@ struct sid_plan {
     sid::DBuf weak;             // runs (column runs, then row runs) of the weakly observed voxels
     sid::DBuf weak_pad;         //   (recomputed exactly after each spectral back projection) and the
     int64_t nweak = 0;          //   zero-padded sensor-lattice copies their kernel reads
+    sid::DBuf weak_part;        //   (partial sums when the tap arrays are split over several CTAs)
     int64_t nweak_cols = 0, nweak_rows = 0;
     double weak_frac = 1e-2;    // ... those with column mass A'1 below this fraction of the largest
     // workspaces
@@ -245,6 +246,8 @@ int conv_poly(sid_plan* p, const float* in_vp, float* out_vp, cudaStream_t st);
 int weak_build(sid_plan* p);
 int weak_fix(sid_plan* p, const float* ip, float* bp, cudaStream_t st);
 int weak_fix_n(sid_plan* p, const float* ip, float* bp, int nb, cudaStream_t st);  // nb back to back
+int weak_qsplit(const sid_plan* p, int64_t nb);  // CTAs per weak run (> 1: a finishing launch adds the parts)
+int64_t libwin_bytes(const sid_plan* p);         // device bytes of the library windows
 int v_to_vp(const sid_plan* p, const float* V, float* vp, int64_t Z, cudaStream_t st);
 int vp_to_v(const sid_plan* p, const float* vp, float* V, int64_t Z, cudaStream_t st);
 int mask_vp(const sid_plan* p, float* vp, int64_t Z, cudaStream_t st);

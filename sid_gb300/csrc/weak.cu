@@ -73,17 +73,25 @@ __global__ void k_pad_lattice(const float* __restrict__ ip, float* __restrict__ 
 // ROW = true:  row runs (fixed v, u = start + j) on padT[q][s][t].
 // Lanes take the cross-axis taps c (m1 of a column run, m2 of a row run) whose
 // lattice line lies on the sensor; when at most 16 do, each half-warp takes its
-// own tap array.  DM >= D bounds the tap loop, JR >= run length the outputs.
+// own tap array.  DM >= D bounds the tap loop (taps m >= D are zero), JR >=
+// run length the outputs; the lattice line is streamed through the taps, so a
+// thread holds DM taps and JR sums.
+// blockIdx.z splits the N^2 tap arrays into qs ranges when there are too few
+// runs to fill the GPU: each CTA then writes its partial sums to
+// qpart[((z nb + volume) nrun_all + run0 + run) JR + j] and k_runs_finish adds
+// them (in a fixed order) into the back projection.
 template <bool ROW, int DM, int JR>
-__global__ void __launch_bounds__(kWeakThreads)
+__global__ void __launch_bounds__(kWeakThreads, 2)
 k_adj_runs(const float* __restrict__ taps, const float* __restrict__ lat, float* __restrict__ bp,
            const WeakRun* __restrict__ runs, int nrun, int N, int Lx, int Ly, int D, int dlo, int lo, int Wp, int Hp,
-           int64_t tbs, int64_t lat_vol, int64_t bp_vol)
+           int64_t tbs, int64_t lat_vol, int64_t bp_vol, int qs, float* __restrict__ qpart, int run0, int nrun_all)
 {
     constexpr int NW = kWeakThreads / 32;
     // blockIdx.y: the volume of a batch (lattice copies and back projections back to back)
-    lat += blockIdx.y * lat_vol;
-    bp += blockIdx.y * bp_vol;
+    const int vol = blockIdx.y;
+    lat += vol * lat_vol;
+    bp += vol * bp_vol;
+    const int qper = (N * N + qs - 1) / qs, qbeg = blockIdx.z * qper, qend = min(N * N, qbeg + qper);
     constexpr int CM = JR + DM - 1;
     __shared__ float part[NW][JR];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -100,26 +108,22 @@ k_adj_runs(const float* __restrict__ taps, const float* __restrict__ lat, float*
 #pragma unroll
         for (int j = 0; j < JR; ++j) acc[j] = 0.f;
         if (c < chi) {
-            for (int q = warp * G + g; q < N * N; q += NW * G) {
+            for (int q = qbeg + warp * G + g; q < qend; q += NW * G) {
                 const int bq = q / N, aq = q - bq * N;
                 const float* kb = taps + (blk0 + bq) * tbs + (int64_t)aq * D * D;
-                // taps along the run axis: K(m1 = c, m2) (column) or K(m1, m2 = c) (row)
-                float k[DM];
-#pragma unroll
-                for (int m = 0; m < DM; ++m)
-                    k[m] = m < D ? __ldg(ROW ? kb + (int64_t)m * D + c : kb + (int64_t)c * D + m) : 0.f;
                 // lattice line along the run axis at cross position fixed + c + dlo
                 const float* line = lat + q * plane + (int64_t)(R.fixed + c + dlo + lo) +
                                     (int64_t)(R.start + dlo + lo) * W;
+                const int nr = R.len + D - 1;
                 float col[CM];
 #pragma unroll
-                for (int r = 0; r < CM; ++r) col[r] = (r < R.len + D - 1) ? __ldg(line + (int64_t)r * W) : 0.f;
+                for (int r = 0; r < CM; ++r) col[r] = r < nr ? __ldg(line + (int64_t)r * W) : 0.f;
+                // taps along the run axis, streamed: K(m1 = c, m2) (column) or K(m1, m2 = c) (row)
 #pragma unroll
                 for (int m = 0; m < DM; ++m) {
-                    if (m < D) {
+                    const float km = m < D ? __ldg(ROW ? kb + (int64_t)m * D + c : kb + (int64_t)c * D + m) : 0.f;
 #pragma unroll
-                        for (int j = 0; j < JR; ++j) acc[j] = fmaf(k[m], col[j + m], acc[j]);
-                    }
+                    for (int j = 0; j < JR; ++j) acc[j] = fmaf(km, col[j + m], acc[j]);
                 }
             }
         }
@@ -135,11 +139,38 @@ k_adj_runs(const float* __restrict__ taps, const float* __restrict__ lat, float*
             float s = 0.f;
 #pragma unroll
             for (int w = 0; w < NW; ++w) s += part[w][threadIdx.x];
-            const int u = ROW ? R.start + (int)threadIdx.x : R.fixed;
-            const int v = ROW ? R.fixed : R.start + (int)threadIdx.x;
-            bp[((int64_t)R.plane * Ly + v) * Lx + u] = s;
+            if (qs > 1) {
+                qpart[(((int64_t)blockIdx.z * gridDim.y + vol) * nrun_all + run0 + rk) * JR + threadIdx.x] = s;
+            } else {
+                const int u = ROW ? R.start + (int)threadIdx.x : R.fixed;
+                const int v = ROW ? R.fixed : R.start + (int)threadIdx.x;
+                bp[((int64_t)R.plane * Ly + v) * Lx + u] = s;
+            }
         }
         __syncthreads();
+    }
+}
+
+// bp[volume][voxel of run, j] = sum over z < qs of the split partial sums (runs
+// [0, ncol) are column runs, the rest row runs)
+template <int JR>
+__global__ void k_runs_finish(const float* __restrict__ qpart, const WeakRun* __restrict__ runs, int nrun_all,
+                              int ncol, int qs, int nb, int Lx, int Ly, float* __restrict__ bp, int64_t bp_vol)
+{
+    const int64_t total = (int64_t)nb * nrun_all * JR;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int j = (int)(i % JR);
+        const int64_t vr = i / JR;
+        const int rk = (int)(vr % nrun_all), vol = (int)(vr / nrun_all);
+        const WeakRun R = runs[rk];
+        if (j >= R.len) continue;
+        float s = 0.f;
+        for (int z = 0; z < qs; ++z) s += qpart[(((int64_t)z * nb + vol) * nrun_all + rk) * JR + j];
+        const bool row = rk >= ncol;
+        const int u = row ? R.start + j : R.fixed;
+        const int v = row ? R.fixed : R.start + j;
+        bp[vol * bp_vol + ((int64_t)R.plane * Ly + v) * Lx + u] = s;
     }
 }
 
@@ -231,6 +262,26 @@ void plane_runs(int plane, const std::vector<std::pair<int, int>>& vu, int Lx, i
         }
 }
 
+// the run kernel for the smallest tap bound DM >= D
+template <bool ROW>
+int launch_runs(int D, dim3 grid, const float* taps, const float* lat, float* bp, const WeakRun* runs, int nrun, int N,
+                int Lx, int Ly, int dlo, int lo, int Wp, int Hp, int64_t tbs, int64_t pv, int64_t nv, float* qpart,
+                int run0, int nrun_all, cudaStream_t st)
+{
+#define SID_RUNS_CASE(DMV)                                                                                         \
+    if (D <= DMV) {                                                                                                \
+        k_adj_runs<ROW, DMV, kRunMax><<<grid, kWeakThreads, 0, st>>>(taps, lat, bp, runs, nrun, N, Lx, Ly, D, dlo, \
+                                                                      lo, Wp, Hp, tbs, pv, nv, (int)grid.z, qpart, \
+                                                                      run0, nrun_all);                             \
+        SID_CHECK_LAUNCH();                                                                                        \
+        return SID_OK;                                                                                             \
+    }
+    SID_RUNS_CASE(16) SID_RUNS_CASE(20) SID_RUNS_CASE(25) SID_RUNS_CASE(28) SID_RUNS_CASE(32)
+#undef SID_RUNS_CASE
+    set_error("spectral plan: tap extent %d above the run kernel's %d", D, kRunDMax);
+    return SID_EINVAL;
+}
+
 }  // namespace
 
 // List the weakly observed voxels: s = A'1 through the plan's most accurate
@@ -298,6 +349,16 @@ int weak_build(sid_plan* p)
     return SID_OK;
 }
 
+// Tap-array split of the run kernel for nb volumes: qs CTAs per run until
+// ~16 CTAs per SM are in the grid (one volume's few hundred runs, each walking
+// all N^2 tap arrays in one CTA, left most SMs idle).
+int weak_qsplit(const sid_plan* p, int64_t nb)
+{
+    const int64_t nall = p->nweak_cols + p->nweak_rows;
+    if (nall == 0) return 1;
+    return (int)std::max<int64_t>(1, std::min<int64_t>(16, cdiv(16 * sm_count(), nall * nb)));
+}
+
 // Overwrite the listed voxels of nb spectral back projections bp[b] = A' ip[b]
 // (polyphase volumes and images back to back) with their exact values.
 int weak_fix_n(sid_plan* p, const float* ip, float* bp, int nb, cudaStream_t st)
@@ -326,25 +387,21 @@ int weak_fix_n(sid_plan* p, const float* ip, float* bp, int nb, cudaStream_t st)
     SID_CHECK_LAUNCH();
     const WeakRun* runs = p->weak.as<WeakRun>();
     const float* taps = p->taps_f.as<float>();
-    const int nc = (int)p->nweak_cols, nr = (int)p->nweak_rows;
-    if (nc) {
-        const dim3 grid((unsigned)nc, (unsigned)nb);
-        if (D <= 16)
-            k_adj_runs<false, 16, kRunMax><<<grid, kWeakThreads, 0, st>>>(taps, pad, bp, runs, nc, N, Lx, Ly, D, dlo,
-                                                                          lo, Wp, Hp, tbs, pv, nv);
-        else
-            k_adj_runs<false, 32, kRunMax><<<grid, kWeakThreads, 0, st>>>(taps, pad, bp, runs, nc, N, Lx, Ly, D, dlo,
-                                                                          lo, Wp, Hp, tbs, pv, nv);
-        SID_CHECK_LAUNCH();
+    const int nc = (int)p->nweak_cols, nr = (int)p->nweak_rows, nall = nc + nr;
+    const int qs = weak_qsplit(p, nb);
+    float* qpart = nullptr;
+    if (qs > 1) {
+        SID_TRY(p->weak_part.alloc((size_t)qs * nb * nall * kRunMax * sizeof(float)));
+        qpart = p->weak_part.as<float>();
     }
-    if (nr) {
-        const dim3 grid((unsigned)nr, (unsigned)nb);
-        if (D <= 16)
-            k_adj_runs<true, 16, kRunMax><<<grid, kWeakThreads, 0, st>>>(taps, padT, bp, runs + nc, nr, N, Lx, Ly, D,
-                                                                         dlo, lo, Wp, Hp, tbs, pv, nv);
-        else
-            k_adj_runs<true, 32, kRunMax><<<grid, kWeakThreads, 0, st>>>(taps, padT, bp, runs + nc, nr, N, Lx, Ly, D,
-                                                                         dlo, lo, Wp, Hp, tbs, pv, nv);
+    if (nc) SID_TRY(launch_runs<false>(D, dim3((unsigned)nc, (unsigned)nb, (unsigned)qs), taps, pad, bp, runs, nc, N, Lx,
+                                      Ly, dlo, lo, Wp, Hp, tbs, pv, nv, qpart, 0, nall, st));
+    if (nr) SID_TRY(launch_runs<true>(D, dim3((unsigned)nr, (unsigned)nb, (unsigned)qs), taps, padT, bp, runs + nc, nr, N,
+                                     Lx, Ly, dlo, lo, Wp, Hp, tbs, pv, nv, qpart, nc, nall, st));
+    if (qs > 1) {
+        const int64_t tot = (int64_t)nb * nall * kRunMax;
+        k_runs_finish<kRunMax><<<(unsigned)std::min<int64_t>(cdiv(tot, 256), 4096), 256, 0, st>>>(
+            qpart, runs, nall, nc, qs, nb, Lx, Ly, bp, nv);
         SID_CHECK_LAUNCH();
     }
     return SID_OK;
