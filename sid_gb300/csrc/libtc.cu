@@ -21,7 +21,7 @@
 //   3. k_lib_synth: per neuron and output phase, the inverse real DFT of the
 //      window spectrum straight from the contraction's output, written into
 //      the library row (pixels outside the frame dropped; the rest of each row
-//      is zero).
+//      is zero), on a second stream beside the next pass's pack.
 // Precision: 24-bit window spectra, box spectra split into two BF16 parts
 // (16-17 bits), three MMA passes with FP32 accumulation -- about 1e-5 relative
 // per row, against FP32 rounding for the tap kernels of library.cu.
@@ -44,7 +44,10 @@ struct LibWin {
     DBuf tw;             // L float2: exp(2 pi i k / L)
     DBuf kh, kl;         // window tap spectra, 24-bit planes [f][b'a'][abc]
     DBuf bpl;            // B operand planes of one pass
-    DBuf tco, cols;      // contraction output [f][neuron][b'a'], neurons in pass order
+    DBuf tco, cols;      // contraction outputs [2][f][neuron][b'a'] (alternate passes), neurons in pass order
+    // the synthesis of pass k runs on `side` beside the pack of pass k + 1
+    cudaStream_t side = nullptr;
+    cudaEvent_t tc_done[2] = {nullptr, nullptr}, syn_done[2] = {nullptr, nullptr};
 };
 
 namespace {
@@ -265,6 +268,11 @@ void libwin_free(sid_plan* p)
     w->kh.release();
     w->kl.release();
     w->tw.release();
+    if (w->side) cudaStreamDestroy(w->side);
+    for (int b = 0; b < 2; ++b) {
+        if (w->tc_done[b]) cudaEventDestroy(w->tc_done[b]);
+        if (w->syn_done[b]) cudaEventDestroy(w->syn_done[b]);
+    }
     delete w;
     p->libwin = nullptr;
 }
@@ -296,6 +304,11 @@ static int libwin_ensure(sid_plan* p, int64_t Wo)
     const size_t nent = (size_t)(w->nf * n_out * n_in_pad);
     SID_TRY(w->kh.alloc(nent * sizeof(ushort2)));
     SID_TRY(w->kl.alloc(nent * sizeof(uchar2)));
+    SID_CUDA_TRY(cudaStreamCreateWithFlags(&w->side, cudaStreamNonBlocking));
+    for (int b = 0; b < 2; ++b) {
+        SID_CUDA_TRY(cudaEventCreateWithFlags(&w->tc_done[b], cudaEventDisableTiming));
+        SID_CUDA_TRY(cudaEventCreateWithFlags(&w->syn_done[b], cudaEventDisableTiming));
+    }
     return build_khat_f24(p, L, w->tw.as<float2>(), w->kh.as<ushort2>(), w->kl.as<uchar2>());
 }
 
@@ -366,7 +379,8 @@ extern "C" int sid_library_spectral(sid_plan* p, const float* const* recon, int6
     const int64_t bn_max = n_neur > 32 ? 128 : 64;
     SID_TRY(w->bpl.alloc((size_t)(kLibBPlanes * nf * bn_max * max_kpb) * sizeof(uint16_t)));
     const int gmax = (int)std::min<int64_t>(n_neur, G);
-    SID_TRY(w->tco.alloc((size_t)(nf * gmax * n_out) * sizeof(float2)));
+    const size_t tco_elems = (size_t)(nf * gmax * n_out);
+    SID_TRY(w->tco.alloc(2 * tco_elems * sizeof(float2)));
     SID_TRY(w->cols.alloc((size_t)n_neur * sizeof(int)));
     SID_CUDA_TRY(cudaMemcpyAsync(w->cols.p, order.data(), order.size() * sizeof(int), cudaMemcpyHostToDevice, st));
     const int64_t P = p->X * p->Y;
@@ -377,8 +391,11 @@ extern "C" int sid_library_spectral(sid_plan* p, const float* const* recon, int6
     const int64_t H1 = L / 2 + 1;
     const size_t synth_smem = (size_t)(L + kLibSynthWarps * (H1 * L + H1 * Wo)) * sizeof(float2);
     SID_CUDA_TRY(cudaFuncSetAttribute(k_lib_synth, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)synth_smem));
-    for (const Pass& ps : passes) {
+    for (size_t k = 0; k < passes.size(); ++k) {
+        const Pass& ps = passes[k];
         const int bn = ps.nb <= 32 ? 64 : 128;
+        const int buf = (int)(k & 1);
+        float2* tco = w->tco.as<float2>() + buf * tco_elems;
         const int64_t kpb = 64 * (int64_t)ps.nkb, nchb = kpb / 2;
         const size_t plane = (size_t)(nf * bn * kpb);
         uint16_t* bh = w->bpl.as<uint16_t>();
@@ -394,14 +411,20 @@ extern "C" int sid_library_spectral(sid_plan* p, const float* const* recon, int6
         else
             SID_TRY(launch_pack<6>(grid, dpack, dbox, cols, ps.nb, cbase, (int)nchb, (int)n_in, (int)N, (int)p->g.dlo,
                                    (int)L, bn, w->tw.as<float2>(), h32, m32, l32, st));
+        // the contraction output buffer is free once the synthesis two passes back has read it
+        if (k >= 2) SID_CUDA_TRY(cudaStreamWaitEvent(st, w->syn_done[buf], 0));
         SID_TRY(spec_tc_forward_raw(w->kh.p, w->kl.p, n_out, 2 * n_in_pad, ps.akb0, bh, kLibBPlanes, kpb, nf, ps.nb,
-                                    w->tco.as<float2>(), p->errflag.as<int>(), st));
+                                    tco, p->errflag.as<int>(), st));
+        SID_CUDA_TRY(cudaEventRecord(w->tc_done[buf], st));
+        SID_CUDA_TRY(cudaStreamWaitEvent(w->side, w->tc_done[buf], 0));
         k_lib_synth<<<dim3((unsigned)cdiv(n_out, kLibSynthWarps), (unsigned)ps.nb), kLibSynthWarps * 32, synth_smem,
-                      st>>>(w->tco.as<float2>(), dbox, cols, ps.nb, (int)n_out, (int)N, (int)L, (int)Wo, (int)p->g.dlo,
-                            p->X, p->Y, w->tw.as<float2>(), out, ldn, ldp);
+                      w->side>>>(tco, dbox, cols, ps.nb, (int)n_out, (int)N, (int)L, (int)Wo, (int)p->g.dlo, p->X, p->Y,
+                                 w->tw.as<float2>(), out, ldn, ldp);
         SID_CHECK_LAUNCH();
+        SID_CUDA_TRY(cudaEventRecord(w->syn_done[buf], w->side));
     }
-    // the staging buffers are read by the kernels above: wait before the host
-    // vectors go out of scope and before the workspaces can be reused
+    // join the synthesis stream (in order: its last event covers every pass), then
+    // wait: the staging buffers are read by the kernels above until they finish
+    SID_CUDA_TRY(cudaStreamWaitEvent(st, w->syn_done[(passes.size() - 1) & 1], 0));
     return plan_sync(p, st);
 }
