@@ -228,8 +228,30 @@ int sid_library(sid_plan* plan, const float* const* recon, int64_t n_comp, const
 int sid_library_spectral(sid_plan* plan, const float* const* recon, int64_t n_comp, const double* centers,
                          const uint8_t* neur_id, int64_t n_neur, int64_t neur_rad, double axial, float* out,
                          int out_layout, void* stream);
-/* The crop boxes the call above uses (host only): boxes[6n..6n+5] = 0-based
- * half-open x0 x1 y0 y1 z0 z1 of neuron n (generate_LFM_library_GPU.m:68-88). */
+/* forward_model = generate_LFM_library_CPU(centers, psf_ballistic, r, dim, m, kernel)
+ *                                              generate_LFM_library_CPU.m:1
+ * Each neuron is the kernel W (kernel: kx x ky x kz single, HOST, MATLAB
+ * order; or, when kernel is NULL, the ball x^2 + y^2 + (z r/rr)^2 <= r^2 over
+ * meshgrid(-r:r, -r:r, -rr:rr) with rr = r / dim_z) painted at round(W index -
+ * [r+1, r+1, rr+1] + centre) (voxels outside the volume dropped),
+ * forward-projected (project_forward_patched.m: for odd Nnum its centred patch
+ * projection is the frame's conv2 'same' projection) and divided by its L2
+ * norm.  method SID_METHOD_DIRECT (FP32 lenslet taps) or
+ * SID_METHOD_SPECTRAL_MIXED (tensor-core windows).  centers: HOST n_neur x 3
+ * double, 1-based; out (device) as sid_library: dense rows, the reference's
+ * sparse matrix holds their nonzeros.  Synchronises the stream. */
+int sid_library_kernel(sid_plan* plan, int method, const double* centers, int64_t n_neur, double r, double dim_z,
+                       const float* kernel, int64_t kx, int64_t ky, int64_t kz, float* out, int out_layout,
+                       void* stream);
+/* The voxels the call above paints (host only): counts[n] per neuron; when xyz
+ * is not NULL, 0-based (x, y, z) triples (and the kernel values) of all neurons
+ * back to back, at most cap of them. */
+int sid_library_kernel_voxels(const double* centers, int64_t n_neur, double r, double dim_z, const float* kernel,
+                              int64_t kx, int64_t ky, int64_t kz, int64_t X, int64_t Y, int64_t Z, int64_t* counts,
+                              int32_t* xyz, float* values, int64_t cap);
+/* The crop boxes sid_library and sid_library_spectral use (host only):
+ * boxes[6n..6n+5] = 0-based half-open x0 x1 y0 y1 z0 z1 of neuron n
+ * (generate_LFM_library_GPU.m:68-88). */
 int sid_library_boxes(const double* centers, int64_t n_neur, int64_t neur_rad, double axial, int64_t X,
                       int64_t Y, int64_t Z, int32_t* boxes);
 

@@ -368,6 +368,96 @@ def generate_library(recon, centers, neur_id, H, neur_rad, axial, image_size=Non
     return out
 
 
+def library_kernel_shape(r, dim, kernel=None):
+    """(W, r, rr) of generate_LFM_library_CPU.m:18,27-36: the given kernel with
+    r = (size(W,1)-1)/2, rr = (size(W,3)-1)/2, or the ball
+    X.^2 + Y.^2 + (Z*r/rr).^2 <= r^2 over meshgrid(-r:r, -r:r, -rr:rr),
+    rr = r/dim(3)."""
+    if kernel is not None:
+        W = np.asarray(kernel, dtype=np.float32)
+        if W.ndim == 2:
+            W = W[:, :, None]
+        return np.asfortranarray(W), (W.shape[0] - 1) / 2.0, (W.shape[2] - 1) / 2.0
+    r = float(r)
+    rr = r / float(dim[2])
+    xs = np.arange(-r, r + 0.5, 1.0)
+    zs = -rr + np.arange(int(np.floor(2 * rr + 1e-10)) + 1, dtype=np.float64)
+    X, Y, Z = np.meshgrid(xs, xs, zs)  # MATLAB meshgrid: X along columns, Y along rows
+    W = (X ** 2 + Y ** 2 + (Z * r / rr) ** 2 <= r ** 2).astype(np.float32)
+    return np.asfortranarray(W), r, rr
+
+
+def library_kernel_voxels(centers, r, dim, m, Z, kernel=None):
+    """Per neuron the 0-based voxels and kernel values generate_LFM_library_CPU.m
+    :39-49 paints: bbb = round(BWW - [r+1, r+1, rr+1] + centre) for the nonzero
+    kernel entries BWW in find() order, kept inside [1, m(1)] x [1, m(2)] x [1, Z]."""
+    W, rk, rr = library_kernel_shape(r, dim, kernel)
+    flat = W.ravel(order="F")
+    idx = np.flatnonzero(flat != 0)
+    i, j, k = np.unravel_index(idx, W.shape, order="F")
+    BWW = np.stack([i + 1, j + 1, k + 1], 1).astype(np.float64)
+    out = []
+    for c in np.asarray(centers, dtype=np.float64).reshape(-1, 3):
+        bbb = _mround((BWW - np.array([rk + 1, rk + 1, rr + 1])) + c)
+        keep = ((bbb[:, 0] <= m[0]) & (bbb[:, 0] > 0) & (bbb[:, 1] <= m[1]) & (bbb[:, 1] > 0)
+                & (bbb[:, 2] <= Z) & (bbb[:, 2] > 0))
+        out.append((bbb[keep].astype(np.int64) - 1, flat[idx][keep]))
+    return out
+
+
+def project_forward_patched(pixels, values, dims, Nnum, H):
+    """project_forward_patched.m:8-73 in FP64: paint the 1-based voxels into a
+    patch of an odd number of lenslets, conv2 'full' every (phase, depth) slice
+    with its PSF, paste the result centred on the patch, clipped to the sensor."""
+    from scipy.signal import convolve2d
+    pixels = np.asarray(pixels, dtype=np.int64)
+    N = int(Nnum)
+    px_min, px_max = pixels.min(0), pixels.max(0)
+    off_ml = (px_min[:2] - 1) // N
+    off_px = off_ml * N
+    n_ml = -(-px_max[:2] // N) - off_ml
+    n_ml = n_ml + (n_ml % 2 == 0)
+    off_z = px_min[2] - 1
+    n_z = px_max[2] - off_z
+    vol = np.zeros((n_ml[0] * N, n_ml[1] * N, n_z))
+    for (x, y, z), v in zip(pixels, values):
+        vol[x - off_px[0] - 1, y - off_px[1] - 1, z - off_z - 1] = v
+    total = None
+    for i in range(N):
+        for j in range(N):
+            for k in range(n_z):
+                t = np.zeros(vol.shape[:2])
+                t[i::N, j::N] = vol[i::N, j::N, k]
+                if not t.any():
+                    continue
+                c = convolve2d(t, np.asarray(H[:, :, i, j, off_z + k], dtype=np.float64), mode="full")
+                total = c if total is None else total + c
+    img = np.zeros((int(dims[0]), int(dims[1])))
+    if total is None:
+        return img
+    pj = total.shape
+    center = off_px + np.ceil((n_ml / 2.0) * N).astype(np.int64)
+    x0, x1 = max(1, center[0] - pj[0] // 2), min(int(dims[0]), center[0] + pj[0] // 2)
+    y0, y1 = max(1, center[1] - pj[1] // 2), min(int(dims[1]), center[1] + pj[1] // 2)
+    p0, p1 = x0 - (center[0] - pj[0] // 2 - 1), x1 - (center[0] - pj[0] // 2 - 1)
+    q0, q1 = y0 - (center[1] - pj[1] // 2 - 1), y1 - (center[1] - pj[1] // 2 - 1)
+    img[x0 - 1:x1, y0 - 1:y1] = total[p0 - 1:p1, q0 - 1:q1]
+    return img
+
+
+def generate_library_cpu(centers, H, r, dim, m, kernel=None):
+    """forward_model rows of generate_LFM_library_CPU.m:37-54 (dense, FP64):
+    each neuron's painted kernel through project_forward_patched, divided by
+    its L2 norm."""
+    H = _psf(H)
+    Z, N = H.shape[4], H.shape[2]
+    rows = []
+    for vox, vals in library_kernel_voxels(centers, r, dim, m, Z, kernel):
+        Q = project_forward_patched(vox + 1, vals.astype(np.float64), m[:2], N, H).ravel(order="F")
+        rows.append(Q / np.linalg.norm(Q))
+    return np.asarray(rows)
+
+
 # ----------------------------------------------------------------------------
 # NNLS: LS_nnls.m:59-172 and fast_nnls.m:21-199
 # ----------------------------------------------------------------------------

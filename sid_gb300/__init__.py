@@ -21,8 +21,10 @@ from .lfm import (  # noqa: F401
     forwardProjectACC,
     forwardProjectGPU,
     generate_kernel,
+    generate_LFM_library_CPU,
     generate_LFM_library_GPU,
     library_boxes,
+    library_kernel_voxels,
     reconstruct_S,
     set_default_method,
     to_device,

@@ -272,7 +272,7 @@ k_lib_tile(const float* __restrict__ taps, const float* __restrict__ packed, con
             asm volatile("cp.async.wait_group 0;" ::: "memory");
         }
         __syncthreads();
-        const int c = z0 + st / N, bb = st - (st / N) * N;
+        const int bb = st - (st / N) * N;  // input row phase of this stage (depth z0 + st / N)
         const float* tb0 = sm + (st & 1) * N * tsz;
         if (ds < a.W) {
 #pragma unroll
@@ -384,11 +384,22 @@ static void neuron_box(const double* centers, int64_t n_neur, int64_t n, int64_t
     box6[5] = (int)std::min<int64_t>(z + zr, Z);
 }
 
+void lib_box_window(const sid_plan* p, LibBox& b)
+{
+    // output lenslets reached from the box: s = u + m + dlo
+    const int N = (int)p->N;
+    const int umin = b.x0 / N, umax = (b.x1 - 1) / N;
+    const int vmin = b.y0 / N, vmax = (b.y1 - 1) / N;
+    b.s0 = (int)std::max<int64_t>(0, umin + p->g.dlo);
+    b.s1 = (int)std::min<int64_t>(p->Lx, umax + p->g.dhi + 1);
+    b.t0 = (int)std::max<int64_t>(0, vmin + p->g.dlo);
+    b.t1 = (int)std::min<int64_t>(p->Ly, vmax + p->g.dhi + 1);
+}
+
 int lib_stage(sid_plan* p, const char* who, const float* const* recon, int64_t n_comp, const double* centers,
               const uint8_t* neur_id, int64_t n_neur, int64_t neur_rad, double axial, std::vector<LibBox>& boxes,
               cudaStream_t st)
 {
-    const int64_t N = p->N;
     boxes.resize((size_t)n_neur);
     int64_t off = 0;
     for (int64_t n = 0; n < n_neur; ++n) {
@@ -404,13 +415,7 @@ int lib_stage(sid_plan* p, const char* who, const float* const* recon, int64_t n
         b.ncomp = nc;
         b.off = (int)off;
         off += (int64_t)(b.x1 - b.x0) * (b.y1 - b.y0) * (b.z1 - b.z0);
-        // output lenslets reached from the box: s = u + m + dlo
-        const int umin = b.x0 / (int)N, umax = (b.x1 - 1) / (int)N;
-        const int vmin = b.y0 / (int)N, vmax = (b.y1 - 1) / (int)N;
-        b.s0 = (int)std::max<int64_t>(0, umin + p->g.dlo);
-        b.s1 = (int)std::min<int64_t>(p->Lx, umax + p->g.dhi + 1);
-        b.t0 = (int)std::max<int64_t>(0, vmin + p->g.dlo);
-        b.t1 = (int)std::min<int64_t>(p->Ly, vmax + p->g.dhi + 1);
+        lib_box_window(p, b);
         boxes[(size_t)n] = b;
         SID_REQUIRE(off < INT32_MAX, "%s: boxes too large", who);
     }
@@ -442,19 +447,17 @@ extern "C" int sid_library_boxes(const double* centers, int64_t n_neur, int64_t 
     return SID_OK;
 }
 
-extern "C" int sid_library(sid_plan* p, const float* const* recon, int64_t n_comp, const double* centers,
-                           const uint8_t* neur_id, int64_t n_neur, int64_t neur_rad, double axial, float* out,
-                           int out_layout, void* stream)
+namespace sid {
+
+// Forward projections of the staged boxes (lib_stage) into the library rows
+// through the FP32 lenslet taps; leaves `st` to be synchronised by the caller
+// (the host tables are uploaded by pageable copies, so they may go out of scope).
+int lib_run_direct(sid_plan* p, const char* who, const std::vector<LibBox>& boxes, float* out, int out_layout,
+                   cudaStream_t st)
 {
-    SID_REQUIRE(p && recon && centers && neur_id && out, "sid_library: NULL argument");
-    SID_REQUIRE(n_comp >= 1 && n_neur >= 1 && neur_rad >= 0 && axial > 0,
-                "sid_library: need n_comp >= 1, n_neur >= 1, neur_rad >= 0, axial > 0");
-    SID_REQUIRE(out_layout == 0 || out_layout == 1, "sid_library: out_layout must be 0 (n x P) or 1 (P x n)");
-    SID_REQUIRE(p->taps_f.p, "sid_library: the plan needs SID_PLAN_DIRECT (lenslet taps)");
-    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    SID_REQUIRE(p->taps_f.p, "%s: the plan has no lenslet taps", who);
+    const int64_t n_neur = (int64_t)boxes.size();
     const int64_t N = p->N, D = p->g.D;
-    std::vector<LibBox> boxes;
-    SID_TRY(lib_stage(p, "sid_library", recon, n_comp, centers, neur_id, n_neur, neur_rad, axial, boxes, st));
     int max_ns = 0, ntgM = 0, span = 0, nrv = 0, bwm = 0;
     for (const LibBox& b : boxes) {
         const int umin = b.x0 / (int)N, umax = (b.x1 - 1) / (int)N;
@@ -483,8 +486,8 @@ extern "C" int sid_library(sid_plan* p, const float* const* recon, int64_t n_com
     const size_t tile_bytes =
         (size_t)N * Dp * (Dp + kLibT) * sizeof(float) + (size_t)(D * D + 4 * N * kLibG) * sizeof(int);
     if (!tiled) {
-        SID_REQUIRE(tile_bytes <= 200 * 1024, "sid_library: tap tiles (%zu bytes) exceed shared memory", tile_bytes);
-        SID_REQUIRE(max_ns * ntgM <= 256, "sid_library: neuron radius too large for one CTA (%d output groups)",
+        SID_REQUIRE(tile_bytes <= 200 * 1024, "%s: tap tiles (%zu bytes) exceed shared memory", who, tile_bytes);
+        SID_REQUIRE(max_ns * ntgM <= 256, "%s: neuron radius too large for one CTA (%d output groups)", who,
                     max_ns * ntgM);
     }
     // groups of up to kLibG neurons with the same depth window, in window order
@@ -527,8 +530,236 @@ extern "C" int sid_library(sid_plan* p, const float* const* recon, int64_t n_com
                                                             p->X, p->Y, out, ldn, ldp);
         SID_CHECK_LAUNCH();
     }
-    // the staging buffers are read by the kernels above: wait before the host
-    // vectors go out of scope and before the workspaces can be reused
+    return SID_OK;
+}
+
+// ---------------------------------------------------------------------------
+// generate_LFM_library_CPU.m:18-70 with project_forward_patched.m:8-73: every
+// neuron is a kernel W (given, or the ball x^2 + y^2 + (z r/rr)^2 <= r^2 over
+// meshgrid(-r:r, -r:r, -rr:rr), rr = r / dim(3)) painted at its centre,
+// forward-projected, and L2-normalised.  The patch projection of
+// project_forward_patched.m (an odd number of lenslets, conv2 'full', pasted
+// centred and clipped to the sensor) equals the frame's conv2 'same'
+// projection of the painted volume for odd Nnum, so the rows come from the
+// library kernels above.
+
+// Voxel (0-based) and value of the kernel entries neuron n keeps:
+// bbb = round(BWW - [r+1, r+1, rr+1] + centre) inside [1, X] x [1, Y] x [1, Z]
+// for every nonzero W(BWW) in find(W) order (generate_LFM_library_CPU.m:39-49).
+struct KernVox {
+    int x, y, z;
+    float v;
+};
+
+static double mround_d(double v) { return v < 0 ? -std::floor(-v + 0.5) : std::floor(v + 0.5); }
+
+// W in MATLAB order (wx x wy x wz) with its r, rr; or the ball when W is null
+struct KernelShape {
+    std::vector<float> w;
+    int64_t wx = 0, wy = 0, wz = 0;
+    double r = 0, rr = 0;
+};
+
+static int kernel_shape(const char* who, double r, double dim_z, const float* W, int64_t wx, int64_t wy, int64_t wz,
+                        KernelShape& ks)
+{
+    if (W) {
+        SID_REQUIRE(wx >= 1 && wy >= 1 && wz >= 1, "%s: kernel dimensions must be positive", who);
+        ks.wx = wx; ks.wy = wy; ks.wz = wz;
+        ks.w.assign(W, W + wx * wy * wz);
+        ks.r = (double)(wx - 1) / 2.0;   // generate_LFM_library_CPU.m:31-32
+        ks.rr = (double)(wz - 1) / 2.0;
+        return SID_OK;
+    }
+    SID_REQUIRE(r >= 0 && r == std::floor(r) && r <= 1024, "%s: the ball radius must be a whole number in [0, 1024]",
+                who);
+    SID_REQUIRE(dim_z > 0, "%s: dim(3) must be positive", who);
+    ks.r = r;
+    ks.rr = r / dim_z;  // generate_LFM_library_CPU.m:18
+    // meshgrid(-r:r, -r:r, -rr:rr): X along columns, Y along rows, Z along pages;
+    // -rr:rr holds floor(2 rr) + 1 values -rr + k
+    const int64_t n = 2 * (int64_t)r + 1, nz = (int64_t)std::floor(2.0 * ks.rr + 1e-10) + 1;
+    SID_REQUIRE(nz >= 1 && nz <= 4096, "%s: axial extent %lld outside [1, 4096]", who, (long long)nz);
+    ks.wx = n; ks.wy = n; ks.wz = nz;
+    ks.w.assign((size_t)(n * n * nz), 0.f);
+    for (int64_t k = 0; k < nz; ++k)
+        for (int64_t j = 0; j < n; ++j)
+            for (int64_t i = 0; i < n; ++i) {
+                const double xv = -r + (double)j, yv = -r + (double)i, zv = -ks.rr + (double)k;
+                const double t = zv * r / ks.rr;
+                const bool in = ks.rr > 0 ? (xv * xv + yv * yv + t * t <= r * r) : (xv * xv + yv * yv <= r * r);
+                ks.w[(size_t)(i + n * (j + n * k))] = in ? 1.f : 0.f;
+            }
+    return SID_OK;
+}
+
+static void kernel_voxels(const KernelShape& ks, const double* centers, int64_t n_neur, int64_t n, int64_t X,
+                          int64_t Y, int64_t Z, std::vector<KernVox>& out)
+{
+    out.clear();
+    const double cx = centers[n], cy = centers[n + n_neur], cz = centers[n + 2 * n_neur];
+    for (int64_t k = 0; k < ks.wz; ++k)
+        for (int64_t j = 0; j < ks.wy; ++j)
+            for (int64_t i = 0; i < ks.wx; ++i) {
+                const float v = ks.w[(size_t)(i + ks.wx * (j + ks.wy * k))];
+                if (v == 0.f) continue;  // find(W): nonzero entries (NaN included)
+                const double bx = mround_d(((double)(i + 1) - (ks.r + 1)) + cx);
+                const double by = mround_d(((double)(j + 1) - (ks.r + 1)) + cy);
+                const double bz = mround_d(((double)(k + 1) - (ks.rr + 1)) + cz);
+                if (bx <= (double)X && bx > 0 && by <= (double)Y && by > 0 && bz <= (double)Z && bz > 0)
+                    out.push_back({(int)bx - 1, (int)by - 1, (int)bz - 1, v});
+            }
+}
+
+// Boxes around each neuron's painted voxels, their values packed into p->ws[2].
+static int lib_stage_kernel(sid_plan* p, const char* who, const KernelShape& ks, const double* centers,
+                            int64_t n_neur, std::vector<LibBox>& boxes, cudaStream_t st)
+{
+    boxes.resize((size_t)n_neur);
+    std::vector<float> packed;
+    std::vector<KernVox> vox;
+    for (int64_t n = 0; n < n_neur; ++n) {
+        kernel_voxels(ks, centers, n_neur, n, p->X, p->Y, p->Z, vox);
+        SID_REQUIRE(!vox.empty(), "%s: neuron %lld has no kernel voxel inside the volume", who, (long long)(n + 1));
+        LibBox b;
+        b.x0 = b.y0 = b.z0 = INT32_MAX;
+        b.x1 = b.y1 = b.z1 = 0;
+        for (const KernVox& q : vox) {
+            b.x0 = std::min(b.x0, q.x); b.x1 = std::max(b.x1, q.x + 1);
+            b.y0 = std::min(b.y0, q.y); b.y1 = std::max(b.y1, q.y + 1);
+            b.z0 = std::min(b.z0, q.z); b.z1 = std::max(b.z1, q.z + 1);
+        }
+        b.ncomp = 1;
+        b.off = (int)packed.size();
+        const int bw = b.x1 - b.x0, bh = b.y1 - b.y0;
+        packed.resize(packed.size() + (size_t)bw * bh * (b.z1 - b.z0), 0.f);
+        for (const KernVox& q : vox)
+            packed[(size_t)b.off + (size_t)((q.x - b.x0) + bw * ((q.y - b.y0) + (int64_t)bh * (q.z - b.z0)))] = q.v;
+        SID_REQUIRE(packed.size() < (size_t)INT32_MAX, "%s: kernels too large", who);
+        lib_box_window(p, b);
+        boxes[(size_t)n] = b;
+    }
+    SID_TRY(p->ws[3].alloc(boxes.size() * sizeof(LibBox)));
+    SID_TRY(p->ws[2].alloc(packed.size() * sizeof(float)));
+    SID_CUDA_TRY(cudaMemcpyAsync(p->ws[3].p, boxes.data(), boxes.size() * sizeof(LibBox), cudaMemcpyHostToDevice, st));
+    SID_CUDA_TRY(cudaMemcpyAsync(p->ws[2].p, packed.data(), packed.size() * sizeof(float), cudaMemcpyHostToDevice, st));
+    // the host tables must outlive the copies
     SID_CUDA_TRY(cudaStreamSynchronize(st));
+    return SID_OK;
+}
+
+constexpr int kNormChunks = 256;
+
+// part[c][n] = sum of squares of row n over pixel chunk c (FP64 sums)
+__global__ void k_row_sumsq(const float* __restrict__ out, int64_t n_neur, int64_t P, int64_t ldn, int64_t ldp,
+                            double* __restrict__ part)
+{
+    const int64_t chunk = (P + kNormChunks - 1) / kNormChunks;
+    const int c = blockIdx.x;
+    const int64_t p0 = c * chunk, p1 = min(P, p0 + chunk);
+    for (int64_t n = blockIdx.y * (int64_t)blockDim.x + threadIdx.x; n < n_neur; n += (int64_t)gridDim.y * blockDim.x) {
+        double s = 0.0;
+        for (int64_t q = p0; q < p1; ++q) {
+            const double v = out[n * ldn + q * ldp];
+            s += v * v;
+        }
+        part[c * n_neur + n] = s;
+    }
+}
+
+// row n /= sqrt(sum over chunks of part[c][n]) (generate_LFM_library_CPU.m:52: Q = Q / norm(Q))
+__global__ void k_row_scale(float* __restrict__ out, int64_t n_neur, int64_t P, int64_t ldn, int64_t ldp,
+                            const double* __restrict__ part)
+{
+    const int64_t n = blockIdx.y;
+    __shared__ double inv;
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int c = 0; c < kNormChunks; ++c) s += part[c * n_neur + n];
+        inv = 1.0 / sqrt(s);
+    }
+    __syncthreads();
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < P; q += (int64_t)gridDim.x * blockDim.x) {
+        float* o = out + n * ldn + q * ldp;
+        *o = (float)((double)*o * inv);
+    }
+}
+
+}  // namespace sid
+
+using namespace sid;
+
+extern "C" int sid_library(sid_plan* p, const float* const* recon, int64_t n_comp, const double* centers,
+                           const uint8_t* neur_id, int64_t n_neur, int64_t neur_rad, double axial, float* out,
+                           int out_layout, void* stream)
+{
+    SID_REQUIRE(p && recon && centers && neur_id && out, "sid_library: NULL argument");
+    SID_REQUIRE(n_comp >= 1 && n_neur >= 1 && neur_rad >= 0 && axial > 0,
+                "sid_library: need n_comp >= 1, n_neur >= 1, neur_rad >= 0, axial > 0");
+    SID_REQUIRE(out_layout == 0 || out_layout == 1, "sid_library: out_layout must be 0 (n x P) or 1 (P x n)");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    std::vector<LibBox> boxes;
+    SID_TRY(lib_stage(p, "sid_library", recon, n_comp, centers, neur_id, n_neur, neur_rad, axial, boxes, st));
+    SID_TRY(lib_run_direct(p, "sid_library", boxes, out, out_layout, st));
+    // the staging buffers are read by the kernels above: wait before the
+    // workspaces can be reused
+    SID_CUDA_TRY(cudaStreamSynchronize(st));
+    return SID_OK;
+}
+
+extern "C" int sid_library_kernel(sid_plan* p, int method, const double* centers, int64_t n_neur, double r,
+                                  double dim_z, const float* kernel, int64_t kx, int64_t ky, int64_t kz, float* out,
+                                  int out_layout, void* stream)
+{
+    const char* who = "sid_library_kernel";
+    SID_REQUIRE(p && centers && out, "%s: NULL argument", who);
+    SID_REQUIRE(n_neur >= 1, "%s: need n_neur >= 1", who);
+    SID_REQUIRE(out_layout == 0 || out_layout == 1, "%s: out_layout must be 0 (n x P) or 1 (P x n)", who);
+    SID_REQUIRE(method == SID_METHOD_DIRECT || method == SID_METHOD_SPECTRAL_MIXED,
+                "%s: method must be SID_METHOD_DIRECT or SID_METHOD_SPECTRAL_MIXED", who);
+    // the centred paste of project_forward_patched.m:63-72 matches the frame's 'same' projection for odd Nnum
+    SID_REQUIRE(p->N % 2 == 1, "%s: the patch projection's centring needs an odd Nnum", who);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    KernelShape ks;
+    SID_TRY(kernel_shape(who, r, dim_z, kernel, kx, ky, kz, ks));
+    std::vector<LibBox> boxes;
+    SID_TRY(lib_stage_kernel(p, who, ks, centers, n_neur, boxes, st));
+    SID_TRY(method == SID_METHOD_DIRECT ? lib_run_direct(p, who, boxes, out, out_layout, st)
+                                        : lib_run_spectral(p, who, boxes, out, out_layout, st));
+    const int64_t P = p->X * p->Y;
+    const int64_t ldn = out_layout == 0 ? 1 : P, ldp = out_layout == 0 ? n_neur : 1;
+    SID_TRY(p->red.alloc((size_t)(kNormChunks * n_neur) * sizeof(double)));
+    k_row_sumsq<<<dim3(kNormChunks, (unsigned)std::min<int64_t>(cdiv(n_neur, 128), 64)), 128, 0, st>>>(
+        out, n_neur, P, ldn, ldp, p->red.as<double>());
+    SID_CHECK_LAUNCH();
+    k_row_scale<<<dim3(64, (unsigned)n_neur), 256, 0, st>>>(out, n_neur, P, ldn, ldp, p->red.as<double>());
+    SID_CHECK_LAUNCH();
+    return plan_sync(p, st);
+}
+
+extern "C" int sid_library_kernel_voxels(const double* centers, int64_t n_neur, double r, double dim_z,
+                                         const float* kernel, int64_t kx, int64_t ky, int64_t kz, int64_t X, int64_t Y,
+                                         int64_t Z, int64_t* counts, int32_t* xyz, float* values, int64_t cap)
+{
+    const char* who = "sid_library_kernel_voxels";
+    SID_REQUIRE(centers && counts && n_neur >= 0, "%s: bad argument", who);
+    KernelShape ks;
+    SID_TRY(kernel_shape(who, r, dim_z, kernel, kx, ky, kz, ks));
+    std::vector<KernVox> vox;
+    int64_t at = 0;
+    for (int64_t n = 0; n < n_neur; ++n) {
+        kernel_voxels(ks, centers, n_neur, n, X, Y, Z, vox);
+        counts[n] = (int64_t)vox.size();
+        for (const KernVox& q : vox) {
+            if (xyz && at < cap) {
+                xyz[3 * at] = q.x;
+                xyz[3 * at + 1] = q.y;
+                xyz[3 * at + 2] = q.z;
+                if (values) values[at] = q.v;
+            }
+            ++at;
+        }
+    }
+    SID_REQUIRE(!xyz || at <= cap, "%s: %lld voxels exceed the capacity %lld", who, (long long)at, (long long)cap);
     return SID_OK;
 }

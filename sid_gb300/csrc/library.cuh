@@ -24,4 +24,15 @@ int lib_stage(sid_plan* p, const char* who, const float* const* recon, int64_t n
               const uint8_t* neur_id, int64_t n_neur, int64_t neur_rad, double axial, std::vector<LibBox>& boxes,
               cudaStream_t st);
 
+// Forward projections of the staged boxes into the library rows: FP32
+// lenslet taps (library.cu) or the tensor-core windows (libtc.cu).  Both
+// leave `st` unsynchronised.
+int lib_run_direct(sid_plan* p, const char* who, const std::vector<LibBox>& boxes, float* out, int out_layout,
+                   cudaStream_t st);
+int lib_run_spectral(sid_plan* p, const char* who, const std::vector<LibBox>& boxes, float* out, int out_layout,
+                     cudaStream_t st);
+
+// LibBox lattice window fields (s0..t1) of a box whose x0..z1 are set
+void lib_box_window(const sid_plan* p, LibBox& b);
+
 }  // namespace sid

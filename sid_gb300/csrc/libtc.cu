@@ -323,31 +323,21 @@ static int launch_pack(dim3 grid, const float* packed, const LibBox* boxes, cons
     return SID_OK;
 }
 
-}  // namespace sid
-
-using namespace sid;
-
-extern "C" int sid_library_spectral(sid_plan* p, const float* const* recon, int64_t n_comp, const double* centers,
-                                    const uint8_t* neur_id, int64_t n_neur, int64_t neur_rad, double axial,
-                                    float* out, int out_layout, void* stream)
+// Forward projections of the staged boxes (lib_stage: boxes in p->ws[3] and
+// `boxes`, packed values in p->ws[2]) into the library rows, on the tensor
+// cores; leaves `st` to be synchronised by the caller.
+int lib_run_spectral(sid_plan* p, const char* who, const std::vector<LibBox>& boxes, float* out, int out_layout,
+                     cudaStream_t st)
 {
-    SID_REQUIRE(p && recon && centers && neur_id && out, "sid_library_spectral: NULL argument");
-    SID_REQUIRE(n_comp >= 1 && n_neur >= 1 && neur_rad >= 0 && axial > 0,
-                "sid_library_spectral: need n_comp >= 1, n_neur >= 1, neur_rad >= 0, axial > 0");
-    SID_REQUIRE(out_layout == 0 || out_layout == 1,
-                "sid_library_spectral: out_layout must be 0 (n x P) or 1 (P x n)");
-    SID_REQUIRE(!p->adj_separate, "sid_library_spectral: the spectral form needs odd PSF crop widths");
-    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    SID_REQUIRE(!p->adj_separate, "%s: the spectral form needs odd PSF crop widths", who);
+    const int64_t n_neur = (int64_t)boxes.size();
     const int64_t N = p->N, D = p->g.D, n_out = N * N, n_in = N * N * p->Z, n_in_pad = cdiv(n_in, 8) * 8;
-    std::vector<LibBox> boxes;
-    SID_TRY(lib_stage(p, "sid_library_spectral", recon, n_comp, centers, neur_id, n_neur, neur_rad, axial, boxes,
-                      st));
     int span = 1, mu = 1;
     for (const LibBox& b : boxes) {
         span = std::max(span, std::max((b.x1 - 1) / (int)N - b.x0 / (int)N, (b.y1 - 1) / (int)N - b.y0 / (int)N) + 1);
         mu = std::max(mu, (int)std::max(cdiv(b.x1 - b.x0, N), cdiv(b.y1 - b.y0, N)));
     }
-    SID_REQUIRE(mu <= 6, "sid_library_spectral: boxes of more than 6 lattice points per phase (use sid_library)");
+    SID_REQUIRE(mu <= 6, "%s: boxes of more than 6 lattice points per phase (use the FP32 tap form)", who);
     SID_TRY(libwin_ensure(p, span + D - 1));
     LibWin* w = p->libwin;
     const int64_t L = w->L, nf = w->nf, Wo = w->Wo;
@@ -423,8 +413,29 @@ extern "C" int sid_library_spectral(sid_plan* p, const float* const* recon, int6
         SID_CHECK_LAUNCH();
         SID_CUDA_TRY(cudaEventRecord(w->syn_done[buf], w->side));
     }
-    // join the synthesis stream (in order: its last event covers every pass), then
-    // wait: the staging buffers are read by the kernels above until they finish
+    // join the synthesis stream (in order: its last event covers every pass)
     SID_CUDA_TRY(cudaStreamWaitEvent(st, w->syn_done[(passes.size() - 1) & 1], 0));
+    return SID_OK;
+}
+
+}  // namespace sid
+
+using namespace sid;
+
+extern "C" int sid_library_spectral(sid_plan* p, const float* const* recon, int64_t n_comp, const double* centers,
+                                    const uint8_t* neur_id, int64_t n_neur, int64_t neur_rad, double axial,
+                                    float* out, int out_layout, void* stream)
+{
+    SID_REQUIRE(p && recon && centers && neur_id && out, "sid_library_spectral: NULL argument");
+    SID_REQUIRE(n_comp >= 1 && n_neur >= 1 && neur_rad >= 0 && axial > 0,
+                "sid_library_spectral: need n_comp >= 1, n_neur >= 1, neur_rad >= 0, axial > 0");
+    SID_REQUIRE(out_layout == 0 || out_layout == 1,
+                "sid_library_spectral: out_layout must be 0 (n x P) or 1 (P x n)");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    std::vector<LibBox> boxes;
+    SID_TRY(lib_stage(p, "sid_library_spectral", recon, n_comp, centers, neur_id, n_neur, neur_rad, axial, boxes,
+                      st));
+    SID_TRY(lib_run_spectral(p, "sid_library_spectral", boxes, out, out_layout, st));
+    // the staging buffers are read by the kernels above until they finish
     return plan_sync(p, st);
 }

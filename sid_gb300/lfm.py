@@ -595,3 +595,61 @@ def generate_LFM_library_GPU(recon, centers, neur_id, psf, options, layout="rows
               ids.ctypes.data, n, int(options["neur_rad"]), float(options["axial"]), out.data_ptr(),
               0 if layout == "rows" else 1, _stream_ptr())
     return out
+
+
+def _kernel_args(kernel):
+    if kernel is None:
+        return None, 0, 0, 0, None
+    W = np.asfortranarray(np.asarray(kernel, dtype=np.float32))
+    if W.ndim == 2:
+        W = W[:, :, None]
+    return W.ctypes.data, W.shape[0], W.shape[1], W.shape[2], W
+
+
+def library_kernel_voxels(centers, r, dim, m, Z, kernel=None):
+    """The voxels generate_LFM_library_CPU.m:39-49 paints per neuron: a list of
+    (count, 3) 0-based (x, y, z) arrays and their kernel values, computed by
+    libsid's host code."""
+    c = np.asfortranarray(np.asarray(centers, dtype=np.float64).reshape(-1, 3))
+    n = c.shape[0]
+    kp, kx, ky, kz, keep = _kernel_args(kernel)
+    dz = float(np.asarray(dim, dtype=np.float64).ravel()[2]) if kernel is None else 1.0
+    counts = np.zeros(n, dtype=np.int64)
+    _lib.call("sid_library_kernel_voxels", c.ctypes.data, n, float(r), dz, kp, kx, ky, kz, int(m[0]), int(m[1]),
+              int(Z), counts.ctypes.data, None, None, 0)
+    tot = int(counts.sum())
+    xyz = np.zeros((max(tot, 1), 3), dtype=np.int32)
+    vals = np.zeros(max(tot, 1), dtype=np.float32)
+    _lib.call("sid_library_kernel_voxels", c.ctypes.data, n, float(r), dz, kp, kx, ky, kz, int(m[0]), int(m[1]),
+              int(Z), counts.ctypes.data, xyz.ctypes.data, vals.ctypes.data, tot)
+    del keep
+    out, at = [], 0
+    for k in counts:
+        out.append((xyz[at:at + k].copy(), vals[at:at + k].copy()))
+        at += int(k)
+    return out
+
+
+def generate_LFM_library_CPU(centers, psf, r, dim, m, kernel=None, layout="rows", method="direct"):
+    """forward_model = generate_LFM_library_CPU(centers, psf_ballistic, r, dim, m, kernel)
+    (generate_LFM_library_CPU.m:1): every neuron is the kernel (or the ball of
+    radius r, axial radius r / dim(3)) painted at its centre, forward-projected
+    and L2-normalised.  Returns the dense (n, X*Y) rows on the GPU ('rows') or
+    their transpose ('columns'); the reference's sparse matrix holds their
+    nonzeros.  method 'direct' (FP32 lenslet taps) or 'spectral'
+    (tensor-core windows)."""
+    if method not in ("direct", "spectral"):
+        raise ValueError(f"method must be 'direct' or 'spectral', not {method!r}")
+    H = psf["H"] if isinstance(psf, dict) else psf
+    X, Y = int(m[0]), int(m[1])
+    proj = _plan_for(H, (X, Y), None, "direct")
+    c = np.asfortranarray(np.asarray(centers, dtype=np.float64).reshape(-1, 3))
+    n = c.shape[0]
+    kp, kx, ky, kz, keep = _kernel_args(kernel)
+    dz = float(np.asarray(dim, dtype=np.float64).ravel()[2]) if kernel is None else 1.0
+    out = _fortran_tensor((n, X * Y) if layout == "rows" else (X * Y, n), "cuda")
+    _lib.call("sid_library_kernel", proj._plan, _lib.METHODS["direct" if method == "direct" else "spectral_mixed"],
+              c.ctypes.data, n, float(r), dz, kp, kx, ky, kz, out.data_ptr(), 0 if layout == "rows" else 1,
+              _stream_ptr())
+    del keep
+    return out

@@ -31,6 +31,8 @@
  *              imgs X x Y x n, X X x Y x Z x n (groups of components per pass)
  *   [X, hist] = sid_mex('isra_ex', plan, Htf, Xguess, maxIter, mode, p, lambda, method)   mode 0 basic, 1 TV
  *   X        = sid_mex('ls_deconv_ex', plan, df, max_iter, lamb_L1, lamb_L2, lamb_TV_L2, lamb_TV_L1, method)
+ *   F        = sid_mex('library_kernel', plan, centers, r, dim, kernel, method)   kernel [] for the ball;
+ *              method 'direct' or 'spectral'; F n x P single gpuArray of L2-normalised rows
  *   F        = sid_mex('library', plan, recon, centers, neur_id, neur_rad, axial[, method])   recon: cell of
  *              volumes; method 'direct' (default, FP32 lenslet taps) or 'spectral' (tensor-core windows)
  *   Fm       = sid_mex('spatial_update', T, Y, template, opts)     template: logical (R - bg_sub) x P
@@ -748,6 +750,43 @@ void mexFunction(int nlhs, mxArray* plhs[], int nrhs, const mxArray* prhs[])
                                                                  NULL);
         for (mwSize k = 0; k < nc; ++k) mxGPUDestroyGPUArray(vols[k]);
         mxDestroyArray(ids);
+        if (rc != SID_OK) mxGPUDestroyGPUArray(F);
+        check(rc, cmd);
+        plhs[0] = mxGPUCreateMxArrayOnGPU(F);
+        mxGPUDestroyGPUArray(F);
+        return;
+    }
+    if (!strcmp(cmd, "library_kernel")) {
+        /* F = sid_mex('library_kernel', plan, centers, r, dim, kernel, method): centers n x 3 double, kernel a
+         * single array (or [] for the ball of radius r, axial radius r / dim(3)); F n x P single gpuArray */
+        if (nrhs < 7) mexErrMsgIdAndTxt("sid:library_kernel", "usage: sid_mex('library_kernel', plan, centers, r, dim, kernel, method)");
+        sid_plan* p = plan_arg(prhs[1]);
+        char m[16];
+        if (mxGetString(prhs[6], m, sizeof(m)) != 0 || (strcmp(m, "direct") && strcmp(m, "spectral")))
+            mexErrMsgIdAndTxt("sid:library_kernel", "method must be 'direct' or 'spectral'");
+        if (!mxIsDouble(prhs[2]) || mxGetNumberOfDimensions(prhs[2]) != 2 || mxGetN(prhs[2]) != 3)
+            mexErrMsgIdAndTxt("sid:library_kernel", "centers must be an n x 3 double matrix");
+        if (!mxIsDouble(prhs[4]) || mxGetNumberOfElements(prhs[4]) < 3)
+            mexErrMsgIdAndTxt("sid:library_kernel", "dim must be a 3-element double vector");
+        const mwSize n = mxGetM(prhs[2]);
+        const float* W = NULL;
+        int64_t kd[3] = {0, 0, 0};
+        if (!mxIsEmpty(prhs[5])) {
+            if (!mxIsSingle(prhs[5])) mexErrMsgIdAndTxt("sid:library_kernel", "kernel must be single");
+            const mwSize nd = mxGetNumberOfDimensions(prhs[5]);
+            const mwSize* dd = mxGetDimensions(prhs[5]);
+            kd[0] = (int64_t)dd[0];
+            kd[1] = (int64_t)dd[1];
+            kd[2] = nd > 2 ? (int64_t)dd[2] : 1;
+            W = (const float*)mxGetData(prhs[5]);
+        }
+        int64_t info[14];
+        sid_plan_info(p, info);
+        mwSize df[2] = {n, (mwSize)(info[3] * info[4])};
+        mxGPUArray* F = mxGPUCreateGPUArray(2, df, mxSINGLE_CLASS, mxREAL, MX_GPU_DO_NOT_INITIALIZE);
+        int rc = sid_library_kernel(p, strcmp(m, "direct") ? SID_METHOD_SPECTRAL_MIXED : SID_METHOD_DIRECT,
+                                    mxGetPr(prhs[2]), (int64_t)n, mxGetScalar(prhs[3]), mxGetPr(prhs[4])[2], W, kd[0],
+                                    kd[1], kd[2], (float*)mxGPUGetData(F), 0, NULL);
         if (rc != SID_OK) mxGPUDestroyGPUArray(F);
         check(rc, cmd);
         plhs[0] = mxGPUCreateMxArrayOnGPU(F);

@@ -33,6 +33,9 @@ bool mxIsEmpty(const mxArray* a);
 bool mxIsStruct(const mxArray* a);
 bool mxIsChar(const mxArray* a);
 bool mxIsSingle(const mxArray* a);
+bool mxIsDouble(const mxArray* a);
+size_t mxGetM(const mxArray* a);
+size_t mxGetN(const mxArray* a);
 mxArray* mxCreateDoubleScalar(double v);
 mxArray* mxCreateDoubleMatrix(mwSize m, mwSize n, mxComplexity c);
 mxArray* mxCreateNumericMatrix(mwSize m, mwSize n, mxClassID cls, mxComplexity c);

@@ -99,3 +99,70 @@ def test_spectral_library_many_passes(gpu, oracle):
     ref = oracle.generate_library(recon, centers[pick], neur_id[pick], H, 12, 6.0)
     for k, n in enumerate(pick):
         assert rel_l2(spec[n], ref[k]) < 5e-5, n
+
+
+def _kernel_centers(X, Y, Z, n, seed):
+    rng = np.random.default_rng(seed)
+    c = np.stack([rng.uniform(-3, X + 3, n), rng.uniform(-3, Y + 3, n), rng.uniform(0.2, Z + 0.8, n)], 1)
+    c[:6, 0] = np.arange(6) + 0.5          # exact halves: MATLAB rounds away from zero
+    c[6:12, 2] = 0.5 + np.arange(6) % Z
+    c[12] = [1.0, 1.0, 1.0]                 # corner
+    return c
+
+
+@pytest.mark.parametrize("r,dimz,kernel", [(4, 2.0, None), (3, 1.6, None), (2, 0.5, None),
+                                          (0, 1.0, "custom"), (0, 1.0, "even")])
+def test_kernel_voxels_bit_exact(sidlib, oracle, r, dimz, kernel):
+    """The voxels generate_LFM_library_CPU.m:39-49 paints (ball with integer
+    and fractional axial radius, a given kernel with zeros, and one of even
+    size whose offsets are half-integers): libsid's host code against the
+    oracle, index for index."""
+    from sid_gb300 import library_kernel_voxels
+    X, Y, Z = 60, 45, 9
+    W = None
+    if kernel == "custom":
+        W = np.random.default_rng(1).random((5, 7, 3)).astype(np.float32)
+        W[W < 0.3] = 0
+    elif kernel == "even":
+        W = np.random.default_rng(2).random((4, 4, 2)).astype(np.float32) + 0.1
+    c = _kernel_centers(X, Y, Z, 60, 9)
+    got = library_kernel_voxels(c, r, [1, 1, dimz], (X, Y, Z), Z, kernel=W)
+    ref = oracle.library_kernel_voxels(c, r, [1, 1, dimz], (X, Y, Z), Z, kernel=W)
+    assert len(got) == len(ref)
+    for (gx, gv), (rx, rv) in zip(got, ref):
+        np.testing.assert_array_equal(gx, rx)
+        np.testing.assert_array_equal(gv, rv)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("method,bar", [("direct", 1e-5), ("spectral", 3e-5)])
+@pytest.mark.parametrize("case", ["ball", "kernel"])
+def test_library_cpu_form_matches_oracle(gpu, oracle, method, bar, case):
+    """generate_LFM_library_CPU (generate_LFM_library_CPU.m:18-70): the painted
+    kernels through the frame projection, L2-normalised, against the oracle's
+    literal patch projection (project_forward_patched.m:8-73: odd lenslet
+    patch, conv2 'full', centred paste clipped to the sensor) in FP64."""
+    import sid_gb300 as s
+    from sid_gb300 import synthetic
+    N, Z, M, L = 5, 7, 41, 12
+    X = N * L
+    H = synthetic.gaussian_psf(M, N, Z, sigma_min=1.5, sigma_max=6.0)
+    rng = np.random.default_rng(21)
+    c = np.stack([rng.uniform(1, X, 10), rng.uniform(1, X, 10), rng.uniform(1, Z, 10)], 1)
+    c[0] = [1.0, 1.0, 1.0]
+    c[1] = [X - 0.5, X / 2, Z]
+    c[2] = [30.5, 12.5, 3.5]
+    W = None
+    if case == "kernel":
+        W = rng.random((7, 7, 3)).astype(np.float32)
+        W[W < 0.2] = 0
+    r, dim = 4, [1.0, 1.0, 2.0]
+    got = s.to_numpy(s.generate_LFM_library_CPU(c, {"H": H}, r, dim, (X, X, Z), kernel=W, method=method))
+    ref = oracle.generate_library_cpu(c, H, r, dim, (X, X), kernel=W)
+    assert got.shape == ref.shape
+    worst = max(rel_l2(got[n], ref[n]) for n in range(len(c)))
+    assert worst < bar, worst
+    np.testing.assert_allclose(np.linalg.norm(got.astype(np.float64), axis=1), 1.0, rtol=1e-5)
+    cols = s.to_numpy(s.generate_LFM_library_CPU(c, {"H": H}, r, dim, (X, X, Z), kernel=W, method=method,
+                                                 layout="columns"))
+    np.testing.assert_array_equal(cols, got.T)
