@@ -263,6 +263,11 @@ int sid_ctx_create(sid_ctx** ctx);
 int sid_ctx_destroy(sid_ctx* ctx);
 /* Wait for `stream`; SID_ETIMEOUT if a device-side wait ran out of budget. */
 int sid_ctx_sync(sid_ctx* ctx, void* stream);
+/* CUDA-event timing of the tensor-core GEMM launches (with their split-K sum
+ * or mirror) inside sid_gram / sid_cross, without the operand conversions:
+ * enable, run, then read the total and the number of timed calls (read resets). */
+int sid_ctx_timing_enable(sid_ctx* ctx, int on);
+int sid_ctx_timing_read(sid_ctx* ctx, double* total_ms, int64_t* launches);
 
 /* Precision of the contractions. */
 #define SID_PREC_FP32  0 /* FP32 SIMT: the plain path */

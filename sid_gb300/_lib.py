@@ -89,6 +89,8 @@ SIGNATURES = {
     "sid_selftest_wait_timeout": [ctypes.c_uint32, I32],
     "sid_library": [P, P, I64, P, P, I64, I64, F64, P, I32, P],
     "sid_library_spectral": [P, P, I64, P, P, I64, I64, F64, P, I32, P],
+    "sid_ctx_timing_enable": [P, I32],
+    "sid_ctx_timing_read": [P, P, P],
     "sid_library_kernel": [P, I32, P, I64, F64, F64, P, I64, I64, I64, P, I32, P],
     "sid_library_kernel_voxels": [P, I64, F64, F64, P, I64, I64, I64, I64, I64, I64, P, P, P, I64],
     "sid_library_boxes": [P, I64, I64, F64, I64, I64, I64, P],

@@ -81,8 +81,11 @@ int contract(sid_ctx* c, const float* A, const void* B, bool b_f16, int64_t m, i
         SID_TRY(copy16_blk(static_cast<const uint16_t*>(B), k, n, ldb, c->b_hi.as<uint16_t>(), st));
         const void* As[2] = {c->a_hi.p, c->a_lo.p};
         const void* Bs[2] = {c->b_hi.p, c->b_hi.p};
-        return gemm_tn_ds(As, Bs, split ? 2 : 1, m, n, k, false, C, ldc, alpha, sw + 14, beta, bn, splitk,
-                          c->ws.as<float>(), (int64_t)(c->ws.bytes / sizeof(float)), err, st);
+        c->timer.begin(st);
+        const int rc = gemm_tn_ds(As, Bs, split ? 2 : 1, m, n, k, false, C, ldc, alpha, sw + 14, beta, bn, splitk,
+                                  c->ws.as<float>(), (int64_t)(c->ws.bytes / sizeof(float)), err, st);
+        c->timer.finish(st);
+        return rc;
     }
     // FP32 x FP32: BF16 hi/lo splits of both (no scaling needed: BF16 keeps the FP32 exponent range)
     SID_TRY(c->a_hi.alloc(abytes));
@@ -99,11 +102,16 @@ int contract(sid_ctx* c, const float* A, const void* B, bool b_f16, int64_t m, i
     }
     const void* As[3] = {c->a_hi.p, c->a_hi.p, c->a_lo.p};
     const void* Bs[3] = {bh, bl, bh};
+    int rc;
+    c->timer.begin(st);
     if (same && beta == 0.f)  // A'A: hi*hi + hi*lo + lo*hi is symmetric as a whole
-        return gemm_tn_sym(As, Bs, split ? 3 : 1, m, k, true, C, ldc, alpha, bn, splitk, c->ws.as<float>(),
-                           (int64_t)(c->ws.bytes / sizeof(float)), err, st);
-    return gemm_tn(As, Bs, split ? 3 : 1, m, n, k, true, C, ldc, alpha, beta, bn, splitk, c->ws.as<float>(),
-                   (int64_t)(c->ws.bytes / sizeof(float)), err, st);
+        rc = gemm_tn_sym(As, Bs, split ? 3 : 1, m, k, true, C, ldc, alpha, bn, splitk, c->ws.as<float>(),
+                         (int64_t)(c->ws.bytes / sizeof(float)), err, st);
+    else
+        rc = gemm_tn(As, Bs, split ? 3 : 1, m, n, k, true, C, ldc, alpha, beta, bn, splitk, c->ws.as<float>(),
+                     (int64_t)(c->ws.bytes / sizeof(float)), err, st);
+    c->timer.finish(st);
+    return rc;
 }
 
 }  // namespace sid
@@ -133,6 +141,7 @@ extern "C" int sid_ctx_destroy(sid_ctx* c)
     if (!c) return SID_OK;
     DBuf* b[] = {&c->a_hi, &c->a_lo, &c->b_hi, &c->b_lo, &c->ws, &c->scal, &c->errflag, &c->scales};
     for (DBuf* x : b) x->release();
+    c->timer.release();
     for (DBuf& x : c->nn) x.release();
     for (DBuf& x : c->mf) x.release();
     for (DBuf& x : c->bg) x.release();
@@ -163,4 +172,28 @@ extern "C" int sid_cross(sid_ctx* c, const float* A, const void* Y, int ydtype, 
     const bool f16 = ydtype == SID_DTYPE_F16;
     SID_REQUIRE(!(f16 && prec == SID_PREC_FP32), "sid_cross: an FP16 movie needs SID_PREC_SPLIT or SID_PREC_BF16");
     return contract(c, A, Y, f16, K, F, P, P, P, h, K, 1.f, 0.f, prec, static_cast<cudaStream_t>(stream));
+}
+
+extern "C" int sid_ctx_timing_enable(sid_ctx* c, int on)
+{
+    SID_REQUIRE(c, "sid_ctx_timing_enable: NULL context");
+    if (on && !c->timer.on) c->timer.used = 0;
+    c->timer.on = on != 0;
+    return SID_OK;
+}
+
+extern "C" int sid_ctx_timing_read(sid_ctx* c, double* total_ms, int64_t* launches)
+{
+    SID_REQUIRE(c && total_ms && launches, "sid_ctx_timing_read: NULL argument");
+    double t = 0.0;
+    for (size_t i = 0; i < c->timer.used; ++i) {
+        SID_CUDA_TRY(cudaEventSynchronize(c->timer.end[i]));
+        float ms = 0.f;
+        SID_CUDA_TRY(cudaEventElapsedTime(&ms, c->timer.beg[i], c->timer.end[i]));
+        t += ms;
+    }
+    *total_ms = t;
+    *launches = (int64_t)c->timer.used;
+    c->timer.used = 0;
+    return SID_OK;
 }

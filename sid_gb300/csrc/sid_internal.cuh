@@ -268,4 +268,5 @@ struct sid_ctx {
     sid::DBuf mf[8];   // NMF step workspaces (T_update / S_update)
     sid::DBuf bg[6];   // movie scans (rank-1 background, standard-deviation image)
     sid::DBuf pix[6];  // K-blocked 16-bit copies of pixel-major factors and their right operands
+    sid::KTimer timer; // tensor-core GEMM launches of sid_gram / sid_cross (sid_ctx_timing_*)
 };

@@ -47,6 +47,17 @@ class Context:
     def sync(self):
         _lib.call("sid_ctx_sync", self._ctx, _stream_ptr())
 
+    def timing(self, on: bool):
+        """Time the tensor-core GEMM launches of gram / cross (sid_ctx_timing_enable)."""
+        _lib.call("sid_ctx_timing_enable", self._ctx, 1 if on else 0)
+
+    def timing_read(self):
+        """(total_ms, timed calls) of the GEMM launches since the last read."""
+        ms = ctypes.c_double()
+        n = ctypes.c_int64()
+        _lib.call("sid_ctx_timing_read", self._ctx, ctypes.byref(ms), ctypes.byref(n))
+        return ms.value, n.value
+
     def gram(self, A, prec="split") -> torch.Tensor:
         """G = A'*A for A (P x K)."""
         A = to_device(A)
