@@ -319,33 +319,44 @@ static int64_t gemm_tiles(int m, int n, int bn, bool sym)
 }
 
 // Tile width and split-K choice (the project's autotuner for this kernel).
-// For each tile width BN in {256, 192, 128, 64} split K until there are >= 4 waves
-// of CTAs on the SMs (or a split would hold fewer than 8 K blocks), then
-// estimate the time as waves x K blocks per CTA x BN / efficiency(BN) and keep
-// the fastest.  The efficiencies model tcgen05's shared-memory operand traffic
-// per MMA: A (128 x 16) plus B (BN x 16) must be read for 128*BN*16 MACs, so
-// BN = 64 is limited by shared-memory bandwidth (measured) and BN = 256
-// amortises A best.  A symmetric product counts only the tiles it computes.
+// For each tile width BN in {256, 192, 128, 64} and each split of K into s
+// parts of >= 8 K blocks (s <= 64), estimate the time in units of one 64-deep
+// K block of one 128 x 256 tile (~0.75 us for three passes) as
+//   waves x (K blocks per CTA x BN / efficiency(BN) + 1024)    (+ s m n / 4096 if s > 1)
+// with waves = ceil(tiles x s / SMs), 1024 the fixed cost of a CTA (TMEM
+// allocation, pipeline fill, the drain of its tile; ~3 us) and the last term
+// the split-K sum's traffic, and keep the fastest: the split that fills the
+// last wave best, not merely the first that gives four waves.  The
+// efficiencies model tcgen05's shared-memory operand traffic per MMA:
+// A (128 x 16) plus B (BN x 16) must be read for 128*BN*16 MACs, so BN = 64
+// is limited by shared-memory bandwidth (measured) and BN = 256 amortises A
+// best.  A symmetric product counts only the tiles it computes (the 800-wide
+// Gram: 19 tiles of 256 columns hold 1.95x the triangle's outputs, 28 of 128
+// columns 1.43x).
 static void gemm_autotune_impl(int m, int n, int nkb, bool sym, int* bn, int* splitk)
 {
     const int sms = sm_count();
     const int cands[4] = {256, 192, 128, 64};
-    const double eff[4] = {1.0, 0.95, 0.85, 0.45};
+    // measured on the 800-wide Gram at P = 1,010,025 (of the MMA work each width computes):
+    // 256 at 99 % of the BF16 peak, 192 at 77 %, 128 at 53 %
+    const double eff[4] = {1.0, 0.78, 0.55, 0.45};
     double best = 1e300;
     int bbn = 256, bs = 1;
     for (int i = 0; i < 4; ++i) {
         const int c = cands[i];
         const int64_t tiles = gemm_tiles(m, n, c, sym);
-        int s = 1;
-        while (tiles * s < 4 * sms && nkb / (s + 1) >= 8) ++s;
-        const int64_t kb_per = cdiv(nkb, s);
-        s = (int)cdiv(nkb, kb_per);
-        const int64_t waves = cdiv(tiles * s, sms);
-        const double t = (double)waves * (double)kb_per * (double)c / eff[i];
-        if (t < best * (1.0 - 1e-9)) {
-            best = t;
-            bbn = c;
-            bs = s;
+        for (int s0 = 1; s0 <= 64; ++s0) {
+            if (s0 > 1 && nkb / s0 < 8) break;
+            const int64_t kb_per = cdiv(nkb, s0);
+            const int s = (int)cdiv(nkb, kb_per);
+            const int64_t waves = cdiv(tiles * s, sms);
+            const double t = (double)waves * ((double)kb_per * (double)c / eff[i] + 1024.0) +
+                             (s > 1 ? (double)s * (double)m * (double)n / 4096.0 : 0.0);
+            if (t < best * (1.0 - 1e-9)) {
+                best = t;
+                bbn = c;
+                bs = s;
+            }
         }
     }
     *bn = bbn;
