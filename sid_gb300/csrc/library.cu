@@ -671,17 +671,19 @@ __global__ void k_row_sumsq(const float* __restrict__ out, int64_t n_neur, int64
 __global__ void k_row_scale(float* __restrict__ out, int64_t n_neur, int64_t P, int64_t ldn, int64_t ldp,
                             const double* __restrict__ part)
 {
-    const int64_t n = blockIdx.y;
     __shared__ double inv;
-    if (threadIdx.x == 0) {
-        double s = 0.0;
-        for (int c = 0; c < kNormChunks; ++c) s += part[c * n_neur + n];
-        inv = 1.0 / sqrt(s);
-    }
-    __syncthreads();
-    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < P; q += (int64_t)gridDim.x * blockDim.x) {
-        float* o = out + n * ldn + q * ldp;
-        *o = (float)((double)*o * inv);
+    for (int64_t n = blockIdx.y; n < n_neur; n += gridDim.y) {
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double s = 0.0;
+            for (int c = 0; c < kNormChunks; ++c) s += part[c * n_neur + n];
+            inv = 1.0 / sqrt(s);
+        }
+        __syncthreads();
+        for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < P; q += (int64_t)gridDim.x * blockDim.x) {
+            float* o = out + n * ldn + q * ldp;
+            *o = (float)((double)*o * inv);
+        }
     }
 }
 
@@ -732,7 +734,8 @@ extern "C" int sid_library_kernel(sid_plan* p, int method, const double* centers
     k_row_sumsq<<<dim3(kNormChunks, (unsigned)std::min<int64_t>(cdiv(n_neur, 128), 64)), 128, 0, st>>>(
         out, n_neur, P, ldn, ldp, p->red.as<double>());
     SID_CHECK_LAUNCH();
-    k_row_scale<<<dim3(64, (unsigned)n_neur), 256, 0, st>>>(out, n_neur, P, ldn, ldp, p->red.as<double>());
+    k_row_scale<<<dim3(64, (unsigned)std::min<int64_t>(n_neur, 65535)), 256, 0, st>>>(out, n_neur, P, ldn, ldp,
+                                                                                    p->red.as<double>());
     SID_CHECK_LAUNCH();
     return plan_sync(p, st);
 }

@@ -331,6 +331,7 @@ int lib_run_spectral(sid_plan* p, const char* who, const std::vector<LibBox>& bo
 {
     SID_REQUIRE(!p->adj_separate, "%s: the spectral form needs odd PSF crop widths", who);
     const int64_t n_neur = (int64_t)boxes.size();
+    if (n_neur == 0) return SID_OK;
     const int64_t N = p->N, D = p->g.D, n_out = N * N, n_in = N * N * p->Z, n_in_pad = cdiv(n_in, 8) * 8;
     int span = 1, mu = 1;
     for (const LibBox& b : boxes) {
