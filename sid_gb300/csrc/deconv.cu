@@ -160,17 +160,45 @@ static int dot(const float* a, const float* b, int64_t n, double* scratch, doubl
 
 // ISRA update, deconvRL.m:52,55,85-87:
 //   e = Htf ./ (B + lambda); e(isinf(e)) = 0; X = X .* e; X(isnan(X)) = 0
+__device__ __forceinline__ float isra_one(float x, float h, float b, float lambda)
+{
+    const float den = (lambda != 0.f) ? b + lambda : b;
+    float e = __fdiv_rn(h, den);
+    if (isinf(e)) e = 0.f;
+    const float v = x * e;
+    return isnan(v) ? 0.f : v;
+}
+
 __global__ void k_isra_update(float* __restrict__ x, const float* __restrict__ htf, const float* __restrict__ b,
                               float lambda, int64_t n)
 {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const float den = (lambda != 0.f) ? b[i] + lambda : b[i];
-        float e = __fdiv_rn(htf[i], den);
-        if (isinf(e)) e = 0.f;
-        float v = x[i] * e;
-        if (isnan(v)) v = 0.f;
-        x[i] = v;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        x[i] = isra_one(x[i], htf[i], b[i], lambda);
+}
+
+// the same on 16-byte-aligned arrays, four elements per load (the tail n % 4 by the first threads)
+__global__ void k_isra_update4(float* __restrict__ x, const float* __restrict__ htf, const float* __restrict__ b,
+                               float lambda, int64_t n)
+{
+    const int64_t n4 = n >> 2;
+    float4* x4 = reinterpret_cast<float4*>(x);
+    const float4* h4 = reinterpret_cast<const float4*>(htf);
+    const float4* b4 = reinterpret_cast<const float4*>(b);
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n4; i += (int64_t)gridDim.x * blockDim.x) {
+        const float4 xv = x4[i], hv = h4[i], bv = b4[i];
+        x4[i] = make_float4(isra_one(xv.x, hv.x, bv.x, lambda), isra_one(xv.y, hv.y, bv.y, lambda),
+                            isra_one(xv.z, hv.z, bv.z, lambda), isra_one(xv.w, hv.w, bv.w, lambda));
     }
+    const int64_t t = 4 * n4 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t < n) x[t] = isra_one(x[t], htf[t], b[t], lambda);
+}
+
+static void launch_isra_update(float* x, const float* htf, const float* b, float lambda, int64_t n, cudaStream_t st)
+{
+    const bool al = ((reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(htf) |
+                      reinterpret_cast<uintptr_t>(b)) & 15u) == 0;
+    if (al) k_isra_update4<<<1216, 256, 0, st>>>(x, htf, b, lambda, n);
+    else k_isra_update<<<2048, 256, 0, st>>>(x, htf, b, lambda, n);
 }
 
 // Poisson RL ratio in sensor space: r = y / AX, 0 where not finite (AX = 0,
@@ -376,7 +404,7 @@ static dim3 poly_grid(const sid_plan* p) { return dim3((unsigned)cdiv(p->Lx * p-
 
 static int isra_update(sid_plan* p, float* xp, const float* hp, float lambda, cudaStream_t st)
 {
-    k_isra_update<<<2048, 256, 0, st>>>(xp, hp, p->bp.as<float>(), lambda, vol_plane_elems(p) * p->Z);
+    launch_isra_update(xp, hp, p->bp.as<float>(), lambda, vol_plane_elems(p) * p->Z, st);
     SID_CHECK_LAUNCH();
     return SID_OK;
 }
@@ -537,7 +565,7 @@ extern "C" int sid_deconv_rl_poisson(sid_plan* p, int method, const float* y, fl
         SID_CHECK_LAUNCH();
         SID_TRY(adj_poly(p, method, ip, bp, st));
         // X <- X .* (A'r ./ A'1): the ISRA update with numerator A'r, denominator A'1
-        k_isra_update<<<2048, 256, 0, st>>>(xp, bp, np_, 0.f, n);
+        launch_isra_update(xp, bp, np_, 0.f, n, st);
         SID_CHECK_LAUNCH();
     }
     SID_TRY(vp_to_v(p, xp, X, p->Z, st));
@@ -787,7 +815,7 @@ extern "C" int sid_deconv_isra_batched(sid_plan* p, int method, int64_t nb, cons
         for (int it = 0; it < maxIter; ++it) {
             SID_TRY(fwd_poly_batch(p, method, xp, ip, n, st));
             SID_TRY(adj_poly_batch(p, method, ip, bp, n, st));
-            k_isra_update<<<2048, 256, 0, st>>>(xp, hp, bp, lambda, n * nv);
+            launch_isra_update(xp, hp, bp, lambda, n * nv, st);
             SID_CHECK_LAUNCH();
         }
         for (int b = 0; b < n; ++b) SID_TRY(vp_to_v(p, xp + b * nv, X[b0 + b], p->Z, st));

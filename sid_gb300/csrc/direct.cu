@@ -25,23 +25,51 @@ namespace sid {
 
 // ---------------------------------------------------------------- layouts --
 // Vp[c][b][a][v][u] <- V(a+N*u, b+N*v, c); zero outside X x Y.  V may be a
-// caller's host array (device view): each CTA reads one contiguous row.
-__global__ void k_v_to_vp(const float* __restrict__ V, float* __restrict__ Vp, int64_t X, int64_t Y,
-                          int N, int Lx, int Ly)
+// caller's host array (device view).  One CTA per (kLayoutRows lattice rows v,
+// input row phase b, depth c): it reads the rows y = b + N v (contiguous) into
+// shared memory and writes, per column phase a, the rows' lattice points as
+// one contiguous run of kLayoutRows x Lx values.
+constexpr int kLayoutRows = 8;
+constexpr int kLayoutBatch = 4;  // loads per row and thread kept in flight
+
+__global__ void __launch_bounds__(256)
+k_v_to_vp(const float* __restrict__ V, float* __restrict__ Vp, int64_t X, int64_t Y, int N, int Lx, int Ly)
 {
-    extern __shared__ float s[];
-    const int y = blockIdx.x;  // 0 .. N*Ly-1
-    const int c = blockIdx.y;
-    const int b = y % N, v = y / N;
+    extern __shared__ float s[];  // [kLayoutRows][N * Lx]
+    const int v0 = blockIdx.x * kLayoutRows, b = blockIdx.y, c = blockIdx.z;
     const int W = N * Lx;
-    const bool yin = y < Y;
-    for (int x = threadIdx.x; x < W; x += blockDim.x)
-        s[x] = (yin && x < X) ? V[x + X * ((int64_t)y + Y * c)] : 0.f;
+    const int nr = min(kLayoutRows, Ly - v0);
+    // all rows' loads of a column block are issued before any is stored (the
+    // source may sit across the host link: many requests in flight per thread)
+    for (int x0 = 0; x0 < W; x0 += kLayoutBatch * blockDim.x) {
+        float t[kLayoutRows][kLayoutBatch];
+#pragma unroll
+        for (int r = 0; r < kLayoutRows; ++r) {
+            const int64_t y = b + (int64_t)N * (v0 + r);
+            const float* row = V + X * (y + Y * c);
+#pragma unroll
+            for (int k = 0; k < kLayoutBatch; ++k) {
+                const int x = x0 + threadIdx.x + k * blockDim.x;
+                t[r][k] = (r < nr && y < Y && x < X) ? row[x] : 0.f;
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < kLayoutRows; ++r)
+#pragma unroll
+            for (int k = 0; k < kLayoutBatch; ++k) {
+                const int x = x0 + threadIdx.x + k * blockDim.x;
+                if (r < nr && x < W) s[r * W + x] = t[r][k];
+            }
+    }
     __syncthreads();
     const int64_t plane = (int64_t)Ly * Lx;
-    for (int idx = threadIdx.x; idx < W; idx += blockDim.x) {
-        const int a = idx / Lx, u = idx - a * Lx;
-        Vp[(((int64_t)c * N + b) * N + a) * plane + (int64_t)v * Lx + u] = s[a + N * u];
+    const int run = nr * Lx;
+    for (int a = 0; a < N; ++a) {
+        float* dst = Vp + (((int64_t)c * N + b) * N + a) * plane + (int64_t)v0 * Lx;
+        for (int e = threadIdx.x; e < run; e += blockDim.x) {
+            const int r = e / Lx, u = e - r * Lx;
+            dst[e] = s[r * W + a + N * u];
+        }
     }
 }
 
@@ -492,17 +520,29 @@ int direct_adjoint(sid_plan* p, const float* ip, float* bp, int* err, cudaStream
 }
 
 // Layout launchers.
+static int layout_launch_check(const sid_plan* p, int64_t Z, size_t* smem)
+{
+    *smem = (size_t)(kLayoutRows * p->N * p->Lx) * sizeof(float);
+    SID_REQUIRE(*smem <= 200 * 1024, "volume layout: rows of %lld lenslets x %lld too long", (long long)p->Lx,
+                (long long)p->N);
+    SID_REQUIRE(Z <= 65535, "volume layout: %lld depths above the grid limit", (long long)Z);
+    return SID_OK;
+}
+
 int v_to_vp(const sid_plan* p, const float* V, float* vp, int64_t Z, cudaStream_t st)
 {
-    dim3 grid((unsigned)(p->N * p->Ly), (unsigned)Z);
-    k_v_to_vp<<<grid, 256, (size_t)(p->N * p->Lx) * sizeof(float), st>>>(V, vp, p->X, p->Y, (int)p->N,
-                                                                          (int)p->Lx, (int)p->Ly);
+    size_t sm = 0;
+    SID_TRY(layout_launch_check(p, Z, &sm));
+    SID_CUDA_TRY(cudaFuncSetAttribute(k_v_to_vp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    dim3 grid((unsigned)cdiv(p->Ly, kLayoutRows), (unsigned)p->N, (unsigned)Z);
+    k_v_to_vp<<<grid, 256, sm, st>>>(V, vp, p->X, p->Y, (int)p->N, (int)p->Lx, (int)p->Ly);
     SID_CHECK_LAUNCH();
     return SID_OK;
 }
 
 int vp_to_v(const sid_plan* p, const float* vp, float* V, int64_t Z, cudaStream_t st)
 {
+    SID_REQUIRE(Z <= 65535, "volume layout: %lld depths above the grid limit", (long long)Z);
     dim3 grid((unsigned)p->Y, (unsigned)Z);
     k_vp_to_v<<<grid, 256, (size_t)(p->N * p->Lx) * sizeof(float), st>>>(vp, V, p->X, p->Y, (int)p->N,
                                                                           (int)p->Lx, (int)p->Ly);
