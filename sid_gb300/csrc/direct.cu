@@ -533,7 +533,7 @@ int v_to_vp(const sid_plan* p, const float* V, float* vp, int64_t Z, cudaStream_
 {
     size_t sm = 0;
     SID_TRY(layout_launch_check(p, Z, &sm));
-    SID_CUDA_TRY(cudaFuncSetAttribute(k_v_to_vp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    SID_TRY(smem_attr((const void*)k_v_to_vp, sm));
     dim3 grid((unsigned)cdiv(p->Ly, kLayoutRows), (unsigned)p->N, (unsigned)Z);
     k_v_to_vp<<<grid, 256, sm, st>>>(V, vp, p->X, p->Y, (int)p->N, (int)p->Lx, (int)p->Ly);
     SID_CHECK_LAUNCH();

@@ -396,7 +396,7 @@ static int launch_r2c(const float* in, float2* out, const float2* tw, const FftD
 {
     const size_t sm = r2c_bytes(d, P);
     SID_REQUIRE(sm <= 200 * 1024, "spectral projector: lenslet grid too large for the FFT kernels");
-    SID_CUDA_TRY(cudaFuncSetAttribute(k_fft_r2c<P, QT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    SID_TRY(smem_attr((const void*)k_fft_r2c<P, QT>, sm));
     k_fft_r2c<P, QT><<<fft_grid(k_fft_r2c<P, QT>, sm, nch), kFftThreads, sm, st>>>(in, out, tw, d, nch);
     SID_CHECK_LAUNCH();
     return SID_OK;
@@ -408,7 +408,7 @@ static int launch_c2r(const float2* in, float* out, const float2* tw, const FftD
 {
     const size_t sm = c2r_bytes(d, P);
     SID_REQUIRE(sm <= 200 * 1024, "spectral projector: lenslet grid too large for the FFT kernels");
-    SID_CUDA_TRY(cudaFuncSetAttribute(k_fft_c2r<P, QT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    SID_TRY(smem_attr((const void*)k_fft_c2r<P, QT>, sm));
     k_fft_c2r<P, QT><<<fft_grid(k_fft_c2r<P, QT>, sm, nch), kFftThreads, sm, st>>>(in, out, tw, d, N, X, Y, nch);
     SID_CHECK_LAUNCH();
     return SID_OK;

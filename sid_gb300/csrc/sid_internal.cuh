@@ -57,6 +57,11 @@ inline int64_t cdiv(int64_t a, int64_t b) { return (a + b - 1) / b; }
 // Streaming multiprocessors of the current device (cudaDevAttrMultiProcessorCount,
 // looked up once per device ordinal; 152 on GB300).
 int sm_count();
+// cudaFuncSetAttribute(func, MaxDynamicSharedMemorySize, bytes) only when the
+// current device's setting for func is below bytes (kept per device and
+// function): the call costs host time, and a launch sequence of many small
+// kernels paid it on every launch.
+int smem_attr(const void* func, size_t bytes);
 // The power of two that brings a largest magnitude amax into [2^13, 2^14)
 // (1 for a zero or non-finite amax): the scale of an FP16 hi/lo split.
 __device__ __forceinline__ float pow2_for(float amax)
@@ -190,6 +195,7 @@ struct sid_plan {
     sid::DBuf weak_pad;         //   (recomputed exactly after each spectral back projection) and the
     int64_t nweak = 0;          //   zero-padded sensor-lattice copies their kernel reads
     sid::DBuf weak_part;        //   (partial sums when the tap arrays are split over several CTAs)
+    std::vector<int> weak_cz, weak_rz;  // column / row runs of depths [0, z) (Z + 1 entries each)
     int64_t nweak_cols = 0, nweak_rows = 0;
     double weak_frac = 1e-2;    // ... those with column mass A'1 below this fraction of the largest
     // workspaces
@@ -219,6 +225,12 @@ int spectral_forward(sid_plan* p, bool i16, const float* vp, float* ip, cudaStre
 // storage formats of the tap spectra
 enum SpecFmt { FMT_F32 = 0, FMT_I16 = 1, FMT_F24 = 2 };
 int spectral_adjoint(sid_plan* p, int fmt, const float* ip, float* bp, cudaStream_t st);
+// the forward contraction over input channels [c0, c1) (c0 on a 4-channel
+// boundary) from p->vhat into p->ihat, added to it when accum
+int spectral_forward_part(sid_plan* p, bool i16, int64_t c0, int64_t c1, bool accum, cudaStream_t st);
+int ensure_spec_ws(sid_plan* p);  // the channel spectra buffers p->vhat, p->ihat of one volume
+// the back projection's contraction alone: sensor lattice ip -> channel spectra p->vhat
+int spectral_adjoint_spectra(sid_plan* p, int fmt, const float* ip, cudaStream_t st);
 // nb (<= 4) polyphase volumes / images back to back
 int spectral_forward_batch(sid_plan* p, bool i16, const float* vp, float* ip, int nb, cudaStream_t st);
 int spectral_adjoint_batch(sid_plan* p, int fmt, const float* ip, float* bp, int nb, cudaStream_t st);
@@ -247,6 +259,9 @@ int weak_build(sid_plan* p);
 int weak_fix(sid_plan* p, const float* ip, float* bp, cudaStream_t st);
 int weak_fix_n(sid_plan* p, const float* ip, float* bp, int nb, cudaStream_t st);  // nb back to back
 int weak_qsplit(const sid_plan* p, int64_t nb);  // CTAs per weak run (> 1: a finishing launch adds the parts)
+bool weak_runs_path(const sid_plan* p);          // the weak voxels go through the run kernels
+int weak_pad(sid_plan* p, const float* ip, int nb, cudaStream_t st);                   // lattice copies
+int weak_runs(sid_plan* p, float* bp, int nb, int64_t z0, int64_t z1, cudaStream_t st);  // depths [z0, z1)
 int64_t libwin_bytes(const sid_plan* p);         // device bytes of the library windows
 int v_to_vp(const sid_plan* p, const float* V, float* vp, int64_t Z, cudaStream_t st);
 int vp_to_v(const sid_plan* p, const float* vp, float* V, int64_t Z, cudaStream_t st);

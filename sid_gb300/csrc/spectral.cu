@@ -543,20 +543,23 @@ template <> struct KLoad<true> {
 // 16-byte loads in flight per lane) and reduces them with warp shuffles.
 constexpr int kRB = 4;
 
+// The reduction may be restricted to the vectors [jv0, jv1) of each row (input
+// channels [EPL jv0, EPL jv1)); accum adds the result to ihat instead of
+// storing it (a projection formed depth slab by depth slab).
 template <bool I16>
 __global__ void __launch_bounds__(512)
 k_spec_fwd(const uint4* __restrict__ khat, const float* __restrict__ rstep, const float2* __restrict__ vhat,
-           float2* __restrict__ ihat, int n_in, int64_t n_in_pad, int n_out, int nf)
+           float2* __restrict__ ihat, int n_in, int64_t n_in_pad, int n_out, int nf, int jv0, int jv1, int accum)
 {
     using KL = KLoad<I16>;
     constexpr int EPL = KL::EPL;
-    extern __shared__ float2 xv[];  // [n_in_pad]
+    extern __shared__ float2 xv[];  // [EPL (jv1 - jv0)]: channels EPL jv0 ..
     const int f = blockIdx.x;
-    for (int k = threadIdx.x; k < n_in_pad; k += blockDim.x)
-        xv[k] = (k < n_in) ? vhat[(int64_t)k * nf + f] : make_float2(0.f, 0.f);
+    const int kb = EPL * jv0, nk = EPL * (jv1 - jv0);
+    for (int k = threadIdx.x; k < nk; k += blockDim.x)
+        xv[k] = (kb + k < n_in) ? vhat[(int64_t)(kb + k) * nf + f] : make_float2(0.f, 0.f);
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    const int nvec = (int)(n_in_pad / EPL);
     const int64_t rowvec = n_in_pad / EPL;  // uint4 per row
     for (int o0 = warp * kRB; o0 < n_out; o0 += nw * kRB) {
         float ar[kRB], ai[kRB];
@@ -568,13 +571,13 @@ k_spec_fwd(const uint4* __restrict__ khat, const float* __restrict__ rstep, cons
             kr[r] = khat + ((int64_t)f * n_out + o) * rowvec;
         }
 #pragma unroll 2
-        for (int j = lane; j < nvec; j += 32) {
+        for (int j = jv0 + lane; j < jv1; j += 32) {
             uint4 q[kRB];
 #pragma unroll
             for (int r = 0; r < kRB; ++r) q[r] = __ldcs(kr[r] + j);
             float2 x[EPL];
 #pragma unroll
-            for (int e = 0; e < EPL; ++e) x[e] = xv[EPL * j + e];
+            for (int e = 0; e < EPL; ++e) x[e] = xv[EPL * (j - jv0) + e];
 #pragma unroll
             for (int r = 0; r < kRB; ++r) {
                 float2 kk[EPL];
@@ -603,7 +606,13 @@ k_spec_fwd(const uint4* __restrict__ khat, const float* __restrict__ rstep, cons
                 if (lane == r) { re = ar[r]; im = ai[r]; }
             const int o = o0 + lane;
             const float st = I16 ? rstep[(int64_t)f * n_out + o] : 1.f;
-            ihat[(int64_t)o * nf + f] = make_float2(re * st, im * st);
+            float2* dst = ihat + (int64_t)o * nf + f;
+            if (accum) {
+                const float2 prev = *dst;
+                *dst = make_float2(prev.x + re * st, prev.y + im * st);
+            } else {
+                *dst = make_float2(re * st, im * st);
+            }
         }
     }
 }
@@ -813,7 +822,7 @@ k_spec_adj_b(const uint4* __restrict__ khat, const uint4* __restrict__ klo, cons
 }
 
 // ------------------------------------------------------------- launchers --
-static int ensure_spec_ws(sid_plan* p)
+int ensure_spec_ws(sid_plan* p)
 {
     const int64_t n_in = p->N * p->N * p->Z, n_out = p->N * p->N;
     SID_TRY(p->vhat.alloc((size_t)(n_in * p->nf) * sizeof(float2)));
@@ -827,8 +836,8 @@ static int configure_dft(const sid_plan* p)
     SID_REQUIRE(r2c_smem(d) <= 220 * 1024 && c2r_smem(d) <= 220 * 1024,
                 "spectral projector: lenslet grid %lldx%lld (L=%lld) exceeds the DFT kernels' shared memory",
                 (long long)p->Lx, (long long)p->Ly, (long long)p->L);
-    SID_CUDA_TRY(cudaFuncSetAttribute(k_dft_r2c, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)r2c_smem(d)));
-    SID_CUDA_TRY(cudaFuncSetAttribute(k_dft_c2r, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c2r_smem(d)));
+    SID_TRY(smem_attr((const void*)k_dft_r2c, r2c_smem(d)));
+    SID_TRY(smem_attr((const void*)k_dft_c2r, c2r_smem(d)));
     return SID_OK;
 }
 
@@ -896,26 +905,41 @@ int spectral_forward(sid_plan* p, bool i16, const float* vp, float* ip, cudaStre
     SID_TRY(configure_dft(p));
     const int64_t n_in = p->N * p->N * p->Z, n_out = p->N * p->N, n_in_pad = spec_nin_pad(p);
     SID_TRY(dft_r2c(p, vp, p->vhat.as<float2>(), n_in, st));
-    const size_t sm = (size_t)n_in_pad * sizeof(float2);
-    p->timer.begin(st);
-    if (i16) {
-        SID_CUDA_TRY(cudaFuncSetAttribute(k_spec_fwd<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-        k_spec_fwd<true><<<(unsigned)p->nf, 512, sm, st>>>(p->khat_i16.as<uint4>(), p->rstep.as<float>(),
-                                                          p->vhat.as<float2>(), p->ihat.as<float2>(), (int)n_in,
-                                                          n_in_pad, (int)n_out, (int)p->nf);
-    } else {
-        SID_CUDA_TRY(cudaFuncSetAttribute(k_spec_fwd<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-        k_spec_fwd<false><<<(unsigned)p->nf, 512, sm, st>>>(p->khat_f32.as<uint4>(), nullptr, p->vhat.as<float2>(),
-                                                           p->ihat.as<float2>(), (int)n_in, n_in_pad, (int)n_out,
-                                                           (int)p->nf);
-    }
-    p->timer.finish(st);
-    SID_CHECK_LAUNCH();
+    SID_TRY(spectral_forward_part(p, i16, 0, n_in, false, st));
+    (void)n_in_pad;
     SID_TRY(dft_c2r(p, p->ihat.as<float2>(), ip, n_out, st));
     return SID_OK;
 }
 
-int spectral_adjoint(sid_plan* p, int fmt, const float* ip, float* bp, cudaStream_t st)
+int spectral_forward_part(sid_plan* p, bool i16, int64_t c0, int64_t c1, bool accum, cudaStream_t st)
+{
+    SID_TRY(spec_check(p, i16 ? FMT_I16 : FMT_F32));
+    SID_TRY(ensure_spec_ws(p));
+    const int64_t n_in = p->N * p->N * p->Z, n_out = p->N * p->N, n_in_pad = spec_nin_pad(p);
+    const int epl = i16 ? 4 : 2;
+    SID_REQUIRE(c0 >= 0 && c0 < c1 && c1 <= n_in && c0 % epl == 0,
+                "spectral forward: channel range [%lld, %lld) not on a %d-channel boundary", (long long)c0,
+                (long long)c1, epl);
+    const int jv0 = (int)(c0 / epl), jv1 = (int)(c1 == n_in ? n_in_pad / epl : cdiv(c1, epl));
+    const size_t sm = (size_t)(jv1 - jv0) * epl * sizeof(float2);
+    p->timer.begin(st);
+    if (i16) {
+        SID_TRY(smem_attr((const void*)k_spec_fwd<true>, sm));
+        k_spec_fwd<true><<<(unsigned)p->nf, 512, sm, st>>>(p->khat_i16.as<uint4>(), p->rstep.as<float>(),
+                                                          p->vhat.as<float2>(), p->ihat.as<float2>(), (int)n_in,
+                                                          n_in_pad, (int)n_out, (int)p->nf, jv0, jv1, accum ? 1 : 0);
+    } else {
+        SID_TRY(smem_attr((const void*)k_spec_fwd<false>, sm));
+        k_spec_fwd<false><<<(unsigned)p->nf, 512, sm, st>>>(p->khat_f32.as<uint4>(), nullptr, p->vhat.as<float2>(),
+                                                           p->ihat.as<float2>(), (int)n_in, n_in_pad, (int)n_out,
+                                                           (int)p->nf, jv0, jv1, accum ? 1 : 0);
+    }
+    p->timer.finish(st);
+    SID_CHECK_LAUNCH();
+    return SID_OK;
+}
+
+int spectral_adjoint_spectra(sid_plan* p, int fmt, const float* ip, cudaStream_t st)
 {
     SID_TRY(spec_check(p, fmt));
     SID_TRY(ensure_spec_ws(p));
@@ -938,8 +962,13 @@ int spectral_adjoint(sid_plan* p, int fmt, const float* ip, float* bp, cudaStrea
                                                              n_in_pad, (int)n_out, (int)p->nf);
     p->timer.finish(st);
     SID_CHECK_LAUNCH();
-    SID_TRY(dft_c2r(p, p->vhat.as<float2>(), bp, n_in, st));
     return SID_OK;
+}
+
+int spectral_adjoint(sid_plan* p, int fmt, const float* ip, float* bp, cudaStream_t st)
+{
+    SID_TRY(spectral_adjoint_spectra(p, fmt, ip, st));
+    return dft_c2r(p, p->vhat.as<float2>(), bp, p->N * p->N * p->Z, st);
 }
 
 // nb (2..4) volumes per call: vp holds nb polyphase volumes, ip nb polyphase images
@@ -959,7 +988,7 @@ static int launch_fwd_b(sid_plan* p, int64_t n_in, int64_t n_in_pad, int64_t n_o
     const size_t sm = (size_t)NB * n_in_pad * sizeof(float2);
     SID_REQUIRE(sm <= 227 * 1024, "spectral projector: %d volumes of %lld channels exceed shared memory", NB,
                 (long long)n_in);
-    SID_CUDA_TRY(cudaFuncSetAttribute(k_spec_fwd_b<I16, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    SID_TRY(smem_attr((const void*)k_spec_fwd_b<I16, NB>, sm));
     k_spec_fwd_b<I16, NB><<<(unsigned)p->nf, 512, sm, st>>>(I16 ? p->khat_i16.as<uint4>() : p->khat_f32.as<uint4>(),
                                                            I16 ? p->rstep.as<float>() : nullptr, p->vhat.as<float2>(),
                                                            p->ihat.as<float2>(), (int)n_in, n_in_pad, (int)n_out,

@@ -151,18 +151,22 @@ k_adj_runs(const float* __restrict__ taps, const float* __restrict__ lat, float*
     }
 }
 
-// bp[volume][voxel of run, j] = sum over z < qs of the split partial sums (runs
-// [0, ncol) are column runs, the rest row runs)
+// bp[volume][voxel of run, j] = sum over z < qs of the split partial sums, for
+// the runs [lo1, hi1) and [lo2, hi2) (runs [0, ncol) are column runs, the rest
+// row runs)
 template <int JR>
 __global__ void k_runs_finish(const float* __restrict__ qpart, const WeakRun* __restrict__ runs, int nrun_all,
-                              int ncol, int qs, int nb, int Lx, int Ly, float* __restrict__ bp, int64_t bp_vol)
+                              int ncol, int qs, int nb, int Lx, int Ly, float* __restrict__ bp, int64_t bp_vol,
+                              int lo1, int hi1, int lo2, int hi2)
 {
-    const int64_t total = (int64_t)nb * nrun_all * JR;
+    const int n1 = hi1 - lo1, cnt = n1 + (hi2 - lo2);
+    const int64_t total = (int64_t)nb * cnt * JR;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
          i += (int64_t)gridDim.x * blockDim.x) {
         const int j = (int)(i % JR);
         const int64_t vr = i / JR;
-        const int rk = (int)(vr % nrun_all), vol = (int)(vr / nrun_all);
+        const int t = (int)(vr % cnt), vol = (int)(vr / cnt);
+        const int rk = t < n1 ? lo1 + t : lo2 + (t - n1);
         const WeakRun R = runs[rk];
         if (j >= R.len) continue;
         float s = 0.f;
@@ -336,6 +340,15 @@ int weak_build(sid_plan* p)
             vu.push_back({(int)((list[k] % plane) / Lx), (int)(list[k] % Lx)});
         plane_runs(pl, vu, (int)Lx, (int)Ly, cols, rows);
     }
+    // runs of depths [0, z): the runs come plane by plane, depth-major
+    p->weak_cz.assign((size_t)Z + 1, 0);
+    p->weak_rz.assign((size_t)Z + 1, 0);
+    for (const WeakRun& r : cols) ++p->weak_cz[(size_t)(r.plane / (N * N)) + 1];
+    for (const WeakRun& r : rows) ++p->weak_rz[(size_t)(r.plane / (N * N)) + 1];
+    for (int64_t z = 0; z < Z; ++z) {
+        p->weak_cz[(size_t)z + 1] += p->weak_cz[(size_t)z];
+        p->weak_rz[(size_t)z + 1] += p->weak_rz[(size_t)z];
+    }
     std::vector<WeakRun> all(cols);
     all.insert(all.end(), rows.begin(), rows.end());
     SID_TRY(p->weak.alloc(all.size() * sizeof(WeakRun)));
@@ -361,50 +374,97 @@ int weak_qsplit(const sid_plan* p, int64_t nb)
 
 // Overwrite the listed voxels of nb spectral back projections bp[b] = A' ip[b]
 // (polyphase volumes and images back to back) with their exact values.
-int weak_fix_n(sid_plan* p, const float* ip, float* bp, int nb, cudaStream_t st)
+struct WeakGeom {
+    int N, Lx, Ly, D, dlo, lo, Wp, Hp;
+    int64_t tbs, ni, nv, pv;
+};
+
+static WeakGeom weak_geom(const sid_plan* p)
+{
+    WeakGeom g;
+    g.N = (int)p->N; g.Lx = (int)p->Lx; g.Ly = (int)p->Ly; g.D = (int)p->g.D; g.dlo = (int)p->g.dlo;
+    g.lo = (int)std::max<int64_t>(0, -p->g.dlo);
+    const int hi = (int)std::max<int64_t>(0, p->g.D - 1 + p->g.dlo);
+    g.Wp = g.Lx + g.lo + hi;
+    g.Hp = g.Ly + g.lo + hi;
+    g.tbs = cdiv(p->N * p->g.D * p->g.D, 32) * 32;
+    g.ni = (int64_t)g.N * g.N * g.Lx * g.Ly;
+    g.nv = g.ni * p->Z;
+    g.pv = (int64_t)g.N * g.N * g.Wp * g.Hp;  // one volume's padded lattice copy
+    return g;
+}
+
+bool weak_runs_path(const sid_plan* p) { return p->nweak == 0 || p->g.D <= kRunDMax; }
+
+// Zero-padded (and transposed) copies of nb sensor lattices for the run kernel.
+int weak_pad(sid_plan* p, const float* ip, int nb, cudaStream_t st)
+{
+    if (p->nweak == 0) return SID_OK;
+    SID_REQUIRE(weak_runs_path(p), "weak voxels: the run kernel needs a tap extent of at most %d", kRunDMax);
+    const WeakGeom g = weak_geom(p);
+    SID_TRY(p->weak_pad.alloc((size_t)(2 * nb * g.pv) * sizeof(float)));
+    float* pad = p->weak_pad.as<float>();
+    k_pad_lattice<<<1024, 256, 0, st>>>(ip, pad, p->nweak_rows ? pad + nb * g.pv : nullptr, nb * g.N * g.N, g.Lx,
+                                        g.Ly, g.lo, g.Wp, g.Hp);
+    SID_CHECK_LAUNCH();
+    return SID_OK;
+}
+
+// The weak voxels of depths [z0, z1) of nb back projections, from the copies
+// of weak_pad.
+int weak_runs(sid_plan* p, float* bp, int nb, int64_t z0, int64_t z1, cudaStream_t st)
 {
     if (p->nweak == 0) return SID_OK;
     SID_REQUIRE(p->taps_f.p, "spectral plan: lenslet taps missing for the weak-voxel back projection");
-    const int64_t tbs = cdiv(p->N * p->g.D * p->g.D, 32) * 32;
-    const int N = (int)p->N, Lx = (int)p->Lx, Ly = (int)p->Ly, D = (int)p->g.D, dlo = (int)p->g.dlo;
-    const int64_t ni = (int64_t)N * N * Lx * Ly, nv = ni * p->Z;
-    if (p->g.D > kRunDMax) {
-        const unsigned grid = (unsigned)std::min<int64_t>(p->nweak, 152 * 8);
-        for (int b = 0; b < nb; ++b) {
-            k_adj_voxel<<<grid, kWeakThreads, 0, st>>>(p->taps_f.as<float>(), ip + b * ni, bp + b * nv,
-                                                       p->weak.as<int>(), (int)p->nweak, N, Lx, Ly, D, dlo, tbs);
-            SID_CHECK_LAUNCH();
-        }
-        return SID_OK;
-    }
-    const int lo = (int)std::max<int64_t>(0, -p->g.dlo), hi = (int)std::max<int64_t>(0, p->g.D - 1 + p->g.dlo);
-    const int Wp = Lx + lo + hi, Hp = Ly + lo + hi;
-    const int64_t pv = (int64_t)N * N * Wp * Hp;  // one volume's padded lattice copy
-    SID_TRY(p->weak_pad.alloc((size_t)(2 * nb * pv) * sizeof(float)));
-    float* pad = p->weak_pad.as<float>();
-    float* padT = pad + nb * pv;
-    k_pad_lattice<<<1024, 256, 0, st>>>(ip, pad, p->nweak_rows ? padT : nullptr, nb * N * N, Lx, Ly, lo, Wp, Hp);
-    SID_CHECK_LAUNCH();
+    const WeakGeom g = weak_geom(p);
+    const float* pad = p->weak_pad.as<float>();
+    const float* padT = pad + nb * g.pv;
     const WeakRun* runs = p->weak.as<WeakRun>();
     const float* taps = p->taps_f.as<float>();
-    const int nc = (int)p->nweak_cols, nr = (int)p->nweak_rows, nall = nc + nr;
+    const int nc = (int)p->nweak_cols, nall = nc + (int)p->nweak_rows;
+    const int c0 = p->weak_cz[(size_t)z0], c1 = p->weak_cz[(size_t)z1];
+    const int r0 = p->weak_rz[(size_t)z0], r1 = p->weak_rz[(size_t)z1];
+    if (c1 == c0 && r1 == r0) return SID_OK;
     const int qs = weak_qsplit(p, nb);
     float* qpart = nullptr;
     if (qs > 1) {
         SID_TRY(p->weak_part.alloc((size_t)qs * nb * nall * kRunMax * sizeof(float)));
         qpart = p->weak_part.as<float>();
     }
-    if (nc) SID_TRY(launch_runs<false>(D, dim3((unsigned)nc, (unsigned)nb, (unsigned)qs), taps, pad, bp, runs, nc, N, Lx,
-                                      Ly, dlo, lo, Wp, Hp, tbs, pv, nv, qpart, 0, nall, st));
-    if (nr) SID_TRY(launch_runs<true>(D, dim3((unsigned)nr, (unsigned)nb, (unsigned)qs), taps, padT, bp, runs + nc, nr, N,
-                                     Lx, Ly, dlo, lo, Wp, Hp, tbs, pv, nv, qpart, nc, nall, st));
+    if (c1 > c0)
+        SID_TRY(launch_runs<false>(g.D, dim3((unsigned)(c1 - c0), (unsigned)nb, (unsigned)qs), taps, pad, bp,
+                                   runs + c0, c1 - c0, g.N, g.Lx, g.Ly, g.dlo, g.lo, g.Wp, g.Hp, g.tbs, g.pv, g.nv,
+                                   qpart, c0, nall, st));
+    if (r1 > r0)
+        SID_TRY(launch_runs<true>(g.D, dim3((unsigned)(r1 - r0), (unsigned)nb, (unsigned)qs), taps, padT, bp,
+                                  runs + nc + r0, r1 - r0, g.N, g.Lx, g.Ly, g.dlo, g.lo, g.Wp, g.Hp, g.tbs, g.pv,
+                                  g.nv, qpart, nc + r0, nall, st));
     if (qs > 1) {
-        const int64_t tot = (int64_t)nb * nall * kRunMax;
+        const int64_t tot = (int64_t)nb * ((c1 - c0) + (r1 - r0)) * kRunMax;
         k_runs_finish<kRunMax><<<(unsigned)std::min<int64_t>(cdiv(tot, 256), 4096), 256, 0, st>>>(
-            qpart, runs, nall, nc, qs, nb, Lx, Ly, bp, nv);
+            qpart, runs, nall, nc, qs, nb, g.Lx, g.Ly, bp, g.nv, c0, c1, nc + r0, nc + r1);
         SID_CHECK_LAUNCH();
     }
     return SID_OK;
+}
+
+int weak_fix_n(sid_plan* p, const float* ip, float* bp, int nb, cudaStream_t st)
+{
+    if (p->nweak == 0) return SID_OK;
+    SID_REQUIRE(p->taps_f.p, "spectral plan: lenslet taps missing for the weak-voxel back projection");
+    if (!weak_runs_path(p)) {
+        const WeakGeom g = weak_geom(p);
+        const unsigned grid = (unsigned)std::min<int64_t>(p->nweak, 152 * 8);
+        for (int b = 0; b < nb; ++b) {
+            k_adj_voxel<<<grid, kWeakThreads, 0, st>>>(p->taps_f.as<float>(), ip + b * g.ni, bp + b * g.nv,
+                                                       p->weak.as<int>(), (int)p->nweak, g.N, g.Lx, g.Ly, g.D, g.dlo,
+                                                       g.tbs);
+            SID_CHECK_LAUNCH();
+        }
+        return SID_OK;
+    }
+    SID_TRY(weak_pad(p, ip, nb, st));
+    return weak_runs(p, bp, nb, 0, p->Z, st);
 }
 
 int weak_fix(sid_plan* p, const float* ip, float* bp, cudaStream_t st) { return weak_fix_n(p, ip, bp, 1, st); }
