@@ -418,11 +418,7 @@ static int launch_fwd(sid_plan* p, const float* vp, float* parts, int zsplit, in
 {
     constexpr int WQ = R + D - 1, WR = 32 + D - 1;
     const size_t smem = (size_t)(2 * tbs + 2 * WQ * WR) * sizeof(float);
-    static bool configured = false;
-    if (!configured) {
-        SID_CUDA_TRY(cudaFuncSetAttribute(k_fwd_direct<R, D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        configured = true;
-    }
+    SID_TRY(smem_attr((const void*)k_fwd_direct<R, D>, smem));  // smem depends on the plan's Nnum
     dim3 grid((unsigned)cdiv(p->Lx, 32), (unsigned)cdiv(p->Ly, R), (unsigned)(p->N * zsplit));
     const int64_t part_stride = p->N * p->N * p->Ly * p->Lx;
     p->timer.begin(st);
@@ -439,11 +435,7 @@ static int launch_adj(sid_plan* p, const float* ip, float* bp, int64_t tbs, int*
 {
     constexpr int WQ = R + D - 1, WR = 32 + D - 1;
     const size_t smem = (size_t)(2 * tbs + 2 * WQ * WR) * sizeof(float);
-    static bool configured = false;
-    if (!configured) {
-        SID_CUDA_TRY(cudaFuncSetAttribute(k_adj_direct<R, D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        configured = true;
-    }
+    SID_TRY(smem_attr((const void*)k_adj_direct<R, D>, smem));
     dim3 grid((unsigned)cdiv(p->Lx, 32), (unsigned)cdiv(p->Ly, R), (unsigned)(p->N * p->Z));
     p->timer.begin(st);
     k_adj_direct<R, D><<<grid, (unsigned)(32 * p->N), smem, st>>>(

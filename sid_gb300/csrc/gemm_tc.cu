@@ -294,11 +294,7 @@ static int launch_gemm(const GemmMaps& maps, int npass, int m, int n, int nkb, i
                        cudaStream_t st)
 {
     using SM = GemmSmem<BN, STAGES>;
-    static bool configured = false;
-    if (!configured) {
-        SID_CUDA_TRY(cudaFuncSetAttribute(k_gemm_tc<BN, STAGES>, cudaFuncAttributeMaxDynamicSharedMemorySize, SM::TOTAL));
-        configured = true;
-    }
+    SID_TRY(smem_attr((const void*)k_gemm_tc<BN, STAGES>, SM::TOTAL));
     const int kb_per = (int)cdiv(nkb, splitk);
     dim3 grid((unsigned)cdiv(m, GEMM_BM), (unsigned)cdiv(n, BN), (unsigned)splitk);
     k_gemm_tc<BN, STAGES><<<grid, GEMM_THREADS, SM::TOTAL, st>>>(maps, npass, m, n, nkb, kb_per, bf16 ? 1 : 0, out, ldc,

@@ -472,12 +472,7 @@ static int launch_spec_tc(const SpecTcMaps& maps, int rows, int nkb, int akb0, i
                           int* err, cudaStream_t st)
 {
     using SM = SpecTcSmem<BN, STAGES, NBP>;
-    static bool configured = false;
-    if (!configured) {
-        SID_CUDA_TRY(cudaFuncSetAttribute(k_spec_tc<BN, STAGES, NBP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          SM::TOTAL));
-        configured = true;
-    }
+    SID_TRY(smem_attr((const void*)k_spec_tc<BN, STAGES, NBP>, SM::TOTAL));
     const int nmt = (int)cdiv(rows, TC_BM);
     const int64_t nitems = (int64_t)nmt * nf;
     const unsigned grid = (unsigned)std::min<int64_t>(nitems, sm_count());
