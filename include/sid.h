@@ -268,6 +268,11 @@ int sid_ctx_sync(sid_ctx* ctx, void* stream);
  * enable, run, then read the total and the number of timed calls (read resets). */
 int sid_ctx_timing_enable(sid_ctx* ctx, int on);
 int sid_ctx_timing_read(sid_ctx* ctx, double* total_ms, int64_t* launches);
+/* The tensor-core GEMM's tile plan (host only; the project's autotuner): for
+ * C (m x n) = A'B with a k-deep reduction (symmetric: A'A, tiles on and above
+ * the diagonal) on `sms` SMs, the tile width bn (256, 192, 128 or 64 columns
+ * of 128-row tiles) and the number of K splits the contractions use. */
+int sid_gemm_tile_plan(int64_t m, int64_t n, int64_t k, int symmetric, int sms, int* bn, int* splitk);
 
 /* Precision of the contractions. */
 #define SID_PREC_FP32  0 /* FP32 SIMT: the plain path */

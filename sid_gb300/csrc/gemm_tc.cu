@@ -329,9 +329,8 @@ static int64_t gemm_tiles(int m, int n, int bn, bool sym)
 // best.  A symmetric product counts only the tiles it computes (the 800-wide
 // Gram: 19 tiles of 256 columns hold 1.95x the triangle's outputs, 28 of 128
 // columns 1.43x).
-static void gemm_autotune_impl(int m, int n, int nkb, bool sym, int* bn, int* splitk)
+static void gemm_autotune_sms(int m, int n, int nkb, bool sym, int sms, int* bn, int* splitk)
 {
-    const int sms = sm_count();
     const int cands[4] = {256, 192, 128, 64};
     // measured on the 800-wide Gram at P = 1,010,025 (of the MMA work each width computes):
     // 256 at 99 % of the BF16 peak, 192 at 77 %, 128 at 53 %
@@ -357,6 +356,11 @@ static void gemm_autotune_impl(int m, int n, int nkb, bool sym, int* bn, int* sp
     }
     *bn = bbn;
     *splitk = bs;
+}
+
+static void gemm_autotune_impl(int m, int n, int nkb, bool sym, int* bn, int* splitk)
+{
+    gemm_autotune_sms(m, n, nkb, sym, sm_count(), bn, splitk);
 }
 
 void gemm_autotune(int m, int n, int nkb, int* bn, int* splitk) { gemm_autotune_impl(m, n, nkb, false, bn, splitk); }
@@ -448,3 +452,13 @@ int gemm_tn_sym(const void* const* A, const void* const* B, int npass, int64_t m
 }
 
 }  // namespace sid
+
+extern "C" int sid_gemm_tile_plan(int64_t m, int64_t n, int64_t k, int symmetric, int sms, int* bn, int* splitk)
+{
+    SID_REQUIRE(bn && splitk, "sid_gemm_tile_plan: NULL output");
+    SID_REQUIRE(m > 0 && n > 0 && k > 0 && sms > 0 && m <= INT32_MAX && n <= INT32_MAX,
+                "sid_gemm_tile_plan: bad sizes");
+    SID_REQUIRE(!symmetric || m == n, "sid_gemm_tile_plan: a symmetric product needs m == n");
+    sid::gemm_autotune_sms((int)m, (int)n, (int)sid::cdiv(k, sid::GEMM_BK), symmetric != 0, sms, bn, splitk);
+    return SID_OK;
+}
