@@ -9,7 +9,6 @@
 #include <climits>
 #include <cstdarg>
 #include <cstring>
-#include <map>
 #include <mutex>
 #include <vector>
 
@@ -110,16 +109,7 @@ static int build_taps(sid_plan* p, const float* dH, const std::vector<int>& lo,
 
 int smem_attr(const void* func, size_t bytes)
 {
-    static std::mutex mu;
-    static std::map<std::pair<int, const void*>, size_t> set;
-    int dev = 0;
-    SID_CUDA_TRY(cudaGetDevice(&dev));
-    std::lock_guard<std::mutex> lock(mu);
-    size_t& cur = set[std::make_pair(dev, func)];
-    if (bytes > cur) {
-        SID_CUDA_TRY(cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
-        cur = bytes;
-    }
+    SID_CUDA_TRY(cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
     return SID_OK;
 }
 

@@ -57,10 +57,11 @@ inline int64_t cdiv(int64_t a, int64_t b) { return (a + b - 1) / b; }
 // Streaming multiprocessors of the current device (cudaDevAttrMultiProcessorCount,
 // looked up once per device ordinal; 152 on GB300).
 int sm_count();
-// cudaFuncSetAttribute(func, MaxDynamicSharedMemorySize, bytes) only when the
-// current device's setting for func is below bytes (kept per device and
-// function): the call costs host time, and a launch sequence of many small
-// kernels paid it on every launch.
+// cudaFuncSetAttribute(func, MaxDynamicSharedMemorySize, bytes) for the launch
+// that follows.  Set on every launch, not once per process: the setting
+// belongs to the current context and device (a device reset, as MATLAB's
+// reset(gpuDevice) does, or a second device starts from the default), and the
+// size can grow with the plan (the direct kernels' tap tiles with Nnum).
 int smem_attr(const void* func, size_t bytes);
 // The power of two that brings a largest magnitude amax into [2^13, 2^14)
 // (1 for a zero or non-finite amax): the scale of an FP16 hi/lo split.
