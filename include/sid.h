@@ -100,6 +100,13 @@ int sid_plan_info(const sid_plan* plan, int64_t* info);
  * FFT-based values carry only absolute accuracy, which the multiplicative
  * solvers' divisions by A'(.) amplify.  Rebuilds the list (synchronous). */
 int sid_plan_set_weak_fraction(sid_plan* plan, double frac);
+/* The runs the weakly observed voxels are recomputed in (host only): for a
+ * strictly ascending list of polyphase voxel indices (plane (c N + b) N + a,
+ * then v, then u), runs[4r..4r+3] = plane, fixed coordinate, first voxel and
+ * length (<= 24) of run r: column runs (fixed u, v = first..) plane by plane,
+ * then row runs (fixed v, u = first..); every voxel lies in exactly one run. */
+int sid_weak_runs_plan(const int32_t* list, int64_t n, int64_t N, int64_t Lx, int64_t Ly, int32_t* runs, int64_t cap,
+                       int64_t* ncols, int64_t* nrows);
 
 /* TOTALprojection = forwardProjectGPU(H, realspace)   forwardProjectGPU.m:1
  *                 = forwardProjectACC(H, realspace, CAindex)  forwardProjectACC.m:1

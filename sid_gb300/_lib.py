@@ -91,6 +91,7 @@ SIGNATURES = {
     "sid_library_spectral": [P, P, I64, P, P, I64, I64, F64, P, I32, P],
     "sid_ctx_timing_enable": [P, I32],
     "sid_gemm_tile_plan": [I64, I64, I64, I32, I32, P, P],
+    "sid_weak_runs_plan": [P, I64, I64, I64, I64, P, I64, P, P],
     "sid_ctx_timing_read": [P, P, P],
     "sid_library_kernel": [P, I32, P, I64, F64, F64, P, I64, I64, I64, P, I32, P],
     "sid_library_kernel_voxels": [P, I64, F64, F64, P, I64, I64, I64, I64, I64, I64, P, P, P, I64],

@@ -481,3 +481,39 @@ extern "C" int sid_plan_set_weak_fraction(sid_plan* p, double frac)
     p->weak_frac = frac;
     return weak_build(p);
 }
+
+extern "C" int sid_weak_runs_plan(const int32_t* list, int64_t n, int64_t N, int64_t Lx, int64_t Ly, int32_t* runs,
+                                  int64_t cap, int64_t* ncols, int64_t* nrows)
+{
+    SID_REQUIRE((list || n == 0) && ncols && nrows && N >= 1 && Lx >= 1 && Ly >= 1, "sid_weak_runs_plan: bad argument");
+    const int64_t plane = Lx * Ly;
+    for (int64_t k = 1; k < n; ++k)
+        SID_REQUIRE(list[k] > list[k - 1], "sid_weak_runs_plan: voxel list not strictly ascending at %lld",
+                    (long long)k);
+    // the grouping of weak_build: plane by plane, each plane's voxels into column and row runs
+    std::vector<WeakRun> cols, rows;
+    for (int64_t k = 0; k < n;) {
+        const int pl = (int)(list[k] / plane);
+        std::vector<std::pair<int, int>> vu;
+        for (; k < n && list[k] / plane == pl; ++k)
+            vu.push_back({(int)((list[k] % plane) / Lx), (int)(list[k] % Lx)});
+        plane_runs(pl, vu, (int)Lx, (int)Ly, cols, rows);
+    }
+    *ncols = (int64_t)cols.size();
+    *nrows = (int64_t)rows.size();
+    const int64_t total = *ncols + *nrows;
+    if (runs) {
+        SID_REQUIRE(total <= cap, "sid_weak_runs_plan: %lld runs exceed the capacity %lld", (long long)total,
+                    (long long)cap);
+        int64_t at = 0;
+        for (const std::vector<WeakRun>* v : {&cols, &rows})
+            for (const WeakRun& r : *v) {
+                runs[4 * at] = r.plane;
+                runs[4 * at + 1] = r.fixed;
+                runs[4 * at + 2] = r.start;
+                runs[4 * at + 3] = r.len;
+                ++at;
+            }
+    }
+    return SID_OK;
+}
