@@ -720,7 +720,10 @@ extern "C" int sid_library_kernel(sid_plan* p, int method, const double* centers
     SID_REQUIRE(method == SID_METHOD_DIRECT || method == SID_METHOD_SPECTRAL_MIXED,
                 "%s: method must be SID_METHOD_DIRECT or SID_METHOD_SPECTRAL_MIXED", who);
     // the centred paste of project_forward_patched.m:63-72 matches the frame's 'same' projection for odd Nnum
+    // and odd PSF width; with an even width its index range runs past the projection (MATLAB stops there)
     SID_REQUIRE(p->N % 2 == 1, "%s: the patch projection's centring needs an odd Nnum", who);
+    SID_REQUIRE(p->M % 2 == 1, "%s: the patch projection's paste needs an odd PSF width (M = %lld)", who,
+                (long long)p->M);
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     KernelShape ks;
     SID_TRY(kernel_shape(who, r, dim_z, kernel, kx, ky, kz, ks));

@@ -166,3 +166,39 @@ def test_library_cpu_form_matches_oracle(gpu, oracle, method, bar, case):
     cols = s.to_numpy(s.generate_LFM_library_CPU(c, {"H": H}, r, dim, (X, X, Z), kernel=W, method=method,
                                                  layout="columns"))
     np.testing.assert_array_equal(cols, got.T)
+
+
+@pytest.mark.parametrize("M", [21, 23])
+def test_patch_projection_equals_frame_projection(oracle, M):
+    """project_forward_patched.m's patch (an odd number of lenslets, conv2
+    'full', pasted centred and clipped) equals the frame's conv2 'same'
+    projection of the painted volume for odd Nnum and odd PSF width: the
+    identity the library's CPU-twin form rests on (FP64, CPU).  With an even
+    width the paste's index range runs one past the projection (MATLAB stops
+    with an index error; so does the oracle)."""
+    from sid_gb300 import synthetic
+    N, Z = 5, 4
+    X = N * 8
+    H = synthetic.gaussian_psf(M, N, Z, sigma_min=1.0, sigma_max=3.0)
+    rng = np.random.default_rng(4)
+    c = np.stack([rng.uniform(1, X, 6), rng.uniform(1, X, 6), rng.uniform(1, Z, 6)], 1)
+    c[0] = [1.0, 1.0, 1.0]
+    c[1] = [X - 0.3, 3.5, Z]
+    rows = oracle.generate_library_cpu(c, H, 3, [1, 1, 1.5], (X, X))
+    for n, (vox, vals) in enumerate(oracle.library_kernel_voxels(c, 3, [1, 1, 1.5], (X, X), Z)):
+        V = np.zeros((X, X, Z), order="F")
+        V[vox[:, 0], vox[:, 1], vox[:, 2]] = vals
+        ref = oracle.forward_project(H, V).ravel(order="F")
+        ref = ref / np.linalg.norm(ref)
+        np.testing.assert_allclose(rows[n], ref, rtol=0, atol=1e-12)
+
+
+def test_patch_projection_even_width_fails_like_the_reference(oracle):
+    """An even PSF width makes the 'full' projection even, and the centred
+    paste's range for a neuron away from the sensor's far edges one pixel
+    longer than it (project_forward_patched.m:63-72): an index error."""
+    from sid_gb300 import synthetic
+    N, Z, X = 5, 2, 80
+    H = synthetic.gaussian_psf(22, N, Z, sigma_min=1.0, sigma_max=2.0)
+    with pytest.raises(ValueError):
+        oracle.generate_library_cpu(np.array([[40.0, 40.0, 1.0]]), H, 3, [1, 1, 1.0], (X, X))
