@@ -41,7 +41,7 @@ def parse():
     ap.add_argument("--compare", default="direct,spectral_f32",
                     help="other methods timed after the main region (comma list, '' for none)")
     ap.add_argument("--compare-steps", type=int, default=3)
-    ap.add_argument("--config", default="cfg1", choices=["cfg0", "cfg1"])
+    ap.add_argument("--config", default="1005x1005x31", choices=["225x225x11", "1005x1005x31"])
     ap.add_argument("--depths", type=int, default=0,
                     help="keep only the first Z depth planes (a smaller case of the same lateral geometry, for "
                          "profiling captures; the line then names the reduced workload)")
@@ -83,9 +83,9 @@ def replica_throughput(ms, steps, world, device):
     return ms, world * steps / (ms / 1e3)
 
 
-def workload_name(config, X, Y, Z, N, M):
+def workload_name(X, Y, Z, N, M):
     """The workload string both arms print (the same ISRA step on the same data)."""
-    return f"{config}: ISRA iteration on {X}x{Y}x{Z}, Nnum {N}, PSF {M}^2x{N}^2x{Z}"
+    return f"ISRA iteration on {X}x{Y}x{Z}, Nnum {N}, PSF {M}^2x{N}^2x{Z}"
 
 
 def workload(config, depths=0):
@@ -292,7 +292,7 @@ def nnls_workload(args, P_proj):
     P = P_proj.X * P_proj.Y
     A, Y16, Yf, T, lib_ms = nnls_inputs(P_proj, K, F)
     ctx = s.Context()
-    out = {"workload": f"library {K} neurons (cfg2) + temporal NNLS {K} x {F} frames, P = {P} (cfg3), FP16 movie"}
+    out = {"workload": f"library {K} neurons + temporal NNLS {K} x {F} frames, P = {P}, FP16 movie"}
     direct, spec = lib_ms["sid_library"], lib_ms["sid_library_spectral"]
     out["library_ms"] = direct["ms"]
     out["library_neurons_per_s"] = K / (direct["ms"] / 1e3)
@@ -616,7 +616,7 @@ def run_reference(args):
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_iter * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": workload_name(args.config, V.shape[0], V.shape[1], V.shape[2], H.shape[2],
+            "config": {"workload": workload_name(V.shape[0], V.shape[1], V.shape[2], H.shape[2],
                                                  H.shape[0]),
                        "parallelism": "host cores (OpenMP)"},
             "extrapolated": True,
@@ -892,7 +892,7 @@ def main():
                                            "spectral_mixed_f32": "f32 (16-bit forward / FP32 back-projection spectra)"}
             .get(args.method, "f32"),
             "data": "synthetic (seeded Gaussian PSF + blob volume, shapes of the 1005^2x31 configuration)",
-            "config": {"workload": workload_name(args.config, X, Y, Z, info["Nnum"], info["M"]),
+            "config": {"workload": workload_name(X, Y, Z, info["Nnum"], info["M"]),
                        "method": args.method, "parallelism": "replicas" if world > 1 else "1 GPU",
                        "l2": "per-iteration working set (tap spectra streamed once per projection, "
                              f"{ws_gb:.1f} GB per iteration) "

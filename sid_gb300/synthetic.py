@@ -18,8 +18,8 @@ import numpy as np
 
 CONFIGS = {
     # Nnum, lenslets per side, depth planes, PSF side
-    "cfg0": dict(Nnum=15, lenslets=15, Z=11, M=195),
-    "cfg1": dict(Nnum=15, lenslets=67, Z=31, M=345),
+    "225x225x11": dict(Nnum=15, lenslets=15, Z=11, M=195),
+    "1005x1005x31": dict(Nnum=15, lenslets=67, Z=31, M=345),
 }
 
 
@@ -67,12 +67,13 @@ def blob_volume(X: int, Y: int, Z: int, n_blobs: int, sigma=(2.0, 2.0), amp="uni
 
 
 def config_inputs(name: str, seed_psf=0, seed_vol=1):
-    """(H, V) for cfg0 (40 blobs, sigma 2, U(0.5,2) amplitudes) or cfg1 (2000
-    blobs, sigma U(2,4), log-normal amplitudes)."""
+    """(H, V) for the 225 x 225 x 11 frame (40 blobs, sigma 2, U(0.5,2)
+    amplitudes) or the 1005 x 1005 x 31 frame (2000 blobs, sigma U(2,4),
+    log-normal amplitudes)."""
     c = CONFIGS[name]
     X = c["Nnum"] * c["lenslets"]
     H = gaussian_psf(c["M"], c["Nnum"], c["Z"], seed=seed_psf)
-    if name == "cfg0":
+    if name == "225x225x11":
         V = blob_volume(X, X, c["Z"], 40, sigma=(2.0, 2.0), amp="uniform", seed=seed_vol)
     else:
         V = blob_volume(X, X, c["Z"], 2000, sigma=(2.0, 4.0), amp="lognormal", seed=seed_vol)

@@ -33,7 +33,7 @@ def test_isra_matches_oracle(small, method, tol):
     assert rel_l2(out, ref) < 10 * tol, rel_l2(out, ref)
 
 
-def test_isra_cfg0_mixed_vs_fp64(gpu, oracle):
+def test_isra_frame225_mixed_vs_fp64(gpu, oracle):
     """8 ISRA iterations on the 225 x 225 x 11 configuration (Nnum 15, PSF 195):
     the mixed-precision spectral forms (16-bit forward; 24-bit float or FP32
     back projection) against the FP64 oracle, bar 1e-4.  (16-bit block-float
@@ -42,7 +42,7 @@ def test_isra_cfg0_mixed_vs_fp64(gpu, oracle):
     sensor have tiny back projections, and the division diverges.)"""
     import sid_gb300 as s
     from sid_gb300 import synthetic
-    H, V = synthetic.config_inputs("cfg0")
+    H, V = synthetic.config_inputs("225x225x11")
     y = oracle.forward_project(H, V)
     fwd = lambda v: oracle.forward_project(H, v)  # noqa: E731
     bwd = lambda i: oracle.backward_project(H, i)  # noqa: E731

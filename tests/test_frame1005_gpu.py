@@ -22,11 +22,11 @@ TOL = {"direct": 1e-5, "spectral_f32": 1e-5, "spectral_mixed": 1e-4, "spectral_m
 
 
 @pytest.fixture(scope="module")
-def cfg1(gpu):
+def frame1005(gpu):
     import torch
     import sid_gb300 as s
     from sid_gb300 import synthetic
-    H, V = synthetic.config_inputs("cfg1")
+    H, V = synthetic.config_inputs("1005x1005x31")
     P = s.Projector(H, V.shape[:2], None, methods=("direct", "spectral_f32", "spectral_mixed"))
     y = synthetic.poisson_image(s.to_numpy(P.forward(V, method="spectral_f32")))
     yield H, V, y, P
@@ -34,9 +34,9 @@ def cfg1(gpu):
     torch.cuda.empty_cache()
 
 
-def test_cfg1_dot_product_16_pairs(cfg1):
+def test_frame1005_dot_product_16_pairs(frame1005):
     import torch
-    H, V, y, P = cfg1
+    H, V, y, P = frame1005
     X, Y, Z = V.shape
     g = torch.Generator(device="cuda").manual_seed(11)
     x = torch.empty((Z, Y, X), device="cuda").permute(2, 1, 0)
@@ -53,10 +53,10 @@ def test_cfg1_dot_product_16_pairs(cfg1):
 
 
 @pytest.mark.parametrize("objective", ["poisson", "ls"])
-def test_cfg1_finite_differences_64_voxels(cfg1, objective):
+def test_frame1005_finite_differences_64_voxels(frame1005, objective):
     import torch
     import sid_gb300 as s
-    H, V, y, P = cfg1
+    H, V, y, P = frame1005
     X, Y, Z = V.shape
     # a point away from the solution, so that the gradients are O(1)
     x = np.asfortranarray((0.5 * V + 0.5 * V.mean()).astype(np.float32))
@@ -82,9 +82,9 @@ def test_cfg1_finite_differences_64_voxels(cfg1, objective):
     torch.cuda.synchronize()
 
 
-def test_cfg1_projections_vs_fp64_sampled(cfg1, oracle):
+def test_frame1005_projections_vs_fp64_sampled(frame1005, oracle):
     import sid_gb300 as s
-    H, V, y, P = cfg1
+    H, V, y, P = frame1005
     X, Y, Z = V.shape
     rng = np.random.default_rng(7)
     pix = np.stack([rng.integers(0, X, 256), rng.integers(0, Y, 256)], axis=1)
@@ -98,14 +98,14 @@ def test_cfg1_projections_vs_fp64_sampled(cfg1, oracle):
         assert rel_l2(b, ref_b) < TOL[m], (m, rel_l2(b, ref_b))
 
 
-def test_cfg1_weak_voxels_exact(cfg1):
+def test_frame1005_weak_voxels_exact(frame1005):
     """Voxels whose PSF falls mostly off the sensor (column mass A'1 below 1e-2
     of the largest) get exact back projections from every spectral
     form: per entry within 1e-5 of the direct path, where an FFT-based value
     alone has no correct digits."""
     import torch
     import sid_gb300 as s
-    H, V, y, P = cfg1
+    H, V, y, P = frame1005
     nweak = P.info()["weak_voxels"]
     assert nweak > 0
     ones = torch.ones((V.shape[1], V.shape[0]), device="cuda").t()
@@ -119,12 +119,12 @@ def test_cfg1_weak_voxels_exact(cfg1):
         assert err < 1e-5, (m, err)
 
 
-def test_cfg1_isra_30_iterations(cfg1):
+def test_frame1005_isra_30_iterations(frame1005):
     """30 ISRA iterations from Htf = A'y: the mixed-precision and FP32 spectral
     forms against the FP32 direct path (itself within 1e-5 of FP64 per
     projection)."""
     import sid_gb300 as s
-    H, V, y, P = cfg1
+    H, V, y, P = frame1005
     Htf = P.adjoint(y, method="direct")
     ref = s.to_numpy(P.isra(Htf, Htf, 30, method="direct"))
     for m in ("spectral_f32", "spectral_mixed", "spectral_mixed_f32"):
@@ -132,13 +132,13 @@ def test_cfg1_isra_30_iterations(cfg1):
         assert rel_l2(out, ref) < TOL[m], (m, rel_l2(out, ref))
 
 
-def test_cfg1_rl_poisson_30_iterations(cfg1):
+def test_frame1005_rl_poisson_30_iterations(frame1005):
     """30 Poisson-RL iterations, spectral forms against the FP32 direct path,
     bar 1e-4: the ratio y ./ AX makes this iteration more sensitive than ISRA,
     and two FP32 forms that agree to ~1e-7 per projection end ~2e-5 apart
     whatever the weak-voxel threshold."""
     import sid_gb300 as s
-    H, V, y, P = cfg1
+    H, V, y, P = frame1005
     X0 = P.adjoint(y, method="direct")
     ref = s.to_numpy(P.rl_poisson(y, X0, 30, method="direct"))
     for m in ("spectral_f32", "spectral_mixed"):
@@ -148,7 +148,7 @@ def test_cfg1_rl_poisson_30_iterations(cfg1):
 
 # FP32 lenslet taps; tensor-core windows (24-bit window spectra, two-part box spectra)
 @pytest.mark.parametrize("fn,bar", [("sid_library", 1e-5), ("sid_library_spectral", 3e-5)])
-def test_cfg2_library_sampled_pixels(cfg1, fn, bar):
+def test_library_800_neurons_sampled_pixels(frame1005, fn, bar):
     """Library generation at the 800-neuron size (generate_LFM_library_GPU.m:
     63-109: neur_rad 12, axial 2, one component): 20 neurons' rows against an
     FP64 restatement at 500 sampled pixels each inside their sensor footprints,
@@ -159,7 +159,7 @@ def test_cfg2_library_sampled_pixels(cfg1, fn, bar):
     import torch
     import sid_gb300 as s
     from sid_gb300 import _lib, synthetic
-    H, V, y, P = cfg1
+    H, V, y, P = frame1005
     X, Y, Z = V.shape
     M, N = H.shape[0], H.shape[2]
     cf = M // 2

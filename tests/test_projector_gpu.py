@@ -60,18 +60,18 @@ def test_even_width_follows_reference_centring(gpu, oracle):
 
 
 @pytest.fixture(scope="module")
-def cfg0(gpu):
+def frame225(gpu):
     from sid_gb300 import Projector, synthetic
-    H, V = synthetic.config_inputs("cfg0")
+    H, V = synthetic.config_inputs("225x225x11")
     P = Projector(H, V.shape[:2], None, methods=ALL)
     return H, V, P
 
 
 @pytest.mark.parametrize("method", ALL)
-def test_cfg0_forward_adjoint_vs_oracle(cfg0, oracle, method):
-    """Full cfg0 geometry (Nnum 15, 225 x 225 x 11, PSF 195): specialised D=15 kernels."""
+def test_frame225_forward_adjoint_vs_oracle(frame225, oracle, method):
+    """Full 225 x 225 x 11 geometry (Nnum 15, 225 x 225 x 11, PSF 195): specialised D=15 kernels."""
     from sid_gb300 import to_numpy
-    H, V, P = cfg0
+    H, V, P = frame225
     ref_f = oracle.forward_project(H, V)
     f = to_numpy(P.forward(V, method=method))
     assert rel_l2(f, ref_f) < TOL[method], rel_l2(f, ref_f)
@@ -82,11 +82,11 @@ def test_cfg0_forward_adjoint_vs_oracle(cfg0, oracle, method):
 
 
 @pytest.mark.parametrize("method", ALL)
-def test_dot_product_adjoint(cfg0, method):
+def test_dot_product_adjoint(frame225, method):
     """<A x, y> == <x, A^T y> on random pairs, in FP32 on the GPU."""
     import torch
     from sid_gb300.lfm import _fortran_tensor
-    H, V, P = cfg0
+    H, V, P = frame225
     g = torch.Generator(device="cuda").manual_seed(11)
     for _ in range(4):
         x = _fortran_tensor((P.X, P.Y, P.Z), "cuda")
@@ -100,9 +100,9 @@ def test_dot_product_adjoint(cfg0, method):
         assert abs(lhs - rhs) / abs(lhs) < (1e-5 if method in ("direct", "spectral_f32") else 1e-4)
 
 
-def test_host_entry_points_match_device(cfg0):
+def test_host_entry_points_match_device(frame225):
     from sid_gb300 import to_numpy
-    H, V, P = cfg0
+    H, V, P = frame225
     f_dev = to_numpy(P.forward(V))
     f_host = P.forward_host(V)
     np.testing.assert_array_equal(f_dev, f_host)
