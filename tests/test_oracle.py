@@ -57,6 +57,23 @@ def test_sampled_pixels_match_full(oracle):
                                rtol=1e-14)
 
 
+@pytest.mark.parametrize("M,N", [(11, 3), (10, 5)])
+def test_cpu_baseline_computes_the_forward_projection(oracle, M, N):
+    """The timed CPU baseline (FP32 lenslet-sparse loop) is the forward
+    projection: equal to the FP64 oracle to FP32 rounding over all columns, and
+    a column range [y0, y1) gives exactly those columns of the whole result."""
+    rng = np.random.default_rng(M + N)
+    Z, X, Y = 3, 4 * N + 2, 3 * N + 1
+    H = rng.random((M, M, N, N, Z)).astype(np.float32)
+    V = (rng.random((X, Y, Z)) * (rng.random((X, Y, Z)) < 0.3)).astype(np.float32)
+    full = oracle.baseline_forward_f32(H, V, nthreads=2)
+    assert rel_l2(full, oracle.forward_project(H, V)) < 1e-6
+    y0, y1 = 2, Y - 3
+    part = oracle.baseline_forward_f32(H, V, y0, y1, nthreads=1)
+    np.testing.assert_array_equal(part[:, y0:y1], full[:, y0:y1])
+    assert not part[:, :y0].any() and not part[:, y1:].any()
+
+
 def test_matlab_quantile(oracle):
     rng = np.random.default_rng(0)
     v = rng.random(1001)
