@@ -4,8 +4,10 @@ volume (Nnum 15, 67 x 67 lenslets, PSF 345 x 345 x 15 x 15 x 31), one GPU.
 A step is one ISRA iteration (deconvRL.m:46-87): one forward projection, one
 back projection and the fused multiplicative update, computed by libsid with
 the method chosen by --method (default: the mixed-precision spectral form,
-tap spectra stored as 16-bit block floating point, FP32 arithmetic).  Inputs are seeded synthetic
-data with the shapes of the benchmark configuration.
+forward tap spectra stored as 16-bit block floating point, back projection
+tap spectra as 24-bit floats with the weakly observed voxels recomputed from
+the FP32 taps, FP32 arithmetic).  Inputs are seeded synthetic data with the
+shapes of the benchmark configuration.
 
 Prints ONE JSON line (rank 0).  --impl reference times the CPU restatement of
 the reference's projection (the FP32 lenslet-sparse loop of oracle/sid_oracle.c,
