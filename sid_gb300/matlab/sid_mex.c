@@ -148,6 +148,26 @@ static double field_or(const mxArray* s, const char* name, double dflt)
     return (f && !mxIsEmpty(f)) ? mxGetScalar(f) : dflt;
 }
 
+/* A microlens mask (double or logical, X*Y elements) as a uint8 host array
+ * the caller destroys. */
+static mxArray* mask_u8(const mxArray* a, mwSize n, const char* cmd)
+{
+    if (mxGetNumberOfElements(a) != n)
+        mexErrMsgIdAndTxt("sid:type", "%s: microlenses must have the image's X*Y elements", cmd);
+    if (!mxIsLogical(a) && !(mxIsDouble(a) && !mxIsComplex(a)))
+        mexErrMsgIdAndTxt("sid:type", "%s: microlenses must be a real double or logical array", cmd);
+    mxArray* t = mxCreateNumericMatrix(n, 1, mxUINT8_CLASS, mxREAL);
+    uint8_t* dst = (uint8_t*)mxGetData(t);
+    if (mxIsLogical(a)) {
+        const mxLogical* src = mxGetLogicals(a);
+        for (mwSize i = 0; i < n; ++i) dst[i] = src[i] ? 1 : 0;
+    } else {
+        const double* src = mxGetPr(a);
+        for (mwSize i = 0; i < n; ++i) dst[i] = src[i] != 0.0;
+    }
+    return t;
+}
+
 /* out = f(plan, in) for a single-precision array, on the device or the host */
 typedef int (*dev_fn)(sid_plan*, int, const float*, float*, void*);
 typedef int (*host_fn)(sid_plan*, int, const float*, float*);
@@ -185,10 +205,14 @@ void mexFunction(int nlhs, mxArray* plhs[], int nrhs, const mxArray* prhs[])
         const mxArray* H = prhs[1];
         if (!mxIsSingle(H) || mxGetNumberOfDimensions(H) < 4) mexErrMsgIdAndTxt("sid:plan", "H must be single M x M x N x N x Z");
         const mwSize* d = mxGetDimensions(H);
+        if (d[0] != d[1] || d[2] != d[3]) mexErrMsgIdAndTxt("sid:plan", "H must be single M x M x N x N x Z");
         const int64_t Z = mxGetNumberOfDimensions(H) > 4 ? (int64_t)d[4] : 1;
         int32_t* ca = NULL;
         int32_t cabuf[2 * 4096];
         if (!mxIsEmpty(prhs[2])) {
+            if (!mxIsDouble(prhs[2]) || mxIsComplex(prhs[2]) || Z > 4096 ||
+                mxGetNumberOfElements(prhs[2]) != (mwSize)(2 * Z))
+                mexErrMsgIdAndTxt("sid:plan", "CAindex must be a real Z x 2 double array (Z <= 4096)");
             const double* c = mxGetPr(prhs[2]);
             for (int64_t i = 0; i < 2 * Z && i < 2 * 4096; ++i) cabuf[i] = (int32_t)c[i];
             ca = cabuf;
@@ -225,6 +249,11 @@ void mexFunction(int nlhs, mxArray* plhs[], int nrhs, const mxArray* prhs[])
     if (!strcmp(cmd, "isra")) {
         sid_plan* p = plan_arg(prhs[1]);
         if (!mxIsSingle(prhs[2]) || !mxIsSingle(prhs[3])) mexErrMsgIdAndTxt("sid:type", "isra: single inputs");
+        int64_t info[14];
+        sid_plan_info(p, info);
+        if (mxGetNumberOfElements(prhs[2]) != (mwSize)(info[3] * info[4] * info[2]) ||
+            mxGetNumberOfElements(prhs[3]) != (mwSize)(info[3] * info[4] * info[2]))
+            mexErrMsgIdAndTxt("sid:type", "isra: Htf and Xguess must be X x Y x Z volumes of the plan");
         plhs[0] = mxDuplicateArray(prhs[3]);
         check(sid_deconv_isra_host(p, method_arg(nrhs, prhs, 6), (const float*)mxGetData(prhs[2]),
                                    (float*)mxGetData(plhs[0]), (int)mxGetScalar(prhs[4]), (float)mxGetScalar(prhs[5])),
@@ -553,10 +582,9 @@ void mexFunction(int nlhs, mxArray* plhs[], int nrhs, const mxArray* prhs[])
         const mxGPUArray* ml = NULL;
         mxArray* tmp_ml = NULL;
         if (nrhs > 3 && !mxIsEmpty(prhs[3])) {
-            const mwSize nm = mxGetNumberOfElements(prhs[3]);
-            tmp_ml = mxCreateNumericMatrix(nm, 1, mxUINT8_CLASS, mxREAL);
-            uint8_t* dst = (uint8_t*)mxGetData(tmp_ml);
-            for (mwSize i = 0; i < nm; ++i) dst[i] = mxGetPr(prhs[3])[i] != 0.0;
+            int64_t pinfo[14];
+            sid_plan_info(p, pinfo);
+            tmp_ml = mask_u8(prhs[3], (mwSize)(pinfo[3] * pinfo[4]), cmd);
             ml = mxGPUCreateFromMxArray(tmp_ml);
         }
         const mxArray* o = nrhs > 4 ? prhs[4] : NULL;
@@ -618,10 +646,9 @@ void mexFunction(int nlhs, mxArray* plhs[], int nrhs, const mxArray* prhs[])
         const mxGPUArray* ml = NULL;
         mxArray* tmp_ml = NULL;
         if (nrhs > 3 && !mxIsEmpty(prhs[3])) {
-            const mwSize nm = mxGetNumberOfElements(prhs[3]);
-            tmp_ml = mxCreateNumericMatrix(nm, 1, mxUINT8_CLASS, mxREAL);
-            uint8_t* dst = (uint8_t*)mxGetData(tmp_ml);
-            for (mwSize i = 0; i < nm; ++i) dst[i] = mxGetPr(prhs[3])[i] != 0.0;
+            int64_t pinfo[14];
+            sid_plan_info(p, pinfo);
+            tmp_ml = mask_u8(prhs[3], (mwSize)(pinfo[3] * pinfo[4]), cmd);
             ml = mxGPUCreateFromMxArray(tmp_ml);
         }
         const mxArray* o = nrhs > 4 ? prhs[4] : NULL;
@@ -736,6 +763,10 @@ void mexFunction(int nlhs, mxArray* plhs[], int nrhs, const mxArray* prhs[])
             ptrs[k] = (const float*)mxGPUGetDataReadOnly(vols[k]);
         }
         const mwSize n = mxGetDimensions(prhs[3])[0];
+        if (!mxIsLogical(prhs[4]) || mxGetNumberOfElements(prhs[4]) != n * nc) {
+            for (mwSize k = 0; k < nc; ++k) mxGPUDestroyGPUArray(vols[k]);
+            mexErrMsgIdAndTxt("sid:library", "neur_id must be an n x numel(recon) logical array");
+        }
         mxArray* ids = mxCreateNumericMatrix(n, nc, mxUINT8_CLASS, mxREAL);
         const mxLogical* nid = mxGetLogicals(prhs[4]);
         uint8_t* idp = (uint8_t*)mxGetData(ids);

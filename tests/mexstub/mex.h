@@ -34,6 +34,8 @@ bool mxIsStruct(const mxArray* a);
 bool mxIsChar(const mxArray* a);
 bool mxIsSingle(const mxArray* a);
 bool mxIsDouble(const mxArray* a);
+bool mxIsLogical(const mxArray* a);
+bool mxIsComplex(const mxArray* a);
 size_t mxGetM(const mxArray* a);
 size_t mxGetN(const mxArray* a);
 mxArray* mxCreateDoubleScalar(double v);
