@@ -372,6 +372,8 @@ void mexFunction(int nlhs, mxArray* plhs[], int nrhs, const mxArray* prhs[])
             const mxArray* f;
             if (tu && (f = mxGetField(o, 0, "active")) && !mxIsEmpty(f)) {
                 /* logical P-vector -> uint8 gpuArray */
+                if (!mxIsLogical(f) || mxGetNumberOfElements(f) != (mwSize)P)
+                    mexErrMsgIdAndTxt("sid:type", "%s: opts.active must be a logical vector of P elements", cmd);
                 tmp_act = mxCreateNumericMatrix((mwSize)P, 1, mxUINT8_CLASS, mxREAL);
                 const mxLogical* src = mxGetLogicals(f);
                 uint8_t* dst = (uint8_t*)mxGetData(tmp_act);
@@ -516,6 +518,8 @@ void mexFunction(int nlhs, mxArray* plhs[], int nrhs, const mxArray* prhs[])
     if (!strcmp(cmd, "quantile")) {
         /* q = sid_mex('quantile', x, p): x single gpuArray, p double vector */
         const mxGPUArray* x = gpu_arg(prhs[1], 0, cmd);
+        if (!mxIsDouble(prhs[2]) || mxIsComplex(prhs[2]))
+            mexErrMsgIdAndTxt("sid:type", "quantile: p must be a real double vector");
         const int np = (int)mxGetNumberOfElements(prhs[2]);
         plhs[0] = mxCreateDoubleMatrix(1, (mwSize)np, mxREAL);
         const int rc = sid_quantile(ctx(cmd), (const float*)mxGPUGetDataReadOnly(x),
@@ -694,6 +698,8 @@ void mexFunction(int nlhs, mxArray* plhs[], int nrhs, const mxArray* prhs[])
         const int pn = (int)mxGetScalar(prhs[6]);
         float lam3[3] = {0.f, 0.f, 0.f};
         const mwSize nl = mxGetNumberOfElements(prhs[7]);
+        if (nl && (!mxIsDouble(prhs[7]) || mxIsComplex(prhs[7])))
+            mexErrMsgIdAndTxt("sid:type", "isra_ex: the TV weights must be a real double vector");
         for (mwSize i = 0; i < nl && i < 3; ++i) lam3[i] = (float)mxGetPr(prhs[7])[i];
         mxGPUArray* X = gpu_copy(x0);
         mxGPUArray* hist = NULL;
@@ -728,6 +734,8 @@ void mexFunction(int nlhs, mxArray* plhs[], int nrhs, const mxArray* prhs[])
         const mxGPUArray* df = gpu_arg(prhs[2], 0, cmd);
         float tv[3] = {0.f, 0.f, 0.f};
         const mwSize nt = mxGetNumberOfElements(prhs[6]);
+        if (nt && (!mxIsDouble(prhs[6]) || mxIsComplex(prhs[6])))
+            mexErrMsgIdAndTxt("sid:type", "ls_deconv_ex: lamb_TV_L2 must be a real double vector");
         for (mwSize i = 0; i < nt && i < 3; ++i) tv[i] = (float)mxGetPr(prhs[6])[i];
         mxGPUArray* X = gpu_copy(df);
         int rc = sid_deconv_ls_ex(p, method_arg(nrhs, prhs, 8), (float*)mxGPUGetData(X), (int)mxGetScalar(prhs[3]),
@@ -834,8 +842,8 @@ void mexFunction(int nlhs, mxArray* plhs[], int nrhs, const mxArray* prhs[])
         const mxArray* o = nrhs > 4 ? prhs[4] : NULL;
         const int bg = (int)field_or(o, "bg_sub", 1.0);
         const mwSize R = dt[0], F = dt[1], P = dy[0];
-        if (mxGetNumberOfElements(prhs[3]) != (R - (mwSize)bg) * P)
-            mexErrMsgIdAndTxt("sid:spatial_update", "template must be (R - bg_sub) x P");
+        if (!mxIsLogical(prhs[3]) || mxGetNumberOfElements(prhs[3]) != (R - (mwSize)bg) * P)
+            mexErrMsgIdAndTxt("sid:spatial_update", "template must be a (R - bg_sub) x P logical array");
         mxArray* tm = mxCreateNumericMatrix(R - (mwSize)bg, P, mxUINT8_CLASS, mxREAL);
         const mxLogical* tl = mxGetLogicals(prhs[3]);
         uint8_t* tp = (uint8_t*)mxGetData(tm);
