@@ -172,12 +172,15 @@ static mxArray* mask_u8(const mxArray* a, mwSize n, const char* cmd)
 typedef int (*dev_fn)(sid_plan*, int, const float*, float*, void*);
 typedef int (*host_fn)(sid_plan*, int, const float*, float*);
 
-static mxArray* project(sid_plan* p, int method, const mxArray* in, mwSize nd, const mwSize* dims, dev_fn fd,
-                        host_fn fh, const char* cmd)
+static mxArray* project(sid_plan* p, int method, const mxArray* in, mwSize in_n, mwSize nd, const mwSize* dims,
+                        dev_fn fd, host_fn fh, const char* cmd)
 {
     if (mxIsGPUArray(in)) {
         const mxGPUArray* gin = mxGPUCreateFromMxArray(in);
-        if (mxGPUGetClassID(gin) != mxSINGLE_CLASS) mexErrMsgIdAndTxt("sid:type", "%s: input must be single", cmd);
+        if (mxGPUGetClassID(gin) != mxSINGLE_CLASS || mxGPUGetNumberOfElements(gin) != in_n) {
+            mxGPUDestroyGPUArray(gin);
+            mexErrMsgIdAndTxt("sid:type", "%s: input must be a single array of the plan's size", cmd);
+        }
         mxGPUArray* gout = mxGPUCreateGPUArray(nd, dims, mxSINGLE_CLASS, mxREAL, MX_GPU_DO_NOT_INITIALIZE);
         int rc = fd(p, method, (const float*)mxGPUGetDataReadOnly(gin), (float*)mxGPUGetData(gout), NULL);
         if (rc == SID_OK) rc = sid_plan_sync(p, NULL);
@@ -188,6 +191,7 @@ static mxArray* project(sid_plan* p, int method, const mxArray* in, mwSize nd, c
         return out;
     }
     if (!mxIsSingle(in)) mexErrMsgIdAndTxt("sid:type", "%s: input must be single", cmd);
+    if (mxGetNumberOfElements(in) != in_n) mexErrMsgIdAndTxt("sid:type", "%s: input has the wrong size for the plan", cmd);
     mxArray* out = mxCreateNumericArray(nd, dims, mxSINGLE_CLASS, mxREAL);
     check(fh(p, method, (const float*)mxGetData(in), (float*)mxGetData(out)), cmd);
     return out;
@@ -242,8 +246,9 @@ void mexFunction(int nlhs, mxArray* plhs[], int nrhs, const mxArray* prhs[])
         sid_plan_info(p, info);
         const int fwd = !strcmp(cmd, "forward");
         mwSize dims[3] = {(mwSize)info[3], (mwSize)info[4], (mwSize)info[2]};
-        plhs[0] = project(p, method_arg(nrhs, prhs, 3), prhs[2], fwd ? 2 : 3, dims, fwd ? sid_forward : sid_adjoint,
-                          fwd ? sid_forward_host : sid_adjoint_host, cmd);
+        const mwSize in_n = (mwSize)(info[3] * info[4] * (fwd ? info[2] : 1));
+        plhs[0] = project(p, method_arg(nrhs, prhs, 3), prhs[2], in_n, fwd ? 2 : 3, dims,
+                          fwd ? sid_forward : sid_adjoint, fwd ? sid_forward_host : sid_adjoint_host, cmd);
         return;
     }
     if (!strcmp(cmd, "isra")) {
