@@ -169,6 +169,22 @@ static mxArray* mask_u8(const mxArray* a, mwSize n, const char* cmd)
 }
 
 /* out = f(plan, in) for a single-precision array, on the device or the host */
+/* Elements of the plan's volume (what = 'v': X*Y*Z) or sensor image ('i': X*Y). */
+static mwSize plan_numel(const sid_plan* p, char what)
+{
+    int64_t info[14];
+    sid_plan_info(p, info);
+    return (mwSize)(info[3] * info[4] * (what == 'v' ? info[2] : 1));
+}
+
+/* A device argument must hold exactly n elements: the kernels read that many. */
+static void need_numel(const mxGPUArray* g, mwSize n, const char* cmd, const char* what)
+{
+    if (mxGPUGetNumberOfElements(g) != n)
+        mexErrMsgIdAndTxt("sid:type", "%s: %s has %llu elements, the plan needs %llu", cmd, what,
+                          (unsigned long long)mxGPUGetNumberOfElements(g), (unsigned long long)n);
+}
+
 typedef int (*dev_fn)(sid_plan*, int, const float*, float*, void*);
 typedef int (*host_fn)(sid_plan*, int, const float*, float*);
 
@@ -652,6 +668,7 @@ void mexFunction(int nlhs, mxArray* plhs[], int nrhs, const mxArray* prhs[])
         /* [X, lam] = sid_mex('reconstruct', plan, img, microlenses, opts, method): img X x Y single gpuArray */
         sid_plan* p = plan_arg(prhs[1]);
         const mxGPUArray* img = gpu_arg(prhs[2], 0, cmd);
+        need_numel(img, plan_numel(p, 'i'), cmd, "img");
         const mxGPUArray* ml = NULL;
         mxArray* tmp_ml = NULL;
         if (nrhs > 3 && !mxIsEmpty(prhs[3])) {
@@ -698,6 +715,8 @@ void mexFunction(int nlhs, mxArray* plhs[], int nrhs, const mxArray* prhs[])
         sid_plan* p = plan_arg(prhs[1]);
         const mxGPUArray* htf = gpu_arg(prhs[2], 0, cmd);
         const mxGPUArray* x0 = gpu_arg(prhs[3], 0, cmd);
+        need_numel(htf, plan_numel(p, 'v'), cmd, "Htf");
+        need_numel(x0, plan_numel(p, 'v'), cmd, "Xguess");
         const int maxIter = (int)mxGetScalar(prhs[4]);
         const int mode = (int)mxGetScalar(prhs[5]);
         const int pn = (int)mxGetScalar(prhs[6]);
@@ -737,6 +756,7 @@ void mexFunction(int nlhs, mxArray* plhs[], int nrhs, const mxArray* prhs[])
         /* X = sid_mex('ls_deconv_ex', plan, df, max_iter, lamb_L1, lamb_L2, lamb_TV_L2, lamb_TV_L1, method) */
         sid_plan* p = plan_arg(prhs[1]);
         const mxGPUArray* df = gpu_arg(prhs[2], 0, cmd);
+        need_numel(df, plan_numel(p, 'v'), cmd, "df");
         float tv[3] = {0.f, 0.f, 0.f};
         const mwSize nt = mxGetNumberOfElements(prhs[6]);
         if (nt && (!mxIsDouble(prhs[6]) || mxIsComplex(prhs[6])))
@@ -773,6 +793,7 @@ void mexFunction(int nlhs, mxArray* plhs[], int nrhs, const mxArray* prhs[])
         const float* ptrs[4096];
         for (mwSize k = 0; k < nc; ++k) {
             vols[k] = gpu_arg(mxGetCell(rc_cell, k), 0, cmd);
+            need_numel(vols[k], plan_numel(p, 'v'), cmd, "recon{k}");
             ptrs[k] = (const float*)mxGPUGetDataReadOnly(vols[k]);
         }
         const mwSize n = mxGetDimensions(prhs[3])[0];
