@@ -158,6 +158,16 @@ class Projector:
         """Free the plan's solver and projection workspaces (sid_plan_release_workspaces)."""
         _lib.call("sid_plan_release_workspaces", self._plan)
 
+    def _need(self, who, kind, *arrays):
+        """Every array holds the plan's volume (kind 'v': X*Y*Z elements) or
+        sensor image ('i': X*Y): libsid reads exactly that many."""
+        n = self.X * self.Y * (self.Z if kind == "v" else 1)
+        for a in arrays:
+            m = a.numel() if isinstance(a, torch.Tensor) else int(np.size(a))
+            if m != n:
+                raise ValueError(f"{who}: expected the plan's {'volume' if kind == 'v' else 'image'} "
+                                 f"({n} elements), got {m}")
+
     def _method(self, method):
         m = method or self.default_method
         if m not in _lib.METHODS:
@@ -186,12 +196,14 @@ class Projector:
     def forward_host(self, V, method=None) -> np.ndarray:
         """Host-array form (inputs and result on the host, copies inside)."""
         Vn = np.asfortranarray(np.asarray(V, dtype=np.float32))
+        self._need("forward_host", "v", Vn)
         I = np.zeros((self.X, self.Y), dtype=np.float32, order="F")
         _lib.call("sid_forward_host", self._plan, self._method(method), Vn.ctypes.data, I.ctypes.data)
         return I
 
     def adjoint_host(self, I, method=None) -> np.ndarray:
         In = np.asfortranarray(np.asarray(I, dtype=np.float32))
+        self._need("adjoint_host", "i", In)
         V = np.zeros((self.X, self.Y, self.Z), dtype=np.float32, order="F")
         _lib.call("sid_adjoint_host", self._plan, self._method(method), In.ctypes.data, V.ctypes.data)
         return V
@@ -204,6 +216,7 @@ class Projector:
     def isra(self, Htf, Xguess, maxIter, lam=0.0, method=None) -> torch.Tensor:
         Htf = to_device(Htf)
         X = to_device(Xguess).clone()
+        self._need("isra", "v", Htf, X)
         _lib.call("sid_deconv_isra", self._plan, self._method(method), Htf.data_ptr(), X.data_ptr(),
                   int(maxIter), float(lam), _stream_ptr())
         return X
@@ -214,6 +227,7 @@ class Projector:
         returns Xguess_history (maxIter x X x Y x Z, deconvRL.m:10,90-92)."""
         Htf = to_device(Htf)
         X = to_device(Xguess).clone()
+        self._need("isra_ex", "v", Htf, X)
         lam3 = np.zeros(3, dtype=np.float32)
         lv = np.asarray(lam, dtype=np.float64).ravel()
         if mode == "TV":
@@ -236,6 +250,7 @@ class Projector:
         """[forwardProjectGPU(H, V) for V in volumes], up to four volumes per
         pass over the tap spectra."""
         vs = [to_device(v) for v in volumes]
+        self._need("forward_batched", "v", *vs)
         outs = [_fortran_tensor((self.X, self.Y), vs[0].device) for _ in vs]
         _lib.call("sid_forward_batched", self._plan, self._method(method), len(vs),
                   ctypes.cast(self._ptr_array(vs), ctypes.c_void_p), ctypes.cast(self._ptr_array(outs), ctypes.c_void_p),
@@ -245,6 +260,7 @@ class Projector:
     def adjoint_batched(self, images, method=None):
         """[backwardProjectGPU_new(H, I) for I in images]."""
         ims = [to_device(i) for i in images]
+        self._need("adjoint_batched", "i", *ims)
         outs = [_fortran_tensor((self.X, self.Y, self.Z), ims[0].device) for _ in ims]
         _lib.call("sid_adjoint_batched", self._plan, self._method(method), len(ims),
                   ctypes.cast(self._ptr_array(ims), ctypes.c_void_p), ctypes.cast(self._ptr_array(outs), ctypes.c_void_p),
@@ -258,6 +274,7 @@ class Projector:
         xs = [to_device(x).clone() for x in Xguesses]
         if len(hs) != len(xs):
             raise ValueError("isra_batched: Htf and Xguess lists differ in length")
+        self._need("isra_batched", "v", *hs, *xs)
         _lib.call("sid_deconv_isra_batched", self._plan, self._method(method), len(hs),
                   ctypes.cast(self._ptr_array(hs), ctypes.c_void_p), ctypes.cast(self._ptr_array(xs), ctypes.c_void_p),
                   int(maxIter), float(lam), _stream_ptr())
@@ -268,6 +285,8 @@ class Projector:
         X <- X .* A'(y ./ AX) ./ A'1 (the reference's deconvRL is the ISRA form)."""
         y = to_device(y)
         X = to_device(Xguess).clone()
+        self._need("rl_poisson", "i", y)
+        self._need("rl_poisson", "v", X)
         _lib.call("sid_deconv_rl_poisson", self._plan, self._method(method), y.data_ptr(), X.data_ptr(),
                   int(maxIter), _stream_ptr())
         return X
@@ -278,6 +297,7 @@ class Projector:
         conversions, Htf on a copy engine during the first projections."""
         Hn = np.asfortranarray(np.asarray(Htf, dtype=np.float32))
         X = np.array(Xguess, dtype=np.float32, order="F", copy=True)
+        self._need("isra_host", "v", Hn, X)
         _lib.call("sid_deconv_isra_host", self._plan, self._method(method), Hn.ctypes.data, X.ctypes.data,
                   int(maxIter), float(lam))
         return X
@@ -287,6 +307,7 @@ class Projector:
         if not (isinstance(X, np.ndarray) and X.dtype == np.float32 and X.flags.f_contiguous):
             raise TypeError("X must be a Fortran-ordered float32 array")
         Hn = np.asfortranarray(np.asarray(Htf, dtype=np.float32))
+        self._need("isra_host_inplace", "v", Hn, X)
         _lib.call("sid_deconv_isra_host", self._plan, self._method(method), Hn.ctypes.data, X.ctypes.data,
                   int(maxIter), float(lam))
         return X
@@ -365,6 +386,7 @@ class Projector:
     def ls_deconv_batched(self, dfs, max_iter=8, lamb_L1=0.0, lamb_L2=0.0, method=None):
         """LS_deconv (plain mode) for several volumes; lamb_L1: one value or one per volume."""
         xs = [to_device(d).clone() for d in dfs]
+        self._need("ls_deconv_batched", "v", *xs)
         l1 = np.broadcast_to(np.asarray(lamb_L1, dtype=np.float32), (len(xs),)).copy()
         _lib.call("sid_deconv_ls_batched", self._plan, self._method(method), len(xs),
                   ctypes.cast(self._ptr_array(xs), ctypes.c_void_p), int(max_iter), l1.ctypes.data,
@@ -374,6 +396,7 @@ class Projector:
     def ls_deconv(self, df, max_iter=8, lamb_L1=0.0, lamb_L2=0.0, method=None, lamb_TV_L2=(0.0, 0.0, 0.0),
                   lamb_TV_L1=0.0) -> torch.Tensor:
         X = to_device(df).clone()
+        self._need("ls_deconv", "v", X)
         tv = np.zeros(3, dtype=np.float32)
         tv[:] = np.asarray(lamb_TV_L2, dtype=np.float32).ravel()[:3]
         _lib.call("sid_deconv_ls_ex", self._plan, self._method(method), X.data_ptr(), int(max_iter),

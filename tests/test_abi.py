@@ -83,3 +83,20 @@ def test_every_entry_point_rejects_null_arguments(sidlib):
         rc = getattr(sidlib, name)(*args)
         assert rc == _lib.SID_EINVAL, (name, rc)
         assert sidlib.sid_last_error(), name
+
+
+def test_projector_mirror_checks_sizes_before_calling_libsid():
+    """The Python mirror refuses host arrays of the wrong element count before
+    any libsid call (the C side reads exactly the plan's volume or image)."""
+    from sid_gb300.lfm import Projector
+    P = Projector.__new__(Projector)  # geometry only: no plan, so any libsid call would fail differently
+    P.X, P.Y, P.Z, P.default_method = 6, 5, 3, "direct"
+    vol, img = np.zeros((6, 5, 3), np.float32), np.zeros((6, 5), np.float32)
+    P._need("t", "v", vol)
+    P._need("t", "i", img)
+    with pytest.raises(ValueError, match="volume"):
+        P.forward_host(np.zeros((6, 5, 2), np.float32))
+    with pytest.raises(ValueError, match="image"):
+        P.adjoint_host(np.zeros((5, 5), np.float32))
+    with pytest.raises(ValueError, match="volume"):
+        P.isra_host(vol, np.zeros((6, 5, 4), np.float32), 1)
