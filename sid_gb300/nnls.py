@@ -112,6 +112,12 @@ def _movie(Y):
     return (_to_device_half(Y) if half else to_device(Y)), half
 
 
+def _need(who, what, t, n):
+    """t holds n elements (libsid reads exactly that many from a device pointer)."""
+    if t is not None and t.numel() != n:
+        raise ValueError(f"{who}: {what} must hold {n} elements, got {t.numel()}")
+
+
 def _ls_nnls(self, A, Y, opts=None, G=None, x=None, prec="split", return_iters=False):
     """[X, G] = LS_nnls(A, Y, opts, G, x) (LS_nnls.m:1) on the GPU."""
     A = to_device(A)
@@ -119,8 +125,11 @@ def _ls_nnls(self, A, Y, opts=None, G=None, x=None, prec="split", return_iters=F
     P, K = A.shape
     F = Yd.shape[1]
     o = _opts("ls_nnls", opts)
+    _need("LS_nnls", "Y's rows x frames", Yd, P * F)
     Gd = to_device(G) if G is not None else _fortran_tensor((K, K), A.device)
     X = to_device(x).clone() if x is not None else _fortran_tensor((K, F), A.device)
+    _need("LS_nnls", "G", Gd, K * K)
+    _need("LS_nnls", "x", X, K * F)
     it = torch.zeros(F, dtype=torch.int32, device=A.device)
     _lib.call("sid_ls_nnls", self._ctx, A.data_ptr(), Yd.data_ptr(), _lib.DTYPE_F16 if half else _lib.DTYPE_F32,
               P, K, F, ctypes.byref(o), Gd.data_ptr(), 1 if G is not None else 0, X.data_ptr(),
@@ -167,6 +176,12 @@ def _fast_nnls(self, A, Y, opts=None, Q=None, df=None, h=None, prec="split", ret
         Yd, half = None, False
         F = dfd.shape[1]
     P = Ad.shape[0] if Ad is not None else 0
+    if Ad is not None and Yd is not None:
+        _need("fast_nnls", "Y (the rows of A x frames)", Yd, P * F)
+    _need("fast_nnls", "warm_start", W, K * F)
+    _need("fast_nnls", "Q", Qd, K * K)
+    _need("fast_nnls", "h", hd, K)
+    _need("fast_nnls", "df", dfd, K * F)
     X = _fortran_tensor((K, F), "cuda")
     Qo = _fortran_tensor((K, K), "cuda")
     ho = torch.empty(K, dtype=torch.float32, device="cuda")
